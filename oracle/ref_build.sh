@@ -1,0 +1,13 @@
+#!/bin/sh
+# Builds oracle/_ref/ref_probe from the reference's own host sources where they
+# lie (grids.cpp, r_lut.cpp, nist_loader.cpp; header-only host physics).  Runs
+# only where the reference tree is mounted; the output never leaves oracle/_ref.
+set -e
+REF=${SM2D_REFERENCE:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+[ -d "$REF/src" ] || { echo "reference tree not found at $REF" >&2; exit 1; }
+mkdir -p "$HERE/_ref"
+g++ -O2 -std=c++17 -ffp-contract=off -I"$REF/src/include" \
+    "$REF/src/core/grids.cpp" "$REF/src/lut/r_lut.cpp" "$REF/src/lut/nist_loader.cpp" \
+    "$HERE/ref_probe.cpp" -o "$HERE/_ref/ref_probe"
+echo "$HERE/_ref/ref_probe"

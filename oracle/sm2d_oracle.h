@@ -1,0 +1,117 @@
+/*
+ * sm2d_oracle.h -- CPU oracle for the SM_2D deterministic phase-space
+ * transport step (K1..K6).  TEST INFRASTRUCTURE ONLY: this code is the
+ * checker that the CUDA path is compared against.  Nothing in the product
+ * (sm_2d_gb300/) includes, links or calls it; only tests/, the smoke check
+ * and the CPU-baseline leg of bench.py load it.
+ *
+ * It restates the reference kernels one function at a time, in the
+ * reference's own arithmetic order, so that the float build reproduces the
+ * reference GPU dumps (results/one_step_case_*) and the double build is the
+ * FP64 oracle of the same method.  Every function cites the reference
+ * file:line it follows.
+ *
+ * Pinning: the float build is checked against the reference GPU golden dumps
+ * results/one_step_case_{A,B,C,D} and against fixtures generated from the
+ * reference's host grid/LUT code (tests/golden/).
+ */
+#ifndef SM2D_ORACLE_H
+#define SM2D_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifdef ORC_FP64
+typedef double orc_real;
+#else
+typedef float orc_real;
+#endif
+
+#define ORC_KB 32          /* slots per cell     (device_psic.cuh:30)   */
+#define ORC_KB_OUT 32      /* slots per bucket   (device_bucket.cuh:26) */
+#define ORC_EMPTY 0xFFFFFFFFu
+
+typedef struct orc_config {
+    /* spatial grid */
+    int Nx, Nz;
+    float dx, dz, x_min, z_min;
+    /* local-bin layout: theta_local, E_local, x_sub, z_sub */
+    int nt_local, ne_local, nx_sub, nz_sub;
+    /* transport controls (TransportConfig, incident_particle_config.hpp:176) */
+    float E_fine_on, E_fine_off, weight_active_min;
+    float step_coarse;
+    float sigma_x_initial;     /* beam sigma_x, used by K2 and the post-convolution */
+    float E0;                  /* beam energy for the Fermi-Eyges precompute         */
+    int enable_straggling, enable_nuclear;
+    /* method options (0 = reference behaviour) */
+    int seed_slot_mode;        /* 0: seed uses storage slot; 1: rank of bid in cell */
+    int energy_split;          /* 0: single E bin + fold; 1: mean-preserving 2-bin  */
+    /* EnergyGrid::E_min/E_max (the constructor arguments; DeviceRLUT takes
+     * these, not edges[0]/edges[N]).  0 means "use the edges". */
+    float grid_E_min, grid_E_max;
+} orc_config;
+
+typedef struct orc_audit {       /* AuditReport, k5_audit.cuh:5-27 */
+    float W_error; int W_pass; float E_error; int E_pass;
+    float W_in_total, W_out_total, W_cutoff_total, W_nuclear_total, W_boundary_total;
+    float W_source_out_of_grid_total, W_source_slot_drop_total, W_transport_drop_total;
+    double E_in_total, E_out_total, E_dep_total, E_cutoff_total, E_nuclear_total;
+    double E_boundary_total, E_source_out_of_grid_total, E_source_slot_drop_total;
+    double E_transport_drop_total;
+    int processed_cells;
+} orc_audit;
+
+typedef struct orc_ctx orc_ctx;
+
+/* ---- grids and tables (usable without a context) ---- */
+int  orc_energy_grid_log(float E_min, float E_max, int N, float* edges, float* rep);
+int  orc_energy_grid_piecewise(int n_groups, const float* groups /* 3*n */, float* edges, float* rep);
+void orc_angular_grid(float th_min, float th_max, int N, float* edges, float* rep);
+void orc_generate_rlut(int N_E, const float* rep, float* R, float* S,
+                       float* logE, float* logR, float* logS);
+void orc_fe_precompute(float E0, int Nz, float dz, float sigma_x0,
+                       float* A, float* B, float* sigma_total);
+void orc_postprocess(const double* edep_in, const float* sigma_total, float sigma_x0,
+                     int Nx, int Nz, float dx, double* edep_out);
+
+/* ---- transport context ---- */
+orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* theta_edges,
+                    int N_E, const float* E_edges);
+void orc_destroy(orc_ctx* c);
+int  orc_local_bins(const orc_ctx* c);
+
+/* source injection (k1k6_pipeline.cu:300-551, gpu_transport_wrapper.cu:339-460) */
+void orc_inject(orc_ctx* c, float x0, float z0, float theta0, float E0, float W_total,
+                float sigma_x, float sigma_theta, float sigma_E,
+                int n_samples, unsigned seed);
+/* overwrite psi_in directly (golden inputs); values are orc_real */
+void orc_set_psi_in(orc_ctx* c, const uint32_t* bid, const orc_real* val);
+void orc_get_psi_in(const orc_ctx* c, uint32_t* bid, orc_real* val);
+
+/* one K1..K6 iteration; returns 1 if work was done, 0 if transport finished */
+int  orc_step(orc_ctx* c);
+int  orc_run(orc_ctx* c, int max_iterations);     /* returns iterations run */
+void orc_get_mask(const orc_ctx* c, uint8_t* mask);
+int  orc_get_lists(const orc_ctx* c, uint32_t* active, int* n_active,
+                   uint32_t* coarse, int* n_coarse);
+void orc_get_tallies(const orc_ctx* c, double* edep, float* w_cut, double* e_cut,
+                     float* w_nuc, double* e_nuc, float* w_bnd, double* e_bnd);
+void orc_get_audit(const orc_ctx* c, orc_audit* out);
+/* scalars: [0]=transport_dropped_weight [1]=transport_dropped_energy
+ * [2]=audit residual energy [3]=source_injected_weight [4]=source_injected_energy
+ * [5]=source_out_of_grid_weight [6]=source_out_of_grid_energy
+ * [7]=source_slot_dropped_weight [8]=source_slot_dropped_energy
+ * [9]=source_representation_loss_energy [10]=iterations [11]=cell_steps
+ * [12]=occupied input slots summed over cell-steps [13]=output slots summed */
+void orc_get_scalars(const orc_ctx* c, double* out14);
+void orc_get_fe(const orc_ctx* c, float* A, float* B, float* sigma_total);
+
+/* run several independent contexts on n_threads host threads */
+int  orc_run_many(orc_ctx** ctxs, int n, int max_iterations, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

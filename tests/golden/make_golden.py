@@ -1,0 +1,63 @@
+"""Regenerate the golden fixtures in this directory from the SM_2D reference.
+
+Two sources, both produced by the reference itself:
+
+1. ``one_step_case_{A,B,C,D}/`` -- the reference GPU build's own debug dumps
+   (SM2D_ENABLE_DEBUG_DUMPS=ON, commit aeef09b2) for one K1..K6 iteration of
+   a 150 MeV beam on an 80x40 grid at 0.5 mm: the phase space after source
+   injection (``debug_ps_raw_iter_00_initial.csv``), after K2/K3 + K4
+   (``debug_ps_raw_iter_01_after_K4.csv``), and the channel totals.  The
+   case INI files are stored beside them as JSON.
+2. ``ref_host_tables.json`` -- grids, R-LUTs and host lookups printed by
+   ``oracle/ref_probe`` linked against the reference's own host sources
+   (``oracle/ref_build.sh``).
+
+Run from the repository root in a container where the reference tree is
+mounted:  python tests/golden/make_golden.py
+"""
+import configparser
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+REF = os.environ.get("SM2D_REFERENCE", "/root/reference")
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+FILES = ["debug_ps_raw_iter_00_initial.csv", "debug_ps_raw_iter_01_after_K4.csv",
+         "debug_channels_totals_iter01.csv", "debug_cells_iter_01_after_K4.csv"]
+
+
+def one_step_cases():
+    for case in "ABCD":
+        src = os.path.join(REF, "results", f"one_step_case_{case}")
+        dst = os.path.join(HERE, f"one_step_case_{case}")
+        os.makedirs(dst, exist_ok=True)
+        for f in FILES:
+            shutil.copyfile(os.path.join(src, f), os.path.join(dst, f))
+        ini = [f for f in os.listdir(src) if f.endswith(".ini")][0]
+        cp = configparser.ConfigParser()
+        cp.read(os.path.join(src, ini))
+        cfg = {s: dict(cp[s]) for s in cp.sections()}
+        cfg["output"].pop("output_dir", None)
+        with open(os.path.join(dst, "case.json"), "w") as fh:
+            json.dump(cfg, fh, indent=1, sort_keys=True)
+
+
+def host_tables():
+    exe = subprocess.run(["sh", os.path.join(ROOT, "oracle", "ref_build.sh")], check=True,
+                         capture_output=True, text=True).stdout.strip().splitlines()[-1]
+    out = subprocess.run([exe], check=True, capture_output=True, text=True, cwd="/tmp").stdout
+    data = json.loads(out)
+    with open(os.path.join(HERE, "ref_host_tables.json"), "w") as fh:
+        json.dump(data, fh)
+
+
+if __name__ == "__main__":
+    if not os.path.isdir(REF):
+        sys.exit(f"reference tree not found at {REF}")
+    one_step_cases()
+    host_tables()
+    print("golden fixtures written to", HERE)
