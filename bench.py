@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Benchmark: spots/s of the SM_2D K1..K6 transport step on one GB300.
+
+Workload (the production single-beam case): a 150 MeV Gaussian proton beam
+(sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 1 % of E0, 1000 LCG samples,
+seed 42) into homogeneous water, 200 x 400 cells of 0.5 mm (100 x 200 mm),
+full coarse/fine pipeline with the conservation audit every iteration, FP32
+phase space.  Phase-space grids are the ones the reference code builds and
+runs: 36 angular bins on +-0.35 rad, the default piecewise 1029-bin energy
+grid, 256 local bins (4 theta x 2 E x 8 x_sub x 4 z_sub).  `--grid log` runs
+the 256 log-E / 512 theta / 128-local-bin variant with the energy-split
+method instead.  A step is one spot transported to completion (until the
+in-flight weight falls below 1e-6 of the injected weight).
+
+Arms: default = libsm2d.so on the GPU; `--impl reference` = the reference's
+algorithm on the host cores (the CPU restatement in oracle/, all threads, one
+spot per thread), since the reference has no CPU transport of its own.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "spots/s on 1 GB300, surrogate+batched vs plain K1–K6, at ≤1% dose error"
+BEAM = dict(x0=0.0, z0=0.0, theta0=0.0, E0=150.0, W=1.0, sigma_x=3.8, sigma_theta=0.002, sigma_E=1.5,
+            n_samples=1000, seed=42)
+MAX_IT = 4000
+
+
+SMALL = False   # --small: 100 x 200 cells and an 80 MeV beam, for profiler captures
+
+
+def make_config(grid: str):
+    import sm_2d_gb300 as sm
+    if SMALL:
+        cfg = sm.Config.reference_runner(100, 200, 0.5, 0.5, N_theta=36, sigma_x_initial=BEAM["sigma_x"],
+                                         E0=BEAM["E0"])
+        cfg.max_iterations = MAX_IT
+        return cfg.production()
+    if grid == "log":
+        cfg = sm.Config.log_grid(200, 400, 0.5, 0.5, N_E=256, E_min=0.1, E_max=250.0, N_theta=512,
+                                 theta_max=np.pi / 2, layout=sm.LAYOUT_B128, E_fine_on=10.0, E_fine_off=11.0,
+                                 sigma_x_initial=BEAM["sigma_x"], E0=BEAM["E0"], energy_split=1)
+    else:
+        cfg = sm.Config.reference_runner(200, 400, 0.5, 0.5, N_theta=36, sigma_x_initial=BEAM["sigma_x"],
+                                         E0=BEAM["E0"])
+    cfg.max_iterations = MAX_IT
+    return cfg.production()
+
+
+def workload_desc(grid, L):
+    if grid == "log":
+        ph = "256 log E bins 0.1-250 MeV, 512 theta bins +-pi/2, 128 local bins (8x4x4x1), energy-split method"
+    else:
+        ph = "reference grids: 1029 piecewise E bins, 36 theta bins +-0.35 rad, 256 local bins (4x2x8x4)"
+    return ("150 MeV Gaussian beam (sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 1.5 MeV, 1000 samples) "
+            f"in water 200x400 cells @0.5 mm; {ph}; full K1-K6 + audit per iteration; until in-flight "
+            f"weight < 1e-6 W0")
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm_ = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median(sm_)) if sm_ else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------- CPU arm
+def cpu_spots_per_s(grid: str, n_threads: int, n_spots: int):
+    """Transport n_spots independent copies of the workload on the CPU oracle,
+    n_threads at a time; returns (spots/s, wall seconds)."""
+    from oracle import oracle as orc
+    cfg = make_config(grid)
+    oc = cfg.oracle_config()
+    oracles = []
+    for i in range(n_spots):
+        o = orc.Oracle(oc, cfg.theta_edges, cfg.E_edges)
+        b = dict(BEAM)
+        o.inject(**b)
+        oracles.append(o)
+    t0 = time.perf_counter()
+    orc.run_many(oracles, MAX_IT, n_threads)
+    dt = time.perf_counter() - t0
+    for o in oracles:
+        o.close()
+    return n_spots / dt, dt
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n_threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_spots_per_s(args.grid, n_threads, n_threads)
+    vals, walls = [], []
+    for _ in range(args.steps):
+        v, dt = cpu_spots_per_s(args.grid, n_threads, n_threads)
+        vals.append(v)
+        walls.append(dt)
+    value = float(len(vals) * n_threads / sum(walls))
+    cfg = make_config(args.grid)
+    sample = f"{n_threads} spots per step (one per host thread), full transport of each"
+    line = {"metric": METRIC, "value": value, "unit": "spots/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(walls)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload_desc(args.grid, cfg.layout), "grid": args.grid},
+            "cpu_baseline": {"value": value, "unit": "spots/s", "cores": n_threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "spots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu_arm(args):
+    import torch
+    import sm_2d_gb300 as sm
+    from sm_2d_gb300.runtime import Beam
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.all_reduce(torch.zeros(1, device="cuda"))
+            torch.cuda.synchronize()
+
+    cfg = make_config(args.grid)
+    t = sm.Transport(cfg)
+    ext = torch.cuda.ExternalStream(t.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
+    # pinned beam description and dose buffer for the end-to-end leg
+    beam_buf = torch.zeros(64, dtype=torch.uint8).pin_memory()
+    beam = Beam.from_address(beam_buf.data_ptr())
+    b = dict(BEAM, seed=BEAM["seed"] + 7919 * rank)
+    for k, v in dict(x0=b["x0"], z0=b["z0"], theta0=b["theta0"], E0=b["E0"], W_total=b["W"],
+                     sigma_x=b["sigma_x"], sigma_theta=b["sigma_theta"], sigma_E=b["sigma_E"],
+                     n_samples=b["n_samples"], seed=b["seed"]).items():
+        setattr(beam, k, v)
+    dose_host = torch.zeros(cfg.Nx * cfg.Nz, dtype=torch.float64).pin_memory()
+    dose_np = dose_host.numpy()
+
+    def one_spot():
+        t.reset()
+        t.inject_async(beam)
+        t.run_async(MAX_IT)
+
+    for _ in range(max(args.warmup, 3)):
+        one_spot()
+    torch.cuda.synchronize()
+    iters_per_spot = t.scalars()["iterations"]
+
+    # ---- timed region: K spots, device time per spot, L2 flushed between spots
+    times = []
+    launches = 0
+    barrier()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            one_spot()
+            e1.record(ext)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            s = t.scalars()
+            launches += 6 + 4 * (int(s["iterations"]) + 1)
+    barrier()
+    total_ms = float(np.sum(times))
+    if dist:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    spots = args.steps * world
+    value = spots / (total_ms / 1e3)
+    sc = t.scalars()
+    cell_steps = sc["cell_steps"]
+
+    # ---- end to end through the public API with pinned host buffers
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        one_spot()
+        t.dose_async(dose_np)
+        e1.record(ext)
+        e1.synchronize()
+        e2e_times.append(e0.elapsed_time(e1))
+    e2e_ms = float(np.sum(e2e_times))
+    if dist:
+        tt = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    e2e_value = spots / (e2e_ms / 1e3)
+
+    # ---- per-kernel device time: eager replay of one spot with CUDA events
+    # around every launch on the library stream
+    t.reset()
+    t.inject_async(beam)
+    n_it, ms, n_launch = t.run_profiled(MAX_IT)
+    ps = t.scalars()
+    L = t.L
+    slot_bytes = 4 + 4 * L
+    alg_bytes = (ps["slots_in"] + ps["slots_out"]) * slot_bytes + 44.0 * ps["cell_steps"]
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peaks = json.load(open(peaks_path))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg_bytes / (ms["transport"] / 1e3) / 1e9 if ms["transport"] > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "k_transport_traffic.json")
+    if os.path.exists(tp):
+        tr = json.load(open(tp))
+        traffic = tr.get("dram_bytes_per_launch")
+    step_total = sum(ms.values())
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_src, "kernel": "k_transport",
+                "algorithmic_bytes_per_launch": alg_bytes / max(n_it, 1),
+                "avg_launch_ms": ms["transport"] / max(n_it, 1),
+                "stage_share": {k: v / step_total for k, v in ms.items()} if step_total else {},
+                "note": "per-launch times from an eager replay of one spot with CUDA events around each "
+                        "kernel on the library stream"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        n_threads = os.cpu_count() or 1
+        v, dt = cpu_spots_per_s(args.grid, n_threads, n_threads)
+        cpu = {"value": v, "unit": "spots/s", "cores": n_threads, "kind": "port",
+               "sample": f"{n_threads} spots, one per host thread, full transport ({dt:.1f} s wall)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "spots/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": workload_desc(args.grid, cfg.layout), "grid": args.grid,
+                           "method": "plain K1-K6 (direct neighbour scatter)", "iterations_per_spot":
+                           iters_per_spot, "l2": "flushed (256 MB write) between timed spots",
+                           "parallelism": f"replicas by spot x{world}"},
+                "cell_steps_per_s": cell_steps * world / (total_ms / 1e3) if total_ms else None,
+                "e2e": {"value": e2e_value, "unit": "spots/s", "h2d_bytes_per_step": 40,
+                        "d2h_bytes_per_step": int(cfg.Nx * cfg.Nz * 8)},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": launches}
+        print(json.dumps(line))
+    t.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", default="reference", choices=["reference", "log"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--small", action="store_true",
+                    help="100x200 cells, 80 MeV beam: a small case for profiler captures (not a bench line)")
+    args = ap.parse_args()
+    if args.small:
+        global SMALL
+        SMALL = True
+        BEAM["E0"] = 80.0
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,213 @@
+/*
+ * sm2d.h -- C ABI of the GB300 (sm_103a) SM_2D phase-space transport step.
+ *
+ * One handle holds one transport problem: a spatial grid of Nx x Nz cells,
+ * a block-sparse phase space with 32 slots per cell (24-bit block ids
+ * (b_E << 12) | b_theta, LOCAL_BINS local bins per slot), the R-LUT, the
+ * per-cell tallies and the device-resident iteration state.  Every entry
+ * point returns 0 on success and a negative SM2D_ERR_* code on failure;
+ * sm2d_last_error() gives the message.  Plain pointers and sizes only.
+ *
+ * Reference interfaces each entry replaces (paths inside the SM_2D project):
+ *   sm2d_create / sm2d_destroy  K1K6PipelineState::allocate/cleanup + init_pipeline_state
+ *                               (src/cuda/k1k6_pipeline.cu:853-1215), device_psic_init
+ *                               (src/cuda/device/device_psic.cuh:66-123), DeviceLUTWrapper::init
+ *                               (src/cuda/kernels/k3_finetransport.cuh:114-150)
+ *   sm2d_inject                 inject_source_kernel / inject_gaussian_source_kernel and the
+ *                               source accounting (src/cuda/gpu_transport_wrapper.cu:339-460)
+ *   sm2d_step                   one pass of the loop body (src/cuda/k1k6_pipeline.cu:1606-2038)
+ *   sm2d_run                    run_k1k6_pipeline_transport(DevicePsiC*,...) (k1k6_pipeline.cuh:296)
+ *   sm2d_get_dose               EdepC D2H + lateral post-convolution
+ *                               (src/cuda/gpu_transport_wrapper.cu:531-623)
+ *   sm2d_get_audit              get_audit_report (src/cuda/k1k6_pipeline.cu:1249-1255)
+ *   sm2d_k1_active_mask         run_k1_active_mask / K1_ActiveMask (k1k6_pipeline.cu:1261-1294,
+ *                               src/cuda/kernels/k1_activemask.cu:6-48)
+ *   sm2d_k4_bucket_transfer     run_k4_bucket_transfer / K4_BucketTransfer (k1k6_pipeline.cu:1415-1447,
+ *                               src/cuda/kernels/k4_transfer.cu:174-333)
+ *   sm2d_k5_conservation_audit  run_k5_conservation_audit / K5_ConservationAudit
+ *                               (k1k6_pipeline.cu:1449-1527, src/cuda/kernels/k5_audit.cu:22-167)
+ *   sm2d_compact_lists          compact_active_list / compact_coarse_list (k1k6_pipeline.cu:589-665)
+ */
+#ifndef SM2D_H
+#define SM2D_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SM2D_KB 32
+#define SM2D_KB_OUT 32
+#define SM2D_EMPTY 0xFFFFFFFFu
+
+enum {
+    SM2D_OK = 0,
+    SM2D_ERR_ARG = -1,       /* invalid argument or configuration            */
+    SM2D_ERR_CUDA = -2,      /* a CUDA runtime call failed                    */
+    SM2D_ERR_ALLOC = -3,     /* device allocation failed                      */
+    SM2D_ERR_STATE = -4,     /* call out of order (e.g. step before inject)   */
+    SM2D_ERR_TIMEOUT = -5,   /* a bounded device wait gave up                 */
+    SM2D_ERR_LAYOUT = -6     /* local-bin layout without a compiled kernel    */
+};
+
+/* Problem description.  Pointers are host arrays read during sm2d_create. */
+typedef struct sm2d_problem {
+    int Nx, Nz;                  /* spatial cells                              */
+    float dx, dz;                /* cell size [mm]                             */
+    float x_min, z_min;          /* grid origin [mm]                           */
+    int N_theta;                 /* global angular bins                        */
+    const float* theta_edges;    /* N_theta + 1 (AngularGrid::edges)           */
+    int N_E;                     /* global energy bins                         */
+    const float* E_edges;        /* N_E + 1 (EnergyGrid::edges)                */
+    float E_min, E_max;          /* EnergyGrid::E_min / E_max                  */
+    int nt_local, ne_local;      /* local bins per block: (4,2) or (8,4)       */
+    int nx_sub, nz_sub;          /* sub-cell bins: (8,4) or (4,1)              */
+    /* transport controls (TransportConfig) */
+    float E_fine_on, E_fine_off; /* K1 thresholds [MeV]                        */
+    float weight_active_min;
+    float step_coarse;           /* K2 step [mm] (clamped to min(dx,dz))       */
+    float sigma_x_initial;       /* beam sigma_x [mm]                          */
+    float E0;                    /* beam energy for the Fermi-Eyges precompute */
+    int enable_straggling, enable_nuclear;
+    /* method options: 0 reproduces the reference */
+    int seed_slot_mode;          /* 1: MCS/straggling seed uses the rank of the block id
+                                    in the cell instead of the racy storage slot      */
+    int energy_split;            /* 1: mean-preserving 2-bin energy re-binning          */
+    int use_buckets;             /* 1: emit through DeviceOutflowBucket + K4 (reference
+                                    structure); 0: fused direct neighbour scatter       */
+    int max_iterations;          /* capacity of the audit history                     */
+    /* production-run options (0 = reference behaviour) */
+    float prune_coarse;          /* K2 drops components lighter than this (0: 1e-12)   */
+    float prune_fine;            /* K3 drops components lighter than this (0: 1e-15)   */
+    float split_min_weight;      /* energy split: lighter split parts stay in the major
+                                    bin (energy folded into the deposit)               */
+    float stop_weight_fraction;  /* stop when in-flight weight < this * injected weight */
+    int floor_cutoff;            /* absorb components re-binned up to the lowest bin   */
+    int seed_iteration_salt;     /* salt MCS/straggling seeds with the iteration index */
+} sm2d_problem;
+
+typedef struct sm2d_beam {
+    float x0, z0, theta0, E0, W_total;
+    float sigma_x, sigma_theta, sigma_E;
+    int n_samples;
+    unsigned int seed;
+} sm2d_beam;
+
+/* AuditReport (src/cuda/kernels/k5_audit.cuh:5-27), same field order. */
+typedef struct sm2d_audit {
+    float W_error; int W_pass; float E_error; int E_pass;
+    float W_in_total, W_out_total, W_cutoff_total, W_nuclear_total, W_boundary_total;
+    float W_source_out_of_grid_total, W_source_slot_drop_total, W_transport_drop_total;
+    double E_in_total, E_out_total, E_dep_total, E_cutoff_total, E_nuclear_total;
+    double E_boundary_total, E_source_out_of_grid_total, E_source_slot_drop_total;
+    double E_transport_drop_total;
+    int processed_cells;
+} sm2d_audit;
+
+/* DeviceOutflowBucket (src/cuda/device/device_bucket.cuh:48-57) for L local bins:
+ *   uint32 block_id[32]; uint16 local_count[32]; float value[32][L]; float moment_A,B,C;
+ * sm2d_bucket_bytes(L) is its size. */
+size_t sm2d_bucket_bytes(int local_bins);
+
+typedef struct sm2d_ctx* sm2d_handle;
+
+const char* sm2d_last_error(void);
+int sm2d_version(void);
+int sm2d_create(const sm2d_problem* p, sm2d_handle* out);
+int sm2d_destroy(sm2d_handle h);
+int sm2d_local_bins(sm2d_handle h);
+
+/* source injection into psi_in (pencil or LCG Gaussian beam) */
+int sm2d_inject(sm2d_handle h, const sm2d_beam* beam);
+/* host <-> device phase space (psi_in): bid[Nx*Nz*32], val[Nx*Nz*32*L] */
+int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val);
+int sm2d_get_psi_in(sm2d_handle h, uint32_t* bid, float* val);
+
+/* one K1..K6 iteration; *n_active/*n_coarse are the listed cells (0,0 = done) */
+int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse);
+/* iterate until no cell holds weight or max_iterations passed; the loop runs
+ * on the device (one CUDA-graph launch, no host round trip per iteration) */
+int sm2d_run(sm2d_handle h, int max_iterations, int* iterations_done);
+/* same as sm2d_run, returning the device time of the loop (CUDA events) */
+int sm2d_run_timed(sm2d_handle h, int max_iterations, int* iterations_done, float* ms);
+
+int sm2d_get_mask(sm2d_handle h, uint8_t* mask);
+int sm2d_get_lists(sm2d_handle h, uint32_t* active, int* n_active, uint32_t* coarse, int* n_coarse);
+int sm2d_get_tallies(sm2d_handle h, double* edep, float* w_cut, double* e_cut,
+                     float* w_nuc, double* e_nuc, float* w_bnd, double* e_bnd);
+int sm2d_get_audit(sm2d_handle h, sm2d_audit* out);
+int sm2d_get_audit_history(sm2d_handle h, sm2d_audit* out, int max_entries, int* n_entries);
+/* scalars: [0] transport_dropped_weight [1] transport_dropped_energy
+ * [2] audit residual energy [3] source_injected_weight [4] source_injected_energy
+ * [5] source_out_of_grid_weight [6] source_out_of_grid_energy
+ * [7] source_slot_dropped_weight [8] source_slot_dropped_energy
+ * [9] source_representation_loss_energy [10] iterations [11] cell_steps
+ * [12] occupied input slots summed over cell-steps [13] output slots summed */
+int sm2d_get_scalars(sm2d_handle h, double* out14);
+int sm2d_get_fe(sm2d_handle h, float* A, float* B, float* sigma_total);
+/* EdepC after the lateral MCS post-convolution, [Nz][Nx] row-major */
+int sm2d_get_dose(sm2d_handle h, double* dose);
+/* per-kernel device time of the last sm2d_step (ms): classify, compact,
+ * transport, K4, audit+clear */
+int sm2d_get_step_timing(sm2d_handle h, float* ms5);
+
+/* ---- asynchronous spot pipeline (no host synchronisation; stream order) ---- */
+/* the library's CUDA stream (cudaStream_t) */
+void* sm2d_stream(sm2d_handle h);
+/* clear phase space, tallies and iteration state for a new spot */
+int sm2d_reset(sm2d_handle h);
+/* inject from a host beam description without waiting for the device */
+int sm2d_inject_async(sm2d_handle h, const sm2d_beam* beam);
+/* enqueue the device loop (<= max_iterations more iterations) */
+int sm2d_run_async(sm2d_handle h, int max_iterations);
+/* post-convolved dose [Nz][Nx] into host memory (pinned for an async copy) */
+int sm2d_dose_async(sm2d_handle h, double* host_dose);
+/* replay up to n_iterations eagerly with CUDA events around every kernel;
+ * ms5 receives the summed device time of classify, compact, transport,
+ * K4 gather and audit, *launches the number of kernel launches */
+int sm2d_run_profiled(sm2d_handle h, int n_iterations, int* iterations_done, float* ms5, int* launches);
+
+/* ---- host tables (no GPU needed) ---- */
+/* EnergyGrid(E_min,E_max,N) log grid (grids.cpp:6-24): edges[N+1], rep[N] */
+int sm2d_energy_grid_log(float E_min, float E_max, int N, float* edges, float* rep);
+/* EnergyGrid::CreatePiecewise (grids.cpp:37-97); groups = {E_start,E_end,dE}*n.
+ * Returns N_E; with edges == NULL only counts. */
+int sm2d_energy_grid_piecewise(int n_groups, const float* groups, float* edges, float* rep);
+/* AngularGrid (grids.cpp:121-137): edges[N+1], rep[N] */
+int sm2d_angular_grid(float theta_min, float theta_max, int N, float* edges, float* rep);
+/* GenerateRLUT(grid) (r_lut.cpp:69-129) on representative energies rep[N] */
+int sm2d_range_lut(int N, const float* rep, float* R, float* S, float* logE, float* logR, float* logS);
+/* Fermi-Eyges A(z), B(z), sigma_total(z) (k1k6_pipeline.cu:1061-1176) */
+int sm2d_fermi_eyges(float E0, int Nz, float dz, float sigma_x0, float* A, float* B, float* sigma_total);
+
+/* ---- raw stage entries on caller-owned device memory (stream may be 0) ---- */
+int sm2d_k1_active_mask(const uint32_t* d_block_ids, const float* d_values, uint8_t* d_mask,
+                        const uint8_t* d_mask_prev, int Nx, int Nz, int local_bins,
+                        int b_E_fine_on, int b_E_fine_off, float weight_active_min, void* stream);
+int sm2d_compact_lists(const uint8_t* d_mask, const uint32_t* d_block_ids, const float* d_values,
+                       int Nx, int Nz, int local_bins, uint32_t* d_active, int* d_n_active,
+                       uint32_t* d_coarse, int* d_n_coarse, void* stream);
+int sm2d_k4_bucket_transfer(const void* d_buckets, const int* d_cell_to_bucket_base,
+                            float* d_values_out, uint32_t* d_block_ids_out, int Nx, int Nz,
+                            int local_bins, int nt_local, int ne_local, int nx_sub,
+                            const float* d_E_edges, int N_E, int N_E_local,
+                            double* d_drop_weight_energy /* [2], accumulated */, void* stream);
+int sm2d_k5_conservation_audit(
+    const uint32_t* d_bid_in, const float* d_val_in, const uint32_t* d_bid_out, const float* d_val_out,
+    const double* d_EdepC, const double* d_AbsorbedEnergy_nuclear, const double* d_BoundaryLoss_energy,
+    const double* d_AbsorbedEnergy_cutoff, const double* d_PrevEdepC,
+    const double* d_PrevAbsorbedEnergy_nuclear, const double* d_PrevBoundaryLoss_energy,
+    const double* d_PrevAbsorbedEnergy_cutoff, const float* d_AbsorbedWeight_cutoff,
+    const float* d_AbsorbedWeight_nuclear, const float* d_BoundaryLoss_weight,
+    const float* d_PrevAbsorbedWeight_cutoff, const float* d_PrevAbsorbedWeight_nuclear,
+    const float* d_PrevBoundaryLoss_weight, float source_out_of_grid_weight,
+    float source_slot_dropped_weight, double source_out_of_grid_energy,
+    double source_slot_dropped_energy, float transport_dropped_weight,
+    double transport_dropped_energy, int include_source_terms, const float* d_E_edges, int N_E,
+    int nt_local, int N_E_local, int local_bins, sm2d_audit* d_report, int N_cells, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -32,6 +32,10 @@ class OrcConfig(C.Structure):
         ("enable_straggling", C.c_int), ("enable_nuclear", C.c_int),
         ("seed_slot_mode", C.c_int), ("energy_split", C.c_int),
         ("grid_E_min", C.c_float), ("grid_E_max", C.c_float),
+        ("prune_coarse", C.c_float), ("prune_fine", C.c_float),
+        ("split_min_weight", C.c_float), ("stop_weight_fraction", C.c_float),
+        ("claim_reserve_weight", C.c_float), ("slots_per_cell", C.c_int),
+        ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
     ]
 
 
@@ -73,6 +77,7 @@ def _lib(fp64: bool):
         lib.orc_create.argtypes = [C.POINTER(OrcConfig), C.c_int, P, C.c_int, P]
         lib.orc_destroy.argtypes = [P]
         lib.orc_local_bins.argtypes = [P]
+        lib.orc_slots_per_cell.argtypes = [P]
         lib.orc_inject.argtypes = [P] + [C.c_float] * 8 + [C.c_int, C.c_uint]
         lib.orc_set_psi_in.argtypes = [P, P, P]
         lib.orc_get_psi_in.argtypes = [P, P, P]
@@ -163,7 +168,7 @@ class Oracle:
         defaults = dict(x_min=0.0, z_min=0.0, E_fine_on=10.0, E_fine_off=11.0,
                         weight_active_min=1e-12, step_coarse=5.0, sigma_x_initial=0.0, E0=0.0,
                         enable_straggling=1, enable_nuclear=1, seed_slot_mode=0, energy_split=0,
-                        grid_E_min=0.0, grid_E_max=0.0)
+                        grid_E_min=0.0, grid_E_max=0.0, prune_coarse=0.0, prune_fine=0.0, split_min_weight=0.0, stop_weight_fraction=0.0, claim_reserve_weight=0.0, slots_per_cell=32, floor_cutoff=0, seed_iteration_salt=0)
         defaults.update(cfg)
         for name, _ in OrcConfig._fields_:
             setattr(c, name, defaults[name])
@@ -177,6 +182,7 @@ class Oracle:
         self.Nx, self.Nz = c.Nx, c.Nz
         self.Nc = c.Nx * c.Nz
         self.L = self.lib.orc_local_bins(self.ctx)
+        self.Kb = self.lib.orc_slots_per_cell(self.ctx)
 
     def close(self):
         if self.ctx:
@@ -197,12 +203,12 @@ class Oracle:
     def set_psi_in(self, bid, val):
         bid = np.ascontiguousarray(bid, np.uint32)
         val = np.ascontiguousarray(val, self.dtype)
-        assert bid.size == self.Nc * KB and val.size == self.Nc * KB * self.L
+        assert bid.size == self.Nc * self.Kb and val.size == self.Nc * self.Kb * self.L
         self.lib.orc_set_psi_in(self.ctx, _p(bid), _p(val))
 
     def psi_in(self, values=True):
-        bid = np.zeros(self.Nc * KB, np.uint32)
-        val = np.zeros(self.Nc * KB * self.L, self.dtype) if values else None
+        bid = np.zeros(self.Nc * self.Kb, np.uint32)
+        val = np.zeros(self.Nc * self.Kb * self.L, self.dtype) if values else None
         self.lib.orc_get_psi_in(self.ctx, _p(bid), _p(val) if values else None)
         return bid, val
 
@@ -263,11 +269,11 @@ def run_many(oracles, max_iterations, n_threads):
 
 
 # ---- psi rows in the reference debug-dump format ----------------------------
-def psi_rows(bid, val, L, thresh=1e-12):
+def psi_rows(bid, val, L, thresh=1e-12, Kb=KB):
     """Non-zero rows (cell, slot, bid, lidx, weight) with weight > thresh, the
     filter of the reference raw phase-space dump (k1k6_pipeline.cu:252)."""
-    v = val.reshape(-1, KB, L)
-    b = bid.reshape(-1, KB)
+    v = val.reshape(-1, Kb, L)
+    b = bid.reshape(-1, Kb)
     cells, slots, lidx = np.nonzero((v > thresh) & (b[:, :, None] != EMPTY))
     return dict(cell=cells, slot=slots, bid=b[cells, slots], lidx=lidx,
                 weight=v[cells, slots, lidx])

@@ -75,9 +75,9 @@ enum { FACE_ZP = 0, FACE_ZM = 1, FACE_XP = 2, FACE_XM = 3 };
 /* context                                                                    */
 /* ------------------------------------------------------------------------- */
 typedef struct bucket {           /* DeviceOutflowBucket, device_bucket.cuh:48-57 */
-    uint32_t bid[ORC_KB_OUT];
-    uint16_t count[ORC_KB_OUT];
-    real* val;                    /* [ORC_KB_OUT * L] */
+    uint32_t* bid;                /* [Kb] (the reference: 32 = DEVICE_Kb_out) */
+    uint16_t* count;              /* [Kb] */
+    real* val;                    /* [Kb * L] */
 } bucket;
 
 typedef struct rlut {             /* DeviceRLUT, device_lut.cuh:16-26 */
@@ -95,7 +95,7 @@ typedef struct psi_buf {
 
 struct orc_ctx {
     orc_config cfg;
-    int L, Nc;
+    int L, Nc, Kb;
     int N_theta, N_E;
     real* th_edges;               /* [N_theta+1] */
     real* E_edges;                /* [N_E+1] */
@@ -571,13 +571,14 @@ static inline int bid_distance(uint32_t a, uint32_t b) {
     return abs(ea - eb) * 8 + abs(ta - tb);
 }
 /* find exact / claim empty / fall back to nearest occupied slot */
-static int slot_with_fallback(uint32_t* ids, int n, uint32_t want, uint32_t* sel) {
+static int slot_with_fallback_n(uint32_t* ids, int n, int n_claim, uint32_t want, uint32_t* sel) {
     *sel = want;
     for (int s = 0; s < n; ++s) if (ids[s] == want) return s;
-    for (int s = 0; s < n; ++s) {
+    for (int s = 0; s < n_claim; ++s) {
         if (ids[s] == ORC_EMPTY) { ids[s] = want; return s; }
         if (ids[s] == want) return s;
     }
+    if (n_claim < 0) return -1;    /* light deposit of the split method: no merge */
     int best = -1, bd = 0x7fffffff;
     uint32_t bb = ORC_EMPTY;
     for (int s = 0; s < n; ++s) {
@@ -602,9 +603,32 @@ static int remap_lidx(const orc_ctx* c, int l, uint32_t src, uint32_t dst) {
     if (ed > c->cfg.ne_local - 1) ed = c->cfg.ne_local - 1;
     return enc_lidx(c, td, ed, x, z);
 }
+static int slot_with_fallback(uint32_t* ids, int n, uint32_t want, uint32_t* sel) {
+    return slot_with_fallback_n(ids, n, n, want, sel);
+}
+/* number of slots a deposit of weight w may claim */
+static inline int claimable(const orc_ctx* c, int n, double w) {
+    return (c->cfg.claim_reserve_weight > 0.0f && w < (double)c->cfg.claim_reserve_weight) ? n - 8 : n;
+}
+/* slot claim of a deposit of weight w: light deposits of the split method
+ * claim among the first 24 slots and are dropped (not merged) when those
+ * are taken; heavy ones use all 32 and the nearest-block fallback */
+static int claim_w(const orc_ctx* c, uint32_t* ids, int n, uint32_t want, uint32_t* sel, double w) {
+    int nc = claimable(c, n, w);
+    if (nc < n) {
+        *sel = want;
+        for (int s = 0; s < n; ++s) if (ids[s] == want) return s;
+        for (int s = 0; s < nc; ++s) {
+            if (ids[s] == ORC_EMPTY) { ids[s] = want; return s; }
+            if (ids[s] == want) return s;
+        }
+        return -1;
+    }
+    return slot_with_fallback_n(ids, n, n, want, sel);
+}
 /* psi_out slot claim marks the cell occupied */
-static int psi_slot(orc_ctx* c, psi_buf* p, int cell, uint32_t want, uint32_t* sel) {
-    int s = slot_with_fallback(&p->bid[(size_t)cell * ORC_KB], ORC_KB, want, sel);
+static int psi_slot(orc_ctx* c, psi_buf* p, int cell, uint32_t want, uint32_t* sel, double w) {
+    int s = claim_w(c, &p->bid[(size_t)cell * c->Kb], c->Kb, want, sel, w);
     if (s >= 0) p->occ[cell] = 1;
     return s;
 }
@@ -620,7 +644,7 @@ static inline real e_center(const orc_ctx* c, int b) {
 /* reference: one bin, the one containing E (device_find_bin_edges).
  * energy_split: mean-preserving split between the two neighbouring bin
  * centres (method extension needed on coarse log grids). */
-static eparts bin_energy(const orc_ctx* c, real E) {
+static eparts bin_energy(const orc_ctx* c, real E, real w) {
     eparts p;
     int k = find_bin_edges(c->E_edges, c->N_E, E);
     p.n = 1; p.bin[0] = k; p.frac[0] = RL(1.0); p.bin[1] = k; p.frac[1] = RL(0.0);
@@ -634,6 +658,11 @@ static eparts bin_energy(const orc_ctx* c, real E) {
     real fh = (E - cl) / (ch - cl);
     if (fh <= RL(0.0)) { p.bin[0] = lo; p.Erep = cl; return p; }
     if (fh >= RL(1.0)) { p.bin[0] = hi; p.Erep = ch; return p; }
+    if (w * r_min(fh, RL(1.0) - fh) < (real)c->cfg.split_min_weight) {
+        /* light minor part: keep the whole component in the nearer centre */
+        if (fh >= RL(0.5)) { p.bin[0] = hi; p.Erep = ch; } else { p.bin[0] = lo; p.Erep = cl; }
+        return p;
+    }
     p.n = 2;
     p.bin[0] = lo; p.frac[0] = RL(1.0) - fh;
     p.bin[1] = hi; p.frac[1] = fh;
@@ -644,7 +673,13 @@ static eparts bin_energy(const orc_ctx* c, real E) {
 /* ------------------------------------------------------------------------- */
 /* bucket emission: device_bucket.cuh:431-533 (4-D, theta 2-bin split)       */
 /* ------------------------------------------------------------------------- */
-static real emit_to_bucket(orc_ctx* c, bucket* bk, real theta, real E, real weight, int xs, int zs) {
+/* energy-bin index of local bin l of block bid */
+static inline int ebin_of(const orc_ctx* c, uint32_t bid, int l) {
+    return (int)((bid >> 12) & 0xFFFu) * c->cfg.ne_local + (l / c->cfg.nt_local) % c->cfg.ne_local;
+}
+/* The split method keeps energy when a saturated slot table re-bins a part
+ * into another block: the shift (intended - stored centre) * w goes to *eshift. */
+static real emit_to_bucket(orc_ctx* c, bucket* bk, real theta, real E, real weight, int xs, int zs, double* eshift) {
     if (weight <= RL(0.0)) return RL(0.0);
     real tmin = c->th_edges[0], tmax = c->th_edges[c->N_theta];
     real dth = (tmax - tmin) / (real)c->N_theta;
@@ -664,9 +699,13 @@ static real emit_to_bucket(orc_ctx* c, bucket* bk, real theta, real E, real weig
         real f = r_min(RL(1.0), r_fabs(dlt) / dth);
         tw[1] = f * f;
         tw[0] = RL(1.0) - tw[1];
+        if (c->cfg.energy_split && weight * tw[1] < (real)c->cfg.split_min_weight) {
+            tw[1] = RL(0.0);
+            tw[0] = RL(1.0);
+        }
     }
     real Ec = r_max(c->E_edges[0], r_min(E, c->E_edges[c->N_E]));
-    eparts ep = bin_energy(c, Ec);
+    eparts ep = bin_energy(c, Ec, weight);
     real dropped = RL(0.0);
     for (int ei = 0; ei < ep.n; ++ei) {
         int Eb = ep.bin[ei];
@@ -681,9 +720,11 @@ static real emit_to_bucket(orc_ctx* c, bucket* bk, real theta, real E, real weig
             uint32_t want = enc_block((uint32_t)(tbin / c->cfg.nt_local), bE);
             int l = enc_lidx(c, tbin % c->cfg.nt_local, El, xs, zs);
             uint32_t sel;
-            int s = slot_with_fallback(bk->bid, ORC_KB_OUT, want, &sel);
+            int s = claim_w(c, bk->bid, c->Kb, want, &sel, (double)we);
             if (s < 0) { dropped += we; continue; }
             int le = (sel == want) ? l : remap_lidx(c, l, want, sel);
+            if (sel != want && c->cfg.energy_split && eshift)
+                *eshift += (double)((e_center(c, Eb) - e_center(c, ebin_of(c, sel, le))) * we);
             bk->val[(size_t)s * c->L + le] += we;
             bk->count[s]++;
         }
@@ -718,7 +759,7 @@ static int neighbor(int cell, int face, int Nx, int Nz) {
 
 /* +z emission with N-cell lateral Gaussian split: device_bucket.cuh:857-987 */
 static real emit_lateral_spread(orc_ctx* c, int src, int tz, real theta, real E, real weight,
-                                real xoff, real sigma, real* boundary_w) {
+                                real xoff, real sigma, real* boundary_w, double* eshift) {
     if (weight <= RL(0.0)) return RL(0.0);
     real dropped = RL(0.0);
     sigma = r_max(sigma, RL(1e-6));
@@ -745,7 +786,7 @@ static real emit_lateral_spread(orc_ctx* c, int src, int tz, real theta, real E,
         int bi = bucket_index(c, emit_cell, FACE_ZP);
         if (bi < 0) { dropped += weight * wf; continue; }
         int xt = off < 0 ? c->cfg.nx_sub - 1 : (off > 0 ? 0 : c->cfg.nx_sub / 2);
-        dropped += emit_to_bucket(c, &c->buckets[bi], theta, E, weight * wf, xt, 0);
+        dropped += emit_to_bucket(c, &c->buckets[bi], theta, E, weight * wf, xt, 0, eshift);
     }
     return dropped;
 }
@@ -758,10 +799,14 @@ typedef struct tally {
     float w_cut, w_nuc, w_bnd;
 } tally;
 
+static inline unsigned iter_salt(const orc_ctx* c) {
+    return c->cfg.seed_iteration_salt ? (unsigned)(c->iter - 1) * 0x9E3779B9u : 0u;
+}
+
 static int seed_slot(const orc_ctx* c, const uint32_t* ids, int slot) {
     if (c->cfg.seed_slot_mode == 0) return slot;
     int r = 0;
-    for (int s = 0; s < ORC_KB; ++s)
+    for (int s = 0; s < c->Kb; ++s)
         if (ids[s] != ORC_EMPTY && ids[s] < ids[slot]) ++r;
     return r;
 }
@@ -778,7 +823,7 @@ static int emit_stay(orc_ctx* c, int k3, int cell, real theta_new, real E_new, r
     real dth = (tmax - tmin) / (real)c->N_theta;
     int tbn = (int)((theta_new - tmin) / dth);
     tbn = (int)r_max(RL(0.0), r_min((real)tbn, (real)(c->N_theta - 1)));
-    eparts ep = bin_energy(c, E_new);
+    eparts ep = bin_energy(c, E_new, w_new);
     int nxs = c->cfg.nx_sub;
     real w[64];
     spread_weights_subcell(w, x_new, sig_sub, dx, nxs);
@@ -799,8 +844,8 @@ static int emit_stay(orc_ctx* c, int k3, int cell, real theta_new, real E_new, r
         int Eb = ep.bin[ei];
         uint32_t want = ((uint32_t)(Eb / c->cfg.ne_local) << 12) | ((uint32_t)(tbn / c->cfg.nt_local) & 0xFFFu);
         uint32_t sel;
-        int os = psi_slot(c, po, cell, want, &sel);
         real wpart = c->cfg.energy_split ? w_new * ep.frac[ei] : w_new;
+        int os = psi_slot(c, po, cell, want, &sel, (double)wpart);
         if (os < 0) {
             double *cw = k3 ? &c->k3_slot_w : &c->k2_slot_w, *ce = k3 ? &c->k3_slot_e : &c->k2_slot_e;
             *cw += (double)wpart;
@@ -818,12 +863,13 @@ static int emit_stay(orc_ctx* c, int k3, int cell, real theta_new, real E_new, r
             if (Ebe > e0 + c->cfg.ne_local - 1) Ebe = e0 + c->cfg.ne_local - 1;
         }
         if (!c->cfg.energy_split) E_emit = e_center(c, Ebe);
+        else if (Ebe != Eb) t->edep += (double)((e_center(c, Eb) - e_center(c, Ebe)) * wpart * wcf);
         int tl = tbe % c->cfg.nt_local, El = Ebe % c->cfg.ne_local;
         for (int xs = 0; xs < nxs; ++xs) {
             real wf = (w[xs] / wsum) * wcf;
             if (wf <= RL(0.0)) continue;
             int l = enc_lidx(c, tl, El, xs, zst);
-            po->val[((size_t)cell * ORC_KB + os) * c->L + l] += wpart * wf;
+            po->val[((size_t)cell * c->Kb + os) * c->L + l] += wpart * wf;
         }
     }
     real wl = RL(0.0), wr = RL(0.0);
@@ -848,7 +894,7 @@ static int emit_stay(orc_ctx* c, int k3, int cell, real theta_new, real E_new, r
                     return 1;
                 }
                 real d = emit_to_bucket(c, &c->buckets[bi], theta_new, E_new, ws, nxs - 1,
-                                        sub_bin(z_new, dz, c->cfg.nz_sub));
+                                        sub_bin(z_new, dz, c->cfg.nz_sub), &t->edep);
                 if (d > RL(0.0)) { *bw += (double)d; *be += (double)(E_new * d); }
             } else {
                 t->w_bnd += (float)ws;
@@ -865,7 +911,7 @@ static int emit_stay(orc_ctx* c, int k3, int cell, real theta_new, real E_new, r
                     return 1;
                 }
                 real d = emit_to_bucket(c, &c->buckets[bi], theta_new, E_new, ws, 0,
-                                        sub_bin(z_new, dz, c->cfg.nz_sub));
+                                        sub_bin(z_new, dz, c->cfg.nz_sub), &t->edep);
                 if (d > RL(0.0)) { *bw += (double)d; *be += (double)(E_new * d); }
             } else {
                 t->w_bnd += (float)ws;
@@ -898,13 +944,13 @@ static void emit_cross(orc_ctx* c, int k3, int cell, int face, real theta_new, r
         t->e_bnd += (double)(E_new * w_new);
         return;
     }
-    eparts ep = bin_energy(c, E_new);
+    eparts ep = bin_energy(c, E_new, w_new);
     real E_emit_tr = ep.Erep;
     int fold = k3 || c->cfg.energy_split;
     if (face == FACE_ZP) {
         int tz = cell / Nx + 1;
         real lbw = RL(0.0);
-        real d = emit_lateral_spread(c, cell, tz, theta_new, E_new, w_new, x_new, sig_tr, &lbw);
+        real d = emit_lateral_spread(c, cell, tz, theta_new, E_new, w_new, x_new, sig_tr, &lbw, &t->edep);
         if (lbw > RL(0.0)) {
             t->w_bnd += (float)lbw;
             t->e_bnd += (double)(E_new * lbw);
@@ -928,7 +974,7 @@ static void emit_cross(orc_ctx* c, int k3, int cell, int face, real theta_new, r
         *be += (double)(E_new * w_new);
         return;
     }
-    real d = emit_to_bucket(c, &c->buckets[bi], theta_new, E_new, w_new, xsn, zsn);
+    real d = emit_to_bucket(c, &c->buckets[bi], theta_new, E_new, w_new, xsn, zsn, &t->edep);
     if (d > RL(0.0)) { *bw += (double)d; *be += (double)(E_new * d); }
     if (fold) {
         real tw = r_max(RL(0.0), w_new - d);
@@ -954,14 +1000,14 @@ static void k2_cell(orc_ctx* c, int cell) {
     const rlut* lut = &c->lut;
     tally t = {0};
     real cstep = r_min((real)c->cfg.step_coarse, r_min(dx, dz));
-    const uint32_t* ids = &pi->bid[(size_t)cell * ORC_KB];
-    for (int slot = 0; slot < ORC_KB; ++slot) {
+    const uint32_t* ids = &pi->bid[(size_t)cell * c->Kb];
+    for (int slot = 0; slot < c->Kb; ++slot) {
         uint32_t bid = ids[slot];
         if (bid == ORC_EMPTY) continue;
         uint32_t bt = bid & 0xFFFu, bE = (bid >> 12) & 0xFFFu;
         int sslot = seed_slot(c, ids, slot);
         for (int l = 0; l < c->L; ++l) {
-            real w = pi->val[((size_t)cell * ORC_KB + slot) * c->L + l];
+            real w = pi->val[((size_t)cell * c->Kb + slot) * c->L + l];
             if (w <= RL(0.0)) continue;
             int tl, El, xs, zs;
             dec_lidx(c, l, &tl, &El, &xs, &zs);
@@ -971,7 +1017,7 @@ static void k2_cell(orc_ctx* c, int cell) {
             real dth = (tmax - tmin) / (real)c->N_theta;
             real theta = tmin + ((real)tbin + RL(0.5)) * dth;
             real E = c->E_edges[Ebin] + RL(1.0) * ((c->E_edges[Ebin + 1] - c->E_edges[Ebin]) * RL(0.5));
-            if (w < K2_PRUNE) {
+            if (w < (c->cfg.prune_coarse > 0.0f ? (real)c->cfg.prune_coarse : K2_PRUNE)) {
                 c->k2_prune_w += (double)w;
                 c->k2_prune_e += (double)(E * w);
                 continue;
@@ -1034,7 +1080,7 @@ static void k2_cell(orc_ctx* c, int cell) {
             real sig_tr = r_max(r_sin(r_min(sig_th, RL(1.57))) * step_mm / RL(1.7320508), RL(0.01));
             unsigned pseed = (unsigned)r_min(path0 * RL(1000.0), RL(4294967295.0));
             unsigned ts = ((unsigned)(cell + 1) * SEED_A) ^ ((unsigned)(sslot + 1) * SEED_B) ^
-                          ((unsigned)(l + 1) * SEED_C) ^ (unsigned)(Ebin + 17) ^ (pseed * 747796405u);
+                          ((unsigned)(l + 1) * SEED_C) ^ (unsigned)(Ebin + 17) ^ (pseed * 747796405u) ^ iter_salt(c);
             real scat = (sig_th <= RL(0.0)) ? RL(0.0) : gauss_sample(&ts) * sig_th;
             real theta_new = theta + scat;
             theta_new = r_max(c->th_edges[0], r_min(theta_new, c->th_edges[c->N_theta]));
@@ -1047,7 +1093,7 @@ static void k2_cell(orc_ctx* c, int cell) {
             t.edep += (double)edep;
             t.w_nuc += (float)w_rem;
             t.e_nuc += (double)E_rem;
-            if (E_new <= E_CUTOFF) {
+            if (E_new <= E_CUTOFF || ((c->cfg.energy_split || c->cfg.floor_cutoff) && E_new <= e_center(c, 0))) {
                 t.w_cut += (float)w_new;
                 t.e_cut += (double)(E_new * w_new);
                 continue;
@@ -1066,14 +1112,14 @@ static void k3_cell(orc_ctx* c, int cell) {
     const real dx = (real)c->cfg.dx, dz = (real)c->cfg.dz;
     const rlut* lut = &c->lut;
     tally t = {0};
-    const uint32_t* ids = &pi->bid[(size_t)cell * ORC_KB];
-    for (int slot = 0; slot < ORC_KB; ++slot) {
+    const uint32_t* ids = &pi->bid[(size_t)cell * c->Kb];
+    for (int slot = 0; slot < c->Kb; ++slot) {
         uint32_t bid = ids[slot];
         if (bid == ORC_EMPTY) continue;
         uint32_t bt = bid & 0xFFFu, bE = (bid >> 12) & 0xFFFu;
         int sslot = seed_slot(c, ids, slot);
         for (int l = 0; l < c->L; ++l) {
-            real w = pi->val[((size_t)cell * ORC_KB + slot) * c->L + l];
+            real w = pi->val[((size_t)cell * c->Kb + slot) * c->L + l];
             if (w <= RL(0.0)) continue;
             int tl, El, xs, zs;
             dec_lidx(c, l, &tl, &El, &xs, &zs);
@@ -1085,7 +1131,7 @@ static void k3_cell(orc_ctx* c, int cell) {
             if (Ebin > c->N_E - 1) Ebin = c->N_E - 1;
             real El_ = c->E_edges[Ebin], Eu_ = c->E_edges[Ebin + 1];
             real E = El_ + RL(1.0) * ((Eu_ - El_) * RL(0.5));
-            if (w < K3_PRUNE) {
+            if (w < (c->cfg.prune_fine > 0.0f ? (real)c->cfg.prune_fine : K3_PRUNE)) {
                 c->k3_prune_w += (double)w;
                 c->k3_prune_e += (double)(E * w);
                 continue;
@@ -1113,7 +1159,7 @@ static void k3_cell(orc_ctx* c, int cell) {
             real mean_dE = lut_energy_deposition(lut, E, step);
             real dE;
             if (c->cfg.enable_straggling) {
-                unsigned seed = (unsigned)(cell * 7 + sslot * 13 + l * 17) ^ 0xDEECE66Du;
+                unsigned seed = ((unsigned)(cell * 7 + sslot * 13 + l * 17) ^ 0xDEECE66Du) ^ iter_salt(c);
                 real sE = straggling_sigma(E, step, RL(1.0));
                 if (sE <= RL(0.0)) dE = mean_dE;
                 else {
@@ -1140,7 +1186,7 @@ static void k3_cell(orc_ctx* c, int cell) {
             real sig_x = r_max(r_sqrt(dC), RL(0.01));
             unsigned pseed = (unsigned)r_min((real)iz * dz * RL(1000.0), RL(4294967295.0));
             unsigned ts = ((unsigned)(cell + 1) * SEED_A) ^ ((unsigned)(sslot + 1) * SEED_B) ^
-                          ((unsigned)(l + 1) * SEED_C) ^ (unsigned)(Ebin + 17) ^ (pseed * 747796405u);
+                          ((unsigned)(l + 1) * SEED_C) ^ (unsigned)(Ebin + 17) ^ (pseed * 747796405u) ^ iter_salt(c);
             real scat = (sig_th <= RL(0.0)) ? RL(0.0) : gauss_sample(&ts) * sig_th;
             real theta_new = theta + scat;
             theta_new = r_max(c->th_edges[0], r_min(theta_new, c->th_edges[c->N_theta]));
@@ -1153,7 +1199,7 @@ static void k3_cell(orc_ctx* c, int cell) {
             t.edep += (double)edep;
             t.w_nuc += (float)w_rem;
             t.e_nuc += (double)E_rem;
-            if (E_new <= E_CUTOFF) {
+            if (E_new <= E_CUTOFF || ((c->cfg.energy_split || c->cfg.floor_cutoff) && E_new <= e_center(c, 0))) {
                 t.w_cut += (float)w_new;
                 t.e_cut += (double)(E_new * w_new);
                 continue;
@@ -1183,13 +1229,15 @@ static void k4(orc_ctx* c) {
             int base = c->cell_to_bucket[src];
             if (base < 0) continue;
             bucket* bk = &c->buckets[base + sf];
-            for (int s = 0; s < ORC_KB_OUT; ++s) {
+            for (int s = 0; s < c->Kb; ++s) {
                 uint32_t bid = bk->bid[s];
                 if (bid == ORC_EMPTY) continue;
                 uint32_t bE = (bid >> 12) & 0xFFFu;
                 uint32_t sel;
-                int os = psi_slot(c, po, cell, bid, &sel);
                 const real* v = &bk->val[(size_t)s * c->L];
+                double wsl = 0.0;
+                for (int l = 0; l < c->L; ++l) wsl += (double)v[l];
+                int os = psi_slot(c, po, cell, bid, &sel, wsl);
                 if (os < 0) {
                     double dw = 0.0, de = 0.0;
                     for (int l = 0; l < c->L; ++l) {
@@ -1211,7 +1259,10 @@ static void k4(orc_ctx* c) {
                 for (int l = 0; l < c->L; ++l) {
                     if (v[l] > RL(0.0)) {
                         int le = (sel != bid) ? remap_lidx(c, l, bid, sel) : l;
-                        po->val[((size_t)cell * ORC_KB + os) * c->L + le] += v[l];
+                        if (sel != bid && c->cfg.energy_split)
+                            c->edep[cell] += (double)((e_center(c, ebin_of(c, bid, l)) -
+                                                       e_center(c, ebin_of(c, sel, le))) * v[l]);
+                        po->val[((size_t)cell * c->Kb + os) * c->L + le] += v[l];
                     }
                 }
             }
@@ -1231,13 +1282,13 @@ static void k1_and_lists(orc_ctx* c, int b_on, int b_off) {
         if (!pi->occ[cell]) { c->mask[cell] = 0; continue; }
         float W = 0.0f;
         int on = 0, off = 0, has_w = 0;
-        const uint32_t* ids = &pi->bid[(size_t)cell * ORC_KB];
-        for (int s = 0; s < ORC_KB; ++s) {
+        const uint32_t* ids = &pi->bid[(size_t)cell * c->Kb];
+        for (int s = 0; s < c->Kb; ++s) {
             if (ids[s] == ORC_EMPTY) continue;
             uint32_t bE = (ids[s] >> 12) & 0xFFFu;
             if (bE <= (uint32_t)b_on) on = 1;
             if (bE <= (uint32_t)b_off) off = 1;
-            const real* v = &pi->val[((size_t)cell * ORC_KB + s) * c->L];
+            const real* v = &pi->val[((size_t)cell * c->Kb + s) * c->L];
             for (int l = 0; l < c->L; ++l) {
                 W += (float)v[l];
                 if (v[l] > RL(0.0)) has_w = 1;
@@ -1274,12 +1325,12 @@ static void psi_totals(const orc_ctx* c, const psi_buf* p, double* W, double* E)
     *E = 0.0;
     for (int cell = 0; cell < c->Nc; ++cell) {
         if (!p->occ[cell]) continue;
-        for (int s = 0; s < ORC_KB; ++s) {
-            uint32_t bid = p->bid[(size_t)cell * ORC_KB + s];
+        for (int s = 0; s < c->Kb; ++s) {
+            uint32_t bid = p->bid[(size_t)cell * c->Kb + s];
             if (bid == ORC_EMPTY) continue;
             int bE = (int)((bid >> 12) & 0xFFFu);
             for (int l = 0; l < c->L; ++l) {
-                real w = p->val[((size_t)cell * ORC_KB + s) * c->L + l];
+                real w = p->val[((size_t)cell * c->Kb + s) * c->L + l];
                 if (w <= RL(0.0)) continue;
                 int El = (l / c->cfg.nt_local) % c->cfg.ne_local;
                 int Eb = bE * c->cfg.ne_local + El;
@@ -1303,12 +1354,12 @@ static void k5(orc_ctx* c, float drop_w, double drop_e, int include_source) {
         for (int pass = 0; pass < 2; ++pass) {
             psi_buf* p = pass ? po : pi;
             if (!p->occ[cell]) continue;
-            for (int s = 0; s < ORC_KB; ++s) {
-                uint32_t bid = p->bid[(size_t)cell * ORC_KB + s];
+            for (int s = 0; s < c->Kb; ++s) {
+                uint32_t bid = p->bid[(size_t)cell * c->Kb + s];
                 if (bid == ORC_EMPTY) continue;
                 uint32_t bE = (bid >> 12) & 0xFFFu;
                 for (int l = 0; l < c->L; ++l) {
-                    real w = p->val[((size_t)cell * ORC_KB + s) * c->L + l];
+                    real w = p->val[((size_t)cell * c->Kb + s) * c->L + l];
                     if (w <= RL(0.0)) continue;
                     int El = (l / c->cfg.nt_local) % c->cfg.ne_local;
                     int Eb = (int)bE * c->cfg.ne_local + El;
@@ -1375,8 +1426,8 @@ static void k5(orc_ctx* c, float drop_w, double drop_e, int include_source) {
 static void psi_clear(orc_ctx* c, psi_buf* p) {
     for (int cell = 0; cell < c->Nc; ++cell) {
         if (!p->occ[cell]) continue;
-        for (int s = 0; s < ORC_KB; ++s) {
-            size_t k = (size_t)cell * ORC_KB + s;
+        for (int s = 0; s < c->Kb; ++s) {
+            size_t k = (size_t)cell * c->Kb + s;
             if (p->bid[k] != ORC_EMPTY) {
                 memset(&p->val[k * c->L], 0, sizeof(real) * c->L);
                 p->bid[k] = ORC_EMPTY;
@@ -1391,23 +1442,30 @@ static void psi_clear(orc_ctx* c, psi_buf* p) {
 static void prepare_buckets(orc_ctx* c, const uint32_t* list, int n) {
     for (int i = 0; i < c->Nc; ++i) c->cell_to_bucket[i] = -1;
     if (n * 4 > c->n_buckets_cap) {
-        for (int i = 0; i < c->n_buckets_cap; ++i) free(c->buckets[i].val);
+        for (int i = 0; i < c->n_buckets_cap; ++i) {
+            free(c->buckets[i].val);
+            free(c->buckets[i].bid);
+            free(c->buckets[i].count);
+        }
         free(c->buckets);
         c->n_buckets_cap = n * 4;
         c->buckets = (bucket*)calloc((size_t)c->n_buckets_cap, sizeof(bucket));
-        for (int i = 0; i < c->n_buckets_cap; ++i)
-            c->buckets[i].val = (real*)calloc((size_t)ORC_KB_OUT * c->L, sizeof(real));
+        for (int i = 0; i < c->n_buckets_cap; ++i) {
+            c->buckets[i].val = (real*)calloc((size_t)c->Kb * c->L, sizeof(real));
+            c->buckets[i].bid = (uint32_t*)calloc((size_t)c->Kb, sizeof(uint32_t));
+            c->buckets[i].count = (uint16_t*)calloc((size_t)c->Kb, sizeof(uint16_t));
+        }
     }
     for (int i = 0; i < n; ++i) c->cell_to_bucket[list[i]] = i * 4;
     for (int b = 0; b < n * 4; ++b) {
-        for (int s = 0; s < ORC_KB_OUT; ++s) { c->buckets[b].bid[s] = ORC_EMPTY; c->buckets[b].count[s] = 0; }
-        memset(c->buckets[b].val, 0, sizeof(real) * ORC_KB_OUT * c->L);
+        for (int s = 0; s < c->Kb; ++s) { c->buckets[b].bid[s] = ORC_EMPTY; c->buckets[b].count[s] = 0; }
+        memset(c->buckets[b].val, 0, sizeof(real) * c->Kb * c->L);
     }
 }
 
 static size_t count_slots(const orc_ctx* c, const psi_buf* p, int cell) {
     size_t n = 0;
-    for (int s = 0; s < ORC_KB; ++s) if (p->bid[(size_t)cell * ORC_KB + s] != ORC_EMPTY) ++n;
+    for (int s = 0; s < c->Kb; ++s) if (p->bid[(size_t)cell * c->Kb + s] != ORC_EMPTY) ++n;
     return n;
 }
 
@@ -1419,7 +1477,13 @@ int orc_step(orc_ctx* c) {
     int b_on = e_bin_threshold(c, c->cfg.E_fine_on);
     int b_off = e_bin_threshold(c, c->cfg.E_fine_off);
     k1_and_lists(c, b_on, b_off);
-    if (c->n_active == 0 && c->n_coarse == 0) {
+    int light = 0;
+    if (c->cfg.stop_weight_fraction > 0.0f && c->iter > 1) {
+        double W, E;
+        psi_totals(c, psi_in(c), &W, &E);
+        light = W < (double)c->cfg.stop_weight_fraction * (double)c->src_inj_w;
+    }
+    if ((c->n_active == 0 && c->n_coarse == 0) || light) {
         double W, E;
         psi_totals(c, psi_in(c), &W, &E);
         if (W > 0.0 || E > 0.0) { c->transport_drop_w += W; c->transport_drop_e += E; }
@@ -1510,15 +1574,15 @@ static int inject_one(orc_ctx* c, int cell, real theta, real E, real weight, rea
     uint32_t want = enc_block((uint32_t)(tb / c->cfg.nt_local), (uint32_t)(Eb / c->cfg.ne_local));
     int l = enc_lidx(c, tb % c->cfg.nt_local, Eb % c->cfg.ne_local, xs, zs);
     psi_buf* p = psi_in(c);
-    uint32_t* ids = &p->bid[(size_t)cell * ORC_KB];
+    uint32_t* ids = &p->bid[(size_t)cell * c->Kb];
     int slot = -1;
-    for (int s = 0; s < ORC_KB; ++s) {            /* device_psic_find_or_allocate_slot */
+    for (int s = 0; s < c->Kb; ++s) {            /* device_psic_find_or_allocate_slot */
         if (ids[s] == ORC_EMPTY) { ids[s] = want; slot = s; break; }
         if (ids[s] == want) { slot = s; break; }
     }
     if (slot < 0) return 0;
     p->occ[cell] = 1;
-    p->val[((size_t)cell * ORC_KB + slot) * c->L + l] += weight;
+    p->val[((size_t)cell * c->Kb + slot) * c->L + l] += weight;
     return 1;
 }
 
@@ -1585,6 +1649,7 @@ orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* th_edges, i
     orc_ctx* c = (orc_ctx*)calloc(1, sizeof(orc_ctx));
     c->cfg = *cfg;
     c->L = cfg->nt_local * cfg->ne_local * cfg->nx_sub * cfg->nz_sub;
+    c->Kb = cfg->slots_per_cell > 0 ? cfg->slots_per_cell : 32;
     c->Nc = cfg->Nx * cfg->Nz;
     c->N_theta = N_theta;
     c->N_E = N_E;
@@ -1611,7 +1676,7 @@ orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* th_edges, i
     c->fe_B = (float*)calloc(cfg->Nz, sizeof(float));
     c->fe_sigma = (float*)calloc(cfg->Nz, sizeof(float));
     orc_fe_precompute(cfg->E0, cfg->Nz, cfg->dz, cfg->sigma_x_initial, c->fe_A, c->fe_B, c->fe_sigma);
-    size_t ns = (size_t)c->Nc * ORC_KB;
+    size_t ns = (size_t)c->Nc * c->Kb;
     for (int b = 0; b < 2; ++b) {
         c->buf[b].bid = (uint32_t*)malloc(sizeof(uint32_t) * ns);
         memset(c->buf[b].bid, 0xFF, sizeof(uint32_t) * ns);
@@ -1652,28 +1717,33 @@ void orc_destroy(orc_ctx* c) {
     free(c->w_cut); free(c->w_nuc); free(c->w_bnd);
     free(c->p_edep); free(c->p_e_cut); free(c->p_e_nuc); free(c->p_e_bnd);
     free(c->p_w_cut); free(c->p_w_nuc); free(c->p_w_bnd);
-    for (int i = 0; i < c->n_buckets_cap; ++i) free(c->buckets[i].val);
+    for (int i = 0; i < c->n_buckets_cap; ++i) {
+        free(c->buckets[i].val);
+        free(c->buckets[i].bid);
+        free(c->buckets[i].count);
+    }
     free(c->buckets);
     free(c->cell_to_bucket);
     free(c);
 }
 
 int orc_local_bins(const orc_ctx* c) { return c->L; }
+int orc_slots_per_cell(const orc_ctx* c) { return c->Kb; }
 
 void orc_set_psi_in(orc_ctx* c, const uint32_t* bid, const orc_real* val) {
     psi_buf* p = psi_in(c);
-    size_t ns = (size_t)c->Nc * ORC_KB;
+    size_t ns = (size_t)c->Nc * c->Kb;
     memcpy(p->bid, bid, sizeof(uint32_t) * ns);
     memcpy(p->val, val, sizeof(real) * ns * c->L);
     for (int cell = 0; cell < c->Nc; ++cell) {
         p->occ[cell] = 0;
-        for (int s = 0; s < ORC_KB; ++s) if (p->bid[(size_t)cell * ORC_KB + s] != ORC_EMPTY) p->occ[cell] = 1;
+        for (int s = 0; s < c->Kb; ++s) if (p->bid[(size_t)cell * c->Kb + s] != ORC_EMPTY) p->occ[cell] = 1;
     }
 }
 
 void orc_get_psi_in(const orc_ctx* c, uint32_t* bid, orc_real* val) {
     const psi_buf* p = &c->buf[c->in_idx];
-    size_t ns = (size_t)c->Nc * ORC_KB;
+    size_t ns = (size_t)c->Nc * c->Kb;
     memcpy(bid, p->bid, sizeof(uint32_t) * ns);
     if (val) memcpy(val, p->val, sizeof(real) * ns * c->L);
 }

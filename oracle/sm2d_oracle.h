@@ -29,8 +29,7 @@ typedef double orc_real;
 typedef float orc_real;
 #endif
 
-#define ORC_KB 32          /* slots per cell     (device_psic.cuh:30)   */
-#define ORC_KB_OUT 32      /* slots per bucket   (device_bucket.cuh:26) */
+#define ORC_KB 32          /* default slots per cell and per bucket (device_psic.cuh:30, device_bucket.cuh:26) */
 #define ORC_EMPTY 0xFFFFFFFFu
 
 typedef struct orc_config {
@@ -51,6 +50,30 @@ typedef struct orc_config {
     /* EnergyGrid::E_min/E_max (the constructor arguments; DeviceRLUT takes
      * these, not edges[0]/edges[N]).  0 means "use the edges". */
     float grid_E_min, grid_E_max;
+    /* weight below which K2 / K3 drop a component into the transport-drop
+     * channel; 0 means the reference values 1e-12 / 1e-15 */
+    float prune_coarse, prune_fine;
+    /* energy-split method: a split part lighter than this stays in the major
+     * bin (energy difference folded into the deposit); 0 = always split */
+    float split_min_weight;
+    /* stop when the in-flight weight falls below this fraction of the
+     * injected weight (remainder booked as transport drop); 0 = reference
+     * behaviour (stop only when no cell is listed) */
+    float stop_weight_fraction;
+    /* deposits lighter than this may claim only the first 24 slots of a
+     * cell or bucket and otherwise merge into the nearest block, keeping 8
+     * slots for heavy components; 0 = reference (all 32 claimable) */
+    float claim_reserve_weight;
+    /* block slots per cell (0 = 32, the reference's DEVICE_Kb) */
+    int slots_per_cell;
+    /* 1: a component whose new energy is below the lowest bin centre is
+     * absorbed (cutoff) instead of being re-binned up to that centre, which
+     * otherwise stalls it at the grid floor; 0 = reference */
+    int floor_cutoff;
+    /* 1: MCS / straggling seeds are salted with the iteration index
+     * ((iter-1) * 0x9E3779B9, so the first iteration is unchanged); the
+     * reference re-draws the same numbers for a bin every iteration */
+    int seed_iteration_salt;
 } orc_config;
 
 typedef struct orc_audit {       /* AuditReport, k5_audit.cuh:5-27 */
@@ -81,6 +104,7 @@ orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* theta_edges
                     int N_E, const float* E_edges);
 void orc_destroy(orc_ctx* c);
 int  orc_local_bins(const orc_ctx* c);
+int  orc_slots_per_cell(const orc_ctx* c);
 
 /* source injection (k1k6_pipeline.cu:300-551, gpu_transport_wrapper.cu:339-460) */
 void orc_inject(orc_ctx* c, float x0, float z0, float theta0, float E0, float W_total,

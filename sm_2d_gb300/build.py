@@ -1,0 +1,81 @@
+"""In-tree build of libsm2d.so: the sm_103a CUDA kernels + C ABI.
+
+nvcc compiles the CUDA translation unit for sm_103a only, g++ compiles the
+host tables with -ffp-contract=off (so an Arm host gives the x86 float
+results), and g++ links the shared library against the CUDA runtime.  Both
+compiles run in parallel.  Usage: python -m sm_2d_gb300.build
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OUT = os.path.join(PKG, "_lib")
+LIB = os.path.join(OUT, "libsm2d.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def _cuda_home() -> str:
+    home = os.environ.get("CUDA_HOME") or os.environ.get("CUDA_PATH")
+    if home and os.path.isdir(home):
+        return home
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    return "/usr/local/cuda"
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))] + [os.path.join(ROOT, "include", "sm2d.h")]
+
+
+def up_to_date() -> bool:
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(s) <= t for s in _sources())
+
+
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    cuda = _cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+    cu_obj = os.path.join(OUT, "sm2d_engine.o")
+    cpp_obj = os.path.join(OUT, "sm2d_tables.o")
+    cu_cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-c", "-Xcompiler", "-fPIC,-ffp-contract=off",
+              "--expt-relaxed-constexpr", *inc, os.path.join(CSRC, "sm2d_engine.cu"), "-o", cu_obj]
+    if ptxas_info:
+        cu_cmd.insert(1, "-Xptxas=-v")
+    cpp_cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-c",
+               os.path.join(CSRC, "sm2d_tables.cpp"), "-o", cpp_obj]
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or ptxas_info or r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+        if r.returncode:
+            raise RuntimeError("build step failed: " + " ".join(cmd))
+        return r
+
+    with ThreadPoolExecutor(2) as ex:
+        for f in [ex.submit(run, cu_cmd), ex.submit(run, cpp_cmd)]:
+            f.result()
+    tmp = LIB + ".tmp"
+    run(["g++", "-shared", "-o", tmp, cu_obj, cpp_obj, "-L" + os.path.join(cuda, "lib64"),
+         "-L" + os.path.join(cuda, "targets", "sbsa-linux", "lib"), "-L" + os.path.join(cuda, "targets", "x86_64-linux", "lib"),
+         "-lcudart", "-Wl,-rpath," + os.path.join(cuda, "lib64")])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True, ptxas_info="--ptxas" in sys.argv))

@@ -1,0 +1,259 @@
+// sm2d_device.cuh -- device-side physics, slot tables and bin encodings of
+// the transport step.  Float arithmetic follows the reference's expression
+// order (device_physics.cuh, device_lut.cuh, device_bucket.cuh,
+// device_psic.cuh) so that per-bin results agree with the reference build to
+// a few ulp; CUDA's own logf/expf/sinf/cosf/erff/sqrtf are called, as the
+// reference does.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sm2d.h"
+
+namespace sm2d {
+
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+constexpr int kKb = 32;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// Local-bin layout: lidx = t + NT*(e + NE*(x + NX*z))  (local_bins.hpp:62-78)
+template <int NT_, int NE_, int NX_, int NZ_>
+struct Layout {
+    static constexpr int NT = NT_, NE = NE_, NX = NX_, NZ = NZ_;
+    static constexpr int L = NT * NE * NX * NZ;
+    __device__ __forceinline__ static int enc(int t, int e, int x, int z) { return t + NT * (e + NE * (x + NX * z)); }
+    __device__ __forceinline__ static void dec(int l, int& t, int& e, int& x, int& z) {
+        t = l % NT;
+        int r = l / NT;
+        e = r % NE;
+        r /= NE;
+        x = r % NX;
+        z = r / NX;
+    }
+};
+using LayoutRef = Layout<4, 2, 8, 4>;    // 256 bins: the layout the reference code builds
+using LayoutB128 = Layout<8, 4, 4, 1>;   // 128 bins: 8 theta x 4 E x 4 x_sub
+
+// Device-resident iteration state: counters, per-iteration accumulators and
+// cumulative run totals.  Written only by device code between host syncs.
+struct IterState {
+    int parity;            // psi_in = buffer[parity]
+    int iter;              // transport iterations done
+    int n_active, n_coarse;
+    int done;              // no listed cell: transport finished
+    int max_iter;          // stop after this many iterations (device loop)
+    unsigned blocks_done;  // audit kernel completion counter
+    int include_source;    // next audit lifts source losses (first iteration)
+    int halt;              // this pass does no transport (finished or iteration limit)
+    int pad1;
+    // per-iteration accumulators (reset by the compaction kernel)
+    double drop_w, drop_e;
+    double Win, Ein, Wout, Eout, Wcut, Wnuc, Wbnd, Edep, Ecut, Enuc, Ebnd;
+    double slots_out_it;
+    // cumulative
+    double transport_drop_w, transport_drop_e, audit_residual;
+    double cell_steps, slots_in, slots_out;
+    // source accounting
+    float src_inj_w, src_oog_w, src_slot_w, pad0;
+    double src_inj_e, src_oog_e, src_slot_e, src_rep_loss;
+    double tot_w, tot_e;   // scratch for phase-space totals
+    sm2d_audit last;
+};
+
+struct Dev {
+    int Nx, Nz, Nc;
+    float dx, dz;
+    int N_theta, N_E;
+    const float* th;      // theta edges [N_theta+1]
+    const float* Ee;      // energy edges [N_E+1]
+    int lutN;
+    float lutEmin, lutEmax;
+    const float *R, *logE, *logR;
+    const float *feA, *feB;
+    float E_fine_on, wmin, step_coarse, sx0;
+    int b_on, b_off;
+    int straggle, nuclear, seed_mode, esplit;
+    float prune_coarse, prune_fine, split_min_w, stop_frac;
+    int floor_cutoff, salt;
+    uint32_t* bid[2];
+    float* val[2];
+    uint8_t* occ[2];
+    double *edep, *e_cut, *e_nuc, *e_bnd;
+    float *w_cut, *w_nuc, *w_bnd;
+    uint8_t* mask;        // bit0 current, bit1 previous iteration
+    uint8_t* cls;         // 0 idle, 1 coarse (K2), 2 active (K3)
+    uint32_t *active, *coarse;
+    int* blk;             // per classify-block counts [2*nblk]
+    int nblk;
+    IterState* it;
+    sm2d_audit* hist;
+    int hist_cap;
+    unsigned char* buckets;  // DeviceOutflowBucket array (bucket mode)
+    int* c2b;                // cell -> bucket base (bucket mode)
+    int bucket_bytes;
+};
+
+// ---------------------------------------------------------------- encodings
+__device__ __forceinline__ uint32_t make_bid(uint32_t bt, uint32_t be) { return (bt & 0xFFFu) | ((be & 0xFFFu) << 12); }
+__device__ __forceinline__ float sub_offset(int s, int n, float d) { return d * ((0.5f + (float)s) / (float)n - 0.5f); }
+__device__ __forceinline__ int sub_bin(float off, float d, int n) {
+    int b = (int)(((off / d) + 0.5f) * (float)n);
+    return b < 0 ? 0 : (b >= n ? n - 1 : b);
+}
+
+// ---------------------------------------------------------------- LUT (device_lut.cuh:34-214)
+__device__ __forceinline__ int find_bin(const float* __restrict__ e, int N, float E) {
+    if (E <= e[0]) return 0;
+    if (E >= e[N]) return N - 1;
+    int lo = 0, hi = N;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (e[mid + 1] <= E) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+__device__ __forceinline__ float lut_range(const Dev& d, float E) {
+    float Ec = fmaxf(d.lutEmin, fminf(E, d.lutEmax));
+    int b = find_bin(d.Ee, d.lutN, Ec);
+    if (b == d.lutN - 1 || Ec >= d.lutEmax) return d.R[d.lutN - 1];
+    float le = logf(Ec);
+    float lr = d.logR[b] + (d.logR[b + 1] - d.logR[b]) * (le - d.logE[b]) / (d.logE[b + 1] - d.logE[b]);
+    return expf(lr);
+}
+__device__ __forceinline__ float lut_energy_of_range(const Dev& d, float r) {
+    if (r <= 0.0f) return d.lutEmin;
+    int lo = 0, hi = d.lutN;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (d.R[mid] < r) lo = mid + 1; else hi = mid;
+    }
+    int b = max(0, min(lo, d.lutN - 2));
+    float lr = logf(r);
+    float dl = d.logR[b + 1] - d.logR[b];
+    if (fabsf(dl) < 1e-10f) return expf(d.logE[b]);
+    float le = d.logE[b] + (d.logE[b + 1] - d.logE[b]) * (lr - d.logR[b]) / dl;
+    return expf(le);
+}
+__device__ __forceinline__ float lut_energy_loss(const Dev& d, float E, float s) {
+    float r = lut_range(d, E) - s;
+    float En = (r <= 0.0f) ? d.lutEmin : lut_energy_of_range(d, r);
+    return E - En;
+}
+__device__ __forceinline__ float fine_step_limit(const Dev& d, float E) {
+    float v = 0.01f * lut_range(d, E);
+    float floor_ = E < 2.0f ? 0.1f : (E < 20.0f ? 0.25f : (E < 100.0f ? 0.5f : 1.0f));
+    v = fmaxf(v, floor_);
+    if (E < 0.5f) v = fminf(v, 0.05f);
+    else if (E < 5.0f) v = fminf(v, 0.2f);
+    else if (E < 20.0f) v = fminf(v, 0.5f);
+    return v;
+}
+
+// ---------------------------------------------------------------- physics (device_physics.cuh)
+constexpr float kMp = 938.272f, kMe = 0.511f, kX0 = 360.8f;
+
+__device__ __forceinline__ float highland(float E, float ds) {
+    float g = (E + kMp) / kMp;
+    float b2 = 1.0f - 1.0f / (g * g);
+    float beta = sqrtf(fmaxf(b2, 0.0f));
+    float p = sqrtf(fmaxf((E + kMp) * (E + kMp) - kMp * kMp, 0.0f));
+    float t = ds / kX0;
+    if (t < 1e-6f) return 0.0f;
+    float br = fmaxf(1.0f + 0.038f * logf(t), 0.25f);
+    return (13.6f * 1.0f / (beta * p)) * sqrtf(t) * br;
+}
+__device__ __forceinline__ float scatter_power(float E, float ds) {
+    float th = highland(E, ds);
+    if (ds < 1e-6f) return 0.0f;
+    return th * th / ds;
+}
+// LCG + Box-Muller draw of the transport kernels
+__device__ __forceinline__ float normal_draw(unsigned& s) {
+    s = 1664525u * s + 1013904223u;
+    float u1 = (float)(s >> 16) / 65536.0f;
+    s = 1664525u * s + 1013904223u;
+    float u2 = (float)(s >> 16) / 65536.0f;
+    u1 = fmaxf(u1, 1e-6f);
+    return sqrtf(-2.0f * logf(u1)) * cosf(2.0f * 3.14159265358979323846f * u2);
+}
+__device__ __forceinline__ float vav_xi(float beta, float rho, float ds_cm) {
+    return (0.307f / 2.0f) * 0.555f * (1.0f * 1.0f / (beta * beta)) * rho * ds_cm;
+}
+__device__ __forceinline__ float bohr_sigma(float E, float ds, float rho) {
+    float g = (E + kMp) / kMp;
+    float beta = sqrtf(fmaxf(1.0f - 1.0f / (g * g), 0.01f));
+    return 0.156f * sqrtf(rho * ds) / beta;
+}
+__device__ __forceinline__ float straggling_sigma(float E, float ds, float rho) {
+    float g = (E + kMp) / kMp;
+    float beta = sqrtf(fmaxf(1.0f - 1.0f / (g * g), 0.0f));
+    float xi = vav_xi(beta, rho, ds / 10.0f);
+    float mr = kMe / kMp;
+    float tmax = (2.0f * kMe * beta * beta * g * g) / fmaxf(1.0f + 2.0f * g * mr + mr * mr, 1e-10f);
+    float kappa = fmaxf(xi / fmaxf(tmax, 1e-10f), 1e-6f);
+    if (kappa > 10.0f) return bohr_sigma(E, ds, rho);
+    float landau = 4.0f * xi / 2.355f;
+    if (kappa < 0.01f) return landau;
+    float w = 1.0f / (1.0f + kappa);
+    return w * landau + (1.0f - w) * bohr_sigma(E, ds, rho);
+}
+__device__ __forceinline__ float nuclear_xs(float E) {
+    if (E < 5.0f) return 0.0f;
+    if (E >= 20.0f) return 0.0012f * fmaxf(1.0f - 0.15f * logf(E / 100.0f), 0.4f);
+    return 0.0016f * ((E - 5.0f) / 15.0f);
+}
+__device__ __forceinline__ float gauss_cdf(float x, float mu, float sigma) {
+    if (sigma < 1e-10f) return (x >= mu) ? 1.0f : 0.0f;
+    float c = 0.5f * (1.0f + erff((x - mu) / sigma * 0.70710678f));
+    return fminf(1.0f, fmaxf(0.0f, c));
+}
+
+// ---------------------------------------------------------------- slot tables
+__device__ __forceinline__ int bid_distance(uint32_t a, uint32_t b) {
+    int ta = (int)(a & 0xFFFu), ea = (int)((a >> 12) & 0xFFFu);
+    int tb = (int)(b & 0xFFFu), eb = (int)((b >> 12) & 0xFFFu);
+    return abs(ea - eb) * 8 + abs(ta - tb);
+}
+// exact match, then CAS-claim an empty slot, then nearest occupied block
+// (device_psic.cuh:208-260 and device_bucket.cuh:61-128, same protocol)
+__device__ __forceinline__ int claim_slot(uint32_t* ids, uint32_t want, uint32_t& sel) {
+    volatile uint32_t* v = ids;
+    sel = want;
+#pragma unroll 4
+    for (int s = 0; s < kKb; ++s)
+        if (v[s] == want) return s;
+    for (int s = 0; s < kKb; ++s) {
+        uint32_t old = atomicCAS(&ids[s], kEmpty, want);
+        if (old == kEmpty || old == want) return s;
+    }
+    for (int s = 0; s < kKb; ++s)
+        if (v[s] == want) return s;
+    int best = -1, bd = 0x7fffffff;
+    uint32_t bb = kEmpty;
+    for (int s = 0; s < kKb; ++s) {
+        uint32_t e = v[s];
+        if (e == kEmpty) continue;
+        int dd = bid_distance(e, want);
+        if (dd < bd) { bd = dd; best = s; bb = e; }
+    }
+    if (best >= 0) sel = bb;
+    return best;
+}
+template <class Lay>
+__device__ __forceinline__ int remap_lidx(int l, uint32_t src, uint32_t dst) {
+    if (src == dst) return l;
+    int t, e, x, z;
+    Lay::dec(l, t, e, x, z);
+    int tg = (int)(src & 0xFFFu) * Lay::NT + t;
+    int eg = (int)((src >> 12) & 0xFFFu) * Lay::NE + e;
+    int td = max(0, min(tg - (int)(dst & 0xFFFu) * Lay::NT, Lay::NT - 1));
+    int ed = max(0, min(eg - (int)((dst >> 12) & 0xFFFu) * Lay::NE, Lay::NE - 1));
+    return Lay::enc(td, ed, x, z);
+}
+
+// DeviceOutflowBucket (device_bucket.cuh:48-57) with L local bins.
+__host__ __device__ constexpr int bucket_bytes_for(int L) { return 32 * 4 + 32 * 2 + 32 * L * 4 + 12; }
+__device__ __forceinline__ uint32_t* bucket_ids(unsigned char* b) { return reinterpret_cast<uint32_t*>(b); }
+__device__ __forceinline__ float* bucket_vals(unsigned char* b) { return reinterpret_cast<float*>(b + 192); }
+
+}  // namespace sm2d

@@ -1,0 +1,1599 @@
+// sm2d_engine.cu -- kernels, device-resident iteration loop and C ABI of the
+// SM_2D transport step on GB300 (sm_103a).
+//
+// One iteration (the body of the reference host loop k1k6_pipeline.cu:1606-2038)
+// is four kernels that read every count from device memory:
+//   k_classify   K1 active mask + per-block list counts (warp per occupied cell)
+//   k_compact    ordered active/coarse lists, iteration bookkeeping, loop condition
+//   k_transport  K2/K3 for every listed cell, warp per cell, with the K4 scatter
+//                fused (direct mode) or written to DeviceOutflowBucket (bucket mode,
+//                then k_bucket_gather = K4_BucketTransfer)
+//   k_audit      K5 audit of the iteration, clear of the consumed buffer, K6 swap
+// sm2d_run captures that body once into a CUDA graph whose while-conditional
+// node repeats it on the device until no cell holds weight.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sm2d.h"
+#include "sm2d_device.cuh"
+#include "sm2d_tables.h"
+#include "sm2d_transport.cuh"
+
+namespace sm2d {
+
+static thread_local std::string g_err;
+static int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return fail(SM2D_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                            \
+    } while (0)
+
+constexpr int kThreads = 256;
+
+// ------------------------------------------------------------------ warp helpers
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------------ injection
+// device_psic_inject_source (device_psic.cuh:347-450): clamp into the cell,
+// sub-cell bins, nearest global bins, CAS claim without fallback.
+template <class Lay>
+__device__ bool inject_one(const Dev& d, int par, int cell, float theta, float E, float w, float x, float z) {
+    if (w <= 0.0f || cell < 0 || cell >= d.Nc) return false;
+    const float dx = d.dx, dz = d.dz;
+    x = fmaxf(0.0f, fminf(x, dx));
+    z = fmaxf(0.0f, fminf(z, dz));
+    const int xs = sub_bin(x - dx * 0.5f, dx, Lay::NX), zs = sub_bin(z - dz * 0.5f, dz, Lay::NZ);
+    const float tmin = d.th[0], tmax = d.th[d.N_theta];
+    theta = fmaxf(tmin, fminf(theta, tmax));
+    E = fmaxf(d.Ee[0], fminf(E, d.Ee[d.N_E]));
+    const float cont = (theta - tmin) / ((tmax - tmin) / (float)d.N_theta);
+    int tb = (int)cont;
+    float ft = cont - (float)tb;
+    int Eb = find_bin(d.Ee, d.N_E, E);
+    const float lo = d.Ee[Eb], hi = d.Ee[Eb + 1];
+    float fE = (hi - lo) > 1e-10f ? (E - lo) / (hi - lo) : 0.0f;
+    if (tb >= d.N_theta - 1) { tb = d.N_theta - 1; ft = 0.0f; }
+    if (Eb >= d.N_E - 1) { Eb = d.N_E - 1; fE = 0.0f; }
+    if (ft >= 0.5f && tb < d.N_theta - 1) tb++;
+    if (fE >= 0.5f && Eb < d.N_E - 1) Eb++;
+    const uint32_t want = make_bid((uint32_t)(tb / Lay::NT), (uint32_t)(Eb / Lay::NE));
+    const int l = Lay::enc(tb % Lay::NT, Eb % Lay::NE, xs, zs);
+    uint32_t* ids = d.bid[par] + (size_t)cell * kKb;
+    for (int s = 0; s < kKb; ++s) {
+        const uint32_t old = atomicCAS(&ids[s], kEmpty, want);
+        if (old == kEmpty || old == want) {
+            d.occ[par][cell] = 1;
+            atomicAdd(d.val[par] + ((size_t)cell * kKb + s) * Lay::L + l, w);
+            return true;
+        }
+    }
+    return false;
+}
+
+// LCG/Box-Muller of the source kernel (k1k6_pipeline.cu:433-447)
+__device__ __forceinline__ float source_normal(unsigned& s) {
+    s = 1664525u * s + 1013904223u;
+    const float u1 = (float)(s >> 16) / 65536.0f;
+    s = 1664525u * s + 1013904223u;
+    const float u2 = (float)(s >> 16) / 65536.0f;
+    const float r = sqrtf(-2.0f * logf(fmaxf(u1, 1e-10f)));
+    const float th = (float)(2.0 * 3.14159265358979323846 * (double)u2);
+    return r * cosf(th);
+}
+
+struct BeamArgs {
+    float x0, z0, theta0, E0, W, sx, sth, sE, x_min, z_min;
+    int n;
+    unsigned seed;
+};
+
+template <class Lay>
+__global__ void k_inject(Dev d, BeamArgs b, int gaussian) {
+    const int par = d.it->parity;
+    if (!gaussian) {  // inject_source_kernel pencil branch (k1k6_pipeline.cu:325-343)
+        if (blockIdx.x || threadIdx.x) return;
+        const float xr = b.x0 - b.x_min, zr = b.z0 - b.z_min;
+        int cx = (int)(xr / d.dx), cz = (int)(zr / d.dz);
+        cx = cx < 0 ? 0 : (cx >= d.Nx ? d.Nx - 1 : cx);
+        cz = cz < 0 ? 0 : (cz >= d.Nz ? d.Nz - 1 : cz);
+        inject_one<Lay>(d, par, cz * d.Nx + cx, b.theta0, b.E0, b.W, xr - cx * d.dx, zr - cz * d.dz);
+        return;
+    }
+    // inject_gaussian_source_kernel (k1k6_pipeline.cu:451-551)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    unsigned s = b.seed + (unsigned)i;
+    const float xs = b.x0 + b.sx * source_normal(s);
+    float ts = b.theta0 + b.sth * source_normal(s);
+    float Es = b.E0 + b.sE * source_normal(s);
+    Es = fmaxf(d.Ee[0], fminf(Es, d.Ee[d.N_E]));
+    ts = fmaxf(d.th[0], fminf(ts, d.th[d.N_theta]));
+    const float xr = xs - b.x_min, zr = b.z0 - b.z_min;
+    const int ix = (int)(xr / d.dx), iz = (int)(zr / d.dz);
+    const float ws = b.W / b.n;
+    IterState* it = d.it;
+    if (ix < 0 || ix >= d.Nx || iz < 0 || iz >= d.Nz) {
+        atomicAdd(&it->src_oog_w, ws);
+        atomicAdd(&it->src_oog_e, (double)(Es * ws));
+        return;
+    }
+    if (inject_one<Lay>(d, par, iz * d.Nx + ix, ts, Es, ws, xr - ix * d.dx, zr - iz * d.dz)) {
+        atomicAdd(&it->src_inj_w, ws);
+        atomicAdd(&it->src_inj_e, (double)(Es * ws));
+    } else {
+        atomicAdd(&it->src_slot_w, ws);
+        atomicAdd(&it->src_slot_e, (double)(Es * ws));
+    }
+}
+
+// Weight and bin-centre energy of the w > 0 bins of buffer `buf`
+// (compute_psic_total_weight_energy, k1k6_pipeline.cu:706-768).
+template <class Lay>
+__global__ void k_totals(Dev d, int which) {
+    const int buf = d.it->parity ^ which;
+    const int lane = threadIdx.x & 31;
+    const int cell0 = (blockIdx.x * blockDim.x + threadIdx.x) - lane;
+    const int cell = cell0 + lane;
+    unsigned ob = __ballot_sync(kFull, cell < d.Nc && d.occ[buf][cell]);
+    double W = 0.0, E = 0.0;
+    while (ob) {
+        const int c = cell0 + __ffs(ob) - 1;
+        ob &= ob - 1;
+        const uint32_t b = d.bid[buf][(size_t)c * kKb + lane];
+        unsigned used = __ballot_sync(kFull, b != kEmpty);
+        while (used) {
+            const int s = __ffs(used) - 1;
+            used &= used - 1;
+            const uint32_t bs = __shfl_sync(kFull, b, s);
+            const float* v = d.val[buf] + ((size_t)c * kKb + s) * Lay::L;
+            for (int l = lane; l < Lay::L; l += 32) {
+                const float w = v[l];
+                if (w <= 0.0f) continue;
+                int Eb = (int)((bs >> 12) & 0xFFFu) * Lay::NE + (l / Lay::NT) % Lay::NE;
+                Eb = max(0, min(Eb, d.N_E - 1));
+                W += (double)w;
+                E += (double)w * (double)e_center(d, Eb);
+            }
+        }
+    }
+    W = warp_sum(W);
+    E = warp_sum(E);
+    if (lane == 0 && (W != 0.0 || E != 0.0)) {
+        atomicAdd(&d.it->tot_w, W);
+        atomicAdd(&d.it->tot_e, E);
+    }
+}
+
+// ------------------------------------------------------------------ K1
+// K1_ActiveMask (k1_activemask.cu:6-48) for the occupied cells; the class of
+// each cell (active / coarse with w > 0, compact_coarse_list
+// k1k6_pipeline.cu:625-665) and per-block counts for the ordered compaction.
+template <class Lay>
+__global__ void __launch_bounds__(kThreads) k_classify(Dev d) {
+    const int par = d.it->parity;
+    const int lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cell0 = cell - lane;
+    const bool inb = cell < d.Nc;
+    const bool occ = inb && d.occ[par][cell];
+    unsigned ob = __ballot_sync(kFull, occ);
+    int on = 0, off = 0, hw = 0;
+    float W = 0.0f;
+    while (ob) {
+        const int src = __ffs(ob) - 1;
+        ob &= ob - 1;
+        const int c = cell0 + src;
+        const uint32_t b = d.bid[par][(size_t)c * kKb + lane];
+        const bool used = b != kEmpty;
+        const uint32_t be = (b >> 12) & 0xFFFu;
+        const int c_on = __any_sync(kFull, used && be <= (uint32_t)d.b_on);
+        const int c_off = __any_sync(kFull, used && be <= (uint32_t)d.b_off);
+        unsigned um = __ballot_sync(kFull, used);
+        float ws = 0.0f;
+        int pos = 0;
+        while (um) {
+            const int s = __ffs(um) - 1;
+            um &= um - 1;
+            const float4* v = reinterpret_cast<const float4*>(d.val[par] + ((size_t)c * kKb + s) * Lay::L);
+            for (int q = lane; q < Lay::L / 4; q += 32) {
+                const float4 f = v[q];
+                ws += (f.x + f.y) + (f.z + f.w);
+                pos |= (f.x > 0.0f) | (f.y > 0.0f) | (f.z > 0.0f) | (f.w > 0.0f);
+            }
+        }
+        ws = warp_sumf(ws);
+        ws = __shfl_sync(kFull, ws, 0);
+        const int c_hw = __any_sync(kFull, pos);
+        if (lane == src) { on = c_on; off = c_off; hw = c_hw; W = ws; }
+    }
+    uint8_t cls = 0;
+    if (inb) {
+        const uint8_t m_old = d.mask[cell];
+        const bool prev = (m_old & 1) != 0;
+        const bool act = occ && (on || (prev && off)) && W > d.wmin;
+        cls = act ? 2 : ((occ && hw) ? 1 : 0);
+        d.mask[cell] = (uint8_t)((act ? 1 : 0) | (prev ? 2 : 0));
+        d.cls[cell] = cls;
+    }
+    const int na = __syncthreads_count(cls == 2);
+    const int nc = __syncthreads_count(cls == 1);
+    if (threadIdx.x == 0) {
+        d.blk[2 * blockIdx.x] = na;
+        d.blk[2 * blockIdx.x + 1] = nc;
+    }
+}
+
+// Ordered compaction (ascending cell index) of the classes into the active
+// and coarse lists; the last block finalises the counts, resets the
+// per-iteration accumulators and sets the device loop condition.
+__global__ void __launch_bounds__(kThreads) k_compact(Dev d, cudaGraphConditionalHandle cond, int use_cond) {
+    __shared__ int s_pre[2];
+    __shared__ int s_warp[2][kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (wid == 0) {
+        int a = 0, c = 0;
+        for (int b = lane; b < (int)blockIdx.x; b += 32) {
+            a += d.blk[2 * b];
+            c += d.blk[2 * b + 1];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(kFull, a, o);
+            c += __shfl_down_sync(kFull, c, o);
+        }
+        if (lane == 0) { s_pre[0] = a; s_pre[1] = c; }
+    }
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint8_t cls = cell < d.Nc ? d.cls[cell] : 0;
+    const unsigned ba = __ballot_sync(kFull, cls == 2), bc = __ballot_sync(kFull, cls == 1);
+    if (lane == 0) { s_warp[0][wid] = __popc(ba); s_warp[1][wid] = __popc(bc); }
+    __syncthreads();
+    int oa = s_pre[0], oc = s_pre[1];
+    for (int w = 0; w < wid; ++w) { oa += s_warp[0][w]; oc += s_warp[1][w]; }
+    const unsigned lt = (1u << lane) - 1u;
+    if (cls == 2) d.active[oa + __popc(ba & lt)] = (uint32_t)cell;
+    if (cls == 1) d.coarse[oc + __popc(bc & lt)] = (uint32_t)cell;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        int na = s_pre[0], nc = s_pre[1];
+        for (int w = 0; w < kThreads / 32; ++w) { na += s_warp[0][w]; nc += s_warp[1][w]; }
+        IterState* it = d.it;
+        it->n_active = na;
+        it->n_coarse = nc;
+        // C1 stopping rule: in-flight weight (the last audit's W_out) below a
+        // fraction of the injected weight ends the run; the rest is booked as
+        // a terminal transport drop (k1k6_pipeline.cu:1677-1706 books it too)
+        const bool light = d.stop_frac > 0.0f && it->iter > 0 && (na + nc) > 0 &&
+                           it->last.W_out_total < d.stop_frac * it->src_inj_w;
+        if (light) {
+            it->transport_drop_w += it->last.W_out_total;
+            it->transport_drop_e += it->last.E_out_total;
+            na = nc = 0;
+            it->n_active = it->n_coarse = 0;
+        }
+        const bool done = (na + nc) == 0;
+        it->done = done ? 1 : 0;
+        const bool halt = done || it->iter >= it->max_iter;
+        it->halt = halt ? 1 : 0;
+        it->drop_w = it->drop_e = 0.0;
+        it->Win = it->Ein = it->Wout = it->Eout = 0.0;
+        it->Wcut = it->Wnuc = it->Wbnd = 0.0;
+        it->Edep = it->Ecut = it->Enuc = it->Ebnd = 0.0;
+        it->slots_out_it = 0.0;
+        it->blocks_done = 0;
+        if (!halt) it->cell_steps += (double)(na + nc);
+        if (use_cond) cudaGraphSetConditional(cond, (!halt && it->iter + 1 < it->max_iter) ? 1u : 0u);
+    }
+}
+
+// ------------------------------------------------------------------ K2/K3
+template <class Lay, bool BUCKET>
+__global__ void __launch_bounds__(kThreads) k_transport(Dev d) {
+    IterState* it = d.it;
+    if (it->halt) return;
+    const int par = it->parity;
+    const int n_co = it->n_coarse, n = n_co + it->n_active;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
+        const bool k3 = wi >= n_co;
+        const int cell = (int)(k3 ? d.active[wi - n_co] : d.coarse[wi]);
+        const uint32_t myb = d.bid[par][(size_t)cell * kKb + lane];
+        const bool used = myb != kEmpty;
+        unsigned um = __ballot_sync(kFull, used);
+        int rank = 0;
+        if (d.seed_mode) {
+            for (int t = 0; t < 32; ++t) {
+                const uint32_t bt = __shfl_sync(kFull, myb, t);
+                rank += (bt != kEmpty && bt < myb) ? 1 : 0;
+            }
+        }
+        Tally t{};
+        const int n_slots = __popc(um);
+        const unsigned salt = d.salt ? (unsigned)it->iter * 0x9E3779B9u : 0u;
+        while (um) {
+            const int s = __ffs(um) - 1;
+            um &= um - 1;
+            const uint32_t bid = __shfl_sync(kFull, myb, s);
+            const int sslot = d.seed_mode ? __shfl_sync(kFull, rank, s) : s;
+            const float4* v = reinterpret_cast<const float4*>(d.val[par] + ((size_t)cell * kKb + s) * Lay::L);
+            for (int q = lane; q < Lay::L / 4; q += 32) {
+                const float4 f = v[q];
+#pragma unroll 1
+                for (int k = 0; k < 4; ++k) {
+                    const float wk = k == 0 ? f.x : (k == 1 ? f.y : (k == 2 ? f.z : f.w));
+                    if (wk > 0.0f) transport_bin<Lay, BUCKET>(d, par, k3, cell, bid, sslot, 4 * q + k, wk, salt, t);
+                }
+            }
+        }
+        // per-cell commit: one warp owns the cell's tallies in this iteration
+        t.edep = warp_sum(t.edep);
+        t.e_cut = warp_sum(t.e_cut);
+        t.e_nuc = warp_sum(t.e_nuc);
+        t.e_bnd = warp_sum(t.e_bnd);
+        t.w_cut = warp_sumf(t.w_cut);
+        t.w_nuc = warp_sumf(t.w_nuc);
+        t.w_bnd = warp_sumf(t.w_bnd);
+        t.drop_w = warp_sum(t.drop_w);
+        t.drop_e = warp_sum(t.drop_e);
+        t.Win = warp_sum(t.Win);
+        t.Ein = warp_sum(t.Ein);
+        if (lane == 0) {
+            // K5 takes max(0, cumulative - previous) per cell (k5_audit.cu:93-99)
+            const double e0 = d.edep[cell], e1 = e0 + t.edep;
+            const double c0 = d.e_cut[cell], c1 = c0 + t.e_cut;
+            const double n0 = d.e_nuc[cell], n1 = n0 + t.e_nuc;
+            const double b0 = d.e_bnd[cell], b1 = b0 + t.e_bnd;
+            const float wc0 = d.w_cut[cell], wc1 = wc0 + t.w_cut;
+            const float wn0 = d.w_nuc[cell], wn1 = wn0 + t.w_nuc;
+            const float wb0 = d.w_bnd[cell], wb1 = wb0 + t.w_bnd;
+            d.edep[cell] = e1; d.e_cut[cell] = c1; d.e_nuc[cell] = n1; d.e_bnd[cell] = b1;
+            d.w_cut[cell] = wc1; d.w_nuc[cell] = wn1; d.w_bnd[cell] = wb1;
+            atomicAdd(&it->Edep, fmax(0.0, e1 - e0));
+            atomicAdd(&it->Ecut, fmax(0.0, c1 - c0));
+            atomicAdd(&it->Enuc, fmax(0.0, n1 - n0));
+            atomicAdd(&it->Ebnd, fmax(0.0, b1 - b0));
+            atomicAdd(&it->Wcut, (double)fmaxf(0.0f, wc1 - wc0));
+            atomicAdd(&it->Wnuc, (double)fmaxf(0.0f, wn1 - wn0));
+            atomicAdd(&it->Wbnd, (double)fmaxf(0.0f, wb1 - wb0));
+            atomicAdd(&it->Win, t.Win);
+            atomicAdd(&it->Ein, t.Ein);
+            if (t.drop_w != 0.0 || t.drop_e != 0.0) {
+                atomicAdd(&it->drop_w, t.drop_w);
+                atomicAdd(&it->drop_e, t.drop_e);
+            }
+            atomicAdd(&it->slots_in, (double)n_slots);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ bucket mode (reference structure)
+template <class Lay>
+__global__ void k_bucket_prep(Dev d) {
+    IterState* it = d.it;
+    if (it->halt) return;
+    const int n_co = it->n_coarse, n = n_co + it->n_active;
+    const int i = blockIdx.x;
+    if (i >= n) return;
+    const int cell = (int)(i < n_co ? d.coarse[i] : d.active[i - n_co]);
+    if (threadIdx.x == 0) d.c2b[cell] = 4 * i;
+    for (int f = 0; f < 4; ++f) {   // clear_buckets_kernel (k1k6_pipeline.cu:554-573)
+        unsigned char* b = d.buckets + (size_t)(4 * i + f) * d.bucket_bytes;
+        if (threadIdx.x < 32) bucket_ids(b)[threadIdx.x] = kEmpty;
+        if (threadIdx.x < 32) reinterpret_cast<uint16_t*>(b + 128)[threadIdx.x] = 0;
+        float* v = bucket_vals(b);
+        for (int k = threadIdx.x; k < 32 * Lay::L + 3; k += blockDim.x) v[k] = 0.0f;
+    }
+}
+
+// K4_BucketTransfer (k4_transfer.cu:174-333): per destination cell, pull the
+// facing buckets of its four neighbours into psi_out (claim with fallback,
+// lidx remap, drop accounting).  Warp per destination cell.
+template <class Lay>
+__device__ void bucket_gather_cell(const unsigned char* buckets, int bucket_bytes, const int* c2b, uint32_t* ids_out,
+                                   float* vals_out, uint8_t* occ_out, int cell, int Nx, int Nz, const float* Ee,
+                                   int N_E, double* drop_w, double* drop_e, int lane) {
+    const int ix = cell % Nx, iz = cell / Nx;
+    for (int face = 0; face < 4; ++face) {
+        int src = -1;
+        if (face == 0 && iz > 0) src = cell - Nx;
+        if (face == 1 && iz + 1 < Nz) src = cell + Nx;
+        if (face == 2 && ix > 0) src = cell - 1;
+        if (face == 3 && ix + 1 < Nx) src = cell + 1;
+        if (src < 0) continue;
+        const int base = c2b[src];
+        if (base < 0) continue;
+        const unsigned char* b = buckets + (size_t)(base + face) * bucket_bytes;
+        const uint32_t sb = reinterpret_cast<const uint32_t*>(b)[lane];
+        unsigned um = __ballot_sync(kFull, sb != kEmpty);
+        const float* bv = reinterpret_cast<const float*>(b + 192);
+        while (um) {
+            const int s = __ffs(um) - 1;
+            um &= um - 1;
+            const uint32_t bid = __shfl_sync(kFull, sb, s);
+            int os = 0;
+            uint32_t sel = bid;
+            if (lane == 0) {
+                os = claim_slot(ids_out + (size_t)cell * kKb, bid, sel);
+                if (os >= 0 && occ_out) occ_out[cell] = 1;
+            }
+            os = __shfl_sync(kFull, os, 0);
+            sel = __shfl_sync(kFull, sel, 0);
+            const float* v = bv + (size_t)s * Lay::L;
+            if (os < 0) {
+                double dw = 0.0, de = 0.0;
+                for (int l = lane; l < Lay::L; l += 32) {
+                    const float w = v[l];
+                    if (w > 0.0f) {
+                        int Eb = (int)((bid >> 12) & 0xFFFu) * Lay::NE + (l / Lay::NT) % Lay::NE;
+                        Eb = max(0, min(Eb, N_E - 1));
+                        const float E = Ee[Eb] + 1.0f * (0.5f * (Ee[Eb + 1] - Ee[Eb]));
+                        dw += (double)w;
+                        de += (double)E * (double)w;
+                    }
+                }
+                dw = warp_sum(dw);
+                de = warp_sum(de);
+                if (lane == 0) { atomicAdd(drop_w, dw); atomicAdd(drop_e, de); }
+                continue;
+            }
+            float* o = vals_out + ((size_t)cell * kKb + os) * Lay::L;
+            for (int l = lane; l < Lay::L; l += 32) {
+                const float w = v[l];
+                if (w > 0.0f) atomicAdd(o + (sel != bid ? remap_lidx<Lay>(l, bid, sel) : l), w);
+            }
+        }
+    }
+}
+
+template <class Lay>
+__global__ void __launch_bounds__(kThreads) k_bucket_gather(Dev d) {
+    IterState* it = d.it;
+    if (it->halt) return;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int out = it->parity ^ 1;
+    for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < d.Nc; cell += nw)
+        bucket_gather_cell<Lay>(d.buckets, d.bucket_bytes, d.c2b, d.bid[out], d.val[out], d.occ[out], cell, d.Nx, d.Nz,
+                                d.Ee, d.N_E, &it->drop_w, &it->drop_e, lane);
+}
+
+// ------------------------------------------------------------------ K5 + clear + K6
+__device__ void finalize_audit(Dev& d) {
+    volatile IterState* v = d.it;
+    IterState* it = d.it;
+    sm2d_audit r;
+    memset(&r, 0, sizeof r);
+    r.W_in_total = (float)v->Win;
+    r.W_out_total = (float)v->Wout;
+    r.W_cutoff_total = (float)v->Wcut;
+    r.W_nuclear_total = (float)v->Wnuc;
+    r.W_boundary_total = (float)v->Wbnd;
+    r.E_in_total = v->Ein;
+    r.E_out_total = v->Eout;
+    r.E_dep_total = v->Edep;
+    r.E_cutoff_total = v->Ecut;
+    r.E_nuclear_total = v->Enuc;
+    r.E_boundary_total = v->Ebnd;
+    const double dw = v->drop_w, de = v->drop_e;
+    r.W_transport_drop_total = fmaxf(0.0f, (float)dw);
+    r.E_transport_drop_total = fmax(0.0, de);
+    if (v->include_source) {
+        const float wso = fmaxf(0.0f, v->src_oog_w), wss = fmaxf(0.0f, v->src_slot_w);
+        const double eso = fmax(0.0, v->src_oog_e), ess = fmax(0.0, v->src_slot_e);
+        r.W_in_total += wso + wss;
+        r.E_in_total += eso + ess;
+        r.W_source_out_of_grid_total = wso;
+        r.W_source_slot_drop_total = wss;
+        r.E_source_out_of_grid_total = eso;
+        r.E_source_slot_drop_total = ess;
+    }
+    r.processed_cells = d.Nc;
+    const float Wr = r.W_out_total + r.W_cutoff_total + r.W_nuclear_total + r.W_boundary_total +
+                     r.W_transport_drop_total + r.W_source_out_of_grid_total + r.W_source_slot_drop_total;
+    const float We = fabsf(r.W_in_total - Wr) / fmaxf(r.W_in_total, 1e-20f);
+    r.W_error = We;
+    r.W_pass = (isfinite(We) && We < 1e-6f) ? 1 : 0;
+    const double Er = r.E_out_total + r.E_dep_total + r.E_cutoff_total + r.E_nuclear_total + r.E_boundary_total +
+                      r.E_transport_drop_total + r.E_source_out_of_grid_total + r.E_source_slot_drop_total;
+    const float Ee_ = (float)(fabs(r.E_in_total - Er) / fmax(r.E_in_total, 1e-20));
+    r.E_error = Ee_;
+    r.E_pass = (isfinite(Ee_) && Ee_ < 1e-5f) ? 1 : 0;
+    const double resid = r.E_in_total - Er;
+    if (isfinite(resid)) it->audit_residual += resid;
+    it->transport_drop_w += dw;
+    it->transport_drop_e += de;
+    it->slots_out += v->slots_out_it;
+    const int k = it->iter;
+    if (k < d.hist_cap) d.hist[k] = r;
+    it->last = r;
+    it->iter = k + 1;
+    it->include_source = 0;
+    it->parity ^= 1;
+    it->blocks_done = 0;
+}
+
+template <class Lay, bool BUCKET>
+__global__ void __launch_bounds__(kThreads) k_audit(Dev d) {
+    __shared__ double s_acc[3][kThreads / 32];
+    __shared__ int s_last;
+    IterState* it = d.it;
+    if (it->halt) return;
+    const int in = it->parity, out = in ^ 1;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cell0 = cell - lane;
+    const bool inb = cell < d.Nc;
+    unsigned bo = __ballot_sync(kFull, inb && d.occ[out][cell]);
+    unsigned bi = __ballot_sync(kFull, inb && d.occ[in][cell]);
+    double W = 0.0, E = 0.0, S = 0.0;
+    while (bo) {   // W/E of psi_out (k5_audit.cu:77-88)
+        const int c = cell0 + __ffs(bo) - 1;
+        bo &= bo - 1;
+        const uint32_t b = d.bid[out][(size_t)c * kKb + lane];
+        unsigned um = __ballot_sync(kFull, b != kEmpty);
+        S += (lane == 0) ? (double)__popc(um) : 0.0;
+        while (um) {
+            const int s = __ffs(um) - 1;
+            um &= um - 1;
+            const uint32_t bs = __shfl_sync(kFull, b, s);
+            const float* v = d.val[out] + ((size_t)c * kKb + s) * Lay::L;
+            for (int l = lane; l < Lay::L; l += 32) {
+                const float w = v[l];
+                if (w <= 0.0f) continue;
+                int Eb = (int)((bs >> 12) & 0xFFFu) * Lay::NE + (l / Lay::NT) % Lay::NE;
+                Eb = max(0, min(Eb, d.N_E - 1));
+                W += (double)w;
+                E += (double)w * (double)(d.Ee[Eb] + 1.0f * (0.5f * (d.Ee[Eb + 1] - d.Ee[Eb])));
+            }
+        }
+    }
+    while (bi) {   // clear the consumed buffer: only its claimed slots hold values
+        const int c = cell0 + __ffs(bi) - 1;
+        bi &= bi - 1;
+        uint32_t* ids = d.bid[in] + (size_t)c * kKb;
+        const uint32_t b = ids[lane];
+        unsigned um = __ballot_sync(kFull, b != kEmpty);
+        while (um) {
+            const int s = __ffs(um) - 1;
+            um &= um - 1;
+            float4* v = reinterpret_cast<float4*>(d.val[in] + ((size_t)c * kKb + s) * Lay::L);
+            for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        ids[lane] = kEmpty;
+        if (lane == 0) d.occ[in][c] = 0;
+    }
+    if (BUCKET) {   // release the bucket map of this iteration's listed cells
+        const int n_co = it->n_coarse, n = n_co + it->n_active;
+        for (int i = cell; i < n; i += gridDim.x * blockDim.x)
+            d.c2b[i < n_co ? d.coarse[i] : d.active[i - n_co]] = -1;
+    }
+    W = warp_sum(W);
+    E = warp_sum(E);
+    S = warp_sum(S);
+    if (lane == 0) { s_acc[0][wid] = W; s_acc[1][wid] = E; s_acc[2][wid] = S; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0, c = 0;
+        for (int w = 0; w < kThreads / 32; ++w) { a += s_acc[0][w]; b += s_acc[1][w]; c += s_acc[2][w]; }
+        if (a != 0.0) atomicAdd(&it->Wout, a);
+        if (b != 0.0) atomicAdd(&it->Eout, b);
+        if (c != 0.0) atomicAdd(&it->slots_out_it, c);
+        __threadfence();
+        const unsigned prev = atomicAdd(&it->blocks_done, 1u);
+        s_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        finalize_audit(d);
+    }
+}
+
+// ------------------------------------------------------------------ spot pipeline helpers
+// Clear every claimed slot of both buffers (reset between spots).
+template <class Lay>
+__global__ void __launch_bounds__(kThreads) k_clear_all(Dev d) {
+    const int lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cell0 = cell - lane;
+    for (int b = 0; b < 2; ++b) {
+        unsigned bo = __ballot_sync(kFull, cell < d.Nc && d.occ[b][cell]);
+        while (bo) {
+            const int c = cell0 + __ffs(bo) - 1;
+            bo &= bo - 1;
+            uint32_t* ids = d.bid[b] + (size_t)c * kKb;
+            const uint32_t x = ids[lane];
+            unsigned um = __ballot_sync(kFull, x != kEmpty);
+            while (um) {
+                const int s = __ffs(um) - 1;
+                um &= um - 1;
+                float4* v = reinterpret_cast<float4*>(d.val[b] + ((size_t)c * kKb + s) * Lay::L);
+                for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            ids[lane] = kEmpty;
+            if (lane == 0) d.occ[b][c] = 0;
+        }
+    }
+}
+
+__global__ void k_reset_state(IterState* it) {
+    if (threadIdx.x || blockIdx.x) return;
+    memset(it, 0, sizeof(IterState));
+    it->max_iter = INT_MAX;
+}
+
+__global__ void k_set_iter_limit(IterState* it, int more) {
+    if (threadIdx.x || blockIdx.x) return;
+    const long long lim = (long long)it->iter + more;
+    it->max_iter = lim > INT_MAX ? INT_MAX : (int)lim;
+}
+
+// Source accounting after injection (gpu_transport_wrapper.cu:339-460): the
+// pencil path books W and E0*W; the represented energy comes from k_totals.
+__global__ void k_source_finalize(IterState* it, const BeamArgs* b, int gaussian) {
+    if (threadIdx.x || blockIdx.x) return;
+    if (!gaussian) {
+        it->src_inj_w = b->W;
+        it->src_inj_e = (double)b->E0 * (double)b->W;
+    }
+    double loss = it->src_inj_e - it->tot_e;
+    if (fabs(loss) < 1e-12) loss = 0.0;
+    it->src_rep_loss = loss;
+    it->include_source = 1;
+    it->done = 0;
+}
+
+template <class Lay>
+__global__ void k_inject_dev(Dev d, const BeamArgs* bp, int gaussian) {
+    const BeamArgs b = *bp;
+    const int par = d.it->parity;
+    if (!gaussian) {
+        if (blockIdx.x || threadIdx.x) return;
+        const float xr = b.x0 - b.x_min, zr = b.z0 - b.z_min;
+        int cx = (int)(xr / d.dx), cz = (int)(zr / d.dz);
+        cx = cx < 0 ? 0 : (cx >= d.Nx ? d.Nx - 1 : cx);
+        cz = cz < 0 ? 0 : (cz >= d.Nz ? d.Nz - 1 : cz);
+        inject_one<Lay>(d, par, cz * d.Nx + cx, b.theta0, b.E0, b.W, xr - cx * d.dx, zr - cz * d.dz);
+        return;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    unsigned s = b.seed + (unsigned)i;
+    const float xs = b.x0 + b.sx * source_normal(s);
+    float ts = b.theta0 + b.sth * source_normal(s);
+    float Es = b.E0 + b.sE * source_normal(s);
+    Es = fmaxf(d.Ee[0], fminf(Es, d.Ee[d.N_E]));
+    ts = fmaxf(d.th[0], fminf(ts, d.th[d.N_theta]));
+    const float xr = xs - b.x_min, zr = b.z0 - b.z_min;
+    const int ix = (int)(xr / d.dx), iz = (int)(zr / d.dz);
+    const float ws = b.W / b.n;
+    IterState* it = d.it;
+    if (ix < 0 || ix >= d.Nx || iz < 0 || iz >= d.Nz) {
+        atomicAdd(&it->src_oog_w, ws);
+        atomicAdd(&it->src_oog_e, (double)(Es * ws));
+        return;
+    }
+    if (inject_one<Lay>(d, par, iz * d.Nx + ix, ts, Es, ws, xr - ix * d.dx, zr - iz * d.dz)) {
+        atomicAdd(&it->src_inj_w, ws);
+        atomicAdd(&it->src_inj_e, (double)(Es * ws));
+    } else {
+        atomicAdd(&it->src_slot_w, ws);
+        atomicAdd(&it->src_slot_e, (double)(Es * ws));
+    }
+}
+
+// Lateral MCS post-convolution of EdepC, one thread per output cell
+// (gpu_transport_wrapper.cu:551-616; kernels built on the host at create).
+__global__ void k_dose(const double* __restrict__ edep, const int* __restrict__ half, const double* __restrict__ ker,
+                       int kstride, int Nx, int Nz, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Nx * Nz) return;
+    const int iz = i / Nx, ix = i - iz * Nx;
+    const int h = half[iz];
+    if (h == 0) { out[i] = edep[i]; return; }
+    const double* k = ker + (size_t)iz * kstride;
+    const double* row = edep + (size_t)iz * Nx;
+    double acc = 0.0;
+    for (int j = -h; j <= h; ++j) {
+        const int x = ix + j;
+        if (x >= 0 && x < Nx) acc += row[x] * k[j + h];
+    }
+    out[i] = acc;
+}
+
+// ------------------------------------------------------------------ raw stage entries
+template <int L>
+__global__ void k_raw_k1(const uint32_t* __restrict__ bid, const float* __restrict__ val, uint8_t* mask,
+                         const uint8_t* prev, int Nc, int b_on, int b_off, float wmin) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= Nc) return;
+    float W = 0.0f;
+    bool on = false, off = false;
+    for (int s = 0; s < kKb; ++s) {
+        const uint32_t b = bid[(size_t)cell * kKb + s];
+        if (b == kEmpty) continue;
+        const uint32_t be = (b >> 12) & 0xFFFu;
+        if (be <= (uint32_t)b_on) on = true;
+        if (be <= (uint32_t)b_off) off = true;
+        const float* v = val + ((size_t)cell * kKb + s) * L;
+        for (int l = 0; l < L; ++l) W += v[l];
+    }
+    const bool p = prev != nullptr && prev[cell] != 0;
+    mask[cell] = ((on || (p && off)) && W > wmin) ? 1 : 0;
+}
+
+template <int L>
+__global__ void k_raw_compact(const uint8_t* mask, const uint32_t* bid, const float* val, int Nc, uint32_t* active,
+                              int* n_active, uint32_t* coarse, int* n_coarse) {
+    __shared__ int s_w[2][32];
+    __shared__ int s_base[2];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    if (threadIdx.x == 0) { s_base[0] = 0; s_base[1] = 0; }
+    __syncthreads();
+    for (int c0 = 0; c0 < Nc; c0 += blockDim.x) {
+        const int cell = c0 + threadIdx.x;
+        int a = 0, c = 0;
+        if (cell < Nc) {
+            if (mask[cell] == 1) {
+                a = 1;
+            } else if (mask[cell] == 0) {
+                for (int s = 0; s < kKb && !c; ++s) {
+                    if (bid[(size_t)cell * kKb + s] == kEmpty) continue;
+                    const float* v = val + ((size_t)cell * kKb + s) * L;
+                    for (int l = 0; l < L; ++l)
+                        if (v[l] > 0.0f) { c = 1; break; }
+                }
+            }
+        }
+        const unsigned ba = __ballot_sync(kFull, a), bc = __ballot_sync(kFull, c);
+        if (lane == 0) { s_w[0][wid] = __popc(ba); s_w[1][wid] = __popc(bc); }
+        __syncthreads();
+        int oa = s_base[0], oc = s_base[1];
+        for (int w = 0; w < wid; ++w) { oa += s_w[0][w]; oc += s_w[1][w]; }
+        const unsigned lt = (1u << lane) - 1u;
+        if (a) active[oa + __popc(ba & lt)] = (uint32_t)cell;
+        if (c) coarse[oc + __popc(bc & lt)] = (uint32_t)cell;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int w = 0; w < nwarp; ++w) { s_base[0] += s_w[0][w]; s_base[1] += s_w[1][w]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { *n_active = s_base[0]; *n_coarse = s_base[1]; }
+}
+
+template <class Lay>
+__global__ void k_raw_gather(const unsigned char* buckets, int bucket_bytes, const int* c2b, uint32_t* ids_out,
+                             float* vals_out, int Nx, int Nz, const float* Ee, int N_E, double* drop) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < Nx * Nz; cell += nw)
+        bucket_gather_cell<Lay>(buckets, bucket_bytes, c2b, ids_out, vals_out, nullptr, cell, Nx, Nz, Ee, N_E, drop,
+                                drop + 1, lane);
+}
+
+struct RawK5 {
+    const uint32_t *bid_in, *bid_out;
+    const float *val_in, *val_out;
+    const double *edep, *e_nuc, *e_bnd, *e_cut, *p_edep, *p_e_nuc, *p_e_bnd, *p_e_cut;
+    const float *w_cut, *w_nuc, *w_bnd, *p_w_cut, *p_w_nuc, *p_w_bnd;
+    const float* Ee;
+    int N_E, NT, NE, L, Nc;
+};
+
+// K5_ConservationAudit over caller arrays (k5_audit.cu:22-167); the totals are
+// reduced hierarchically in double and finalised by the last block.
+__global__ void k_raw_k5(RawK5 a, double* acc /* [11] + counter */, float s_oog_w, float s_slot_w, double s_oog_e,
+                         double s_slot_e, float drop_w, double drop_e, int inc_src, sm2d_audit* rep) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[11] = {0};
+    if (cell < a.Nc) {
+        for (int pass = 0; pass < 2; ++pass) {
+            const uint32_t* bid = pass ? a.bid_out : a.bid_in;
+            const float* val = pass ? a.val_out : a.val_in;
+            for (int s = 0; s < kKb; ++s) {
+                const uint32_t b = bid[(size_t)cell * kKb + s];
+                if (b == kEmpty) continue;
+                for (int l = 0; l < a.L; ++l) {
+                    const float w = val[((size_t)cell * kKb + s) * a.L + l];
+                    if (w <= 0.0f) continue;
+                    int Eb = (int)((b >> 12) & 0xFFFu) * a.NE + (l / a.NT) % a.NE;
+                    Eb = max(0, min(Eb, a.N_E - 1));
+                    const float E = a.Ee[Eb] + 1.0f * (0.5f * (a.Ee[Eb + 1] - a.Ee[Eb]));
+                    v[pass] += (double)w;
+                    v[2 + pass] += (double)w * (double)E;
+                }
+            }
+        }
+        v[4] = fmaxf(0.0f, a.w_cut[cell] - a.p_w_cut[cell]);
+        v[5] = fmaxf(0.0f, a.w_nuc[cell] - a.p_w_nuc[cell]);
+        v[6] = fmaxf(0.0f, a.w_bnd[cell] - a.p_w_bnd[cell]);
+        v[7] = fmax(0.0, a.edep[cell] - a.p_edep[cell]);
+        v[8] = fmax(0.0, a.e_cut[cell] - a.p_e_cut[cell]);
+        v[9] = fmax(0.0, a.e_nuc[cell] - a.p_e_nuc[cell]);
+        v[10] = fmax(0.0, a.e_bnd[cell] - a.p_e_bnd[cell]);
+    }
+    for (int k = 0; k < 11; ++k) {
+        const double s = warp_sum(v[k]);
+        if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(&acc[k], s);
+    }
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned* cnt = reinterpret_cast<unsigned*>(&acc[11]);
+        s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!(s_last && threadIdx.x == 0)) return;
+    __threadfence();
+    volatile double* A = acc;
+    sm2d_audit r;
+    memset(&r, 0, sizeof r);
+    r.W_in_total = (float)A[0];
+    r.W_out_total = (float)A[1];
+    r.E_in_total = A[2];
+    r.E_out_total = A[3];
+    r.W_cutoff_total = (float)A[4];
+    r.W_nuclear_total = (float)A[5];
+    r.W_boundary_total = (float)A[6];
+    r.E_dep_total = A[7];
+    r.E_cutoff_total = A[8];
+    r.E_nuclear_total = A[9];
+    r.E_boundary_total = A[10];
+    r.W_transport_drop_total = fmaxf(0.0f, drop_w);
+    r.E_transport_drop_total = fmax(0.0, drop_e);
+    if (inc_src) {
+        const float wso = fmaxf(0.0f, s_oog_w), wss = fmaxf(0.0f, s_slot_w);
+        const double eso = fmax(0.0, s_oog_e), ess = fmax(0.0, s_slot_e);
+        r.W_in_total += wso + wss;
+        r.E_in_total += eso + ess;
+        r.W_source_out_of_grid_total = wso;
+        r.W_source_slot_drop_total = wss;
+        r.E_source_out_of_grid_total = eso;
+        r.E_source_slot_drop_total = ess;
+    }
+    r.processed_cells = a.Nc;
+    const float Wr = r.W_out_total + r.W_cutoff_total + r.W_nuclear_total + r.W_boundary_total +
+                     r.W_transport_drop_total + r.W_source_out_of_grid_total + r.W_source_slot_drop_total;
+    r.W_error = fabsf(r.W_in_total - Wr) / fmaxf(r.W_in_total, 1e-20f);
+    r.W_pass = (isfinite(r.W_error) && r.W_error < 1e-6f) ? 1 : 0;
+    const double Er = r.E_out_total + r.E_dep_total + r.E_cutoff_total + r.E_nuclear_total + r.E_boundary_total +
+                      r.E_transport_drop_total + r.E_source_out_of_grid_total + r.E_source_slot_drop_total;
+    r.E_error = (float)(fabs(r.E_in_total - Er) / fmax(r.E_in_total, 1e-20));
+    r.E_pass = (isfinite(r.E_error) && r.E_error < 1e-5f) ? 1 : 0;
+    *rep = r;
+}
+
+// ================================================================== engine
+struct Ctx {
+    sm2d_problem p{};
+    std::vector<float> th, Ee, feA, feB, feS;
+    int L = 0, layout = 0;  // 0: LayoutRef, 1: LayoutB128
+    Dev d{};
+    IterState* it_host = nullptr;  // pinned mirror
+    cudaStream_t s = nullptr;
+    std::vector<void*> allocs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphConditionalHandle cond{};
+    cudaEvent_t ev[8] = {};
+    float step_ms[5] = {};
+    int nblk = 0, grid_transport = 0;
+    bool injected = false;
+    BeamArgs* beam_dev = nullptr;   // device copy of the current beam
+    int* dose_half = nullptr;       // per-row half width of the lateral kernel
+    double* dose_ker = nullptr;     // per-row kernel weights
+    double* dose_dev = nullptr;     // convolved dose
+    int dose_stride = 1;
+    std::vector<cudaEvent_t> pev;   // event pool of the profiled replay
+};
+
+static int dalloc(Ctx& c, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(SM2D_ERR_ALLOC, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    c.allocs.push_back(*p);
+    return 0;
+}
+
+template <class Lay>
+struct Impl {
+    static int launch_body(Ctx& c, bool timed, bool use_cond) {
+        const int nb = c.nblk;
+        if (timed) CK(cudaEventRecord(c.ev[0], c.s));
+        k_classify<Lay><<<nb, kThreads, 0, c.s>>>(c.d);
+        if (timed) CK(cudaEventRecord(c.ev[1], c.s));
+        k_compact<<<nb, kThreads, 0, c.s>>>(c.d, c.cond, use_cond ? 1 : 0);
+        if (timed) CK(cudaEventRecord(c.ev[2], c.s));
+        if (c.p.use_buckets) {
+            k_bucket_prep<Lay><<<c.d.Nc, kThreads, 0, c.s>>>(c.d);
+            k_transport<Lay, true><<<c.grid_transport, kThreads, 0, c.s>>>(c.d);
+            if (timed) CK(cudaEventRecord(c.ev[3], c.s));
+            k_bucket_gather<Lay><<<c.grid_transport, kThreads, 0, c.s>>>(c.d);
+        } else {
+            k_transport<Lay, false><<<c.grid_transport, kThreads, 0, c.s>>>(c.d);
+            if (timed) CK(cudaEventRecord(c.ev[3], c.s));
+        }
+        if (timed) CK(cudaEventRecord(c.ev[4], c.s));
+        if (c.p.use_buckets) k_audit<Lay, true><<<nb, kThreads, 0, c.s>>>(c.d);
+        else k_audit<Lay, false><<<nb, kThreads, 0, c.s>>>(c.d);
+        if (timed) CK(cudaEventRecord(c.ev[5], c.s));
+        CK(cudaGetLastError());
+        return 0;
+    }
+    static int inject(Ctx& c, const BeamArgs& b, bool gaussian) {
+        if (gaussian) k_inject<Lay><<<(b.n + 255) / 256, 256, 0, c.s>>>(c.d, b, 1);
+        else k_inject<Lay><<<1, 32, 0, c.s>>>(c.d, b, 0);
+        CK(cudaGetLastError());
+        return 0;
+    }
+    static int clear_all(Ctx& c, int) {
+        k_clear_all<Lay><<<c.nblk, kThreads, 0, c.s>>>(c.d);
+        CK(cudaGetLastError());
+        return 0;
+    }
+    static int inject_dev(Ctx& c, int n, bool gaussian) {
+        if (gaussian) k_inject_dev<Lay><<<(n + 255) / 256, 256, 0, c.s>>>(c.d, c.beam_dev, 1);
+        else k_inject_dev<Lay><<<1, 32, 0, c.s>>>(c.d, c.beam_dev, 0);
+        CK(cudaGetLastError());
+        return 0;
+    }
+    static int totals(Ctx& c, int which) {
+        k_totals<Lay><<<c.nblk, kThreads, 0, c.s>>>(c.d, which);
+        CK(cudaGetLastError());
+        return 0;
+    }
+};
+
+#define DISPATCH(c, fn, ...) ((c).layout == 0 ? Impl<LayoutRef>::fn(c, __VA_ARGS__) : Impl<LayoutB128>::fn(c, __VA_ARGS__))
+
+static int sync_state(Ctx& c) {
+    CK(cudaMemcpyAsync(c.it_host, c.d.it, sizeof(IterState), cudaMemcpyDeviceToHost, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+static int push_state(Ctx& c) {
+    CK(cudaMemcpyAsync(c.d.it, c.it_host, sizeof(IterState), cudaMemcpyHostToDevice, c.s));
+    return 0;
+}
+
+static int build_graph(Ctx& c) {
+    if (c.exec) return 0;
+    CK(cudaGraphCreate(&c.graph, 0));
+    CK(cudaGraphConditionalHandleCreate(&c.cond, c.graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = c.cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, c.graph, nullptr, nullptr, 0, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(c.s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int rc = DISPATCH(c, launch_body, false, true);
+    cudaGraph_t captured = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c.s, &captured);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    CK(cudaGraphInstantiate(&c.exec, c.graph, 0));
+    return 0;
+}
+
+}  // namespace sm2d
+
+using namespace sm2d;
+
+struct sm2d_ctx : sm2d::Ctx {};
+
+extern "C" {
+
+const char* sm2d_last_error(void) { return g_err.c_str(); }
+int sm2d_version(void) { return 1; }
+size_t sm2d_bucket_bytes(int L) { return (size_t)bucket_bytes_for(L); }
+
+int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
+    if (!p || !out) return fail(SM2D_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (p->Nx <= 0 || p->Nz <= 0 || p->N_theta <= 0 || p->N_E <= 1 || !p->theta_edges || !p->E_edges)
+        return fail(SM2D_ERR_ARG, "invalid grid");
+    if (!(p->dx > 0.0f) || !(p->dz > 0.0f)) return fail(SM2D_ERR_ARG, "cell size must be positive");
+    if ((long long)p->Nx * p->Nz > (1LL << 30)) return fail(SM2D_ERR_ARG, "grid too large");
+    int layout;
+    if (p->nt_local == 4 && p->ne_local == 2 && p->nx_sub == 8 && p->nz_sub == 4) layout = 0;
+    else if (p->nt_local == 8 && p->ne_local == 4 && p->nx_sub == 4 && p->nz_sub == 1) layout = 1;
+    else return fail(SM2D_ERR_LAYOUT, "local layout (%d,%d,%d,%d) not compiled; use (4,2,8,4) or (8,4,4,1)",
+                     p->nt_local, p->ne_local, p->nx_sub, p->nz_sub);
+    if (p->N_theta / p->nt_local > 4095 || p->N_E / p->ne_local > 4095)
+        return fail(SM2D_ERR_ARG, "grid exceeds the 12-bit block indices");
+    sm2d_ctx* c = new sm2d_ctx();
+    c->p = *p;
+    c->layout = layout;
+    c->L = p->nt_local * p->ne_local * p->nx_sub * p->nz_sub;
+    c->th.assign(p->theta_edges, p->theta_edges + p->N_theta + 1);
+    c->Ee.assign(p->E_edges, p->E_edges + p->N_E + 1);
+    auto bail = [&](int rc) { sm2d_destroy(c); return rc; };
+    if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(SM2D_ERR_CUDA, "no CUDA device"));
+    for (auto& e : c->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "event create"));
+    const int N = p->N_E;
+    std::vector<float> rep(N), R(N), S(N), lE(N), lR(N), lS(N);
+    for (int i = 0; i < N; ++i) rep[i] = std::sqrt(c->Ee[i] * c->Ee[i + 1]);
+    range_lut(N, rep.data(), R.data(), S.data(), lE.data(), lR.data(), lS.data());
+    c->feA.resize(p->Nz);
+    c->feB.resize(p->Nz);
+    c->feS.resize(p->Nz);
+    fermi_eyges_moments(p->E0, p->Nz, p->dz, p->sigma_x_initial, c->feA.data(), c->feB.data(), c->feS.data());
+    Dev& d = c->d;
+    d.Nx = p->Nx; d.Nz = p->Nz; d.Nc = p->Nx * p->Nz;
+    d.dx = p->dx; d.dz = p->dz;
+    d.N_theta = p->N_theta; d.N_E = N;
+    d.lutN = N;
+    d.lutEmin = p->E_min > 0.0f ? p->E_min : c->Ee[0];
+    d.lutEmax = p->E_max > 0.0f ? p->E_max : c->Ee[N];
+    d.E_fine_on = p->E_fine_on; d.wmin = p->weight_active_min;
+    d.step_coarse = p->step_coarse; d.sx0 = p->sigma_x_initial;
+    // compute_b_E_threshold: EnergyGrid::FindBin(E) / N_E_local
+    auto find_bin_host = [&](float E) {
+        if (E < c->Ee[0]) return 0;
+        if (E >= c->Ee[N]) return N - 1;
+        int lo = 0, hi = N;
+        while (lo < hi) { int m = (lo + hi) / 2; if (c->Ee[m + 1] <= E) lo = m + 1; else hi = m; }
+        return lo;
+    };
+    d.b_on = find_bin_host(p->E_fine_on) / p->ne_local;
+    d.b_off = find_bin_host(p->E_fine_off) / p->ne_local;
+    d.straggle = p->enable_straggling; d.nuclear = p->enable_nuclear;
+    d.seed_mode = p->seed_slot_mode; d.esplit = p->energy_split;
+    d.prune_coarse = p->prune_coarse > 0.0f ? p->prune_coarse : 1e-12f;
+    d.prune_fine = p->prune_fine > 0.0f ? p->prune_fine : 1e-15f;
+    d.split_min_w = p->split_min_weight;
+    d.stop_frac = p->stop_weight_fraction;
+    d.floor_cutoff = p->floor_cutoff;
+    d.salt = p->seed_iteration_salt;
+    const size_t Nc = (size_t)d.Nc, ns = Nc * kKb;
+    void* q;
+    int rc;
+#define A(ptr, type, n)                                              \
+    if ((rc = dalloc(*c, &q, sizeof(type) * (size_t)(n)))) return bail(rc); \
+    ptr = reinterpret_cast<type*>(q)
+    float *th_d, *Ee_d, *R_d, *lE_d, *lR_d, *fa, *fb;
+    A(th_d, float, p->N_theta + 1);
+    A(Ee_d, float, N + 1);
+    A(R_d, float, N);
+    A(lE_d, float, N);
+    A(lR_d, float, N);
+    A(fa, float, p->Nz);
+    A(fb, float, p->Nz);
+    d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d; d.feA = fa; d.feB = fb;
+    for (int b = 0; b < 2; ++b) {
+        A(d.bid[b], uint32_t, ns);
+        A(d.val[b], float, ns * c->L);
+        A(d.occ[b], uint8_t, Nc);
+    }
+    A(d.edep, double, Nc); A(d.e_cut, double, Nc); A(d.e_nuc, double, Nc); A(d.e_bnd, double, Nc);
+    A(d.w_cut, float, Nc); A(d.w_nuc, float, Nc); A(d.w_bnd, float, Nc);
+    A(d.mask, uint8_t, Nc); A(d.cls, uint8_t, Nc);
+    A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
+    c->nblk = (int)((Nc + kThreads - 1) / kThreads);
+    d.nblk = c->nblk;
+    A(d.blk, int, 2 * c->nblk);
+    A(d.it, IterState, 1);
+    d.hist_cap = p->max_iterations > 0 ? p->max_iterations : 4096;
+    A(d.hist, sm2d_audit, d.hist_cap);
+    d.bucket_bytes = bucket_bytes_for(c->L);
+    if (p->use_buckets) {
+        A(d.buckets, unsigned char, (size_t)Nc * 4 * d.bucket_bytes);
+        A(d.c2b, int, Nc);
+        if (cudaMemsetAsync(d.c2b, 0xFF, Nc * sizeof(int), c->s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "memset"));
+    }
+    A(c->beam_dev, BeamArgs, 1);
+    {   // lateral post-convolution kernels per depth row
+        std::vector<int> half(p->Nz, 0);
+        std::vector<double> k(p->Nx + 2);
+        int hmax = 1;
+        for (int iz = 0; iz < p->Nz; ++iz) {
+            half[iz] = lateral_kernel(c->feS[iz], p->sigma_x_initial, p->dx, p->Nx, k.data());
+            hmax = std::max(hmax, half[iz]);
+        }
+        c->dose_stride = 2 * hmax + 1;
+        std::vector<double> ker((size_t)p->Nz * c->dose_stride, 0.0);
+        for (int iz = 0; iz < p->Nz; ++iz)
+            if (half[iz]) lateral_kernel(c->feS[iz], p->sigma_x_initial, p->dx, p->Nx, &ker[(size_t)iz * c->dose_stride]);
+        A(c->dose_half, int, p->Nz);
+        A(c->dose_ker, double, ker.size());
+        A(c->dose_dev, double, Nc);
+        if (cudaMemcpy(c->dose_half, half.data(), sizeof(int) * p->Nz, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(c->dose_ker, ker.data(), sizeof(double) * ker.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(SM2D_ERR_CUDA, "dose kernel upload"));
+    }
+#undef A
+    if (cudaMallocHost(&c->it_host, sizeof(IterState)) != cudaSuccess) return bail(fail(SM2D_ERR_ALLOC, "pinned"));
+    memset(c->it_host, 0, sizeof(IterState));
+    c->it_host->max_iter = INT_MAX;
+    cudaStream_t s = c->s;
+    bool ok = cudaMemcpyAsync(th_d, c->th.data(), sizeof(float) * (p->N_theta + 1), cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(Ee_d, c->Ee.data(), sizeof(float) * (N + 1), cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(R_d, R.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(lE_d, lE.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(lR_d, lR.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(fa, c->feA.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(fb, c->feB.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    for (int b = 0; b < 2 && ok; ++b)
+        ok = cudaMemsetAsync(d.bid[b], 0xFF, ns * 4, s) == cudaSuccess &&
+             cudaMemsetAsync(d.val[b], 0, ns * c->L * 4, s) == cudaSuccess &&
+             cudaMemsetAsync(d.occ[b], 0, Nc, s) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(d.edep, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_cut, 0, Nc * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.e_nuc, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_bnd, 0, Nc * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.w_cut, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.w_nuc, 0, Nc * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.w_bnd, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.mask, 0, Nc, s) == cudaSuccess &&
+         cudaMemsetAsync(d.cls, 0, Nc, s) == cudaSuccess;
+    if (!ok) return bail(fail(SM2D_ERR_CUDA, "initial copies failed"));
+    {   // grid origin of the beam description is fixed per problem
+        BeamArgs origin{};
+        origin.x_min = p->x_min;
+        origin.z_min = p->z_min;
+        if (cudaMemcpyAsync(c->beam_dev, &origin, sizeof origin, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return bail(fail(SM2D_ERR_CUDA, "beam origin upload"));
+    }
+    if (push_state(*c)) return bail(SM2D_ERR_CUDA);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    c->grid_transport = std::max(1, std::min((int)((Nc + 7) / 8), 8 * std::max(sms, 1)));
+    if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "create sync"));
+    *out = c;
+    return 0;
+}
+
+int sm2d_destroy(sm2d_handle h) {
+    if (!h) return 0;
+    if (h->s) cudaStreamSynchronize(h->s);
+    if (h->exec) cudaGraphExecDestroy(h->exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : h->pev) cudaEventDestroy(e);
+    if (h->it_host) cudaFreeHost(h->it_host);
+    if (h->s) cudaStreamDestroy(h->s);
+    delete h;
+    return 0;
+}
+
+int sm2d_local_bins(sm2d_handle h) { return h ? h->L : SM2D_ERR_ARG; }
+
+int sm2d_inject(sm2d_handle h, const sm2d_beam* b) {
+    if (!h || !b) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    int rc = sync_state(c);
+    if (rc) return rc;
+    const bool gaussian = (b->n_samples > 1) || (b->sigma_x > 0.0f) || (b->sigma_theta > 0.0f);  // wrapper.cu:246
+    if (gaussian && b->n_samples <= 0) return fail(SM2D_ERR_ARG, "n_samples must be positive");
+    IterState& it = *c.it_host;
+    it.src_inj_w = it.src_oog_w = it.src_slot_w = 0.0f;
+    it.src_inj_e = it.src_oog_e = it.src_slot_e = 0.0;
+    it.tot_w = it.tot_e = 0.0;
+    if ((rc = push_state(c))) return rc;
+    BeamArgs a{b->x0, b->z0, b->theta0, b->E0, b->W_total, b->sigma_x, b->sigma_theta, b->sigma_E,
+               c.p.x_min, c.p.z_min, b->n_samples, b->seed};
+    if ((rc = DISPATCH(c, inject, a, gaussian))) return rc;
+    if ((rc = DISPATCH(c, totals, 0))) return rc;
+    if ((rc = sync_state(c))) return rc;
+    if (!gaussian) {
+        it.src_inj_w = b->W_total;
+        it.src_inj_e = (double)b->E0 * (double)b->W_total;
+    }
+    double loss = it.src_inj_e - it.tot_e;
+    if (std::fabs(loss) < 1e-12) loss = 0.0;
+    it.src_rep_loss = loss;
+    it.include_source = 1;
+    it.done = 0;
+    if ((rc = push_state(c))) return rc;
+    CK(cudaStreamSynchronize(c.s));
+    c.injected = true;
+    return 0;
+}
+
+int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
+    if (!h || !bid || !val) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    int rc = sync_state(c);
+    if (rc) return rc;
+    const int par = c.it_host->parity;
+    const size_t ns = (size_t)c.d.Nc * kKb;
+    std::vector<uint8_t> occ(c.d.Nc, 0);
+    for (size_t i = 0; i < ns; ++i)
+        if (bid[i] != kEmpty) occ[i / kKb] = 1;
+    CK(cudaMemcpyAsync(c.d.bid[par], bid, ns * 4, cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.val[par], val, ns * c.L * 4, cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), c.d.Nc, cudaMemcpyHostToDevice, c.s));
+    c.it_host->done = 0;
+    if ((rc = push_state(c))) return rc;
+    CK(cudaStreamSynchronize(c.s));
+    c.injected = true;
+    return 0;
+}
+
+int sm2d_get_psi_in(sm2d_handle h, uint32_t* bid, float* val) {
+    if (!h || !bid) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    int rc = sync_state(c);
+    if (rc) return rc;
+    const int par = c.it_host->parity;
+    const size_t ns = (size_t)c.d.Nc * kKb;
+    CK(cudaMemcpyAsync(bid, c.d.bid[par], ns * 4, cudaMemcpyDeviceToHost, c.s));
+    if (val) CK(cudaMemcpyAsync(val, c.d.val[par], ns * c.L * 4, cudaMemcpyDeviceToHost, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+
+int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space: call sm2d_inject or sm2d_set_psi_in first");
+    int rc = DISPATCH(c, launch_body, true, false);
+    if (rc) return rc;
+    if ((rc = sync_state(c))) return rc;
+    float ms[5];
+    for (int k = 0; k < 5; ++k) CK(cudaEventElapsedTime(&ms[k], c.ev[k], c.ev[k + 1]));
+    // ms: classify, compact, transport(+bucket prep), K4 gather, audit
+    for (int k = 0; k < 5; ++k) c.step_ms[k] = ms[k];
+    if (n_active) *n_active = c.it_host->done ? 0 : c.it_host->n_active;
+    if (n_coarse) *n_coarse = c.it_host->done ? 0 : c.it_host->n_coarse;
+    return 0;
+}
+
+static int run_impl(Ctx& c, int max_it, int* done_iters, float* ms) {
+    if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space: call sm2d_inject or sm2d_set_psi_in first");
+    if (max_it <= 0) return fail(SM2D_ERR_ARG, "max_iterations must be positive");
+    int rc = build_graph(c);
+    if (rc) return rc;
+    if ((rc = sync_state(c))) return rc;
+    const int start = c.it_host->iter;
+    c.it_host->max_iter = start + max_it;
+    if ((rc = push_state(c))) return rc;
+    if (ms) CK(cudaEventRecord(c.ev[6], c.s));
+    CK(cudaGraphLaunch(c.exec, c.s));
+    if (ms) CK(cudaEventRecord(c.ev[7], c.s));
+    CK(cudaStreamSynchronize(c.s));
+    if (ms) CK(cudaEventElapsedTime(ms, c.ev[6], c.ev[7]));
+    if ((rc = sync_state(c))) return rc;
+    c.it_host->max_iter = INT_MAX;
+    if ((rc = push_state(c))) return rc;
+    CK(cudaStreamSynchronize(c.s));
+    if (done_iters) *done_iters = c.it_host->iter - start;
+    return 0;
+}
+
+int sm2d_run(sm2d_handle h, int max_it, int* done_iters) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    return run_impl(*h, max_it, done_iters, nullptr);
+}
+
+int sm2d_run_timed(sm2d_handle h, int max_it, int* done_iters, float* ms) {
+    if (!h || !ms) return fail(SM2D_ERR_ARG, "null argument");
+    return run_impl(*h, max_it, done_iters, ms);
+}
+
+int sm2d_get_mask(sm2d_handle h, uint8_t* mask) {
+    if (!h || !mask) return fail(SM2D_ERR_ARG, "null argument");
+    CK(cudaMemcpyAsync(mask, h->d.mask, h->d.Nc, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    for (int i = 0; i < h->d.Nc; ++i) mask[i] &= 1;
+    return 0;
+}
+
+int sm2d_get_lists(sm2d_handle h, uint32_t* active, int* na, uint32_t* coarse, int* nc) {
+    if (!h || !na || !nc) return fail(SM2D_ERR_ARG, "null argument");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    *na = h->it_host->done ? 0 : h->it_host->n_active;
+    *nc = h->it_host->done ? 0 : h->it_host->n_coarse;
+    if (active && *na) CK(cudaMemcpyAsync(active, h->d.active, sizeof(uint32_t) * *na, cudaMemcpyDeviceToHost, h->s));
+    if (coarse && *nc) CK(cudaMemcpyAsync(coarse, h->d.coarse, sizeof(uint32_t) * *nc, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+int sm2d_get_tallies(sm2d_handle h, double* edep, float* w_cut, double* e_cut, float* w_nuc, double* e_nuc,
+                     float* w_bnd, double* e_bnd) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    const size_t n = (size_t)h->d.Nc;
+    const Dev& d = h->d;
+    if (edep) CK(cudaMemcpyAsync(edep, d.edep, n * 8, cudaMemcpyDeviceToHost, h->s));
+    if (w_cut) CK(cudaMemcpyAsync(w_cut, d.w_cut, n * 4, cudaMemcpyDeviceToHost, h->s));
+    if (e_cut) CK(cudaMemcpyAsync(e_cut, d.e_cut, n * 8, cudaMemcpyDeviceToHost, h->s));
+    if (w_nuc) CK(cudaMemcpyAsync(w_nuc, d.w_nuc, n * 4, cudaMemcpyDeviceToHost, h->s));
+    if (e_nuc) CK(cudaMemcpyAsync(e_nuc, d.e_nuc, n * 8, cudaMemcpyDeviceToHost, h->s));
+    if (w_bnd) CK(cudaMemcpyAsync(w_bnd, d.w_bnd, n * 4, cudaMemcpyDeviceToHost, h->s));
+    if (e_bnd) CK(cudaMemcpyAsync(e_bnd, d.e_bnd, n * 8, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+int sm2d_get_audit(sm2d_handle h, sm2d_audit* out) {
+    if (!h || !out) return fail(SM2D_ERR_ARG, "null argument");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    *out = h->it_host->last;
+    return 0;
+}
+
+int sm2d_get_audit_history(sm2d_handle h, sm2d_audit* out, int max_entries, int* n) {
+    if (!h || !out || !n) return fail(SM2D_ERR_ARG, "null argument");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    *n = std::min(std::min(h->it_host->iter, h->d.hist_cap), max_entries);
+    if (*n > 0) CK(cudaMemcpyAsync(out, h->d.hist, sizeof(sm2d_audit) * *n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+int sm2d_get_scalars(sm2d_handle h, double* o) {
+    if (!h || !o) return fail(SM2D_ERR_ARG, "null argument");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    const IterState& it = *h->it_host;
+    o[0] = it.transport_drop_w; o[1] = it.transport_drop_e; o[2] = it.audit_residual;
+    o[3] = it.src_inj_w; o[4] = it.src_inj_e; o[5] = it.src_oog_w; o[6] = it.src_oog_e;
+    o[7] = it.src_slot_w; o[8] = it.src_slot_e; o[9] = it.src_rep_loss;
+    o[10] = it.iter; o[11] = it.cell_steps; o[12] = it.slots_in; o[13] = it.slots_out;
+    return 0;
+}
+
+int sm2d_get_fe(sm2d_handle h, float* A, float* B, float* S) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    const size_t n = h->feA.size();
+    if (A) memcpy(A, h->feA.data(), n * 4);
+    if (B) memcpy(B, h->feB.data(), n * 4);
+    if (S) memcpy(S, h->feS.data(), n * 4);
+    return 0;
+}
+
+static int enqueue_dose(Ctx& c) {
+    const int n = c.d.Nc;
+    k_dose<<<(n + 255) / 256, 256, 0, c.s>>>(c.d.edep, c.dose_half, c.dose_ker, c.dose_stride, c.d.Nx, c.d.Nz,
+                                             c.dose_dev);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int sm2d_get_dose(sm2d_handle h, double* dose) {
+    if (!h || !dose) return fail(SM2D_ERR_ARG, "null argument");
+    int rc = enqueue_dose(*h);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dose, h->dose_dev, sizeof(double) * h->d.Nc, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+void* sm2d_stream(sm2d_handle h) { return h ? (void*)h->s : nullptr; }
+
+int sm2d_reset(sm2d_handle h) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    int rc = DISPATCH(c, clear_all, 0);
+    if (rc) return rc;
+    const size_t n = (size_t)c.d.Nc;
+    CK(cudaMemsetAsync(c.d.edep, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(c.d.e_cut, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(c.d.e_nuc, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(c.d.e_bnd, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(c.d.w_cut, 0, n * 4, c.s));
+    CK(cudaMemsetAsync(c.d.w_nuc, 0, n * 4, c.s));
+    CK(cudaMemsetAsync(c.d.w_bnd, 0, n * 4, c.s));
+    CK(cudaMemsetAsync(c.d.mask, 0, n, c.s));
+    CK(cudaMemsetAsync(c.d.cls, 0, n, c.s));
+    k_reset_state<<<1, 1, 0, c.s>>>(c.d.it);
+    CK(cudaGetLastError());
+    c.injected = false;
+    return 0;
+}
+
+int sm2d_inject_async(sm2d_handle h, const sm2d_beam* b) {
+    if (!h || !b) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    const bool gaussian = (b->n_samples > 1) || (b->sigma_x > 0.0f) || (b->sigma_theta > 0.0f);
+    if (gaussian && b->n_samples <= 0) return fail(SM2D_ERR_ARG, "n_samples must be positive");
+    // the beam travels as-is (host struct -> device); x_min/z_min come from the problem
+    static_assert(sizeof(sm2d_beam) == 10 * 4, "beam layout");
+    CK(cudaMemcpyAsync(c.beam_dev, b, 8 * sizeof(float), cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(reinterpret_cast<char*>(c.beam_dev) + offsetof(BeamArgs, n), &b->n_samples,
+                       sizeof(int) + sizeof(unsigned), cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemsetAsync(&c.d.it->src_inj_w, 0, offsetof(IterState, last) - offsetof(IterState, src_inj_w), c.s));
+    int rc = DISPATCH(c, inject_dev, b->n_samples, gaussian);
+    if (rc) return rc;
+    if ((rc = DISPATCH(c, totals, 0))) return rc;
+    k_source_finalize<<<1, 1, 0, c.s>>>(c.d.it, c.beam_dev, gaussian ? 1 : 0);
+    CK(cudaGetLastError());
+    c.injected = true;
+    return 0;
+}
+
+int sm2d_run_async(sm2d_handle h, int max_it) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space: call sm2d_inject or sm2d_set_psi_in first");
+    if (max_it <= 0) return fail(SM2D_ERR_ARG, "max_iterations must be positive");
+    int rc = build_graph(c);
+    if (rc) return rc;
+    k_set_iter_limit<<<1, 1, 0, c.s>>>(c.d.it, max_it);
+    CK(cudaGetLastError());
+    CK(cudaGraphLaunch(c.exec, c.s));
+    return 0;
+}
+
+int sm2d_dose_async(sm2d_handle h, double* host_dose) {
+    if (!h || !host_dose) return fail(SM2D_ERR_ARG, "null argument");
+    int rc = enqueue_dose(*h);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(host_dose, h->dose_dev, sizeof(double) * h->d.Nc, cudaMemcpyDeviceToHost, h->s));
+    return 0;
+}
+
+int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms5, int* launches) {
+    if (!h || !ms5 || n <= 0) return fail(SM2D_ERR_ARG, "invalid argument");
+    Ctx& c = *h;
+    if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space");
+    int rc = sync_state(c);
+    if (rc) return rc;
+    const int start = c.it_host->iter;
+    const size_t need = (size_t)6 * n;
+    while (c.pev.size() < need) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        c.pev.push_back(e);
+    }
+    cudaEvent_t saved[8];
+    memcpy(saved, c.ev, sizeof saved);
+    for (int i = 0; i < n; ++i) {
+        for (int k = 0; k < 6; ++k) c.ev[k] = c.pev[6 * i + k];
+        if ((rc = DISPATCH(c, launch_body, true, false))) break;
+    }
+    memcpy(c.ev, saved, sizeof saved);
+    if (rc) return rc;
+    if ((rc = sync_state(c))) return rc;
+    const int done = c.it_host->iter - start;
+    for (int k = 0; k < 5; ++k) ms5[k] = 0.0f;
+    for (int i = 0; i < done; ++i)
+        for (int k = 0; k < 5; ++k) {
+            float t = 0.0f;
+            CK(cudaEventElapsedTime(&t, c.pev[6 * i + k], c.pev[6 * i + k + 1]));
+            ms5[k] += t;
+        }
+    if (done_iters) *done_iters = done;
+    if (launches) *launches = done * (c.p.use_buckets ? 6 : 4);
+    return 0;
+}
+
+int sm2d_get_step_timing(sm2d_handle h, float* ms5) {
+    if (!h || !ms5) return fail(SM2D_ERR_ARG, "null argument");
+    memcpy(ms5, h->step_ms, sizeof h->step_ms);
+    return 0;
+}
+
+// ---------------------------------------------------------------- host tables
+int sm2d_energy_grid_log(float E_min, float E_max, int N, float* edges, float* rep) {
+    if (N <= 0 || !(E_min > 0.0f) || !(E_max > E_min) || !edges || !rep) return fail(SM2D_ERR_ARG, "invalid grid");
+    energy_grid_log(E_min, E_max, N, edges, rep);
+    return 0;
+}
+int sm2d_energy_grid_piecewise(int n, const float* g, float* edges, float* rep) {
+    if (n <= 0 || !g) return fail(SM2D_ERR_ARG, "invalid groups");
+    for (int k = 0; k < n; ++k)
+        if (!(g[3 * k + 2] > 0.0f) || !(g[3 * k + 1] > g[3 * k])) return fail(SM2D_ERR_ARG, "invalid group %d", k);
+    if (edges && !rep) return fail(SM2D_ERR_ARG, "rep is null");
+    return energy_grid_piecewise(n, g, edges, rep);
+}
+int sm2d_angular_grid(float lo, float hi, int N, float* edges, float* rep) {
+    if (N <= 0 || !(hi > lo) || !edges || !rep) return fail(SM2D_ERR_ARG, "invalid grid");
+    angular_grid(lo, hi, N, edges, rep);
+    return 0;
+}
+int sm2d_range_lut(int N, const float* rep, float* R, float* S, float* logE, float* logR, float* logS) {
+    if (N <= 0 || !rep || !R || !S || !logE || !logR || !logS) return fail(SM2D_ERR_ARG, "null argument");
+    range_lut(N, rep, R, S, logE, logR, logS);
+    return 0;
+}
+int sm2d_fermi_eyges(float E0, int Nz, float dz, float sx0, float* A, float* B, float* S) {
+    if (Nz <= 0 || !(dz > 0.0f) || !A || !B || !S) return fail(SM2D_ERR_ARG, "invalid argument");
+    fermi_eyges_moments(E0, Nz, dz, sx0, A, B, S);
+    return 0;
+}
+
+// ---------------------------------------------------------------- raw stage entries
+int sm2d_k1_active_mask(const uint32_t* bid, const float* val, uint8_t* mask, const uint8_t* prev, int Nx, int Nz,
+                        int L, int b_on, int b_off, float wmin, void* stream) {
+    if (!bid || !val || !mask || Nx <= 0 || Nz <= 0) return fail(SM2D_ERR_ARG, "invalid argument");
+    const int Nc = Nx * Nz, blocks = (Nc + 255) / 256;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (L == 256) k_raw_k1<256><<<blocks, 256, 0, s>>>(bid, val, mask, prev, Nc, b_on, b_off, wmin);
+    else if (L == 128) k_raw_k1<128><<<blocks, 256, 0, s>>>(bid, val, mask, prev, Nc, b_on, b_off, wmin);
+    else return fail(SM2D_ERR_LAYOUT, "local_bins must be 256 or 128");
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int sm2d_compact_lists(const uint8_t* mask, const uint32_t* bid, const float* val, int Nx, int Nz, int L,
+                       uint32_t* active, int* n_active, uint32_t* coarse, int* n_coarse, void* stream) {
+    if (!mask || !bid || !val || !active || !coarse || !n_active || !n_coarse) return fail(SM2D_ERR_ARG, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (L == 256) k_raw_compact<256><<<1, 1024, 0, s>>>(mask, bid, val, Nx * Nz, active, n_active, coarse, n_coarse);
+    else if (L == 128) k_raw_compact<128><<<1, 1024, 0, s>>>(mask, bid, val, Nx * Nz, active, n_active, coarse, n_coarse);
+    else return fail(SM2D_ERR_LAYOUT, "local_bins must be 256 or 128");
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int sm2d_k4_bucket_transfer(const void* buckets, const int* c2b, float* val_out, uint32_t* bid_out, int Nx, int Nz,
+                            int L, int nt_local, int ne_local, int nx_sub, const float* Ee, int N_E, int N_E_local,
+                            double* drop, void* stream) {
+    if (!buckets || !c2b || !val_out || !bid_out || !Ee || !drop) return fail(SM2D_ERR_ARG, "null argument");
+    (void)N_E_local;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int blocks = std::max(1, std::min((Nx * Nz + 7) / 8, 65535));
+    if (L == 256 && nt_local == 4 && ne_local == 2 && nx_sub == 8)
+        k_raw_gather<LayoutRef><<<blocks, 256, 0, s>>>((const unsigned char*)buckets, bucket_bytes_for(256), c2b,
+                                                        bid_out, val_out, Nx, Nz, Ee, N_E, drop);
+    else if (L == 128 && nt_local == 8 && ne_local == 4 && nx_sub == 4)
+        k_raw_gather<LayoutB128><<<blocks, 256, 0, s>>>((const unsigned char*)buckets, bucket_bytes_for(128), c2b,
+                                                         bid_out, val_out, Nx, Nz, Ee, N_E, drop);
+    else return fail(SM2D_ERR_LAYOUT, "layout not compiled");
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int sm2d_k5_conservation_audit(const uint32_t* bid_in, const float* val_in, const uint32_t* bid_out,
+                               const float* val_out, const double* EdepC, const double* e_nuc, const double* e_bnd,
+                               const double* e_cut, const double* p_edep, const double* p_e_nuc,
+                               const double* p_e_bnd, const double* p_e_cut, const float* w_cut,
+                               const float* w_nuc, const float* w_bnd, const float* p_w_cut,
+                               const float* p_w_nuc, const float* p_w_bnd, float s_oog_w, float s_slot_w,
+                               double s_oog_e, double s_slot_e, float drop_w, double drop_e, int inc_src,
+                               const float* Ee, int N_E, int nt_local, int N_E_local, int L, sm2d_audit* d_report,
+                               int N_cells, void* stream) {
+    if (!bid_in || !val_in || !bid_out || !val_out || !EdepC || !Ee || !d_report || N_cells <= 0)
+        return fail(SM2D_ERR_ARG, "invalid argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    static double* acc = nullptr;
+    if (!acc) CK(cudaMalloc(&acc, 12 * sizeof(double)));
+    CK(cudaMemsetAsync(acc, 0, 12 * sizeof(double), s));
+    RawK5 a{bid_in, bid_out, val_in, val_out, EdepC, e_nuc, e_bnd, e_cut, p_edep, p_e_nuc, p_e_bnd, p_e_cut,
+            w_cut, w_nuc, w_bnd, p_w_cut, p_w_nuc, p_w_bnd, Ee, N_E, nt_local, N_E_local, L, N_cells};
+    k_raw_k5<<<(N_cells + 255) / 256, 256, 0, s>>>(a, acc, s_oog_w, s_slot_w, s_oog_e, s_slot_e, drop_w, drop_e, inc_src,
+                                                   d_report);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+}  // extern "C"

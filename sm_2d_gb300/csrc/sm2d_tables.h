@@ -1,0 +1,11 @@
+// sm2d_tables.h -- host-side tables of the transport step (see sm2d_tables.cpp).
+#pragma once
+
+namespace sm2d {
+void energy_grid_log(float E_min, float E_max, int N, float* edges, float* rep);
+int energy_grid_piecewise(int n_groups, const float* groups, float* edges, float* rep);
+void angular_grid(float lo, float hi, int N, float* edges, float* rep);
+void range_lut(int N, const float* rep, float* R, float* S, float* logE, float* logR, float* logS);
+void fermi_eyges_moments(float E0, int Nz, float dz, float sigma_x0, float* A, float* B, float* sigma);
+int lateral_kernel(float sigma_total, float sigma_x0, float dx, int Nx, double* k);
+}  // namespace sm2d

@@ -1,0 +1,507 @@
+// sm2d_transport.cuh -- per-bin coarse (K2) and fine (K3) transport and the
+// emission of the moved weight, for one warp per listed cell.
+//
+// Method (reference files cited inline): every nonzero local bin of a
+// listed cell is one component at its bin-centre angle/energy and sub-cell
+// centre.  K2 (cells without low-energy blocks) takes a step of
+// min(step_coarse, dx, dz), split at the fine-transport threshold; K3 takes
+// an R-limited step capped by the distance to the cell boundary, with
+// hashed Vavilov straggling.  Both apply nuclear attenuation and one hashed
+// MCS angle sample, then either cross a face or stay in the cell.
+//
+// Emission is written through a Sink:
+//   * direct mode scatters straight into psi_out of the destination cell
+//     (the neighbour-scatter form of K4 fused into the transport kernel);
+//   * bucket mode writes the reference's DeviceOutflowBucket of the source
+//     cell and face; sm2d_k4_gather then moves it (K4_BucketTransfer).
+#pragma once
+#include "sm2d_device.cuh"
+
+namespace sm2d {
+
+enum { FACE_ZP = 0, FACE_ZM = 1, FACE_XP = 2, FACE_XM = 3 };
+
+struct Tally {                // per-lane accumulators of one cell
+    double edep, e_cut, e_nuc, e_bnd;
+    float w_cut, w_nuc, w_bnd;
+    double drop_w, drop_e;    // slot / bucket / prune drops
+    double Win, Ein;          // psi_in weight and energy of the cell
+};
+
+__device__ __forceinline__ float e_center(const Dev& d, int b) { return d.Ee[b] + 0.5f * (d.Ee[b + 1] - d.Ee[b]); }
+
+struct EParts {
+    int n;
+    int bin[2];
+    float frac[2];
+    float Erep;
+};
+// Energy re-binning of an emitted component: the bin containing E
+// (device_find_bin_edges), or with the energy split a mean-preserving pair of
+// neighbouring bin centres.
+__device__ __forceinline__ EParts bin_energy(const Dev& d, float E, float w) {
+    EParts p;
+    int k = find_bin(d.Ee, d.N_E, E);
+    p.n = 1;
+    p.bin[0] = p.bin[1] = k;
+    p.frac[0] = 1.0f;
+    p.frac[1] = 0.0f;
+    p.Erep = e_center(d, k);
+    if (!d.esplit) return p;
+    float ck = p.Erep;
+    int lo = E >= ck ? k : k - 1, hi = lo + 1;
+    if (lo < 0 || hi > d.N_E - 1) return p;
+    float cl = e_center(d, lo), ch = e_center(d, hi);
+    float fh = (E - cl) / (ch - cl);
+    if (fh <= 0.0f) { p.bin[0] = lo; p.Erep = cl; return p; }
+    if (fh >= 1.0f) { p.bin[0] = hi; p.Erep = ch; return p; }
+    if (w * fminf(fh, 1.0f - fh) < d.split_min_w) {   // light minor part stays with the major bin
+        if (fh >= 0.5f) { p.bin[0] = hi; p.Erep = ch; } else { p.bin[0] = lo; p.Erep = cl; }
+        return p;
+    }
+    p.n = 2;
+    p.bin[0] = lo; p.frac[0] = 1.0f - fh;
+    p.bin[1] = hi; p.frac[1] = fh;
+    p.Erep = p.frac[0] * cl + p.frac[1] * ch;
+    return p;
+}
+
+template <class Lay, bool BUCKET>
+struct Sink {
+    // Place weight w of local bin lidx of block `want`: bucket (bcell, face)
+    // in bucket mode, psi_out of dcell in direct mode.  Returns the weight
+    // that found no slot.
+    __device__ __forceinline__ static float put(const Dev& d, int par, int bcell, int face, int dcell,
+                                                uint32_t want, int lidx, float w, double& eshift) {
+        uint32_t* ids;
+        float* vals;
+        if (BUCKET) {
+            int base = d.c2b[bcell];
+            if (base < 0) return w;
+            unsigned char* b = d.buckets + (size_t)(base + face) * d.bucket_bytes;
+            ids = bucket_ids(b);
+            vals = bucket_vals(b);
+        } else {
+            ids = d.bid[par ^ 1] + (size_t)dcell * kKb;
+            vals = d.val[par ^ 1] + (size_t)dcell * kKb * Lay::L;
+        }
+        uint32_t sel;
+        int s = claim_slot(ids, want, sel);
+        if (s < 0) return w;
+        if (!BUCKET) d.occ[par ^ 1][dcell] = 1;
+        int le = (sel == want) ? lidx : remap_lidx<Lay>(lidx, want, sel);
+        if (sel != want && d.esplit) {   // split method: a re-binned part keeps its energy
+            const int e0 = (int)((want >> 12) & 0xFFFu) * Lay::NE + (lidx / Lay::NT) % Lay::NE;
+            const int e1 = (int)((sel >> 12) & 0xFFFu) * Lay::NE + (le / Lay::NT) % Lay::NE;
+            eshift += (double)((e_center(d, e0) - e_center(d, e1)) * w);
+        }
+        atomicAdd(vals + (size_t)s * Lay::L + le, w);
+        return 0.0f;
+    }
+};
+
+// Two-bin theta split around the nearest bin centre with frac^2 weight to
+// the neighbour, energy re-binning, slot claim (device_bucket.cuh:431-533).
+template <class Lay, bool BUCKET>
+__device__ float emit_component(const Dev& d, int par, int bcell, int face, int dcell, float theta, float E,
+                                float weight, int xs, int zs, double& eshift) {
+    if (weight <= 0.0f) return 0.0f;
+    const float tmin = d.th[0], tmax = d.th[d.N_theta];
+    const float dth = (tmax - tmin) / (float)d.N_theta;
+    const float tc = fmaxf(tmin, fminf(theta, tmax));
+    const float c0 = tmin + 0.5f * dth;
+    int bc = (int)floorf((tc - c0) / dth + 0.5f);
+    bc = max(0, min(bc, d.N_theta - 1));
+    const float delta = tc - (c0 + (float)bc * dth);
+    int tb1 = bc;
+    if (delta > 0.0f && bc < d.N_theta - 1) tb1 = bc + 1;
+    else if (delta < 0.0f && bc > 0) tb1 = bc - 1;
+    float tw0 = 1.0f, tw1 = 0.0f;
+    if (tb1 != bc) {
+        float f = fminf(1.0f, fabsf(delta) / dth);
+        tw1 = f * f;
+        tw0 = 1.0f - tw1;
+        if (d.esplit && weight * tw1 < d.split_min_w) { tw1 = 0.0f; tw0 = 1.0f; }
+    }
+    const float Ec = fmaxf(d.Ee[0], fminf(E, d.Ee[d.N_E]));
+    const EParts ep = bin_energy(d, Ec, weight);
+    float dropped = 0.0f;
+    for (int ei = 0; ei < ep.n; ++ei) {
+        const int Eb = ep.bin[ei];
+        const int El = Eb % Lay::NE;
+        const uint32_t bE = (uint32_t)(Eb / Lay::NE);
+#pragma unroll
+        for (int ti = 0; ti < 2; ++ti) {
+            const float wt = ti ? tw1 : tw0;
+            if (wt <= 0.0f) continue;
+            float we = weight * wt;
+            if (d.esplit) we = we * ep.frac[ei];
+            const int tb = ti ? tb1 : bc;
+            const uint32_t want = make_bid((uint32_t)(tb / Lay::NT), bE);
+            const int l = Lay::enc(tb % Lay::NT, El, xs, zs);
+            dropped += Sink<Lay, BUCKET>::put(d, par, bcell, face, dcell, want, l, we, eshift);
+        }
+    }
+    return dropped;
+}
+
+// +z crossing with the N-cell lateral Gaussian split: the share of column
+// ix+k goes through the +z bucket of cell (ix+k, iz) to cell (ix+k, iz+1)
+// (device_bucket.cuh:857-987).
+template <class Lay, bool BUCKET>
+__device__ float emit_forward(const Dev& d, int par, int src, int my_cls, float theta, float E, float weight,
+                              float xoff, float sigma, float& boundary_w, double& eshift) {
+    if (weight <= 0.0f) return 0.0f;
+    constexpr int N = 11;
+    sigma = fmaxf(sigma, 1e-6f);
+    float w[N];
+    {
+        const float dx = d.dx;
+        const float xmin = xoff - 0.5f * (float)N * dx;
+        float prev = gauss_cdf(xmin, xoff, sigma);
+        for (int i = 0; i < N; ++i) {
+            float cur = gauss_cdf(xmin + (float)(i + 1) * dx, xoff, sigma);
+            w[i] = cur - prev;
+            prev = cur;
+        }
+        float s = 0.0f;
+        for (int i = 0; i < N; ++i) s += w[i];
+        if (s > 1e-10f) {
+            for (int i = 0; i < N; ++i) w[i] /= s;
+        } else {
+            for (int i = 0; i < N; ++i) w[i] = (i == N / 2) ? 1.0f : 0.0f;
+        }
+    }
+    float s = 0.0f;
+    for (int i = 0; i < N; ++i) { w[i] = fmaxf(0.0f, w[i]); s += w[i]; }
+    if (s < 1e-12f) {
+        for (int i = 0; i < N; ++i) w[i] = 0.0f;
+        w[N / 2] = 1.0f;
+    } else {
+        for (int i = 0; i < N; ++i) w[i] /= s;
+    }
+    const int ixs = src % d.Nx, izs = src / d.Nx, tz = izs + 1;
+    float dropped = 0.0f;
+    for (int i = 0; i < N; ++i) {
+        const float wf = w[i];
+        if (wf <= 0.0f) continue;
+        const int off = i - N / 2;
+        const int ixt = ixs + off;
+        if (ixt < 0 || ixt >= d.Nx || tz >= d.Nz) { boundary_w += weight * wf; continue; }
+        const int ecell = ixt + izs * d.Nx;
+        // the bucket of another column exists only if that cell is listed
+        // in the same pass (k1k6_pipeline.cu:800-847 maps one list at a time)
+        if (ecell != src && d.cls[ecell] != my_cls) { dropped += weight * wf; continue; }
+        const int xt = off < 0 ? Lay::NX - 1 : (off > 0 ? 0 : Lay::NX / 2);
+        dropped += emit_component<Lay, BUCKET>(d, par, ecell, FACE_ZP, ecell + d.Nx, theta, E, weight * wf, xt, 0,
+                                               eshift);
+    }
+    return dropped;
+}
+
+// Component stays in its cell: re-bin angle/energy, spread over the x
+// sub-bins, send Gaussian tails past the cell edges to the lateral
+// neighbours, fold the re-binning energy error into the deposit
+// (k2_coarsetransport.cu:460-690, k3_finetransport.cu:504-747).
+template <class Lay, bool BUCKET>
+__device__ void emit_stay(const Dev& d, int par, bool k3, int cell, float theta_new, float E_new, float w_new,
+                          float x_new, float z_new, float sig_sub, float sig_cell, Tally& t) {
+    const float dx = d.dx, dz = d.dz;
+    const float tmin = d.th[0], tmax = d.th[d.N_theta];
+    const float dth = (tmax - tmin) / (float)d.N_theta;
+    int tbn = (int)((theta_new - tmin) / dth);
+    tbn = (int)fmaxf(0.0f, fminf((float)tbn, (float)(d.N_theta - 1)));
+    const EParts ep = bin_energy(d, E_new, w_new);
+    float w[Lay::NX];
+    {
+        const float sg = fmaxf(sig_sub, 1e-6f);
+        const float dxs = dx / (float)Lay::NX;
+        const float xmin = -dx * 0.5f;
+        float prev = gauss_cdf(xmin, x_new, sg);
+        for (int i = 0; i < Lay::NX; ++i) {
+            float cur = gauss_cdf(xmin + (float)(i + 1) * dxs, x_new, sg);
+            w[i] = cur - prev;
+            prev = cur;
+        }
+        float s = 0.0f;
+        for (int i = 0; i < Lay::NX; ++i) s += w[i];
+        if (s > 1e-10f) {
+            for (int i = 0; i < Lay::NX; ++i) w[i] /= s;
+        } else {
+            for (int i = 0; i < Lay::NX; ++i) w[i] = (i == Lay::NX / 2) ? 1.0f : 0.0f;
+        }
+    }
+    const int ix = cell % d.Nx;
+    const int zst = sub_bin(z_new, dz, Lay::NZ);
+    const float lb = -dx * 0.5f, rb = dx * 0.5f;
+    const float win = gauss_cdf(rb, x_new, sig_cell) - gauss_cdf(lb, x_new, sig_cell);
+    const float wcf = fminf(1.0f, fmaxf(0.0f, win));
+    float wsum = 0.0f;
+    for (int i = 0; i < Lay::NX; ++i) { w[i] = fmaxf(0.0f, w[i]); wsum += w[i]; }
+    if (wsum < 1e-12f) {
+        for (int i = 0; i < Lay::NX; ++i) w[i] = 0.0f;
+        w[Lay::NX / 2] = 1.0f;
+        wsum = 1.0f;
+    }
+    const int outp = par ^ 1;
+    uint32_t* ids = d.bid[outp] + (size_t)cell * kKb;
+    float* vals = d.val[outp] + (size_t)cell * kKb * Lay::L;
+    float E_emit = ep.Erep;
+    for (int ei = 0; ei < ep.n; ++ei) {
+        const int Eb = ep.bin[ei];
+        const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
+        uint32_t sel;
+        const int os = claim_slot(ids, want, sel);
+        const float wpart = d.esplit ? w_new * ep.frac[ei] : w_new;
+        if (os < 0) {
+            t.drop_w += (double)wpart;
+            t.drop_e += (double)(E_new * wpart);
+            if (!d.esplit) return;
+            continue;
+        }
+        d.occ[outp][cell] = 1;
+        int tbe = tbn, Ebe = Eb;
+        if (sel != want) {
+            const int t0 = (int)(sel & 0xFFFu) * Lay::NT, e0 = (int)((sel >> 12) & 0xFFFu) * Lay::NE;
+            tbe = max(t0, min(tbe, t0 + Lay::NT - 1));
+            Ebe = max(e0, min(Ebe, e0 + Lay::NE - 1));
+        }
+        if (!d.esplit) E_emit = e_center(d, Ebe);
+        else if (Ebe != Eb) t.edep += (double)((e_center(d, Eb) - e_center(d, Ebe)) * wpart * wcf);
+        const int tl = tbe % Lay::NT, El = Ebe % Lay::NE;
+        float* vs = vals + (size_t)os * Lay::L;
+        for (int xs = 0; xs < Lay::NX; ++xs) {
+            const float wf = (w[xs] / wsum) * wcf;
+            if (wf <= 0.0f) continue;
+            atomicAdd(vs + Lay::enc(tl, El, xs, zst), wpart * wf);
+        }
+    }
+    float wl = 0.0f, wr = 0.0f;
+    if (wcf < 1.0f - 1e-6f) {
+        const float wlr = fmaxf(0.0f, gauss_cdf(lb, x_new, sig_cell));
+        const float wrr = fmaxf(0.0f, 1.0f - gauss_cdf(rb, x_new, sig_cell));
+        const float tt = fmaxf(0.0f, 1.0f - wcf);
+        const float ts = wlr + wrr;
+        if (tt > 0.0f && ts > 1e-12f) {
+            const float sc = tt / ts;
+            wl = wlr * sc;
+            wr = wrr * sc;
+        }
+        if (wl > 0.0f) {
+            const float ws = w_new * wl;
+            if (ix > 0) {
+                const float dr = emit_component<Lay, BUCKET>(d, par, cell, FACE_XM, cell - 1, theta_new, E_new, ws,
+                                                             Lay::NX - 1, zst, t.edep);
+                if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
+            } else {
+                t.w_bnd += ws;
+                t.e_bnd += (double)(E_new * ws);
+            }
+        }
+        if (wr > 0.0f) {
+            const float ws = w_new * wr;
+            if (ix < d.Nx - 1) {
+                const float dr = emit_component<Lay, BUCKET>(d, par, cell, FACE_XP, cell + 1, theta_new, E_new, ws,
+                                                             0, zst, t.edep);
+                if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
+            } else {
+                t.w_bnd += ws;
+                t.e_bnd += (double)(E_new * ws);
+            }
+        }
+    }
+    if (k3 || d.esplit) {
+        float rf = wcf;
+        if (ix > 0) rf += wl;
+        if (ix < d.Nx - 1) rf += wr;
+        rf = fminf(1.0f, fmaxf(0.0f, rf));
+        const float rw = w_new * rf;
+        if (rw > 0.0f) t.edep += (double)((E_new - E_emit) * rw);
+    }
+}
+
+// Component crosses `face` (k2_coarsetransport.cu:363-459, k3_finetransport.cu:380-503).
+template <class Lay, bool BUCKET>
+__device__ void emit_cross(const Dev& d, int par, bool k3, int cell, int my_cls, int face, float theta_new, float E_new,
+                           float w_new, float x_new, float z_new, float sig_tr, Tally& t) {
+    const int ix = cell % d.Nx, iz = cell / d.Nx;
+    int nb = -1;
+    if (face == FACE_ZP) nb = iz + 1 < d.Nz ? cell + d.Nx : -1;
+    else if (face == FACE_ZM) nb = iz > 0 ? cell - d.Nx : -1;
+    else if (face == FACE_XP) nb = ix + 1 < d.Nx ? cell + 1 : -1;
+    else nb = ix > 0 ? cell - 1 : -1;
+    if (nb < 0) {
+        t.w_bnd += w_new;
+        t.e_bnd += (double)(E_new * w_new);
+        return;
+    }
+    const float E_emit = bin_energy(d, E_new, w_new).Erep;
+    const bool fold = k3 || d.esplit;
+    if (face == FACE_ZP) {
+        float lbw = 0.0f;
+        const float dr = emit_forward<Lay, BUCKET>(d, par, cell, my_cls, theta_new, E_new, w_new, x_new, sig_tr, lbw,
+                                                   t.edep);
+        if (lbw > 0.0f) { t.w_bnd += lbw; t.e_bnd += (double)(E_new * lbw); }
+        if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
+        if (fold) {
+            const float tw = fmaxf(0.0f, w_new - lbw - dr);
+            if (tw > 0.0f) t.edep += (double)((E_new - E_emit) * tw);
+        }
+        return;
+    }
+    const float dx = d.dx, dz = d.dz;
+    const float xo = face == FACE_XP ? -dx * 0.5f : (face == FACE_XM ? dx * 0.5f : x_new);
+    const int xsn = sub_bin(xo, dx, Lay::NX);
+    const int zsn = face == FACE_ZM ? Lay::NZ - 1 : sub_bin(z_new, dz, Lay::NZ);
+    const float dr = emit_component<Lay, BUCKET>(d, par, cell, face, nb, theta_new, E_new, w_new, xsn, zsn, t.edep);
+    if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
+    if (fold) {
+        const float tw = fmaxf(0.0f, w_new - dr);
+        if (tw > 0.0f) t.edep += (double)((E_new - E_emit) * tw);
+    }
+}
+
+__device__ __forceinline__ int exit_face(float x, float z, float dx, float dz) {
+    const float eps = 0.001f, hz = dz * 0.5f, hx = dx * 0.5f;
+    if (z >= hz - eps) return FACE_ZP;
+    if (z <= -hz + eps) return FACE_ZM;
+    if (x >= hx - eps) return FACE_XP;
+    if (x <= -hx + eps) return FACE_XM;
+    return -1;
+}
+
+// One component of a listed cell.
+template <class Lay, bool BUCKET>
+__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t bid, int sslot, int lidx, float w,
+                              unsigned salt, Tally& t) {
+    const float dx = d.dx, dz = d.dz;
+    int tl, El, xs, zs;
+    Lay::dec(lidx, tl, El, xs, zs);
+    int tbin = (int)(bid & 0xFFFu) * Lay::NT + tl;
+    int Ebin = (int)((bid >> 12) & 0xFFFu) * Lay::NE + El;
+    if (k3) {
+        tbin = max(0, min(tbin, d.N_theta - 1));
+        Ebin = max(0, min(Ebin, d.N_E - 1));
+    }
+    const float E = d.Ee[Ebin] + 1.0f * ((d.Ee[Ebin + 1] - d.Ee[Ebin]) * 0.5f);
+    t.Win += (double)w;
+    t.Ein += (double)w * (double)E;
+    if (w < (k3 ? d.prune_fine : d.prune_coarse)) {   // prune (k3:175-184, k2:172-177)
+        t.drop_w += (double)w;
+        t.drop_e += (double)(E * w);
+        return;
+    }
+    const float tmin = d.th[0], tmax = d.th[d.N_theta];
+    const float dth = (tmax - tmin) / (float)d.N_theta;
+    const float theta = k3 ? d.th[tbin] + 0.5f * dth : tmin + ((float)tbin + 0.5f) * dth;
+    if (E <= 0.1f) {
+        t.w_cut += w;
+        t.e_cut += (double)(E * w);
+        return;
+    }
+    const float xc = sub_offset(xs, Lay::NX, dx), zc = sub_offset(zs, Lay::NZ, dz);
+    const float hx = dx * 0.5f, hz = dz * 0.5f;
+    const int iz = cell / d.Nx;
+    float step, dE, w_new, w_rem = 0.0f, E_rem = 0.0f, sig_th, sig_x, E_new, edep;
+    unsigned ts;
+    if (k3) {
+        // K3_FineTransport body, k3_finetransport.cu:226-366
+        const float mu0 = cosf(theta), eta0 = sinf(theta);
+        const float szp = (mu0 > 0) ? (hz - zc) / mu0 : 1e30f;
+        const float szm = (mu0 < 0) ? (-hz - zc) / mu0 : 1e30f;
+        const float sxp = (eta0 > 0) ? (hx - xc) / eta0 : 1e30f;
+        const float sxm = (eta0 < 0) ? (-hx - xc) / eta0 : 1e30f;
+        const float sb = fmaxf(fminf(fminf(szp, szm), fminf(sxp, sxm)), 0.0f);
+        step = fminf(fine_step_limit(d, E), sb * 1.001f);
+        const float mean_dE = lut_energy_loss(d, E, step);
+        if (d.straggle) {
+            unsigned seed = ((unsigned)(cell * 7 + sslot * 13 + lidx * 17) ^ 0xDEECE66Du) ^ salt;
+            const float sE = straggling_sigma(E, step, 1.0f);
+            dE = sE <= 0.0f ? mean_dE : fmaxf(mean_dE + normal_draw(seed) * sE, 0.0f);
+        } else {
+            dE = mean_dE;
+        }
+        dE = fminf(dE, E);
+        E_new = E - dE;
+        edep = dE * w;
+        w_new = w;
+        if (d.nuclear) {
+            const float surv = expf(-nuclear_xs(E) * step);
+            w_new = w * surv;
+            w_rem = w - w_new;
+            E_rem = w_rem * E;
+        }
+        const float sm = fmaxf(step, 0.0f);
+        const float Ap = (d.feA && iz < d.Nz) ? d.feA[iz] : 0.0f;
+        const float Bp = (d.feB && iz < d.Nz) ? d.feB[iz] : 0.0f;
+        const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm);
+        sig_th = sqrtf(fmaxf(T * sm, 0.0f));
+        const float dC = fmaxf(2.0f * Bp * sm + Ap * sm * sm + T * sm * sm * sm / 3.0f, 0.0f);
+        sig_x = fmaxf(sqrtf(dC), 0.01f);
+        const unsigned ps = (unsigned)fminf((float)iz * dz * 1000.0f, 4294967295.0f);
+        ts = ((unsigned)(cell + 1) * 2654435761u) ^ ((unsigned)(sslot + 1) * 2246822519u) ^
+             ((unsigned)(lidx + 1) * 3266489917u) ^ (unsigned)(Ebin + 17) ^ (ps * 747796405u) ^ salt;
+    } else {
+        // K2_CoarseTransport body, k2_coarsetransport.cu:186-350
+        float lim = fminf(d.step_coarse, fminf(dx, dz));
+        float rs = lim;
+        bool split = false;
+        if (E > d.E_fine_on + 1e-6f) {
+            const float rtf = lut_range(d, E) - lut_range(d, fmaxf(d.E_fine_on, d.lutEmin));
+            if (rtf > 0.0f && rtf < rs) { rs = rtf; lim = rs; split = true; }
+        }
+        step = lim;
+        dE = fminf(lut_energy_loss(d, E, rs), E);
+        E_new = E - dE;
+        edep = dE * w;
+        const float surv = expf(-nuclear_xs(E) * rs);
+        w_new = w * surv;
+        w_rem = w - w_new;
+        E_rem = w_rem * E;
+        if (split && E_new > d.E_fine_on) {
+            const float ex = E_new - d.E_fine_on;
+            if (ex > 0.0f && w_new > 0.0f) edep += ex * w_new;
+            E_new = d.E_fine_on;
+        }
+        const float p0 = fmaxf(0.0f, (float)iz * dz + (zc + 0.5f * dz));
+        const float sm = fmaxf(rs, 0.0f);
+        const float s0 = p0 > 0.0f ? highland(E, p0) : 0.0f;
+        const float A0 = s0 * s0;
+        const float B0 = 0.5f * A0 * p0;
+        const float C0 = d.sx0 * d.sx0 + (A0 * p0 * p0) / 3.0f;
+        const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm);
+        const float A1 = fmaxf(A0 + T * sm, 0.0f);
+        const float C1 = fmaxf(C0 + 2.0f * B0 * sm + A0 * sm * sm + (1.0f / 3.0f) * T * sm * sm * sm, 0.0f);
+        sig_th = sqrtf(fmaxf(A1 - A0, 0.0f));
+        const float dC = fmaxf(C1 - C0, 0.0f);
+        const float uf = fminf(0.35f, 0.04f + 0.003f * p0);
+        sig_x = fmaxf(sqrtf(fmaxf(dC + uf * C0, 0.0f)), 0.01f);
+        const unsigned ps = (unsigned)fminf(p0 * 1000.0f, 4294967295.0f);
+        ts = ((unsigned)(cell + 1) * 2654435761u) ^ ((unsigned)(sslot + 1) * 2246822519u) ^
+             ((unsigned)(lidx + 1) * 3266489917u) ^ (unsigned)(Ebin + 17) ^ (ps * 747796405u) ^ salt;
+    }
+    const float scat = sig_th <= 0.0f ? 0.0f : normal_draw(ts) * sig_th;
+    const float theta_new = fmaxf(d.th[0], fminf(theta + scat, d.th[d.N_theta]));
+    float x_new = xc + sinf(theta_new) * step;
+    float z_new = zc + cosf(theta_new) * step;
+    const int face = exit_face(x_new, z_new, dx, dz);
+    x_new = fmaxf(-hx, fminf(x_new, hx));
+    z_new = fmaxf(-hz, fminf(z_new, hz));
+    t.edep += (double)edep;
+    t.w_nuc += w_rem;
+    t.e_nuc += (double)E_rem;
+    if (E_new <= 0.1f || ((d.esplit || d.floor_cutoff) && E_new <= e_center(d, 0))) {
+        t.w_cut += w_new;
+        t.e_cut += (double)(E_new * w_new);
+        return;
+    }
+    const int my_cls = k3 ? 2 : 1;
+    if (face >= 0) {
+        const float sig_tr = k3 ? 0.001f : fmaxf(sinf(fminf(sig_th, 1.57f)) * fmaxf(step, 0.0f) / 1.7320508f, 0.01f);
+        emit_cross<Lay, BUCKET>(d, par, k3, cell, my_cls, face, theta_new, E_new, w_new, x_new, z_new, sig_tr, t);
+    } else {
+        emit_stay<Lay, BUCKET>(d, par, k3, cell, theta_new, E_new, w_new, x_new, z_new, k3 ? 0.001f : sig_x, sig_x, t);
+    }
+}
+
+}  // namespace sm2d

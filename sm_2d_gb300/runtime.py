@@ -1,0 +1,431 @@
+"""Host-side mirror of the reference transport interface over the C ABI.
+
+``Transport`` corresponds to one call of the reference wrapper
+``sm_2d::run_k1k6_pipeline_transport(x0, z0, theta0, E0, W, sigma_x,
+sigma_theta, sigma_E, n_samples, seed, Nx, Nz, dx, dz, x_min, z_min, ...,
+edep)`` (src/include/cuda/gpu_transport_wrapper.hpp:78-90) split into its
+steps: allocate (sm2d_create), inject, iterate, read the dose.  Grids are
+built by the library's own host tables (EnergyGrid / AngularGrid
+semantics of src/core/grids.cpp).  Everything runs through libsm2d.so; there
+is no Python or CPU fallback: a missing library or GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import build as _build
+
+KB = 32
+EMPTY = 0xFFFFFFFF
+_LIB = None
+_LOCK = threading.Lock()
+
+
+class Sm2dError(RuntimeError):
+    pass
+
+
+class Problem(C.Structure):
+    _fields_ = [
+        ("Nx", C.c_int), ("Nz", C.c_int), ("dx", C.c_float), ("dz", C.c_float),
+        ("x_min", C.c_float), ("z_min", C.c_float),
+        ("N_theta", C.c_int), ("theta_edges", C.c_void_p),
+        ("N_E", C.c_int), ("E_edges", C.c_void_p), ("E_min", C.c_float), ("E_max", C.c_float),
+        ("nt_local", C.c_int), ("ne_local", C.c_int), ("nx_sub", C.c_int), ("nz_sub", C.c_int),
+        ("E_fine_on", C.c_float), ("E_fine_off", C.c_float), ("weight_active_min", C.c_float),
+        ("step_coarse", C.c_float), ("sigma_x_initial", C.c_float), ("E0", C.c_float),
+        ("enable_straggling", C.c_int), ("enable_nuclear", C.c_int),
+        ("seed_slot_mode", C.c_int), ("energy_split", C.c_int), ("use_buckets", C.c_int),
+        ("max_iterations", C.c_int),
+        ("prune_coarse", C.c_float), ("prune_fine", C.c_float), ("split_min_weight", C.c_float),
+        ("stop_weight_fraction", C.c_float), ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
+    ]
+
+
+class Beam(C.Structure):
+    _fields_ = [("x0", C.c_float), ("z0", C.c_float), ("theta0", C.c_float), ("E0", C.c_float),
+                ("W_total", C.c_float), ("sigma_x", C.c_float), ("sigma_theta", C.c_float),
+                ("sigma_E", C.c_float), ("n_samples", C.c_int), ("seed", C.c_uint)]
+
+
+class Audit(C.Structure):
+    _fields_ = [
+        ("W_error", C.c_float), ("W_pass", C.c_int), ("E_error", C.c_float), ("E_pass", C.c_int),
+        ("W_in_total", C.c_float), ("W_out_total", C.c_float), ("W_cutoff_total", C.c_float),
+        ("W_nuclear_total", C.c_float), ("W_boundary_total", C.c_float),
+        ("W_source_out_of_grid_total", C.c_float), ("W_source_slot_drop_total", C.c_float),
+        ("W_transport_drop_total", C.c_float),
+        ("E_in_total", C.c_double), ("E_out_total", C.c_double), ("E_dep_total", C.c_double),
+        ("E_cutoff_total", C.c_double), ("E_nuclear_total", C.c_double),
+        ("E_boundary_total", C.c_double), ("E_source_out_of_grid_total", C.c_double),
+        ("E_source_slot_drop_total", C.c_double), ("E_transport_drop_total", C.c_double),
+        ("processed_cells", C.c_int),
+    ]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+SCALAR_KEYS = ["transport_dropped_weight", "transport_dropped_energy", "audit_residual_energy",
+               "source_injected_weight", "source_injected_energy", "source_out_of_grid_weight",
+               "source_out_of_grid_energy", "source_slot_dropped_weight", "source_slot_dropped_energy",
+               "source_representation_loss_energy", "iterations", "cell_steps", "slots_in", "slots_out"]
+
+
+def lib(build_if_needed: bool = True):
+    """Load libsm2d.so (building it in-tree when sources are newer)."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB
+        if build_if_needed and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(path):
+            raise Sm2dError(f"CUDA library {path} is missing; run sm_2d_gb300.build")
+        L = C.CDLL(path)
+        P, I, F, D = C.c_void_p, C.c_int, C.c_float, C.c_double
+        L.sm2d_last_error.restype = C.c_char_p
+        L.sm2d_bucket_bytes.restype = C.c_size_t
+        L.sm2d_bucket_bytes.argtypes = [I]
+        L.sm2d_create.argtypes = [C.POINTER(Problem), C.POINTER(P)]
+        for n in ["sm2d_destroy", "sm2d_local_bins"]:
+            getattr(L, n).argtypes = [P]
+        L.sm2d_inject.argtypes = [P, C.POINTER(Beam)]
+        L.sm2d_set_psi_in.argtypes = [P, P, P]
+        L.sm2d_get_psi_in.argtypes = [P, P, P]
+        L.sm2d_step.argtypes = [P, C.POINTER(I), C.POINTER(I)]
+        L.sm2d_run.argtypes = [P, I, C.POINTER(I)]
+        L.sm2d_run_timed.argtypes = [P, I, C.POINTER(I), C.POINTER(F)]
+        L.sm2d_get_mask.argtypes = [P, P]
+        L.sm2d_get_lists.argtypes = [P, P, C.POINTER(I), P, C.POINTER(I)]
+        L.sm2d_get_tallies.argtypes = [P] * 8
+        L.sm2d_get_audit.argtypes = [P, C.POINTER(Audit)]
+        L.sm2d_get_audit_history.argtypes = [P, P, I, C.POINTER(I)]
+        L.sm2d_get_scalars.argtypes = [P, P]
+        L.sm2d_get_fe.argtypes = [P, P, P, P]
+        L.sm2d_get_dose.argtypes = [P, P]
+        L.sm2d_get_step_timing.argtypes = [P, P]
+        L.sm2d_stream.restype = P
+        L.sm2d_stream.argtypes = [P]
+        L.sm2d_reset.argtypes = [P]
+        L.sm2d_inject_async.argtypes = [P, C.POINTER(Beam)]
+        L.sm2d_run_async.argtypes = [P, I]
+        L.sm2d_dose_async.argtypes = [P, P]
+        L.sm2d_run_profiled.argtypes = [P, I, C.POINTER(I), P, C.POINTER(I)]
+        L.sm2d_energy_grid_log.argtypes = [F, F, I, P, P]
+        L.sm2d_energy_grid_piecewise.argtypes = [I, P, P, P]
+        L.sm2d_angular_grid.argtypes = [F, F, I, P, P]
+        L.sm2d_range_lut.argtypes = [I] + [P] * 6
+        L.sm2d_fermi_eyges.argtypes = [F, I, F, F, P, P, P]
+        L.sm2d_k1_active_mask.argtypes = [P, P, P, P, I, I, I, I, I, F, P]
+        L.sm2d_compact_lists.argtypes = [P, P, P, I, I, I, P, P, P, P, P]
+        L.sm2d_k4_bucket_transfer.argtypes = [P, P, P, P, I, I, I, I, I, I, P, I, I, P, P]
+        L.sm2d_k5_conservation_audit.argtypes = ([P] * 18 + [F, F, D, D, F, D, I, P, I, I, I, I, P, I, P])
+        _LIB = L
+        return L
+
+
+def _p(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+def check(rc: int):
+    if rc != 0:
+        raise Sm2dError(f"sm2d error {rc}: {lib().sm2d_last_error().decode()}")
+
+
+# ---------------------------------------------------------------- grids
+def energy_grid_log(E_min, E_max, N):
+    e = np.zeros(N + 1, np.float32)
+    r = np.zeros(N, np.float32)
+    check(lib().sm2d_energy_grid_log(E_min, E_max, N, _p(e), _p(r)))
+    return e, r
+
+
+def energy_grid_piecewise(groups):
+    g = np.asarray(groups, np.float32).reshape(-1)
+    n = lib().sm2d_energy_grid_piecewise(len(groups), _p(g), None, None)
+    if n < 0:
+        check(n)
+    e = np.zeros(n + 1, np.float32)
+    r = np.zeros(n, np.float32)
+    lib().sm2d_energy_grid_piecewise(len(groups), _p(g), _p(e), _p(r))
+    return e, r
+
+
+def angular_grid(lo, hi, N):
+    e = np.zeros(N + 1, np.float32)
+    r = np.zeros(N, np.float32)
+    check(lib().sm2d_angular_grid(lo, hi, N, _p(e), _p(r)))
+    return e, r
+
+
+def range_lut(rep):
+    rep = np.ascontiguousarray(rep, np.float32)
+    out = [np.zeros(rep.size, np.float32) for _ in range(5)]
+    check(lib().sm2d_range_lut(rep.size, _p(rep), *[_p(a) for a in out]))
+    return dict(zip(["R", "S", "logE", "logR", "logS"], out))
+
+
+def fermi_eyges(E0, Nz, dz, sigma_x0):
+    A, B, S = (np.zeros(Nz, np.float32) for _ in range(3))
+    check(lib().sm2d_fermi_eyges(E0, Nz, dz, sigma_x0, _p(A), _p(B), _p(S)))
+    return A, B, S
+
+
+DEFAULT_ENERGY_GROUPS = [(0.1, 2.0, 0.1), (2.0, 20.0, 0.2), (20.0, 100.0, 0.25), (100.0, 250.0, 0.25)]
+LAYOUT_REF = dict(nt_local=4, ne_local=2, nx_sub=8, nz_sub=4)      # 256 local bins
+LAYOUT_B128 = dict(nt_local=8, ne_local=4, nx_sub=4, nz_sub=1)     # 128 local bins
+
+
+@dataclass
+class Config:
+    """Spatial grid, phase-space grids and transport controls of one problem."""
+    Nx: int
+    Nz: int
+    dx: float
+    dz: float
+    theta_edges: np.ndarray
+    E_edges: np.ndarray
+    E_min: float
+    E_max: float
+    x_min: float = 0.0
+    z_min: float = 0.0
+    layout: dict = field(default_factory=lambda: dict(LAYOUT_REF))
+    E_fine_on: float = 10.0
+    E_fine_off: float = 11.0
+    weight_active_min: float = 1e-12
+    step_coarse: float = 5.0
+    sigma_x_initial: float = 0.0
+    E0: float = 0.0
+    enable_straggling: int = 1
+    enable_nuclear: int = 1
+    seed_slot_mode: int = 0
+    energy_split: int = 0
+    use_buckets: int = 0
+    max_iterations: int = 4096
+    prune_coarse: float = 0.0
+    prune_fine: float = 0.0
+    split_min_weight: float = 0.0
+    stop_weight_fraction: float = 0.0
+    floor_cutoff: int = 0
+    seed_iteration_salt: int = 0
+
+    def production(self):
+        """Options of a production run: deterministic rank-ordered seeds salted
+        per iteration, floor cutoff, and the stop at 1e-6 of the injected weight
+        (the reference instead relies on max_iterations)."""
+        self.seed_slot_mode = 1
+        self.seed_iteration_salt = 1
+        self.floor_cutoff = 1
+        self.stop_weight_fraction = 1e-6
+        if self.energy_split:
+            self.split_min_weight = 1e-7
+        return self
+
+    def oracle_config(self):
+        """The same problem as a CPU-oracle configuration dict."""
+        return dict(Nx=self.Nx, Nz=self.Nz, dx=self.dx, dz=self.dz, x_min=self.x_min, z_min=self.z_min,
+                    E_fine_on=self.E_fine_on, E_fine_off=self.E_fine_off,
+                    weight_active_min=self.weight_active_min, step_coarse=self.step_coarse,
+                    sigma_x_initial=self.sigma_x_initial, E0=self.E0,
+                    enable_straggling=self.enable_straggling, enable_nuclear=self.enable_nuclear,
+                    seed_slot_mode=self.seed_slot_mode, energy_split=self.energy_split,
+                    grid_E_min=self.E_min, grid_E_max=self.E_max, prune_coarse=self.prune_coarse,
+                    prune_fine=self.prune_fine, split_min_weight=self.split_min_weight,
+                    stop_weight_fraction=self.stop_weight_fraction, floor_cutoff=self.floor_cutoff,
+                    seed_iteration_salt=self.seed_iteration_salt, **self.layout)
+
+    @staticmethod
+    def reference_runner(Nx, Nz, dx, dz, N_theta=36, E_fine_on=10.0, E_fine_off=11.0, **kw):
+        """The grids GPUTransportRunner::run builds (gpu_transport_runner.cpp:85-98, 172):
+        theta on +-0.35 rad, the default piecewise energy grid, x_min = -Nx*dx/2."""
+        th, _ = angular_grid(-0.35, 0.35, N_theta)
+        e, _ = energy_grid_piecewise(DEFAULT_ENERGY_GROUPS)
+        return Config(Nx=Nx, Nz=Nz, dx=dx, dz=dz, theta_edges=th, E_edges=e, E_min=0.1, E_max=250.0,
+                      x_min=-(Nx * dx) / 2.0, z_min=0.0, E_fine_on=E_fine_on, E_fine_off=E_fine_off, **kw)
+
+    @staticmethod
+    def log_grid(Nx, Nz, dx, dz, N_E=256, E_min=0.1, E_max=250.0, N_theta=512, theta_max=np.pi / 2,
+                 layout=None, **kw):
+        """Log-spaced energy grid and a uniform +-theta_max angular grid (EnergyGrid(E_min,E_max,N))."""
+        th, _ = angular_grid(-theta_max, theta_max, N_theta)
+        e, _ = energy_grid_log(E_min, E_max, N_E)
+        return Config(Nx=Nx, Nz=Nz, dx=dx, dz=dz, theta_edges=th, E_edges=e, E_min=E_min, E_max=E_max,
+                      x_min=-(Nx * dx) / 2.0, layout=dict(layout or LAYOUT_B128), **kw)
+
+
+class Transport:
+    """One transport problem resident on the GPU (handle over the C ABI)."""
+
+    def __init__(self, cfg: Config):
+        self.cfg = cfg
+        self._th = np.ascontiguousarray(cfg.theta_edges, np.float32)
+        self._E = np.ascontiguousarray(cfg.E_edges, np.float32)
+        p = Problem(Nx=cfg.Nx, Nz=cfg.Nz, dx=cfg.dx, dz=cfg.dz, x_min=cfg.x_min, z_min=cfg.z_min,
+                    N_theta=self._th.size - 1, theta_edges=self._th.ctypes.data,
+                    N_E=self._E.size - 1, E_edges=self._E.ctypes.data, E_min=cfg.E_min, E_max=cfg.E_max,
+                    E_fine_on=cfg.E_fine_on, E_fine_off=cfg.E_fine_off,
+                    weight_active_min=cfg.weight_active_min, step_coarse=cfg.step_coarse,
+                    sigma_x_initial=cfg.sigma_x_initial, E0=cfg.E0,
+                    enable_straggling=cfg.enable_straggling, enable_nuclear=cfg.enable_nuclear,
+                    seed_slot_mode=cfg.seed_slot_mode, energy_split=cfg.energy_split,
+                    use_buckets=cfg.use_buckets, max_iterations=cfg.max_iterations,
+                    prune_coarse=cfg.prune_coarse, prune_fine=cfg.prune_fine,
+                    split_min_weight=cfg.split_min_weight, stop_weight_fraction=cfg.stop_weight_fraction,
+                    floor_cutoff=cfg.floor_cutoff, seed_iteration_salt=cfg.seed_iteration_salt, **cfg.layout)
+        h = C.c_void_p()
+        self._lib = lib()
+        check(self._lib.sm2d_create(C.byref(p), C.byref(h)))
+        self.h = h
+        self.Nc = cfg.Nx * cfg.Nz
+        self.L = self._lib.sm2d_local_bins(h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.sm2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- source and phase space
+    def inject(self, x0=0.0, z0=0.0, theta0=0.0, E0=150.0, W=1.0, sigma_x=0.0, sigma_theta=0.0,
+               sigma_E=0.0, n_samples=1, seed=42):
+        b = Beam(x0, z0, theta0, E0, W, sigma_x, sigma_theta, sigma_E, int(n_samples), int(seed) & 0xFFFFFFFF)
+        check(self._lib.sm2d_inject(self.h, C.byref(b)))
+
+    def set_psi_in(self, bid, val):
+        bid = np.ascontiguousarray(bid, np.uint32)
+        val = np.ascontiguousarray(val, np.float32)
+        if bid.size != self.Nc * KB or val.size != self.Nc * KB * self.L:
+            raise ValueError("phase-space arrays have the wrong size")
+        check(self._lib.sm2d_set_psi_in(self.h, _p(bid), _p(val)))
+
+    def psi_in(self, values=True):
+        bid = np.zeros(self.Nc * KB, np.uint32)
+        val = np.zeros(self.Nc * KB * self.L, np.float32) if values else None
+        check(self._lib.sm2d_get_psi_in(self.h, _p(bid), _p(val) if values else None))
+        return bid, val
+
+    # -- iteration
+    def step(self):
+        na, nc = C.c_int(), C.c_int()
+        check(self._lib.sm2d_step(self.h, C.byref(na), C.byref(nc)))
+        return na.value, nc.value
+
+    def run(self, max_iterations=100000):
+        n = C.c_int()
+        check(self._lib.sm2d_run(self.h, int(max_iterations), C.byref(n)))
+        return n.value
+
+    def run_timed(self, max_iterations=100000):
+        n, ms = C.c_int(), C.c_float()
+        check(self._lib.sm2d_run_timed(self.h, int(max_iterations), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    # -- results
+    def mask(self):
+        m = np.zeros(self.Nc, np.uint8)
+        check(self._lib.sm2d_get_mask(self.h, _p(m)))
+        return m
+
+    def lists(self):
+        a = np.zeros(self.Nc, np.uint32)
+        c = np.zeros(self.Nc, np.uint32)
+        na, nc = C.c_int(), C.c_int()
+        check(self._lib.sm2d_get_lists(self.h, _p(a), C.byref(na), _p(c), C.byref(nc)))
+        return a[: na.value].copy(), c[: nc.value].copy()
+
+    def tallies(self):
+        n = self.Nc
+        out = dict(edep=np.zeros(n), w_cut=np.zeros(n, np.float32), e_cut=np.zeros(n),
+                   w_nuc=np.zeros(n, np.float32), e_nuc=np.zeros(n),
+                   w_bnd=np.zeros(n, np.float32), e_bnd=np.zeros(n))
+        check(self._lib.sm2d_get_tallies(self.h, *[_p(out[k]) for k in
+                                                   ["edep", "w_cut", "e_cut", "w_nuc", "e_nuc", "w_bnd", "e_bnd"]]))
+        return out
+
+    def audit(self):
+        a = Audit()
+        check(self._lib.sm2d_get_audit(self.h, C.byref(a)))
+        return a.as_dict()
+
+    def audit_history(self, n_max=100000):
+        arr = (Audit * n_max)()
+        n = C.c_int()
+        check(self._lib.sm2d_get_audit_history(self.h, C.cast(arr, C.c_void_p), n_max, C.byref(n)))
+        return [arr[i].as_dict() for i in range(n.value)]
+
+    def scalars(self):
+        s = np.zeros(14)
+        check(self._lib.sm2d_get_scalars(self.h, _p(s)))
+        return dict(zip(SCALAR_KEYS, s.tolist()))
+
+    def fe(self):
+        A, B, S = (np.zeros(self.cfg.Nz, np.float32) for _ in range(3))
+        check(self._lib.sm2d_get_fe(self.h, _p(A), _p(B), _p(S)))
+        return A, B, S
+
+    def dose(self):
+        """EdepC after the lateral MCS post-convolution, shape [Nz, Nx]."""
+        d = np.zeros(self.Nc)
+        check(self._lib.sm2d_get_dose(self.h, _p(d)))
+        return d.reshape(self.cfg.Nz, self.cfg.Nx)
+
+    # -- asynchronous spot pipeline
+    def reset(self):
+        check(self._lib.sm2d_reset(self.h))
+
+    def inject_async(self, beam: "Beam"):
+        check(self._lib.sm2d_inject_async(self.h, C.byref(beam)))
+
+    def run_async(self, max_iterations=100000):
+        check(self._lib.sm2d_run_async(self.h, int(max_iterations)))
+
+    def dose_async(self, host_out: np.ndarray):
+        check(self._lib.sm2d_dose_async(self.h, _p(host_out)))
+
+    def stream(self):
+        return self._lib.sm2d_stream(self.h)
+
+    def run_profiled(self, n_iterations):
+        n, launches = C.c_int(), C.c_int()
+        ms = np.zeros(5, np.float32)
+        check(self._lib.sm2d_run_profiled(self.h, int(n_iterations), C.byref(n), _p(ms), C.byref(launches)))
+        return n.value, dict(zip(["classify", "compact", "transport", "k4", "audit"], ms.tolist())), launches.value
+
+    def step_timing(self):
+        t = np.zeros(5, np.float32)
+        check(self._lib.sm2d_get_step_timing(self.h, _p(t)))
+        return dict(zip(["classify", "compact", "transport", "k4", "audit"], t.tolist()))
+
+
+def depth_dose(dose_2d: np.ndarray) -> np.ndarray:
+    """get_depth_dose (src/validation/deterministic_beam.cpp:227-236): sum over x."""
+    return np.asarray(dose_2d).sum(axis=1)
+
+
+def bragg_peak_row(dose_2d: np.ndarray) -> int:
+    """find_bragg_peak_z (deterministic_beam.cpp:207-225): first row of the maximum."""
+    pdd = depth_dose(dose_2d)
+    best, row = 0.0, 0
+    for j, v in enumerate(pdd):
+        if v > best:
+            best, row = v, j
+    return row
