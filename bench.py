@@ -223,7 +223,10 @@ def run_gpu_arm(args):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
             s = t.scalars()
-            launches += 6 + 4 * (int(s["iterations"]) + 1)
+            # reset 3 + injection 6 + loop limit 1, then per pass of the device
+            # loop classify, claim pass, bucket and psi_out selection, deposit
+            # pass, finalize (+ bucket move)
+            launches += 10 + (7 if cfg.use_buckets else 6) * (int(s["iterations"]) + 1)
     barrier()
     total_ms = float(np.sum(times))
     if dist:

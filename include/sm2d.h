@@ -143,14 +143,18 @@ int sm2d_get_audit_history(sm2d_handle h, sm2d_audit* out, int max_entries, int*
  * [5] source_out_of_grid_weight [6] source_out_of_grid_energy
  * [7] source_slot_dropped_weight [8] source_slot_dropped_energy
  * [9] source_representation_loss_energy [10] iterations [11] cell_steps
- * [12] occupied input slots summed over cell-steps [13] output slots summed */
-int sm2d_get_scalars(sm2d_handle h, double* out14);
+ * [12] occupied input slots summed over cell-steps [13] output slots summed
+ * [14] claim-table inserts that found no free entry [15] deposits whose
+ * block id had not been gathered (both 0 in a correct run; cumulative
+ * since create) */
+int sm2d_get_scalars(sm2d_handle h, double* out16);
 int sm2d_get_fe(sm2d_handle h, float* A, float* B, float* sigma_total);
 /* EdepC after the lateral MCS post-convolution, [Nz][Nx] row-major */
 int sm2d_get_dose(sm2d_handle h, double* dose);
-/* per-kernel device time of the last sm2d_step (ms): classify, compact,
- * transport, K4, audit+clear */
-int sm2d_get_step_timing(sm2d_handle h, float* ms5);
+/* per-stage device time of the last sm2d_step (ms): classify, ascending
+ * lists, claim pass, slot selection, deposit pass, K4 bucket move,
+ * finalize (audit + clear + swap) */
+int sm2d_get_step_timing(sm2d_handle h, float* ms7);
 
 /* ---- asynchronous spot pipeline (no host synchronisation; stream order) ---- */
 /* the library's CUDA stream (cudaStream_t) */
@@ -164,9 +168,9 @@ int sm2d_run_async(sm2d_handle h, int max_iterations);
 /* post-convolved dose [Nz][Nx] into host memory (pinned for an async copy) */
 int sm2d_dose_async(sm2d_handle h, double* host_dose);
 /* replay up to n_iterations eagerly with CUDA events around every kernel;
- * ms5 receives the summed device time of classify, compact, transport,
- * K4 gather and audit, *launches the number of kernel launches */
-int sm2d_run_profiled(sm2d_handle h, int n_iterations, int* iterations_done, float* ms5, int* launches);
+ * ms7 receives the summed device time of the seven stages listed at
+ * sm2d_get_step_timing, *launches the number of kernel launches */
+int sm2d_run_profiled(sm2d_handle h, int n_iterations, int* iterations_done, float* ms7, int* launches);
 
 /* ---- host tables (no GPU needed) ---- */
 /* EnergyGrid(E_min,E_max,N) log grid (grids.cpp:6-24): edges[N+1], rep[N] */
@@ -206,6 +210,12 @@ int sm2d_k5_conservation_audit(
     double source_slot_dropped_energy, float transport_dropped_weight,
     double transport_dropped_energy, int include_source_terms, const float* d_E_edges, int N_E,
     int nt_local, int N_E_local, int local_bins, sm2d_audit* d_report, int N_cells, void* stream);
+
+/* ---- diagnostics (no counterpart in the reference) ---- */
+/* Evaluate one of the transport's elementary functions (0 exp, 1 log,
+ * 2 sin, 3 cos, 4 erf; sm2d_math.h) on n host values on the device; the
+ * oracle's build of the same header must agree bit for bit. */
+int sm2d_math_eval(int fn, const float* x, float* y, int n);
 
 #ifdef __cplusplus
 }

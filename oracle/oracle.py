@@ -68,8 +68,9 @@ def _lib(fp64: bool):
         if key in _LIBS:
             return _LIBS[key]
         path = os.path.join(BUILD, f"liborc{key}.so")
-        src = os.path.join(HERE, "sm2d_oracle.c")
-        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        srcs = [os.path.join(HERE, "sm2d_oracle.c"), os.path.join(HERE, "sm2d_oracle.h"),
+                os.path.join(HERE, "..", "sm_2d_gb300", "csrc", "sm2d_math.h")]
+        if not os.path.exists(path) or os.path.getmtime(path) < max(os.path.getmtime(f) for f in srcs):
             build()
         lib = C.CDLL(path)
         P = C.c_void_p
@@ -96,6 +97,7 @@ def _lib(fp64: bool):
         lib.orc_generate_rlut.argtypes = [C.c_int] + [P] * 6
         lib.orc_fe_precompute.argtypes = [C.c_float, C.c_int, C.c_float, C.c_float, P, P, P]
         lib.orc_postprocess.argtypes = [P, P, C.c_float, C.c_int, C.c_int, C.c_float, P]
+        lib.orc_math.argtypes = [C.c_int, P, P, C.c_int]
         _LIBS[key] = lib
         return lib
 
@@ -277,3 +279,15 @@ def psi_rows(bid, val, L, thresh=1e-12, Kb=KB):
     cells, slots, lidx = np.nonzero((v > thresh) & (b[:, :, None] != EMPTY))
     return dict(cell=cells, slot=slots, bid=b[cells, slots], lidx=lidx,
                 weight=v[cells, slots, lidx])
+
+
+MATH_FUNCS = ("exp", "log", "sin", "cos", "erf")
+
+
+def math_eval(name: str, x) -> np.ndarray:
+    """The transport's elementary function `name` (sm2d_math.h) as the float
+    oracle evaluates it."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    _lib(False).orc_math(MATH_FUNCS.index(name), x.ctypes.data, y.ctypes.data, x.size)
+    return y

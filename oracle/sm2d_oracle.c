@@ -4,10 +4,14 @@
  *
  * Reference files are cited by their path inside the SM_2D project.  The
  * float build reproduces the reference arithmetic order (no FMA contraction:
- * build with -ffp-contract=off); the double build (-DORC_FP64) evaluates the
- * same method in FP64.
+ * build with -ffp-contract=off) and takes exp/log/sin/cos/erf of the
+ * transport physics from the library's sm2d_math.h, the functions the CUDA
+ * kernels call, so that its per-bin results equal the kernels' bit for bit
+ * (host-side tables keep the C library, as the reference's host code does);
+ * the double build (-DORC_FP64) evaluates the same method in FP64.
  */
 #include "sm2d_oracle.h"
+#include "sm2d_math.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -29,12 +33,12 @@
 #define r_min fmin
 #else
 #define RL(x) (x##f)
-#define r_log logf
-#define r_exp expf
+#define r_log sm2d_logf
+#define r_exp sm2d_expf
 #define r_sqrt sqrtf
-#define r_cos cosf
-#define r_sin sinf
-#define r_erf erff
+#define r_cos sm2d_cosf
+#define r_sin sm2d_sinf
+#define r_erf sm2d_erff
 #define r_fabs fabsf
 #define r_floor floorf
 #define r_ceil ceilf
@@ -1259,9 +1263,12 @@ static void k4(orc_ctx* c) {
                 for (int l = 0; l < c->L; ++l) {
                     if (v[l] > RL(0.0)) {
                         int le = (sel != bid) ? remap_lidx(c, l, bid, sel) : l;
+                        /* split method: the re-binning shift is booked at the
+                           bucket's cell (the emitting side, like the bucket-level
+                           shift), so both K4 forms book it at a listed cell */
                         if (sel != bid && c->cfg.energy_split)
-                            c->edep[cell] += (double)((e_center(c, ebin_of(c, bid, l)) -
-                                                       e_center(c, ebin_of(c, sel, le))) * v[l]);
+                            c->edep[src] += (double)((e_center(c, ebin_of(c, bid, l)) -
+                                                      e_center(c, ebin_of(c, sel, le))) * v[l]);
                         po->val[((size_t)cell * c->Kb + os) * c->L + le] += v[l];
                     }
                 }
@@ -1810,4 +1817,12 @@ int orc_run_many(orc_ctx** ctxs, int n, int max_it, int n_threads) {
     free(th);
     pthread_mutex_destroy(&j.mu);
     return n;
+}
+
+void orc_math(int fn, const float* x, float* y, int n) {
+    for (int i = 0; i < n; ++i) {
+        float v = x[i];
+        y[i] = fn == 0 ? sm2d_expf(v) : fn == 1 ? sm2d_logf(v) : fn == 2 ? sm2d_sinf(v)
+             : fn == 3 ? sm2d_cosf(v) : sm2d_erff(v);
+    }
 }

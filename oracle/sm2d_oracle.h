@@ -98,6 +98,9 @@ void orc_fe_precompute(float E0, int Nz, float dz, float sigma_x0,
                        float* A, float* B, float* sigma_total);
 void orc_postprocess(const double* edep_in, const float* sigma_total, float sigma_x0,
                      int Nx, int Nz, float dx, double* edep_out);
+/* the transport's elementary functions (0 exp, 1 log, 2 sin, 3 cos, 4 erf)
+ * as this build evaluates them, for comparison with the CUDA build */
+void orc_math(int fn, const float* x, float* y, int n);
 
 /* ---- transport context ---- */
 orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* theta_edges,

@@ -51,7 +51,10 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     cu_obj = os.path.join(OUT, "sm2d_engine.o")
     cpp_obj = os.path.join(OUT, "sm2d_tables.o")
-    cu_cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-c", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    # --fmad=false: every float operation rounds on its own, as the oracle's
+    # -ffp-contract=off build does, so that both transport passes (and the
+    # oracle) take the same binning decisions from the same arithmetic
+    cu_cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-c", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "--expt-relaxed-constexpr", *inc, os.path.join(CSRC, "sm2d_engine.cu"), "-o", cu_obj]
     if ptxas_info:
         cu_cmd.insert(1, "-Xptxas=-v")

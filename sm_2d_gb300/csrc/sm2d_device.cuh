@@ -1,14 +1,15 @@
 // sm2d_device.cuh -- device-side physics, slot tables and bin encodings of
 // the transport step.  Float arithmetic follows the reference's expression
 // order (device_physics.cuh, device_lut.cuh, device_bucket.cuh,
-// device_psic.cuh) so that per-bin results agree with the reference build to
-// a few ulp; CUDA's own logf/expf/sinf/cosf/erff/sqrtf are called, as the
-// reference does.
+// device_psic.cuh); exp/log/sin/cos/erf come from sm2d_math.h, which the CPU
+// oracle shares, so per-bin results are bit-identical to the oracle's and
+// within about an ulp of the reference build's.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "sm2d.h"
+#include "sm2d_math.h"
 
 namespace sm2d {
 
@@ -42,14 +43,25 @@ struct IterState {
     int n_active, n_coarse;
     int done;              // no listed cell: transport finished
     int max_iter;          // stop after this many iterations (device loop)
-    unsigned blocks_done;  // audit kernel completion counter
+    unsigned blocks_done;  // last-block counter of the classify and finalize kernels
     int include_source;    // next audit lifts source losses (first iteration)
     int halt;              // this pass does no transport (finished or iteration limit)
+    int occ_n[2];          // length of each buffer's occupied-cell list
+    int n_listed;          // cells of this iteration (active + coarse)
+    int n_items;           // (cell, slot) work items of this iteration
+    int acc_active, acc_coarse, acc_listed, acc_items;   // classify counters
+    int cand_ovf;          // claim-table inserts that found no free entry (cumulative)
+    int cand_miss;         // deposits whose block id was not gathered (cumulative)
+    int wipe;              // claim tables are cleared before the next pass
+    int inj_skip;          // this injection found the phase space occupied
+    uint32_t ctag;         // claim pass number: the tag of claim-table entries
     int pad1;
-    // per-iteration accumulators (reset by the compaction kernel)
-    double drop_w, drop_e;
-    double Win, Ein, Wout, Eout, Wcut, Wnuc, Wbnd, Edep, Ecut, Enuc, Ebnd;
-    double slots_out_it;
+    unsigned long long gen;  // K1 classifications done since create (never reset)
+    // per-iteration accumulators, 14 consecutive doubles (reset by the
+    // classify kernel); the transport adds to the first seven, the finalize
+    // kernel to the last seven, in this order
+    double drop_w, drop_e, Win, Ein, Wout, Eout, slots_out_it;
+    double Edep, Ecut, Enuc, Ebnd, Wcut, Wnuc, Wbnd;
     // cumulative
     double transport_drop_w, transport_drop_e, audit_residual;
     double cell_steps, slots_in, slots_out;
@@ -77,20 +89,31 @@ struct Dev {
     int floor_cutoff, salt;
     uint32_t* bid[2];
     float* val[2];
-    uint8_t* occ[2];
+    int* occ[2];          // per cell: any slot claimed in this buffer
+    int* occ_list[2];     // occupied cells of each buffer, in claim order
     double *edep, *e_cut, *e_nuc, *e_bnd;
     float *w_cut, *w_nuc, *w_bnd;
-    uint8_t* mask;        // bit0 current, bit1 previous iteration
-    uint8_t* cls;         // 0 idle, 1 coarse (K2), 2 active (K3)
-    uint32_t *active, *coarse;
-    int* blk;             // per classify-block counts [2*nblk]
-    int nblk;
+    // this iteration's per-cell tally increments (folded into the cumulative
+    // tallies with the audit's per-cell clamp by the finalize kernel)
+    double *dl_edep, *dl_ecut, *dl_enuc, *dl_ebnd;
+    float *dl_wcut, *dl_wnuc, *dl_wbnd;
+    // K1 mask as the number of the last classification that found the cell
+    // active: bit 0 of the reference mask is act_gen == gen, its hysteresis
+    // input ("was active") is act_gen == gen - 1 at the next classification
+    unsigned long long* act_gen;
+    uint8_t* cls;         // 0 idle, 1 coarse (K2), 2 active (K3); 0 outside the iteration
+    uint32_t* listed;     // this iteration's active + coarse cells (claim order)
+    uint32_t* items;      // (cell << 5) | slot of every claimed slot of a listed cell
+    uint32_t *active, *coarse;   // ascending lists (built on request by k_order_lists)
     IterState* it;
     sm2d_audit* hist;
     int hist_cap;
     unsigned char* buckets;  // DeviceOutflowBucket array (bucket mode)
-    int* c2b;                // cell -> bucket base (bucket mode)
+    int* c2b;                // listed cell -> bucket base 4 * list position, -1 otherwise
     int bucket_bytes;
+    unsigned long long* ctab;  // claim tables: Nc psi_out rows, then 4 * Nc bucket rows
+    int* ccount;               // gathered ids per claim-table row
+    uint32_t* bkt_ids;         // kept ids of each bucket row [4 * Nc][32]
 };
 
 // ---------------------------------------------------------------- encodings
@@ -116,9 +139,9 @@ __device__ __forceinline__ float lut_range(const Dev& d, float E) {
     float Ec = fmaxf(d.lutEmin, fminf(E, d.lutEmax));
     int b = find_bin(d.Ee, d.lutN, Ec);
     if (b == d.lutN - 1 || Ec >= d.lutEmax) return d.R[d.lutN - 1];
-    float le = logf(Ec);
+    float le = sm2d_logf(Ec);
     float lr = d.logR[b] + (d.logR[b + 1] - d.logR[b]) * (le - d.logE[b]) / (d.logE[b + 1] - d.logE[b]);
-    return expf(lr);
+    return sm2d_expf(lr);
 }
 __device__ __forceinline__ float lut_energy_of_range(const Dev& d, float r) {
     if (r <= 0.0f) return d.lutEmin;
@@ -128,11 +151,11 @@ __device__ __forceinline__ float lut_energy_of_range(const Dev& d, float r) {
         if (d.R[mid] < r) lo = mid + 1; else hi = mid;
     }
     int b = max(0, min(lo, d.lutN - 2));
-    float lr = logf(r);
+    float lr = sm2d_logf(r);
     float dl = d.logR[b + 1] - d.logR[b];
-    if (fabsf(dl) < 1e-10f) return expf(d.logE[b]);
+    if (fabsf(dl) < 1e-10f) return sm2d_expf(d.logE[b]);
     float le = d.logE[b] + (d.logE[b + 1] - d.logE[b]) * (lr - d.logR[b]) / dl;
-    return expf(le);
+    return sm2d_expf(le);
 }
 __device__ __forceinline__ float lut_energy_loss(const Dev& d, float E, float s) {
     float r = lut_range(d, E) - s;
@@ -159,7 +182,7 @@ __device__ __forceinline__ float highland(float E, float ds) {
     float p = sqrtf(fmaxf((E + kMp) * (E + kMp) - kMp * kMp, 0.0f));
     float t = ds / kX0;
     if (t < 1e-6f) return 0.0f;
-    float br = fmaxf(1.0f + 0.038f * logf(t), 0.25f);
+    float br = fmaxf(1.0f + 0.038f * sm2d_logf(t), 0.25f);
     return (13.6f * 1.0f / (beta * p)) * sqrtf(t) * br;
 }
 __device__ __forceinline__ float scatter_power(float E, float ds) {
@@ -174,7 +197,7 @@ __device__ __forceinline__ float normal_draw(unsigned& s) {
     s = 1664525u * s + 1013904223u;
     float u2 = (float)(s >> 16) / 65536.0f;
     u1 = fmaxf(u1, 1e-6f);
-    return sqrtf(-2.0f * logf(u1)) * cosf(2.0f * 3.14159265358979323846f * u2);
+    return sqrtf(-2.0f * sm2d_logf(u1)) * sm2d_cosf(2.0f * 3.14159265358979323846f * u2);
 }
 __device__ __forceinline__ float vav_xi(float beta, float rho, float ds_cm) {
     return (0.307f / 2.0f) * 0.555f * (1.0f * 1.0f / (beta * beta)) * rho * ds_cm;
@@ -199,12 +222,12 @@ __device__ __forceinline__ float straggling_sigma(float E, float ds, float rho) 
 }
 __device__ __forceinline__ float nuclear_xs(float E) {
     if (E < 5.0f) return 0.0f;
-    if (E >= 20.0f) return 0.0012f * fmaxf(1.0f - 0.15f * logf(E / 100.0f), 0.4f);
+    if (E >= 20.0f) return 0.0012f * fmaxf(1.0f - 0.15f * sm2d_logf(E / 100.0f), 0.4f);
     return 0.0016f * ((E - 5.0f) / 15.0f);
 }
 __device__ __forceinline__ float gauss_cdf(float x, float mu, float sigma) {
     if (sigma < 1e-10f) return (x >= mu) ? 1.0f : 0.0f;
-    float c = 0.5f * (1.0f + erff((x - mu) / sigma * 0.70710678f));
+    float c = 0.5f * (1.0f + sm2d_erff((x - mu) / sigma * 0.70710678f));
     return fminf(1.0f, fmaxf(0.0f, c));
 }
 
@@ -215,29 +238,90 @@ __device__ __forceinline__ int bid_distance(uint32_t a, uint32_t b) {
     return abs(ea - eb) * 8 + abs(ta - tb);
 }
 // exact match, then CAS-claim an empty slot, then nearest occupied block
-// (device_psic.cuh:208-260 and device_bucket.cuh:61-128, same protocol)
+// (device_psic.cuh:208-260 and device_bucket.cuh:61-128, same protocol);
+// used by the K4 stage entry on caller arrays.
 __device__ __forceinline__ int claim_slot(uint32_t* ids, uint32_t want, uint32_t& sel) {
-    volatile uint32_t* v = ids;
     sel = want;
-#pragma unroll 4
+    volatile uint32_t* v = ids;
     for (int s = 0; s < kKb; ++s)
         if (v[s] == want) return s;
     for (int s = 0; s < kKb; ++s) {
-        uint32_t old = atomicCAS(&ids[s], kEmpty, want);
+        const uint32_t old = atomicCAS(&ids[s], kEmpty, want);
         if (old == kEmpty || old == want) return s;
     }
-    for (int s = 0; s < kKb; ++s)
-        if (v[s] == want) return s;
     int best = -1, bd = 0x7fffffff;
     uint32_t bb = kEmpty;
     for (int s = 0; s < kKb; ++s) {
-        uint32_t e = v[s];
-        if (e == kEmpty) continue;
-        int dd = bid_distance(e, want);
-        if (dd < bd) { bd = dd; best = s; bb = e; }
+        const uint32_t x = v[s];
+        if (x == kEmpty) continue;
+        const int dd = bid_distance(x, want);
+        if (dd < bd) { bd = dd; best = s; bb = x; }
     }
     if (best >= 0) sel = bb;
     return best;
+}
+
+// ---------------------------------------------------------------- claim tables
+// Deterministic slot claims.  A psi_out cell and an outflow bucket keep the
+// first 32 distinct block ids in the order a sequential pass of the step
+// claims them: the coarse (K2) batch before the fine (K3) batch; within a
+// batch, a cell's own in-cell deposits (by psi_in slot, local bin, energy
+// part) before the K4 transfers of faces 0..3 (by bucket slot); a bucket's
+// ids by emitting column, slot, local bin, emission index.  Ids past the
+// 32nd fold into the nearest kept id (smallest bid_distance, lowest slot on
+// ties), as the reference's fallback does once a table is full.  The ids
+// aimed at each container during one pass are gathered with their earliest
+// claim key in an open-addressing row of kCand entries
+// {tag << 32 | bid, (~tag) << 32 | key}; the tag is the claim pass number
+// (one per transport iteration and one per injection), so entries of
+// earlier passes read as free and the rows are never cleared (a wipe runs
+// when the pass number nears its 32-bit limit).  Injection uses the same
+// tables with the sample index as key: the reference's source kernels claim
+// in sample order when run one sample at a time.
+constexpr int kCandLog = 7, kCand = 1 << kCandLog;
+
+__device__ __forceinline__ unsigned cand_hash(uint32_t bid) { return (bid * 0x9E3779B1u) >> (32 - kCandLog); }
+
+__device__ __forceinline__ void cand_insert(unsigned long long* row, int* count, uint32_t tag, uint32_t bid,
+                                            uint32_t key, int* ovf) {
+    const unsigned long long tb = ((unsigned long long)tag << 32) | bid;
+    const unsigned long long k = ((unsigned long long)(0xFFFFFFFFu - tag) << 32) | key;
+    const unsigned h = cand_hash(bid);
+    for (int p = 0; p < kCand; ++p) {
+        unsigned long long* e = row + 2 * ((h + p) & (kCand - 1));
+        const unsigned long long cur = __ldcg(e);
+        if (cur != tb) {
+            if ((uint32_t)(cur >> 32) == tag) continue;   // another id of this pass
+            const unsigned long long old = atomicCAS(e, cur, tb);
+            if (old == cur) atomicAdd(count, 1);
+            else if (old != tb) continue;                 // taken by another id meanwhile
+        }
+        atomicMin(e + 1, k);
+        return;
+    }
+    atomicAdd(ovf, 1);
+}
+
+// Slot assigned to `bid` by the selection of this pass, -1 if not gathered.
+__device__ __forceinline__ int cand_find(const unsigned long long* row, uint32_t tag, uint32_t bid) {
+    const unsigned long long tb = ((unsigned long long)tag << 32) | bid;
+    const unsigned h = cand_hash(bid);
+    for (int p = 0; p < kCand; ++p) {
+        const unsigned long long* e = row + 2 * ((h + p) & (kCand - 1));
+        const unsigned long long cur = __ldcg(e);
+        if (cur == tb) return (int)((uint32_t)__ldcg(e + 1) & 31u);
+        if ((uint32_t)(cur >> 32) != tag) return -1;
+    }
+    return -1;
+}
+
+// First claim in a cell of buffer b puts the cell on that buffer's
+// occupied-cell list.
+__device__ __forceinline__ void mark_occupied(const Dev& d, int b, int cell) {
+    if (*(volatile int*)&d.occ[b][cell] == 0 && atomicExch(&d.occ[b][cell], 1) == 0) {
+        const int k = atomicAdd(&d.it->occ_n[b], 1);
+        d.occ_list[b][k] = cell;
+    }
 }
 template <class Lay>
 __device__ __forceinline__ int remap_lidx(int l, uint32_t src, uint32_t dst) {

@@ -61,42 +61,6 @@ __device__ __forceinline__ float warp_sumf(float v) {
 }
 
 // ------------------------------------------------------------------ injection
-// device_psic_inject_source (device_psic.cuh:347-450): clamp into the cell,
-// sub-cell bins, nearest global bins, CAS claim without fallback.
-template <class Lay>
-__device__ bool inject_one(const Dev& d, int par, int cell, float theta, float E, float w, float x, float z) {
-    if (w <= 0.0f || cell < 0 || cell >= d.Nc) return false;
-    const float dx = d.dx, dz = d.dz;
-    x = fmaxf(0.0f, fminf(x, dx));
-    z = fmaxf(0.0f, fminf(z, dz));
-    const int xs = sub_bin(x - dx * 0.5f, dx, Lay::NX), zs = sub_bin(z - dz * 0.5f, dz, Lay::NZ);
-    const float tmin = d.th[0], tmax = d.th[d.N_theta];
-    theta = fmaxf(tmin, fminf(theta, tmax));
-    E = fmaxf(d.Ee[0], fminf(E, d.Ee[d.N_E]));
-    const float cont = (theta - tmin) / ((tmax - tmin) / (float)d.N_theta);
-    int tb = (int)cont;
-    float ft = cont - (float)tb;
-    int Eb = find_bin(d.Ee, d.N_E, E);
-    const float lo = d.Ee[Eb], hi = d.Ee[Eb + 1];
-    float fE = (hi - lo) > 1e-10f ? (E - lo) / (hi - lo) : 0.0f;
-    if (tb >= d.N_theta - 1) { tb = d.N_theta - 1; ft = 0.0f; }
-    if (Eb >= d.N_E - 1) { Eb = d.N_E - 1; fE = 0.0f; }
-    if (ft >= 0.5f && tb < d.N_theta - 1) tb++;
-    if (fE >= 0.5f && Eb < d.N_E - 1) Eb++;
-    const uint32_t want = make_bid((uint32_t)(tb / Lay::NT), (uint32_t)(Eb / Lay::NE));
-    const int l = Lay::enc(tb % Lay::NT, Eb % Lay::NE, xs, zs);
-    uint32_t* ids = d.bid[par] + (size_t)cell * kKb;
-    for (int s = 0; s < kKb; ++s) {
-        const uint32_t old = atomicCAS(&ids[s], kEmpty, want);
-        if (old == kEmpty || old == want) {
-            d.occ[par][cell] = 1;
-            atomicAdd(d.val[par] + ((size_t)cell * kKb + s) * Lay::L + l, w);
-            return true;
-        }
-    }
-    return false;
-}
-
 // LCG/Box-Muller of the source kernel (k1k6_pipeline.cu:433-447)
 __device__ __forceinline__ float source_normal(unsigned& s) {
     s = 1664525u * s + 1013904223u;
@@ -114,58 +78,140 @@ struct BeamArgs {
     unsigned seed;
 };
 
+// One source sample: inject_source_kernel's pencil branch
+// (k1k6_pipeline.cu:325-343) or sample i of inject_gaussian_source_kernel
+// (k1k6_pipeline.cu:451-551), placed as device_psic_inject_source does
+// (device_psic.cuh:347-450: clamp into the cell, sub-cell bins, nearest
+// global bins).  Returns false when the sample leaves the grid.
+struct InjSample {
+    int cell, l;
+    uint32_t want;
+    float w, E;
+};
 template <class Lay>
-__global__ void k_inject(Dev d, BeamArgs b, int gaussian) {
-    const int par = d.it->parity;
-    if (!gaussian) {  // inject_source_kernel pencil branch (k1k6_pipeline.cu:325-343)
-        if (blockIdx.x || threadIdx.x) return;
+__device__ bool inject_sample(const Dev& d, const BeamArgs& b, int gaussian, int i, InjSample& o) {
+    float theta, E, x, z;
+    if (!gaussian) {
         const float xr = b.x0 - b.x_min, zr = b.z0 - b.z_min;
         int cx = (int)(xr / d.dx), cz = (int)(zr / d.dz);
         cx = cx < 0 ? 0 : (cx >= d.Nx ? d.Nx - 1 : cx);
         cz = cz < 0 ? 0 : (cz >= d.Nz ? d.Nz - 1 : cz);
-        inject_one<Lay>(d, par, cz * d.Nx + cx, b.theta0, b.E0, b.W, xr - cx * d.dx, zr - cz * d.dz);
-        return;
-    }
-    // inject_gaussian_source_kernel (k1k6_pipeline.cu:451-551)
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
-    unsigned s = b.seed + (unsigned)i;
-    const float xs = b.x0 + b.sx * source_normal(s);
-    float ts = b.theta0 + b.sth * source_normal(s);
-    float Es = b.E0 + b.sE * source_normal(s);
-    Es = fmaxf(d.Ee[0], fminf(Es, d.Ee[d.N_E]));
-    ts = fmaxf(d.th[0], fminf(ts, d.th[d.N_theta]));
-    const float xr = xs - b.x_min, zr = b.z0 - b.z_min;
-    const int ix = (int)(xr / d.dx), iz = (int)(zr / d.dz);
-    const float ws = b.W / b.n;
-    IterState* it = d.it;
-    if (ix < 0 || ix >= d.Nx || iz < 0 || iz >= d.Nz) {
-        atomicAdd(&it->src_oog_w, ws);
-        atomicAdd(&it->src_oog_e, (double)(Es * ws));
-        return;
-    }
-    if (inject_one<Lay>(d, par, iz * d.Nx + ix, ts, Es, ws, xr - ix * d.dx, zr - iz * d.dz)) {
-        atomicAdd(&it->src_inj_w, ws);
-        atomicAdd(&it->src_inj_e, (double)(Es * ws));
+        o.cell = cz * d.Nx + cx;
+        theta = b.theta0;
+        E = b.E0;
+        o.w = b.W;
+        x = xr - cx * d.dx;
+        z = zr - cz * d.dz;
     } else {
-        atomicAdd(&it->src_slot_w, ws);
-        atomicAdd(&it->src_slot_e, (double)(Es * ws));
+        unsigned s = b.seed + (unsigned)i;
+        const float xs = b.x0 + b.sx * source_normal(s);
+        float ts = b.theta0 + b.sth * source_normal(s);
+        float Es = b.E0 + b.sE * source_normal(s);
+        Es = fmaxf(d.Ee[0], fminf(Es, d.Ee[d.N_E]));
+        ts = fmaxf(d.th[0], fminf(ts, d.th[d.N_theta]));
+        const float xr = xs - b.x_min, zr = b.z0 - b.z_min;
+        const int ix = (int)(xr / d.dx), iz = (int)(zr / d.dz);
+        o.w = b.W / b.n;
+        o.E = Es;
+        if (ix < 0 || ix >= d.Nx || iz < 0 || iz >= d.Nz) return false;
+        o.cell = iz * d.Nx + ix;
+        theta = ts;
+        E = Es;
+        x = xr - ix * d.dx;
+        z = zr - iz * d.dz;
+    }
+    o.E = E;
+    const float dx = d.dx, dz = d.dz;
+    x = fmaxf(0.0f, fminf(x, dx));
+    z = fmaxf(0.0f, fminf(z, dz));
+    const int xs = sub_bin(x - dx * 0.5f, dx, Lay::NX), zs = sub_bin(z - dz * 0.5f, dz, Lay::NZ);
+    const float tmin = d.th[0], tmax = d.th[d.N_theta];
+    theta = fmaxf(tmin, fminf(theta, tmax));
+    E = fmaxf(d.Ee[0], fminf(E, d.Ee[d.N_E]));
+    const float cont = (theta - tmin) / ((tmax - tmin) / (float)d.N_theta);
+    int tb = (int)cont;
+    float ft = cont - (float)tb;
+    int Eb = find_bin(d.Ee, d.N_E, E);
+    const float lo = d.Ee[Eb], hi = d.Ee[Eb + 1];
+    float fE = (hi - lo) > 1e-10f ? (E - lo) / (hi - lo) : 0.0f;
+    if (tb >= d.N_theta - 1) { tb = d.N_theta - 1; ft = 0.0f; }
+    if (Eb >= d.N_E - 1) { Eb = d.N_E - 1; fE = 0.0f; }
+    if (ft >= 0.5f && tb < d.N_theta - 1) tb++;
+    if (fE >= 0.5f && Eb < d.N_E - 1) Eb++;
+    o.want = make_bid((uint32_t)(tb / Lay::NT), (uint32_t)(Eb / Lay::NE));
+    o.l = Lay::enc(tb % Lay::NT, Eb % Lay::NE, xs, zs);
+    return true;
+}
+
+// Opens an injection: one claim pass, refused (every sample booked as a
+// source slot drop) when psi_in is not empty.
+__global__ void k_inject_begin(IterState* it) {
+    if (threadIdx.x || blockIdx.x) return;
+    it->ctag += 1u;
+    it->inj_skip = it->occ_n[it->parity] != 0 ? 1 : 0;
+}
+
+// Claim pass of the injection: each in-grid sample offers its block to its
+// cell with its sample index as claim key.
+template <class Lay>
+__global__ void k_inject_keys(Dev d, const BeamArgs* bp, int gaussian) {
+    const BeamArgs b = *bp;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (gaussian ? b.n : 1) || d.it->inj_skip) return;
+    InjSample o;
+    if (!inject_sample<Lay>(d, b, gaussian, i, o) || !(o.w > 0.0f)) return;
+    cand_insert(psi_row(d, o.cell), d.ccount + o.cell, d.it->ctag, o.want, (uint32_t)i, &d.it->cand_ovf);
+    mark_occupied(d, d.it->parity, o.cell);
+}
+
+// Deposit pass of the injection: a sample whose block kept a slot adds its
+// weight there; the others are source slot drops (the reference's claim
+// without fallback).
+template <class Lay>
+__global__ void k_inject_deposit(Dev d, const BeamArgs* bp, int gaussian) {
+    const BeamArgs b = *bp;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (gaussian ? b.n : 1)) return;
+    IterState* it = d.it;
+    InjSample o;
+    const bool in = inject_sample<Lay>(d, b, gaussian, i, o);
+    if (!gaussian) {   // the pencil books W and E0 W in k_source_finalize
+        if (in && !it->inj_skip && o.w > 0.0f) {
+            const int s = cand_find(psi_row(d, o.cell), it->ctag, o.want);
+            if (s >= 0 && d.bid[it->parity][(size_t)o.cell * kKb + s] == o.want)
+                atomicAdd(d.val[it->parity] + ((size_t)o.cell * kKb + s) * Lay::L + o.l, o.w);
+        }
+        return;
+    }
+    if (!in) {
+        atomicAdd(&it->src_oog_w, o.w);
+        atomicAdd(&it->src_oog_e, (double)(o.E * o.w));
+        return;
+    }
+    int s = -1;
+    if (!it->inj_skip && o.w > 0.0f) s = cand_find(psi_row(d, o.cell), it->ctag, o.want);
+    if (s >= 0 && d.bid[it->parity][(size_t)o.cell * kKb + s] == o.want) {
+        atomicAdd(d.val[it->parity] + ((size_t)o.cell * kKb + s) * Lay::L + o.l, o.w);
+        atomicAdd(&it->src_inj_w, o.w);
+        atomicAdd(&it->src_inj_e, (double)(o.E * o.w));
+    } else {
+        atomicAdd(&it->src_slot_w, o.w);
+        atomicAdd(&it->src_slot_e, (double)(o.E * o.w));
     }
 }
 
 // Weight and bin-centre energy of the w > 0 bins of buffer `buf`
-// (compute_psic_total_weight_energy, k1k6_pipeline.cu:706-768).
+// (compute_psic_total_weight_energy, k1k6_pipeline.cu:706-768); warp per
+// occupied cell of that buffer.
 template <class Lay>
-__global__ void k_totals(Dev d, int which) {
+__global__ void __launch_bounds__(kThreads) k_totals(Dev d, int which) {
     const int buf = d.it->parity ^ which;
+    const int n = d.it->occ_n[buf];
     const int lane = threadIdx.x & 31;
-    const int cell0 = (blockIdx.x * blockDim.x + threadIdx.x) - lane;
-    const int cell = cell0 + lane;
-    unsigned ob = __ballot_sync(kFull, cell < d.Nc && d.occ[buf][cell]);
+    const int nw = (gridDim.x * blockDim.x) >> 5;
     double W = 0.0, E = 0.0;
-    while (ob) {
-        const int c = cell0 + __ffs(ob) - 1;
-        ob &= ob - 1;
+    for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
+        const int c = d.occ_list[buf][wi];
         const uint32_t b = d.bid[buf][(size_t)c * kKb + lane];
         unsigned used = __ballot_sync(kFull, b != kEmpty);
         while (used) {
@@ -191,36 +237,59 @@ __global__ void k_totals(Dev d, int which) {
     }
 }
 
+// Sum N per-thread values over the block and add them to dst[0..N) with one
+// atomic per value (dst: N consecutive IterState accumulators).
+template <int N>
+__device__ __forceinline__ void block_add(const double (&v)[N], double* dst) {
+    __shared__ double s[N][kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const double x = warp_sum(v[k]);
+        if (lane == 0) s[k][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double a = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) a += s[threadIdx.x][w];
+        if (a != 0.0) atomicAdd(dst + threadIdx.x, a);
+    }
+}
+
 // ------------------------------------------------------------------ K1
-// K1_ActiveMask (k1_activemask.cu:6-48) for the occupied cells; the class of
-// each cell (active / coarse with w > 0, compact_coarse_list
-// k1k6_pipeline.cu:625-665) and per-block counts for the ordered compaction.
+// K1_ActiveMask (k1_activemask.cu:6-48) over the occupied cells of psi_in,
+// warp per cell: the cell's class (active / coarse with w > 0,
+// compact_coarse_list k1k6_pipeline.cu:625-665), its place in this
+// iteration's cell list and bucket map, and one work item per claimed slot.
+// The last block publishes the counts, applies the stopping rules, resets
+// the per-iteration accumulators and sets the device loop condition.
 template <class Lay>
-__global__ void __launch_bounds__(kThreads) k_classify(Dev d) {
-    const int par = d.it->parity;
+__global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphConditionalHandle cond, int use_cond) {
+    __shared__ int s_cnt[2];
+    __shared__ int s_last, s_halt, s_listed;
+    IterState* it = d.it;
+    const int par = it->parity;
+    const int nocc = it->occ_n[par];
+    const unsigned long long g = it->gen + 1;   // number of this classification
     const int lane = threadIdx.x & 31;
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    const int cell0 = cell - lane;
-    const bool inb = cell < d.Nc;
-    const bool occ = inb && d.occ[par][cell];
-    unsigned ob = __ballot_sync(kFull, occ);
-    int on = 0, off = 0, hw = 0;
-    float W = 0.0f;
-    while (ob) {
-        const int src = __ffs(ob) - 1;
-        ob &= ob - 1;
-        const int c = cell0 + src;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < nocc; wi += nw) {
+        const int c = d.occ_list[par][wi];
         const uint32_t b = d.bid[par][(size_t)c * kKb + lane];
         const bool used = b != kEmpty;
         const uint32_t be = (b >> 12) & 0xFFFu;
-        const int c_on = __any_sync(kFull, used && be <= (uint32_t)d.b_on);
-        const int c_off = __any_sync(kFull, used && be <= (uint32_t)d.b_off);
-        unsigned um = __ballot_sync(kFull, used);
+        const bool c_on = __any_sync(kFull, used && be <= (uint32_t)d.b_on);
+        const bool c_off = __any_sync(kFull, used && be <= (uint32_t)d.b_off);
+        const unsigned um = __ballot_sync(kFull, used);
         float ws = 0.0f;
         int pos = 0;
-        while (um) {
-            const int s = __ffs(um) - 1;
-            um &= um - 1;
+        unsigned m = um;
+        while (m) {
+            const int s = __ffs(m) - 1;
+            m &= m - 1;
             const float4* v = reinterpret_cast<const float4*>(d.val[par] + ((size_t)c * kKb + s) * Lay::L);
             for (int q = lane; q < Lay::L / 4; q += 32) {
                 const float4 f = v[q];
@@ -228,63 +297,45 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d) {
                 pos |= (f.x > 0.0f) | (f.y > 0.0f) | (f.z > 0.0f) | (f.w > 0.0f);
             }
         }
-        ws = warp_sumf(ws);
-        ws = __shfl_sync(kFull, ws, 0);
-        const int c_hw = __any_sync(kFull, pos);
-        if (lane == src) { on = c_on; off = c_off; hw = c_hw; W = ws; }
-    }
-    uint8_t cls = 0;
-    if (inb) {
-        const uint8_t m_old = d.mask[cell];
-        const bool prev = (m_old & 1) != 0;
-        const bool act = occ && (on || (prev && off)) && W > d.wmin;
-        cls = act ? 2 : ((occ && hw) ? 1 : 0);
-        d.mask[cell] = (uint8_t)((act ? 1 : 0) | (prev ? 2 : 0));
-        d.cls[cell] = cls;
-    }
-    const int na = __syncthreads_count(cls == 2);
-    const int nc = __syncthreads_count(cls == 1);
-    if (threadIdx.x == 0) {
-        d.blk[2 * blockIdx.x] = na;
-        d.blk[2 * blockIdx.x + 1] = nc;
-    }
-}
-
-// Ordered compaction (ascending cell index) of the classes into the active
-// and coarse lists; the last block finalises the counts, resets the
-// per-iteration accumulators and sets the device loop condition.
-__global__ void __launch_bounds__(kThreads) k_compact(Dev d, cudaGraphConditionalHandle cond, int use_cond) {
-    __shared__ int s_pre[2];
-    __shared__ int s_warp[2][kThreads / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (wid == 0) {
-        int a = 0, c = 0;
-        for (int b = lane; b < (int)blockIdx.x; b += 32) {
-            a += d.blk[2 * b];
-            c += d.blk[2 * b + 1];
+        ws = __shfl_sync(kFull, warp_sumf(ws), 0);
+        const bool hw = __any_sync(kFull, pos);
+        const bool prev = d.act_gen[c] == g - 1;
+        const bool act = (c_on || (prev && c_off)) && ws > d.wmin;
+        const int cls = act ? 2 : (hw ? 1 : 0);
+        int base = 0;
+        if (lane == 0) {
+            d.cls[c] = (uint8_t)cls;
+            if (act) d.act_gen[c] = g;
+            if (cls) {
+                const int idx = atomicAdd(&it->acc_listed, 1);
+                base = atomicAdd(&it->acc_items, __popc(um));
+                d.listed[idx] = (uint32_t)c;
+                d.c2b[c] = 4 * idx;
+                atomicAdd(&s_cnt[act ? 0 : 1], 1);
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_down_sync(kFull, a, o);
-            c += __shfl_down_sync(kFull, c, o);
+        if (cls) {
+            base = __shfl_sync(kFull, base, 0);
+            if (used) d.items[base + __popc(um & lt)] = ((uint32_t)c << 5) | (uint32_t)lane;
         }
-        if (lane == 0) { s_pre[0] = a; s_pre[1] = c; }
     }
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint8_t cls = cell < d.Nc ? d.cls[cell] : 0;
-    const unsigned ba = __ballot_sync(kFull, cls == 2), bc = __ballot_sync(kFull, cls == 1);
-    if (lane == 0) { s_warp[0][wid] = __popc(ba); s_warp[1][wid] = __popc(bc); }
     __syncthreads();
-    int oa = s_pre[0], oc = s_pre[1];
-    for (int w = 0; w < wid; ++w) { oa += s_warp[0][w]; oc += s_warp[1][w]; }
-    const unsigned lt = (1u << lane) - 1u;
-    if (cls == 2) d.active[oa + __popc(ba & lt)] = (uint32_t)cell;
-    if (cls == 1) d.coarse[oc + __popc(bc & lt)] = (uint32_t)cell;
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-        int na = s_pre[0], nc = s_pre[1];
-        for (int w = 0; w < kThreads / 32; ++w) { na += s_warp[0][w]; nc += s_warp[1][w]; }
-        IterState* it = d.it;
-        it->n_active = na;
-        it->n_coarse = nc;
+    if (threadIdx.x == 0) {
+        if (s_cnt[0]) atomicAdd(&it->acc_active, s_cnt[0]);
+        if (s_cnt[1]) atomicAdd(&it->acc_coarse, s_cnt[1]);
+        __threadfence();
+        s_last = atomicAdd(&it->blocks_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        volatile IterState* v = it;
+        int na = v->acc_active, nc = v->acc_coarse;
+        const int nl = v->acc_listed, ni = v->acc_items;
+        it->acc_active = it->acc_coarse = it->acc_listed = it->acc_items = 0;
+        it->gen = g;
+        it->ctag += 1u;   // claim pass of this iteration
         // C1 stopping rule: in-flight weight (the last audit's W_out) below a
         // fraction of the injected weight ends the run; the rest is booked as
         // a terminal transport drop (k1k6_pipeline.cu:1677-1706 books it too)
@@ -294,193 +345,333 @@ __global__ void __launch_bounds__(kThreads) k_compact(Dev d, cudaGraphConditiona
             it->transport_drop_w += it->last.W_out_total;
             it->transport_drop_e += it->last.E_out_total;
             na = nc = 0;
-            it->n_active = it->n_coarse = 0;
         }
+        it->n_active = na;
+        it->n_coarse = nc;
         const bool done = (na + nc) == 0;
         it->done = done ? 1 : 0;
         const bool halt = done || it->iter >= it->max_iter;
         it->halt = halt ? 1 : 0;
-        it->drop_w = it->drop_e = 0.0;
-        it->Win = it->Ein = it->Wout = it->Eout = 0.0;
-        it->Wcut = it->Wnuc = it->Wbnd = 0.0;
-        it->Edep = it->Ecut = it->Enuc = it->Ebnd = 0.0;
-        it->slots_out_it = 0.0;
+        it->n_listed = halt ? 0 : nl;
+        it->n_items = halt ? 0 : ni;
+        double* acc = &it->drop_w;   // the 14 per-iteration accumulators
+        for (int k = 0; k < 14; ++k) acc[k] = 0.0;
         it->blocks_done = 0;
-        if (!halt) it->cell_steps += (double)(na + nc);
+        if (!halt) {
+            it->cell_steps += (double)(na + nc);
+            it->slots_in += (double)ni;
+        }
         if (use_cond) cudaGraphSetConditional(cond, (!halt && it->iter + 1 < it->max_iter) ? 1u : 0u);
+        s_halt = halt ? 1 : 0;
+        s_listed = nl;
+    }
+    __syncthreads();
+    if (s_halt) {   // no transport or finalize follows: release this pass's cell marks
+        for (int i = threadIdx.x; i < s_listed; i += blockDim.x) {
+            const int c = (int)d.listed[i];
+            d.cls[c] = 0;
+            d.c2b[c] = -1;
+        }
+    }
+}
+
+// Ascending active and coarse lists from the classes of this iteration
+// (the reference's ordered compaction); one block, on request of the
+// stepping API.
+__global__ void __launch_bounds__(1024) k_order_lists(Dev d) {
+    __shared__ int s_w[2][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int base_a = 0, base_c = 0;
+    for (int c0 = 0; c0 < d.Nc; c0 += 1024) {
+        const int cell = c0 + (int)threadIdx.x;
+        const int cls = cell < d.Nc ? d.cls[cell] : 0;
+        const unsigned ba = __ballot_sync(kFull, cls == 2), bc = __ballot_sync(kFull, cls == 1);
+        if (lane == 0) { s_w[0][wid] = __popc(ba); s_w[1][wid] = __popc(bc); }
+        __syncthreads();
+        int oa = base_a, oc = base_c, ta = 0, tc = 0;
+        for (int w = 0; w < 32; ++w) {
+            if (w < wid) { oa += s_w[0][w]; oc += s_w[1][w]; }
+            ta += s_w[0][w];
+            tc += s_w[1][w];
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        if (cls == 2) d.active[oa + __popc(ba & lt)] = (uint32_t)cell;
+        if (cls == 1) d.coarse[oc + __popc(bc & lt)] = (uint32_t)cell;
+        base_a += ta;
+        base_c += tc;
+        __syncthreads();
     }
 }
 
 // ------------------------------------------------------------------ K2/K3
-template <class Lay, bool BUCKET>
-__global__ void __launch_bounds__(kThreads) k_transport(Dev d) {
+// One warp per (listed cell, claimed slot) work item: the slot's w > 0 bins
+// are packed into shared memory and spread over the lanes, each lane
+// transporting one bin at a time.  PASS_KEYS gathers the claim candidates;
+// the deposit passes read (and clear) the slot, add the weights, and book
+// per-cell tally increments in the dl_* arrays and the audit sums per block.
+template <class Lay, int PASS>
+__global__ void __launch_bounds__(kThreads, 2) k_transport(Dev d) {
+    constexpr int NW = kThreads / 32, Q = Lay::L / 128;
+    __shared__ float s_w[NW][Lay::L];
+    __shared__ uint16_t s_l[NW][Lay::L];
     IterState* it = d.it;
     if (it->halt) return;
     const int par = it->parity;
-    const int n_co = it->n_coarse, n = n_co + it->n_active;
-    const int lane = threadIdx.x & 31;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
-        const bool k3 = wi >= n_co;
-        const int cell = (int)(k3 ? d.active[wi - n_co] : d.coarse[wi]);
-        const uint32_t myb = d.bid[par][(size_t)cell * kKb + lane];
-        const bool used = myb != kEmpty;
-        unsigned um = __ballot_sync(kFull, used);
-        int rank = 0;
-        if (d.seed_mode) {
-            for (int t = 0; t < 32; ++t) {
-                const uint32_t bt = __shfl_sync(kFull, myb, t);
-                rank += (bt != kEmpty && bt < myb) ? 1 : 0;
-            }
+    const int n = it->n_items;
+    const uint32_t tag = it->ctag;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = gridDim.x * NW;
+    const unsigned salt = d.salt ? (unsigned)it->iter * 0x9E3779B9u : 0u;
+    double g[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // drop_w, drop_e, Win, Ein, Wout, Eout, -
+    for (int wi = blockIdx.x * NW + wid; wi < n; wi += nw) {
+        const uint32_t item = d.items[wi];
+        const int cell = (int)(item >> 5), s = (int)(item & 31u);
+        const bool k3 = d.cls[cell] == 2;
+        const uint32_t mb = d.bid[par][(size_t)cell * kKb + lane];
+        const uint32_t bid = __shfl_sync(kFull, mb, s);
+        // seed slot: the slot index, or the rank of the block id in the cell
+        const int sslot = d.seed_mode ? __popc(__ballot_sync(kFull, mb != kEmpty && mb < bid)) : s;
+        float4* vp = reinterpret_cast<float4*>(d.val[par] + ((size_t)cell * kKb + s) * Lay::L);
+        float4 f[Q];
+        int cnt = 0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            f[q] = PASS == PASS_KEYS ? __ldcg(vp + lane + 32 * q) : __ldcs(vp + lane + 32 * q);
+            cnt += (f[q].x > 0.0f) + (f[q].y > 0.0f) + (f[q].z > 0.0f) + (f[q].w > 0.0f);
         }
-        Tally t{};
-        const int n_slots = __popc(um);
-        const unsigned salt = d.salt ? (unsigned)it->iter * 0x9E3779B9u : 0u;
-        while (um) {
-            const int s = __ffs(um) - 1;
-            um &= um - 1;
-            const uint32_t bid = __shfl_sync(kFull, myb, s);
-            const int sslot = d.seed_mode ? __shfl_sync(kFull, rank, s) : s;
-            const float4* v = reinterpret_cast<const float4*>(d.val[par] + ((size_t)cell * kKb + s) * Lay::L);
-            for (int q = lane; q < Lay::L / 4; q += 32) {
-                const float4 f = v[q];
-#pragma unroll 1
-                for (int k = 0; k < 4; ++k) {
-                    const float wk = k == 0 ? f.x : (k == 1 ? f.y : (k == 2 ? f.z : f.w));
-                    if (wk > 0.0f) transport_bin<Lay, BUCKET>(d, par, k3, cell, bid, sslot, 4 * q + k, wk, salt, t);
+        if (PASS != PASS_KEYS) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) __stcs(vp + lane + 32 * q, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        }
+        int inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += y;
+        }
+        const int total = __shfl_sync(kFull, inc, 31);
+        int pos = inc - cnt;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const float c4[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (c4[k] > 0.0f) {
+                    s_w[wid][pos] = c4[k];
+                    s_l[wid][pos] = (uint16_t)(4 * (lane + 32 * q) + k);
+                    ++pos;
                 }
-            }
         }
-        // per-cell commit: one warp owns the cell's tallies in this iteration
-        t.edep = warp_sum(t.edep);
-        t.e_cut = warp_sum(t.e_cut);
-        t.e_nuc = warp_sum(t.e_nuc);
-        t.e_bnd = warp_sum(t.e_bnd);
-        t.w_cut = warp_sumf(t.w_cut);
-        t.w_nuc = warp_sumf(t.w_nuc);
-        t.w_bnd = warp_sumf(t.w_bnd);
-        t.drop_w = warp_sum(t.drop_w);
-        t.drop_e = warp_sum(t.drop_e);
-        t.Win = warp_sum(t.Win);
-        t.Ein = warp_sum(t.Ein);
+        __syncwarp();
+        Tally t{};
+        for (int j = lane; j < total; j += 32)
+            transport_bin<Lay, PASS>(d, par, k3, cell, bid, s, sslot, (int)s_l[wid][j], s_w[wid][j], salt, tag, t);
+        __syncwarp();
+        if (PASS == PASS_KEYS) continue;
+        const double edep = warp_sum(t.edep), ecut = warp_sum(t.e_cut), enuc = warp_sum(t.e_nuc),
+                     ebnd = warp_sum(t.e_bnd);
+        const float wcut = warp_sumf(t.w_cut), wnuc = warp_sumf(t.w_nuc), wbnd = warp_sumf(t.w_bnd);
         if (lane == 0) {
-            // K5 takes max(0, cumulative - previous) per cell (k5_audit.cu:93-99)
-            const double e0 = d.edep[cell], e1 = e0 + t.edep;
-            const double c0 = d.e_cut[cell], c1 = c0 + t.e_cut;
-            const double n0 = d.e_nuc[cell], n1 = n0 + t.e_nuc;
-            const double b0 = d.e_bnd[cell], b1 = b0 + t.e_bnd;
-            const float wc0 = d.w_cut[cell], wc1 = wc0 + t.w_cut;
-            const float wn0 = d.w_nuc[cell], wn1 = wn0 + t.w_nuc;
-            const float wb0 = d.w_bnd[cell], wb1 = wb0 + t.w_bnd;
-            d.edep[cell] = e1; d.e_cut[cell] = c1; d.e_nuc[cell] = n1; d.e_bnd[cell] = b1;
-            d.w_cut[cell] = wc1; d.w_nuc[cell] = wn1; d.w_bnd[cell] = wb1;
-            atomicAdd(&it->Edep, fmax(0.0, e1 - e0));
-            atomicAdd(&it->Ecut, fmax(0.0, c1 - c0));
-            atomicAdd(&it->Enuc, fmax(0.0, n1 - n0));
-            atomicAdd(&it->Ebnd, fmax(0.0, b1 - b0));
-            atomicAdd(&it->Wcut, (double)fmaxf(0.0f, wc1 - wc0));
-            atomicAdd(&it->Wnuc, (double)fmaxf(0.0f, wn1 - wn0));
-            atomicAdd(&it->Wbnd, (double)fmaxf(0.0f, wb1 - wb0));
-            atomicAdd(&it->Win, t.Win);
-            atomicAdd(&it->Ein, t.Ein);
-            if (t.drop_w != 0.0 || t.drop_e != 0.0) {
-                atomicAdd(&it->drop_w, t.drop_w);
-                atomicAdd(&it->drop_e, t.drop_e);
+            if (edep != 0.0) atomicAdd(d.dl_edep + cell, edep);
+            if (ecut != 0.0) atomicAdd(d.dl_ecut + cell, ecut);
+            if (enuc != 0.0) atomicAdd(d.dl_enuc + cell, enuc);
+            if (ebnd != 0.0) atomicAdd(d.dl_ebnd + cell, ebnd);
+            if (wcut != 0.0f) atomicAdd(d.dl_wcut + cell, wcut);
+            if (wnuc != 0.0f) atomicAdd(d.dl_wnuc + cell, wnuc);
+            if (wbnd != 0.0f) atomicAdd(d.dl_wbnd + cell, wbnd);
+        }
+        g[0] += t.drop_w; g[1] += t.drop_e; g[2] += t.Win; g[3] += t.Ein;
+        g[4] += t.Wout; g[5] += t.Eout;
+    }
+    if (PASS != PASS_KEYS) block_add<7>(g, &it->drop_w);
+}
+
+// ------------------------------------------------------------------ slot selection
+// Selection of one claim-table row by one warp: the gathered ids ordered by
+// claim key; the first 32 become slots 0..31 (written to kept[]), the rest
+// fold into the nearest kept id (smallest bid_distance, lowest slot on
+// ties).  Each entry's key is replaced by its slot for the deposit pass.
+// Returns the number of kept ids.
+struct SelScratch {
+    uint32_t bid[kCand], key[kCand];
+    uint8_t idx[kCand], rank[kCand];
+    uint32_t kept[kKb];
+};
+__device__ int select_row(unsigned long long* row, int* count, uint32_t tag, SelScratch& sh, uint32_t* kept, int lane) {
+    const unsigned lt = (1u << lane) - 1u;
+    const bool any = *(volatile int*)count > 0;
+    int n = 0;
+    if (any) {
+#pragma unroll
+        for (int q = 0; q < kCand / 32; ++q) {
+            const int i = q * 32 + lane;
+            const unsigned long long tb = __ldcg(row + 2 * i);
+            const bool cur = (uint32_t)(tb >> 32) == tag;
+            const unsigned m = __ballot_sync(kFull, cur);
+            if (cur) {
+                const int p = n + __popc(m & lt);
+                sh.bid[p] = (uint32_t)tb;
+                sh.key[p] = (uint32_t)__ldcg(row + 2 * i + 1);
+                sh.idx[p] = (uint8_t)i;
             }
-            atomicAdd(&it->slots_in, (double)n_slots);
+            n += __popc(m);
         }
     }
+    __syncwarp();
+    for (int j = lane; j < n; j += 32) {
+        const uint32_t kj = sh.key[j], bj = sh.bid[j];
+        int r = 0;
+        for (int m = 0; m < n; ++m) {
+            const uint32_t km = sh.key[m];
+            r += (km < kj || (km == kj && sh.bid[m] < bj)) ? 1 : 0;
+        }
+        sh.rank[j] = (uint8_t)r;
+        if (r < kKb) sh.kept[r] = bj;
+    }
+    __syncwarp();
+    const int nk = min(n, kKb);
+    for (int j = lane; j < n; j += 32) {
+        int slot = sh.rank[j];
+        if (slot >= kKb) {
+            const uint32_t want = sh.bid[j];
+            int bd = 0x7fffffff;
+            for (int k = 0; k < kKb; ++k) {
+                const int dd = bid_distance(sh.kept[k], want);
+                if (dd < bd) { bd = dd; slot = k; }
+            }
+        }
+        row[2 * (int)sh.idx[j] + 1] = ((unsigned long long)(0xFFFFFFFFu - tag) << 32) | (uint32_t)slot;
+    }
+    if (kept) kept[lane] = lane < nk ? sh.kept[lane] : kEmpty;
+    if (lane == 0 && any) *count = 0;
+    __syncwarp();
+    return nk;
+}
+
+// Buckets of this pass (warp per listed cell and face): select the kept
+// ids, write them to the bucket (bucket mode: also clear its values), and
+// offer them to the psi_out row of the cell behind the face in bucket-slot
+// order, as K4 claims them.
+template <class Lay, bool BUCKET>
+__global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
+    constexpr int NW = kThreads / 32;
+    __shared__ SelScratch s_sel[NW];
+    IterState* it = d.it;
+    if (it->halt) return;
+    const int out = it->parity ^ 1;
+    const int n = 4 * it->n_listed;
+    const uint32_t tag = it->ctag;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int wi = blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
+        const int face = wi & 3;
+        const int src = (int)d.listed[wi >> 2];
+        uint32_t* kept = d.bkt_ids + (size_t)wi * kKb;
+        const int nk = select_row(bucket_row(d, wi), d.ccount + d.Nc + wi, tag, s_sel[wid], kept, lane);
+        if (BUCKET) {
+            unsigned char* b = d.buckets + (size_t)wi * d.bucket_bytes;
+            bucket_ids(b)[lane] = lane < nk ? s_sel[wid].kept[lane] : kEmpty;
+            reinterpret_cast<uint16_t*>(b + 128)[lane] = 0;
+            float* v = bucket_vals(b);
+            for (int k = lane; k < nk * Lay::L; k += 32) v[k] = 0.0f;
+        }
+        if (nk == 0) continue;
+        const int ix = src % d.Nx, iz = src / d.Nx;
+        int dst = -1;
+        if (face == FACE_ZP && iz + 1 < d.Nz) dst = src + d.Nx;
+        if (face == FACE_ZM && iz > 0) dst = src - d.Nx;
+        if (face == FACE_XP && ix + 1 < d.Nx) dst = src + 1;
+        if (face == FACE_XM && ix > 0) dst = src - 1;
+        if (dst < 0) continue;
+        const int k3 = d.cls[src] == 2 ? 1 : 0;
+        if (lane < nk)
+            cand_insert(psi_row(d, dst), d.ccount + dst, tag, s_sel[wid].kept[lane], k4_key(k3, face, lane),
+                        &it->cand_ovf);
+        if (lane == 0) mark_occupied(d, out, dst);
+    }
+}
+
+// Occupied cells of psi_out (which = 1, a transport pass) or of psi_in
+// (which = 0, an injection), warp per cell: select the kept ids into the
+// cell's slot ids.
+__global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
+    constexpr int NW = kThreads / 32;
+    __shared__ SelScratch s_sel[NW];
+    IterState* it = d.it;
+    if (which && it->halt) return;
+    const int buf = it->parity ^ which;
+    const int n = it->occ_n[buf];
+    const uint32_t tag = it->ctag;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double kept_slots = 0.0;
+    for (int wi = blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
+        const int cell = d.occ_list[buf][wi];
+        const int nk = select_row(psi_row(d, cell), d.ccount + cell, tag, s_sel[wid], d.bid[buf] + (size_t)cell * kKb,
+                                  lane);
+        if (lane == 0) kept_slots += (double)nk;
+    }
+    if (which && lane == 0 && kept_slots != 0.0) atomicAdd(&it->slots_out_it, kept_slots);
 }
 
 // ------------------------------------------------------------------ bucket mode (reference structure)
+// K4_BucketTransfer (k4_transfer.cu:174-333) driven from the source side:
+// warp per (listed cell, face) moves that bucket into psi_out of the
+// neighbour behind the face, each bucket slot into the slot its kept id
+// resolved to (lidx remap when it folded into a nearer id).
 template <class Lay>
-__global__ void k_bucket_prep(Dev d) {
+__global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
     IterState* it = d.it;
     if (it->halt) return;
-    const int n_co = it->n_coarse, n = n_co + it->n_active;
-    const int i = blockIdx.x;
-    if (i >= n) return;
-    const int cell = (int)(i < n_co ? d.coarse[i] : d.active[i - n_co]);
-    if (threadIdx.x == 0) d.c2b[cell] = 4 * i;
-    for (int f = 0; f < 4; ++f) {   // clear_buckets_kernel (k1k6_pipeline.cu:554-573)
-        unsigned char* b = d.buckets + (size_t)(4 * i + f) * d.bucket_bytes;
-        if (threadIdx.x < 32) bucket_ids(b)[threadIdx.x] = kEmpty;
-        if (threadIdx.x < 32) reinterpret_cast<uint16_t*>(b + 128)[threadIdx.x] = 0;
-        float* v = bucket_vals(b);
-        for (int k = threadIdx.x; k < 32 * Lay::L + 3; k += blockDim.x) v[k] = 0.0f;
-    }
-}
-
-// K4_BucketTransfer (k4_transfer.cu:174-333): per destination cell, pull the
-// facing buckets of its four neighbours into psi_out (claim with fallback,
-// lidx remap, drop accounting).  Warp per destination cell.
-template <class Lay>
-__device__ void bucket_gather_cell(const unsigned char* buckets, int bucket_bytes, const int* c2b, uint32_t* ids_out,
-                                   float* vals_out, uint8_t* occ_out, int cell, int Nx, int Nz, const float* Ee,
-                                   int N_E, double* drop_w, double* drop_e, int lane) {
-    const int ix = cell % Nx, iz = cell / Nx;
-    for (int face = 0; face < 4; ++face) {
-        int src = -1;
-        if (face == 0 && iz > 0) src = cell - Nx;
-        if (face == 1 && iz + 1 < Nz) src = cell + Nx;
-        if (face == 2 && ix > 0) src = cell - 1;
-        if (face == 3 && ix + 1 < Nx) src = cell + 1;
-        if (src < 0) continue;
-        const int base = c2b[src];
-        if (base < 0) continue;
-        const unsigned char* b = buckets + (size_t)(base + face) * bucket_bytes;
-        const uint32_t sb = reinterpret_cast<const uint32_t*>(b)[lane];
+    const int out = it->parity ^ 1;
+    const int n = 4 * it->n_listed;
+    const uint32_t tag = it->ctag;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double g[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // drop_w, drop_e, -, -, Wout, Eout, -
+    for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
+        const int face = wi & 3;
+        const int src = (int)d.listed[wi >> 2];
+        const int ix = src % d.Nx, iz = src / d.Nx;
+        int dst = -1;
+        if (face == FACE_ZP && iz + 1 < d.Nz) dst = src + d.Nx;
+        if (face == FACE_ZM && iz > 0) dst = src - d.Nx;
+        if (face == FACE_XP && ix + 1 < d.Nx) dst = src + 1;
+        if (face == FACE_XM && ix > 0) dst = src - 1;
+        if (dst < 0) continue;
+        unsigned char* b = d.buckets + (size_t)wi * d.bucket_bytes;
+        const uint32_t sb = bucket_ids(b)[lane];
         unsigned um = __ballot_sync(kFull, sb != kEmpty);
-        const float* bv = reinterpret_cast<const float*>(b + 192);
+        const float* bv = bucket_vals(b);
+        const uint32_t* kept = d.bid[out] + (size_t)dst * kKb;
         while (um) {
             const int s = __ffs(um) - 1;
             um &= um - 1;
             const uint32_t bid = __shfl_sync(kFull, sb, s);
-            int os = 0;
             uint32_t sel = bid;
-            if (lane == 0) {
-                os = claim_slot(ids_out + (size_t)cell * kKb, bid, sel);
-                if (os >= 0 && occ_out) occ_out[cell] = 1;
-            }
-            os = __shfl_sync(kFull, os, 0);
-            sel = __shfl_sync(kFull, sel, 0);
+            const int os = resolve(d, psi_row(d, dst), kept, tag, bid, sel);
             const float* v = bv + (size_t)s * Lay::L;
-            if (os < 0) {
-                double dw = 0.0, de = 0.0;
-                for (int l = lane; l < Lay::L; l += 32) {
-                    const float w = v[l];
-                    if (w > 0.0f) {
-                        int Eb = (int)((bid >> 12) & 0xFFFu) * Lay::NE + (l / Lay::NT) % Lay::NE;
-                        Eb = max(0, min(Eb, N_E - 1));
-                        const float E = Ee[Eb] + 1.0f * (0.5f * (Ee[Eb + 1] - Ee[Eb]));
-                        dw += (double)w;
-                        de += (double)E * (double)w;
-                    }
-                }
-                dw = warp_sum(dw);
-                de = warp_sum(de);
-                if (lane == 0) { atomicAdd(drop_w, dw); atomicAdd(drop_e, de); }
-                continue;
-            }
-            float* o = vals_out + ((size_t)cell * kKb + os) * Lay::L;
+            float* o = os >= 0 ? d.val[out] + ((size_t)dst * kKb + os) * Lay::L : nullptr;
+            double eshift = 0.0;
             for (int l = lane; l < Lay::L; l += 32) {
                 const float w = v[l];
-                if (w > 0.0f) atomicAdd(o + (sel != bid ? remap_lidx<Lay>(l, bid, sel) : l), w);
+                if (w <= 0.0f) continue;
+                if (os < 0) {
+                    g[0] += (double)w;
+                    g[1] += (double)e_center(d, ebin_of<Lay>(d, bid, l)) * (double)w;
+                    continue;
+                }
+                const int le = sel != bid ? remap_lidx<Lay>(l, bid, sel) : l;
+                atomicAdd(o + le, w);
+                const int Eb = ebin_of<Lay>(d, sel, le);
+                if (sel != bid && d.esplit)
+                    eshift += (double)((e_center(d, ebin_of<Lay>(d, bid, l)) - e_center(d, Eb)) * w);
+                g[4] += (double)w;
+                g[5] += (double)w * (double)e_center(d, Eb);
             }
+            eshift = warp_sum(eshift);
+            if (lane == 0 && eshift != 0.0) atomicAdd(d.dl_edep + src, eshift);
         }
     }
-}
-
-template <class Lay>
-__global__ void __launch_bounds__(kThreads) k_bucket_gather(Dev d) {
-    IterState* it = d.it;
-    if (it->halt) return;
-    const int lane = threadIdx.x & 31;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    const int out = it->parity ^ 1;
-    for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < d.Nc; cell += nw)
-        bucket_gather_cell<Lay>(d.buckets, d.bucket_bytes, d.c2b, d.bid[out], d.val[out], d.occ[out], cell, d.Nx, d.Nz,
-                                d.Ee, d.N_E, &it->drop_w, &it->drop_e, lane);
+    block_add<7>(g, &it->drop_w);
 }
 
 // ------------------------------------------------------------------ K5 + clear + K6
@@ -534,80 +725,81 @@ __device__ void finalize_audit(Dev& d) {
     it->last = r;
     it->iter = k + 1;
     it->include_source = 0;
+    it->occ_n[it->parity] = 0;   // the consumed buffer is empty again
     it->parity ^= 1;
     it->blocks_done = 0;
 }
 
-template <class Lay, bool BUCKET>
-__global__ void __launch_bounds__(kThreads) k_audit(Dev d) {
-    __shared__ double s_acc[3][kThreads / 32];
+// Fold this iteration's increment of tally k of cell c into the cumulative
+// tally; K5 books max(0, cumulative - previous) per cell (k5_audit.cu:93-99).
+__device__ __forceinline__ double fold_tally(const Dev& d, int c, int k) {
+    if (k < 4) {
+        double* cum = k == 0 ? d.edep : (k == 1 ? d.e_cut : (k == 2 ? d.e_nuc : d.e_bnd));
+        double* dl = k == 0 ? d.dl_edep : (k == 1 ? d.dl_ecut : (k == 2 ? d.dl_enuc : d.dl_ebnd));
+        const double x = dl[c];
+        if (x == 0.0) return 0.0;
+        const double e0 = cum[c], e1 = e0 + x;
+        cum[c] = e1;
+        dl[c] = 0.0;
+        return fmax(0.0, e1 - e0);
+    }
+    float* cum = k == 4 ? d.w_cut : (k == 5 ? d.w_nuc : d.w_bnd);
+    float* dl = k == 4 ? d.dl_wcut : (k == 5 ? d.dl_wnuc : d.dl_wbnd);
+    const float x = dl[c];
+    if (x == 0.0f) return 0.0;
+    const float w0 = cum[c], w1 = w0 + x;
+    cum[c] = w1;
+    dl[c] = 0.0f;
+    return (double)fmaxf(0.0f, w1 - w0);
+}
+
+// K5 audit of the iteration and clear of the consumed buffer, warp per
+// occupied cell of psi_in; the last block writes the audit record and swaps
+// the buffers (K6).
+template <class Lay>
+__global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
+    constexpr int NW = kThreads / 32;
+    __shared__ double s_acc[7][NW];
     __shared__ int s_last;
     IterState* it = d.it;
     if (it->halt) return;
-    const int in = it->parity, out = in ^ 1;
+    const int in = it->parity;
+    const int nocc = it->occ_n[in];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    const int cell0 = cell - lane;
-    const bool inb = cell < d.Nc;
-    unsigned bo = __ballot_sync(kFull, inb && d.occ[out][cell]);
-    unsigned bi = __ballot_sync(kFull, inb && d.occ[in][cell]);
-    double W = 0.0, E = 0.0, S = 0.0;
-    while (bo) {   // W/E of psi_out (k5_audit.cu:77-88)
-        const int c = cell0 + __ffs(bo) - 1;
-        bo &= bo - 1;
-        const uint32_t b = d.bid[out][(size_t)c * kKb + lane];
-        unsigned um = __ballot_sync(kFull, b != kEmpty);
-        S += (lane == 0) ? (double)__popc(um) : 0.0;
-        while (um) {
-            const int s = __ffs(um) - 1;
-            um &= um - 1;
-            const uint32_t bs = __shfl_sync(kFull, b, s);
-            const float* v = d.val[out] + ((size_t)c * kKb + s) * Lay::L;
-            for (int l = lane; l < Lay::L; l += 32) {
-                const float w = v[l];
-                if (w <= 0.0f) continue;
-                int Eb = (int)((bs >> 12) & 0xFFFu) * Lay::NE + (l / Lay::NT) % Lay::NE;
-                Eb = max(0, min(Eb, d.N_E - 1));
-                W += (double)w;
-                E += (double)w * (double)(d.Ee[Eb] + 1.0f * (0.5f * (d.Ee[Eb + 1] - d.Ee[Eb])));
-            }
-        }
-    }
-    while (bi) {   // clear the consumed buffer: only its claimed slots hold values
-        const int c = cell0 + __ffs(bi) - 1;
-        bi &= bi - 1;
+    const int nw = gridDim.x * NW;
+    double part = 0.0;   // lane k < 7: audit share of tally k (edep, e_cut, e_nuc, e_bnd, w_cut, w_nuc, w_bnd)
+    for (int wi = blockIdx.x * NW + wid; wi < nocc; wi += nw) {
+        const int c = d.occ_list[in][wi];
+        const int cls = d.cls[c];
         uint32_t* ids = d.bid[in] + (size_t)c * kKb;
-        const uint32_t b = ids[lane];
-        unsigned um = __ballot_sync(kFull, b != kEmpty);
-        while (um) {
-            const int s = __ffs(um) - 1;
-            um &= um - 1;
-            float4* v = reinterpret_cast<float4*>(d.val[in] + ((size_t)c * kKb + s) * Lay::L);
-            for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (cls == 0) {   // unlisted: its claimed slots hold no positive weight, clear what they hold
+            unsigned um = __ballot_sync(kFull, ids[lane] != kEmpty);
+            while (um) {
+                const int s = __ffs(um) - 1;
+                um &= um - 1;
+                float4* v = reinterpret_cast<float4*>(d.val[in] + ((size_t)c * kKb + s) * Lay::L);
+                for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        } else if (lane < 7) {
+            part += fold_tally(d, c, lane);
         }
         ids[lane] = kEmpty;
-        if (lane == 0) d.occ[in][c] = 0;
+        if (lane == 0) {
+            d.occ[in][c] = 0;
+            d.cls[c] = 0;
+            if (cls) d.c2b[c] = -1;
+        }
     }
-    if (BUCKET) {   // release the bucket map of this iteration's listed cells
-        const int n_co = it->n_coarse, n = n_co + it->n_active;
-        for (int i = cell; i < n; i += gridDim.x * blockDim.x)
-            d.c2b[i < n_co ? d.coarse[i] : d.active[i - n_co]] = -1;
-    }
-    W = warp_sum(W);
-    E = warp_sum(E);
-    S = warp_sum(S);
-    if (lane == 0) { s_acc[0][wid] = W; s_acc[1][wid] = E; s_acc[2][wid] = S; }
+    if (lane < 7) s_acc[lane][wid] = part;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0, b = 0, c = 0;
-        for (int w = 0; w < kThreads / 32; ++w) { a += s_acc[0][w]; b += s_acc[1][w]; c += s_acc[2][w]; }
-        if (a != 0.0) atomicAdd(&it->Wout, a);
-        if (b != 0.0) atomicAdd(&it->Eout, b);
-        if (c != 0.0) atomicAdd(&it->slots_out_it, c);
+    if (threadIdx.x < 7) {
+        double a = 0.0;
+        for (int w = 0; w < NW; ++w) a += s_acc[threadIdx.x][w];
+        if (a != 0.0) atomicAdd(&it->Edep + threadIdx.x, a);
         __threadfence();
-        const unsigned prev = atomicAdd(&it->blocks_done, 1u);
-        s_last = (prev == gridDim.x - 1);
     }
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&it->blocks_done, 1u) == gridDim.x - 1;
     __syncthreads();
     if (s_last && threadIdx.x == 0) {
         __threadfence();
@@ -620,13 +812,11 @@ __global__ void __launch_bounds__(kThreads) k_audit(Dev d) {
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_clear_all(Dev d) {
     const int lane = threadIdx.x & 31;
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    const int cell0 = cell - lane;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int b = 0; b < 2; ++b) {
-        unsigned bo = __ballot_sync(kFull, cell < d.Nc && d.occ[b][cell]);
-        while (bo) {
-            const int c = cell0 + __ffs(bo) - 1;
-            bo &= bo - 1;
+        const int n = d.it->occ_n[b];
+        for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
+            const int c = d.occ_list[b][wi];
             uint32_t* ids = d.bid[b] + (size_t)c * kKb;
             const uint32_t x = ids[lane];
             unsigned um = __ballot_sync(kFull, x != kEmpty);
@@ -637,15 +827,40 @@ __global__ void __launch_bounds__(kThreads) k_clear_all(Dev d) {
                 for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             ids[lane] = kEmpty;
-            if (lane == 0) d.occ[b][c] = 0;
+            if (lane == 0) { d.occ[b][c] = 0; d.cls[c] = 0; }
         }
     }
 }
 
 __global__ void k_reset_state(IterState* it) {
     if (threadIdx.x || blockIdx.x) return;
+    // the classification number runs on, one step past the last spot's, so
+    // that no cell reads as active in a previous classification; the claim
+    // pass number runs on too, and restarts after a wipe of the tables when
+    // it nears its 32-bit limit
+    const unsigned long long g = it->gen;
+    uint32_t tag = it->ctag;
+    const int ovf = it->cand_ovf, miss = it->cand_miss;
+    int wipe = 0;
+    if (tag >= 0xFFF00000u) {
+        tag = 0;
+        wipe = 1;
+    }
     memset(it, 0, sizeof(IterState));
+    it->gen = g + 1;
+    it->ctag = tag;
+    it->cand_ovf = ovf;
+    it->cand_miss = miss;
+    it->wipe = wipe;
     it->max_iter = INT_MAX;
+}
+
+// Clear every claim-table row when a tag wrap is pending (grid-stride).
+__global__ void k_wipe(Dev d, size_t n_words, int n_counts) {
+    if (!d.it->wipe) return;
+    const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, st = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = i0; i < n_words; i += st) d.ctab[i] = ~0ull;
+    for (size_t i = i0; i < (size_t)n_counts; i += st) d.ccount[i] = 0;
 }
 
 __global__ void k_set_iter_limit(IterState* it, int more) {
@@ -667,45 +882,6 @@ __global__ void k_source_finalize(IterState* it, const BeamArgs* b, int gaussian
     it->src_rep_loss = loss;
     it->include_source = 1;
     it->done = 0;
-}
-
-template <class Lay>
-__global__ void k_inject_dev(Dev d, const BeamArgs* bp, int gaussian) {
-    const BeamArgs b = *bp;
-    const int par = d.it->parity;
-    if (!gaussian) {
-        if (blockIdx.x || threadIdx.x) return;
-        const float xr = b.x0 - b.x_min, zr = b.z0 - b.z_min;
-        int cx = (int)(xr / d.dx), cz = (int)(zr / d.dz);
-        cx = cx < 0 ? 0 : (cx >= d.Nx ? d.Nx - 1 : cx);
-        cz = cz < 0 ? 0 : (cz >= d.Nz ? d.Nz - 1 : cz);
-        inject_one<Lay>(d, par, cz * d.Nx + cx, b.theta0, b.E0, b.W, xr - cx * d.dx, zr - cz * d.dz);
-        return;
-    }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
-    unsigned s = b.seed + (unsigned)i;
-    const float xs = b.x0 + b.sx * source_normal(s);
-    float ts = b.theta0 + b.sth * source_normal(s);
-    float Es = b.E0 + b.sE * source_normal(s);
-    Es = fmaxf(d.Ee[0], fminf(Es, d.Ee[d.N_E]));
-    ts = fmaxf(d.th[0], fminf(ts, d.th[d.N_theta]));
-    const float xr = xs - b.x_min, zr = b.z0 - b.z_min;
-    const int ix = (int)(xr / d.dx), iz = (int)(zr / d.dz);
-    const float ws = b.W / b.n;
-    IterState* it = d.it;
-    if (ix < 0 || ix >= d.Nx || iz < 0 || iz >= d.Nz) {
-        atomicAdd(&it->src_oog_w, ws);
-        atomicAdd(&it->src_oog_e, (double)(Es * ws));
-        return;
-    }
-    if (inject_one<Lay>(d, par, iz * d.Nx + ix, ts, Es, ws, xr - ix * d.dx, zr - iz * d.dz)) {
-        atomicAdd(&it->src_inj_w, ws);
-        atomicAdd(&it->src_inj_e, (double)(Es * ws));
-    } else {
-        atomicAdd(&it->src_slot_w, ws);
-        atomicAdd(&it->src_slot_e, (double)(Es * ws));
-    }
 }
 
 // Lateral MCS post-convolution of EdepC, one thread per output cell
@@ -787,13 +963,71 @@ __global__ void k_raw_compact(const uint8_t* mask, const uint32_t* bid, const fl
     if (threadIdx.x == 0) { *n_active = s_base[0]; *n_coarse = s_base[1]; }
 }
 
+// K4_BucketTransfer (k4_transfer.cu:174-333) over caller arrays: per
+// destination cell, pull the facing buckets of its four neighbours into
+// psi_out (claim with fallback, lidx remap, drop accounting).  Warp per
+// destination cell.
+template <class Lay>
+__device__ void bucket_gather_cell(const unsigned char* buckets, int bucket_bytes, const int* c2b, uint32_t* ids_out,
+                                   float* vals_out, int cell, int Nx, int Nz, const float* Ee, int N_E, double* drop_w,
+                                   double* drop_e, int lane) {
+    const int ix = cell % Nx, iz = cell / Nx;
+    for (int face = 0; face < 4; ++face) {
+        int src = -1;
+        if (face == 0 && iz > 0) src = cell - Nx;
+        if (face == 1 && iz + 1 < Nz) src = cell + Nx;
+        if (face == 2 && ix > 0) src = cell - 1;
+        if (face == 3 && ix + 1 < Nx) src = cell + 1;
+        if (src < 0) continue;
+        const int base = c2b[src];
+        if (base < 0) continue;
+        const unsigned char* b = buckets + (size_t)(base + face) * bucket_bytes;
+        const uint32_t sb = reinterpret_cast<const uint32_t*>(b)[lane];
+        unsigned um = __ballot_sync(kFull, sb != kEmpty);
+        const float* bv = reinterpret_cast<const float*>(b + 192);
+        while (um) {
+            const int s = __ffs(um) - 1;
+            um &= um - 1;
+            const uint32_t bid = __shfl_sync(kFull, sb, s);
+            int os = 0;
+            uint32_t sel = bid;
+            if (lane == 0) os = claim_slot(ids_out + (size_t)cell * kKb, bid, sel);
+            os = __shfl_sync(kFull, os, 0);
+            sel = __shfl_sync(kFull, sel, 0);
+            const float* v = bv + (size_t)s * Lay::L;
+            if (os < 0) {
+                double dw = 0.0, de = 0.0;
+                for (int l = lane; l < Lay::L; l += 32) {
+                    const float w = v[l];
+                    if (w > 0.0f) {
+                        int Eb = (int)((bid >> 12) & 0xFFFu) * Lay::NE + (l / Lay::NT) % Lay::NE;
+                        Eb = max(0, min(Eb, N_E - 1));
+                        const float E = Ee[Eb] + 1.0f * (0.5f * (Ee[Eb + 1] - Ee[Eb]));
+                        dw += (double)w;
+                        de += (double)E * (double)w;
+                    }
+                }
+                dw = warp_sum(dw);
+                de = warp_sum(de);
+                if (lane == 0) { atomicAdd(drop_w, dw); atomicAdd(drop_e, de); }
+                continue;
+            }
+            float* o = vals_out + ((size_t)cell * kKb + os) * Lay::L;
+            for (int l = lane; l < Lay::L; l += 32) {
+                const float w = v[l];
+                if (w > 0.0f) atomicAdd(o + (sel != bid ? remap_lidx<Lay>(l, bid, sel) : l), w);
+            }
+        }
+    }
+}
+
 template <class Lay>
 __global__ void k_raw_gather(const unsigned char* buckets, int bucket_bytes, const int* c2b, uint32_t* ids_out,
                              float* vals_out, int Nx, int Nz, const float* Ee, int N_E, double* drop) {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < Nx * Nz; cell += nw)
-        bucket_gather_cell<Lay>(buckets, bucket_bytes, c2b, ids_out, vals_out, nullptr, cell, Nx, Nz, Ee, N_E, drop,
+        bucket_gather_cell<Lay>(buckets, bucket_bytes, c2b, ids_out, vals_out, cell, Nx, Nz, Ee, N_E, drop,
                                 drop + 1, lane);
 }
 
@@ -890,6 +1124,14 @@ __global__ void k_raw_k5(RawK5 a, double* acc /* [11] + counter */, float s_oog_
     *rep = r;
 }
 
+// ------------------------------------------------------------------ diagnostics
+__global__ void k_math_eval(int fn, const float* __restrict__ x, float* __restrict__ y, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float v = x[i];
+    y[i] = fn == 0 ? sm2d_expf(v) : fn == 1 ? sm2d_logf(v) : fn == 2 ? sm2d_sinf(v) : fn == 3 ? sm2d_cosf(v) : sm2d_erff(v);
+}
+
 // ================================================================== engine
 struct Ctx {
     sm2d_problem p{};
@@ -902,9 +1144,10 @@ struct Ctx {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphConditionalHandle cond{};
-    cudaEvent_t ev[8] = {};
-    float step_ms[5] = {};
-    int nblk = 0, grid_transport = 0;
+    cudaEvent_t ev[10] = {};   // 0..7 one iteration's stages, 8..9 a whole run
+    float step_ms[7] = {};
+    int grid_cell = 0, grid_transport = 0;   // warp-per-cell kernels, transport
+    size_t ctab_words = 0;                   // claim-table size in 64-bit words
     bool injected = false;
     BeamArgs* beam_dev = nullptr;   // device copy of the current beam
     int* dose_half = nullptr;       // per-row half width of the lateral kernel
@@ -924,48 +1167,65 @@ static int dalloc(Ctx& c, void** p, size_t bytes) {
 
 template <class Lay>
 struct Impl {
-    static int launch_body(Ctx& c, bool timed, bool use_cond) {
-        const int nb = c.nblk;
-        if (timed) CK(cudaEventRecord(c.ev[0], c.s));
-        k_classify<Lay><<<nb, kThreads, 0, c.s>>>(c.d);
-        if (timed) CK(cudaEventRecord(c.ev[1], c.s));
-        k_compact<<<nb, kThreads, 0, c.s>>>(c.d, c.cond, use_cond ? 1 : 0);
-        if (timed) CK(cudaEventRecord(c.ev[2], c.s));
-        if (c.p.use_buckets) {
-            k_bucket_prep<Lay><<<c.d.Nc, kThreads, 0, c.s>>>(c.d);
-            k_transport<Lay, true><<<c.grid_transport, kThreads, 0, c.s>>>(c.d);
-            if (timed) CK(cudaEventRecord(c.ev[3], c.s));
-            k_bucket_gather<Lay><<<c.grid_transport, kThreads, 0, c.s>>>(c.d);
-        } else {
-            k_transport<Lay, false><<<c.grid_transport, kThreads, 0, c.s>>>(c.d);
-            if (timed) CK(cudaEventRecord(c.ev[3], c.s));
-        }
-        if (timed) CK(cudaEventRecord(c.ev[4], c.s));
-        if (c.p.use_buckets) k_audit<Lay, true><<<nb, kThreads, 0, c.s>>>(c.d);
-        else k_audit<Lay, false><<<nb, kThreads, 0, c.s>>>(c.d);
-        if (timed) CK(cudaEventRecord(c.ev[5], c.s));
+    // One iteration: K1 classify, (ascending lists on request), the claim
+    // pass of K2/K3, bucket and psi_out slot selection, the deposit pass of
+    // K2/K3 with the fused K4 scatter or the bucket pair, K5 finalize.
+    // ev[0..7] bracket: classify, lists, claim pass, selection, deposit pass,
+    // K4 bucket move, finalize.
+    static int launch_body(Ctx& c, bool timed, bool use_cond, bool lists) {
+        const int gc = c.grid_cell, gt = c.grid_transport;
+        const bool bk = c.p.use_buckets != 0;
+        auto rec = [&](int k) { return timed ? cudaEventRecord(c.ev[k], c.s) : cudaSuccess; };
+        CK(rec(0));
+        k_classify<Lay><<<gc, kThreads, 0, c.s>>>(c.d, c.cond, use_cond ? 1 : 0);
+        CK(rec(1));
+        if (lists) k_order_lists<<<1, 1024, 0, c.s>>>(c.d);
+        CK(rec(2));
+        k_transport<Lay, PASS_KEYS><<<gt, kThreads, 0, c.s>>>(c.d);
+        CK(rec(3));
+        if (bk) k_select_buckets<Lay, true><<<gc, kThreads, 0, c.s>>>(c.d);
+        else k_select_buckets<Lay, false><<<gc, kThreads, 0, c.s>>>(c.d);
+        k_select_psi<<<gc, kThreads, 0, c.s>>>(c.d, 1);
+        CK(rec(4));
+        if (bk) k_transport<Lay, PASS_BUCKET><<<gt, kThreads, 0, c.s>>>(c.d);
+        else k_transport<Lay, PASS_DIRECT><<<gt, kThreads, 0, c.s>>>(c.d);
+        CK(rec(5));
+        if (bk) k_bucket_push<Lay><<<gc, kThreads, 0, c.s>>>(c.d);
+        CK(rec(6));
+        k_finalize<Lay><<<gc, kThreads, 0, c.s>>>(c.d);
+        CK(rec(7));
         CK(cudaGetLastError());
         return 0;
     }
-    static int inject(Ctx& c, const BeamArgs& b, bool gaussian) {
-        if (gaussian) k_inject<Lay><<<(b.n + 255) / 256, 256, 0, c.s>>>(c.d, b, 1);
-        else k_inject<Lay><<<1, 32, 0, c.s>>>(c.d, b, 0);
-        CK(cudaGetLastError());
+    static int transport_grid(Ctx& c, int sms) {
+        int per_sm = 0;
+        cudaError_t e = c.p.use_buckets
+                            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_BUCKET>, kThreads, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_DIRECT>, kThreads, 0);
+        if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+        const long long items = (long long)c.d.Nc * kKb;   // one warp per item at most
+        const long long full = (long long)std::max(per_sm, 1) * std::max(sms, 1);
+        c.grid_transport = (int)std::max(1LL, std::min(full, (items + kThreads / 32 - 1) / (kThreads / 32)));
         return 0;
     }
     static int clear_all(Ctx& c, int) {
-        k_clear_all<Lay><<<c.nblk, kThreads, 0, c.s>>>(c.d);
+        k_clear_all<Lay><<<c.grid_cell, kThreads, 0, c.s>>>(c.d);
         CK(cudaGetLastError());
         return 0;
     }
+    // injection from the device beam description: claim pass, slot
+    // selection, deposit pass
     static int inject_dev(Ctx& c, int n, bool gaussian) {
-        if (gaussian) k_inject_dev<Lay><<<(n + 255) / 256, 256, 0, c.s>>>(c.d, c.beam_dev, 1);
-        else k_inject_dev<Lay><<<1, 32, 0, c.s>>>(c.d, c.beam_dev, 0);
+        const int blocks = gaussian ? (n + 255) / 256 : 1;
+        k_inject_begin<<<1, 1, 0, c.s>>>(c.d.it);
+        k_inject_keys<Lay><<<blocks, 256, 0, c.s>>>(c.d, c.beam_dev, gaussian ? 1 : 0);
+        k_select_psi<<<c.grid_cell, kThreads, 0, c.s>>>(c.d, 0);
+        k_inject_deposit<Lay><<<blocks, 256, 0, c.s>>>(c.d, c.beam_dev, gaussian ? 1 : 0);
         CK(cudaGetLastError());
         return 0;
     }
     static int totals(Ctx& c, int which) {
-        k_totals<Lay><<<c.nblk, kThreads, 0, c.s>>>(c.d, which);
+        k_totals<Lay><<<c.grid_cell, kThreads, 0, c.s>>>(c.d, which);
         CK(cudaGetLastError());
         return 0;
     }
@@ -996,7 +1256,7 @@ static int build_graph(Ctx& c) {
     CK(cudaGraphAddNode(&node, c.graph, nullptr, nullptr, 0, &np));
     cudaGraph_t body = np.conditional.phGraph_out[0];
     CK(cudaStreamBeginCaptureToGraph(c.s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    int rc = DISPATCH(c, launch_body, false, true);
+    int rc = DISPATCH(c, launch_body, false, true, false);
     cudaGraph_t captured = nullptr;
     cudaError_t e = cudaStreamEndCapture(c.s, &captured);
     if (rc) return rc;
@@ -1023,7 +1283,8 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     if (p->Nx <= 0 || p->Nz <= 0 || p->N_theta <= 0 || p->N_E <= 1 || !p->theta_edges || !p->E_edges)
         return fail(SM2D_ERR_ARG, "invalid grid");
     if (!(p->dx > 0.0f) || !(p->dz > 0.0f)) return fail(SM2D_ERR_ARG, "cell size must be positive");
-    if ((long long)p->Nx * p->Nz > (1LL << 30)) return fail(SM2D_ERR_ARG, "grid too large");
+    // work items pack (cell << 5) | slot into 32 bits
+    if ((long long)p->Nx * p->Nz > (1LL << 27)) return fail(SM2D_ERR_ARG, "grid too large (at most 2^27 cells)");
     int layout;
     if (p->nt_local == 4 && p->ne_local == 2 && p->nx_sub == 8 && p->nz_sub == 4) layout = 0;
     else if (p->nt_local == 8 && p->ne_local == 4 && p->nx_sub == 4 && p->nz_sub == 1) layout = 1;
@@ -1095,24 +1356,31 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     for (int b = 0; b < 2; ++b) {
         A(d.bid[b], uint32_t, ns);
         A(d.val[b], float, ns * c->L);
-        A(d.occ[b], uint8_t, Nc);
+        A(d.occ[b], int, Nc);
+        A(d.occ_list[b], int, Nc);
     }
     A(d.edep, double, Nc); A(d.e_cut, double, Nc); A(d.e_nuc, double, Nc); A(d.e_bnd, double, Nc);
     A(d.w_cut, float, Nc); A(d.w_nuc, float, Nc); A(d.w_bnd, float, Nc);
-    A(d.mask, uint8_t, Nc); A(d.cls, uint8_t, Nc);
+    A(d.dl_edep, double, Nc); A(d.dl_ecut, double, Nc); A(d.dl_enuc, double, Nc); A(d.dl_ebnd, double, Nc);
+    A(d.dl_wcut, float, Nc); A(d.dl_wnuc, float, Nc); A(d.dl_wbnd, float, Nc);
+    A(d.act_gen, unsigned long long, Nc); A(d.cls, uint8_t, Nc);
+    A(d.listed, uint32_t, Nc); A(d.items, uint32_t, ns);
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
-    c->nblk = (int)((Nc + kThreads - 1) / kThreads);
-    d.nblk = c->nblk;
-    A(d.blk, int, 2 * c->nblk);
     A(d.it, IterState, 1);
     d.hist_cap = p->max_iterations > 0 ? p->max_iterations : 4096;
     A(d.hist, sm2d_audit, d.hist_cap);
     d.bucket_bytes = bucket_bytes_for(c->L);
-    if (p->use_buckets) {
-        A(d.buckets, unsigned char, (size_t)Nc * 4 * d.bucket_bytes);
-        A(d.c2b, int, Nc);
-        if (cudaMemsetAsync(d.c2b, 0xFF, Nc * sizeof(int), c->s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "memset"));
-    }
+    if (p->use_buckets) A(d.buckets, unsigned char, (size_t)Nc * 4 * d.bucket_bytes);
+    A(d.c2b, int, Nc);
+    c->ctab_words = (size_t)5 * Nc * 2 * kCand;
+    A(d.ctab, unsigned long long, c->ctab_words);
+    A(d.ccount, int, 5 * Nc);
+    A(d.bkt_ids, uint32_t, (size_t)4 * Nc * kKb);
+    if (cudaMemsetAsync(d.c2b, 0xFF, Nc * sizeof(int), c->s) != cudaSuccess ||
+        cudaMemsetAsync(d.ctab, 0xFF, c->ctab_words * 8, c->s) != cudaSuccess ||
+        cudaMemsetAsync(d.ccount, 0, 5 * Nc * sizeof(int), c->s) != cudaSuccess ||
+        cudaMemsetAsync(d.bkt_ids, 0xFF, (size_t)4 * Nc * kKb * 4, c->s) != cudaSuccess)
+        return bail(fail(SM2D_ERR_CUDA, "memset"));
     A(c->beam_dev, BeamArgs, 1);
     {   // lateral post-convolution kernels per depth row
         std::vector<int> half(p->Nz, 0);
@@ -1148,12 +1416,15 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     for (int b = 0; b < 2 && ok; ++b)
         ok = cudaMemsetAsync(d.bid[b], 0xFF, ns * 4, s) == cudaSuccess &&
              cudaMemsetAsync(d.val[b], 0, ns * c->L * 4, s) == cudaSuccess &&
-             cudaMemsetAsync(d.occ[b], 0, Nc, s) == cudaSuccess;
+             cudaMemsetAsync(d.occ[b], 0, Nc * 4, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.edep, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_cut, 0, Nc * 8, s) == cudaSuccess &&
          cudaMemsetAsync(d.e_nuc, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_bnd, 0, Nc * 8, s) == cudaSuccess &&
          cudaMemsetAsync(d.w_cut, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.w_nuc, 0, Nc * 4, s) == cudaSuccess &&
-         cudaMemsetAsync(d.w_bnd, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.mask, 0, Nc, s) == cudaSuccess &&
-         cudaMemsetAsync(d.cls, 0, Nc, s) == cudaSuccess;
+         cudaMemsetAsync(d.w_bnd, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.act_gen, 0, Nc * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.cls, 0, Nc, s) == cudaSuccess && cudaMemsetAsync(d.dl_edep, 0, Nc * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.dl_ecut, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.dl_enuc, 0, Nc * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.dl_ebnd, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.dl_wcut, 0, Nc * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.dl_wnuc, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.dl_wbnd, 0, Nc * 4, s) == cudaSuccess;
     if (!ok) return bail(fail(SM2D_ERR_CUDA, "initial copies failed"));
     {   // grid origin of the beam description is fixed per problem
         BeamArgs origin{};
@@ -1166,7 +1437,8 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    c->grid_transport = std::max(1, std::min((int)((Nc + 7) / 8), 8 * std::max(sms, 1)));
+    c->grid_cell = std::max(1, std::min((int)((Nc + kThreads / 32 - 1) / (kThreads / 32)), 4 * std::max(sms, 1)));
+    if ((rc = DISPATCH(*c, transport_grid, sms))) return bail(rc);
     if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "create sync"));
     *out = c;
     return 0;
@@ -1194,30 +1466,10 @@ int sm2d_inject(sm2d_handle h, const sm2d_beam* b) {
     Ctx& c = *h;
     int rc = sync_state(c);
     if (rc) return rc;
-    const bool gaussian = (b->n_samples > 1) || (b->sigma_x > 0.0f) || (b->sigma_theta > 0.0f);  // wrapper.cu:246
-    if (gaussian && b->n_samples <= 0) return fail(SM2D_ERR_ARG, "n_samples must be positive");
-    IterState& it = *c.it_host;
-    it.src_inj_w = it.src_oog_w = it.src_slot_w = 0.0f;
-    it.src_inj_e = it.src_oog_e = it.src_slot_e = 0.0;
-    it.tot_w = it.tot_e = 0.0;
-    if ((rc = push_state(c))) return rc;
-    BeamArgs a{b->x0, b->z0, b->theta0, b->E0, b->W_total, b->sigma_x, b->sigma_theta, b->sigma_E,
-               c.p.x_min, c.p.z_min, b->n_samples, b->seed};
-    if ((rc = DISPATCH(c, inject, a, gaussian))) return rc;
-    if ((rc = DISPATCH(c, totals, 0))) return rc;
-    if ((rc = sync_state(c))) return rc;
-    if (!gaussian) {
-        it.src_inj_w = b->W_total;
-        it.src_inj_e = (double)b->E0 * (double)b->W_total;
-    }
-    double loss = it.src_inj_e - it.tot_e;
-    if (std::fabs(loss) < 1e-12) loss = 0.0;
-    it.src_rep_loss = loss;
-    it.include_source = 1;
-    it.done = 0;
-    if ((rc = push_state(c))) return rc;
+    if (c.it_host->occ_n[c.it_host->parity] != 0)
+        return fail(SM2D_ERR_STATE, "phase space not empty: call sm2d_reset before injecting");
+    if ((rc = sm2d_inject_async(h, b))) return rc;
     CK(cudaStreamSynchronize(c.s));
-    c.injected = true;
     return 0;
 }
 
@@ -1228,12 +1480,20 @@ int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
     if (rc) return rc;
     const int par = c.it_host->parity;
     const size_t ns = (size_t)c.d.Nc * kKb;
-    std::vector<uint8_t> occ(c.d.Nc, 0);
-    for (size_t i = 0; i < ns; ++i)
-        if (bid[i] != kEmpty) occ[i / kKb] = 1;
+    std::vector<int> occ(c.d.Nc, 0), list;
+    for (int cell = 0; cell < c.d.Nc; ++cell)
+        for (int k = 0; k < kKb; ++k)
+            if (bid[(size_t)cell * kKb + k] != kEmpty) {
+                occ[cell] = 1;
+                list.push_back(cell);
+                break;
+            }
     CK(cudaMemcpyAsync(c.d.bid[par], bid, ns * 4, cudaMemcpyHostToDevice, c.s));
     CK(cudaMemcpyAsync(c.d.val[par], val, ns * c.L * 4, cudaMemcpyHostToDevice, c.s));
-    CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), c.d.Nc, cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, c.s));
+    if (!list.empty())
+        CK(cudaMemcpyAsync(c.d.occ_list[par], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, c.s));
+    c.it_host->occ_n[par] = (int)list.size();
     c.it_host->done = 0;
     if ((rc = push_state(c))) return rc;
     CK(cudaStreamSynchronize(c.s));
@@ -1258,13 +1518,11 @@ int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse) {
     if (!h) return fail(SM2D_ERR_ARG, "null handle");
     Ctx& c = *h;
     if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space: call sm2d_inject or sm2d_set_psi_in first");
-    int rc = DISPATCH(c, launch_body, true, false);
+    int rc = DISPATCH(c, launch_body, true, false, true);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
-    float ms[5];
-    for (int k = 0; k < 5; ++k) CK(cudaEventElapsedTime(&ms[k], c.ev[k], c.ev[k + 1]));
-    // ms: classify, compact, transport(+bucket prep), K4 gather, audit
-    for (int k = 0; k < 5; ++k) c.step_ms[k] = ms[k];
+    // classify, lists, claim pass, selection, deposit pass, K4 bucket move, finalize
+    for (int k = 0; k < 7; ++k) CK(cudaEventElapsedTime(&c.step_ms[k], c.ev[k], c.ev[k + 1]));
     if (n_active) *n_active = c.it_host->done ? 0 : c.it_host->n_active;
     if (n_coarse) *n_coarse = c.it_host->done ? 0 : c.it_host->n_coarse;
     return 0;
@@ -1279,11 +1537,11 @@ static int run_impl(Ctx& c, int max_it, int* done_iters, float* ms) {
     const int start = c.it_host->iter;
     c.it_host->max_iter = start + max_it;
     if ((rc = push_state(c))) return rc;
-    if (ms) CK(cudaEventRecord(c.ev[6], c.s));
+    if (ms) CK(cudaEventRecord(c.ev[8], c.s));
     CK(cudaGraphLaunch(c.exec, c.s));
-    if (ms) CK(cudaEventRecord(c.ev[7], c.s));
+    if (ms) CK(cudaEventRecord(c.ev[9], c.s));
     CK(cudaStreamSynchronize(c.s));
-    if (ms) CK(cudaEventElapsedTime(ms, c.ev[6], c.ev[7]));
+    if (ms) CK(cudaEventElapsedTime(ms, c.ev[8], c.ev[9]));
     if ((rc = sync_state(c))) return rc;
     c.it_host->max_iter = INT_MAX;
     if ((rc = push_state(c))) return rc;
@@ -1304,9 +1562,13 @@ int sm2d_run_timed(sm2d_handle h, int max_it, int* done_iters, float* ms) {
 
 int sm2d_get_mask(sm2d_handle h, uint8_t* mask) {
     if (!h || !mask) return fail(SM2D_ERR_ARG, "null argument");
-    CK(cudaMemcpyAsync(mask, h->d.mask, h->d.Nc, cudaMemcpyDeviceToHost, h->s));
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    std::vector<unsigned long long> g(h->d.Nc);
+    CK(cudaMemcpyAsync(g.data(), h->d.act_gen, sizeof(unsigned long long) * g.size(), cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
-    for (int i = 0; i < h->d.Nc; ++i) mask[i] &= 1;
+    const unsigned long long cur = h->it_host->gen;
+    for (int i = 0; i < h->d.Nc; ++i) mask[i] = (cur != 0 && g[i] == cur) ? 1 : 0;
     return 0;
 }
 
@@ -1365,6 +1627,7 @@ int sm2d_get_scalars(sm2d_handle h, double* o) {
     o[3] = it.src_inj_w; o[4] = it.src_inj_e; o[5] = it.src_oog_w; o[6] = it.src_oog_e;
     o[7] = it.src_slot_w; o[8] = it.src_slot_e; o[9] = it.src_rep_loss;
     o[10] = it.iter; o[11] = it.cell_steps; o[12] = it.slots_in; o[13] = it.slots_out;
+    o[14] = it.cand_ovf; o[15] = it.cand_miss;
     return 0;
 }
 
@@ -1409,9 +1672,9 @@ int sm2d_reset(sm2d_handle h) {
     CK(cudaMemsetAsync(c.d.w_cut, 0, n * 4, c.s));
     CK(cudaMemsetAsync(c.d.w_nuc, 0, n * 4, c.s));
     CK(cudaMemsetAsync(c.d.w_bnd, 0, n * 4, c.s));
-    CK(cudaMemsetAsync(c.d.mask, 0, n, c.s));
     CK(cudaMemsetAsync(c.d.cls, 0, n, c.s));
     k_reset_state<<<1, 1, 0, c.s>>>(c.d.it);
+    k_wipe<<<c.grid_cell, kThreads, 0, c.s>>>(c.d, c.ctab_words, 5 * c.d.Nc);
     CK(cudaGetLastError());
     c.injected = false;
     return 0;
@@ -1458,44 +1721,45 @@ int sm2d_dose_async(sm2d_handle h, double* host_dose) {
     return 0;
 }
 
-int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms5, int* launches) {
-    if (!h || !ms5 || n <= 0) return fail(SM2D_ERR_ARG, "invalid argument");
+int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* launches) {
+    if (!h || !ms7 || n <= 0) return fail(SM2D_ERR_ARG, "invalid argument");
     Ctx& c = *h;
     if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space");
     int rc = sync_state(c);
     if (rc) return rc;
     const int start = c.it_host->iter;
-    const size_t need = (size_t)6 * n;
+    constexpr int E = 8;   // events per iteration
+    const size_t need = (size_t)E * n;
     while (c.pev.size() < need) {
         cudaEvent_t e;
         CK(cudaEventCreate(&e));
         c.pev.push_back(e);
     }
-    cudaEvent_t saved[8];
+    cudaEvent_t saved[E];
     memcpy(saved, c.ev, sizeof saved);
     for (int i = 0; i < n; ++i) {
-        for (int k = 0; k < 6; ++k) c.ev[k] = c.pev[6 * i + k];
-        if ((rc = DISPATCH(c, launch_body, true, false))) break;
+        for (int k = 0; k < E; ++k) c.ev[k] = c.pev[(size_t)E * i + k];
+        if ((rc = DISPATCH(c, launch_body, true, false, false))) break;
     }
     memcpy(c.ev, saved, sizeof saved);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
     const int done = c.it_host->iter - start;
-    for (int k = 0; k < 5; ++k) ms5[k] = 0.0f;
+    for (int k = 0; k < E - 1; ++k) ms7[k] = 0.0f;
     for (int i = 0; i < done; ++i)
-        for (int k = 0; k < 5; ++k) {
+        for (int k = 0; k < E - 1; ++k) {
             float t = 0.0f;
-            CK(cudaEventElapsedTime(&t, c.pev[6 * i + k], c.pev[6 * i + k + 1]));
-            ms5[k] += t;
+            CK(cudaEventElapsedTime(&t, c.pev[(size_t)E * i + k], c.pev[(size_t)E * i + k + 1]));
+            ms7[k] += t;
         }
     if (done_iters) *done_iters = done;
-    if (launches) *launches = done * (c.p.use_buckets ? 6 : 4);
+    if (launches) *launches = done * (c.p.use_buckets ? 7 : 6);
     return 0;
 }
 
-int sm2d_get_step_timing(sm2d_handle h, float* ms5) {
-    if (!h || !ms5) return fail(SM2D_ERR_ARG, "null argument");
-    memcpy(ms5, h->step_ms, sizeof h->step_ms);
+int sm2d_get_step_timing(sm2d_handle h, float* ms7) {
+    if (!h || !ms7) return fail(SM2D_ERR_ARG, "null argument");
+    memcpy(ms7, h->step_ms, sizeof h->step_ms);
     return 0;
 }
 
@@ -1594,6 +1858,24 @@ int sm2d_k5_conservation_audit(const uint32_t* bid_in, const float* val_in, cons
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     return 0;
+}
+
+// ---------------------------------------------------------------- diagnostics
+int sm2d_math_eval(int fn, const float* x, float* y, int n) {
+    if (!x || !y || n < 0 || fn < 0 || fn > 4) return fail(SM2D_ERR_ARG, "invalid argument");
+    if (n == 0) return 0;
+    float* buf = nullptr;
+    CK(cudaMalloc(&buf, sizeof(float) * 2 * (size_t)n));
+    int rc = 0;
+    if (cudaMemcpy(buf, x, sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "copy");
+    if (!rc) {
+        k_math_eval<<<(n + 255) / 256, 256>>>(fn, buf, buf + n, n);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(y, buf + n, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = fail(SM2D_ERR_CUDA, "math kernel");
+    }
+    cudaFree(buf);
+    return rc;
 }
 
 }  // extern "C"

@@ -9,23 +9,37 @@
 // hashed Vavilov straggling.  Both apply nuclear attenuation and one hashed
 // MCS angle sample, then either cross a face or stay in the cell.
 //
-// Emission is written through a Sink:
-//   * direct mode scatters straight into psi_out of the destination cell
-//     (the neighbour-scatter form of K4 fused into the transport kernel);
-//   * bucket mode writes the reference's DeviceOutflowBucket of the source
-//     cell and face; sm2d_k4_gather then moves it (K4_BucketTransfer).
+// Every bin is transported twice with the same arithmetic.  PASS_KEYS
+// gathers, per psi_out cell and per outflow bucket, the block ids aimed at
+// it with their sequential claim keys (see the claim tables in
+// sm2d_device.cuh); the selection kernels then fix each container's slots.
+// The deposit pass resolves every emission to its slot and adds the weight:
+//   * PASS_DIRECT scatters straight into psi_out of the destination cell
+//     (the neighbour-scatter form of K4 fused into the transport kernel,
+//     through the bucket's kept id as K4 would);
+//   * PASS_BUCKET writes the reference's DeviceOutflowBucket of the source
+//     cell and face; the bucket move kernel then runs K4_BucketTransfer.
 #pragma once
 #include "sm2d_device.cuh"
 
 namespace sm2d {
 
 enum { FACE_ZP = 0, FACE_ZM = 1, FACE_XP = 2, FACE_XM = 3 };
+enum { PASS_KEYS = 0, PASS_DIRECT = 1, PASS_BUCKET = 2 };
 
-struct Tally {                // per-lane accumulators of one cell
+struct Tally {                // per-lane accumulators of one work item
     double edep, e_cut, e_nuc, e_bnd;
     float w_cut, w_nuc, w_bnd;
     double drop_w, drop_e;    // slot / bucket / prune drops
-    double Win, Ein;          // psi_in weight and energy of the cell
+    double Win, Ein;          // psi_in weight and energy of the bins read
+    double Wout, Eout;        // weight and bin-centre energy deposited in psi_out
+};
+
+// The component being transported: its cell, psi_in slot and local bin give
+// the sequential claim order; k3 selects the batch.
+struct Src {
+    int cell, slot, lidx, k3;
+    uint32_t tag;   // classification number of this pass
 };
 
 __device__ __forceinline__ float e_center(const Dev& d, int b) { return d.Ee[b] + 0.5f * (d.Ee[b + 1] - d.Ee[b]); }
@@ -66,45 +80,96 @@ __device__ __forceinline__ EParts bin_energy(const Dev& d, float E, float w) {
     return p;
 }
 
-template <class Lay, bool BUCKET>
-struct Sink {
-    // Place weight w of local bin lidx of block `want`: bucket (bcell, face)
-    // in bucket mode, psi_out of dcell in direct mode.  Returns the weight
-    // that found no slot.
-    __device__ __forceinline__ static float put(const Dev& d, int par, int bcell, int face, int dcell,
-                                                uint32_t want, int lidx, float w, double& eshift) {
-        uint32_t* ids;
-        float* vals;
-        if (BUCKET) {
-            int base = d.c2b[bcell];
-            if (base < 0) return w;
-            unsigned char* b = d.buckets + (size_t)(base + face) * d.bucket_bytes;
-            ids = bucket_ids(b);
-            vals = bucket_vals(b);
-        } else {
-            ids = d.bid[par ^ 1] + (size_t)dcell * kKb;
-            vals = d.val[par ^ 1] + (size_t)dcell * kKb * Lay::L;
+__device__ __forceinline__ unsigned long long* psi_row(const Dev& d, int cell) {
+    return d.ctab + (size_t)cell * (2 * kCand);
+}
+__device__ __forceinline__ unsigned long long* bucket_row(const Dev& d, int bf) {
+    return d.ctab + (size_t)(d.Nc + bf) * (2 * kCand);
+}
+// claim keys: psi_out rows [batch:1][part:3][slot:5][lidx:8][part index:1]
+// (part 0 in-cell deposit, 1 + f the K4 transfer of face f by bucket slot);
+// bucket rows [emitting column 0..10:4][slot:5][lidx:8][emission index:2]
+__device__ __forceinline__ uint32_t stay_key(int k3, int slot, int lidx, int ei) {
+    return ((uint32_t)k3 << 17) | ((uint32_t)slot << 9) | ((uint32_t)lidx << 1) | (uint32_t)ei;
+}
+__device__ __forceinline__ uint32_t k4_key(int k3, int face, int kslot) {
+    return ((uint32_t)k3 << 17) | ((uint32_t)(1 + face) << 14) | (uint32_t)kslot;
+}
+__device__ __forceinline__ uint32_t bucket_key(int col, int slot, int lidx, int seq) {
+    return ((uint32_t)col << 15) | ((uint32_t)slot << 10) | ((uint32_t)lidx << 2) | (uint32_t)seq;
+}
+template <class Lay>
+__device__ __forceinline__ int ebin_of(const Dev& d, uint32_t bid, int l) {
+    return max(0, min((int)((bid >> 12) & 0xFFFu) * Lay::NE + (l / Lay::NT) % Lay::NE, d.N_E - 1));
+}
+
+// Slot of block `want` in a selected container and the kept id there (want
+// itself or the nearest kept id it folds into).  An id that was not
+// gathered (claim-table overflow) takes the nearest kept id and is counted.
+__device__ __forceinline__ int resolve(const Dev& d, const unsigned long long* row, const uint32_t* kept, uint32_t tag,
+                                       uint32_t want, uint32_t& sel) {
+    int s = cand_find(row, tag, want);
+    if (s < 0) {
+        atomicAdd(&d.it->cand_miss, 1);
+        int bd = 0x7fffffff;
+        for (int k = 0; k < kKb; ++k) {
+            const uint32_t x = kept[k];
+            if (x == kEmpty) continue;
+            const int dd = bid_distance(x, want);
+            if (dd < bd) { bd = dd; s = k; }
         }
-        uint32_t sel;
-        int s = claim_slot(ids, want, sel);
-        if (s < 0) return w;
-        if (!BUCKET) d.occ[par ^ 1][dcell] = 1;
-        int le = (sel == want) ? lidx : remap_lidx<Lay>(lidx, want, sel);
-        if (sel != want && d.esplit) {   // split method: a re-binned part keeps its energy
-            const int e0 = (int)((want >> 12) & 0xFFFu) * Lay::NE + (lidx / Lay::NT) % Lay::NE;
-            const int e1 = (int)((sel >> 12) & 0xFFFu) * Lay::NE + (le / Lay::NT) % Lay::NE;
-            eshift += (double)((e_center(d, e0) - e_center(d, e1)) * w);
-        }
-        atomicAdd(vals + (size_t)s * Lay::L + le, w);
+        if (s < 0) { sel = want; return -1; }
+    }
+    sel = kept[s];
+    return s;
+}
+
+// Weight w of local bin lidx of block `want` leaving through bucket
+// (bcell, face) towards dcell; col is the emitting column seen from bcell
+// (0..10, 5 = bcell itself) and seq the emission index within the bin.
+// Returns the weight that found no container.
+template <class Lay, int PASS>
+__device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int bcell, int face, int dcell, int col,
+                                     int seq, uint32_t want, int lidx, float w, Tally& t) {
+    const int base = d.c2b[bcell];
+    if (base < 0) return w;
+    const int bf = base + face;
+    if (PASS == PASS_KEYS) {
+        cand_insert(bucket_row(d, bf), d.ccount + d.Nc + bf, src.tag, want, bucket_key(col, src.slot, src.lidx, seq),
+                    &d.it->cand_ovf);
         return 0.0f;
     }
-};
+    uint32_t selb;
+    const int kb = resolve(d, bucket_row(d, bf), d.bkt_ids + (size_t)bf * kKb, src.tag, want, selb);
+    if (kb < 0) return w;
+    const int le = (selb == want) ? lidx : remap_lidx<Lay>(lidx, want, selb);
+    if (selb != want && d.esplit)   // split method: a re-binned part keeps its energy
+        t.edep += (double)((e_center(d, ebin_of<Lay>(d, want, lidx)) - e_center(d, ebin_of<Lay>(d, selb, le))) * w);
+    if (PASS == PASS_BUCKET) {
+        float* vals = bucket_vals(d.buckets + (size_t)bf * d.bucket_bytes);
+        atomicAdd(vals + (size_t)kb * Lay::L + le, w);
+        return 0.0f;
+    }
+    // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
+    const int out = par ^ 1;
+    uint32_t seld;
+    const int os = resolve(d, psi_row(d, dcell), d.bid[out] + (size_t)dcell * kKb, src.tag, selb, seld);
+    if (os < 0) return w;
+    const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
+    const int e2 = ebin_of<Lay>(d, seld, le2);
+    if (seld != selb && d.esplit)
+        atomicAdd(d.dl_edep + bcell, (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, e2)) * w));
+    atomicAdd(d.val[out] + ((size_t)dcell * kKb + os) * Lay::L + le2, w);
+    t.Wout += (double)w;
+    t.Eout += (double)w * (double)e_center(d, e2);
+    return 0.0f;
+}
 
 // Two-bin theta split around the nearest bin centre with frac^2 weight to
-// the neighbour, energy re-binning, slot claim (device_bucket.cuh:431-533).
-template <class Lay, bool BUCKET>
-__device__ float emit_component(const Dev& d, int par, int bcell, int face, int dcell, float theta, float E,
-                                float weight, int xs, int zs, double& eshift) {
+// the neighbour, energy re-binning, bucket claim (device_bucket.cuh:431-533).
+template <class Lay, int PASS>
+__device__ float emit_component(const Dev& d, const Src& src, int par, int bcell, int face, int dcell, int col,
+                                float theta, float E, float weight, int xs, int zs, Tally& t) {
     if (weight <= 0.0f) return 0.0f;
     const float tmin = d.th[0], tmax = d.th[d.N_theta];
     const float dth = (tmax - tmin) / (float)d.N_theta;
@@ -139,7 +204,7 @@ __device__ float emit_component(const Dev& d, int par, int bcell, int face, int 
             const int tb = ti ? tb1 : bc;
             const uint32_t want = make_bid((uint32_t)(tb / Lay::NT), bE);
             const int l = Lay::enc(tb % Lay::NT, El, xs, zs);
-            dropped += Sink<Lay, BUCKET>::put(d, par, bcell, face, dcell, want, l, we, eshift);
+            dropped += put<Lay, PASS>(d, src, par, bcell, face, dcell, col, 2 * ei + ti, want, l, we, t);
         }
     }
     return dropped;
@@ -148,9 +213,9 @@ __device__ float emit_component(const Dev& d, int par, int bcell, int face, int 
 // +z crossing with the N-cell lateral Gaussian split: the share of column
 // ix+k goes through the +z bucket of cell (ix+k, iz) to cell (ix+k, iz+1)
 // (device_bucket.cuh:857-987).
-template <class Lay, bool BUCKET>
-__device__ float emit_forward(const Dev& d, int par, int src, int my_cls, float theta, float E, float weight,
-                              float xoff, float sigma, float& boundary_w, double& eshift) {
+template <class Lay, int PASS>
+__device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int my_cls, float theta, float E,
+                              float weight, float xoff, float sigma, float& boundary_w, Tally& t) {
     if (weight <= 0.0f) return 0.0f;
     constexpr int N = 11;
     sigma = fmaxf(sigma, 1e-6f);
@@ -193,8 +258,8 @@ __device__ float emit_forward(const Dev& d, int par, int src, int my_cls, float 
         // in the same pass (k1k6_pipeline.cu:800-847 maps one list at a time)
         if (ecell != src && d.cls[ecell] != my_cls) { dropped += weight * wf; continue; }
         const int xt = off < 0 ? Lay::NX - 1 : (off > 0 ? 0 : Lay::NX / 2);
-        dropped += emit_component<Lay, BUCKET>(d, par, ecell, FACE_ZP, ecell + d.Nx, theta, E, weight * wf, xt, 0,
-                                               eshift);
+        dropped += emit_component<Lay, PASS>(d, sc, par, ecell, FACE_ZP, ecell + d.Nx, N - 1 - i, theta, E,
+                                             weight * wf, xt, 0, t);
     }
     return dropped;
 }
@@ -203,77 +268,97 @@ __device__ float emit_forward(const Dev& d, int par, int src, int my_cls, float 
 // sub-bins, send Gaussian tails past the cell edges to the lateral
 // neighbours, fold the re-binning energy error into the deposit
 // (k2_coarsetransport.cu:460-690, k3_finetransport.cu:504-747).
-template <class Lay, bool BUCKET>
-__device__ void emit_stay(const Dev& d, int par, bool k3, int cell, float theta_new, float E_new, float w_new,
-                          float x_new, float z_new, float sig_sub, float sig_cell, Tally& t) {
+template <class Lay, int PASS>
+__device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cell, float theta_new, float E_new,
+                          float w_new, float x_new, float z_new, float sig_sub, float sig_cell, Tally& t) {
     const float dx = d.dx, dz = d.dz;
     const float tmin = d.th[0], tmax = d.th[d.N_theta];
     const float dth = (tmax - tmin) / (float)d.N_theta;
     int tbn = (int)((theta_new - tmin) / dth);
     tbn = (int)fmaxf(0.0f, fminf((float)tbn, (float)(d.N_theta - 1)));
     const EParts ep = bin_energy(d, E_new, w_new);
-    float w[Lay::NX];
-    {
-        const float sg = fmaxf(sig_sub, 1e-6f);
-        const float dxs = dx / (float)Lay::NX;
-        const float xmin = -dx * 0.5f;
-        float prev = gauss_cdf(xmin, x_new, sg);
-        for (int i = 0; i < Lay::NX; ++i) {
-            float cur = gauss_cdf(xmin + (float)(i + 1) * dxs, x_new, sg);
-            w[i] = cur - prev;
-            prev = cur;
-        }
-        float s = 0.0f;
-        for (int i = 0; i < Lay::NX; ++i) s += w[i];
-        if (s > 1e-10f) {
-            for (int i = 0; i < Lay::NX; ++i) w[i] /= s;
-        } else {
-            for (int i = 0; i < Lay::NX; ++i) w[i] = (i == Lay::NX / 2) ? 1.0f : 0.0f;
-        }
-    }
     const int ix = cell % d.Nx;
     const int zst = sub_bin(z_new, dz, Lay::NZ);
     const float lb = -dx * 0.5f, rb = dx * 0.5f;
     const float win = gauss_cdf(rb, x_new, sig_cell) - gauss_cdf(lb, x_new, sig_cell);
     const float wcf = fminf(1.0f, fmaxf(0.0f, win));
-    float wsum = 0.0f;
-    for (int i = 0; i < Lay::NX; ++i) { w[i] = fmaxf(0.0f, w[i]); wsum += w[i]; }
-    if (wsum < 1e-12f) {
-        for (int i = 0; i < Lay::NX; ++i) w[i] = 0.0f;
-        w[Lay::NX / 2] = 1.0f;
-        wsum = 1.0f;
-    }
     const int outp = par ^ 1;
-    uint32_t* ids = d.bid[outp] + (size_t)cell * kKb;
-    float* vals = d.val[outp] + (size_t)cell * kKb * Lay::L;
     float E_emit = ep.Erep;
-    for (int ei = 0; ei < ep.n; ++ei) {
-        const int Eb = ep.bin[ei];
-        const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
-        uint32_t sel;
-        const int os = claim_slot(ids, want, sel);
-        const float wpart = d.esplit ? w_new * ep.frac[ei] : w_new;
-        if (os < 0) {
-            t.drop_w += (double)wpart;
-            t.drop_e += (double)(E_new * wpart);
-            if (!d.esplit) return;
-            continue;
+    if (PASS == PASS_KEYS) {
+        for (int ei = 0; ei < ep.n; ++ei) {
+            const int Eb = ep.bin[ei];
+            const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
+            cand_insert(psi_row(d, cell), d.ccount + cell, sc.tag, want, stay_key(sc.k3, sc.slot, sc.lidx, ei),
+                        &d.it->cand_ovf);
         }
-        d.occ[outp][cell] = 1;
-        int tbe = tbn, Ebe = Eb;
-        if (sel != want) {
-            const int t0 = (int)(sel & 0xFFFu) * Lay::NT, e0 = (int)((sel >> 12) & 0xFFFu) * Lay::NE;
-            tbe = max(t0, min(tbe, t0 + Lay::NT - 1));
-            Ebe = max(e0, min(Ebe, e0 + Lay::NE - 1));
+        mark_occupied(d, outp, cell);
+    } else {
+        float w[Lay::NX];
+        {
+            const float sg = fmaxf(sig_sub, 1e-6f);
+            const float dxs = dx / (float)Lay::NX;
+            const float xmin = -dx * 0.5f;
+            float prev = gauss_cdf(xmin, x_new, sg);
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) {
+                float cur = gauss_cdf(xmin + (float)(i + 1) * dxs, x_new, sg);
+                w[i] = cur - prev;
+                prev = cur;
+            }
+            float s = 0.0f;
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) s += w[i];
+            if (s > 1e-10f) {
+#pragma unroll
+                for (int i = 0; i < Lay::NX; ++i) w[i] /= s;
+            } else {
+#pragma unroll
+                for (int i = 0; i < Lay::NX; ++i) w[i] = (i == Lay::NX / 2) ? 1.0f : 0.0f;
+            }
         }
-        if (!d.esplit) E_emit = e_center(d, Ebe);
-        else if (Ebe != Eb) t.edep += (double)((e_center(d, Eb) - e_center(d, Ebe)) * wpart * wcf);
-        const int tl = tbe % Lay::NT, El = Ebe % Lay::NE;
-        float* vs = vals + (size_t)os * Lay::L;
-        for (int xs = 0; xs < Lay::NX; ++xs) {
-            const float wf = (w[xs] / wsum) * wcf;
-            if (wf <= 0.0f) continue;
-            atomicAdd(vs + Lay::enc(tl, El, xs, zst), wpart * wf);
+        float wsum = 0.0f;
+#pragma unroll
+        for (int i = 0; i < Lay::NX; ++i) { w[i] = fmaxf(0.0f, w[i]); wsum += w[i]; }
+        if (wsum < 1e-12f) {
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) w[i] = 0.0f;
+            w[Lay::NX / 2] = 1.0f;
+            wsum = 1.0f;
+        }
+        const uint32_t* kept = d.bid[outp] + (size_t)cell * kKb;
+        float* vals = d.val[outp] + (size_t)cell * kKb * Lay::L;
+        for (int ei = 0; ei < ep.n; ++ei) {
+            const int Eb = ep.bin[ei];
+            const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
+            uint32_t sel;
+            const int os = resolve(d, psi_row(d, cell), kept, sc.tag, want, sel);
+            const float wpart = d.esplit ? w_new * ep.frac[ei] : w_new;
+            if (os < 0) {
+                t.drop_w += (double)wpart;
+                t.drop_e += (double)(E_new * wpart);
+                if (!d.esplit) return;
+                continue;
+            }
+            int tbe = tbn, Ebe = Eb;
+            if (sel != want) {
+                const int t0 = (int)(sel & 0xFFFu) * Lay::NT, e0 = (int)((sel >> 12) & 0xFFFu) * Lay::NE;
+                tbe = max(t0, min(tbe, t0 + Lay::NT - 1));
+                Ebe = max(e0, min(Ebe, e0 + Lay::NE - 1));
+            }
+            if (!d.esplit) E_emit = e_center(d, Ebe);
+            else if (Ebe != Eb) t.edep += (double)((e_center(d, Eb) - e_center(d, Ebe)) * wpart * wcf);
+            const int tl = tbe % Lay::NT, El = Ebe % Lay::NE;
+            float* vs = vals + (size_t)os * Lay::L;
+            const double Ec_out = (double)e_center(d, max(0, min(Ebe, d.N_E - 1)));
+#pragma unroll
+            for (int xs = 0; xs < Lay::NX; ++xs) {
+                const float wf = (w[xs] / wsum) * wcf;
+                if (wf <= 0.0f) continue;
+                const float ws = wpart * wf;
+                atomicAdd(vs + Lay::enc(tl, El, xs, zst), ws);
+                t.Wout += (double)ws;
+                t.Eout += (double)ws * Ec_out;
+            }
         }
     }
     float wl = 0.0f, wr = 0.0f;
@@ -283,15 +368,15 @@ __device__ void emit_stay(const Dev& d, int par, bool k3, int cell, float theta_
         const float tt = fmaxf(0.0f, 1.0f - wcf);
         const float ts = wlr + wrr;
         if (tt > 0.0f && ts > 1e-12f) {
-            const float sc = tt / ts;
-            wl = wlr * sc;
-            wr = wrr * sc;
+            const float sc_ = tt / ts;
+            wl = wlr * sc_;
+            wr = wrr * sc_;
         }
         if (wl > 0.0f) {
             const float ws = w_new * wl;
             if (ix > 0) {
-                const float dr = emit_component<Lay, BUCKET>(d, par, cell, FACE_XM, cell - 1, theta_new, E_new, ws,
-                                                             Lay::NX - 1, zst, t.edep);
+                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XM, cell - 1, 5, theta_new, E_new, ws,
+                                                           Lay::NX - 1, zst, t);
                 if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
             } else {
                 t.w_bnd += ws;
@@ -301,8 +386,8 @@ __device__ void emit_stay(const Dev& d, int par, bool k3, int cell, float theta_
         if (wr > 0.0f) {
             const float ws = w_new * wr;
             if (ix < d.Nx - 1) {
-                const float dr = emit_component<Lay, BUCKET>(d, par, cell, FACE_XP, cell + 1, theta_new, E_new, ws,
-                                                             0, zst, t.edep);
+                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XP, cell + 1, 5, theta_new, E_new, ws,
+                                                           0, zst, t);
                 if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
             } else {
                 t.w_bnd += ws;
@@ -310,7 +395,7 @@ __device__ void emit_stay(const Dev& d, int par, bool k3, int cell, float theta_
             }
         }
     }
-    if (k3 || d.esplit) {
+    if (PASS != PASS_KEYS && (k3 || d.esplit)) {
         float rf = wcf;
         if (ix > 0) rf += wl;
         if (ix < d.Nx - 1) rf += wr;
@@ -321,9 +406,9 @@ __device__ void emit_stay(const Dev& d, int par, bool k3, int cell, float theta_
 }
 
 // Component crosses `face` (k2_coarsetransport.cu:363-459, k3_finetransport.cu:380-503).
-template <class Lay, bool BUCKET>
-__device__ void emit_cross(const Dev& d, int par, bool k3, int cell, int my_cls, int face, float theta_new, float E_new,
-                           float w_new, float x_new, float z_new, float sig_tr, Tally& t) {
+template <class Lay, int PASS>
+__device__ void emit_cross(const Dev& d, const Src& sc, int par, bool k3, int cell, int my_cls, int face,
+                           float theta_new, float E_new, float w_new, float x_new, float z_new, float sig_tr, Tally& t) {
     const int ix = cell % d.Nx, iz = cell / d.Nx;
     int nb = -1;
     if (face == FACE_ZP) nb = iz + 1 < d.Nz ? cell + d.Nx : -1;
@@ -336,11 +421,11 @@ __device__ void emit_cross(const Dev& d, int par, bool k3, int cell, int my_cls,
         return;
     }
     const float E_emit = bin_energy(d, E_new, w_new).Erep;
-    const bool fold = k3 || d.esplit;
+    const bool fold = PASS != PASS_KEYS && (k3 || d.esplit);
     if (face == FACE_ZP) {
         float lbw = 0.0f;
-        const float dr = emit_forward<Lay, BUCKET>(d, par, cell, my_cls, theta_new, E_new, w_new, x_new, sig_tr, lbw,
-                                                   t.edep);
+        const float dr =
+            emit_forward<Lay, PASS>(d, sc, par, cell, my_cls, theta_new, E_new, w_new, x_new, sig_tr, lbw, t);
         if (lbw > 0.0f) { t.w_bnd += lbw; t.e_bnd += (double)(E_new * lbw); }
         if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
         if (fold) {
@@ -353,7 +438,7 @@ __device__ void emit_cross(const Dev& d, int par, bool k3, int cell, int my_cls,
     const float xo = face == FACE_XP ? -dx * 0.5f : (face == FACE_XM ? dx * 0.5f : x_new);
     const int xsn = sub_bin(xo, dx, Lay::NX);
     const int zsn = face == FACE_ZM ? Lay::NZ - 1 : sub_bin(z_new, dz, Lay::NZ);
-    const float dr = emit_component<Lay, BUCKET>(d, par, cell, face, nb, theta_new, E_new, w_new, xsn, zsn, t.edep);
+    const float dr = emit_component<Lay, PASS>(d, sc, par, cell, face, nb, 5, theta_new, E_new, w_new, xsn, zsn, t);
     if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
     if (fold) {
         const float tw = fmaxf(0.0f, w_new - dr);
@@ -370,10 +455,11 @@ __device__ __forceinline__ int exit_face(float x, float z, float dx, float dz) {
     return -1;
 }
 
-// One component of a listed cell.
-template <class Lay, bool BUCKET>
-__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t bid, int sslot, int lidx, float w,
-                              unsigned salt, Tally& t) {
+// One component of a listed cell: local bin lidx of psi_in slot `slot`
+// (sslot: the slot number the random seeds use).
+template <class Lay, int PASS>
+__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t bid, int slot, int sslot, int lidx,
+                              float w, unsigned salt, uint32_t tag, Tally& t) {
     const float dx = d.dx, dz = d.dz;
     int tl, El, xs, zs;
     Lay::dec(lidx, tl, El, xs, zs);
@@ -406,7 +492,7 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
     unsigned ts;
     if (k3) {
         // K3_FineTransport body, k3_finetransport.cu:226-366
-        const float mu0 = cosf(theta), eta0 = sinf(theta);
+        const float mu0 = sm2d_cosf(theta), eta0 = sm2d_sinf(theta);
         const float szp = (mu0 > 0) ? (hz - zc) / mu0 : 1e30f;
         const float szm = (mu0 < 0) ? (-hz - zc) / mu0 : 1e30f;
         const float sxp = (eta0 > 0) ? (hx - xc) / eta0 : 1e30f;
@@ -426,7 +512,7 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
         edep = dE * w;
         w_new = w;
         if (d.nuclear) {
-            const float surv = expf(-nuclear_xs(E) * step);
+            const float surv = sm2d_expf(-nuclear_xs(E) * step);
             w_new = w * surv;
             w_rem = w - w_new;
             E_rem = w_rem * E;
@@ -454,7 +540,7 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
         dE = fminf(lut_energy_loss(d, E, rs), E);
         E_new = E - dE;
         edep = dE * w;
-        const float surv = expf(-nuclear_xs(E) * rs);
+        const float surv = sm2d_expf(-nuclear_xs(E) * rs);
         w_new = w * surv;
         w_rem = w - w_new;
         E_rem = w_rem * E;
@@ -482,8 +568,8 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
     }
     const float scat = sig_th <= 0.0f ? 0.0f : normal_draw(ts) * sig_th;
     const float theta_new = fmaxf(d.th[0], fminf(theta + scat, d.th[d.N_theta]));
-    float x_new = xc + sinf(theta_new) * step;
-    float z_new = zc + cosf(theta_new) * step;
+    float x_new = xc + sm2d_sinf(theta_new) * step;
+    float z_new = zc + sm2d_cosf(theta_new) * step;
     const int face = exit_face(x_new, z_new, dx, dz);
     x_new = fmaxf(-hx, fminf(x_new, hx));
     z_new = fmaxf(-hz, fminf(z_new, hz));
@@ -496,11 +582,13 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
         return;
     }
     const int my_cls = k3 ? 2 : 1;
+    const Src sc{cell, slot, lidx, k3 ? 1 : 0, tag};
     if (face >= 0) {
-        const float sig_tr = k3 ? 0.001f : fmaxf(sinf(fminf(sig_th, 1.57f)) * fmaxf(step, 0.0f) / 1.7320508f, 0.01f);
-        emit_cross<Lay, BUCKET>(d, par, k3, cell, my_cls, face, theta_new, E_new, w_new, x_new, z_new, sig_tr, t);
+        const float sig_tr = k3 ? 0.001f : fmaxf(sm2d_sinf(fminf(sig_th, 1.57f)) * fmaxf(step, 0.0f) / 1.7320508f, 0.01f);
+        emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, theta_new, E_new, w_new, x_new, z_new, sig_tr, t);
     } else {
-        emit_stay<Lay, BUCKET>(d, par, k3, cell, theta_new, E_new, w_new, x_new, z_new, k3 ? 0.001f : sig_x, sig_x, t);
+        emit_stay<Lay, PASS>(d, sc, par, k3, cell, theta_new, E_new, w_new, x_new, z_new, k3 ? 0.001f : sig_x, sig_x,
+                             t);
     }
 }
 

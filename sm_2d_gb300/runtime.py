@@ -74,7 +74,10 @@ class Audit(C.Structure):
 SCALAR_KEYS = ["transport_dropped_weight", "transport_dropped_energy", "audit_residual_energy",
                "source_injected_weight", "source_injected_energy", "source_out_of_grid_weight",
                "source_out_of_grid_energy", "source_slot_dropped_weight", "source_slot_dropped_energy",
-               "source_representation_loss_energy", "iterations", "cell_steps", "slots_in", "slots_out"]
+               "source_representation_loss_energy", "iterations", "cell_steps", "slots_in", "slots_out",
+               "claim_table_overflows", "claim_misses"]
+# device stages of one iteration, in launch order (sm2d_get_step_timing)
+STAGES = ["classify", "lists", "claims", "select", "transport", "k4", "finalize"]
 
 
 def lib(build_if_needed: bool = True):
@@ -127,6 +130,7 @@ def lib(build_if_needed: bool = True):
         L.sm2d_compact_lists.argtypes = [P, P, P, I, I, I, P, P, P, P, P]
         L.sm2d_k4_bucket_transfer.argtypes = [P, P, P, P, I, I, I, I, I, I, P, I, I, P, P]
         L.sm2d_k5_conservation_audit.argtypes = ([P] * 18 + [F, F, D, D, F, D, I, P, I, I, I, I, P, I, P])
+        L.sm2d_math_eval.argtypes = [I, P, P, I]
         _LIB = L
         return L
 
@@ -373,7 +377,7 @@ class Transport:
         return [arr[i].as_dict() for i in range(n.value)]
 
     def scalars(self):
-        s = np.zeros(14)
+        s = np.zeros(len(SCALAR_KEYS))
         check(self._lib.sm2d_get_scalars(self.h, _p(s)))
         return dict(zip(SCALAR_KEYS, s.tolist()))
 
@@ -406,14 +410,25 @@ class Transport:
 
     def run_profiled(self, n_iterations):
         n, launches = C.c_int(), C.c_int()
-        ms = np.zeros(5, np.float32)
+        ms = np.zeros(len(STAGES), np.float32)
         check(self._lib.sm2d_run_profiled(self.h, int(n_iterations), C.byref(n), _p(ms), C.byref(launches)))
-        return n.value, dict(zip(["classify", "compact", "transport", "k4", "audit"], ms.tolist())), launches.value
+        return n.value, dict(zip(STAGES, ms.tolist())), launches.value
 
     def step_timing(self):
-        t = np.zeros(5, np.float32)
+        t = np.zeros(len(STAGES), np.float32)
         check(self._lib.sm2d_get_step_timing(self.h, _p(t)))
-        return dict(zip(["classify", "compact", "transport", "k4", "audit"], t.tolist()))
+        return dict(zip(STAGES, t.tolist()))
+
+
+MATH_FUNCS = ("exp", "log", "sin", "cos", "erf")
+
+
+def math_eval(name: str, x) -> np.ndarray:
+    """The transport's elementary function `name` evaluated on the device."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    check(lib().sm2d_math_eval(MATH_FUNCS.index(name), _p(x), _p(y), x.size))
+    return y
 
 
 def depth_dose(dose_2d: np.ndarray) -> np.ndarray:
