@@ -210,6 +210,27 @@ int sm2d_k5_conservation_audit(
     double source_slot_dropped_energy, float transport_dropped_weight,
     double transport_dropped_energy, int include_source_terms, const float* d_E_edges, int N_E,
     int nt_local, int N_E_local, int local_bins, sm2d_audit* d_report, int N_cells, void* stream);
+/* The K5 audit above without any device allocation (no counterpart in the
+ * reference; for callers that cannot call cudaMalloc).  Same arguments and
+ * report; the reduction scratch is a file-scope static __device__ array of
+ * 2048 x 11 doubles plus a counter (about 176 KB per device), so N_cells is
+ * limited to 524288 (2048 blocks of 256 cells); larger grids are refused
+ * with SM2D_ERR_ARG.  The block totals are summed in a fixed order, so the
+ * report is the same on every call.  All calls share the scratch: calls
+ * whose kernels overlap on the GPU (other streams or threads) race. */
+int sm2d_k5_conservation_audit_static(
+    const uint32_t* d_bid_in, const float* d_val_in, const uint32_t* d_bid_out, const float* d_val_out,
+    const double* d_EdepC, const double* d_AbsorbedEnergy_nuclear, const double* d_BoundaryLoss_energy,
+    const double* d_AbsorbedEnergy_cutoff, const double* d_PrevEdepC,
+    const double* d_PrevAbsorbedEnergy_nuclear, const double* d_PrevBoundaryLoss_energy,
+    const double* d_PrevAbsorbedEnergy_cutoff, const float* d_AbsorbedWeight_cutoff,
+    const float* d_AbsorbedWeight_nuclear, const float* d_BoundaryLoss_weight,
+    const float* d_PrevAbsorbedWeight_cutoff, const float* d_PrevAbsorbedWeight_nuclear,
+    const float* d_PrevBoundaryLoss_weight, float source_out_of_grid_weight,
+    float source_slot_dropped_weight, double source_out_of_grid_energy,
+    double source_slot_dropped_energy, float transport_dropped_weight,
+    double transport_dropped_energy, int include_source_terms, const float* d_E_edges, int N_E,
+    int nt_local, int N_E_local, int local_bins, sm2d_audit* d_report, int N_cells, void* stream);
 
 /* ---- diagnostics (no counterpart in the reference) ---- */
 /* Evaluate one of the transport's elementary functions (0 exp, 1 log,

@@ -1124,6 +1124,147 @@ __global__ void k_raw_k5(RawK5 a, double* acc /* [11] + counter */, float s_oog_
     *rep = r;
 }
 
+// ---- K5 audit on static scratch (sm2d_k5_conservation_audit_static) ----
+// File-scope scratch of the allocation-free K5 entry: one row of 11 partial
+// sums per block (each written whole by its block, never accumulated) and,
+// after the rows, the block-completion counter, which must be zero when a
+// call starts (cleared by the entry before every launch and by the last
+// block on exit).  All calls share it: calls whose kernels overlap on the
+// GPU race.
+constexpr int kK5StaticMaxBlocks = 2048;                 // 256 cells per block
+constexpr int kK5StaticMaxCells = kK5StaticMaxBlocks * 256;
+static __device__ __align__(256) double g_k5_scratch[kK5StaticMaxBlocks * 11 + 2];
+
+__global__ void __launch_bounds__(256) k_raw_k5_static(RawK5 a, double* scratch, float s_oog_w, float s_slot_w,
+                                                       double s_oog_e, double s_slot_e, float drop_w,
+                                                       double drop_e, int inc_src, sm2d_audit* rep) {
+    __shared__ double s_red[11][8];
+    __shared__ double s_tree[256];
+    __shared__ int s_last;
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double v[11] = {0};
+    if (cell < a.Nc) {
+        for (int pass = 0; pass < 2; ++pass) {
+            const uint32_t* bid = pass ? a.bid_out : a.bid_in;
+            const float* val = pass ? a.val_out : a.val_in;
+            for (int s = 0; s < kKb; ++s) {
+                const uint32_t b = bid[(size_t)cell * kKb + s];
+                if (b == kEmpty) continue;
+                for (int l = 0; l < a.L; ++l) {
+                    const float w = val[((size_t)cell * kKb + s) * a.L + l];
+                    if (w <= 0.0f) continue;
+                    int Eb = (int)((b >> 12) & 0xFFFu) * a.NE + (l / a.NT) % a.NE;
+                    Eb = max(0, min(Eb, a.N_E - 1));
+                    const float E = a.Ee[Eb] + 1.0f * (0.5f * (a.Ee[Eb + 1] - a.Ee[Eb]));
+                    v[pass] += (double)w;
+                    v[2 + pass] += (double)w * (double)E;
+                }
+            }
+        }
+        v[4] = fmaxf(0.0f, a.w_cut[cell] - a.p_w_cut[cell]);
+        v[5] = fmaxf(0.0f, a.w_nuc[cell] - a.p_w_nuc[cell]);
+        v[6] = fmaxf(0.0f, a.w_bnd[cell] - a.p_w_bnd[cell]);
+        v[7] = fmax(0.0, a.edep[cell] - a.p_edep[cell]);
+        v[8] = fmax(0.0, a.e_cut[cell] - a.p_e_cut[cell]);
+        v[9] = fmax(0.0, a.e_nuc[cell] - a.p_e_nuc[cell]);
+        v[10] = fmax(0.0, a.e_bnd[cell] - a.p_e_bnd[cell]);
+    }
+    // block partials in a fixed order: warps, then the 8 warp sums
+    for (int k = 0; k < 11; ++k) {
+        const double w = warp_sum(v[k]);
+        if (lane == 0) s_red[k][wid] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x < 11) {
+        double b = 0.0;
+        for (int w = 0; w < 8; ++w) b += s_red[threadIdx.x][w];
+        scratch[(size_t)blockIdx.x * 11 + threadIdx.x] = b;
+        __threadfence();
+    }
+    __syncthreads();
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(scratch + (size_t)kK5StaticMaxBlocks * 11);
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1ull) == (unsigned long long)(gridDim.x - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    // last block: totals over the block rows in a fixed order (strided
+    // partial sums, then a binary tree), so repeated calls agree bit for bit
+    double tot[11];
+    for (int k = 0; k < 11; ++k) {
+        double p = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            p += *(volatile double*)&scratch[(size_t)b * 11 + k];
+        s_tree[threadIdx.x] = p;
+        __syncthreads();
+        for (int w = 128; w > 0; w >>= 1) {
+            if (threadIdx.x < w) s_tree[threadIdx.x] += s_tree[threadIdx.x + w];
+            __syncthreads();
+        }
+        tot[k] = s_tree[0];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    *cnt = 0ull;   // leave the counter at zero for the next call
+    sm2d_audit r;
+    memset(&r, 0, sizeof r);
+    r.W_in_total = (float)tot[0];
+    r.W_out_total = (float)tot[1];
+    r.E_in_total = tot[2];
+    r.E_out_total = tot[3];
+    r.W_cutoff_total = (float)tot[4];
+    r.W_nuclear_total = (float)tot[5];
+    r.W_boundary_total = (float)tot[6];
+    r.E_dep_total = tot[7];
+    r.E_cutoff_total = tot[8];
+    r.E_nuclear_total = tot[9];
+    r.E_boundary_total = tot[10];
+    r.W_transport_drop_total = fmaxf(0.0f, drop_w);
+    r.E_transport_drop_total = fmax(0.0, drop_e);
+    if (inc_src) {
+        const float wso = fmaxf(0.0f, s_oog_w), wss = fmaxf(0.0f, s_slot_w);
+        const double eso = fmax(0.0, s_oog_e), ess = fmax(0.0, s_slot_e);
+        r.W_in_total += wso + wss;
+        r.E_in_total += eso + ess;
+        r.W_source_out_of_grid_total = wso;
+        r.W_source_slot_drop_total = wss;
+        r.E_source_out_of_grid_total = eso;
+        r.E_source_slot_drop_total = ess;
+    }
+    r.processed_cells = a.Nc;
+    const float Wr = r.W_out_total + r.W_cutoff_total + r.W_nuclear_total + r.W_boundary_total +
+                     r.W_transport_drop_total + r.W_source_out_of_grid_total + r.W_source_slot_drop_total;
+    r.W_error = fabsf(r.W_in_total - Wr) / fmaxf(r.W_in_total, 1e-20f);
+    r.W_pass = (isfinite(r.W_error) && r.W_error < 1e-6f) ? 1 : 0;
+    const double Er = r.E_out_total + r.E_dep_total + r.E_cutoff_total + r.E_nuclear_total + r.E_boundary_total +
+                      r.E_transport_drop_total + r.E_source_out_of_grid_total + r.E_source_slot_drop_total;
+    r.E_error = (float)(fabs(r.E_in_total - Er) / fmax(r.E_in_total, 1e-20));
+    r.E_pass = (isfinite(r.E_error) && r.E_error < 1e-5f) ? 1 : 0;
+    *rep = r;
+}
+
+// Device address of g_k5_scratch, looked up once per device at set-up
+// (with that device current) and cached.
+static int k5_static_scratch(double** out) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static void* addr[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return fail(SM2D_ERR_ARG, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_k5_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(SM2D_ERR_CUDA, "cudaGetSymbolAddress(g_k5_scratch): %s", cudaGetErrorString(e));
+        addr[dev] = p;
+    }
+    *out = static_cast<double*>(addr[dev]);
+    return 0;
+}
+
 // ------------------------------------------------------------------ diagnostics
 __global__ void k_math_eval(int fn, const float* __restrict__ x, float* __restrict__ y, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1855,6 +1996,33 @@ int sm2d_k5_conservation_audit(const uint32_t* bid_in, const float* val_in, cons
             w_cut, w_nuc, w_bnd, p_w_cut, p_w_nuc, p_w_bnd, Ee, N_E, nt_local, N_E_local, L, N_cells};
     k_raw_k5<<<(N_cells + 255) / 256, 256, 0, s>>>(a, acc, s_oog_w, s_slot_w, s_oog_e, s_slot_e, drop_w, drop_e, inc_src,
                                                    d_report);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+int sm2d_k5_conservation_audit_static(
+    const uint32_t* bid_in, const float* val_in, const uint32_t* bid_out, const float* val_out, const double* EdepC,
+    const double* e_nuc, const double* e_bnd, const double* e_cut, const double* p_edep, const double* p_e_nuc,
+    const double* p_e_bnd, const double* p_e_cut, const float* w_cut, const float* w_nuc, const float* w_bnd,
+    const float* p_w_cut, const float* p_w_nuc, const float* p_w_bnd, float s_oog_w, float s_slot_w, double s_oog_e,
+    double s_slot_e, float drop_w, double drop_e, int inc_src, const float* Ee, int N_E, int nt_local, int N_E_local,
+    int L, sm2d_audit* d_report, int N_cells, void* stream) {
+    if (!bid_in || !val_in || !bid_out || !val_out || !EdepC || !Ee || !d_report || N_cells <= 0)
+        return fail(SM2D_ERR_ARG, "invalid argument");
+    if (N_cells > kK5StaticMaxCells)
+        return fail(SM2D_ERR_ARG, "N_cells %d exceeds the static scratch limit of %d cells", N_cells,
+                    kK5StaticMaxCells);
+    double* scratch = nullptr;
+    int rc = k5_static_scratch(&scratch);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    // the completion counter must start at zero
+    CK(cudaMemsetAsync(scratch + (size_t)kK5StaticMaxBlocks * 11, 0, sizeof(unsigned long long), s));
+    RawK5 a{bid_in, bid_out, val_in, val_out, EdepC, e_nuc, e_bnd, e_cut, p_edep, p_e_nuc, p_e_bnd, p_e_cut,
+            w_cut, w_nuc, w_bnd, p_w_cut, p_w_nuc, p_w_bnd, Ee, N_E, nt_local, N_E_local, L, N_cells};
+    k_raw_k5_static<<<(N_cells + 255) / 256, 256, 0, s>>>(a, scratch, s_oog_w, s_slot_w, s_oog_e, s_slot_e, drop_w,
+                                                          drop_e, inc_src, d_report);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     return 0;

@@ -130,6 +130,7 @@ def lib(build_if_needed: bool = True):
         L.sm2d_compact_lists.argtypes = [P, P, P, I, I, I, P, P, P, P, P]
         L.sm2d_k4_bucket_transfer.argtypes = [P, P, P, P, I, I, I, I, I, I, P, I, I, P, P]
         L.sm2d_k5_conservation_audit.argtypes = ([P] * 18 + [F, F, D, D, F, D, I, P, I, I, I, I, P, I, P])
+        L.sm2d_k5_conservation_audit_static.argtypes = L.sm2d_k5_conservation_audit.argtypes
         L.sm2d_math_eval.argtypes = [I, P, P, I]
         _LIB = L
         return L
