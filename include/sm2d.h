@@ -146,8 +146,9 @@ int sm2d_get_audit_history(sm2d_handle h, sm2d_audit* out, int max_entries, int*
  * [12] occupied input slots summed over cell-steps [13] output slots summed
  * [14] claim-table inserts that found no free entry [15] deposits whose
  * block id had not been gathered (both 0 in a correct run; cumulative
- * since create) */
-int sm2d_get_scalars(sm2d_handle h, double* out16);
+ * since create) [16] bin-list overflows of this spot (non-zero: the run
+ * stopped early; sm2d_run/sm2d_step return SM2D_ERR_ALLOC) */
+int sm2d_get_scalars(sm2d_handle h, double* out17);
 int sm2d_get_fe(sm2d_handle h, float* A, float* B, float* sigma_total);
 /* EdepC after the lateral MCS post-convolution, [Nz][Nx] row-major */
 int sm2d_get_dose(sm2d_handle h, double* dose);

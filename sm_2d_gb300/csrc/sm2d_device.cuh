@@ -48,8 +48,10 @@ struct IterState {
     int halt;              // this pass does no transport (finished or iteration limit)
     int occ_n[2];          // length of each buffer's occupied-cell list
     int n_listed;          // cells of this iteration (active + coarse)
-    int n_items;           // (cell, slot) work items of this iteration
-    int acc_active, acc_coarse, acc_listed, acc_items;   // classify counters
+    int n_items;           // claimed slots of the listed cells
+    int n_bins;            // w > 0 local bins of the listed cells (transport work)
+    int acc_active, acc_coarse, acc_listed, acc_items, acc_bins;   // classify counters
+    int bin_ovf;           // the bin list outgrew its capacity (cumulative)
     int cand_ovf;          // claim-table inserts that found no free entry (cumulative)
     int cand_miss;         // deposits whose block id was not gathered (cumulative)
     int wipe;              // claim tables are cleared before the next pass
@@ -103,7 +105,9 @@ struct Dev {
     unsigned long long* act_gen;
     uint8_t* cls;         // 0 idle, 1 coarse (K2), 2 active (K3); 0 outside the iteration
     uint32_t* listed;     // this iteration's active + coarse cells (claim order)
-    uint32_t* items;      // (cell << 5) | slot of every claimed slot of a listed cell
+    uint4* bins;          // w > 0 bins of the listed cells, grouped by cell:
+                          // {cell, slot | seed slot << 5 | lidx << 10 | K3 << 18, w bits, block id}
+    int bins_cap;
     uint32_t *active, *coarse;   // ascending lists (built on request by k_order_lists)
     IterState* it;
     sm2d_audit* hist;

@@ -260,18 +260,23 @@ __device__ __forceinline__ void block_add(const double (&v)[N], double* dst) {
 // K1_ActiveMask (k1_activemask.cu:6-48) over the occupied cells of psi_in,
 // warp per cell: the cell's class (active / coarse with w > 0,
 // compact_coarse_list k1k6_pipeline.cu:625-665), its place in this
-// iteration's cell list and bucket map, and one work item per claimed slot.
-// The last block publishes the counts, applies the stopping rules, resets
-// the per-iteration accumulators and sets the device loop condition.
+// iteration's cell list and bucket map, and, for a listed cell, its w > 0
+// bins appended to the bin list (contiguous per cell) for the transport.
+// The slot values are read as a flat run of float4s, eight loads in flight
+// per lane.  The last block publishes the counts, applies the stopping
+// rules, resets the per-iteration accumulators and sets the device loop
+// condition.
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphConditionalHandle cond, int use_cond) {
+    constexpr int Q = Lay::L / 4, NW = kThreads / 32, U = 8;
     __shared__ int s_cnt[2];
     __shared__ int s_last, s_halt, s_listed;
+    __shared__ uint8_t s_slot[NW][kKb];   // r-th claimed slot of the warp's cell
     IterState* it = d.it;
     const int par = it->parity;
     const int nocc = it->occ_n[par];
     const unsigned long long g = it->gen + 1;   // number of this classification
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const unsigned lt = (1u << lane) - 1u;
     if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
@@ -284,21 +289,29 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         const bool c_on = __any_sync(kFull, used && be <= (uint32_t)d.b_on);
         const bool c_off = __any_sync(kFull, used && be <= (uint32_t)d.b_off);
         const unsigned um = __ballot_sync(kFull, used);
+        __syncwarp();   // the previous cell's slot table is no longer read
+        if (used) s_slot[wid][__popc(um & lt)] = (uint8_t)lane;
+        __syncwarp();
+        const int F = __popc(um) * Q;   // float4s of the claimed slots
+        const float4* vc = reinterpret_cast<const float4*>(d.val[par] + (size_t)c * kKb * Lay::L);
         float ws = 0.0f;
-        int pos = 0;
-        unsigned m = um;
-        while (m) {
-            const int s = __ffs(m) - 1;
-            m &= m - 1;
-            const float4* v = reinterpret_cast<const float4*>(d.val[par] + ((size_t)c * kKb + s) * Lay::L);
-            for (int q = lane; q < Lay::L / 4; q += 32) {
-                const float4 f = v[q];
-                ws += (f.x + f.y) + (f.z + f.w);
-                pos |= (f.x > 0.0f) | (f.y > 0.0f) | (f.z > 0.0f) | (f.w > 0.0f);
+        int nz = 0;
+        for (int f0 = 0; f0 < F; f0 += 32 * U) {
+            float4 r[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int f = f0 + 32 * u + lane;
+                r[u] = f < F ? __ldcg(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                ws += (r[u].x + r[u].y) + (r[u].z + r[u].w);
+                nz += (r[u].x > 0.0f) + (r[u].y > 0.0f) + (r[u].z > 0.0f) + (r[u].w > 0.0f);
             }
         }
         ws = __shfl_sync(kFull, warp_sumf(ws), 0);
-        const bool hw = __any_sync(kFull, pos);
+        for (int o = 16; o > 0; o >>= 1) nz += __shfl_xor_sync(kFull, nz, o);
+        const bool hw = nz > 0;
         const bool prev = d.act_gen[c] == g - 1;
         const bool act = (c_on || (prev && c_off)) && ws > d.wmin;
         const int cls = act ? 2 : (hw ? 1 : 0);
@@ -308,7 +321,8 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
             if (act) d.act_gen[c] = g;
             if (cls) {
                 const int idx = atomicAdd(&it->acc_listed, 1);
-                base = atomicAdd(&it->acc_items, __popc(um));
+                atomicAdd(&it->acc_items, __popc(um));
+                base = atomicAdd(&it->acc_bins, nz);
                 d.listed[idx] = (uint32_t)c;
                 d.c2b[c] = 4 * idx;
                 atomicAdd(&s_cnt[act ? 0 : 1], 1);
@@ -316,7 +330,49 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         }
         if (cls) {
             base = __shfl_sync(kFull, base, 0);
-            if (used) d.items[base + __popc(um & lt)] = ((uint32_t)c << 5) | (uint32_t)lane;
+            if (base + nz > d.bins_cap) {   // no room: the last block stops the run
+                if (lane == 0) atomicAdd(&it->bin_ovf, 1);
+                continue;
+            }
+            // seed slot of each claimed slot: the rank of its block id
+            int rk = 0;
+            for (int t = 0; t < kKb; ++t) {
+                const uint32_t bt = __shfl_sync(kFull, b, t);
+                rk += (bt != kEmpty && bt < b) ? 1 : 0;
+            }
+            const uint32_t k3 = cls == 2 ? 1u : 0u;
+            int off = base;
+            for (int f0 = 0; f0 < F; f0 += 32 * U) {
+                float4 r[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {   // all loads first (L2 hits of the first read)
+                    const int f = f0 + 32 * u + lane;
+                    r[u] = f < F ? __ldcg(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int f = f0 + 32 * u + lane;
+                    const int s = f < F ? s_slot[wid][f / Q] : 0;
+                    const int cnt = (r[u].x > 0.0f) + (r[u].y > 0.0f) + (r[u].z > 0.0f) + (r[u].w > 0.0f);
+                    int inc = cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int y = __shfl_up_sync(kFull, inc, o);
+                        if (lane >= o) inc += y;
+                    }
+                    const uint32_t bs = __shfl_sync(kFull, b, s);
+                    const uint32_t meta = (uint32_t)s | ((uint32_t)__shfl_sync(kFull, rk, s) << 5) | (k3 << 18);
+                    int p = off + inc - cnt;
+                    const float c4[4] = {r[u].x, r[u].y, r[u].z, r[u].w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (c4[k] > 0.0f)
+                            d.bins[p++] = make_uint4((uint32_t)c, meta | ((uint32_t)(4 * (f % Q) + k) << 10),
+                                                     __float_as_uint(c4[k]), bs);
+                    off += __shfl_sync(kFull, inc, 31);
+                }
+            }
         }
     }
     __syncthreads();
@@ -332,8 +388,8 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         __threadfence();
         volatile IterState* v = it;
         int na = v->acc_active, nc = v->acc_coarse;
-        const int nl = v->acc_listed, ni = v->acc_items;
-        it->acc_active = it->acc_coarse = it->acc_listed = it->acc_items = 0;
+        const int nl = v->acc_listed, ni = v->acc_items, nb = v->acc_bins;
+        it->acc_active = it->acc_coarse = it->acc_listed = it->acc_items = it->acc_bins = 0;
         it->gen = g;
         it->ctag += 1u;   // claim pass of this iteration
         // C1 stopping rule: in-flight weight (the last audit's W_out) below a
@@ -350,10 +406,13 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         it->n_coarse = nc;
         const bool done = (na + nc) == 0;
         it->done = done ? 1 : 0;
-        const bool halt = done || it->iter >= it->max_iter;
+        // a bin list that outgrew its capacity ends the run (reported by the
+        // host API as SM2D_ERR_ALLOC)
+        const bool halt = done || it->iter >= it->max_iter || v->bin_ovf != 0;
         it->halt = halt ? 1 : 0;
         it->n_listed = halt ? 0 : nl;
         it->n_items = halt ? 0 : ni;
+        it->n_bins = halt ? 0 : nb;
         double* acc = &it->drop_w;   // the 14 per-iteration accumulators
         for (int k = 0; k < 14; ++k) acc[k] = 0.0;
         it->blocks_done = 0;
@@ -404,84 +463,70 @@ __global__ void __launch_bounds__(1024) k_order_lists(Dev d) {
 }
 
 // ------------------------------------------------------------------ K2/K3
-// One warp per (listed cell, claimed slot) work item: the slot's w > 0 bins
-// are packed into shared memory and spread over the lanes, each lane
-// transporting one bin at a time.  PASS_KEYS gathers the claim candidates;
-// the deposit passes read (and clear) the slot, add the weights, and book
-// per-cell tally increments in the dl_* arrays and the audit sums per block.
+// Sum a per-lane value over runs of lanes with the same cell (the bin list
+// keeps a cell's bins contiguous): afterwards the first lane of each run
+// holds the run's total.
+template <class T>
+__device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const T n = __shfl_down_sync(kFull, v, 1 << i);
+        if (same[i] & (1u << (threadIdx.x & 31))) v += n;
+    }
+    return v;
+}
+
+// One thread per w > 0 bin of the listed cells.  PASS_KEYS gathers the
+// claim candidates; the deposit passes add the weights, book per-cell tally
+// increments in the dl_* arrays (one atomic per cell run of a warp) and the
+// audit sums per block.
 template <class Lay, int PASS>
 __global__ void __launch_bounds__(kThreads, 2) k_transport(Dev d) {
-    constexpr int NW = kThreads / 32, Q = Lay::L / 128;
-    __shared__ float s_w[NW][Lay::L];
-    __shared__ uint16_t s_l[NW][Lay::L];
     IterState* it = d.it;
     if (it->halt) return;
     const int par = it->parity;
-    const int n = it->n_items;
+    const int n = it->n_bins;
     const uint32_t tag = it->ctag;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int nw = gridDim.x * NW;
+    const int lane = threadIdx.x & 31;
     const unsigned salt = d.salt ? (unsigned)it->iter * 0x9E3779B9u : 0u;
     double g[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // drop_w, drop_e, Win, Ein, Wout, Eout, -
-    for (int wi = blockIdx.x * NW + wid; wi < n; wi += nw) {
-        const uint32_t item = d.items[wi];
-        const int cell = (int)(item >> 5), s = (int)(item & 31u);
-        const bool k3 = d.cls[cell] == 2;
-        const uint32_t mb = d.bid[par][(size_t)cell * kKb + lane];
-        const uint32_t bid = __shfl_sync(kFull, mb, s);
-        // seed slot: the slot index, or the rank of the block id in the cell
-        const int sslot = d.seed_mode ? __popc(__ballot_sync(kFull, mb != kEmpty && mb < bid)) : s;
-        float4* vp = reinterpret_cast<float4*>(d.val[par] + ((size_t)cell * kKb + s) * Lay::L);
-        float4 f[Q];
-        int cnt = 0;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            f[q] = PASS == PASS_KEYS ? __ldcg(vp + lane + 32 * q) : __ldcs(vp + lane + 32 * q);
-            cnt += (f[q].x > 0.0f) + (f[q].y > 0.0f) + (f[q].z > 0.0f) + (f[q].w > 0.0f);
+    const int stride = gridDim.x * blockDim.x;
+    for (int w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < n; w0 += stride) {
+        const int i = w0 + lane;
+        Tally t{};
+        int cell = -1;
+        if (i < n) {
+            // the claim pass keeps the list in L2 for the deposit pass
+            const uint4 r = PASS == PASS_KEYS ? __ldcg(d.bins + i) : __ldcs(d.bins + i);
+            cell = (int)r.x;
+            const int slot = (int)(r.y & 31u), sslot = (int)((r.y >> 5) & 31u), lidx = (int)((r.y >> 10) & 0xFFu);
+            const bool k3 = ((r.y >> 18) & 1u) != 0;
+            transport_bin<Lay, PASS>(d, par, k3, cell, r.w, slot, sslot, lidx, __uint_as_float(r.z), salt, tag, t);
         }
         if (PASS != PASS_KEYS) {
+            unsigned same[5];
 #pragma unroll
-            for (int q = 0; q < Q; ++q) __stcs(vp + lane + 32 * q, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+            for (int k = 0; k < 5; ++k) {
+                const int o = 1 << k;
+                const int nc = __shfl_down_sync(kFull, cell, o);
+                same[k] = __ballot_sync(kFull, lane + o < 32 && cell >= 0 && nc == cell);
+            }
+            const double edep = seg_sum(t.edep, same), ecut = seg_sum(t.e_cut, same), enuc = seg_sum(t.e_nuc, same),
+                         ebnd = seg_sum(t.e_bnd, same);
+            const float wcut = seg_sum(t.w_cut, same), wnuc = seg_sum(t.w_nuc, same), wbnd = seg_sum(t.w_bnd, same);
+            const int prev_cell = __shfl_up_sync(kFull, cell, 1);
+            if (cell >= 0 && (lane == 0 || prev_cell != cell)) {
+                if (edep != 0.0) atomicAdd(d.dl_edep + cell, edep);
+                if (ecut != 0.0) atomicAdd(d.dl_ecut + cell, ecut);
+                if (enuc != 0.0) atomicAdd(d.dl_enuc + cell, enuc);
+                if (ebnd != 0.0) atomicAdd(d.dl_ebnd + cell, ebnd);
+                if (wcut != 0.0f) atomicAdd(d.dl_wcut + cell, wcut);
+                if (wnuc != 0.0f) atomicAdd(d.dl_wnuc + cell, wnuc);
+                if (wbnd != 0.0f) atomicAdd(d.dl_wbnd + cell, wbnd);
+            }
+            g[0] += t.drop_w; g[1] += t.drop_e; g[2] += t.Win; g[3] += t.Ein;
+            g[4] += t.Wout; g[5] += t.Eout;
         }
-        int inc = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(kFull, inc, o);
-            if (lane >= o) inc += y;
-        }
-        const int total = __shfl_sync(kFull, inc, 31);
-        int pos = inc - cnt;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const float c4[4] = {f[q].x, f[q].y, f[q].z, f[q].w};
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (c4[k] > 0.0f) {
-                    s_w[wid][pos] = c4[k];
-                    s_l[wid][pos] = (uint16_t)(4 * (lane + 32 * q) + k);
-                    ++pos;
-                }
-        }
-        __syncwarp();
-        Tally t{};
-        for (int j = lane; j < total; j += 32)
-            transport_bin<Lay, PASS>(d, par, k3, cell, bid, s, sslot, (int)s_l[wid][j], s_w[wid][j], salt, tag, t);
-        __syncwarp();
-        if (PASS == PASS_KEYS) continue;
-        const double edep = warp_sum(t.edep), ecut = warp_sum(t.e_cut), enuc = warp_sum(t.e_nuc),
-                     ebnd = warp_sum(t.e_bnd);
-        const float wcut = warp_sumf(t.w_cut), wnuc = warp_sumf(t.w_nuc), wbnd = warp_sumf(t.w_bnd);
-        if (lane == 0) {
-            if (edep != 0.0) atomicAdd(d.dl_edep + cell, edep);
-            if (ecut != 0.0) atomicAdd(d.dl_ecut + cell, ecut);
-            if (enuc != 0.0) atomicAdd(d.dl_enuc + cell, enuc);
-            if (ebnd != 0.0) atomicAdd(d.dl_ebnd + cell, ebnd);
-            if (wcut != 0.0f) atomicAdd(d.dl_wcut + cell, wcut);
-            if (wnuc != 0.0f) atomicAdd(d.dl_wnuc + cell, wnuc);
-            if (wbnd != 0.0f) atomicAdd(d.dl_wbnd + cell, wbnd);
-        }
-        g[0] += t.drop_w; g[1] += t.drop_e; g[2] += t.Win; g[3] += t.Ein;
-        g[4] += t.Wout; g[5] += t.Eout;
     }
     if (PASS != PASS_KEYS) block_add<7>(g, &it->drop_w);
 }
@@ -772,17 +817,14 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
         const int c = d.occ_list[in][wi];
         const int cls = d.cls[c];
         uint32_t* ids = d.bid[in] + (size_t)c * kKb;
-        if (cls == 0) {   // unlisted: its claimed slots hold no positive weight, clear what they hold
-            unsigned um = __ballot_sync(kFull, ids[lane] != kEmpty);
-            while (um) {
-                const int s = __ffs(um) - 1;
-                um &= um - 1;
-                float4* v = reinterpret_cast<float4*>(d.val[in] + ((size_t)c * kKb + s) * Lay::L);
-                for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        } else if (lane < 7) {
-            part += fold_tally(d, c, lane);
+        unsigned um = __ballot_sync(kFull, ids[lane] != kEmpty);
+        while (um) {   // clear the consumed slots
+            const int s = __ffs(um) - 1;
+            um &= um - 1;
+            float4* v = reinterpret_cast<float4*>(d.val[in] + ((size_t)c * kKb + s) * Lay::L);
+            for (int q = lane; q < Lay::L / 4; q += 32) __stcs(v + q, make_float4(0.f, 0.f, 0.f, 0.f));
         }
+        if (cls && lane < 7) part += fold_tally(d, c, lane);
         ids[lane] = kEmpty;
         if (lane == 0) {
             d.occ[in][c] = 0;
@@ -1344,7 +1386,7 @@ struct Impl {
                             ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_BUCKET>, kThreads, 0)
                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_DIRECT>, kThreads, 0);
         if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
-        const long long items = (long long)c.d.Nc * kKb;   // one warp per item at most
+        const long long items = (long long)c.d.bins_cap / 32;   // one warp per 32 bins at most
         const long long full = (long long)std::max(per_sm, 1) * std::max(sms, 1);
         c.grid_transport = (int)std::max(1LL, std::min(full, (items + kThreads / 32 - 1) / (kThreads / 32)));
         return 0;
@@ -1505,7 +1547,12 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.dl_edep, double, Nc); A(d.dl_ecut, double, Nc); A(d.dl_enuc, double, Nc); A(d.dl_ebnd, double, Nc);
     A(d.dl_wcut, float, Nc); A(d.dl_wnuc, float, Nc); A(d.dl_wbnd, float, Nc);
     A(d.act_gen, unsigned long long, Nc); A(d.cls, uint8_t, Nc);
-    A(d.listed, uint32_t, Nc); A(d.items, uint32_t, ns);
+    A(d.listed, uint32_t, Nc);
+    // bin list: room for the w > 0 bins of four full slots per cell of the
+    // grid on average (a listed cell holds at most 32); a run that needs
+    // more stops with SM2D_ERR_ALLOC
+    d.bins_cap = (int)std::min<size_t>((size_t)Nc * 4 * c->L, (size_t)INT_MAX);
+    A(d.bins, uint4, d.bins_cap);
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
     A(d.it, IterState, 1);
     d.hist_cap = p->max_iterations > 0 ? p->max_iterations : 4096;
@@ -1662,6 +1709,7 @@ int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse) {
     int rc = DISPATCH(c, launch_body, true, false, true);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
+    if (c.it_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "bin list capacity (%d bins) exceeded", c.d.bins_cap);
     // classify, lists, claim pass, selection, deposit pass, K4 bucket move, finalize
     for (int k = 0; k < 7; ++k) CK(cudaEventElapsedTime(&c.step_ms[k], c.ev[k], c.ev[k + 1]));
     if (n_active) *n_active = c.it_host->done ? 0 : c.it_host->n_active;
@@ -1688,6 +1736,7 @@ static int run_impl(Ctx& c, int max_it, int* done_iters, float* ms) {
     if ((rc = push_state(c))) return rc;
     CK(cudaStreamSynchronize(c.s));
     if (done_iters) *done_iters = c.it_host->iter - start;
+    if (c.it_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "bin list capacity (%d bins) exceeded", c.d.bins_cap);
     return 0;
 }
 
@@ -1768,7 +1817,7 @@ int sm2d_get_scalars(sm2d_handle h, double* o) {
     o[3] = it.src_inj_w; o[4] = it.src_inj_e; o[5] = it.src_oog_w; o[6] = it.src_oog_e;
     o[7] = it.src_slot_w; o[8] = it.src_slot_e; o[9] = it.src_rep_loss;
     o[10] = it.iter; o[11] = it.cell_steps; o[12] = it.slots_in; o[13] = it.slots_out;
-    o[14] = it.cand_ovf; o[15] = it.cand_miss;
+    o[14] = it.cand_ovf; o[15] = it.cand_miss; o[16] = it.bin_ovf;
     return 0;
 }
 

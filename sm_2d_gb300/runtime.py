@@ -75,7 +75,7 @@ SCALAR_KEYS = ["transport_dropped_weight", "transport_dropped_energy", "audit_re
                "source_injected_weight", "source_injected_energy", "source_out_of_grid_weight",
                "source_out_of_grid_energy", "source_slot_dropped_weight", "source_slot_dropped_energy",
                "source_representation_loss_energy", "iterations", "cell_steps", "slots_in", "slots_out",
-               "claim_table_overflows", "claim_misses"]
+               "claim_table_overflows", "claim_misses", "bin_list_overflows"]
 # device stages of one iteration, in launch order (sm2d_get_step_timing)
 STAGES = ["classify", "lists", "claims", "select", "transport", "k4", "finalize"]
 
