@@ -1,9 +1,10 @@
 """In-tree build of libsm2d.so: the sm_103a CUDA kernels + C ABI.
 
-nvcc compiles the CUDA translation unit for sm_103a only, g++ compiles the
-host tables with -ffp-contract=off (so an Arm host gives the x86 float
-results), and g++ links the shared library against the CUDA runtime.  Both
-compiles run in parallel.  Usage: python -m sm_2d_gb300.build
+nvcc compiles the two CUDA translation units (the engine and the stage
+entries) for sm_103a only, g++ compiles the host tables with
+-ffp-contract=off (so an Arm host gives the x86 float results), and g++
+links the shared library against the CUDA runtime.  The compiles run in
+parallel.  Usage: python -m sm_2d_gb300.build
 """
 from __future__ import annotations
 
@@ -49,15 +50,18 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-    cu_obj = os.path.join(OUT, "sm2d_engine.o")
     cpp_obj = os.path.join(OUT, "sm2d_tables.o")
+    cu_units = ["sm2d_engine.cu", "sm2d_stages.cu"]
+    cu_objs = [os.path.join(OUT, u.replace(".cu", ".o")) for u in cu_units]
     # --fmad=false: every float operation rounds on its own, as the oracle's
     # -ffp-contract=off build does, so that both transport passes (and the
     # oracle) take the same binning decisions from the same arithmetic
-    cu_cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-c", "-Xcompiler", "-fPIC,-ffp-contract=off",
-              "--expt-relaxed-constexpr", *inc, os.path.join(CSRC, "sm2d_engine.cu"), "-o", cu_obj]
+    cu_cmds = [[nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-c", "-Xcompiler",
+                "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr", *inc, os.path.join(CSRC, u), "-o", o]
+               for u, o in zip(cu_units, cu_objs)]
     if ptxas_info:
-        cu_cmd.insert(1, "-Xptxas=-v")
+        for c in cu_cmds:
+            c.insert(1, "-Xptxas=-v")
     cpp_cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-c",
                os.path.join(CSRC, "sm2d_tables.cpp"), "-o", cpp_obj]
 
@@ -69,11 +73,11 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             raise RuntimeError("build step failed: " + " ".join(cmd))
         return r
 
-    with ThreadPoolExecutor(2) as ex:
-        for f in [ex.submit(run, cu_cmd), ex.submit(run, cpp_cmd)]:
+    with ThreadPoolExecutor(len(cu_cmds) + 1) as ex:
+        for f in [ex.submit(run, c) for c in cu_cmds] + [ex.submit(run, cpp_cmd)]:
             f.result()
     tmp = LIB + ".tmp"
-    run(["g++", "-shared", "-o", tmp, cu_obj, cpp_obj, "-L" + os.path.join(cuda, "lib64"),
+    run(["g++", "-shared", "-o", tmp, *cu_objs, cpp_obj, "-L" + os.path.join(cuda, "lib64"),
          "-L" + os.path.join(cuda, "targets", "sbsa-linux", "lib"), "-L" + os.path.join(cuda, "targets", "x86_64-linux", "lib"),
          "-lcudart", "-Wl,-rpath," + os.path.join(cuda, "lib64")])
     os.replace(tmp, LIB)
