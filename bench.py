@@ -9,8 +9,9 @@ phase space.  Phase-space grids are the ones the reference code builds and
 runs: 36 angular bins on +-0.35 rad, the default piecewise 1029-bin energy
 grid, 256 local bins (4 theta x 2 E x 8 x_sub x 4 z_sub).  `--grid log` runs
 the 256 log-E / 512 theta / 128-local-bin variant with the energy-split
-method instead.  A step is one spot transported to completion (until the
-in-flight weight falls below 1e-6 of the injected weight).
+method instead.  A step is one wave: `lanes` spots of that beam (sample seeds
+differ per spot) transported together to completion (until the in-flight
+weight of each falls below 1e-6 of its injected weight).
 
 Arms: default = libsm2d.so on the GPU; `--impl reference` = the reference's
 algorithm on the host cores (the CPU restatement in oracle/, all threads, one
@@ -57,6 +58,22 @@ def make_config(grid: str):
                                          E0=BEAM["E0"])
     cfg.max_iterations = MAX_IT
     return cfg.production()
+
+
+def lane_bytes(cfg):
+    """Device bytes one lane of the engine holds (sm2d_create's allocation)."""
+    nc = cfg.Nx * cfg.Nz
+    L = cfg.layout["nt_local"] * cfg.layout["ne_local"] * cfg.layout["nx_sub"] * cfg.layout["nz_sub"]
+    psi = nc * 32 * (4 + 4 * L)
+    per_cell = nc * (2 * 8 + 44 + 44 + 8 + 1 + 4 + 8)
+    rows = nc * 2048 + (nc // 8) * 4 * (2048 + 128 + 4)
+    bins = nc * L // 4 * 16
+    return psi + per_cell + rows + bins
+
+
+def auto_lanes(cfg, free_bytes, cap=64):
+    """Lanes filling at most 60 % of the free device memory (at most `cap`)."""
+    return int(max(1, min(cap, 0.6 * free_bytes // lane_bytes(cfg))))
 
 
 def workload_desc(grid, L):
@@ -183,33 +200,38 @@ def run_gpu_arm(args):
             torch.cuda.synchronize()
 
     cfg = make_config(args.grid)
+    cfg.lanes = args.lanes if args.lanes > 0 else auto_lanes(cfg, torch.cuda.mem_get_info()[0])
     t = sm.Transport(cfg)
+    B = t.lanes
     ext = torch.cuda.ExternalStream(t.stream())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
-    # pinned beam description and dose buffer for the end-to-end leg
-    beam_buf = torch.zeros(64, dtype=torch.uint8).pin_memory()
-    beam = Beam.from_address(beam_buf.data_ptr())
-    b = dict(BEAM, seed=BEAM["seed"] + 7919 * rank)
-    for k, v in dict(x0=b["x0"], z0=b["z0"], theta0=b["theta0"], E0=b["E0"], W_total=b["W"],
-                     sigma_x=b["sigma_x"], sigma_theta=b["sigma_theta"], sigma_E=b["sigma_E"],
-                     n_samples=b["n_samples"], seed=b["seed"]).items():
-        setattr(beam, k, v)
-    dose_host = torch.zeros(cfg.Nx * cfg.Nz, dtype=torch.float64).pin_memory()
-    dose_np = dose_host.numpy()
 
-    def one_spot():
-        t.reset()
-        t.inject_async(beam)
+    # one wave = B spots of the workload beam, sample seeds differing per spot
+    def make_beams(seed0):
+        out = []
+        for i in range(B):
+            out.append(Beam(BEAM["x0"], BEAM["z0"], BEAM["theta0"], BEAM["E0"], BEAM["W"], BEAM["sigma_x"],
+                            BEAM["sigma_theta"], BEAM["sigma_E"], BEAM["n_samples"], seed0 + i))
+        return out
+    beams = make_beams(BEAM["seed"] + 100003 * rank)
+    beam_arr = (Beam * B)(*beams)
+    lib = t._lib
+
+    def one_wave():
+        t.batch_inject(beams)
         t.run_async(MAX_IT)
 
     for _ in range(max(args.warmup, 3)):
-        one_spot()
+        one_wave()
     torch.cuda.synchronize()
-    iters_per_spot = t.scalars()["iterations"]
+    res = t.batch_results(B)
+    iters = [r["iterations"] for r in res]
 
-    # ---- timed region: K spots, device time per spot, L2 flushed between spots
+    # ---- timed region: K waves of B spots, device time per wave (every wave
+    # streams GBs of phase space, far more than L2; L2 is flushed between waves too)
     times = []
     launches = 0
+    cell_steps = 0.0
     barrier()
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -218,27 +240,31 @@ def run_gpu_arm(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(ext)
-            one_spot()
+            one_wave()
             e1.record(ext)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
-            s = t.scalars()
+            rs = t.batch_results(B)
+            passes = max(r["iterations"] for r in rs) + 1
+            cell_steps += sum(r["cell_steps"] for r in rs)
             # reset 3 + injection 6 + loop limit 1, then per pass of the device
             # loop classify, claim pass, bucket and psi_out selection, deposit
             # pass, finalize (+ bucket move)
-            launches += 10 + (7 if cfg.use_buckets else 6) * (int(s["iterations"]) + 1)
+            launches += 10 + (7 if cfg.use_buckets else 6) * passes
     barrier()
     total_ms = float(np.sum(times))
     if dist:
         tt = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         total_ms = float(tt.item())
-    spots = args.steps * world
+    spots = args.steps * B * world
     value = spots / (total_ms / 1e3)
-    sc = t.scalars()
-    cell_steps = sc["cell_steps"]
 
-    # ---- end to end through the public API with pinned host buffers
+    # ---- end to end through the public batch entry with pinned host buffers:
+    # beam descriptions in, one dose map per spot out
+    dose_host = torch.zeros(B * cfg.Nx * cfg.Nz, dtype=torch.float64).pin_memory()
+    beam_pin = torch.zeros(C.sizeof(Beam) * B, dtype=torch.uint8).pin_memory()
+    C.memmove(beam_pin.data_ptr(), C.addressof(beam_arr), C.sizeof(Beam) * B)
     e2e_times = []
     for _ in range(args.steps):
         flush.zero_()
@@ -246,10 +272,12 @@ def run_gpu_arm(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(ext)
-        one_spot()
-        t.dose_async(dose_np)
+        rc = lib.sm2d_batch_run(t.h, C.c_void_p(beam_pin.data_ptr()), B, MAX_IT, C.c_void_p(dose_host.data_ptr()),
+                                None)
         e1.record(ext)
         e1.synchronize()
+        if rc != 0:
+            raise RuntimeError(lib.sm2d_last_error().decode())
         e2e_times.append(e0.elapsed_time(e1))
     e2e_ms = float(np.sum(e2e_times))
     if dist:
@@ -258,15 +286,14 @@ def run_gpu_arm(args):
         e2e_ms = float(tt.item())
     e2e_value = spots / (e2e_ms / 1e3)
 
-    # ---- per-kernel device time: eager replay of one spot with CUDA events
+    # ---- per-kernel device time: eager replay of one wave with CUDA events
     # around every launch on the library stream
-    t.reset()
-    t.inject_async(beam)
+    t.batch_inject(beams)
     n_it, ms, n_launch = t.run_profiled(MAX_IT)
-    ps = t.scalars()
+    prs = t.batch_results(B)
     L = t.L
     slot_bytes = 4 + 4 * L
-    alg_bytes = (ps["slots_in"] + ps["slots_out"]) * slot_bytes + 44.0 * ps["cell_steps"]
+    alg_bytes = sum((r["slots_in"] + r["slots_out"]) * slot_bytes + 44.0 * r["cell_steps"] for r in prs)
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
         peaks = json.load(open(peaks_path))
@@ -281,11 +308,11 @@ def run_gpu_arm(args):
         traffic = tr.get("dram_bytes_per_launch")
     step_total = sum(ms.values())
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_src, "kernel": "k_transport",
+                "traffic": traffic, "peak_source": peak_src, "kernel": "k_transport (deposit pass)",
                 "algorithmic_bytes_per_launch": alg_bytes / max(n_it, 1),
                 "avg_launch_ms": ms["transport"] / max(n_it, 1),
                 "stage_share": {k: v / step_total for k, v in ms.items()} if step_total else {},
-                "note": "per-launch times from an eager replay of one spot with CUDA events around each "
+                "note": "per-launch times from an eager replay of one wave with CUDA events around each "
                         "kernel on the library stream"}
 
     cpu = None
@@ -300,12 +327,14 @@ def run_gpu_arm(args):
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": workload_desc(args.grid, cfg.layout), "grid": args.grid,
-                           "method": "plain K1-K6 (direct neighbour scatter)", "iterations_per_spot":
-                           iters_per_spot, "l2": "flushed (256 MB write) between timed spots",
-                           "parallelism": f"replicas by spot x{world}"},
+                           "method": "plain K1-K6 (direct neighbour scatter), deterministic slot claims",
+                           "step": f"one wave of {B} spots transported together (lanes)", "lanes": B,
+                           "iterations_per_spot": float(np.mean(iters)),
+                           "l2": "inputs larger than L2 (GBs of phase space per wave); 256 MB flush between waves",
+                           "parallelism": f"{B} spots per GPU, replicas by spot x{world}"},
                 "cell_steps_per_s": cell_steps * world / (total_ms / 1e3) if total_ms else None,
-                "e2e": {"value": e2e_value, "unit": "spots/s", "h2d_bytes_per_step": 40,
-                        "d2h_bytes_per_step": int(cfg.Nx * cfg.Nz * 8)},
+                "e2e": {"value": e2e_value, "unit": "spots/s", "h2d_bytes_per_step": int(C.sizeof(Beam) * B),
+                        "d2h_bytes_per_step": int(cfg.Nx * cfg.Nz * 8 * B)},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "gpu_launches": launches}
         print(json.dumps(line))
@@ -323,6 +352,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", default="reference", choices=["reference", "log"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--lanes", type=int, default=0, help="spots per wave (0: from free device memory)")
     ap.add_argument("--small", action="store_true",
                     help="100x200 cells, 80 MeV beam: a small case for profiler captures (not a bench line)")
     args = ap.parse_args()

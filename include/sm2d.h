@@ -85,6 +85,9 @@ typedef struct sm2d_problem {
     float stop_weight_fraction;  /* stop when in-flight weight < this * injected weight */
     int floor_cutoff;            /* absorb components re-binned up to the lowest bin   */
     int seed_iteration_salt;     /* salt MCS/straggling seeds with the iteration index */
+    /* engine shape */
+    int lanes;                   /* spots transported together by sm2d_batch_run
+                                    (0 or 1: one; the single-spot entries use lane 0) */
 } sm2d_problem;
 
 typedef struct sm2d_beam {
@@ -104,6 +107,22 @@ typedef struct sm2d_audit {
     double E_transport_drop_total;
     int processed_cells;
 } sm2d_audit;
+
+/* Outcome of one spot of sm2d_batch_run (no counterpart in the reference,
+ * whose runner transports one spot per call). */
+typedef struct sm2d_spot_result {
+    int iterations;               /* transport iterations                              */
+    int finished;                 /* 1: no cell held weight any more (or stopping rule) */
+    int weight_audit_failures;    /* iterations whose weight audit failed              */
+    int energy_audit_failures;    /* iterations whose energy audit failed              */
+    double injected_weight, injected_energy;
+    double source_out_of_grid_weight, source_slot_dropped_weight;
+    double transport_dropped_weight, transport_dropped_energy;
+    double audit_residual_energy, representation_loss_energy;
+    double cell_steps;            /* listed cells summed over iterations               */
+    double slots_in, slots_out;   /* occupied psi_in / psi_out slots summed over iterations */
+    sm2d_audit last;              /* audit record of the last iteration                */
+} sm2d_spot_result;
 
 /* DeviceOutflowBucket (src/cuda/device/device_bucket.cuh:48-57) for L local bins:
  *   uint32 block_id[32]; uint16 local_count[32]; float value[32][L]; float moment_A,B,C;
@@ -172,6 +191,27 @@ int sm2d_dose_async(sm2d_handle h, double* host_dose);
  * ms7 receives the summed device time of the seven stages listed at
  * sm2d_get_step_timing, *launches the number of kernel launches */
 int sm2d_run_profiled(sm2d_handle h, int n_iterations, int* iterations_done, float* ms7, int* launches);
+
+/* ---- batched spots (no counterpart in the reference: its runner transports
+ * one spot per call; a plan is a loop over such calls) ---- */
+/* lanes of the engine: spots transported together */
+int sm2d_lanes(sm2d_handle h);
+/* Transport n_spots beams to completion, `lanes` at a time (waves), each
+ * spot exactly as sm2d_reset + sm2d_inject + sm2d_run would (same results,
+ * lane by lane).  dose: host [n_spots][Nz][Nx] for the post-convolved
+ * EdepC of each spot, or NULL; results: host [n_spots] or NULL;
+ * max_iterations bounds each wave.  Blocking. */
+int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, double* dose,
+                   sm2d_spot_result* results);
+/* The steps of one wave of sm2d_batch_run, for callers that drive the loop
+ * themselves: sm2d_batch_inject resets every lane and injects beams[i]
+ * into lane i (lanes past n_beams stay empty; asynchronous, like
+ * sm2d_inject_async); then sm2d_run / sm2d_run_async / sm2d_run_profiled
+ * transport all lanes; sm2d_batch_results and sm2d_batch_dose read the
+ * first n lanes back (blocking). */
+int sm2d_batch_inject(sm2d_handle h, const sm2d_beam* beams, int n_beams);
+int sm2d_batch_results(sm2d_handle h, sm2d_spot_result* results, int n);
+int sm2d_batch_dose(sm2d_handle h, double* dose, int n);
 
 /* ---- host tables (no GPU needed) ---- */
 /* EnergyGrid(E_min,E_max,N) log grid (grids.cpp:6-24): edges[N+1], rep[N] */

@@ -35,30 +35,44 @@ struct Layout {
 using LayoutRef = Layout<4, 2, 8, 4>;    // 256 bins: the layout the reference code builds
 using LayoutB128 = Layout<8, 4, 4, 1>;   // 128 bins: 8 theta x 4 E x 4 x_sub
 
-// Device-resident iteration state: counters, per-iteration accumulators and
-// cumulative run totals.  Written only by device code between host syncs.
-struct IterState {
-    int parity;            // psi_in = buffer[parity]
-    int iter;              // transport iterations done
-    int n_active, n_coarse;
-    int done;              // no listed cell: transport finished
-    int max_iter;          // stop after this many iterations (device loop)
+// The engine holds B lanes: B independent spots, each with its own grid of
+// Nc cells, stacked so that every per-cell array is indexed by
+// gc = lane * Nc + cell.  All lanes advance together, one transport
+// iteration per pass of the kernel sequence; a lane without work idles.
+
+// Iteration state shared by the lanes (one per engine), written only by
+// device code between host syncs.
+struct IterGlobal {
+    int parity;            // occupancy list `parity` lists psi_in, `parity ^ 1` psi_out
+    int halt;              // this pass does no transport (no lane has work, or paused)
+    int pass;              // transport passes done since the last reset
+    int max_pass;          // the device loop pauses after this many passes
     unsigned blocks_done;  // last-block counter of the classify and finalize kernels
-    int include_source;    // next audit lifts source losses (first iteration)
-    int halt;              // this pass does no transport (finished or iteration limit)
-    int occ_n[2];          // length of each buffer's occupied-cell list
-    int n_listed;          // cells of this iteration (active + coarse)
+    int occ_n[2];          // length of each occupancy list
+    int n_listed;          // cells of this pass (active + coarse, all lanes)
     int n_items;           // claimed slots of the listed cells
     int n_bins;            // w > 0 local bins of the listed cells (transport work)
-    int acc_active, acc_coarse, acc_listed, acc_items, acc_bins;   // classify counters
-    int bin_ovf;           // the bin list outgrew its capacity (cumulative)
+    int acc_listed, acc_items, acc_bins;   // classify counters
+    int bin_ovf;           // the bin list outgrew its capacity (since the last reset)
     int cand_ovf;          // claim-table inserts that found no free entry (cumulative)
     int cand_miss;         // deposits whose block id was not gathered (cumulative)
     int wipe;              // claim tables are cleared before the next pass
-    int inj_skip;          // this injection found the phase space occupied
     uint32_t ctag;         // claim pass number: the tag of claim-table entries
-    int pad1;
     unsigned long long gen;  // K1 classifications done since create (never reset)
+};
+
+// Per-lane (per-spot) state.
+struct LaneState {
+    int iter;              // transport iterations of this lane's spot
+    int n_active, n_coarse;
+    int done;              // no listed cell: transport finished (or nothing injected)
+    int include_source;    // next audit lifts source losses (first iteration)
+    int work;              // this pass transports this lane
+    int light;             // stopping rule met at the start of this pass
+    int acc_active, acc_coarse, acc_slots;   // classify counters
+    int inj_skip;          // the last injection found the lane occupied
+    int w_fail, e_fail;    // iterations whose weight / energy audit failed
+    int pad0;
     // per-iteration accumulators, 14 consecutive doubles (reset by the
     // classify kernel); the transport adds to the first seven, the finalize
     // kernel to the last seven, in this order
@@ -68,14 +82,15 @@ struct IterState {
     double transport_drop_w, transport_drop_e, audit_residual;
     double cell_steps, slots_in, slots_out;
     // source accounting
-    float src_inj_w, src_oog_w, src_slot_w, pad0;
+    float src_inj_w, src_oog_w, src_slot_w, pad1;
     double src_inj_e, src_oog_e, src_slot_e, src_rep_loss;
     double tot_w, tot_e;   // scratch for phase-space totals
     sm2d_audit last;
 };
 
 struct Dev {
-    int Nx, Nz, Nc;
+    int Nx, Nz, Nc;       // grid of one lane
+    int B;                // lanes
     float dx, dz;
     int N_theta, N_E;
     const float* th;      // theta edges [N_theta+1]
@@ -89,10 +104,13 @@ struct Dev {
     int straggle, nuclear, seed_mode, esplit;
     float prune_coarse, prune_fine, split_min_w, stop_frac;
     int floor_cutoff, salt;
-    uint32_t* bid[2];
-    float* val[2];
-    int* occ[2];          // per cell: any slot claimed in this buffer
-    int* occ_list[2];     // occupied cells of each buffer, in claim order
+    // phase space, one buffer [B * Nc][32] ids + [B * Nc][32][L] values: the
+    // classify kernel copies psi_in into the bin list and clears it, so the
+    // same storage receives psi_out
+    uint32_t* bid;
+    float* val;
+    int* occ[2];          // per gc: on occupancy list k
+    int* occ_list[2];     // occupancy lists (gc), in claim order
     double *edep, *e_cut, *e_nuc, *e_bnd;
     float *w_cut, *w_nuc, *w_bnd;
     // this iteration's per-cell tally increments (folded into the cumulative
@@ -104,21 +122,25 @@ struct Dev {
     // input ("was active") is act_gen == gen - 1 at the next classification
     unsigned long long* act_gen;
     uint8_t* cls;         // 0 idle, 1 coarse (K2), 2 active (K3); 0 outside the iteration
-    uint32_t* listed;     // this iteration's active + coarse cells (claim order)
+    uint32_t* listed;     // this pass's active + coarse cells (gc, claim order)
+    int listed_cap;
     uint4* bins;          // w > 0 bins of the listed cells, grouped by cell:
-                          // {cell, slot | seed slot << 5 | lidx << 10 | K3 << 18, w bits, block id}
+                          // {gc, slot | seed slot << 5 | lidx << 10 | K3 << 18, w bits, block id}
     int bins_cap;
-    uint32_t *active, *coarse;   // ascending lists (built on request by k_order_lists)
-    IterState* it;
-    sm2d_audit* hist;
+    uint32_t *active, *coarse;   // ascending lists of lane 0 (built on request by k_order_lists)
+    IterGlobal* gs;
+    LaneState* ls;        // [B]
+    sm2d_audit* hist;     // [B][hist_cap]
     int hist_cap;
-    unsigned char* buckets;  // DeviceOutflowBucket array (bucket mode)
-    int* c2b;                // listed cell -> bucket base 4 * list position, -1 otherwise
+    unsigned char* buckets;  // DeviceOutflowBucket array (bucket mode) [4 * listed_cap]
+    int* c2b;                // listed gc -> bucket base 4 * list position, -1 otherwise
     int bucket_bytes;
-    unsigned long long* ctab;  // claim tables: Nc psi_out rows, then 4 * Nc bucket rows
+    unsigned long long* ctab;  // claim tables: B * Nc psi_out rows, then 4 * listed_cap bucket rows
     int* ccount;               // gathered ids per claim-table row
-    uint32_t* bkt_ids;         // kept ids of each bucket row [4 * Nc][32]
+    uint32_t* bkt_ids;         // kept ids of each bucket row [4 * listed_cap][32]
 };
+
+__device__ __forceinline__ int lane_of(const Dev& d, int gc) { return gc / d.Nc; }
 
 // ---------------------------------------------------------------- encodings
 __device__ __forceinline__ uint32_t make_bid(uint32_t bt, uint32_t be) { return (bt & 0xFFFu) | ((be & 0xFFFu) << 12); }
@@ -319,12 +341,11 @@ __device__ __forceinline__ int cand_find(const unsigned long long* row, uint32_t
     return -1;
 }
 
-// First claim in a cell of buffer b puts the cell on that buffer's
-// occupied-cell list.
-__device__ __forceinline__ void mark_occupied(const Dev& d, int b, int cell) {
-    if (*(volatile int*)&d.occ[b][cell] == 0 && atomicExch(&d.occ[b][cell], 1) == 0) {
-        const int k = atomicAdd(&d.it->occ_n[b], 1);
-        d.occ_list[b][k] = cell;
+// The first claim in cell gc puts it on occupancy list k.
+__device__ __forceinline__ void mark_occupied(const Dev& d, int k, int gc) {
+    if (*(volatile int*)&d.occ[k][gc] == 0 && atomicExch(&d.occ[k][gc], 1) == 0) {
+        const int i = atomicAdd(&d.gs->occ_n[k], 1);
+        d.occ_list[k][i] = gc;
     }
 }
 template <class Lay>

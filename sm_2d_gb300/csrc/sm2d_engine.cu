@@ -1,16 +1,26 @@
 // sm2d_engine.cu -- kernels, device-resident iteration loop and C ABI of the
 // SM_2D transport step on GB300 (sm_103a).
 //
-// One iteration (the body of the reference host loop k1k6_pipeline.cu:1606-2038)
-// is four kernels that read every count from device memory:
-//   k_classify   K1 active mask + per-block list counts (warp per occupied cell)
-//   k_compact    ordered active/coarse lists, iteration bookkeeping, loop condition
-//   k_transport  K2/K3 for every listed cell, warp per cell, with the K4 scatter
-//                fused (direct mode) or written to DeviceOutflowBucket (bucket mode,
-//                then k_bucket_gather = K4_BucketTransfer)
-//   k_audit      K5 audit of the iteration, clear of the consumed buffer, K6 swap
-// sm2d_run captures that body once into a CUDA graph whose while-conditional
-// node repeats it on the device until no cell holds weight.
+// The engine holds B lanes, B independent spots stacked in one set of arrays
+// (gc = lane * Nc + cell).  One pass of the iteration -- the body of the
+// reference host loop k1k6_pipeline.cu:1606-2038 -- transports every lane
+// that still has work, with these kernels, all counts read from device
+// memory:
+//   k_classify         K1 mask and classes of the occupied cells, cell list,
+//                      the w > 0 bins of the listed cells copied into the bin
+//                      list (psi_in is cleared as it is read), stopping rules,
+//                      device loop condition
+//   k_transport<KEYS>  K2/K3 per bin: the block ids each emission claims,
+//                      with their sequential claim keys
+//   k_select_buckets   bucket slots, then K4's claims on psi_out
+//   k_select_psi       psi_out slots
+//   k_transport<...>   K2/K3 per bin again, depositing into psi_out (fused K4)
+//                      or into the DeviceOutflowBucket array (then
+//                      k_bucket_push = K4_BucketTransfer)
+//   k_finalize         K5 audit per lane, K6 swap
+// sm2d_run and the batch entries capture the pass once into a CUDA graph
+// whose while-conditional node repeats it on the device until no lane has
+// work.  The single-spot entries drive lane 0 of a one-lane engine.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,6 +41,26 @@
 
 namespace sm2d {
 
+constexpr int kMaxLanes = 256;   // per-lane sums are staged in shared memory
+
+// Per-lane sums of a block staged in shared memory, flushed with one atomic
+// per (lane, value) at the end of the block.
+template <int N>
+struct LaneSums {
+    double v[kMaxLanes][N];
+    __device__ void zero(int B) {
+        for (int i = threadIdx.x; i < B * N; i += blockDim.x) (&v[0][0])[i] = 0.0;
+    }
+    __device__ void flush(const Dev& d, int first) {   // into LaneState doubles starting at `first`
+        for (int i = threadIdx.x; i < d.B * N; i += blockDim.x) {
+            const double x = (&v[0][0])[i];
+            if (x != 0.0) atomicAdd(reinterpret_cast<double*>(d.ls + i / N) + first + i % N, x);
+        }
+    }
+};
+// index of a LaneState double member, for LaneSums::flush
+#define LANE_DOUBLE(member) ((int)(offsetof(LaneState, member) / sizeof(double)))
+
 // ------------------------------------------------------------------ injection
 // LCG/Box-Muller of the source kernel (k1k6_pipeline.cu:433-447)
 __device__ __forceinline__ float source_normal(unsigned& s) {
@@ -44,10 +74,14 @@ __device__ __forceinline__ float source_normal(unsigned& s) {
 }
 
 struct BeamArgs {
-    float x0, z0, theta0, E0, W, sx, sth, sE, x_min, z_min;
+    float x0, z0, theta0, E0, W, sx, sth, sE;
     int n;
     unsigned seed;
 };
+__device__ __forceinline__ bool beam_gaussian(const BeamArgs& b) {   // gpu_transport_wrapper.cu:246
+    return b.n > 1 || b.sx > 0.0f || b.sth > 0.0f;
+}
+__device__ __forceinline__ int beam_samples(const BeamArgs& b) { return beam_gaussian(b) ? max(b.n, 0) : 1; }
 
 // One source sample: inject_source_kernel's pencil branch
 // (k1k6_pipeline.cu:325-343) or sample i of inject_gaussian_source_kernel
@@ -55,15 +89,15 @@ struct BeamArgs {
 // (device_psic.cuh:347-450: clamp into the cell, sub-cell bins, nearest
 // global bins).  Returns false when the sample leaves the grid.
 struct InjSample {
-    int cell, l;
+    int cell, l;   // lane-local cell
     uint32_t want;
     float w, E;
 };
 template <class Lay>
-__device__ bool inject_sample(const Dev& d, const BeamArgs& b, int gaussian, int i, InjSample& o) {
+__device__ bool inject_sample(const Dev& d, const BeamArgs& b, float x_min, float z_min, int i, InjSample& o) {
     float theta, E, x, z;
-    if (!gaussian) {
-        const float xr = b.x0 - b.x_min, zr = b.z0 - b.z_min;
+    if (!beam_gaussian(b)) {
+        const float xr = b.x0 - x_min, zr = b.z0 - z_min;
         int cx = (int)(xr / d.dx), cz = (int)(zr / d.dz);
         cx = cx < 0 ? 0 : (cx >= d.Nx ? d.Nx - 1 : cx);
         cz = cz < 0 ? 0 : (cz >= d.Nz ? d.Nz - 1 : cz);
@@ -80,7 +114,7 @@ __device__ bool inject_sample(const Dev& d, const BeamArgs& b, int gaussian, int
         float Es = b.E0 + b.sE * source_normal(s);
         Es = fmaxf(d.Ee[0], fminf(Es, d.Ee[d.N_E]));
         ts = fmaxf(d.th[0], fminf(ts, d.th[d.N_theta]));
-        const float xr = xs - b.x_min, zr = b.z0 - b.z_min;
+        const float xr = xs - x_min, zr = b.z0 - z_min;
         const int ix = (int)(xr / d.dx), iz = (int)(zr / d.dz);
         o.w = b.W / b.n;
         o.E = Es;
@@ -114,82 +148,83 @@ __device__ bool inject_sample(const Dev& d, const BeamArgs& b, int gaussian, int
     return true;
 }
 
-// Opens an injection: one claim pass, refused (every sample booked as a
-// source slot drop) when psi_in is not empty.
-__global__ void k_inject_begin(IterState* it) {
+// Opens an injection into the lanes whose beam has samples: one claim pass.
+// check_empty (single-lane engines) refuses an injection into an occupied
+// phase space: every sample is then booked as a source slot drop.
+__global__ void k_inject_begin(Dev d, int check_empty) {
     if (threadIdx.x || blockIdx.x) return;
-    it->ctag += 1u;
-    it->inj_skip = it->occ_n[it->parity] != 0 ? 1 : 0;
+    d.gs->ctag += 1u;
+    d.ls[0].inj_skip = (check_empty && d.gs->occ_n[d.gs->parity] != 0) ? 1 : 0;
 }
 
 // Claim pass of the injection: each in-grid sample offers its block to its
-// cell with its sample index as claim key.
+// cell with its sample index as claim key (the reference's source kernels
+// claim in sample order when run one sample at a time).  Thread per
+// (lane, sample).
 template <class Lay>
-__global__ void k_inject_keys(Dev d, const BeamArgs* bp, int gaussian) {
-    const BeamArgs b = *bp;
+__global__ void k_inject_keys(Dev d, const BeamArgs* beams, int max_n, float x_min, float z_min) {
+    const int lane = blockIdx.y;
+    const BeamArgs b = beams[lane];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (gaussian ? b.n : 1) || d.it->inj_skip) return;
+    if (i >= min(beam_samples(b), max_n) || d.ls[lane].inj_skip) return;
     InjSample o;
-    if (!inject_sample<Lay>(d, b, gaussian, i, o) || !(o.w > 0.0f)) return;
-    cand_insert(psi_row(d, o.cell), d.ccount + o.cell, d.it->ctag, o.want, (uint32_t)i, &d.it->cand_ovf);
-    mark_occupied(d, d.it->parity, o.cell);
+    if (!inject_sample<Lay>(d, b, x_min, z_min, i, o) || !(o.w > 0.0f)) return;
+    const int gc = lane * d.Nc + o.cell;
+    cand_insert(psi_row(d, gc), d.ccount + gc, d.gs->ctag, o.want, (uint32_t)i, &d.gs->cand_ovf);
+    mark_occupied(d, d.gs->parity, gc);
 }
 
 // Deposit pass of the injection: a sample whose block kept a slot adds its
 // weight there; the others are source slot drops (the reference's claim
-// without fallback).
+// without fallback).  The pencil books W and E0 W in k_source_finalize.
 template <class Lay>
-__global__ void k_inject_deposit(Dev d, const BeamArgs* bp, int gaussian) {
-    const BeamArgs b = *bp;
+__global__ void k_inject_deposit(Dev d, const BeamArgs* beams, int max_n, float x_min, float z_min) {
+    const int lane = blockIdx.y;
+    const BeamArgs b = beams[lane];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (gaussian ? b.n : 1)) return;
-    IterState* it = d.it;
+    if (i >= min(beam_samples(b), max_n)) return;
+    LaneState& L = d.ls[lane];
     InjSample o;
-    const bool in = inject_sample<Lay>(d, b, gaussian, i, o);
-    if (!gaussian) {   // the pencil books W and E0 W in k_source_finalize
-        if (in && !it->inj_skip && o.w > 0.0f) {
-            const int s = cand_find(psi_row(d, o.cell), it->ctag, o.want);
-            if (s >= 0 && d.bid[it->parity][(size_t)o.cell * kKb + s] == o.want)
-                atomicAdd(d.val[it->parity] + ((size_t)o.cell * kKb + s) * Lay::L + o.l, o.w);
-        }
-        return;
-    }
-    if (!in) {
-        atomicAdd(&it->src_oog_w, o.w);
-        atomicAdd(&it->src_oog_e, (double)(o.E * o.w));
-        return;
-    }
+    const bool in = inject_sample<Lay>(d, b, x_min, z_min, i, o);
+    const int gc = lane * d.Nc + o.cell;
     int s = -1;
-    if (!it->inj_skip && o.w > 0.0f) s = cand_find(psi_row(d, o.cell), it->ctag, o.want);
-    if (s >= 0 && d.bid[it->parity][(size_t)o.cell * kKb + s] == o.want) {
-        atomicAdd(d.val[it->parity] + ((size_t)o.cell * kKb + s) * Lay::L + o.l, o.w);
-        atomicAdd(&it->src_inj_w, o.w);
-        atomicAdd(&it->src_inj_e, (double)(o.E * o.w));
+    if (in && !L.inj_skip && o.w > 0.0f) {
+        s = cand_find(psi_row(d, gc), d.gs->ctag, o.want);
+        if (s >= 0 && d.bid[(size_t)gc * kKb + s] != o.want) s = -1;
+    }
+    if (s >= 0) atomicAdd(d.val + ((size_t)gc * kKb + s) * Lay::L + o.l, o.w);
+    if (!beam_gaussian(b)) return;
+    if (!in) {
+        atomicAdd(&L.src_oog_w, o.w);
+        atomicAdd(&L.src_oog_e, (double)(o.E * o.w));
+    } else if (s >= 0) {
+        atomicAdd(&L.src_inj_w, o.w);
+        atomicAdd(&L.src_inj_e, (double)(o.E * o.w));
     } else {
-        atomicAdd(&it->src_slot_w, o.w);
-        atomicAdd(&it->src_slot_e, (double)(o.E * o.w));
+        atomicAdd(&L.src_slot_w, o.w);
+        atomicAdd(&L.src_slot_e, (double)(o.E * o.w));
     }
 }
 
-// Weight and bin-centre energy of the w > 0 bins of buffer `buf`
-// (compute_psic_total_weight_energy, k1k6_pipeline.cu:706-768); warp per
-// occupied cell of that buffer.
+// Weight and bin-centre energy of the w > 0 bins on occupancy list `which`
+// relative to psi_in (compute_psic_total_weight_energy,
+// k1k6_pipeline.cu:706-768), per lane; warp per occupied cell.
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_totals(Dev d, int which) {
-    const int buf = d.it->parity ^ which;
-    const int n = d.it->occ_n[buf];
+    const int k = d.gs->parity ^ which;
+    const int n = d.gs->occ_n[k];
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    double W = 0.0, E = 0.0;
     for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
-        const int c = d.occ_list[buf][wi];
-        const uint32_t b = d.bid[buf][(size_t)c * kKb + lane];
+        const int gc = d.occ_list[k][wi];
+        const uint32_t b = d.bid[(size_t)gc * kKb + lane];
         unsigned used = __ballot_sync(kFull, b != kEmpty);
+        double W = 0.0, E = 0.0;
         while (used) {
             const int s = __ffs(used) - 1;
             used &= used - 1;
             const uint32_t bs = __shfl_sync(kFull, b, s);
-            const float* v = d.val[buf] + ((size_t)c * kKb + s) * Lay::L;
+            const float* v = d.val + ((size_t)gc * kKb + s) * Lay::L;
             for (int l = lane; l < Lay::L; l += 32) {
                 const float w = v[l];
                 if (w <= 0.0f) continue;
@@ -199,17 +234,38 @@ __global__ void __launch_bounds__(kThreads) k_totals(Dev d, int which) {
                 E += (double)w * (double)e_center(d, Eb);
             }
         }
-    }
-    W = warp_sum(W);
-    E = warp_sum(E);
-    if (lane == 0 && (W != 0.0 || E != 0.0)) {
-        atomicAdd(&d.it->tot_w, W);
-        atomicAdd(&d.it->tot_e, E);
+        W = warp_sum(W);
+        E = warp_sum(E);
+        if (lane == 0 && (W != 0.0 || E != 0.0)) {
+            LaneState& L = d.ls[lane_of(d, gc)];
+            atomicAdd(&L.tot_w, W);
+            atomicAdd(&L.tot_e, E);
+        }
     }
 }
 
+// Source accounting after an injection (gpu_transport_wrapper.cu:339-460):
+// the pencil books W and E0 W; the represented energy comes from k_totals.
+// Thread per lane.
+__global__ void k_source_finalize(Dev d, const BeamArgs* beams) {
+    const int lane = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lane >= d.B) return;
+    LaneState& L = d.ls[lane];
+    const BeamArgs b = beams[lane];
+    if (!beam_gaussian(b)) {
+        L.src_inj_w = b.W;
+        L.src_inj_e = (double)b.E0 * (double)b.W;
+    }
+    double loss = L.src_inj_e - L.tot_e;
+    if (fabs(loss) < 1e-12) loss = 0.0;
+    L.src_rep_loss = loss;
+    L.include_source = 1;
+    L.done = 0;
+    L.light = 0;
+}
+
 // Sum N per-thread values over the block and add them to dst[0..N) with one
-// atomic per value (dst: N consecutive IterState accumulators).
+// atomic per value.
 template <int N>
 __device__ __forceinline__ void block_add(const double (&v)[N], double* dst) {
     __shared__ double s[N][kThreads / 32];
@@ -230,31 +286,42 @@ __device__ __forceinline__ void block_add(const double (&v)[N], double* dst) {
 // ------------------------------------------------------------------ K1
 // K1_ActiveMask (k1_activemask.cu:6-48) over the occupied cells of psi_in,
 // warp per cell: the cell's class (active / coarse with w > 0,
-// compact_coarse_list k1k6_pipeline.cu:625-665), its place in this
-// iteration's cell list and bucket map, and, for a listed cell, its w > 0
-// bins appended to the bin list (contiguous per cell) for the transport.
-// The slot values are read as a flat run of float4s, eight loads in flight
-// per lane.  The last block publishes the counts, applies the stopping
-// rules, resets the per-iteration accumulators and sets the device loop
-// condition.
+// compact_coarse_list k1k6_pipeline.cu:625-665), its place in this pass's
+// cell list and bucket map, and, for a listed cell, its w > 0 bins appended
+// to the bin list (contiguous per cell) for the transport.  The slot values
+// are read as a flat run of float4s, eight loads in flight per lane; the
+// cell is then cleared, so that the storage can receive psi_out.  A lane
+// whose stopping rule was met consumes its cells without transport.  The
+// last block publishes the counts, settles each lane, resets the per-lane
+// accumulators and sets the device loop condition.
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphConditionalHandle cond, int use_cond) {
     constexpr int Q = Lay::L / 4, NW = kThreads / 32, U = 8;
-    __shared__ int s_cnt[2];
-    __shared__ int s_last, s_halt, s_listed;
+    __shared__ int s_cnt[kMaxLanes][3];   // listed active, listed coarse, their slots
+    __shared__ int s_last;
     __shared__ uint8_t s_slot[NW][kKb];   // r-th claimed slot of the warp's cell
-    IterState* it = d.it;
-    const int par = it->parity;
-    const int nocc = it->occ_n[par];
-    const unsigned long long g = it->gen + 1;   // number of this classification
+    IterGlobal* gs = d.gs;
+    if (gs->pass >= gs->max_pass) {   // paused: leave the phase space as it is
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            gs->halt = 1;
+            if (use_cond) cudaGraphSetConditional(cond, 0u);
+        }
+        return;
+    }
+    const int par = gs->parity;
+    const int nocc = gs->occ_n[par];
+    const unsigned long long g = gs->gen + 1;   // number of this classification
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
+    for (int i = threadIdx.x; i < d.B * 3; i += blockDim.x) (&s_cnt[0][0])[i] = 0;
     __syncthreads();
     for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < nocc; wi += nw) {
         const int c = d.occ_list[par][wi];
-        const uint32_t b = d.bid[par][(size_t)c * kKb + lane];
+        const int ln = lane_of(d, c);
+        const bool light = d.ls[ln].light != 0;
+        uint32_t* ids = d.bid + (size_t)c * kKb;
+        const uint32_t b = ids[lane];
         const bool used = b != kEmpty;
         const uint32_t be = (b >> 12) & 0xFFFu;
         const bool c_on = __any_sync(kFull, used && be <= (uint32_t)d.b_on);
@@ -264,7 +331,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         if (used) s_slot[wid][__popc(um & lt)] = (uint8_t)lane;
         __syncwarp();
         const int F = __popc(um) * Q;   // float4s of the claimed slots
-        const float4* vc = reinterpret_cast<const float4*>(d.val[par] + (size_t)c * kKb * Lay::L);
+        float4* vc = reinterpret_cast<float4*>(d.val + (size_t)c * kKb * Lay::L);
         float ws = 0.0f;
         int nz = 0;
         for (int f0 = 0; f0 < F; f0 += 32 * U) {
@@ -284,128 +351,136 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         for (int o = 16; o > 0; o >>= 1) nz += __shfl_xor_sync(kFull, nz, o);
         const bool hw = nz > 0;
         const bool prev = d.act_gen[c] == g - 1;
-        const bool act = (c_on || (prev && c_off)) && ws > d.wmin;
-        const int cls = act ? 2 : (hw ? 1 : 0);
+        const bool act = !light && (c_on || (prev && c_off)) && ws > d.wmin;
+        const int cls = light ? 0 : (act ? 2 : (hw ? 1 : 0));
         int base = 0;
         if (lane == 0) {
             d.cls[c] = (uint8_t)cls;
             if (act) d.act_gen[c] = g;
             if (cls) {
-                const int idx = atomicAdd(&it->acc_listed, 1);
-                atomicAdd(&it->acc_items, __popc(um));
-                base = atomicAdd(&it->acc_bins, nz);
-                d.listed[idx] = (uint32_t)c;
-                d.c2b[c] = 4 * idx;
-                atomicAdd(&s_cnt[act ? 0 : 1], 1);
+                const int idx = atomicAdd(&gs->acc_listed, 1);
+                atomicAdd(&gs->acc_items, __popc(um));
+                base = atomicAdd(&gs->acc_bins, nz);
+                if (idx < d.listed_cap) {
+                    d.listed[idx] = (uint32_t)c;
+                    d.c2b[c] = 4 * idx;
+                }
+                atomicAdd(&s_cnt[ln][act ? 0 : 1], 1);
+                atomicAdd(&s_cnt[ln][2], __popc(um));
             }
         }
         if (cls) {
+            const int idx_ok = __shfl_sync(kFull, lane == 0 ? (d.c2b[c] >= 0 ? 1 : 0) : 0, 0);
             base = __shfl_sync(kFull, base, 0);
-            if (base + nz > d.bins_cap) {   // no room: the last block stops the run
-                if (lane == 0) atomicAdd(&it->bin_ovf, 1);
-                continue;
-            }
-            // seed slot of each claimed slot: the rank of its block id
-            int rk = 0;
-            for (int t = 0; t < kKb; ++t) {
-                const uint32_t bt = __shfl_sync(kFull, b, t);
-                rk += (bt != kEmpty && bt < b) ? 1 : 0;
-            }
-            const uint32_t k3 = cls == 2 ? 1u : 0u;
-            int off = base;
-            for (int f0 = 0; f0 < F; f0 += 32 * U) {
-                float4 r[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {   // all loads first (L2 hits of the first read)
-                    const int f = f0 + 32 * u + lane;
-                    r[u] = f < F ? __ldcg(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q)
-                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!idx_ok || base + nz > d.bins_cap) {   // no room: the last block stops the run
+                if (lane == 0) atomicAdd(&gs->bin_ovf, 1);
+            } else {
+                // seed slot of each claimed slot: the rank of its block id
+                int rk = 0;
+                for (int t = 0; t < kKb; ++t) {
+                    const uint32_t bt = __shfl_sync(kFull, b, t);
+                    rk += (bt != kEmpty && bt < b) ? 1 : 0;
                 }
+                const uint32_t k3 = cls == 2 ? 1u : 0u;
+                int off = base;
+                for (int f0 = 0; f0 < F; f0 += 32 * U) {
+                    float4 r[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int f = f0 + 32 * u + lane;
-                    const int s = f < F ? s_slot[wid][f / Q] : 0;
-                    const int cnt = (r[u].x > 0.0f) + (r[u].y > 0.0f) + (r[u].z > 0.0f) + (r[u].w > 0.0f);
-                    int inc = cnt;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int y = __shfl_up_sync(kFull, inc, o);
-                        if (lane >= o) inc += y;
+                    for (int u = 0; u < U; ++u) {   // all loads first (L2 hits of the first read)
+                        const int f = f0 + 32 * u + lane;
+                        r[u] = f < F ? __ldcg(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q)
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
-                    const uint32_t bs = __shfl_sync(kFull, b, s);
-                    const uint32_t meta = (uint32_t)s | ((uint32_t)__shfl_sync(kFull, rk, s) << 5) | (k3 << 18);
-                    int p = off + inc - cnt;
-                    const float c4[4] = {r[u].x, r[u].y, r[u].z, r[u].w};
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (c4[k] > 0.0f)
-                            d.bins[p++] = make_uint4((uint32_t)c, meta | ((uint32_t)(4 * (f % Q) + k) << 10),
-                                                     __float_as_uint(c4[k]), bs);
-                    off += __shfl_sync(kFull, inc, 31);
+                    for (int u = 0; u < U; ++u) {
+                        const int f = f0 + 32 * u + lane;
+                        const int s = f < F ? s_slot[wid][f / Q] : 0;
+                        const int cnt = (r[u].x > 0.0f) + (r[u].y > 0.0f) + (r[u].z > 0.0f) + (r[u].w > 0.0f);
+                        int inc = cnt;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int y = __shfl_up_sync(kFull, inc, o);
+                            if (lane >= o) inc += y;
+                        }
+                        const uint32_t bs = __shfl_sync(kFull, b, s);
+                        const uint32_t meta = (uint32_t)s | ((uint32_t)__shfl_sync(kFull, rk, s) << 5) | (k3 << 18);
+                        int p = off + inc - cnt;
+                        const float c4[4] = {r[u].x, r[u].y, r[u].z, r[u].w};
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (c4[k] > 0.0f)
+                                d.bins[p++] = make_uint4((uint32_t)c, meta | ((uint32_t)(4 * (f % Q) + k) << 10),
+                                                         __float_as_uint(c4[k]), bs);
+                        off += __shfl_sync(kFull, inc, 31);
+                    }
                 }
             }
         }
+        // psi_in of the cell is consumed: clear it for psi_out
+        for (int f = lane; f < F; f += 32) __stcs(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q, make_float4(0.f, 0.f, 0.f, 0.f));
+        ids[lane] = kEmpty;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        if (s_cnt[0]) atomicAdd(&it->acc_active, s_cnt[0]);
-        if (s_cnt[1]) atomicAdd(&it->acc_coarse, s_cnt[1]);
-        __threadfence();
-        s_last = atomicAdd(&it->blocks_done, 1u) == gridDim.x - 1;
+    for (int i = threadIdx.x; i < d.B; i += blockDim.x) {
+        if (s_cnt[i][0]) atomicAdd(&d.ls[i].acc_active, s_cnt[i][0]);
+        if (s_cnt[i][1]) atomicAdd(&d.ls[i].acc_coarse, s_cnt[i][1]);
+        if (s_cnt[i][2]) atomicAdd(&d.ls[i].acc_slots, s_cnt[i][2]);
     }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&gs->blocks_done, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!s_last) return;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        volatile IterState* v = it;
-        int na = v->acc_active, nc = v->acc_coarse;
-        const int nl = v->acc_listed, ni = v->acc_items, nb = v->acc_bins;
-        it->acc_active = it->acc_coarse = it->acc_listed = it->acc_items = it->acc_bins = 0;
-        it->gen = g;
-        it->ctag += 1u;   // claim pass of this iteration
-        // C1 stopping rule: in-flight weight (the last audit's W_out) below a
-        // fraction of the injected weight ends the run; the rest is booked as
-        // a terminal transport drop (k1k6_pipeline.cu:1677-1706 books it too)
-        const bool light = d.stop_frac > 0.0f && it->iter > 0 && (na + nc) > 0 &&
-                           it->last.W_out_total < d.stop_frac * it->src_inj_w;
-        if (light) {
-            it->transport_drop_w += it->last.W_out_total;
-            it->transport_drop_e += it->last.E_out_total;
-            na = nc = 0;
+    __threadfence();
+    // settle each lane: counts, C1 stopping rule, accumulators
+    __shared__ int s_work;
+    if (threadIdx.x == 0) s_work = 0;
+    __syncthreads();
+    for (int ln = threadIdx.x; ln < d.B; ln += blockDim.x) {
+        LaneState& L = d.ls[ln];
+        volatile LaneState* v = &L;
+        const int na = v->acc_active, nc = v->acc_coarse, nsl = v->acc_slots;
+        L.acc_active = L.acc_coarse = L.acc_slots = 0;
+        if (L.light) {
+            // in-flight weight below a fraction of the injected weight ends
+            // the spot; the rest is booked as a terminal transport drop
+            // (k1k6_pipeline.cu:1677-1706 books it too)
+            L.transport_drop_w += L.last.W_out_total;
+            L.transport_drop_e += L.last.E_out_total;
+            L.light = 0;
         }
-        it->n_active = na;
-        it->n_coarse = nc;
-        const bool done = (na + nc) == 0;
-        it->done = done ? 1 : 0;
-        // a bin list that outgrew its capacity ends the run (reported by the
-        // host API as SM2D_ERR_ALLOC)
-        const bool halt = done || it->iter >= it->max_iter || v->bin_ovf != 0;
-        it->halt = halt ? 1 : 0;
-        it->n_listed = halt ? 0 : nl;
-        it->n_items = halt ? 0 : ni;
-        it->n_bins = halt ? 0 : nb;
-        double* acc = &it->drop_w;   // the 14 per-iteration accumulators
+        L.n_active = na;
+        L.n_coarse = nc;
+        const bool work = (na + nc) > 0;
+        L.done = work ? 0 : 1;
+        L.work = work ? 1 : 0;
+        double* acc = &L.drop_w;   // the 14 per-iteration accumulators
         for (int k = 0; k < 14; ++k) acc[k] = 0.0;
-        it->blocks_done = 0;
-        if (!halt) {
-            it->cell_steps += (double)(na + nc);
-            it->slots_in += (double)ni;
+        if (work) {
+            L.cell_steps += (double)(na + nc);
+            L.slots_in += (double)nsl;
+            atomicAdd(&s_work, 1);
         }
-        if (use_cond) cudaGraphSetConditional(cond, (!halt && it->iter + 1 < it->max_iter) ? 1u : 0u);
-        s_halt = halt ? 1 : 0;
-        s_listed = nl;
     }
     __syncthreads();
-    if (s_halt) {   // no transport or finalize follows: release this pass's cell marks
-        for (int i = threadIdx.x; i < s_listed; i += blockDim.x) {
-            const int c = (int)d.listed[i];
-            d.cls[c] = 0;
-            d.c2b[c] = -1;
-        }
-    }
+    if (threadIdx.x != 0) return;
+    volatile IterGlobal* v = gs;
+    const int nl = v->acc_listed, ni = v->acc_items, nb = v->acc_bins;
+    gs->acc_listed = gs->acc_items = gs->acc_bins = 0;
+    gs->gen = g;
+    gs->ctag += 1u;   // claim pass of this iteration
+    // a cell or bin list that outgrew its capacity ends the run (reported by
+    // the host API as SM2D_ERR_ALLOC)
+    const bool halt = s_work == 0 || v->bin_ovf != 0;
+    gs->halt = halt ? 1 : 0;
+    gs->n_listed = halt ? 0 : min(nl, d.listed_cap);
+    gs->n_items = halt ? 0 : ni;
+    gs->n_bins = halt ? 0 : nb;
+    gs->blocks_done = 0;
+    if (use_cond) cudaGraphSetConditional(cond, (!halt && gs->pass + 1 < gs->max_pass) ? 1u : 0u);
 }
 
-// Ascending active and coarse lists from the classes of this iteration
+// Ascending active and coarse lists of lane 0 from the classes of this pass
 // (the reference's ordered compaction); one block, on request of the
 // stepping API.
 __global__ void __launch_bounds__(1024) k_order_lists(Dev d) {
@@ -450,17 +525,20 @@ __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
 // One thread per w > 0 bin of the listed cells.  PASS_KEYS gathers the
 // claim candidates; the deposit passes add the weights, book per-cell tally
 // increments in the dl_* arrays (one atomic per cell run of a warp) and the
-// audit sums per block.
+// per-lane audit sums (staged per block in shared memory).
 template <class Lay, int PASS>
 __global__ void __launch_bounds__(kThreads, 2) k_transport(Dev d) {
-    IterState* it = d.it;
-    if (it->halt) return;
-    const int par = it->parity;
-    const int n = it->n_bins;
-    const uint32_t tag = it->ctag;
+    __shared__ LaneSums<6> s_sum;   // drop_w, drop_e, Win, Ein, Wout, Eout
+    IterGlobal* gs = d.gs;
+    if (gs->halt) return;
+    const int par = gs->parity;
+    const int n = gs->n_bins;
+    const uint32_t tag = gs->ctag;
     const int lane = threadIdx.x & 31;
-    const unsigned salt = d.salt ? (unsigned)it->iter * 0x9E3779B9u : 0u;
-    double g[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // drop_w, drop_e, Win, Ein, Wout, Eout, -
+    if (PASS != PASS_KEYS) {
+        s_sum.zero(d.B);
+        __syncthreads();
+    }
     const int stride = gridDim.x * blockDim.x;
     for (int w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < n; w0 += stride) {
         const int i = w0 + lane;
@@ -470,9 +548,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_transport(Dev d) {
             // the claim pass keeps the list in L2 for the deposit pass
             const uint4 r = PASS == PASS_KEYS ? __ldcg(d.bins + i) : __ldcs(d.bins + i);
             cell = (int)r.x;
+            const int ln = lane_of(d, cell);
             const int slot = (int)(r.y & 31u), sslot = (int)((r.y >> 5) & 31u), lidx = (int)((r.y >> 10) & 0xFFu);
             const bool k3 = ((r.y >> 18) & 1u) != 0;
-            transport_bin<Lay, PASS>(d, par, k3, cell, r.w, slot, sslot, lidx, __uint_as_float(r.z), salt, tag, t);
+            const unsigned salt = d.salt ? (unsigned)d.ls[ln].iter * 0x9E3779B9u : 0u;
+            transport_bin<Lay, PASS>(d, par, k3, cell, cell - ln * d.Nc, r.w, slot, sslot, lidx, __uint_as_float(r.z),
+                                     salt, tag, t);
         }
         if (PASS != PASS_KEYS) {
             unsigned same[5];
@@ -485,6 +566,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_transport(Dev d) {
             const double edep = seg_sum(t.edep, same), ecut = seg_sum(t.e_cut, same), enuc = seg_sum(t.e_nuc, same),
                          ebnd = seg_sum(t.e_bnd, same);
             const float wcut = seg_sum(t.w_cut, same), wnuc = seg_sum(t.w_nuc, same), wbnd = seg_sum(t.w_bnd, same);
+            const double dw = seg_sum(t.drop_w, same), de = seg_sum(t.drop_e, same), wi = seg_sum(t.Win, same),
+                         ei = seg_sum(t.Ein, same), wo = seg_sum(t.Wout, same), eo = seg_sum(t.Eout, same);
             const int prev_cell = __shfl_up_sync(kFull, cell, 1);
             if (cell >= 0 && (lane == 0 || prev_cell != cell)) {
                 if (edep != 0.0) atomicAdd(d.dl_edep + cell, edep);
@@ -494,12 +577,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_transport(Dev d) {
                 if (wcut != 0.0f) atomicAdd(d.dl_wcut + cell, wcut);
                 if (wnuc != 0.0f) atomicAdd(d.dl_wnuc + cell, wnuc);
                 if (wbnd != 0.0f) atomicAdd(d.dl_wbnd + cell, wbnd);
+                double* ls = s_sum.v[lane_of(d, cell)];
+                if (dw != 0.0) atomicAdd(ls + 0, dw);
+                if (de != 0.0) atomicAdd(ls + 1, de);
+                atomicAdd(ls + 2, wi);
+                atomicAdd(ls + 3, ei);
+                if (wo != 0.0) atomicAdd(ls + 4, wo);
+                if (eo != 0.0) atomicAdd(ls + 5, eo);
             }
-            g[0] += t.drop_w; g[1] += t.drop_e; g[2] += t.Win; g[3] += t.Ein;
-            g[4] += t.Wout; g[5] += t.Eout;
         }
     }
-    if (PASS != PASS_KEYS) block_add<7>(g, &it->drop_w);
+    if (PASS != PASS_KEYS) {
+        __syncthreads();
+        s_sum.flush(d, LANE_DOUBLE(drop_w));
+    }
 }
 
 // ------------------------------------------------------------------ slot selection
@@ -572,17 +663,17 @@ template <class Lay, bool BUCKET>
 __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
     constexpr int NW = kThreads / 32;
     __shared__ SelScratch s_sel[NW];
-    IterState* it = d.it;
-    if (it->halt) return;
-    const int out = it->parity ^ 1;
-    const int n = 4 * it->n_listed;
-    const uint32_t tag = it->ctag;
+    IterGlobal* gs = d.gs;
+    if (gs->halt) return;
+    const int out = gs->parity ^ 1;
+    const int n = 4 * gs->n_listed;
+    const uint32_t tag = gs->ctag;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int wi = blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
         const int face = wi & 3;
         const int src = (int)d.listed[wi >> 2];
         uint32_t* kept = d.bkt_ids + (size_t)wi * kKb;
-        const int nk = select_row(bucket_row(d, wi), d.ccount + d.Nc + wi, tag, s_sel[wid], kept, lane);
+        const int nk = select_row(bucket_row(d, wi), d.ccount + (size_t)d.B * d.Nc + wi, tag, s_sel[wid], kept, lane);
         if (BUCKET) {
             unsigned char* b = d.buckets + (size_t)wi * d.bucket_bytes;
             bucket_ids(b)[lane] = lane < nk ? s_sel[wid].kept[lane] : kEmpty;
@@ -591,7 +682,7 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
             for (int k = lane; k < nk * Lay::L; k += 32) v[k] = 0.0f;
         }
         if (nk == 0) continue;
-        const int ix = src % d.Nx, iz = src / d.Nx;
+        const int ix = src % d.Nx, iz = (src / d.Nx) % d.Nz;
         int dst = -1;
         if (face == FACE_ZP && iz + 1 < d.Nz) dst = src + d.Nx;
         if (face == FACE_ZM && iz > 0) dst = src - d.Nx;
@@ -601,7 +692,7 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
         const int k3 = d.cls[src] == 2 ? 1 : 0;
         if (lane < nk)
             cand_insert(psi_row(d, dst), d.ccount + dst, tag, s_sel[wid].kept[lane], k4_key(k3, face, lane),
-                        &it->cand_ovf);
+                        &gs->cand_ovf);
         if (lane == 0) mark_occupied(d, out, dst);
     }
 }
@@ -612,20 +703,22 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
 __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
     constexpr int NW = kThreads / 32;
     __shared__ SelScratch s_sel[NW];
-    IterState* it = d.it;
-    if (which && it->halt) return;
-    const int buf = it->parity ^ which;
-    const int n = it->occ_n[buf];
-    const uint32_t tag = it->ctag;
+    __shared__ LaneSums<1> s_sum;
+    IterGlobal* gs = d.gs;
+    if (which && gs->halt) return;
+    const int k = gs->parity ^ which;
+    const int n = gs->occ_n[k];
+    const uint32_t tag = gs->ctag;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double kept_slots = 0.0;
+    s_sum.zero(d.B);
+    __syncthreads();
     for (int wi = blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
-        const int cell = d.occ_list[buf][wi];
-        const int nk = select_row(psi_row(d, cell), d.ccount + cell, tag, s_sel[wid], d.bid[buf] + (size_t)cell * kKb,
-                                  lane);
-        if (lane == 0) kept_slots += (double)nk;
+        const int gc = d.occ_list[k][wi];
+        const int nk = select_row(psi_row(d, gc), d.ccount + gc, tag, s_sel[wid], d.bid + (size_t)gc * kKb, lane);
+        if (which && lane == 0) atomicAdd(&s_sum.v[lane_of(d, gc)][0], (double)nk);
     }
-    if (which && lane == 0 && kept_slots != 0.0) atomicAdd(&it->slots_out_it, kept_slots);
+    __syncthreads();
+    if (which) s_sum.flush(d, LANE_DOUBLE(slots_out_it));
 }
 
 // ------------------------------------------------------------------ bucket mode (reference structure)
@@ -635,18 +728,19 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
 // resolved to (lidx remap when it folded into a nearer id).
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
-    IterState* it = d.it;
-    if (it->halt) return;
-    const int out = it->parity ^ 1;
-    const int n = 4 * it->n_listed;
-    const uint32_t tag = it->ctag;
+    __shared__ LaneSums<6> s_sum;   // drop_w, drop_e, -, -, Wout, Eout
+    IterGlobal* gs = d.gs;
+    if (gs->halt) return;
+    const int n = 4 * gs->n_listed;
+    const uint32_t tag = gs->ctag;
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    double g[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // drop_w, drop_e, -, -, Wout, Eout, -
+    s_sum.zero(d.B);
+    __syncthreads();
     for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
         const int face = wi & 3;
         const int src = (int)d.listed[wi >> 2];
-        const int ix = src % d.Nx, iz = src / d.Nx;
+        const int ix = src % d.Nx, iz = (src / d.Nx) % d.Nz;
         int dst = -1;
         if (face == FACE_ZP && iz + 1 < d.Nz) dst = src + d.Nx;
         if (face == FACE_ZM && iz > 0) dst = src - d.Nx;
@@ -657,7 +751,8 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
         const uint32_t sb = bucket_ids(b)[lane];
         unsigned um = __ballot_sync(kFull, sb != kEmpty);
         const float* bv = bucket_vals(b);
-        const uint32_t* kept = d.bid[out] + (size_t)dst * kKb;
+        const uint32_t* kept = d.bid + (size_t)dst * kKb;
+        double g[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         while (um) {
             const int s = __ffs(um) - 1;
             um &= um - 1;
@@ -665,7 +760,7 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
             uint32_t sel = bid;
             const int os = resolve(d, psi_row(d, dst), kept, tag, bid, sel);
             const float* v = bv + (size_t)s * Lay::L;
-            float* o = os >= 0 ? d.val[out] + ((size_t)dst * kKb + os) * Lay::L : nullptr;
+            float* o = os >= 0 ? d.val + ((size_t)dst * kKb + os) * Lay::L : nullptr;
             double eshift = 0.0;
             for (int l = lane; l < Lay::L; l += 32) {
                 const float w = v[l];
@@ -686,14 +781,23 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
             eshift = warp_sum(eshift);
             if (lane == 0 && eshift != 0.0) atomicAdd(d.dl_edep + src, eshift);
         }
+        double* ls = s_sum.v[lane_of(d, src)];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double x = warp_sum(g[k]);
+            if (lane == 0 && x != 0.0) atomicAdd(ls + k, x);
+        }
     }
-    block_add<7>(g, &it->drop_w);
+    __syncthreads();
+    s_sum.flush(d, LANE_DOUBLE(drop_w));
 }
 
-// ------------------------------------------------------------------ K5 + clear + K6
-__device__ void finalize_audit(Dev& d) {
-    volatile IterState* v = d.it;
-    IterState* it = d.it;
+// ------------------------------------------------------------------ K5 + K6
+// Audit record of one lane's iteration (k5_audit.cu:22-167) from its
+// accumulators, and the lane's bookkeeping.
+__device__ void finalize_lane(const Dev& d, int ln) {
+    volatile LaneState* v = d.ls + ln;
+    LaneState& L = d.ls[ln];
     sm2d_audit r;
     memset(&r, 0, sizeof r);
     r.W_in_total = (float)v->Win;
@@ -732,18 +836,20 @@ __device__ void finalize_audit(Dev& d) {
     r.E_error = Ee_;
     r.E_pass = (isfinite(Ee_) && Ee_ < 1e-5f) ? 1 : 0;
     const double resid = r.E_in_total - Er;
-    if (isfinite(resid)) it->audit_residual += resid;
-    it->transport_drop_w += dw;
-    it->transport_drop_e += de;
-    it->slots_out += v->slots_out_it;
-    const int k = it->iter;
-    if (k < d.hist_cap) d.hist[k] = r;
-    it->last = r;
-    it->iter = k + 1;
-    it->include_source = 0;
-    it->occ_n[it->parity] = 0;   // the consumed buffer is empty again
-    it->parity ^= 1;
-    it->blocks_done = 0;
+    if (isfinite(resid)) L.audit_residual += resid;
+    L.transport_drop_w += dw;
+    L.transport_drop_e += de;
+    L.slots_out += v->slots_out_it;
+    const int k = L.iter;
+    if (k < d.hist_cap) d.hist[(size_t)ln * d.hist_cap + k] = r;
+    L.last = r;
+    L.w_fail += r.W_pass ? 0 : 1;
+    L.e_fail += r.E_pass ? 0 : 1;
+    L.iter = k + 1;
+    L.include_source = 0;
+    // C1 stopping rule, applied by the next classification: in-flight
+    // weight below a fraction of the injected weight
+    L.light = (d.stop_frac > 0.0f && r.W_out_total < d.stop_frac * L.src_inj_w) ? 1 : 0;
 }
 
 // Fold this iteration's increment of tally k of cell c into the cumulative
@@ -769,145 +875,136 @@ __device__ __forceinline__ double fold_tally(const Dev& d, int c, int k) {
     return (double)fmaxf(0.0f, w1 - w0);
 }
 
-// K5 audit of the iteration and clear of the consumed buffer, warp per
-// occupied cell of psi_in; the last block writes the audit record and swaps
-// the buffers (K6).
-template <class Lay>
+// K5 audit of the iteration, warp per cell of psi_in's list (whose storage
+// the classify kernel already cleared); the last block writes each working
+// lane's audit record and swaps the occupancy lists (K6).
 __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
     constexpr int NW = kThreads / 32;
-    __shared__ double s_acc[7][NW];
+    __shared__ LaneSums<7> s_sum;   // Edep, Ecut, Enuc, Ebnd, Wcut, Wnuc, Wbnd
     __shared__ int s_last;
-    IterState* it = d.it;
-    if (it->halt) return;
-    const int in = it->parity;
-    const int nocc = it->occ_n[in];
+    IterGlobal* gs = d.gs;
+    if (gs->halt) return;
+    const int in = gs->parity;
+    const int nocc = gs->occ_n[in];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nw = gridDim.x * NW;
-    double part = 0.0;   // lane k < 7: audit share of tally k (edep, e_cut, e_nuc, e_bnd, w_cut, w_nuc, w_bnd)
+    s_sum.zero(d.B);
+    __syncthreads();
     for (int wi = blockIdx.x * NW + wid; wi < nocc; wi += nw) {
         const int c = d.occ_list[in][wi];
         const int cls = d.cls[c];
-        uint32_t* ids = d.bid[in] + (size_t)c * kKb;
-        unsigned um = __ballot_sync(kFull, ids[lane] != kEmpty);
-        while (um) {   // clear the consumed slots
-            const int s = __ffs(um) - 1;
-            um &= um - 1;
-            float4* v = reinterpret_cast<float4*>(d.val[in] + ((size_t)c * kKb + s) * Lay::L);
-            for (int q = lane; q < Lay::L / 4; q += 32) __stcs(v + q, make_float4(0.f, 0.f, 0.f, 0.f));
+        if (cls && lane < 7) {
+            const double x = fold_tally(d, c, lane);
+            if (x != 0.0) atomicAdd(&s_sum.v[lane_of(d, c)][lane], x);
         }
-        if (cls && lane < 7) part += fold_tally(d, c, lane);
-        ids[lane] = kEmpty;
         if (lane == 0) {
             d.occ[in][c] = 0;
             d.cls[c] = 0;
             if (cls) d.c2b[c] = -1;
         }
     }
-    if (lane < 7) s_acc[lane][wid] = part;
     __syncthreads();
-    if (threadIdx.x < 7) {
-        double a = 0.0;
-        for (int w = 0; w < NW; ++w) a += s_acc[threadIdx.x][w];
-        if (a != 0.0) atomicAdd(&it->Edep + threadIdx.x, a);
-        __threadfence();
-    }
+    s_sum.flush(d, LANE_DOUBLE(Edep));
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&it->blocks_done, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) s_last = atomicAdd(&gs->blocks_done, 1u) == gridDim.x - 1;
     __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-        __threadfence();
-        finalize_audit(d);
+    if (!s_last) return;
+    __threadfence();
+    for (int ln = threadIdx.x; ln < d.B; ln += blockDim.x)
+        if (d.ls[ln].work) finalize_lane(d, ln);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        gs->occ_n[in] = 0;   // the consumed list is empty again
+        gs->parity = in ^ 1;
+        gs->pass += 1;
+        gs->blocks_done = 0;
     }
 }
 
 // ------------------------------------------------------------------ spot pipeline helpers
-// Clear every claimed slot of both buffers (reset between spots).
+// Clear the phase space of every listed cell of both occupancy lists (reset
+// between spots).
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_clear_all(Dev d) {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int b = 0; b < 2; ++b) {
-        const int n = d.it->occ_n[b];
+    for (int k = 0; k < 2; ++k) {
+        const int n = d.gs->occ_n[k];
         for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
-            const int c = d.occ_list[b][wi];
-            uint32_t* ids = d.bid[b] + (size_t)c * kKb;
+            const int c = d.occ_list[k][wi];
+            uint32_t* ids = d.bid + (size_t)c * kKb;
             const uint32_t x = ids[lane];
             unsigned um = __ballot_sync(kFull, x != kEmpty);
             while (um) {
                 const int s = __ffs(um) - 1;
                 um &= um - 1;
-                float4* v = reinterpret_cast<float4*>(d.val[b] + ((size_t)c * kKb + s) * Lay::L);
+                float4* v = reinterpret_cast<float4*>(d.val + ((size_t)c * kKb + s) * Lay::L);
                 for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             ids[lane] = kEmpty;
-            if (lane == 0) { d.occ[b][c] = 0; d.cls[c] = 0; }
+            if (lane == 0) { d.occ[k][c] = 0; d.cls[c] = 0; d.c2b[c] = -1; }
         }
     }
 }
 
-__global__ void k_reset_state(IterState* it) {
+// New spots in every lane: zero the iteration and lane states.  The
+// classification number runs on, one step past the last spot's, so that no
+// cell reads as active in a previous classification; the claim pass number
+// runs on too, and restarts after a wipe of the claim tables when it nears
+// its 32-bit limit.
+__global__ void k_reset_state(Dev d) {
     if (threadIdx.x || blockIdx.x) return;
-    // the classification number runs on, one step past the last spot's, so
-    // that no cell reads as active in a previous classification; the claim
-    // pass number runs on too, and restarts after a wipe of the tables when
-    // it nears its 32-bit limit
-    const unsigned long long g = it->gen;
-    uint32_t tag = it->ctag;
-    const int ovf = it->cand_ovf, miss = it->cand_miss;
+    IterGlobal* gs = d.gs;
+    const unsigned long long g = gs->gen;
+    uint32_t tag = gs->ctag;
+    const int ovf = gs->cand_ovf, miss = gs->cand_miss;
     int wipe = 0;
     if (tag >= 0xFFF00000u) {
         tag = 0;
         wipe = 1;
     }
-    memset(it, 0, sizeof(IterState));
-    it->gen = g + 1;
-    it->ctag = tag;
-    it->cand_ovf = ovf;
-    it->cand_miss = miss;
-    it->wipe = wipe;
-    it->max_iter = INT_MAX;
+    memset(gs, 0, sizeof(IterGlobal));
+    gs->gen = g + 1;
+    gs->ctag = tag;
+    gs->cand_ovf = ovf;
+    gs->cand_miss = miss;
+    gs->wipe = wipe;
+    gs->max_pass = INT_MAX;
+    for (int ln = 0; ln < d.B; ++ln) {
+        memset(&d.ls[ln], 0, sizeof(LaneState));
+        d.ls[ln].done = 1;
+    }
 }
 
 // Clear every claim-table row when a tag wrap is pending (grid-stride).
-__global__ void k_wipe(Dev d, size_t n_words, int n_counts) {
-    if (!d.it->wipe) return;
+__global__ void k_wipe(Dev d, size_t n_words, size_t n_counts) {
+    if (!d.gs->wipe) return;
     const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, st = (size_t)gridDim.x * blockDim.x;
     for (size_t i = i0; i < n_words; i += st) d.ctab[i] = ~0ull;
-    for (size_t i = i0; i < (size_t)n_counts; i += st) d.ccount[i] = 0;
+    for (size_t i = i0; i < n_counts; i += st) d.ccount[i] = 0;
 }
 
-__global__ void k_set_iter_limit(IterState* it, int more) {
+__global__ void k_set_pass_limit(IterGlobal* gs, int more) {
     if (threadIdx.x || blockIdx.x) return;
-    const long long lim = (long long)it->iter + more;
-    it->max_iter = lim > INT_MAX ? INT_MAX : (int)lim;
+    const long long lim = (long long)gs->pass + more;
+    gs->max_pass = lim > INT_MAX ? INT_MAX : (int)lim;
 }
 
-// Source accounting after injection (gpu_transport_wrapper.cu:339-460): the
-// pencil path books W and E0*W; the represented energy comes from k_totals.
-__global__ void k_source_finalize(IterState* it, const BeamArgs* b, int gaussian) {
-    if (threadIdx.x || blockIdx.x) return;
-    if (!gaussian) {
-        it->src_inj_w = b->W;
-        it->src_inj_e = (double)b->E0 * (double)b->W;
-    }
-    double loss = it->src_inj_e - it->tot_e;
-    if (fabs(loss) < 1e-12) loss = 0.0;
-    it->src_rep_loss = loss;
-    it->include_source = 1;
-    it->done = 0;
-}
-
-// Lateral MCS post-convolution of EdepC, one thread per output cell
-// (gpu_transport_wrapper.cu:551-616; kernels built on the host at create).
+// Lateral MCS post-convolution of EdepC, one thread per output cell of each
+// lane (gpu_transport_wrapper.cu:551-616; kernels built on the host at
+// create).
 __global__ void k_dose(const double* __restrict__ edep, const int* __restrict__ half, const double* __restrict__ ker,
-                       int kstride, int Nx, int Nz, double* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= Nx * Nz) return;
-    const int iz = i / Nx, ix = i - iz * Nx;
+                       int kstride, int Nx, int Nz, int B, double* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nc = (long long)Nx * Nz;
+    if (i >= nc * B) return;
+    const int lc = (int)(i % nc);
+    const int iz = lc / Nx, ix = lc - iz * Nx;
     const int h = half[iz];
     if (h == 0) { out[i] = edep[i]; return; }
     const double* k = ker + (size_t)iz * kstride;
-    const double* row = edep + (size_t)iz * Nx;
+    const double* row = edep + (i - lc) + (size_t)iz * Nx;
     double acc = 0.0;
     for (int j = -h; j <= h; ++j) {
         const int x = ix + j;
@@ -921,8 +1018,10 @@ struct Ctx {
     sm2d_problem p{};
     std::vector<float> th, Ee, feA, feB, feS;
     int L = 0, layout = 0;  // 0: LayoutRef, 1: LayoutB128
+    int B = 1;
     Dev d{};
-    IterState* it_host = nullptr;  // pinned mirror
+    IterGlobal* gs_host = nullptr;  // pinned mirrors
+    LaneState* ls_host = nullptr;
     cudaStream_t s = nullptr;
     std::vector<void*> allocs;
     cudaGraph_t graph = nullptr;
@@ -932,11 +1031,13 @@ struct Ctx {
     float step_ms[7] = {};
     int grid_cell = 0, grid_transport = 0;   // warp-per-cell kernels, transport
     size_t ctab_words = 0;                   // claim-table size in 64-bit words
+    size_t ccount_n = 0;
     bool injected = false;
-    BeamArgs* beam_dev = nullptr;   // device copy of the current beam
+    BeamArgs* beams_dev = nullptr;  // device beams, one per lane
+    BeamArgs* beams_host = nullptr; // pinned staging
     int* dose_half = nullptr;       // per-row half width of the lateral kernel
     double* dose_ker = nullptr;     // per-row kernel weights
-    double* dose_dev = nullptr;     // convolved dose
+    double* dose_dev = nullptr;     // convolved dose [B][Nc]
     int dose_stride = 1;
     std::vector<cudaEvent_t> pev;   // event pool of the profiled replay
 };
@@ -947,6 +1048,13 @@ static int dalloc(Ctx& c, void** p, size_t bytes) {
     if (e != cudaSuccess) return fail(SM2D_ERR_ALLOC, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
     c.allocs.push_back(*p);
     return 0;
+}
+
+static BeamArgs beam_args(const sm2d_beam& b) {
+    return BeamArgs{b.x0, b.z0, b.theta0, b.E0, b.W_total, b.sigma_x, b.sigma_theta, b.sigma_E, b.n_samples, b.seed};
+}
+static bool host_gaussian(const sm2d_beam& b) {   // gpu_transport_wrapper.cu:246
+    return (b.n_samples > 1) || (b.sigma_x > 0.0f) || (b.sigma_theta > 0.0f);
 }
 
 template <class Lay>
@@ -976,7 +1084,7 @@ struct Impl {
         CK(rec(5));
         if (bk) k_bucket_push<Lay><<<gc, kThreads, 0, c.s>>>(c.d);
         CK(rec(6));
-        k_finalize<Lay><<<gc, kThreads, 0, c.s>>>(c.d);
+        k_finalize<<<gc, kThreads, 0, c.s>>>(c.d);
         CK(rec(7));
         CK(cudaGetLastError());
         return 0;
@@ -987,9 +1095,9 @@ struct Impl {
                             ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_BUCKET>, kThreads, 0)
                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_DIRECT>, kThreads, 0);
         if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
-        const long long items = (long long)c.d.bins_cap / 32;   // one warp per 32 bins at most
+        const long long blocks_for_cap = ((long long)c.d.bins_cap + kThreads - 1) / kThreads;
         const long long full = (long long)std::max(per_sm, 1) * std::max(sms, 1);
-        c.grid_transport = (int)std::max(1LL, std::min(full, (items + kThreads / 32 - 1) / (kThreads / 32)));
+        c.grid_transport = (int)std::max(1LL, std::min(full, blocks_for_cap));
         return 0;
     }
     static int clear_all(Ctx& c, int) {
@@ -997,19 +1105,16 @@ struct Impl {
         CK(cudaGetLastError());
         return 0;
     }
-    // injection from the device beam description: claim pass, slot
-    // selection, deposit pass
-    static int inject_dev(Ctx& c, int n, bool gaussian) {
-        const int blocks = gaussian ? (n + 255) / 256 : 1;
-        k_inject_begin<<<1, 1, 0, c.s>>>(c.d.it);
-        k_inject_keys<Lay><<<blocks, 256, 0, c.s>>>(c.d, c.beam_dev, gaussian ? 1 : 0);
+    // injection of the beams in beams_dev (one per lane, max_n samples at
+    // most): claim pass, slot selection, deposit pass, source accounting
+    static int inject(Ctx& c, int max_n, bool check_empty) {
+        const dim3 grid((unsigned)((std::max(max_n, 1) + 255) / 256), (unsigned)c.B);
+        k_inject_begin<<<1, 1, 0, c.s>>>(c.d, check_empty ? 1 : 0);
+        k_inject_keys<Lay><<<grid, 256, 0, c.s>>>(c.d, c.beams_dev, max_n, c.p.x_min, c.p.z_min);
         k_select_psi<<<c.grid_cell, kThreads, 0, c.s>>>(c.d, 0);
-        k_inject_deposit<Lay><<<blocks, 256, 0, c.s>>>(c.d, c.beam_dev, gaussian ? 1 : 0);
-        CK(cudaGetLastError());
-        return 0;
-    }
-    static int totals(Ctx& c, int which) {
-        k_totals<Lay><<<c.grid_cell, kThreads, 0, c.s>>>(c.d, which);
+        k_inject_deposit<Lay><<<grid, 256, 0, c.s>>>(c.d, c.beams_dev, max_n, c.p.x_min, c.p.z_min);
+        k_totals<Lay><<<c.grid_cell, kThreads, 0, c.s>>>(c.d, 0);
+        k_source_finalize<<<(c.B + 255) / 256, 256, 0, c.s>>>(c.d, c.beams_dev);
         CK(cudaGetLastError());
         return 0;
     }
@@ -1018,12 +1123,14 @@ struct Impl {
 #define DISPATCH(c, fn, ...) ((c).layout == 0 ? Impl<LayoutRef>::fn(c, __VA_ARGS__) : Impl<LayoutB128>::fn(c, __VA_ARGS__))
 
 static int sync_state(Ctx& c) {
-    CK(cudaMemcpyAsync(c.it_host, c.d.it, sizeof(IterState), cudaMemcpyDeviceToHost, c.s));
+    CK(cudaMemcpyAsync(c.gs_host, c.d.gs, sizeof(IterGlobal), cudaMemcpyDeviceToHost, c.s));
+    CK(cudaMemcpyAsync(c.ls_host, c.d.ls, sizeof(LaneState) * c.B, cudaMemcpyDeviceToHost, c.s));
     CK(cudaStreamSynchronize(c.s));
     return 0;
 }
 static int push_state(Ctx& c) {
-    CK(cudaMemcpyAsync(c.d.it, c.it_host, sizeof(IterState), cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.gs, c.gs_host, sizeof(IterGlobal), cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.ls, c.ls_host, sizeof(LaneState) * c.B, cudaMemcpyHostToDevice, c.s));
     return 0;
 }
 
@@ -1049,6 +1156,52 @@ static int build_graph(Ctx& c) {
     return 0;
 }
 
+// Zero the per-cell tallies and mask history of every lane and the lane
+// and iteration states (the phase space itself: clear_all).
+static int reset_lanes(Ctx& c) {
+    int rc = DISPATCH(c, clear_all, 0);
+    if (rc) return rc;
+    const size_t n = (size_t)c.B * c.d.Nc;
+    const Dev& d = c.d;
+    CK(cudaMemsetAsync(d.edep, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(d.e_cut, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(d.e_nuc, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(d.e_bnd, 0, n * 8, c.s));
+    CK(cudaMemsetAsync(d.w_cut, 0, n * 4, c.s));
+    CK(cudaMemsetAsync(d.w_nuc, 0, n * 4, c.s));
+    CK(cudaMemsetAsync(d.w_bnd, 0, n * 4, c.s));
+    CK(cudaMemsetAsync(d.cls, 0, n, c.s));
+    k_reset_state<<<1, 1, 0, c.s>>>(c.d);
+    k_wipe<<<c.grid_cell, kThreads, 0, c.s>>>(c.d, c.ctab_words, c.ccount_n);
+    CK(cudaGetLastError());
+    c.injected = false;
+    return 0;
+}
+
+static int enqueue_dose(Ctx& c) {
+    const long long n = (long long)c.B * c.d.Nc;
+    k_dose<<<(unsigned)((n + 255) / 256), 256, 0, c.s>>>(c.d.edep, c.dose_half, c.dose_ker, c.dose_stride, c.d.Nx,
+                                                         c.d.Nz, c.B, c.dose_dev);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+// Beams into the device (lane 0 = *b for a single spot; empty beams elsewhere)
+static int stage_beams(Ctx& c, const sm2d_beam* beams, int n, int* max_n) {
+    int mx = 1;
+    for (int ln = 0; ln < c.B; ++ln) {
+        if (ln < n) {
+            c.beams_host[ln] = beam_args(beams[ln]);
+            if (host_gaussian(beams[ln])) mx = std::max(mx, beams[ln].n_samples);
+        } else {
+            c.beams_host[ln] = BeamArgs{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0, 0u};
+        }
+    }
+    CK(cudaMemcpyAsync(c.beams_dev, c.beams_host, sizeof(BeamArgs) * c.B, cudaMemcpyHostToDevice, c.s));
+    *max_n = mx;
+    return 0;
+}
+
 }  // namespace sm2d
 
 using namespace sm2d;
@@ -1057,15 +1210,16 @@ struct sm2d_ctx : sm2d::Ctx {};
 
 extern "C" {
 
-
 int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     if (!p || !out) return fail(SM2D_ERR_ARG, "null argument");
     *out = nullptr;
     if (p->Nx <= 0 || p->Nz <= 0 || p->N_theta <= 0 || p->N_E <= 1 || !p->theta_edges || !p->E_edges)
         return fail(SM2D_ERR_ARG, "invalid grid");
     if (!(p->dx > 0.0f) || !(p->dz > 0.0f)) return fail(SM2D_ERR_ARG, "cell size must be positive");
-    // work items pack (cell << 5) | slot into 32 bits
-    if ((long long)p->Nx * p->Nz > (1LL << 27)) return fail(SM2D_ERR_ARG, "grid too large (at most 2^27 cells)");
+    const int B = p->lanes > 1 ? p->lanes : 1;
+    if (B > kMaxLanes) return fail(SM2D_ERR_ARG, "at most %d lanes", kMaxLanes);
+    // bin records and claim tables index cells of all lanes with 32 bits
+    if ((long long)p->Nx * p->Nz * B > (1LL << 30)) return fail(SM2D_ERR_ARG, "grid x lanes too large (at most 2^30 cells)");
     int layout;
     if (p->nt_local == 4 && p->ne_local == 2 && p->nx_sub == 8 && p->nz_sub == 4) layout = 0;
     else if (p->nt_local == 8 && p->ne_local == 4 && p->nx_sub == 4 && p->nz_sub == 1) layout = 1;
@@ -1076,6 +1230,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     sm2d_ctx* c = new sm2d_ctx();
     c->p = *p;
     c->layout = layout;
+    c->B = B;
     c->L = p->nt_local * p->ne_local * p->nx_sub * p->nz_sub;
     c->th.assign(p->theta_edges, p->theta_edges + p->N_theta + 1);
     c->Ee.assign(p->E_edges, p->E_edges + p->N_E + 1);
@@ -1093,7 +1248,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     c->feS.resize(p->Nz);
     fermi_eyges_moments(p->E0, p->Nz, p->dz, p->sigma_x_initial, c->feA.data(), c->feB.data(), c->feS.data());
     Dev& d = c->d;
-    d.Nx = p->Nx; d.Nz = p->Nz; d.Nc = p->Nx * p->Nz;
+    d.Nx = p->Nx; d.Nz = p->Nz; d.Nc = p->Nx * p->Nz; d.B = B;
     d.dx = p->dx; d.dz = p->dz;
     d.N_theta = p->N_theta; d.N_E = N;
     d.lutN = N;
@@ -1119,7 +1274,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     d.stop_frac = p->stop_weight_fraction;
     d.floor_cutoff = p->floor_cutoff;
     d.salt = p->seed_iteration_salt;
-    const size_t Nc = (size_t)d.Nc, ns = Nc * kKb;
+    const size_t Nc = (size_t)d.Nc, NcB = Nc * B, ns = NcB * kKb;
     void* q;
     int rc;
 #define A(ptr, type, n)                                              \
@@ -1134,40 +1289,39 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(fa, float, p->Nz);
     A(fb, float, p->Nz);
     d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d; d.feA = fa; d.feB = fb;
-    for (int b = 0; b < 2; ++b) {
-        A(d.bid[b], uint32_t, ns);
-        A(d.val[b], float, ns * c->L);
-        A(d.occ[b], int, Nc);
-        A(d.occ_list[b], int, Nc);
+    A(d.bid, uint32_t, ns);
+    A(d.val, float, ns * c->L);
+    for (int k = 0; k < 2; ++k) {
+        A(d.occ[k], int, NcB);
+        A(d.occ_list[k], int, NcB);
     }
-    A(d.edep, double, Nc); A(d.e_cut, double, Nc); A(d.e_nuc, double, Nc); A(d.e_bnd, double, Nc);
-    A(d.w_cut, float, Nc); A(d.w_nuc, float, Nc); A(d.w_bnd, float, Nc);
-    A(d.dl_edep, double, Nc); A(d.dl_ecut, double, Nc); A(d.dl_enuc, double, Nc); A(d.dl_ebnd, double, Nc);
-    A(d.dl_wcut, float, Nc); A(d.dl_wnuc, float, Nc); A(d.dl_wbnd, float, Nc);
-    A(d.act_gen, unsigned long long, Nc); A(d.cls, uint8_t, Nc);
-    A(d.listed, uint32_t, Nc);
-    // bin list: room for the w > 0 bins of four full slots per cell of the
-    // grid on average (a listed cell holds at most 32); a run that needs
-    // more stops with SM2D_ERR_ALLOC
-    d.bins_cap = (int)std::min<size_t>((size_t)Nc * 4 * c->L, (size_t)INT_MAX);
+    A(d.edep, double, NcB); A(d.e_cut, double, NcB); A(d.e_nuc, double, NcB); A(d.e_bnd, double, NcB);
+    A(d.w_cut, float, NcB); A(d.w_nuc, float, NcB); A(d.w_bnd, float, NcB);
+    A(d.dl_edep, double, NcB); A(d.dl_ecut, double, NcB); A(d.dl_enuc, double, NcB); A(d.dl_ebnd, double, NcB);
+    A(d.dl_wcut, float, NcB); A(d.dl_wnuc, float, NcB); A(d.dl_wbnd, float, NcB);
+    A(d.act_gen, unsigned long long, NcB); A(d.cls, uint8_t, NcB); A(d.c2b, int, NcB);
+    // cell list: every cell of a single lane; an eighth of the cells (at
+    // least 4096) per lane of a batch -- a spot lists a few percent
+    d.listed_cap = B == 1 ? (int)Nc : (int)std::min<size_t>(NcB, (size_t)B * std::max<size_t>(Nc / 8, 4096));
+    A(d.listed, uint32_t, d.listed_cap);
+    // bin list: the w > 0 bins of one full slot per cell of a single lane on
+    // average, a quarter of that per lane of a batch (a spot holds a few
+    // hundred thousand); a pass that needs more stops with SM2D_ERR_ALLOC
+    d.bins_cap = (int)std::min<size_t>((B == 1 ? Nc * c->L : NcB * c->L / 4), (size_t)INT_MAX);
     A(d.bins, uint4, d.bins_cap);
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
-    A(d.it, IterState, 1);
-    d.hist_cap = p->max_iterations > 0 ? p->max_iterations : 4096;
-    A(d.hist, sm2d_audit, d.hist_cap);
+    A(d.gs, IterGlobal, 1);
+    A(d.ls, LaneState, B);
+    d.hist_cap = B == 1 ? (p->max_iterations > 0 ? p->max_iterations : 4096) : 0;
+    A(d.hist, sm2d_audit, std::max(1, B * d.hist_cap));
     d.bucket_bytes = bucket_bytes_for(c->L);
-    if (p->use_buckets) A(d.buckets, unsigned char, (size_t)Nc * 4 * d.bucket_bytes);
-    A(d.c2b, int, Nc);
-    c->ctab_words = (size_t)5 * Nc * 2 * kCand;
+    if (p->use_buckets) A(d.buckets, unsigned char, (size_t)4 * d.listed_cap * d.bucket_bytes);
+    c->ctab_words = ((size_t)NcB + (size_t)4 * d.listed_cap) * 2 * kCand;
+    c->ccount_n = (size_t)NcB + (size_t)4 * d.listed_cap;
     A(d.ctab, unsigned long long, c->ctab_words);
-    A(d.ccount, int, 5 * Nc);
-    A(d.bkt_ids, uint32_t, (size_t)4 * Nc * kKb);
-    if (cudaMemsetAsync(d.c2b, 0xFF, Nc * sizeof(int), c->s) != cudaSuccess ||
-        cudaMemsetAsync(d.ctab, 0xFF, c->ctab_words * 8, c->s) != cudaSuccess ||
-        cudaMemsetAsync(d.ccount, 0, 5 * Nc * sizeof(int), c->s) != cudaSuccess ||
-        cudaMemsetAsync(d.bkt_ids, 0xFF, (size_t)4 * Nc * kKb * 4, c->s) != cudaSuccess)
-        return bail(fail(SM2D_ERR_CUDA, "memset"));
-    A(c->beam_dev, BeamArgs, 1);
+    A(d.ccount, int, c->ccount_n);
+    A(d.bkt_ids, uint32_t, (size_t)4 * d.listed_cap * kKb);
+    A(c->beams_dev, BeamArgs, B);
     {   // lateral post-convolution kernels per depth row
         std::vector<int> half(p->Nz, 0);
         std::vector<double> k(p->Nx + 2);
@@ -1182,15 +1336,20 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
             if (half[iz]) lateral_kernel(c->feS[iz], p->sigma_x_initial, p->dx, p->Nx, &ker[(size_t)iz * c->dose_stride]);
         A(c->dose_half, int, p->Nz);
         A(c->dose_ker, double, ker.size());
-        A(c->dose_dev, double, Nc);
+        A(c->dose_dev, double, NcB);
         if (cudaMemcpy(c->dose_half, half.data(), sizeof(int) * p->Nz, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(c->dose_ker, ker.data(), sizeof(double) * ker.size(), cudaMemcpyHostToDevice) != cudaSuccess)
             return bail(fail(SM2D_ERR_CUDA, "dose kernel upload"));
     }
 #undef A
-    if (cudaMallocHost(&c->it_host, sizeof(IterState)) != cudaSuccess) return bail(fail(SM2D_ERR_ALLOC, "pinned"));
-    memset(c->it_host, 0, sizeof(IterState));
-    c->it_host->max_iter = INT_MAX;
+    if (cudaMallocHost(&c->gs_host, sizeof(IterGlobal)) != cudaSuccess ||
+        cudaMallocHost(&c->ls_host, sizeof(LaneState) * B) != cudaSuccess ||
+        cudaMallocHost(&c->beams_host, sizeof(BeamArgs) * B) != cudaSuccess)
+        return bail(fail(SM2D_ERR_ALLOC, "pinned host state"));
+    memset(c->gs_host, 0, sizeof(IterGlobal));
+    memset(c->ls_host, 0, sizeof(LaneState) * B);
+    c->gs_host->max_pass = INT_MAX;
+    for (int ln = 0; ln < B; ++ln) c->ls_host[ln].done = 1;
     cudaStream_t s = c->s;
     bool ok = cudaMemcpyAsync(th_d, c->th.data(), sizeof(float) * (p->N_theta + 1), cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(Ee_d, c->Ee.data(), sizeof(float) * (N + 1), cudaMemcpyHostToDevice, s) == cudaSuccess &&
@@ -1199,31 +1358,27 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
               cudaMemcpyAsync(lR_d, lR.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(fa, c->feA.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(fb, c->feB.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess;
-    for (int b = 0; b < 2 && ok; ++b)
-        ok = cudaMemsetAsync(d.bid[b], 0xFF, ns * 4, s) == cudaSuccess &&
-             cudaMemsetAsync(d.val[b], 0, ns * c->L * 4, s) == cudaSuccess &&
-             cudaMemsetAsync(d.occ[b], 0, Nc * 4, s) == cudaSuccess;
-    ok = ok && cudaMemsetAsync(d.edep, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_cut, 0, Nc * 8, s) == cudaSuccess &&
-         cudaMemsetAsync(d.e_nuc, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_bnd, 0, Nc * 8, s) == cudaSuccess &&
-         cudaMemsetAsync(d.w_cut, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.w_nuc, 0, Nc * 4, s) == cudaSuccess &&
-         cudaMemsetAsync(d.w_bnd, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.act_gen, 0, Nc * 8, s) == cudaSuccess &&
-         cudaMemsetAsync(d.cls, 0, Nc, s) == cudaSuccess && cudaMemsetAsync(d.dl_edep, 0, Nc * 8, s) == cudaSuccess &&
-         cudaMemsetAsync(d.dl_ecut, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.dl_enuc, 0, Nc * 8, s) == cudaSuccess &&
-         cudaMemsetAsync(d.dl_ebnd, 0, Nc * 8, s) == cudaSuccess && cudaMemsetAsync(d.dl_wcut, 0, Nc * 4, s) == cudaSuccess &&
-         cudaMemsetAsync(d.dl_wnuc, 0, Nc * 4, s) == cudaSuccess && cudaMemsetAsync(d.dl_wbnd, 0, Nc * 4, s) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(d.bid, 0xFF, ns * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.val, 0, ns * c->L * 4, s) == cudaSuccess;
+    for (int k = 0; k < 2 && ok; ++k) ok = cudaMemsetAsync(d.occ[k], 0, NcB * 4, s) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(d.edep, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_cut, 0, NcB * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.e_nuc, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_bnd, 0, NcB * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.w_cut, 0, NcB * 4, s) == cudaSuccess && cudaMemsetAsync(d.w_nuc, 0, NcB * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.w_bnd, 0, NcB * 4, s) == cudaSuccess && cudaMemsetAsync(d.act_gen, 0, NcB * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.cls, 0, NcB, s) == cudaSuccess && cudaMemsetAsync(d.c2b, 0xFF, NcB * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.dl_edep, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.dl_ecut, 0, NcB * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.dl_enuc, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.dl_ebnd, 0, NcB * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.dl_wcut, 0, NcB * 4, s) == cudaSuccess && cudaMemsetAsync(d.dl_wnuc, 0, NcB * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.dl_wbnd, 0, NcB * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.ctab, 0xFF, c->ctab_words * 8, s) == cudaSuccess &&
+         cudaMemsetAsync(d.ccount, 0, c->ccount_n * sizeof(int), s) == cudaSuccess &&
+         cudaMemsetAsync(d.bkt_ids, 0xFF, (size_t)4 * d.listed_cap * kKb * 4, s) == cudaSuccess;
     if (!ok) return bail(fail(SM2D_ERR_CUDA, "initial copies failed"));
-    {   // grid origin of the beam description is fixed per problem
-        BeamArgs origin{};
-        origin.x_min = p->x_min;
-        origin.z_min = p->z_min;
-        if (cudaMemcpyAsync(c->beam_dev, &origin, sizeof origin, cudaMemcpyHostToDevice, s) != cudaSuccess)
-            return bail(fail(SM2D_ERR_CUDA, "beam origin upload"));
-    }
     if (push_state(*c)) return bail(SM2D_ERR_CUDA);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    c->grid_cell = std::max(1, std::min((int)((Nc + kThreads / 32 - 1) / (kThreads / 32)), 4 * std::max(sms, 1)));
+    c->grid_cell = std::max(1, std::min((int)((NcB + kThreads / 32 - 1) / (kThreads / 32)), 4 * std::max(sms, 1)));
     if ((rc = DISPATCH(*c, transport_grid, sms))) return bail(rc);
     if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "create sync"));
     *out = c;
@@ -1239,20 +1394,36 @@ int sm2d_destroy(sm2d_handle h) {
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : h->pev) cudaEventDestroy(e);
-    if (h->it_host) cudaFreeHost(h->it_host);
+    if (h->gs_host) cudaFreeHost(h->gs_host);
+    if (h->ls_host) cudaFreeHost(h->ls_host);
+    if (h->beams_host) cudaFreeHost(h->beams_host);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
     return 0;
 }
 
 int sm2d_local_bins(sm2d_handle h) { return h ? h->L : SM2D_ERR_ARG; }
+int sm2d_lanes(sm2d_handle h) { return h ? h->B : SM2D_ERR_ARG; }
+
+// ---------------------------------------------------------------- single spot (lane 0)
+int sm2d_inject_async(sm2d_handle h, const sm2d_beam* b) {
+    if (!h || !b) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    if (host_gaussian(*b) && b->n_samples <= 0) return fail(SM2D_ERR_ARG, "n_samples must be positive");
+    int max_n = 1;
+    int rc = stage_beams(c, b, 1, &max_n);
+    if (rc) return rc;
+    if ((rc = DISPATCH(c, inject, max_n, true))) return rc;
+    c.injected = true;
+    return 0;
+}
 
 int sm2d_inject(sm2d_handle h, const sm2d_beam* b) {
     if (!h || !b) return fail(SM2D_ERR_ARG, "null argument");
     Ctx& c = *h;
     int rc = sync_state(c);
     if (rc) return rc;
-    if (c.it_host->occ_n[c.it_host->parity] != 0)
+    if (c.gs_host->occ_n[c.gs_host->parity] != 0)
         return fail(SM2D_ERR_STATE, "phase space not empty: call sm2d_reset before injecting");
     if ((rc = sm2d_inject_async(h, b))) return rc;
     CK(cudaStreamSynchronize(c.s));
@@ -1262,9 +1433,12 @@ int sm2d_inject(sm2d_handle h, const sm2d_beam* b) {
 int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
     if (!h || !bid || !val) return fail(SM2D_ERR_ARG, "null argument");
     Ctx& c = *h;
+    if (c.B != 1) return fail(SM2D_ERR_STATE, "sm2d_set_psi_in needs a single-lane engine");
     int rc = sync_state(c);
     if (rc) return rc;
-    const int par = c.it_host->parity;
+    if ((rc = DISPATCH(c, clear_all, 0))) return rc;   // drop what the lists hold
+    CK(cudaStreamSynchronize(c.s));
+    const int par = c.gs_host->parity;
     const size_t ns = (size_t)c.d.Nc * kKb;
     std::vector<int> occ(c.d.Nc, 0), list;
     for (int cell = 0; cell < c.d.Nc; ++cell)
@@ -1274,13 +1448,14 @@ int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
                 list.push_back(cell);
                 break;
             }
-    CK(cudaMemcpyAsync(c.d.bid[par], bid, ns * 4, cudaMemcpyHostToDevice, c.s));
-    CK(cudaMemcpyAsync(c.d.val[par], val, ns * c.L * 4, cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.bid, bid, ns * 4, cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.val, val, ns * c.L * 4, cudaMemcpyHostToDevice, c.s));
     CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, c.s));
     if (!list.empty())
         CK(cudaMemcpyAsync(c.d.occ_list[par], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, c.s));
-    c.it_host->occ_n[par] = (int)list.size();
-    c.it_host->done = 0;
+    c.gs_host->occ_n[par] = (int)list.size();
+    c.gs_host->occ_n[par ^ 1] = 0;
+    c.ls_host[0].done = 0;
     if ((rc = push_state(c))) return rc;
     CK(cudaStreamSynchronize(c.s));
     c.injected = true;
@@ -1290,12 +1465,9 @@ int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
 int sm2d_get_psi_in(sm2d_handle h, uint32_t* bid, float* val) {
     if (!h || !bid) return fail(SM2D_ERR_ARG, "null argument");
     Ctx& c = *h;
-    int rc = sync_state(c);
-    if (rc) return rc;
-    const int par = c.it_host->parity;
     const size_t ns = (size_t)c.d.Nc * kKb;
-    CK(cudaMemcpyAsync(bid, c.d.bid[par], ns * 4, cudaMemcpyDeviceToHost, c.s));
-    if (val) CK(cudaMemcpyAsync(val, c.d.val[par], ns * c.L * 4, cudaMemcpyDeviceToHost, c.s));
+    CK(cudaMemcpyAsync(bid, c.d.bid, ns * 4, cudaMemcpyDeviceToHost, c.s));
+    if (val) CK(cudaMemcpyAsync(val, c.d.val, ns * c.L * 4, cudaMemcpyDeviceToHost, c.s));
     CK(cudaStreamSynchronize(c.s));
     return 0;
 }
@@ -1307,11 +1479,11 @@ int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse) {
     int rc = DISPATCH(c, launch_body, true, false, true);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
-    if (c.it_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "bin list capacity (%d bins) exceeded", c.d.bins_cap);
+    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
     // classify, lists, claim pass, selection, deposit pass, K4 bucket move, finalize
     for (int k = 0; k < 7; ++k) CK(cudaEventElapsedTime(&c.step_ms[k], c.ev[k], c.ev[k + 1]));
-    if (n_active) *n_active = c.it_host->done ? 0 : c.it_host->n_active;
-    if (n_coarse) *n_coarse = c.it_host->done ? 0 : c.it_host->n_coarse;
+    if (n_active) *n_active = c.ls_host[0].done ? 0 : c.ls_host[0].n_active;
+    if (n_coarse) *n_coarse = c.ls_host[0].done ? 0 : c.ls_host[0].n_coarse;
     return 0;
 }
 
@@ -1321,8 +1493,8 @@ static int run_impl(Ctx& c, int max_it, int* done_iters, float* ms) {
     int rc = build_graph(c);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
-    const int start = c.it_host->iter;
-    c.it_host->max_iter = start + max_it;
+    const int start = c.ls_host[0].iter;
+    c.gs_host->max_pass = (int)std::min<long long>((long long)c.gs_host->pass + max_it, INT_MAX);
     if ((rc = push_state(c))) return rc;
     if (ms) CK(cudaEventRecord(c.ev[8], c.s));
     CK(cudaGraphLaunch(c.exec, c.s));
@@ -1330,11 +1502,11 @@ static int run_impl(Ctx& c, int max_it, int* done_iters, float* ms) {
     CK(cudaStreamSynchronize(c.s));
     if (ms) CK(cudaEventElapsedTime(ms, c.ev[8], c.ev[9]));
     if ((rc = sync_state(c))) return rc;
-    c.it_host->max_iter = INT_MAX;
+    c.gs_host->max_pass = INT_MAX;
     if ((rc = push_state(c))) return rc;
     CK(cudaStreamSynchronize(c.s));
-    if (done_iters) *done_iters = c.it_host->iter - start;
-    if (c.it_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "bin list capacity (%d bins) exceeded", c.d.bins_cap);
+    if (done_iters) *done_iters = c.ls_host[0].iter - start;
+    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
     return 0;
 }
 
@@ -1355,7 +1527,7 @@ int sm2d_get_mask(sm2d_handle h, uint8_t* mask) {
     std::vector<unsigned long long> g(h->d.Nc);
     CK(cudaMemcpyAsync(g.data(), h->d.act_gen, sizeof(unsigned long long) * g.size(), cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
-    const unsigned long long cur = h->it_host->gen;
+    const unsigned long long cur = h->gs_host->gen;
     for (int i = 0; i < h->d.Nc; ++i) mask[i] = (cur != 0 && g[i] == cur) ? 1 : 0;
     return 0;
 }
@@ -1364,8 +1536,9 @@ int sm2d_get_lists(sm2d_handle h, uint32_t* active, int* na, uint32_t* coarse, i
     if (!h || !na || !nc) return fail(SM2D_ERR_ARG, "null argument");
     int rc = sync_state(*h);
     if (rc) return rc;
-    *na = h->it_host->done ? 0 : h->it_host->n_active;
-    *nc = h->it_host->done ? 0 : h->it_host->n_coarse;
+    const LaneState& L = h->ls_host[0];
+    *na = L.done ? 0 : L.n_active;
+    *nc = L.done ? 0 : L.n_coarse;
     if (active && *na) CK(cudaMemcpyAsync(active, h->d.active, sizeof(uint32_t) * *na, cudaMemcpyDeviceToHost, h->s));
     if (coarse && *nc) CK(cudaMemcpyAsync(coarse, h->d.coarse, sizeof(uint32_t) * *nc, cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
@@ -1392,7 +1565,7 @@ int sm2d_get_audit(sm2d_handle h, sm2d_audit* out) {
     if (!h || !out) return fail(SM2D_ERR_ARG, "null argument");
     int rc = sync_state(*h);
     if (rc) return rc;
-    *out = h->it_host->last;
+    *out = h->ls_host[0].last;
     return 0;
 }
 
@@ -1400,7 +1573,7 @@ int sm2d_get_audit_history(sm2d_handle h, sm2d_audit* out, int max_entries, int*
     if (!h || !out || !n) return fail(SM2D_ERR_ARG, "null argument");
     int rc = sync_state(*h);
     if (rc) return rc;
-    *n = std::min(std::min(h->it_host->iter, h->d.hist_cap), max_entries);
+    *n = std::min(std::min(h->ls_host[0].iter, h->d.hist_cap), max_entries);
     if (*n > 0) CK(cudaMemcpyAsync(out, h->d.hist, sizeof(sm2d_audit) * *n, cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
     return 0;
@@ -1410,12 +1583,13 @@ int sm2d_get_scalars(sm2d_handle h, double* o) {
     if (!h || !o) return fail(SM2D_ERR_ARG, "null argument");
     int rc = sync_state(*h);
     if (rc) return rc;
-    const IterState& it = *h->it_host;
-    o[0] = it.transport_drop_w; o[1] = it.transport_drop_e; o[2] = it.audit_residual;
-    o[3] = it.src_inj_w; o[4] = it.src_inj_e; o[5] = it.src_oog_w; o[6] = it.src_oog_e;
-    o[7] = it.src_slot_w; o[8] = it.src_slot_e; o[9] = it.src_rep_loss;
-    o[10] = it.iter; o[11] = it.cell_steps; o[12] = it.slots_in; o[13] = it.slots_out;
-    o[14] = it.cand_ovf; o[15] = it.cand_miss; o[16] = it.bin_ovf;
+    const LaneState& L = h->ls_host[0];
+    const IterGlobal& G = *h->gs_host;
+    o[0] = L.transport_drop_w; o[1] = L.transport_drop_e; o[2] = L.audit_residual;
+    o[3] = L.src_inj_w; o[4] = L.src_inj_e; o[5] = L.src_oog_w; o[6] = L.src_oog_e;
+    o[7] = L.src_slot_w; o[8] = L.src_slot_e; o[9] = L.src_rep_loss;
+    o[10] = L.iter; o[11] = L.cell_steps; o[12] = L.slots_in; o[13] = L.slots_out;
+    o[14] = G.cand_ovf; o[15] = G.cand_miss; o[16] = G.bin_ovf;
     return 0;
 }
 
@@ -1425,14 +1599,6 @@ int sm2d_get_fe(sm2d_handle h, float* A, float* B, float* S) {
     if (A) memcpy(A, h->feA.data(), n * 4);
     if (B) memcpy(B, h->feB.data(), n * 4);
     if (S) memcpy(S, h->feS.data(), n * 4);
-    return 0;
-}
-
-static int enqueue_dose(Ctx& c) {
-    const int n = c.d.Nc;
-    k_dose<<<(n + 255) / 256, 256, 0, c.s>>>(c.d.edep, c.dose_half, c.dose_ker, c.dose_stride, c.d.Nx, c.d.Nz,
-                                             c.dose_dev);
-    CK(cudaGetLastError());
     return 0;
 }
 
@@ -1449,43 +1615,7 @@ void* sm2d_stream(sm2d_handle h) { return h ? (void*)h->s : nullptr; }
 
 int sm2d_reset(sm2d_handle h) {
     if (!h) return fail(SM2D_ERR_ARG, "null handle");
-    Ctx& c = *h;
-    int rc = DISPATCH(c, clear_all, 0);
-    if (rc) return rc;
-    const size_t n = (size_t)c.d.Nc;
-    CK(cudaMemsetAsync(c.d.edep, 0, n * 8, c.s));
-    CK(cudaMemsetAsync(c.d.e_cut, 0, n * 8, c.s));
-    CK(cudaMemsetAsync(c.d.e_nuc, 0, n * 8, c.s));
-    CK(cudaMemsetAsync(c.d.e_bnd, 0, n * 8, c.s));
-    CK(cudaMemsetAsync(c.d.w_cut, 0, n * 4, c.s));
-    CK(cudaMemsetAsync(c.d.w_nuc, 0, n * 4, c.s));
-    CK(cudaMemsetAsync(c.d.w_bnd, 0, n * 4, c.s));
-    CK(cudaMemsetAsync(c.d.cls, 0, n, c.s));
-    k_reset_state<<<1, 1, 0, c.s>>>(c.d.it);
-    k_wipe<<<c.grid_cell, kThreads, 0, c.s>>>(c.d, c.ctab_words, 5 * c.d.Nc);
-    CK(cudaGetLastError());
-    c.injected = false;
-    return 0;
-}
-
-int sm2d_inject_async(sm2d_handle h, const sm2d_beam* b) {
-    if (!h || !b) return fail(SM2D_ERR_ARG, "null argument");
-    Ctx& c = *h;
-    const bool gaussian = (b->n_samples > 1) || (b->sigma_x > 0.0f) || (b->sigma_theta > 0.0f);
-    if (gaussian && b->n_samples <= 0) return fail(SM2D_ERR_ARG, "n_samples must be positive");
-    // the beam travels as-is (host struct -> device); x_min/z_min come from the problem
-    static_assert(sizeof(sm2d_beam) == 10 * 4, "beam layout");
-    CK(cudaMemcpyAsync(c.beam_dev, b, 8 * sizeof(float), cudaMemcpyHostToDevice, c.s));
-    CK(cudaMemcpyAsync(reinterpret_cast<char*>(c.beam_dev) + offsetof(BeamArgs, n), &b->n_samples,
-                       sizeof(int) + sizeof(unsigned), cudaMemcpyHostToDevice, c.s));
-    CK(cudaMemsetAsync(&c.d.it->src_inj_w, 0, offsetof(IterState, last) - offsetof(IterState, src_inj_w), c.s));
-    int rc = DISPATCH(c, inject_dev, b->n_samples, gaussian);
-    if (rc) return rc;
-    if ((rc = DISPATCH(c, totals, 0))) return rc;
-    k_source_finalize<<<1, 1, 0, c.s>>>(c.d.it, c.beam_dev, gaussian ? 1 : 0);
-    CK(cudaGetLastError());
-    c.injected = true;
-    return 0;
+    return reset_lanes(*h);
 }
 
 int sm2d_run_async(sm2d_handle h, int max_it) {
@@ -1495,7 +1625,7 @@ int sm2d_run_async(sm2d_handle h, int max_it) {
     if (max_it <= 0) return fail(SM2D_ERR_ARG, "max_iterations must be positive");
     int rc = build_graph(c);
     if (rc) return rc;
-    k_set_iter_limit<<<1, 1, 0, c.s>>>(c.d.it, max_it);
+    k_set_pass_limit<<<1, 1, 0, c.s>>>(c.d.gs, max_it);
     CK(cudaGetLastError());
     CK(cudaGraphLaunch(c.exec, c.s));
     return 0;
@@ -1515,7 +1645,7 @@ int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* la
     if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space");
     int rc = sync_state(c);
     if (rc) return rc;
-    const int start = c.it_host->iter;
+    const int start = c.ls_host[0].iter;
     constexpr int E = 8;   // events per iteration
     const size_t need = (size_t)E * n;
     while (c.pev.size() < need) {
@@ -1532,7 +1662,7 @@ int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* la
     memcpy(c.ev, saved, sizeof saved);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
-    const int done = c.it_host->iter - start;
+    const int done = c.ls_host[0].iter - start;
     for (int k = 0; k < E - 1; ++k) ms7[k] = 0.0f;
     for (int i = 0; i < done; ++i)
         for (int k = 0; k < E - 1; ++k) {
@@ -1548,6 +1678,94 @@ int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* la
 int sm2d_get_step_timing(sm2d_handle h, float* ms7) {
     if (!h || !ms7) return fail(SM2D_ERR_ARG, "null argument");
     memcpy(ms7, h->step_ms, sizeof h->step_ms);
+    return 0;
+}
+
+// ---------------------------------------------------------------- batched spots
+static void fill_result(const LaneState& L, sm2d_spot_result& r) {
+    r.iterations = L.iter;
+    r.finished = L.done;
+    r.weight_audit_failures = L.w_fail;
+    r.energy_audit_failures = L.e_fail;
+    r.injected_weight = L.src_inj_w;
+    r.injected_energy = L.src_inj_e;
+    r.source_out_of_grid_weight = L.src_oog_w;
+    r.source_slot_dropped_weight = L.src_slot_w;
+    r.transport_dropped_weight = L.transport_drop_w;
+    r.transport_dropped_energy = L.transport_drop_e;
+    r.audit_residual_energy = L.audit_residual;
+    r.representation_loss_energy = L.src_rep_loss;
+    r.cell_steps = L.cell_steps;
+    r.slots_in = L.slots_in;
+    r.slots_out = L.slots_out;
+    r.last = L.last;
+}
+
+static int check_beams(const sm2d_beam* beams, int n) {
+    for (int i = 0; i < n; ++i)
+        if (host_gaussian(beams[i]) && beams[i].n_samples <= 0)
+            return fail(SM2D_ERR_ARG, "spot %d: n_samples must be positive", i);
+    return 0;
+}
+
+int sm2d_batch_inject(sm2d_handle h, const sm2d_beam* beams, int n) {
+    if (!h || (!beams && n > 0) || n < 0) return fail(SM2D_ERR_ARG, "invalid argument");
+    Ctx& c = *h;
+    if (n > c.B) return fail(SM2D_ERR_ARG, "%d beams for %d lanes", n, c.B);
+    int rc = check_beams(beams, n);
+    if (rc) return rc;
+    if ((rc = reset_lanes(c))) return rc;
+    int max_n = 1;
+    if ((rc = stage_beams(c, beams, n, &max_n))) return rc;
+    if ((rc = DISPATCH(c, inject, max_n, false))) return rc;
+    c.injected = true;
+    return 0;
+}
+
+int sm2d_batch_results(sm2d_handle h, sm2d_spot_result* results, int n) {
+    if (!h || !results || n < 0 || n > h->B) return fail(SM2D_ERR_ARG, "invalid argument");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) fill_result(h->ls_host[i], results[i]);
+    return 0;
+}
+
+int sm2d_batch_dose(sm2d_handle h, double* dose, int n) {
+    if (!h || !dose || n < 0 || n > h->B) return fail(SM2D_ERR_ARG, "invalid argument");
+    int rc = enqueue_dose(*h);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dose, h->dose_dev, sizeof(double) * h->d.Nc * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, double* dose,
+                   sm2d_spot_result* results) {
+    if (!h || (!beams && n_spots > 0) || n_spots < 0 || max_iterations <= 0) return fail(SM2D_ERR_ARG, "invalid argument");
+    Ctx& c = *h;
+    int rc = check_beams(beams, n_spots);
+    if (rc) return rc;
+    if ((rc = build_graph(c))) return rc;
+    const size_t nc = (size_t)c.d.Nc;
+    for (int w0 = 0; w0 < n_spots; w0 += c.B) {
+        const int nw = std::min(c.B, n_spots - w0);
+        if ((rc = sm2d_batch_inject(h, beams + w0, nw))) return rc;
+        k_set_pass_limit<<<1, 1, 0, c.s>>>(c.d.gs, max_iterations);
+        CK(cudaGetLastError());
+        CK(cudaGraphLaunch(c.exec, c.s));
+        if (dose) {
+            if ((rc = enqueue_dose(c))) return rc;
+            CK(cudaMemcpyAsync(dose + (size_t)w0 * nc, c.dose_dev, sizeof(double) * nc * nw, cudaMemcpyDeviceToHost,
+                               c.s));
+        }
+        if (results) {
+            if ((rc = sync_state(c))) return rc;
+            for (int i = 0; i < nw; ++i) fill_result(c.ls_host[i], results[w0 + i]);
+            if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
+        }
+    }
+    if ((rc = sync_state(c))) return rc;
+    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
     return 0;
 }
 

@@ -84,7 +84,7 @@ __device__ __forceinline__ unsigned long long* psi_row(const Dev& d, int cell) {
     return d.ctab + (size_t)cell * (2 * kCand);
 }
 __device__ __forceinline__ unsigned long long* bucket_row(const Dev& d, int bf) {
-    return d.ctab + (size_t)(d.Nc + bf) * (2 * kCand);
+    return d.ctab + ((size_t)d.B * d.Nc + bf) * (2 * kCand);
 }
 // claim keys: psi_out rows [batch:1][part:3][slot:5][lidx:8][part index:1]
 // (part 0 in-cell deposit, 1 + f the K4 transfer of face f by bucket slot);
@@ -110,7 +110,7 @@ __device__ __forceinline__ int resolve(const Dev& d, const unsigned long long* r
                                        uint32_t want, uint32_t& sel) {
     int s = cand_find(row, tag, want);
     if (s < 0) {
-        atomicAdd(&d.it->cand_miss, 1);
+        atomicAdd(&d.gs->cand_miss, 1);
         int bd = 0x7fffffff;
         for (int k = 0; k < kKb; ++k) {
             const uint32_t x = kept[k];
@@ -135,8 +135,9 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
     if (base < 0) return w;
     const int bf = base + face;
     if (PASS == PASS_KEYS) {
-        cand_insert(bucket_row(d, bf), d.ccount + d.Nc + bf, src.tag, want, bucket_key(col, src.slot, src.lidx, seq),
-                    &d.it->cand_ovf);
+        cand_insert(bucket_row(d, bf), d.ccount + (size_t)d.B * d.Nc + bf, src.tag, want,
+                    bucket_key(col, src.slot, src.lidx, seq),
+                    &d.gs->cand_ovf);
         return 0.0f;
     }
     uint32_t selb;
@@ -151,15 +152,14 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
         return 0.0f;
     }
     // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
-    const int out = par ^ 1;
     uint32_t seld;
-    const int os = resolve(d, psi_row(d, dcell), d.bid[out] + (size_t)dcell * kKb, src.tag, selb, seld);
+    const int os = resolve(d, psi_row(d, dcell), d.bid + (size_t)dcell * kKb, src.tag, selb, seld);
     if (os < 0) return w;
     const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
     const int e2 = ebin_of<Lay>(d, seld, le2);
     if (seld != selb && d.esplit)
         atomicAdd(d.dl_edep + bcell, (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, e2)) * w));
-    atomicAdd(d.val[out] + ((size_t)dcell * kKb + os) * Lay::L + le2, w);
+    atomicAdd(d.val + ((size_t)dcell * kKb + os) * Lay::L + le2, w);
     t.Wout += (double)w;
     t.Eout += (double)w * (double)e_center(d, e2);
     return 0.0f;
@@ -245,7 +245,7 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
     } else {
         for (int i = 0; i < N; ++i) w[i] /= s;
     }
-    const int ixs = src % d.Nx, izs = src / d.Nx, tz = izs + 1;
+    const int ixs = src % d.Nx, izs = (src / d.Nx) % d.Nz, tz = izs + 1;
     float dropped = 0.0f;
     for (int i = 0; i < N; ++i) {
         const float wf = w[i];
@@ -253,7 +253,7 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
         const int off = i - N / 2;
         const int ixt = ixs + off;
         if (ixt < 0 || ixt >= d.Nx || tz >= d.Nz) { boundary_w += weight * wf; continue; }
-        const int ecell = ixt + izs * d.Nx;
+        const int ecell = src + off;   // same row of the same lane
         // the bucket of another column exists only if that cell is listed
         // in the same pass (k1k6_pipeline.cu:800-847 maps one list at a time)
         if (ecell != src && d.cls[ecell] != my_cls) { dropped += weight * wf; continue; }
@@ -289,7 +289,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             const int Eb = ep.bin[ei];
             const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
             cand_insert(psi_row(d, cell), d.ccount + cell, sc.tag, want, stay_key(sc.k3, sc.slot, sc.lidx, ei),
-                        &d.it->cand_ovf);
+                        &d.gs->cand_ovf);
         }
         mark_occupied(d, outp, cell);
     } else {
@@ -325,8 +325,8 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             w[Lay::NX / 2] = 1.0f;
             wsum = 1.0f;
         }
-        const uint32_t* kept = d.bid[outp] + (size_t)cell * kKb;
-        float* vals = d.val[outp] + (size_t)cell * kKb * Lay::L;
+        const uint32_t* kept = d.bid + (size_t)cell * kKb;
+        float* vals = d.val + (size_t)cell * kKb * Lay::L;
         for (int ei = 0; ei < ep.n; ++ei) {
             const int Eb = ep.bin[ei];
             const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
@@ -409,7 +409,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
 template <class Lay, int PASS>
 __device__ void emit_cross(const Dev& d, const Src& sc, int par, bool k3, int cell, int my_cls, int face,
                            float theta_new, float E_new, float w_new, float x_new, float z_new, float sig_tr, Tally& t) {
-    const int ix = cell % d.Nx, iz = cell / d.Nx;
+    const int ix = cell % d.Nx, iz = (cell / d.Nx) % d.Nz;
     int nb = -1;
     if (face == FACE_ZP) nb = iz + 1 < d.Nz ? cell + d.Nx : -1;
     else if (face == FACE_ZM) nb = iz > 0 ? cell - d.Nx : -1;
@@ -455,11 +455,12 @@ __device__ __forceinline__ int exit_face(float x, float z, float dx, float dz) {
     return -1;
 }
 
-// One component of a listed cell: local bin lidx of psi_in slot `slot`
-// (sslot: the slot number the random seeds use).
+// One component of a listed cell gc (lane-local index lc, which the random
+// seeds use): local bin lidx of psi_in slot `slot` (sslot: the slot number
+// the seeds use).  par selects the occupancy list of psi_out (par ^ 1).
 template <class Lay, int PASS>
-__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t bid, int slot, int sslot, int lidx,
-                              float w, unsigned salt, uint32_t tag, Tally& t) {
+__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int lc, uint32_t bid, int slot, int sslot,
+                              int lidx, float w, unsigned salt, uint32_t tag, Tally& t) {
     const float dx = d.dx, dz = d.dz;
     int tl, El, xs, zs;
     Lay::dec(lidx, tl, El, xs, zs);
@@ -487,7 +488,7 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
     }
     const float xc = sub_offset(xs, Lay::NX, dx), zc = sub_offset(zs, Lay::NZ, dz);
     const float hx = dx * 0.5f, hz = dz * 0.5f;
-    const int iz = cell / d.Nx;
+    const int iz = lc / d.Nx;
     float step, dE, w_new, w_rem = 0.0f, E_rem = 0.0f, sig_th, sig_x, E_new, edep;
     unsigned ts;
     if (k3) {
@@ -501,7 +502,7 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
         step = fminf(fine_step_limit(d, E), sb * 1.001f);
         const float mean_dE = lut_energy_loss(d, E, step);
         if (d.straggle) {
-            unsigned seed = ((unsigned)(cell * 7 + sslot * 13 + lidx * 17) ^ 0xDEECE66Du) ^ salt;
+            unsigned seed = ((unsigned)(lc * 7 + sslot * 13 + lidx * 17) ^ 0xDEECE66Du) ^ salt;
             const float sE = straggling_sigma(E, step, 1.0f);
             dE = sE <= 0.0f ? mean_dE : fmaxf(mean_dE + normal_draw(seed) * sE, 0.0f);
         } else {
@@ -525,7 +526,7 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
         const float dC = fmaxf(2.0f * Bp * sm + Ap * sm * sm + T * sm * sm * sm / 3.0f, 0.0f);
         sig_x = fmaxf(sqrtf(dC), 0.01f);
         const unsigned ps = (unsigned)fminf((float)iz * dz * 1000.0f, 4294967295.0f);
-        ts = ((unsigned)(cell + 1) * 2654435761u) ^ ((unsigned)(sslot + 1) * 2246822519u) ^
+        ts = ((unsigned)(lc + 1) * 2654435761u) ^ ((unsigned)(sslot + 1) * 2246822519u) ^
              ((unsigned)(lidx + 1) * 3266489917u) ^ (unsigned)(Ebin + 17) ^ (ps * 747796405u) ^ salt;
     } else {
         // K2_CoarseTransport body, k2_coarsetransport.cu:186-350
@@ -563,7 +564,7 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, uint32_t
         const float uf = fminf(0.35f, 0.04f + 0.003f * p0);
         sig_x = fmaxf(sqrtf(fmaxf(dC + uf * C0, 0.0f)), 0.01f);
         const unsigned ps = (unsigned)fminf(p0 * 1000.0f, 4294967295.0f);
-        ts = ((unsigned)(cell + 1) * 2654435761u) ^ ((unsigned)(sslot + 1) * 2246822519u) ^
+        ts = ((unsigned)(lc + 1) * 2654435761u) ^ ((unsigned)(sslot + 1) * 2246822519u) ^
              ((unsigned)(lidx + 1) * 3266489917u) ^ (unsigned)(Ebin + 17) ^ (ps * 747796405u) ^ salt;
     }
     const float scat = sig_th <= 0.0f ? 0.0f : normal_draw(ts) * sig_th;

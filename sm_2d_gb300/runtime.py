@@ -44,6 +44,7 @@ class Problem(C.Structure):
         ("max_iterations", C.c_int),
         ("prune_coarse", C.c_float), ("prune_fine", C.c_float), ("split_min_weight", C.c_float),
         ("stop_weight_fraction", C.c_float), ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
+        ("lanes", C.c_int),
     ]
 
 
@@ -69,6 +70,23 @@ class Audit(C.Structure):
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class SpotResult(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int), ("finished", C.c_int), ("weight_audit_failures", C.c_int),
+        ("energy_audit_failures", C.c_int),
+        ("injected_weight", C.c_double), ("injected_energy", C.c_double),
+        ("source_out_of_grid_weight", C.c_double), ("source_slot_dropped_weight", C.c_double),
+        ("transport_dropped_weight", C.c_double), ("transport_dropped_energy", C.c_double),
+        ("audit_residual_energy", C.c_double), ("representation_loss_energy", C.c_double),
+        ("cell_steps", C.c_double), ("slots_in", C.c_double), ("slots_out", C.c_double), ("last", Audit),
+    ]
+
+    def as_dict(self):
+        out = {n: getattr(self, n) for n, _ in self._fields_ if n != "last"}
+        out["last"] = self.last.as_dict()
+        return out
 
 
 SCALAR_KEYS = ["transport_dropped_weight", "transport_dropped_energy", "audit_residual_energy",
@@ -132,6 +150,11 @@ def lib(build_if_needed: bool = True):
         L.sm2d_k5_conservation_audit.argtypes = ([P] * 18 + [F, F, D, D, F, D, I, P, I, I, I, I, P, I, P])
         L.sm2d_k5_conservation_audit_static.argtypes = L.sm2d_k5_conservation_audit.argtypes
         L.sm2d_math_eval.argtypes = [I, P, P, I]
+        L.sm2d_lanes.argtypes = [P]
+        L.sm2d_batch_run.argtypes = [P, P, I, I, P, P]
+        L.sm2d_batch_inject.argtypes = [P, P, I]
+        L.sm2d_batch_results.argtypes = [P, P, I]
+        L.sm2d_batch_dose.argtypes = [P, P, I]
         _LIB = L
         return L
 
@@ -221,6 +244,7 @@ class Config:
     stop_weight_fraction: float = 0.0
     floor_cutoff: int = 0
     seed_iteration_salt: int = 0
+    lanes: int = 1          # spots transported together by Transport.batch_run
 
     def production(self):
         """Options of a production run: deterministic rank-ordered seeds salted
@@ -284,13 +308,15 @@ class Transport:
                     use_buckets=cfg.use_buckets, max_iterations=cfg.max_iterations,
                     prune_coarse=cfg.prune_coarse, prune_fine=cfg.prune_fine,
                     split_min_weight=cfg.split_min_weight, stop_weight_fraction=cfg.stop_weight_fraction,
-                    floor_cutoff=cfg.floor_cutoff, seed_iteration_salt=cfg.seed_iteration_salt, **cfg.layout)
+                    floor_cutoff=cfg.floor_cutoff, seed_iteration_salt=cfg.seed_iteration_salt, lanes=cfg.lanes,
+                    **cfg.layout)
         h = C.c_void_p()
         self._lib = lib()
         check(self._lib.sm2d_create(C.byref(p), C.byref(h)))
         self.h = h
         self.Nc = cfg.Nx * cfg.Nz
         self.L = self._lib.sm2d_local_bins(h)
+        self.lanes = self._lib.sm2d_lanes(h)
 
     def close(self):
         if getattr(self, "h", None):
@@ -408,6 +434,32 @@ class Transport:
 
     def stream(self):
         return self._lib.sm2d_stream(self.h)
+
+    def batch_run(self, beams, max_iterations=100000, dose=True, results=True):
+        """Transport a list of Beam structures, `lanes` at a time.  Returns
+        (dose [n, Nz, Nx] or None, list of result dicts or None)."""
+        n = len(beams)
+        arr = (Beam * max(n, 1))(*beams)
+        d = np.zeros((n, self.cfg.Nz, self.cfg.Nx)) if dose else None
+        r = (SpotResult * max(n, 1))() if results else None
+        check(self._lib.sm2d_batch_run(self.h, C.cast(arr, C.c_void_p), n, int(max_iterations),
+                                       _p(d) if dose else None, C.cast(r, C.c_void_p) if results else None))
+        return d, ([r[i].as_dict() for i in range(n)] if results else None)
+
+    def batch_inject(self, beams):
+        """Reset every lane and inject beams[i] into lane i (asynchronous)."""
+        arr = (Beam * max(len(beams), 1))(*beams)
+        check(self._lib.sm2d_batch_inject(self.h, C.cast(arr, C.c_void_p), len(beams)))
+
+    def batch_results(self, n):
+        r = (SpotResult * max(n, 1))()
+        check(self._lib.sm2d_batch_results(self.h, C.cast(r, C.c_void_p), n))
+        return [r[i].as_dict() for i in range(n)]
+
+    def batch_dose(self, n):
+        d = np.zeros((n, self.cfg.Nz, self.cfg.Nx))
+        check(self._lib.sm2d_batch_dose(self.h, _p(d), n))
+        return d
 
     def run_profiled(self, n_iterations):
         n, launches = C.c_int(), C.c_int()
