@@ -77,6 +77,9 @@ def auto_lanes(cfg, free_bytes, cap=64):
 
 
 def workload_desc(grid, L):
+    if SMALL:
+        return ("profiling case: 80 MeV Gaussian beam (sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 0.8 MeV, "
+                "1000 samples) in water 100x200 cells @0.5 mm; reference grids; full K1-K6 + audit per iteration")
     if grid == "log":
         ph = "256 log E bins 0.1-250 MeV, 512 theta bins +-pi/2, 128 local bins (8x4x4x1), energy-split method"
     else:
@@ -303,9 +306,11 @@ def run_gpu_arm(args):
     achieved = alg_bytes / (ms["transport"] / 1e3) / 1e9 if ms["transport"] > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "k_transport_traffic.json")
-    if os.path.exists(tp):
+    if os.path.exists(tp) and not SMALL and args.grid == "reference":
+        # DRAM bytes per deposit launch from the ncu capture of this workload
+        # (recorded per lane; the lanes' work adds up)
         tr = json.load(open(tp))
-        traffic = tr.get("dram_bytes_per_launch")
+        traffic = tr["dram_bytes_per_launch_per_lane"] * B
     step_total = sum(ms.values())
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_src, "kernel": "k_transport (deposit pass)",
@@ -360,6 +365,7 @@ def main():
         global SMALL
         SMALL = True
         BEAM["E0"] = 80.0
+        BEAM["sigma_E"] = 0.8
     if args.impl == "reference":
         return run_reference_arm(args)
     return run_gpu_arm(args)

@@ -1655,14 +1655,24 @@ int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* la
     }
     cudaEvent_t saved[E];
     memcpy(saved, c.ev, sizeof saved);
-    for (int i = 0; i < n; ++i) {
-        for (int k = 0; k < E; ++k) c.ev[k] = c.pev[(size_t)E * i + k];
-        if ((rc = DISPATCH(c, launch_body, true, false, false))) break;
+    // passes in chunks of 16, stopping once no lane has work
+    int launched = 0;
+    const int start_pass = c.gs_host->pass;
+    while (launched < n) {
+        const int m = std::min(16, n - launched);
+        for (int i = launched; i < launched + m; ++i) {
+            for (int k = 0; k < E; ++k) c.ev[k] = c.pev[(size_t)E * i + k];
+            if ((rc = DISPATCH(c, launch_body, true, false, false))) break;
+        }
+        if (rc) break;
+        launched += m;
+        if ((rc = sync_state(c))) break;
+        if (c.gs_host->halt) break;
     }
     memcpy(c.ev, saved, sizeof saved);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
-    const int done = c.ls_host[0].iter - start;
+    const int done = c.gs_host->pass - start_pass;   // passes that transported
     for (int k = 0; k < E - 1; ++k) ms7[k] = 0.0f;
     for (int i = 0; i < done; ++i)
         for (int k = 0; k < E - 1; ++k) {
@@ -1670,8 +1680,8 @@ int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* la
             CK(cudaEventElapsedTime(&t, c.pev[(size_t)E * i + k], c.pev[(size_t)E * i + k + 1]));
             ms7[k] += t;
         }
-    if (done_iters) *done_iters = done;
-    if (launches) *launches = done * (c.p.use_buckets ? 7 : 6);
+    if (done_iters) *done_iters = c.ls_host[0].iter - start;
+    if (launches) *launches = launched * (c.p.use_buckets ? 7 : 6);
     return 0;
 }
 

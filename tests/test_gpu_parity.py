@@ -261,5 +261,6 @@ def test_async_spot_pipeline_matches_blocking_api():
         t.reset()
         t.inject_async(b)
         n_it, ms, launches = t.run_profiled(3000)
-        assert n_it == n_ref and launches == (7 if cfg.use_buckets else 6) * n_it
+        per = 7 if cfg.use_buckets else 6
+        assert n_it == n_ref and per * (n_it + 1) <= launches <= per * (n_it + 16)
         assert ms["transport"] > 0 and all(v >= 0 for v in ms.values())
