@@ -212,6 +212,9 @@ int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_i
 int sm2d_batch_inject(sm2d_handle h, const sm2d_beam* beams, int n_beams);
 int sm2d_batch_results(sm2d_handle h, sm2d_spot_result* results, int n);
 int sm2d_batch_dose(sm2d_handle h, double* dose, int n);
+/* audit record of every iteration of lane `lane`'s spot (up to the history
+ * capacity, problem.max_iterations) */
+int sm2d_batch_audit_history(sm2d_handle h, int lane, sm2d_audit* out, int max_entries, int* n_entries);
 
 /* ---- host tables (no GPU needed) ---- */
 /* EnergyGrid(E_min,E_max,N) log grid (grids.cpp:6-24): edges[N+1], rep[N] */

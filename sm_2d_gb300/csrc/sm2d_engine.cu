@@ -527,7 +527,7 @@ __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
 // increments in the dl_* arrays (one atomic per cell run of a warp) and the
 // per-lane audit sums (staged per block in shared memory).
 template <class Lay, int PASS>
-__global__ void __launch_bounds__(kThreads, 2) k_transport(Dev d) {
+__global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 4 : 3) k_transport(Dev d) {
     __shared__ LaneSums<6> s_sum;   // drop_w, drop_e, Win, Ein, Wout, Eout
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
@@ -1029,7 +1029,7 @@ struct Ctx {
     cudaGraphConditionalHandle cond{};
     cudaEvent_t ev[10] = {};   // 0..7 one iteration's stages, 8..9 a whole run
     float step_ms[7] = {};
-    int grid_cell = 0, grid_transport = 0;   // warp-per-cell kernels, transport
+    int grid_cell = 0, grid_transport = 0, grid_keys = 0;   // warp-per-cell kernels, deposit pass, claim pass
     size_t ctab_words = 0;                   // claim-table size in 64-bit words
     size_t ccount_n = 0;
     bool injected = false;
@@ -1065,7 +1065,7 @@ struct Impl {
     // ev[0..7] bracket: classify, lists, claim pass, selection, deposit pass,
     // K4 bucket move, finalize.
     static int launch_body(Ctx& c, bool timed, bool use_cond, bool lists) {
-        const int gc = c.grid_cell, gt = c.grid_transport;
+        const int gc = c.grid_cell, gt = c.grid_transport, gk = c.grid_keys;
         const bool bk = c.p.use_buckets != 0;
         auto rec = [&](int k) { return timed ? cudaEventRecord(c.ev[k], c.s) : cudaSuccess; };
         CK(rec(0));
@@ -1073,7 +1073,7 @@ struct Impl {
         CK(rec(1));
         if (lists) k_order_lists<<<1, 1024, 0, c.s>>>(c.d);
         CK(rec(2));
-        k_transport<Lay, PASS_KEYS><<<gt, kThreads, 0, c.s>>>(c.d);
+        k_transport<Lay, PASS_KEYS><<<gk, kThreads, 0, c.s>>>(c.d);
         CK(rec(3));
         if (bk) k_select_buckets<Lay, true><<<gc, kThreads, 0, c.s>>>(c.d);
         else k_select_buckets<Lay, false><<<gc, kThreads, 0, c.s>>>(c.d);
@@ -1089,15 +1089,20 @@ struct Impl {
         CK(cudaGetLastError());
         return 0;
     }
+    // grids of the two transport passes: every resident block once (the
+    // kernels stride over the bin list)
     static int transport_grid(Ctx& c, int sms) {
-        int per_sm = 0;
+        int per_sm = 0, per_sm_keys = 0;
         cudaError_t e = c.p.use_buckets
                             ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_BUCKET>, kThreads, 0)
                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_DIRECT>, kThreads, 0);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_keys, k_transport<Lay, PASS_KEYS>, kThreads, 0);
         if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
         const long long blocks_for_cap = ((long long)c.d.bins_cap + kThreads - 1) / kThreads;
-        const long long full = (long long)std::max(per_sm, 1) * std::max(sms, 1);
-        c.grid_transport = (int)std::max(1LL, std::min(full, blocks_for_cap));
+        const long long s = std::max(sms, 1);
+        c.grid_transport = (int)std::max(1LL, std::min((long long)std::max(per_sm, 1) * s, blocks_for_cap));
+        c.grid_keys = (int)std::max(1LL, std::min((long long)std::max(per_sm_keys, 1) * s, blocks_for_cap));
         return 0;
     }
     static int clear_all(Ctx& c, int) {
@@ -1312,7 +1317,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
     A(d.gs, IterGlobal, 1);
     A(d.ls, LaneState, B);
-    d.hist_cap = B == 1 ? (p->max_iterations > 0 ? p->max_iterations : 4096) : 0;
+    d.hist_cap = p->max_iterations > 0 ? p->max_iterations : 4096;
     A(d.hist, sm2d_audit, std::max(1, B * d.hist_cap));
     d.bucket_bytes = bucket_bytes_for(c->L);
     if (p->use_buckets) A(d.buckets, unsigned char, (size_t)4 * d.listed_cap * d.bucket_bytes);
@@ -1575,6 +1580,18 @@ int sm2d_get_audit_history(sm2d_handle h, sm2d_audit* out, int max_entries, int*
     if (rc) return rc;
     *n = std::min(std::min(h->ls_host[0].iter, h->d.hist_cap), max_entries);
     if (*n > 0) CK(cudaMemcpyAsync(out, h->d.hist, sizeof(sm2d_audit) * *n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+int sm2d_batch_audit_history(sm2d_handle h, int lane, sm2d_audit* out, int max_entries, int* n) {
+    if (!h || !out || !n || lane < 0 || lane >= h->B) return fail(SM2D_ERR_ARG, "invalid argument");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    *n = std::min(std::min(h->ls_host[lane].iter, h->d.hist_cap), max_entries);
+    if (*n > 0)
+        CK(cudaMemcpyAsync(out, h->d.hist + (size_t)lane * h->d.hist_cap, sizeof(sm2d_audit) * *n,
+                           cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
     return 0;
 }

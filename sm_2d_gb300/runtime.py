@@ -155,6 +155,7 @@ def lib(build_if_needed: bool = True):
         L.sm2d_batch_inject.argtypes = [P, P, I]
         L.sm2d_batch_results.argtypes = [P, P, I]
         L.sm2d_batch_dose.argtypes = [P, P, I]
+        L.sm2d_batch_audit_history.argtypes = [P, I, P, I, C.POINTER(I)]
         _LIB = L
         return L
 
@@ -455,6 +456,12 @@ class Transport:
         r = (SpotResult * max(n, 1))()
         check(self._lib.sm2d_batch_results(self.h, C.cast(r, C.c_void_p), n))
         return [r[i].as_dict() for i in range(n)]
+
+    def batch_audit_history(self, lane, n_max=100000):
+        arr = (Audit * n_max)()
+        n = C.c_int()
+        check(self._lib.sm2d_batch_audit_history(self.h, int(lane), C.cast(arr, C.c_void_p), n_max, C.byref(n)))
+        return [arr[i].as_dict() for i in range(n.value)]
 
     def batch_dose(self, n):
         d = np.zeros((n, self.cfg.Nz, self.cfg.Nx))
