@@ -60,6 +60,22 @@ def make_config(grid: str):
     return cfg.production()
 
 
+def spot_seeds(rank, lanes):
+    """Sample seeds of one wave on `rank`: disjoint across ranks (replicas by
+    spot), consecutive within a wave."""
+    return [BEAM["seed"] + 100003 * rank + i for i in range(lanes)]
+
+
+def max_over_ranks(x, dist, device):
+    """The largest of a per-rank value (timings take the slowest rank)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def lane_bytes(cfg):
     """Device bytes one lane of the engine holds (sm2d_create's allocation)."""
     nc = cfg.Nx * cfg.Nz
@@ -210,13 +226,8 @@ def run_gpu_arm(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
 
     # one wave = B spots of the workload beam, sample seeds differing per spot
-    def make_beams(seed0):
-        out = []
-        for i in range(B):
-            out.append(Beam(BEAM["x0"], BEAM["z0"], BEAM["theta0"], BEAM["E0"], BEAM["W"], BEAM["sigma_x"],
-                            BEAM["sigma_theta"], BEAM["sigma_E"], BEAM["n_samples"], seed0 + i))
-        return out
-    beams = make_beams(BEAM["seed"] + 100003 * rank)
+    beams = [Beam(BEAM["x0"], BEAM["z0"], BEAM["theta0"], BEAM["E0"], BEAM["W"], BEAM["sigma_x"],
+                  BEAM["sigma_theta"], BEAM["sigma_E"], BEAM["n_samples"], seed) for seed in spot_seeds(rank, B)]
     beam_arr = (Beam * B)(*beams)
     lib = t._lib
 
@@ -255,11 +266,7 @@ def run_gpu_arm(args):
             # pass, finalize (+ bucket move)
             launches += 10 + (7 if cfg.use_buckets else 6) * passes
     barrier()
-    total_ms = float(np.sum(times))
-    if dist:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(np.sum(times), dist, "cuda")
     spots = args.steps * B * world
     value = spots / (total_ms / 1e3)
 
@@ -282,11 +289,7 @@ def run_gpu_arm(args):
         if rc != 0:
             raise RuntimeError(lib.sm2d_last_error().decode())
         e2e_times.append(e0.elapsed_time(e1))
-    e2e_ms = float(np.sum(e2e_times))
-    if dist:
-        tt = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
+    e2e_ms = max_over_ranks(np.sum(e2e_times), dist, "cuda")
     e2e_value = spots / (e2e_ms / 1e3)
 
     # ---- per-kernel device time: eager replay of one wave with CUDA events

@@ -128,6 +128,79 @@ __device__ __forceinline__ int resolve(const Dev& d, const unsigned long long* r
 // (bcell, face) towards dcell; col is the emitting column seen from bcell
 // (0..10, 5 = bcell itself) and seq the emission index within the bin.
 // Returns the weight that found no container.
+// Angle and energy re-binning of an emitted component at (theta, E), the
+// weight-independent part of emit_component: the nearest theta-bin centre
+// and its neighbour with the frac^2 share, and the energy bin (with the
+// energy split: the neighbouring centres and the upper share).  The lateral
+// spread emits the same (theta, E) into up to 11 cells, so it is computed
+// once per component.
+struct EmitPlan {
+    int bc, tb1;      // theta: nearest centre bin, neighbour (== bc: none)
+    float tw1;        // frac^2 share of the neighbour
+    int k;            // energy bin containing E (device_find_bin_edges)
+    int lo, hi;       // split method: centres around E (lo < 0: no split)
+    float fh;         // split method: share of hi
+};
+__device__ __forceinline__ EmitPlan plan_emission(const Dev& d, float theta, float E) {
+    EmitPlan p;
+    const float tmin = d.th[0], tmax = d.th[d.N_theta];
+    const float dth = (tmax - tmin) / (float)d.N_theta;
+    const float tc = fmaxf(tmin, fminf(theta, tmax));
+    const float c0 = tmin + 0.5f * dth;
+    int bc = (int)floorf((tc - c0) / dth + 0.5f);
+    bc = max(0, min(bc, d.N_theta - 1));
+    const float delta = tc - (c0 + (float)bc * dth);
+    int tb1 = bc;
+    if (delta > 0.0f && bc < d.N_theta - 1) tb1 = bc + 1;
+    else if (delta < 0.0f && bc > 0) tb1 = bc - 1;
+    p.bc = bc;
+    p.tb1 = tb1;
+    p.tw1 = 0.0f;
+    if (tb1 != bc) {
+        const float f = fminf(1.0f, fabsf(delta) / dth);
+        p.tw1 = f * f;
+    }
+    const float Ec = fmaxf(d.Ee[0], fminf(E, d.Ee[d.N_E]));
+    const int k = find_bin(d.Ee, d.N_E, Ec);
+    p.k = k;
+    p.lo = -1;
+    p.hi = -1;
+    p.fh = 0.0f;
+    if (d.esplit) {
+        const float ck = e_center(d, k);
+        const int lo = Ec >= ck ? k : k - 1, hi = lo + 1;
+        if (lo >= 0 && hi <= d.N_E - 1) {
+            const float cl = e_center(d, lo), ch = e_center(d, hi);
+            p.lo = lo;
+            p.hi = hi;
+            p.fh = (Ec - cl) / (ch - cl);
+        }
+    }
+    return p;
+}
+// bin_energy of a planned component of weight w
+__device__ __forceinline__ EParts plan_energy(const Dev& d, const EmitPlan& p, float w) {
+    EParts e;
+    e.n = 1;
+    e.bin[0] = e.bin[1] = p.k;
+    e.frac[0] = 1.0f;
+    e.frac[1] = 0.0f;
+    e.Erep = e_center(d, p.k);
+    if (!d.esplit || p.lo < 0) return e;
+    const float cl = e_center(d, p.lo), ch = e_center(d, p.hi), fh = p.fh;
+    if (fh <= 0.0f) { e.bin[0] = p.lo; e.Erep = cl; return e; }
+    if (fh >= 1.0f) { e.bin[0] = p.hi; e.Erep = ch; return e; }
+    if (w * fminf(fh, 1.0f - fh) < d.split_min_w) {   // light minor part stays with the major bin
+        if (fh >= 0.5f) { e.bin[0] = p.hi; e.Erep = ch; } else { e.bin[0] = p.lo; e.Erep = cl; }
+        return e;
+    }
+    e.n = 2;
+    e.bin[0] = p.lo; e.frac[0] = 1.0f - fh;
+    e.bin[1] = p.hi; e.frac[1] = fh;
+    e.Erep = e.frac[0] * cl + e.frac[1] * ch;
+    return e;
+}
+
 template <class Lay, int PASS>
 __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int bcell, int face, int dcell, int col,
                                      int seq, uint32_t want, int lidx, float w, Tally& t) {
@@ -166,30 +239,19 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
 }
 
 // Two-bin theta split around the nearest bin centre with frac^2 weight to
-// the neighbour, energy re-binning, bucket claim (device_bucket.cuh:431-533).
+// the neighbour, energy re-binning, bucket claim (device_bucket.cuh:431-533),
+// for a component planned by plan_emission.
 template <class Lay, int PASS>
 __device__ float emit_component(const Dev& d, const Src& src, int par, int bcell, int face, int dcell, int col,
-                                float theta, float E, float weight, int xs, int zs, Tally& t) {
+                                const EmitPlan& pl, float weight, int xs, int zs, Tally& t) {
     if (weight <= 0.0f) return 0.0f;
-    const float tmin = d.th[0], tmax = d.th[d.N_theta];
-    const float dth = (tmax - tmin) / (float)d.N_theta;
-    const float tc = fmaxf(tmin, fminf(theta, tmax));
-    const float c0 = tmin + 0.5f * dth;
-    int bc = (int)floorf((tc - c0) / dth + 0.5f);
-    bc = max(0, min(bc, d.N_theta - 1));
-    const float delta = tc - (c0 + (float)bc * dth);
-    int tb1 = bc;
-    if (delta > 0.0f && bc < d.N_theta - 1) tb1 = bc + 1;
-    else if (delta < 0.0f && bc > 0) tb1 = bc - 1;
     float tw0 = 1.0f, tw1 = 0.0f;
-    if (tb1 != bc) {
-        float f = fminf(1.0f, fabsf(delta) / dth);
-        tw1 = f * f;
+    if (pl.tb1 != pl.bc) {
+        tw1 = pl.tw1;
         tw0 = 1.0f - tw1;
         if (d.esplit && weight * tw1 < d.split_min_w) { tw1 = 0.0f; tw0 = 1.0f; }
     }
-    const float Ec = fmaxf(d.Ee[0], fminf(E, d.Ee[d.N_E]));
-    const EParts ep = bin_energy(d, Ec, weight);
+    const EParts ep = plan_energy(d, pl, weight);
     float dropped = 0.0f;
     for (int ei = 0; ei < ep.n; ++ei) {
         const int Eb = ep.bin[ei];
@@ -201,7 +263,7 @@ __device__ float emit_component(const Dev& d, const Src& src, int par, int bcell
             if (wt <= 0.0f) continue;
             float we = weight * wt;
             if (d.esplit) we = we * ep.frac[ei];
-            const int tb = ti ? tb1 : bc;
+            const int tb = ti ? pl.tb1 : pl.bc;
             const uint32_t want = make_bid((uint32_t)(tb / Lay::NT), bE);
             const int l = Lay::enc(tb % Lay::NT, El, xs, zs);
             dropped += put<Lay, PASS>(d, src, par, bcell, face, dcell, col, 2 * ei + ti, want, l, we, t);
@@ -246,6 +308,7 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
         for (int i = 0; i < N; ++i) w[i] /= s;
     }
     const int ixs = src % d.Nx, izs = (src / d.Nx) % d.Nz, tz = izs + 1;
+    const EmitPlan pl = plan_emission(d, theta, E);
     float dropped = 0.0f;
     for (int i = 0; i < N; ++i) {
         const float wf = w[i];
@@ -258,8 +321,8 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
         // in the same pass (k1k6_pipeline.cu:800-847 maps one list at a time)
         if (ecell != src && d.cls[ecell] != my_cls) { dropped += weight * wf; continue; }
         const int xt = off < 0 ? Lay::NX - 1 : (off > 0 ? 0 : Lay::NX / 2);
-        dropped += emit_component<Lay, PASS>(d, sc, par, ecell, FACE_ZP, ecell + d.Nx, N - 1 - i, theta, E,
-                                             weight * wf, xt, 0, t);
+        dropped += emit_component<Lay, PASS>(d, sc, par, ecell, FACE_ZP, ecell + d.Nx, N - 1 - i, pl, weight * wf,
+                                             xt, 0, t);
     }
     return dropped;
 }
@@ -363,6 +426,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
     }
     float wl = 0.0f, wr = 0.0f;
     if (wcf < 1.0f - 1e-6f) {
+        const EmitPlan pl = plan_emission(d, theta_new, E_new);
         const float wlr = fmaxf(0.0f, gauss_cdf(lb, x_new, sig_cell));
         const float wrr = fmaxf(0.0f, 1.0f - gauss_cdf(rb, x_new, sig_cell));
         const float tt = fmaxf(0.0f, 1.0f - wcf);
@@ -375,8 +439,8 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
         if (wl > 0.0f) {
             const float ws = w_new * wl;
             if (ix > 0) {
-                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XM, cell - 1, 5, theta_new, E_new, ws,
-                                                           Lay::NX - 1, zst, t);
+                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XM, cell - 1, 5, pl, ws, Lay::NX - 1,
+                                                           zst, t);
                 if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
             } else {
                 t.w_bnd += ws;
@@ -386,8 +450,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
         if (wr > 0.0f) {
             const float ws = w_new * wr;
             if (ix < d.Nx - 1) {
-                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XP, cell + 1, 5, theta_new, E_new, ws,
-                                                           0, zst, t);
+                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XP, cell + 1, 5, pl, ws, 0, zst, t);
                 if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
             } else {
                 t.w_bnd += ws;
@@ -438,7 +501,8 @@ __device__ void emit_cross(const Dev& d, const Src& sc, int par, bool k3, int ce
     const float xo = face == FACE_XP ? -dx * 0.5f : (face == FACE_XM ? dx * 0.5f : x_new);
     const int xsn = sub_bin(xo, dx, Lay::NX);
     const int zsn = face == FACE_ZM ? Lay::NZ - 1 : sub_bin(z_new, dz, Lay::NZ);
-    const float dr = emit_component<Lay, PASS>(d, sc, par, cell, face, nb, 5, theta_new, E_new, w_new, xsn, zsn, t);
+    const float dr =
+        emit_component<Lay, PASS>(d, sc, par, cell, face, nb, 5, plan_emission(d, theta_new, E_new), w_new, xsn, zsn, t);
     if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
     if (fold) {
         const float tw = fmaxf(0.0f, w_new - dr);
