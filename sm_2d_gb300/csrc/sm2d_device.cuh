@@ -98,8 +98,10 @@ struct Dev {
     int lutN;
     float lutEmin, lutEmax;
     const float *R, *logE, *logR;
-    const float *feA, *feB;
-    float E_fine_on, wmin, step_coarse, sx0;
+    // per lane: Fermi-Eyges moments A(z), B(z), sigma_total(z) [B][Nz] of the
+    // lane's beam (k1k6_pipeline.cu:1061-1206) and its initial sigma_x [B]
+    const float *feA, *feB, *feS, *sx0;
+    float E_fine_on, wmin, step_coarse;
     int b_on, b_off;
     int straggle, nuclear, seed_mode, esplit;
     float prune_coarse, prune_fine, split_min_w, stop_frac;

@@ -552,8 +552,8 @@ __global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 4 : 3) k_transpo
             const int slot = (int)(r.y & 31u), sslot = (int)((r.y >> 5) & 31u), lidx = (int)((r.y >> 10) & 0xFFu);
             const bool k3 = ((r.y >> 18) & 1u) != 0;
             const unsigned salt = d.salt ? (unsigned)d.ls[ln].iter * 0x9E3779B9u : 0u;
-            transport_bin<Lay, PASS>(d, par, k3, cell, cell - ln * d.Nc, r.w, slot, sslot, lidx, __uint_as_float(r.z),
-                                     salt, tag, t);
+            transport_bin<Lay, PASS>(d, par, k3, cell, ln, cell - ln * d.Nc, r.w, slot, sslot, lidx,
+                                     __uint_as_float(r.z), salt, tag, t);
         }
         if (PASS != PASS_KEYS) {
             unsigned same[5];
@@ -991,19 +991,45 @@ __global__ void k_set_pass_limit(IterGlobal* gs, int more) {
     gs->max_pass = lim > INT_MAX ? INT_MAX : (int)lim;
 }
 
+// Lateral post-convolution kernels of every lane from its sigma_total(z)
+// and initial sigma_x (the kernel of gpu_transport_wrapper.cu:551-616):
+// a Gaussian of sigma^2 = sigma_total^2 - sigma_x0^2 over +-ceil(3 sigma/dx)
+// cells (at most Nx/2), normalised; thread per (lane, row).
+__global__ void k_dose_tables(const float* __restrict__ feS, const float* __restrict__ sx0, float dx, int Nx, int Nz,
+                              int B, int stride, int* __restrict__ half, double* __restrict__ ker) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B * Nz) return;
+    const int ln = i / Nz;
+    const float st = feS[i], s0 = sx0[ln];
+    const float msq = st * st - s0 * s0;
+    double* k = ker + (size_t)i * stride;
+    if (msq <= 1e-6f) { half[i] = 0; return; }
+    const float sc = sqrtf(msq) / dx;
+    int h = (int)ceilf(3.0f * sc);
+    h = max(1, min(h, Nx / 2));
+    double sum = 0.0;
+    for (int j = -h; j <= h; ++j) {
+        const double v = exp(-0.5 * ((double)j * j) / ((double)sc * sc));
+        k[j + h] = v;
+        sum += v;
+    }
+    for (int j = 0; j <= 2 * h; ++j) k[j] /= sum;
+    half[i] = h;
+}
+
 // Lateral MCS post-convolution of EdepC, one thread per output cell of each
-// lane (gpu_transport_wrapper.cu:551-616; kernels built on the host at
-// create).
+// lane, with that lane's row kernels.
 __global__ void k_dose(const double* __restrict__ edep, const int* __restrict__ half, const double* __restrict__ ker,
                        int kstride, int Nx, int Nz, int B, double* __restrict__ out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nc = (long long)Nx * Nz;
     if (i >= nc * B) return;
     const int lc = (int)(i % nc);
+    const long long ln = i / nc;
     const int iz = lc / Nx, ix = lc - iz * Nx;
-    const int h = half[iz];
+    const int h = half[ln * Nz + iz];
     if (h == 0) { out[i] = edep[i]; return; }
-    const double* k = ker + (size_t)iz * kstride;
+    const double* k = ker + (size_t)(ln * Nz + iz) * kstride;
     const double* row = edep + (i - lc) + (size_t)iz * Nx;
     double acc = 0.0;
     for (int j = -h; j <= h; ++j) {
@@ -1016,7 +1042,12 @@ __global__ void k_dose(const double* __restrict__ edep, const int* __restrict__ 
 // ================================================================== engine
 struct Ctx {
     sm2d_problem p{};
-    std::vector<float> th, Ee, feA, feB, feS;
+    std::vector<float> th, Ee, feA, feB, feS;   // Fermi-Eyges tables of the problem's E0 and sigma_x
+    // per-lane Fermi-Eyges tables: host copy [feA B*Nz | feB B*Nz | feS B*Nz |
+    // sigma_x B] of fe_dev, and the (E0, sigma_x) each lane's tables are for
+    std::vector<float> fe_host, fe_E0, fe_sx;
+    float* fe_dev = nullptr;
+    int fe_lo = 0, fe_hi = -1;      // lanes whose tables changed since the last upload
     int L = 0, layout = 0;  // 0: LayoutRef, 1: LayoutB128
     int B = 1;
     Dev d{};
@@ -1035,10 +1066,10 @@ struct Ctx {
     bool injected = false;
     BeamArgs* beams_dev = nullptr;  // device beams, one per lane
     BeamArgs* beams_host = nullptr; // pinned staging
-    int* dose_half = nullptr;       // per-row half width of the lateral kernel
-    double* dose_ker = nullptr;     // per-row kernel weights
+    int* dose_half = nullptr;       // per-lane, per-row half width of the lateral kernel [B][Nz]
+    double* dose_ker = nullptr;     // its weights [B][Nz][dose_stride]
     double* dose_dev = nullptr;     // convolved dose [B][Nc]
-    int dose_stride = 1;
+    int dose_stride = 1;            // 2 (Nx/2) + 1: the widest kernel
     std::vector<cudaEvent_t> pev;   // event pool of the profiled replay
 };
 
@@ -1191,6 +1222,45 @@ static int enqueue_dose(Ctx& c) {
     return 0;
 }
 
+// Fermi-Eyges tables of lane ln for a beam of energy E0 and width sigma_x
+// (gpu_transport_wrapper.cu:273-276 hands the beam's E0 and sigma_x to the
+// precompute of k1k6_pipeline.cu:1061-1206); recomputed only when they change.
+static void set_lane_fe(Ctx& c, int ln, float E0, float sx) {
+    if (c.fe_E0[ln] == E0 && c.fe_sx[ln] == sx) return;
+    const int Nz = c.d.Nz;
+    const size_t BN = (size_t)c.B * Nz;
+    float* A = c.fe_host.data() + (size_t)ln * Nz;
+    fermi_eyges_moments(E0, Nz, c.d.dz, sx, A, A + BN, A + 2 * BN);
+    c.fe_host[3 * BN + ln] = sx;
+    c.fe_E0[ln] = E0;
+    c.fe_sx[ln] = sx;
+    c.fe_lo = std::min(c.fe_lo, ln);
+    c.fe_hi = std::max(c.fe_hi, ln);
+}
+
+// Upload the changed lanes' tables and rebuild their lateral dose kernels.
+// The copies are from pageable memory, which the copy call has read by the
+// time it returns, so fe_host may change right after.
+static int upload_lane_fe(Ctx& c) {
+    if (c.fe_hi < c.fe_lo) return 0;
+    const int Nz = c.d.Nz, lo = c.fe_lo, n = c.fe_hi - c.fe_lo + 1;
+    const size_t BN = (size_t)c.B * Nz;
+    for (int k = 0; k < 3; ++k)
+        CK(cudaMemcpyAsync(c.fe_dev + k * BN + (size_t)lo * Nz, c.fe_host.data() + k * BN + (size_t)lo * Nz,
+                           sizeof(float) * (size_t)n * Nz, cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.fe_dev + 3 * BN + lo, c.fe_host.data() + 3 * BN + lo, sizeof(float) * n,
+                       cudaMemcpyHostToDevice, c.s));
+    const int rows = n * Nz;
+    k_dose_tables<<<(rows + 127) / 128, 128, 0, c.s>>>(c.fe_dev + 2 * BN + (size_t)lo * Nz, c.fe_dev + 3 * BN + lo,
+                                                      c.d.dx, c.d.Nx, Nz, n, c.dose_stride,
+                                                      c.dose_half + (size_t)lo * Nz,
+                                                      c.dose_ker + (size_t)lo * Nz * c.dose_stride);
+    CK(cudaGetLastError());
+    c.fe_lo = c.B;
+    c.fe_hi = -1;
+    return 0;
+}
+
 // Beams into the device (lane 0 = *b for a single spot; empty beams elsewhere)
 static int stage_beams(Ctx& c, const sm2d_beam* beams, int n, int* max_n) {
     int mx = 1;
@@ -1260,7 +1330,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     d.lutEmin = p->E_min > 0.0f ? p->E_min : c->Ee[0];
     d.lutEmax = p->E_max > 0.0f ? p->E_max : c->Ee[N];
     d.E_fine_on = p->E_fine_on; d.wmin = p->weight_active_min;
-    d.step_coarse = p->step_coarse; d.sx0 = p->sigma_x_initial;
+    d.step_coarse = p->step_coarse;
     // compute_b_E_threshold: EnergyGrid::FindBin(E) / N_E_local
     auto find_bin_host = [&](float E) {
         if (E < c->Ee[0]) return 0;
@@ -1285,15 +1355,16 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
 #define A(ptr, type, n)                                              \
     if ((rc = dalloc(*c, &q, sizeof(type) * (size_t)(n)))) return bail(rc); \
     ptr = reinterpret_cast<type*>(q)
-    float *th_d, *Ee_d, *R_d, *lE_d, *lR_d, *fa, *fb;
+    float *th_d, *Ee_d, *R_d, *lE_d, *lR_d;
     A(th_d, float, p->N_theta + 1);
     A(Ee_d, float, N + 1);
     A(R_d, float, N);
     A(lE_d, float, N);
     A(lR_d, float, N);
-    A(fa, float, p->Nz);
-    A(fb, float, p->Nz);
-    d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d; d.feA = fa; d.feB = fb;
+    const size_t BN = (size_t)B * p->Nz;
+    A(c->fe_dev, float, 3 * BN + B);
+    d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d;
+    d.feA = c->fe_dev; d.feB = c->fe_dev + BN; d.feS = c->fe_dev + 2 * BN; d.sx0 = c->fe_dev + 3 * BN;
     A(d.bid, uint32_t, ns);
     A(d.val, float, ns * c->L);
     for (int k = 0; k < 2; ++k) {
@@ -1327,25 +1398,12 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.ccount, int, c->ccount_n);
     A(d.bkt_ids, uint32_t, (size_t)4 * d.listed_cap * kKb);
     A(c->beams_dev, BeamArgs, B);
-    {   // lateral post-convolution kernels per depth row
-        std::vector<int> half(p->Nz, 0);
-        std::vector<double> k(p->Nx + 2);
-        int hmax = 1;
-        for (int iz = 0; iz < p->Nz; ++iz) {
-            half[iz] = lateral_kernel(c->feS[iz], p->sigma_x_initial, p->dx, p->Nx, k.data());
-            hmax = std::max(hmax, half[iz]);
-        }
-        c->dose_stride = 2 * hmax + 1;
-        std::vector<double> ker((size_t)p->Nz * c->dose_stride, 0.0);
-        for (int iz = 0; iz < p->Nz; ++iz)
-            if (half[iz]) lateral_kernel(c->feS[iz], p->sigma_x_initial, p->dx, p->Nx, &ker[(size_t)iz * c->dose_stride]);
-        A(c->dose_half, int, p->Nz);
-        A(c->dose_ker, double, ker.size());
-        A(c->dose_dev, double, NcB);
-        if (cudaMemcpy(c->dose_half, half.data(), sizeof(int) * p->Nz, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(c->dose_ker, ker.data(), sizeof(double) * ker.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(fail(SM2D_ERR_CUDA, "dose kernel upload"));
-    }
+    // lateral post-convolution kernels per lane and depth row: half widths
+    // are at most Nx/2
+    c->dose_stride = 2 * std::max(1, p->Nx / 2) + 1;
+    A(c->dose_half, int, BN);
+    A(c->dose_ker, double, BN * c->dose_stride);
+    A(c->dose_dev, double, NcB);
 #undef A
     if (cudaMallocHost(&c->gs_host, sizeof(IterGlobal)) != cudaSuccess ||
         cudaMallocHost(&c->ls_host, sizeof(LaneState) * B) != cudaSuccess ||
@@ -1360,9 +1418,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
               cudaMemcpyAsync(Ee_d, c->Ee.data(), sizeof(float) * (N + 1), cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(R_d, R.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(lE_d, lE.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-              cudaMemcpyAsync(lR_d, lR.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-              cudaMemcpyAsync(fa, c->feA.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-              cudaMemcpyAsync(fb, c->feB.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess;
+              cudaMemcpyAsync(lR_d, lR.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.bid, 0xFF, ns * 4, s) == cudaSuccess &&
          cudaMemsetAsync(d.val, 0, ns * c->L * 4, s) == cudaSuccess;
     for (int k = 0; k < 2 && ok; ++k) ok = cudaMemsetAsync(d.occ[k], 0, NcB * 4, s) == cudaSuccess;
@@ -1379,6 +1435,24 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
          cudaMemsetAsync(d.ccount, 0, c->ccount_n * sizeof(int), s) == cudaSuccess &&
          cudaMemsetAsync(d.bkt_ids, 0xFF, (size_t)4 * d.listed_cap * kKb * 4, s) == cudaSuccess;
     if (!ok) return bail(fail(SM2D_ERR_CUDA, "initial copies failed"));
+    // every lane starts with the problem's tables
+    c->fe_host.assign(3 * BN + B, 0.0f);
+    c->fe_E0.assign(B, -1.0f);
+    c->fe_sx.assign(B, -1.0f);
+    c->fe_lo = B;
+    c->fe_hi = -1;
+    for (int ln = 0; ln < B; ++ln) {
+        if (ln == 0) set_lane_fe(*c, 0, p->E0, p->sigma_x_initial);
+        else {
+            for (int k = 0; k < 3; ++k)
+                std::copy_n(c->fe_host.data() + k * BN, p->Nz, c->fe_host.data() + k * BN + (size_t)ln * p->Nz);
+            c->fe_host[3 * BN + ln] = p->sigma_x_initial;
+            c->fe_E0[ln] = p->E0;
+            c->fe_sx[ln] = p->sigma_x_initial;
+            c->fe_hi = ln;
+        }
+    }
+    if (upload_lane_fe(*c)) return bail(SM2D_ERR_CUDA);
     if (push_state(*c)) return bail(SM2D_ERR_CUDA);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -1418,6 +1492,8 @@ int sm2d_inject_async(sm2d_handle h, const sm2d_beam* b) {
     int max_n = 1;
     int rc = stage_beams(c, b, 1, &max_n);
     if (rc) return rc;
+    set_lane_fe(c, 0, c.p.E0, c.p.sigma_x_initial);   // a single spot keeps the problem's tables
+    if ((rc = upload_lane_fe(c))) return rc;
     if ((rc = DISPATCH(c, inject, max_n, true))) return rc;
     c.injected = true;
     return 0;
@@ -1744,6 +1820,8 @@ int sm2d_batch_inject(sm2d_handle h, const sm2d_beam* beams, int n) {
     if ((rc = reset_lanes(c))) return rc;
     int max_n = 1;
     if ((rc = stage_beams(c, beams, n, &max_n))) return rc;
+    for (int ln = 0; ln < n; ++ln) set_lane_fe(c, ln, beams[ln].E0, beams[ln].sigma_x);
+    if ((rc = upload_lane_fe(c))) return rc;
     if ((rc = DISPATCH(c, inject, max_n, false))) return rc;
     c.injected = true;
     return 0;

@@ -519,12 +519,12 @@ __device__ __forceinline__ int exit_face(float x, float z, float dx, float dz) {
     return -1;
 }
 
-// One component of a listed cell gc (lane-local index lc, which the random
-// seeds use): local bin lidx of psi_in slot `slot` (sslot: the slot number
+// One component of a listed cell gc of lane ln (lane-local index lc, which
+// the random seeds use): local bin lidx of psi_in slot `slot` (sslot: the slot number
 // the seeds use).  par selects the occupancy list of psi_out (par ^ 1).
 template <class Lay, int PASS>
-__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int lc, uint32_t bid, int slot, int sslot,
-                              int lidx, float w, unsigned salt, uint32_t tag, Tally& t) {
+__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, int lc, uint32_t bid, int slot,
+                              int sslot, int lidx, float w, unsigned salt, uint32_t tag, Tally& t) {
     const float dx = d.dx, dz = d.dz;
     int tl, El, xs, zs;
     Lay::dec(lidx, tl, El, xs, zs);
@@ -583,8 +583,8 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int lc, 
             E_rem = w_rem * E;
         }
         const float sm = fmaxf(step, 0.0f);
-        const float Ap = (d.feA && iz < d.Nz) ? d.feA[iz] : 0.0f;
-        const float Bp = (d.feB && iz < d.Nz) ? d.feB[iz] : 0.0f;
+        const float Ap = iz < d.Nz ? d.feA[(size_t)ln * d.Nz + iz] : 0.0f;
+        const float Bp = iz < d.Nz ? d.feB[(size_t)ln * d.Nz + iz] : 0.0f;
         const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm);
         sig_th = sqrtf(fmaxf(T * sm, 0.0f));
         const float dC = fmaxf(2.0f * Bp * sm + Ap * sm * sm + T * sm * sm * sm / 3.0f, 0.0f);
@@ -619,7 +619,8 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int lc, 
         const float s0 = p0 > 0.0f ? highland(E, p0) : 0.0f;
         const float A0 = s0 * s0;
         const float B0 = 0.5f * A0 * p0;
-        const float C0 = d.sx0 * d.sx0 + (A0 * p0 * p0) / 3.0f;
+        const float sx0 = d.sx0[ln];
+        const float C0 = sx0 * sx0 + (A0 * p0 * p0) / 3.0f;
         const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm);
         const float A1 = fmaxf(A0 + T * sm, 0.0f);
         const float C1 = fmaxf(C0 + 2.0f * B0 * sm + A0 * sm * sm + (1.0f / 3.0f) * T * sm * sm * sm, 0.0f);
