@@ -196,19 +196,34 @@ int sm2d_run_profiled(sm2d_handle h, int n_iterations, int* iterations_done, flo
  * one spot per call; a plan is a loop over such calls) ---- */
 /* lanes of the engine: spots transported together */
 int sm2d_lanes(sm2d_handle h);
-/* Transport n_spots beams to completion, `lanes` at a time (waves), each
- * spot exactly as sm2d_reset + sm2d_inject + sm2d_run would (same results,
- * lane by lane).  dose: host [n_spots][Nz][Nx] for the post-convolved
- * EdepC of each spot, or NULL; results: host [n_spots] or NULL;
- * max_iterations bounds each wave.  Blocking. */
+/* Transport a plan of n_spots beams to completion, each spot as an engine
+ * created with problem.E0 = beam.E0 and problem.sigma_x_initial =
+ * beam.sigma_x would transport it alone (sm2d_inject + sm2d_run; the
+ * reference hands the beam's E0 and sigma_x to its Fermi-Eyges precompute).
+ * `lanes` spots are in flight; a lane whose spot finishes takes the next
+ * spot of the plan inside the device loop (one graph launch for the plan).
+ * dose: host [n_spots][Nz][Nx] for the post-convolved EdepC of each spot,
+ * or NULL; results: host [n_spots] or NULL.  A spot that reaches
+ * max_iterations ends there: its remaining weight is booked as a transport
+ * drop and its result reads finished = 0.  Blocking. */
 int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, double* dose,
                    sm2d_spot_result* results);
-/* The steps of one wave of sm2d_batch_run, for callers that drive the loop
- * themselves: sm2d_batch_inject resets every lane and injects beams[i]
- * into lane i (lanes past n_beams stay empty; asynchronous, like
- * sm2d_inject_async); then sm2d_run / sm2d_run_async / sm2d_run_profiled
- * transport all lanes; sm2d_batch_results and sm2d_batch_dose read the
- * first n lanes back (blocking). */
+/* The three steps of sm2d_batch_run: sm2d_plan_load stages the plan on the
+ * device (its Fermi-Eyges tables computed on the host threads; with_dose
+ * keeps a device dose map per spot), sm2d_plan_run_async transports it on
+ * the engine's stream, sm2d_plan_results waits and copies dose (NULL: none)
+ * and results (NULL: none) back.  sm2d_plan_stats: device passes and refill
+ * rounds of the last plan. */
+int sm2d_plan_load(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, int with_dose);
+int sm2d_plan_run_async(sm2d_handle h);
+int sm2d_plan_results(sm2d_handle h, double* dose, sm2d_spot_result* results);
+int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills);
+/* One wave of spots, for callers that drive the loop themselves:
+ * sm2d_batch_inject resets every lane and injects beams[i] into lane i
+ * (lanes past n_beams stay empty; asynchronous, like sm2d_inject_async);
+ * then sm2d_run / sm2d_run_async / sm2d_run_profiled transport all lanes,
+ * max_iterations passes at most; sm2d_batch_results and sm2d_batch_dose
+ * read the first n lanes back (blocking). */
 int sm2d_batch_inject(sm2d_handle h, const sm2d_beam* beams, int n_beams);
 int sm2d_batch_results(sm2d_handle h, sm2d_spot_result* results, int n);
 int sm2d_batch_dose(sm2d_handle h, double* dose, int n);

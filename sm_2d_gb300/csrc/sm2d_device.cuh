@@ -16,6 +16,14 @@ namespace sm2d {
 constexpr uint32_t kEmpty = 0xFFFFFFFFu;
 constexpr int kKb = 32;
 constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kMaxLanes = 256;   // per-lane sums are staged in shared memory
+
+// One beam on the device (sm2d_beam).
+struct BeamArgs {
+    float x0, z0, theta0, E0, W, sx, sth, sE;
+    int n;
+    unsigned seed;
+};
 
 // Local-bin layout: lidx = t + NT*(e + NE*(x + NX*z))  (local_bins.hpp:62-78)
 template <int NT_, int NE_, int NX_, int NZ_>
@@ -59,6 +67,19 @@ struct IterGlobal {
     int wipe;              // claim tables are cleared before the next pass
     uint32_t ctag;         // claim pass number: the tag of claim-table entries
     unsigned long long gen;  // K1 classifications done since create (never reset)
+    // spot plan (sm2d_batch_run): lanes that finish take the plan's next
+    // spot inside the device loop; plan_n == 0 outside a plan
+    int plan_n;            // spots of the plan
+    int plan_next;         // next spot to hand out
+    int lane_max_it;       // iteration limit of one spot
+    int refills;           // refill rounds run
+    int occ_mark;          // psi_in's occupancy list length when the injection opened
+    int n_fin;             // lanes whose spot finished at this classification
+    int fin[kMaxLanes];    // those lanes, ascending
+    const BeamArgs* plan_beams;   // [plan_n]
+    const float* plan_fe;         // [plan_n][3 Nz + 1]: A(z), B(z), sigma_total(z), sigma_x
+    double* plan_dose;            // [plan_n][Nc] convolved dose, or null
+    sm2d_spot_result* plan_res;   // [plan_n]
 };
 
 // Per-lane (per-spot) state.
@@ -72,7 +93,9 @@ struct LaneState {
     int acc_active, acc_coarse, acc_slots;   // classify counters
     int inj_skip;          // the last injection found the lane occupied
     int w_fail, e_fail;    // iterations whose weight / energy audit failed
-    int pad0;
+    int spot;              // plan spot in this lane (-1: none)
+    int refill;            // the next injection fills this lane
+    int stopped;           // the spot reached the iteration limit of a plan
     // per-iteration accumulators, 14 consecutive doubles (reset by the
     // classify kernel); the transport adds to the first seven, the finalize
     // kernel to the last seven, in this order
@@ -100,7 +123,7 @@ struct Dev {
     const float *R, *logE, *logR;
     // per lane: Fermi-Eyges moments A(z), B(z), sigma_total(z) [B][Nz] of the
     // lane's beam (k1k6_pipeline.cu:1061-1206) and its initial sigma_x [B]
-    const float *feA, *feB, *feS, *sx0;
+    float *feA, *feB, *feS, *sx0;
     float E_fine_on, wmin, step_coarse;
     int b_on, b_off;
     int straggle, nuclear, seed_mode, esplit;

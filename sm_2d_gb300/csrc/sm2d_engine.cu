@@ -31,6 +31,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "sm2d.h"
@@ -41,7 +43,6 @@
 
 namespace sm2d {
 
-constexpr int kMaxLanes = 256;   // per-lane sums are staged in shared memory
 
 // Per-lane sums of a block staged in shared memory, flushed with one atomic
 // per (lane, value) at the end of the block.
@@ -73,11 +74,6 @@ __device__ __forceinline__ float source_normal(unsigned& s) {
     return r * cosf(th);
 }
 
-struct BeamArgs {
-    float x0, z0, theta0, E0, W, sx, sth, sE;
-    int n;
-    unsigned seed;
-};
 __device__ __forceinline__ bool beam_gaussian(const BeamArgs& b) {   // gpu_transport_wrapper.cu:246
     return b.n > 1 || b.sx > 0.0f || b.sth > 0.0f;
 }
@@ -150,72 +146,79 @@ __device__ bool inject_sample(const Dev& d, const BeamArgs& b, float x_min, floa
 
 // Opens an injection into the lanes whose beam has samples: one claim pass.
 // check_empty (single-lane engines) refuses an injection into an occupied
-// phase space: every sample is then booked as a source slot drop.
+// phase space: every sample is then booked as a source slot drop.  The
+// injected cells are appended to psi_in's occupancy list from occ_mark on.
 __global__ void k_inject_begin(Dev d, int check_empty) {
     if (threadIdx.x || blockIdx.x) return;
     d.gs->ctag += 1u;
+    d.gs->occ_mark = d.gs->occ_n[d.gs->parity];
     d.ls[0].inj_skip = (check_empty && d.gs->occ_n[d.gs->parity] != 0) ? 1 : 0;
 }
 
 // Claim pass of the injection: each in-grid sample offers its block to its
 // cell with its sample index as claim key (the reference's source kernels
-// claim in sample order when run one sample at a time).  Thread per
-// (lane, sample).
+// claim in sample order when run one sample at a time).  Blocks (x, lane),
+// grid-stride over the lane's samples; with refill_only, only the lanes a
+// plan refills.
 template <class Lay>
-__global__ void k_inject_keys(Dev d, const BeamArgs* beams, int max_n, float x_min, float z_min) {
+__global__ void k_inject_keys(Dev d, const BeamArgs* beams, float x_min, float z_min, int refill_only) {
     const int lane = blockIdx.y;
+    if ((refill_only && !d.ls[lane].refill) || d.ls[lane].inj_skip) return;
     const BeamArgs b = beams[lane];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= min(beam_samples(b), max_n) || d.ls[lane].inj_skip) return;
-    InjSample o;
-    if (!inject_sample<Lay>(d, b, x_min, z_min, i, o) || !(o.w > 0.0f)) return;
-    const int gc = lane * d.Nc + o.cell;
-    cand_insert(psi_row(d, gc), d.ccount + gc, d.gs->ctag, o.want, (uint32_t)i, &d.gs->cand_ovf);
-    mark_occupied(d, d.gs->parity, gc);
+    const int ns = beam_samples(b);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        InjSample o;
+        if (!inject_sample<Lay>(d, b, x_min, z_min, i, o) || !(o.w > 0.0f)) continue;
+        const int gc = lane * d.Nc + o.cell;
+        cand_insert(psi_row(d, gc), d.ccount + gc, d.gs->ctag, o.want, (uint32_t)i, &d.gs->cand_ovf);
+        mark_occupied(d, d.gs->parity, gc);
+    }
 }
 
 // Deposit pass of the injection: a sample whose block kept a slot adds its
 // weight there; the others are source slot drops (the reference's claim
 // without fallback).  The pencil books W and E0 W in k_source_finalize.
 template <class Lay>
-__global__ void k_inject_deposit(Dev d, const BeamArgs* beams, int max_n, float x_min, float z_min) {
+__global__ void k_inject_deposit(Dev d, const BeamArgs* beams, float x_min, float z_min, int refill_only) {
     const int lane = blockIdx.y;
-    const BeamArgs b = beams[lane];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= min(beam_samples(b), max_n)) return;
     LaneState& L = d.ls[lane];
-    InjSample o;
-    const bool in = inject_sample<Lay>(d, b, x_min, z_min, i, o);
-    const int gc = lane * d.Nc + o.cell;
-    int s = -1;
-    if (in && !L.inj_skip && o.w > 0.0f) {
-        s = cand_find(psi_row(d, gc), d.gs->ctag, o.want);
-        if (s >= 0 && d.bid[(size_t)gc * kKb + s] != o.want) s = -1;
-    }
-    if (s >= 0) atomicAdd(d.val + ((size_t)gc * kKb + s) * Lay::L + o.l, o.w);
-    if (!beam_gaussian(b)) return;
-    if (!in) {
-        atomicAdd(&L.src_oog_w, o.w);
-        atomicAdd(&L.src_oog_e, (double)(o.E * o.w));
-    } else if (s >= 0) {
-        atomicAdd(&L.src_inj_w, o.w);
-        atomicAdd(&L.src_inj_e, (double)(o.E * o.w));
-    } else {
-        atomicAdd(&L.src_slot_w, o.w);
-        atomicAdd(&L.src_slot_e, (double)(o.E * o.w));
+    if (refill_only && !L.refill) return;
+    const BeamArgs b = beams[lane];
+    const int ns = beam_samples(b);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        InjSample o;
+        const bool in = inject_sample<Lay>(d, b, x_min, z_min, i, o);
+        const int gc = lane * d.Nc + o.cell;
+        int s = -1;
+        if (in && !L.inj_skip && o.w > 0.0f) {
+            s = cand_find(psi_row(d, gc), d.gs->ctag, o.want);
+            if (s >= 0 && d.bid[(size_t)gc * kKb + s] != o.want) s = -1;
+        }
+        if (s >= 0) atomicAdd(d.val + ((size_t)gc * kKb + s) * Lay::L + o.l, o.w);
+        if (!beam_gaussian(b)) continue;
+        if (!in) {
+            atomicAdd(&L.src_oog_w, o.w);
+            atomicAdd(&L.src_oog_e, (double)(o.E * o.w));
+        } else if (s >= 0) {
+            atomicAdd(&L.src_inj_w, o.w);
+            atomicAdd(&L.src_inj_e, (double)(o.E * o.w));
+        } else {
+            atomicAdd(&L.src_slot_w, o.w);
+            atomicAdd(&L.src_slot_e, (double)(o.E * o.w));
+        }
     }
 }
 
-// Weight and bin-centre energy of the w > 0 bins on occupancy list `which`
-// relative to psi_in (compute_psic_total_weight_energy,
-// k1k6_pipeline.cu:706-768), per lane; warp per occupied cell.
+// Weight and bin-centre energy of the w > 0 bins of the cells the last
+// injection put on psi_in's occupancy list (compute_psic_total_weight_energy,
+// k1k6_pipeline.cu:706-768), per lane; warp per cell.
 template <class Lay>
-__global__ void __launch_bounds__(kThreads) k_totals(Dev d, int which) {
-    const int k = d.gs->parity ^ which;
+__global__ void __launch_bounds__(kThreads) k_totals(Dev d) {
+    const int k = d.gs->parity;
     const int n = d.gs->occ_n[k];
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
+    for (int wi = d.gs->occ_mark + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); wi < n; wi += nw) {
         const int gc = d.occ_list[k][wi];
         const uint32_t b = d.bid[(size_t)gc * kKb + lane];
         unsigned used = __ballot_sync(kFull, b != kEmpty);
@@ -246,11 +249,13 @@ __global__ void __launch_bounds__(kThreads) k_totals(Dev d, int which) {
 
 // Source accounting after an injection (gpu_transport_wrapper.cu:339-460):
 // the pencil books W and E0 W; the represented energy comes from k_totals.
-// Thread per lane.
-__global__ void k_source_finalize(Dev d, const BeamArgs* beams) {
+// Thread per lane (the refilled lanes only, with refill_only).
+__global__ void k_source_finalize(Dev d, const BeamArgs* beams, int refill_only) {
     const int lane = blockIdx.x * blockDim.x + threadIdx.x;
     if (lane >= d.B) return;
     LaneState& L = d.ls[lane];
+    if (refill_only && !L.refill) return;
+    L.refill = 0;
     const BeamArgs b = beams[lane];
     if (!beam_gaussian(b)) {
         L.src_inj_w = b.W;
@@ -293,9 +298,11 @@ __device__ __forceinline__ void block_add(const double (&v)[N], double* dst) {
 // cell is then cleared, so that the storage can receive psi_out.  A lane
 // whose stopping rule was met consumes its cells without transport.  The
 // last block publishes the counts, settles each lane, resets the per-lane
-// accumulators and sets the device loop condition.
+// accumulators and sets the device loop condition; in a spot plan it also
+// lists the lanes whose spot just finished and sets the refill condition.
 template <class Lay>
-__global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphConditionalHandle cond, int use_cond) {
+__global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphConditionalHandle cond,
+                                                       cudaGraphConditionalHandle rcond, int use_cond) {
     constexpr int Q = Lay::L / 4, NW = kThreads / 32, U = 8;
     __shared__ int s_cnt[kMaxLanes][3];   // listed active, listed coarse, their slots
     __shared__ int s_last;
@@ -304,7 +311,10 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     if (gs->pass >= gs->max_pass) {   // paused: leave the phase space as it is
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             gs->halt = 1;
-            if (use_cond) cudaGraphSetConditional(cond, 0u);
+            if (use_cond) {
+                cudaGraphSetConditional(cond, 0u);
+                cudaGraphSetConditional(rcond, 0u);
+            }
         }
         return;
     }
@@ -434,11 +444,14 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     __threadfence();
     // settle each lane: counts, C1 stopping rule, accumulators
     __shared__ int s_work;
+    __shared__ uint8_t s_fin[kMaxLanes];
+    const bool plan = gs->plan_n > 0;
     if (threadIdx.x == 0) s_work = 0;
     __syncthreads();
     for (int ln = threadIdx.x; ln < d.B; ln += blockDim.x) {
         LaneState& L = d.ls[ln];
         volatile LaneState* v = &L;
+        const bool was_running = v->done == 0;
         const int na = v->acc_active, nc = v->acc_coarse, nsl = v->acc_slots;
         L.acc_active = L.acc_coarse = L.acc_slots = 0;
         if (L.light) {
@@ -454,6 +467,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         const bool work = (na + nc) > 0;
         L.done = work ? 0 : 1;
         L.work = work ? 1 : 0;
+        s_fin[ln] = (plan && was_running && !work) ? 1 : 0;
         double* acc = &L.drop_w;   // the 14 per-iteration accumulators
         for (int k = 0; k < 14; ++k) acc[k] = 0.0;
         if (work) {
@@ -469,15 +483,23 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     gs->acc_listed = gs->acc_items = gs->acc_bins = 0;
     gs->gen = g;
     gs->ctag += 1u;   // claim pass of this iteration
+    int nf = 0;
+    for (int ln = 0; ln < d.B; ++ln)
+        if (s_fin[ln]) gs->fin[nf++] = ln;
+    gs->n_fin = nf;
     // a cell or bin list that outgrew its capacity ends the run (reported by
-    // the host API as SM2D_ERR_ALLOC)
-    const bool halt = s_work == 0 || v->bin_ovf != 0;
+    // the host API as SM2D_ERR_ALLOC); a plan runs on while a spot finished
+    // (its lane is refilled at the end of this pass)
+    const bool halt = (s_work == 0 && nf == 0) || v->bin_ovf != 0;
     gs->halt = halt ? 1 : 0;
     gs->n_listed = halt ? 0 : min(nl, d.listed_cap);
     gs->n_items = halt ? 0 : ni;
     gs->n_bins = halt ? 0 : nb;
     gs->blocks_done = 0;
-    if (use_cond) cudaGraphSetConditional(cond, (!halt && gs->pass + 1 < gs->max_pass) ? 1u : 0u);
+    if (use_cond) {
+        cudaGraphSetConditional(cond, (!halt && gs->pass + 1 < gs->max_pass) ? 1u : 0u);
+        cudaGraphSetConditional(rcond, (!halt && nf > 0) ? 1u : 0u);
+    }
 }
 
 // Ascending active and coarse lists of lane 0 from the classes of this pass
@@ -697,9 +719,9 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
     }
 }
 
-// Occupied cells of psi_out (which = 1, a transport pass) or of psi_in
-// (which = 0, an injection), warp per cell: select the kept ids into the
-// cell's slot ids.
+// Occupied cells of psi_out (which = 1, a transport pass) or the cells an
+// injection put on psi_in's list (which = 0), warp per cell: select the kept
+// ids into the cell's slot ids.
 __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
     constexpr int NW = kThreads / 32;
     __shared__ SelScratch s_sel[NW];
@@ -712,7 +734,7 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     s_sum.zero(d.B);
     __syncthreads();
-    for (int wi = blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
+    for (int wi = (which ? 0 : gs->occ_mark) + blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
         const int gc = d.occ_list[k][wi];
         const int nk = select_row(psi_row(d, gc), d.ccount + gc, tag, s_sel[wid], d.bid + (size_t)gc * kKb, lane);
         if (which && lane == 0) atomicAdd(&s_sum.v[lane_of(d, gc)][0], (double)nk);
@@ -850,6 +872,12 @@ __device__ void finalize_lane(const Dev& d, int ln) {
     // C1 stopping rule, applied by the next classification: in-flight
     // weight below a fraction of the injected weight
     L.light = (d.stop_frac > 0.0f && r.W_out_total < d.stop_frac * L.src_inj_w) ? 1 : 0;
+    // a plan's spot at its iteration limit ends the same way, unfinished
+    // (the terminal residual of k1k6_pipeline.cu:1677-1706)
+    if (!L.light && d.gs->plan_n > 0 && k + 1 >= d.gs->lane_max_it) {
+        L.light = 1;
+        L.stopped = 1;
+    }
 }
 
 // Fold this iteration's increment of tally k of cell c into the cumulative
@@ -974,6 +1002,7 @@ __global__ void k_reset_state(Dev d) {
     for (int ln = 0; ln < d.B; ++ln) {
         memset(&d.ls[ln], 0, sizeof(LaneState));
         d.ls[ln].done = 1;
+        d.ls[ln].spot = -1;
     }
 }
 
@@ -991,30 +1020,37 @@ __global__ void k_set_pass_limit(IterGlobal* gs, int more) {
     gs->max_pass = lim > INT_MAX ? INT_MAX : (int)lim;
 }
 
-// Lateral post-convolution kernels of every lane from its sigma_total(z)
-// and initial sigma_x (the kernel of gpu_transport_wrapper.cu:551-616):
-// a Gaussian of sigma^2 = sigma_total^2 - sigma_x0^2 over +-ceil(3 sigma/dx)
-// cells (at most Nx/2), normalised; thread per (lane, row).
+// Lateral post-convolution kernel of one depth row (the kernel of
+// gpu_transport_wrapper.cu:551-616): a Gaussian of sigma^2 = sigma_total^2 -
+// sigma_x0^2, in cells, over +-ceil(3 sigma) cells (at most Nx/2),
+// normalised.  Half width 0 leaves the row as it is.
+__device__ __forceinline__ int lateral_half(float st, float s0, float dx, int Nx, double* sc) {
+    const float msq = st * st - s0 * s0;
+    if (msq <= 1e-6f) return 0;
+    const float c = sqrtf(msq) / dx;
+    *sc = (double)c;
+    const int h = (int)ceilf(3.0f * c);
+    return max(1, min(h, Nx / 2));
+}
+__device__ __forceinline__ double lateral_tap(int j, double sc) { return exp(-0.5 * ((double)j * j) / (sc * sc)); }
+
+// The row kernels of every lane from its sigma_total(z) and initial sigma_x;
+// thread per (lane, row).
 __global__ void k_dose_tables(const float* __restrict__ feS, const float* __restrict__ sx0, float dx, int Nx, int Nz,
                               int B, int stride, int* __restrict__ half, double* __restrict__ ker) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= B * Nz) return;
-    const int ln = i / Nz;
-    const float st = feS[i], s0 = sx0[ln];
-    const float msq = st * st - s0 * s0;
+    double sc = 0.0;
+    const int h = lateral_half(feS[i], sx0[i / Nz], dx, Nx, &sc);
+    half[i] = h;
+    if (h == 0) return;
     double* k = ker + (size_t)i * stride;
-    if (msq <= 1e-6f) { half[i] = 0; return; }
-    const float sc = sqrtf(msq) / dx;
-    int h = (int)ceilf(3.0f * sc);
-    h = max(1, min(h, Nx / 2));
     double sum = 0.0;
     for (int j = -h; j <= h; ++j) {
-        const double v = exp(-0.5 * ((double)j * j) / ((double)sc * sc));
-        k[j + h] = v;
-        sum += v;
+        k[j + h] = lateral_tap(j, sc);
+        sum += k[j + h];
     }
     for (int j = 0; j <= 2 * h; ++j) k[j] /= sum;
-    half[i] = h;
 }
 
 // Lateral MCS post-convolution of EdepC, one thread per output cell of each
@@ -1039,6 +1075,146 @@ __global__ void k_dose(const double* __restrict__ edep, const int* __restrict__ 
     out[i] = acc;
 }
 
+// ------------------------------------------------------------------ spot plan
+// Outcome of a lane's spot (sm2d_spot_result).
+__host__ __device__ inline void lane_result(const LaneState& L, sm2d_spot_result& r) {
+    r.iterations = L.iter;
+    r.finished = (L.done && !L.stopped) ? 1 : 0;
+    r.weight_audit_failures = L.w_fail;
+    r.energy_audit_failures = L.e_fail;
+    r.injected_weight = L.src_inj_w;
+    r.injected_energy = L.src_inj_e;
+    r.source_out_of_grid_weight = L.src_oog_w;
+    r.source_slot_dropped_weight = L.src_slot_w;
+    r.transport_dropped_weight = L.transport_drop_w;
+    r.transport_dropped_energy = L.transport_drop_e;
+    r.audit_residual_energy = L.audit_residual;
+    r.representation_loss_energy = L.src_rep_loss;
+    r.cell_steps = L.cell_steps;
+    r.slots_in = L.slots_in;
+    r.slots_out = L.slots_out;
+    r.last = L.last;
+}
+
+// Opens a plan of n spots, each limited to max_it iterations.
+__global__ void k_plan_begin(Dev d, const BeamArgs* beams, const float* fe, double* dose, sm2d_spot_result* res, int n,
+                             int max_it) {
+    if (threadIdx.x || blockIdx.x) return;
+    IterGlobal* gs = d.gs;
+    gs->plan_n = n;
+    gs->plan_next = 0;
+    gs->lane_max_it = max_it;
+    gs->refills = 0;
+    gs->n_fin = 0;
+    gs->plan_beams = beams;
+    gs->plan_fe = fe;
+    gs->plan_dose = dose;
+    gs->plan_res = res;
+    gs->max_pass = INT_MAX;
+}
+__global__ void k_plan_end(Dev d) {
+    if (threadIdx.x || blockIdx.x) return;
+    d.gs->plan_n = 0;
+}
+
+// Each lane whose spot finished at this classification: the lateral
+// post-convolution of its dose into the plan's dose map of the spot, with
+// the kernel k_dose_tables builds, then its tallies cleared for the next
+// spot.  Block per (depth row, finished lane).
+__global__ void __launch_bounds__(128) k_lane_complete(Dev d) {
+    extern __shared__ double s_k[];
+    __shared__ double s_sum;
+    const IterGlobal* gs = d.gs;
+    if ((int)blockIdx.y >= gs->n_fin) return;
+    const int ln = gs->fin[blockIdx.y];
+    const int iz = blockIdx.x;
+    const size_t row = (size_t)ln * d.Nc + (size_t)iz * d.Nx;
+    const int spot = d.ls[ln].spot;
+    double* out = gs->plan_dose;
+    if (out && spot >= 0) {
+        double sc = 0.0;
+        const int h = lateral_half(d.feS[(size_t)ln * d.Nz + iz], d.sx0[ln], d.dx, d.Nx, &sc);
+        double* dst = out + (size_t)spot * d.Nc + (size_t)iz * d.Nx;
+        if (h == 0) {
+            for (int ix = threadIdx.x; ix < d.Nx; ix += blockDim.x) dst[ix] = d.edep[row + ix];
+        } else {
+            for (int j = threadIdx.x; j <= 2 * h; j += blockDim.x) s_k[j] = lateral_tap(j - h, sc);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double sum = 0.0;
+                for (int j = 0; j <= 2 * h; ++j) sum += s_k[j];
+                s_sum = sum;
+            }
+            __syncthreads();
+            for (int j = threadIdx.x; j <= 2 * h; j += blockDim.x) s_k[j] /= s_sum;
+            __syncthreads();
+            for (int ix = threadIdx.x; ix < d.Nx; ix += blockDim.x) {
+                double acc = 0.0;
+                for (int j = -h; j <= h; ++j) {
+                    const int x = ix + j;
+                    if (x >= 0 && x < d.Nx) acc += d.edep[row + x] * s_k[j + h];
+                }
+                dst[ix] = acc;
+            }
+        }
+    }
+    __syncthreads();
+    for (int ix = threadIdx.x; ix < d.Nx; ix += blockDim.x) {
+        d.edep[row + ix] = 0.0; d.e_cut[row + ix] = 0.0; d.e_nuc[row + ix] = 0.0; d.e_bnd[row + ix] = 0.0;
+        d.w_cut[row + ix] = 0.0f; d.w_nuc[row + ix] = 0.0f; d.w_bnd[row + ix] = 0.0f;
+    }
+}
+
+// Results of the finished spots, then the plan's next spots into the idle
+// lanes in lane order: lane state cleared, beam and Fermi-Eyges tables of
+// the spot, refill flag for the injection kernels that follow.  One block.
+__global__ void __launch_bounds__(256) k_lane_assign(Dev d, BeamArgs* beams) {
+    __shared__ int s_lane[kMaxLanes], s_spot[kMaxLanes];
+    __shared__ int s_n;
+    IterGlobal* gs = d.gs;
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < gs->n_fin; ++j) {
+            LaneState& L = d.ls[gs->fin[j]];
+            if (L.spot >= 0 && gs->plan_res) lane_result(L, gs->plan_res[L.spot]);
+            L.spot = -1;
+        }
+        gs->n_fin = 0;
+        int n = 0;
+        for (int ln = 0; ln < d.B && gs->plan_next < gs->plan_n; ++ln)
+            if (d.ls[ln].done && d.ls[ln].spot < 0) {
+                s_lane[n] = ln;
+                s_spot[n] = gs->plan_next++;
+                ++n;
+            }
+        s_n = n;
+        gs->refills += 1;
+    }
+    __syncthreads();
+    const int Nz = d.Nz;
+    for (int k = 0; k < s_n; ++k) {
+        const int ln = s_lane[k], sp = s_spot[k];
+        int* w = reinterpret_cast<int*>(d.ls + ln);
+        for (int i = threadIdx.x; i < (int)(sizeof(LaneState) / 4); i += blockDim.x) w[i] = 0;
+        const float* fe = gs->plan_fe + (size_t)sp * (3 * Nz + 1);
+        for (int i = threadIdx.x; i < Nz; i += blockDim.x) {
+            d.feA[(size_t)ln * Nz + i] = fe[i];
+            d.feB[(size_t)ln * Nz + i] = fe[Nz + i];
+            d.feS[(size_t)ln * Nz + i] = fe[2 * Nz + i];
+        }
+        if (threadIdx.x == 0) {
+            d.sx0[ln] = fe[3 * Nz];
+            beams[ln] = gs->plan_beams[sp];
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < s_n; k += blockDim.x) {
+        LaneState& L = d.ls[s_lane[k]];
+        L.spot = s_spot[k];
+        L.refill = 1;
+        L.done = 1;
+    }
+}
+
 // ================================================================== engine
 struct Ctx {
     sm2d_problem p{};
@@ -1057,7 +1233,8 @@ struct Ctx {
     std::vector<void*> allocs;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaGraphConditionalHandle cond{};
+    cudaGraphConditionalHandle cond{};    // device loop: another pass
+    cudaGraphConditionalHandle rcond{};   // spot plan: refill after this pass
     cudaEvent_t ev[10] = {};   // 0..7 one iteration's stages, 8..9 a whole run
     float step_ms[7] = {};
     int grid_cell = 0, grid_transport = 0, grid_keys = 0;   // warp-per-cell kernels, deposit pass, claim pass
@@ -1071,6 +1248,18 @@ struct Ctx {
     double* dose_dev = nullptr;     // convolved dose [B][Nc]
     int dose_stride = 1;            // 2 (Nx/2) + 1: the widest kernel
     std::vector<cudaEvent_t> pev;   // event pool of the profiled replay
+    // spot plan: device copies of the plan's beams, Fermi-Eyges tables,
+    // results and dose maps (grown on demand), and their host staging
+    int plan_n = 0, plan_max_it = 0;
+    bool plan_dose_on = false;
+    int plan_max_n = 1024;          // sizes the injection grid of a refill
+    size_t plan_cap = 0, plan_dose_cap = 0;
+    BeamArgs* plan_beams_dev = nullptr;
+    float* plan_fe_dev = nullptr;
+    sm2d_spot_result* plan_res_dev = nullptr;
+    double* plan_dose_dev = nullptr;
+    std::vector<BeamArgs> plan_beams_host;
+    std::vector<float> plan_fe_host;
 };
 
 static int dalloc(Ctx& c, void** p, size_t bytes) {
@@ -1100,7 +1289,7 @@ struct Impl {
         const bool bk = c.p.use_buckets != 0;
         auto rec = [&](int k) { return timed ? cudaEventRecord(c.ev[k], c.s) : cudaSuccess; };
         CK(rec(0));
-        k_classify<Lay><<<gc, kThreads, 0, c.s>>>(c.d, c.cond, use_cond ? 1 : 0);
+        k_classify<Lay><<<gc, kThreads, 0, c.s>>>(c.d, c.cond, c.rcond, use_cond ? 1 : 0);
         CK(rec(1));
         if (lists) k_order_lists<<<1, 1024, 0, c.s>>>(c.d);
         CK(rec(2));
@@ -1141,18 +1330,31 @@ struct Impl {
         CK(cudaGetLastError());
         return 0;
     }
-    // injection of the beams in beams_dev (one per lane, max_n samples at
-    // most): claim pass, slot selection, deposit pass, source accounting
-    static int inject(Ctx& c, int max_n, bool check_empty) {
-        const dim3 grid((unsigned)((std::max(max_n, 1) + 255) / 256), (unsigned)c.B);
+    // injection of the beams in beams_dev (one per lane; the kernels stride
+    // over a lane's samples, max_n sizes the grid): claim pass, slot
+    // selection, deposit pass, source accounting.  refill_only: the lanes
+    // a plan refills.
+    static int inject(Ctx& c, int max_n, bool check_empty, bool refill_only) {
+        const int gx = std::min((std::max(max_n, 1) + 255) / 256, 16);
+        const dim3 grid((unsigned)gx, (unsigned)c.B);
+        const int ro = refill_only ? 1 : 0;
         k_inject_begin<<<1, 1, 0, c.s>>>(c.d, check_empty ? 1 : 0);
-        k_inject_keys<Lay><<<grid, 256, 0, c.s>>>(c.d, c.beams_dev, max_n, c.p.x_min, c.p.z_min);
+        k_inject_keys<Lay><<<grid, 256, 0, c.s>>>(c.d, c.beams_dev, c.p.x_min, c.p.z_min, ro);
         k_select_psi<<<c.grid_cell, kThreads, 0, c.s>>>(c.d, 0);
-        k_inject_deposit<Lay><<<grid, 256, 0, c.s>>>(c.d, c.beams_dev, max_n, c.p.x_min, c.p.z_min);
-        k_totals<Lay><<<c.grid_cell, kThreads, 0, c.s>>>(c.d, 0);
-        k_source_finalize<<<(c.B + 255) / 256, 256, 0, c.s>>>(c.d, c.beams_dev);
+        k_inject_deposit<Lay><<<grid, 256, 0, c.s>>>(c.d, c.beams_dev, c.p.x_min, c.p.z_min, ro);
+        k_totals<Lay><<<c.grid_cell, kThreads, 0, c.s>>>(c.d);
+        k_source_finalize<<<(c.B + 255) / 256, 256, 0, c.s>>>(c.d, c.beams_dev, ro);
         CK(cudaGetLastError());
         return 0;
+    }
+    // refill of a spot plan: finished lanes' dose and results, next spots
+    // into the idle lanes, their injection
+    static int refill(Ctx& c, int) {
+        const size_t smem = sizeof(double) * (size_t)c.dose_stride;
+        k_lane_complete<<<dim3((unsigned)c.d.Nz, (unsigned)c.B), 128, smem, c.s>>>(c.d);
+        k_lane_assign<<<1, 256, 0, c.s>>>(c.d, c.beams_dev);
+        CK(cudaGetLastError());
+        return inject(c, c.plan_max_n, false, true);
     }
 };
 
@@ -1182,12 +1384,36 @@ static int build_graph(Ctx& c) {
     cudaGraphNode_t node;
     CK(cudaGraphAddNode(&node, c.graph, nullptr, nullptr, 0, &np));
     cudaGraph_t body = np.conditional.phGraph_out[0];
+    CK(cudaGraphConditionalHandleCreate(&c.rcond, body, 0, 0));
     CK(cudaStreamBeginCaptureToGraph(c.s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int rc = DISPATCH(c, launch_body, false, true, false);
     cudaGraph_t captured = nullptr;
     cudaError_t e = cudaStreamEndCapture(c.s, &captured);
     if (rc) return rc;
     if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    // the refill of a spot plan: an if-node after the pass's last kernel
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(body, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn), sinks;
+    CK(cudaGraphGetNodes(body, nodes.data(), &nn));
+    for (cudaGraphNode_t n : nodes) {
+        size_t nd = 0;
+        CK(cudaGraphNodeGetDependentNodes(n, nullptr, nullptr, &nd));
+        if (nd == 0) sinks.push_back(n);
+    }
+    cudaGraphNodeParams ip{};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = c.rcond;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    cudaGraphNode_t ifn;
+    CK(cudaGraphAddNode(&ifn, body, sinks.data(), nullptr, sinks.size(), &ip));
+    cudaGraph_t rbody = ip.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(c.s, rbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    rc = DISPATCH(c, refill, 0);
+    e = cudaStreamEndCapture(c.s, &captured);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "refill capture: %s", cudaGetErrorString(e));
     CK(cudaGraphInstantiate(&c.exec, c.graph, 0));
     return 0;
 }
@@ -1401,6 +1627,10 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     // lateral post-convolution kernels per lane and depth row: half widths
     // are at most Nx/2
     c->dose_stride = 2 * std::max(1, p->Nx / 2) + 1;
+    if (sizeof(double) * c->dose_stride > 48 * 1024 &&
+        cudaFuncSetAttribute(k_lane_complete, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(double) * c->dose_stride)) != cudaSuccess)
+        return bail(fail(SM2D_ERR_ARG, "Nx too large for the dose kernel"));
     A(c->dose_half, int, BN);
     A(c->dose_ker, double, BN * c->dose_stride);
     A(c->dose_dev, double, NcB);
@@ -1476,6 +1706,8 @@ int sm2d_destroy(sm2d_handle h) {
     if (h->gs_host) cudaFreeHost(h->gs_host);
     if (h->ls_host) cudaFreeHost(h->ls_host);
     if (h->beams_host) cudaFreeHost(h->beams_host);
+    for (void* p : {(void*)h->plan_beams_dev, (void*)h->plan_fe_dev, (void*)h->plan_res_dev, (void*)h->plan_dose_dev})
+        if (p) cudaFree(p);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
     return 0;
@@ -1494,7 +1726,7 @@ int sm2d_inject_async(sm2d_handle h, const sm2d_beam* b) {
     if (rc) return rc;
     set_lane_fe(c, 0, c.p.E0, c.p.sigma_x_initial);   // a single spot keeps the problem's tables
     if ((rc = upload_lane_fe(c))) return rc;
-    if ((rc = DISPATCH(c, inject, max_n, true))) return rc;
+    if ((rc = DISPATCH(c, inject, max_n, true, false))) return rc;
     c.injected = true;
     return 0;
 }
@@ -1785,24 +2017,6 @@ int sm2d_get_step_timing(sm2d_handle h, float* ms7) {
 }
 
 // ---------------------------------------------------------------- batched spots
-static void fill_result(const LaneState& L, sm2d_spot_result& r) {
-    r.iterations = L.iter;
-    r.finished = L.done;
-    r.weight_audit_failures = L.w_fail;
-    r.energy_audit_failures = L.e_fail;
-    r.injected_weight = L.src_inj_w;
-    r.injected_energy = L.src_inj_e;
-    r.source_out_of_grid_weight = L.src_oog_w;
-    r.source_slot_dropped_weight = L.src_slot_w;
-    r.transport_dropped_weight = L.transport_drop_w;
-    r.transport_dropped_energy = L.transport_drop_e;
-    r.audit_residual_energy = L.audit_residual;
-    r.representation_loss_energy = L.src_rep_loss;
-    r.cell_steps = L.cell_steps;
-    r.slots_in = L.slots_in;
-    r.slots_out = L.slots_out;
-    r.last = L.last;
-}
 
 static int check_beams(const sm2d_beam* beams, int n) {
     for (int i = 0; i < n; ++i)
@@ -1822,7 +2036,7 @@ int sm2d_batch_inject(sm2d_handle h, const sm2d_beam* beams, int n) {
     if ((rc = stage_beams(c, beams, n, &max_n))) return rc;
     for (int ln = 0; ln < n; ++ln) set_lane_fe(c, ln, beams[ln].E0, beams[ln].sigma_x);
     if ((rc = upload_lane_fe(c))) return rc;
-    if ((rc = DISPATCH(c, inject, max_n, false))) return rc;
+    if ((rc = DISPATCH(c, inject, max_n, false, false))) return rc;
     c.injected = true;
     return 0;
 }
@@ -1831,7 +2045,7 @@ int sm2d_batch_results(sm2d_handle h, sm2d_spot_result* results, int n) {
     if (!h || !results || n < 0 || n > h->B) return fail(SM2D_ERR_ARG, "invalid argument");
     int rc = sync_state(*h);
     if (rc) return rc;
-    for (int i = 0; i < n; ++i) fill_result(h->ls_host[i], results[i]);
+    for (int i = 0; i < n; ++i) lane_result(h->ls_host[i], results[i]);
     return 0;
 }
 
@@ -1844,34 +2058,130 @@ int sm2d_batch_dose(sm2d_handle h, double* dose, int n) {
     return 0;
 }
 
-int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, double* dose,
-                   sm2d_spot_result* results) {
-    if (!h || (!beams && n_spots > 0) || n_spots < 0 || max_iterations <= 0) return fail(SM2D_ERR_ARG, "invalid argument");
+// ---------------------------------------------------------------- spot plan
+int sm2d_plan_load(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, int with_dose) {
+    if (!h || (!beams && n_spots > 0) || n_spots < 0 || max_iterations <= 0)
+        return fail(SM2D_ERR_ARG, "invalid argument");
     Ctx& c = *h;
     int rc = check_beams(beams, n_spots);
     if (rc) return rc;
     if ((rc = build_graph(c))) return rc;
-    const size_t nc = (size_t)c.d.Nc;
-    for (int w0 = 0; w0 < n_spots; w0 += c.B) {
-        const int nw = std::min(c.B, n_spots - w0);
-        if ((rc = sm2d_batch_inject(h, beams + w0, nw))) return rc;
-        k_set_pass_limit<<<1, 1, 0, c.s>>>(c.d.gs, max_iterations);
-        CK(cudaGetLastError());
-        CK(cudaGraphLaunch(c.exec, c.s));
-        if (dose) {
-            if ((rc = enqueue_dose(c))) return rc;
-            CK(cudaMemcpyAsync(dose + (size_t)w0 * nc, c.dose_dev, sizeof(double) * nc * nw, cudaMemcpyDeviceToHost,
-                               c.s));
+    const int Nz = c.d.Nz;
+    const size_t per = 3 * (size_t)Nz + 1, n = (size_t)n_spots;
+    // grow the device plan buffers (after the previous plan's work)
+    if (n > c.plan_cap || (with_dose && n > c.plan_dose_cap)) {
+        CK(cudaStreamSynchronize(c.s));
+        auto grow = [&](void** p, size_t bytes) -> int {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+            cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+            return e == cudaSuccess ? 0 : fail(SM2D_ERR_ALLOC, "plan buffers (%zu bytes): %s", bytes, cudaGetErrorString(e));
+        };
+        if (n > c.plan_cap) {
+            c.plan_cap = 0;
+            if ((rc = grow((void**)&c.plan_beams_dev, sizeof(BeamArgs) * n)) ||
+                (rc = grow((void**)&c.plan_fe_dev, sizeof(float) * per * n)) ||
+                (rc = grow((void**)&c.plan_res_dev, sizeof(sm2d_spot_result) * n)))
+                return rc;
+            c.plan_cap = n;
         }
-        if (results) {
-            if ((rc = sync_state(c))) return rc;
-            for (int i = 0; i < nw; ++i) fill_result(c.ls_host[i], results[w0 + i]);
-            if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
+        if (with_dose && n > c.plan_dose_cap) {
+            c.plan_dose_cap = 0;
+            if ((rc = grow((void**)&c.plan_dose_dev, sizeof(double) * (size_t)c.d.Nc * n))) return rc;
+            c.plan_dose_cap = n;
         }
     }
-    if ((rc = sync_state(c))) return rc;
+    c.plan_beams_host.resize(n);
+    for (size_t i = 0; i < n; ++i) c.plan_beams_host[i] = beam_args(beams[i]);
+    // Fermi-Eyges tables per distinct (E0, sigma_x), on the host threads
+    c.plan_fe_host.resize(per * n);
+    std::unordered_map<unsigned long long, int> first;
+    std::vector<int> src(n), uniq;
+    for (size_t i = 0; i < n; ++i) {
+        unsigned eb, sb;
+        memcpy(&eb, &beams[i].E0, 4);
+        memcpy(&sb, &beams[i].sigma_x, 4);
+        auto ins = first.emplace(((unsigned long long)eb << 32) | sb, (int)i);
+        src[i] = ins.first->second;
+        if (ins.second) uniq.push_back((int)i);
+    }
+    auto fe_of = [&](int t, int T) {
+        for (size_t k = t; k < uniq.size(); k += T) {
+            const int i = uniq[k];
+            float* f = c.plan_fe_host.data() + per * i;
+            fermi_eyges_moments(beams[i].E0, Nz, c.d.dz, beams[i].sigma_x, f, f + Nz, f + 2 * Nz);
+            f[3 * Nz] = beams[i].sigma_x;
+        }
+    };
+    const int T = (int)std::min<size_t>({(size_t)std::max(1u, std::thread::hardware_concurrency()), 16, uniq.size() / 16 + 1});
+    if (T <= 1) fe_of(0, 1);
+    else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < T; ++t) pool.emplace_back(fe_of, t, T);
+        for (auto& th : pool) th.join();
+    }
+    for (size_t i = 0; i < n; ++i)
+        if (src[i] != (int)i) std::copy_n(c.plan_fe_host.data() + per * src[i], per, c.plan_fe_host.data() + per * i);
+    // pageable sources: each copy has read its source when it returns
+    if (n) {
+        CK(cudaMemcpyAsync(c.plan_beams_dev, c.plan_beams_host.data(), sizeof(BeamArgs) * n, cudaMemcpyHostToDevice, c.s));
+        CK(cudaMemcpyAsync(c.plan_fe_dev, c.plan_fe_host.data(), sizeof(float) * per * n, cudaMemcpyHostToDevice, c.s));
+    }
+    c.plan_n = n_spots;
+    c.plan_max_it = max_iterations;
+    c.plan_dose_on = with_dose != 0;
+    return 0;
+}
+
+int sm2d_plan_run_async(sm2d_handle h) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    if (c.plan_n == 0) return 0;
+    int rc = reset_lanes(c);
+    if (rc) return rc;
+    k_plan_begin<<<1, 1, 0, c.s>>>(c.d, c.plan_beams_dev, c.plan_fe_dev, c.plan_dose_on ? c.plan_dose_dev : nullptr,
+                                   c.plan_res_dev, c.plan_n, c.plan_max_it);
+    CK(cudaGetLastError());
+    if ((rc = DISPATCH(c, refill, 0))) return rc;   // the first spots into every lane
+    CK(cudaGraphLaunch(c.exec, c.s));
+    k_plan_end<<<1, 1, 0, c.s>>>(c.d);
+    CK(cudaGetLastError());
+    c.injected = false;
+    // the lanes now hold plan spots' tables: the next injection rebuilds its own
+    std::fill(c.fe_E0.begin(), c.fe_E0.end(), NAN);
+    return 0;
+}
+
+int sm2d_plan_results(sm2d_handle h, double* dose, sm2d_spot_result* results) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    const size_t n = (size_t)c.plan_n;
+    if (dose && !c.plan_dose_on) return fail(SM2D_ERR_STATE, "the plan was loaded without dose maps");
+    if (results && n)
+        CK(cudaMemcpyAsync(results, c.plan_res_dev, sizeof(sm2d_spot_result) * n, cudaMemcpyDeviceToHost, c.s));
+    if (dose && n)
+        CK(cudaMemcpyAsync(dose, c.plan_dose_dev, sizeof(double) * (size_t)c.d.Nc * n, cudaMemcpyDeviceToHost, c.s));
+    int rc = sync_state(c);
+    if (rc) return rc;
     if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
     return 0;
+}
+
+int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    if (passes) *passes = h->gs_host->pass;
+    if (refills) *refills = h->gs_host->refills;
+    return 0;
+}
+
+int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, double* dose,
+                   sm2d_spot_result* results) {
+    int rc = sm2d_plan_load(h, beams, n_spots, max_iterations, dose ? 1 : 0);
+    if (rc) return rc;
+    if ((rc = sm2d_plan_run_async(h))) return rc;
+    return sm2d_plan_results(h, dose, results);
 }
 
 }  // extern "C"

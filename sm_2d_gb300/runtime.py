@@ -156,6 +156,10 @@ def lib(build_if_needed: bool = True):
         L.sm2d_batch_results.argtypes = [P, P, I]
         L.sm2d_batch_dose.argtypes = [P, P, I]
         L.sm2d_batch_audit_history.argtypes = [P, I, P, I, C.POINTER(I)]
+        L.sm2d_plan_load.argtypes = [P, P, I, I, I]
+        L.sm2d_plan_run_async.argtypes = [P]
+        L.sm2d_plan_results.argtypes = [P, P, P]
+        L.sm2d_plan_stats.argtypes = [P, C.POINTER(I), C.POINTER(I)]
         _LIB = L
         return L
 
@@ -437,8 +441,9 @@ class Transport:
         return self._lib.sm2d_stream(self.h)
 
     def batch_run(self, beams, max_iterations=100000, dose=True, results=True):
-        """Transport a list of Beam structures, `lanes` at a time.  Returns
-        (dose [n, Nz, Nx] or None, list of result dicts or None)."""
+        """Transport a plan (list of Beam structures), `lanes` spots in flight,
+        finished lanes refilled on the device.  Returns (dose [n, Nz, Nx] or
+        None, list of result dicts or None)."""
         n = len(beams)
         arr = (Beam * max(n, 1))(*beams)
         d = np.zeros((n, self.cfg.Nz, self.cfg.Nx)) if dose else None
@@ -446,6 +451,29 @@ class Transport:
         check(self._lib.sm2d_batch_run(self.h, C.cast(arr, C.c_void_p), n, int(max_iterations),
                                        _p(d) if dose else None, C.cast(r, C.c_void_p) if results else None))
         return d, ([r[i].as_dict() for i in range(n)] if results else None)
+
+    def plan_load(self, beams, max_iterations=100000, dose=True):
+        """Stage a plan on the device (sm2d_plan_load)."""
+        arr = (Beam * max(len(beams), 1))(*beams)
+        check(self._lib.sm2d_plan_load(self.h, C.cast(arr, C.c_void_p), len(beams), int(max_iterations),
+                                       1 if dose else 0))
+        self._plan_n = len(beams)
+
+    def plan_run_async(self):
+        check(self._lib.sm2d_plan_run_async(self.h))
+
+    def plan_results(self, dose=True, results=True):
+        n = getattr(self, "_plan_n", 0)
+        d = np.zeros((n, self.cfg.Nz, self.cfg.Nx)) if dose else None
+        r = (SpotResult * max(n, 1))() if results else None
+        check(self._lib.sm2d_plan_results(self.h, _p(d) if dose else None, C.cast(r, C.c_void_p) if results else None))
+        return d, ([r[i].as_dict() for i in range(n)] if results else None)
+
+    def plan_stats(self):
+        """(device passes, refill rounds) of the last plan."""
+        p, r = C.c_int(), C.c_int()
+        check(self._lib.sm2d_plan_stats(self.h, C.byref(p), C.byref(r)))
+        return p.value, r.value
 
     def batch_inject(self, beams):
         """Reset every lane and inject beams[i] into lane i (asynchronous)."""

@@ -1,9 +1,10 @@
-"""Batched spots (sm2d_batch_run): every spot of a batch -- lanes
-transported together, in waves -- equals the same spot transported alone
-on a single-lane engine (inject + run), as the reference runner transports
-one spot per call with the Fermi-Eyges tables of that spot's energy and
-width (gpu_transport_wrapper.cu:273-276): same iteration count and audit
-record, dose within 1e-5 of its maximum."""
+"""Batched spots.  A plan (sm2d_batch_run: lanes in flight, a finished lane
+refilled with the plan's next spot inside the device loop) and a wave
+(sm2d_batch_inject + run) transport every spot as a single-lane engine
+transports it alone (inject + run), as the reference runner transports one
+spot per call with the Fermi-Eyges tables of that spot's energy and width
+(gpu_transport_wrapper.cu:273-276): same iteration count and audit record,
+dose within 1e-5 of its maximum."""
 import numpy as np
 import pytest
 
@@ -20,47 +21,104 @@ def _cfg(lanes, E0=40.0, sigma_x=1.5):
 
 
 def _beams():
-    # uneven spots: energies, widths, positions and sample seeds differ
+    # uneven spots: energies (so iteration counts), widths, positions and
+    # sample seeds differ
     out = []
     for i, (E0, x0, sx) in enumerate([(40.0, 0.0, 1.5), (30.0, -2.0, 1.0), (35.0, 1.5, 2.0), (40.0, 3.0, 1.0),
-                                      (25.0, 0.5, 1.5)]):
+                                      (25.0, 0.5, 1.5), (20.0, -1.0, 1.2), (32.0, 2.0, 1.8)]):
         out.append(Beam(x0, 0.0, 0.0, E0, 1.0, sx, 0.002, 0.01 * E0, 300, 11 + i))
     return out
 
 
-def test_batch_equals_single_spots():
+def _single(b, max_it=3000):
+    with sm.Transport(_cfg(1, b.E0, b.sigma_x)) as one:
+        one.inject(b.x0, b.z0, b.theta0, b.E0, b.W_total, b.sigma_x, b.sigma_theta, b.sigma_E, b.n_samples, b.seed)
+        n = one.run(max_it)
+        wfail = sum(1 for h in one.audit_history() if not h["W_pass"])
+        return dict(n=n, dose=one.dose(), sc=one.scalars(), au=one.audit(), wfail=wfail)
+
+
+@pytest.fixture(scope="module")
+def singles():
+    return [_single(b) for b in _beams()]
+
+
+def _check_spot(i, r, dose, ref):
+    assert r["finished"] == 1 and r["iterations"] == ref["n"], (i, r["iterations"], ref["n"])
+    assert abs(r["weight_audit_failures"] - ref["wfail"]) <= 1, (i, r["weight_audit_failures"], ref["wfail"])
+    sc, au = ref["sc"], ref["au"]
+    assert abs(r["injected_energy"] - sc["source_injected_energy"]) <= 1e-9 * sc["source_injected_energy"]
+    assert abs(r["transport_dropped_energy"] - sc["transport_dropped_energy"]) <= 1e-6
+    for k in ("W_in_total", "W_out_total", "E_in_total", "E_dep_total", "E_nuclear_total"):
+        assert abs(r["last"][k] - au[k]) <= 1e-9 + 1e-5 * abs(au[k]), (i, k)
+    m = ref["dose"].max()
+    err = np.abs(dose - ref["dose"]).max()
+    assert err <= 1e-5 * m, (i, float(err / m))
+
+
+def test_plan_equals_single_spots(singles):
     beams = _beams()
-    ref_dose, ref_res = [], []
-    for b in beams:
-        with sm.Transport(_cfg(1, b.E0, b.sigma_x)) as one:
-            one.inject(b.x0, b.z0, b.theta0, b.E0, b.W_total, b.sigma_x, b.sigma_theta, b.sigma_E, b.n_samples,
-                       b.seed)
-            n = one.run(3000)
-            ref_dose.append(one.dose())
-            wfail = sum(1 for h in one.audit_history() if not h["W_pass"])
-            ref_res.append((n, one.scalars(), one.audit(), wfail))
-    with sm.Transport(_cfg(3)) as many:   # 5 spots on 3 lanes: two waves, the second one partial
+    with sm.Transport(_cfg(3)) as many:   # 7 spots on 3 lanes: lanes refilled as their spots finish
         assert many.lanes == 3
         dose, res = many.batch_run(beams, 3000)
-        # a single spot afterwards is back on the problem's tables (lane 0
-        # last held those of beams[3], 1.0 mm wide)
+        passes, refills = many.plan_stats()
+        # a single spot afterwards is back on the problem's tables
         b = beams[0]
         many.reset()
         many.inject(b.x0, b.z0, b.theta0, b.E0, b.W_total, b.sigma_x, b.sigma_theta, b.sigma_E, b.n_samples, b.seed)
-        assert many.run(3000) == ref_res[0][0]
+        assert many.run(3000) == singles[0]["n"]
         single_again = many.dose()
+    for i in range(len(beams)):
+        _check_spot(i, res[i], dose[i], singles[i])
+    # the first fill and at least one refill per finishing round; fewer
+    # passes than waves of 3 would need
+    n_it = [s["n"] for s in singles]
+    assert refills >= 3
+    waves = sum(max(n_it[k:k + 3]) + 1 for k in range(0, len(n_it), 3))
+    assert passes < waves, (passes, waves)
+    assert np.abs(single_again - singles[0]["dose"]).max() <= 1e-5 * singles[0]["dose"].max()
+
+
+def test_wave_equals_single_spots(singles):
+    beams = _beams()[:3]
+    with sm.Transport(_cfg(4)) as many:   # 3 spots on 4 lanes: one lane stays empty
+        many.batch_inject(beams)
+        many.run(3000)
+        res = many.batch_results(4)
+        dose = many.batch_dose(4)
+    for i in range(3):
+        _check_spot(i, res[i], dose[i], singles[i])
+    assert res[3]["iterations"] == 0 and not dose[3].any()
+
+
+def test_plan_iteration_limit():
+    """A spot cut at max_iterations: unfinished, its in-flight weight and
+    energy booked as a transport drop (the terminal residual)."""
+    beams = _beams()[:4]
+    lim = 25
+    with sm.Transport(_cfg(2)) as many:
+        _, res = many.batch_run(beams, lim, dose=False)
     for i, b in enumerate(beams):
-        n, sc, au, wfail = ref_res[i]
+        ref = _single(b, lim)
         r = res[i]
-        assert r["finished"] == 1 and r["iterations"] == n, (i, r["iterations"], n)
-        assert abs(r["weight_audit_failures"] - wfail) <= 1, (i, r["weight_audit_failures"], wfail)
-        assert abs(r["injected_energy"] - sc["source_injected_energy"]) <= 1e-9 * sc["source_injected_energy"]
-        assert abs(r["transport_dropped_energy"] - sc["transport_dropped_energy"]) <= 1e-6
-        for k in ("W_in_total", "W_out_total", "E_in_total", "E_dep_total", "E_nuclear_total"):
-            assert abs(r["last"][k] - au[k]) <= 1e-9 + 1e-5 * abs(au[k]), (i, k)
-        m = ref_dose[i].max()
-        assert np.abs(dose[i] - ref_dose[i]).max() <= 1e-5 * m, (i, float(np.abs(dose[i] - ref_dose[i]).max() / m))
-    assert np.abs(single_again - ref_dose[0]).max() <= 1e-5 * ref_dose[0].max()
+        assert r["finished"] == 0 and r["iterations"] == lim == ref["n"], (i, r)
+        want_w = ref["sc"]["transport_dropped_weight"] + ref["au"]["W_out_total"]
+        want_e = ref["sc"]["transport_dropped_energy"] + ref["au"]["E_out_total"]
+        assert abs(r["transport_dropped_weight"] - want_w) <= 1e-5 * want_w, (i, r["transport_dropped_weight"], want_w)
+        assert abs(r["transport_dropped_energy"] - want_e) <= 1e-5 * want_e
+
+
+def test_plan_repeats():
+    """The same plan twice on one engine: same iteration counts, and dose
+    equal up to the order of float atomic additions (1e-6 of its maximum)."""
+    beams = _beams()
+    with sm.Transport(_cfg(3)) as many:
+        d1, r1 = many.batch_run(beams, 3000)
+        many.plan_load(beams, 3000)
+        many.plan_run_async()
+        d2, r2 = many.plan_results()
+    assert [r["iterations"] for r in r1] == [r["iterations"] for r in r2]
+    assert np.abs(d1 - d2).max() <= 1e-6 * d1.max()
 
 
 def test_batch_refuses_bad_beams():
