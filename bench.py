@@ -1,17 +1,25 @@
 #!/usr/bin/env python
 """Benchmark: spots/s of the SM_2D K1..K6 transport step on one GB300.
 
-Workload (the production single-beam case): a 150 MeV Gaussian proton beam
-(sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 1 % of E0, 1000 LCG samples,
-seed 42) into homogeneous water, 200 x 400 cells of 0.5 mm (100 x 200 mm),
-full coarse/fine pipeline with the conservation audit every iteration, FP32
-phase space.  Phase-space grids are the ones the reference code builds and
-runs: 36 angular bins on +-0.35 rad, the default piecewise 1029-bin energy
-grid, 256 local bins (4 theta x 2 E x 8 x_sub x 4 z_sub).  `--grid log` runs
-the 256 log-E / 512 theta / 128-local-bin variant with the energy-split
-method instead.  A step is one wave: `lanes` spots of that beam (sample seeds
-differ per spot) transported together to completion (until the in-flight
-weight of each falls below 1e-6 of its injected weight).
+Workload (default, `--workload plan512`, the batching form): a plan of 512
+independent pencil-beam spots, energies uniform on the 2 MeV layers of
+70-230 MeV, lateral offsets on a 5 mm grid over +-50 mm, sigma_x uniform in
+3-6 mm, weights lognormal(0, 0.5), sigma_theta 2 mrad, sigma_E 1 % of E0,
+1000 LCG samples per spot; each spot on its own 200 x 400 water domain of
+0.5 mm cells; parameters drawn from a seeded generator.  `--workload c2`
+runs the production single beam instead: spots of a 150 MeV Gaussian beam
+(sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 1 % of E0, 1000 samples), sample
+seeds differing per spot.  Full coarse/fine pipeline with the conservation
+audit every iteration, FP32 phase space, each spot until its in-flight
+weight falls below 1e-6 of its injected weight.  Phase-space grids are the
+ones the reference code builds and runs: 36 angular bins on +-0.35 rad, the
+default piecewise 1029-bin energy grid, 256 local bins (4 theta x 2 E x 8
+x_sub x 4 z_sub).  `--grid log` runs the 256 log-E / 512 theta /
+128-local-bin variant with the energy-split method instead.
+
+A step is the whole plan: `lanes` spots in flight, a lane refilled with the
+plan's next spot inside the device loop as its spot finishes, the lateral
+post-convolution of every spot's dose on the device.
 
 Arms: default = libsm2d.so on the GPU; `--impl reference` = the reference's
 algorithm on the host cores (the CPU restatement in oracle/, all threads, one
@@ -36,6 +44,7 @@ sys.path.insert(0, ROOT)
 METRIC = "spots/s on 1 GB300, surrogate+batched vs plain K1–K6, at ≤1% dose error"
 BEAM = dict(x0=0.0, z0=0.0, theta0=0.0, E0=150.0, W=1.0, sigma_x=3.8, sigma_theta=0.002, sigma_E=1.5,
             n_samples=1000, seed=42)
+PLAN_SEED = 2024
 MAX_IT = 4000
 
 
@@ -60,10 +69,29 @@ def make_config(grid: str):
     return cfg.production()
 
 
-def spot_seeds(rank, lanes):
-    """Sample seeds of one wave on `rank`: disjoint across ranks (replicas by
-    spot), consecutive within a wave."""
-    return [BEAM["seed"] + 100003 * rank + i for i in range(lanes)]
+def spot_seeds(rank, n):
+    """Sample seeds of a plan of n spots on `rank`: disjoint across ranks
+    (replicas by spot), consecutive within a plan."""
+    return [BEAM["seed"] + 100003 * rank + i for i in range(n)]
+
+
+def plan_spots(workload, rank, n):
+    """The plan of `rank`: n spot descriptions (dicts of sm2d_beam fields).
+    plan512 draws energy layer, offset, width and weight per spot from a
+    generator seeded by rank; c2 repeats the production beam."""
+    seeds = spot_seeds(rank, n)
+    if workload == "c2" or SMALL:
+        return [dict(BEAM, seed=s) for s in seeds]
+    rng = np.random.default_rng(PLAN_SEED + rank)
+    out = []
+    for s in seeds:
+        E0 = 70.0 + 2.0 * int(rng.integers(0, 81))
+        x0 = -50.0 + 5.0 * int(rng.integers(0, 21))
+        sx = float(rng.uniform(3.0, 6.0))
+        w = float(rng.lognormal(0.0, 0.5))
+        out.append(dict(x0=x0, z0=0.0, theta0=0.0, E0=E0, W=w, sigma_x=sx, sigma_theta=0.002, sigma_E=0.01 * E0,
+                        n_samples=1000, seed=s))
+    return out
 
 
 def max_over_ranks(x, dist, device):
@@ -92,7 +120,7 @@ def auto_lanes(cfg, free_bytes, cap=64):
     return int(max(1, min(cap, 0.6 * free_bytes // lane_bytes(cfg))))
 
 
-def workload_desc(grid, L):
+def workload_desc(workload, grid, n_spots):
     if SMALL:
         return ("profiling case: 80 MeV Gaussian beam (sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 0.8 MeV, "
                 "1000 samples) in water 100x200 cells @0.5 mm; reference grids; full K1-K6 + audit per iteration")
@@ -100,9 +128,15 @@ def workload_desc(grid, L):
         ph = "256 log E bins 0.1-250 MeV, 512 theta bins +-pi/2, 128 local bins (8x4x4x1), energy-split method"
     else:
         ph = "reference grids: 1029 piecewise E bins, 36 theta bins +-0.35 rad, 256 local bins (4x2x8x4)"
-    return ("150 MeV Gaussian beam (sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 1.5 MeV, 1000 samples) "
-            f"in water 200x400 cells @0.5 mm; {ph}; full K1-K6 + audit per iteration; until in-flight "
-            f"weight < 1e-6 W0")
+    if workload == "c2":
+        spots = (f"{n_spots} spots of a 150 MeV Gaussian beam (sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 1.5 MeV, "
+                 "1000 samples, sample seeds per spot)")
+    else:
+        spots = (f"{n_spots} pencil-beam spots: E uniform on 70-230 MeV 2 MeV layers, x0 on a 5 mm grid over "
+                 "+-50 mm, sigma_x U[3,6] mm, weights lognormal(0,0.5), sigma_theta 2 mrad, sigma_E 1% E0, "
+                 f"1000 samples each (generator seed {PLAN_SEED})")
+    return (f"{spots}; each spot in its own water domain 200x400 cells @0.5 mm; {ph}; full K1-K6 + audit per "
+            "iteration + lateral dose post-convolution; each spot until in-flight weight < 1e-6 W0")
 
 
 # ---------------------------------------------------------------- clocks
@@ -151,16 +185,16 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU arm
-def cpu_spots_per_s(grid: str, n_threads: int, n_spots: int):
-    """Transport n_spots independent copies of the workload on the CPU oracle,
-    n_threads at a time; returns (spots/s, wall seconds)."""
+def cpu_spots_per_s(grid: str, workload: str, n_threads: int, n_spots: int):
+    """Transport the first n_spots spots of the plan on the CPU oracle (each
+    with the Fermi-Eyges tables of its own energy and width), n_threads at a
+    time; returns (spots/s, wall seconds)."""
     from oracle import oracle as orc
     cfg = make_config(grid)
-    oc = cfg.oracle_config()
     oracles = []
-    for i in range(n_spots):
+    for b in plan_spots(workload, 0, n_spots):
+        oc = dict(cfg.oracle_config(), E0=b["E0"], sigma_x_initial=b["sigma_x"])
         o = orc.Oracle(oc, cfg.theta_edges, cfg.E_edges)
-        b = dict(BEAM)
         o.inject(**b)
         oracles.append(o)
     t0 = time.perf_counter()
@@ -177,19 +211,19 @@ def run_reference_arm(args):
         return 0
     n_threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_spots_per_s(args.grid, n_threads, n_threads)
+        cpu_spots_per_s(args.grid, args.workload, n_threads, n_threads)
     vals, walls = [], []
     for _ in range(args.steps):
-        v, dt = cpu_spots_per_s(args.grid, n_threads, n_threads)
+        v, dt = cpu_spots_per_s(args.grid, args.workload, n_threads, n_threads)
         vals.append(v)
         walls.append(dt)
     value = float(len(vals) * n_threads / sum(walls))
-    cfg = make_config(args.grid)
-    sample = f"{n_threads} spots per step (one per host thread), full transport of each"
+    sample = (f"the first {n_threads} spots of the plan per step (one per host thread), full transport of each "
+              "(the plan's spots are independent: spots/s of a sample is the plan's rate)")
     line = {"metric": METRIC, "value": value, "unit": "spots/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(walls)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_desc(args.grid, cfg.layout), "grid": args.grid},
+            "config": {"workload": workload_desc(args.workload, args.grid, args.spots), "grid": args.grid},
             "cpu_baseline": {"value": value, "unit": "spots/s", "cores": n_threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "spots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -224,28 +258,24 @@ def run_gpu_arm(args):
     B = t.lanes
     ext = torch.cuda.ExternalStream(t.stream())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
-
-    # one wave = B spots of the workload beam, sample seeds differing per spot
-    beams = [Beam(BEAM["x0"], BEAM["z0"], BEAM["theta0"], BEAM["E0"], BEAM["W"], BEAM["sigma_x"],
-                  BEAM["sigma_theta"], BEAM["sigma_E"], BEAM["n_samples"], seed) for seed in spot_seeds(rank, B)]
-    beam_arr = (Beam * B)(*beams)
     lib = t._lib
 
-    def one_wave():
-        t.batch_inject(beams)
-        t.run_async(MAX_IT)
+    # this rank's plan: the spots are independent (replicas by spot)
+    n = args.spots
+    spots = plan_spots(args.workload, rank, n)
+    beams = [Beam(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
+                  b["n_samples"], b["seed"]) for b in spots]
+    beam_arr = (Beam * n)(*beams)
 
+    # ---- device-resident plan: beams and Fermi-Eyges tables staged in HBM
+    # before the timed region; each step transports the whole plan and
+    # leaves the post-convolved dose of every spot in HBM
+    t.plan_load(beams, MAX_IT, dose=True)
     for _ in range(max(args.warmup, 3)):
-        one_wave()
+        t.plan_run_async()
     torch.cuda.synchronize()
-    res = t.batch_results(B)
-    iters = [r["iterations"] for r in res]
-
-    # ---- timed region: K waves of B spots, device time per wave (every wave
-    # streams GBs of phase space, far more than L2; L2 is flushed between waves too)
-    times = []
-    launches = 0
-    cell_steps = 0.0
+    times, launches, cell_steps, bins_done, iters = [], 0, 0.0, 0.0, []
+    per_pass = 7 if cfg.use_buckets else 6
     barrier()
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -254,27 +284,31 @@ def run_gpu_arm(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(ext)
-            one_wave()
+            t.plan_run_async()
             e1.record(ext)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
-            rs = t.batch_results(B)
-            passes = max(r["iterations"] for r in rs) + 1
+            _, rs = t.plan_results(dose=False)
+            passes, refills, bins = t.plan_stats()
             cell_steps += sum(r["cell_steps"] for r in rs)
-            # reset 3 + injection 6 + loop limit 1, then per pass of the device
-            # loop classify, claim pass, bucket and psi_out selection, deposit
-            # pass, finalize (+ bucket move)
-            launches += 10 + (7 if cfg.use_buckets else 6) * passes
+            bins_done += bins
+            iters = [r["iterations"] for r in rs]
+            # reset 3, plan begin 1, first fill 8 (dose/tally clear, lane
+            # assignment, injection 6), plan end 1; per pass of the device loop
+            # (the halting one included) classify, claim pass, bucket and psi_out
+            # selection, deposit pass, finalize (+ bucket move); 8 per refill
+            launches += 13 + (passes + 1) * per_pass + 8 * (refills - 1)
     barrier()
     total_ms = max_over_ranks(np.sum(times), dist, "cuda")
-    spots = args.steps * B * world
-    value = spots / (total_ms / 1e3)
+    value = args.steps * n * world / (total_ms / 1e3)
+    unfinished = sum(1 for r in rs if not r["finished"])
 
     # ---- end to end through the public batch entry with pinned host buffers:
-    # beam descriptions in, one dose map per spot out
-    dose_host = torch.zeros(B * cfg.Nx * cfg.Nz, dtype=torch.float64).pin_memory()
-    beam_pin = torch.zeros(C.sizeof(Beam) * B, dtype=torch.uint8).pin_memory()
-    C.memmove(beam_pin.data_ptr(), C.addressof(beam_arr), C.sizeof(Beam) * B)
+    # beam descriptions in (the Fermi-Eyges tables computed on the host per
+    # spot), one post-convolved dose map per spot out
+    dose_host = torch.zeros(n * cfg.Nx * cfg.Nz, dtype=torch.float64).pin_memory()
+    beam_pin = torch.zeros(C.sizeof(Beam) * n, dtype=torch.uint8).pin_memory()
+    C.memmove(beam_pin.data_ptr(), C.addressof(beam_arr), C.sizeof(Beam) * n)
     e2e_times = []
     for _ in range(args.steps):
         flush.zero_()
@@ -282,7 +316,7 @@ def run_gpu_arm(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(ext)
-        rc = lib.sm2d_batch_run(t.h, C.c_void_p(beam_pin.data_ptr()), B, MAX_IT, C.c_void_p(dose_host.data_ptr()),
+        rc = lib.sm2d_batch_run(t.h, C.c_void_p(beam_pin.data_ptr()), n, MAX_IT, C.c_void_p(dose_host.data_ptr()),
                                 None)
         e1.record(ext)
         e1.synchronize()
@@ -290,13 +324,13 @@ def run_gpu_arm(args):
             raise RuntimeError(lib.sm2d_last_error().decode())
         e2e_times.append(e0.elapsed_time(e1))
     e2e_ms = max_over_ranks(np.sum(e2e_times), dist, "cuda")
-    e2e_value = spots / (e2e_ms / 1e3)
+    e2e_value = args.steps * n * world / (e2e_ms / 1e3)
 
-    # ---- per-kernel device time: eager replay of one wave with CUDA events
-    # around every launch on the library stream
-    t.batch_inject(beams)
+    # ---- per-kernel device time: eager replay of one wave of the plan's first
+    # `lanes` spots with CUDA events around every launch on the library stream
+    t.batch_inject(beams[:B])
     n_it, ms, n_launch = t.run_profiled(MAX_IT)
-    prs = t.batch_results(B)
+    prs = t.batch_results(min(B, n))
     L = t.L
     slot_bytes = 4 + 4 * L
     alg_bytes = sum((r["slots_in"] + r["slots_out"]) * slot_bytes + 44.0 * r["cell_steps"] for r in prs)
@@ -308,10 +342,10 @@ def run_gpu_arm(args):
         peak, peak_src = 6800.0, "fallback"
     achieved = alg_bytes / (ms["transport"] / 1e3) / 1e9 if ms["transport"] > 0 else 0.0
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "k_transport_traffic.json")
+    tp = os.path.join(ROOT, "profiles", f"k_transport_traffic_{args.workload}.json")
     if os.path.exists(tp) and not SMALL and args.grid == "reference":
-        # DRAM bytes per deposit launch from the ncu capture of this workload
-        # (recorded per lane; the lanes' work adds up)
+        # DRAM bytes per deposit launch from an ncu capture of the same wave at
+        # fewer lanes, scaled by the lane count (the lanes' work adds up)
         tr = json.load(open(tp))
         traffic = tr["dram_bytes_per_launch_per_lane"] * B
     step_total = sum(ms.values())
@@ -320,29 +354,31 @@ def run_gpu_arm(args):
                 "algorithmic_bytes_per_launch": alg_bytes / max(n_it, 1),
                 "avg_launch_ms": ms["transport"] / max(n_it, 1),
                 "stage_share": {k: v / step_total for k, v in ms.items()} if step_total else {},
-                "note": "per-launch times from an eager replay of one wave with CUDA events around each "
-                        "kernel on the library stream"}
+                "note": "per-launch times from an eager replay of one wave (the plan's first lanes' spots) with "
+                        "CUDA events around each kernel on the library stream"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         n_threads = os.cpu_count() or 1
-        v, dt = cpu_spots_per_s(args.grid, n_threads, n_threads)
+        v, dt = cpu_spots_per_s(args.grid, args.workload, n_threads, n_threads)
         cpu = {"value": v, "unit": "spots/s", "cores": n_threads, "kind": "port",
-               "sample": f"{n_threads} spots, one per host thread, full transport ({dt:.1f} s wall)"}
+               "sample": f"the plan's first {n_threads} spots, one per host thread, full transport ({dt:.1f} s wall)"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "spots/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": workload_desc(args.grid, cfg.layout), "grid": args.grid,
+                "config": {"workload": workload_desc(args.workload, args.grid, n), "grid": args.grid,
                            "method": "plain K1-K6 (direct neighbour scatter), deterministic slot claims",
-                           "step": f"one wave of {B} spots transported together (lanes)", "lanes": B,
-                           "iterations_per_spot": float(np.mean(iters)),
-                           "l2": "inputs larger than L2 (GBs of phase space per wave); 256 MB flush between waves",
-                           "parallelism": f"{B} spots per GPU, replicas by spot x{world}"},
+                           "step": f"one plan of {n} spots, {B} in flight (lanes), lanes refilled on the device",
+                           "lanes": B, "spots_per_step": n, "iterations_per_spot": float(np.mean(iters)),
+                           "unfinished_spots": unfinished,
+                           "l2": "inputs larger than L2 (GBs of phase space per step); 256 MB flush between steps",
+                           "parallelism": f"{n} spots per GPU per step, replicas by spot x{world}"},
                 "cell_steps_per_s": cell_steps * world / (total_ms / 1e3) if total_ms else None,
-                "e2e": {"value": e2e_value, "unit": "spots/s", "h2d_bytes_per_step": int(C.sizeof(Beam) * B),
-                        "d2h_bytes_per_step": int(cfg.Nx * cfg.Nz * 8 * B)},
+                "bins_per_s": bins_done * world / (total_ms / 1e3) if total_ms else None,
+                "e2e": {"value": e2e_value, "unit": "spots/s", "h2d_bytes_per_step": int(C.sizeof(Beam) * n),
+                        "d2h_bytes_per_step": int(cfg.Nx * cfg.Nz * 8 * n)},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "gpu_launches": launches}
         print(json.dumps(line))
@@ -355,12 +391,14 @@ def run_gpu_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", default="reference", choices=["reference", "log"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--lanes", type=int, default=0, help="spots per wave (0: from free device memory)")
+    ap.add_argument("--lanes", type=int, default=0, help="spots in flight (0: from free device memory)")
+    ap.add_argument("--workload", default="plan512", choices=["plan512", "c2"])
+    ap.add_argument("--spots", type=int, default=512, help="spots per step (the plan)")
     ap.add_argument("--small", action="store_true",
                     help="100x200 cells, 80 MeV beam: a small case for profiler captures (not a bench line)")
     args = ap.parse_args()

@@ -212,12 +212,13 @@ int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_i
  * device (its Fermi-Eyges tables computed on the host threads; with_dose
  * keeps a device dose map per spot), sm2d_plan_run_async transports it on
  * the engine's stream, sm2d_plan_results waits and copies dose (NULL: none)
- * and results (NULL: none) back.  sm2d_plan_stats: device passes and refill
- * rounds of the last plan. */
+ * and results (NULL: none) back.  sm2d_plan_stats: device passes, refill
+ * rounds and transported bins (local bins with weight) since the last
+ * plan's start (or the last reset). */
 int sm2d_plan_load(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, int with_dose);
 int sm2d_plan_run_async(sm2d_handle h);
 int sm2d_plan_results(sm2d_handle h, double* dose, sm2d_spot_result* results);
-int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills);
+int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills, double* bins);
 /* One wave of spots, for callers that drive the loop themselves:
  * sm2d_batch_inject resets every lane and injects beams[i] into lane i
  * (lanes past n_beams stay empty; asynchronous, like sm2d_inject_async);

@@ -73,6 +73,7 @@ struct IterGlobal {
     int plan_next;         // next spot to hand out
     int lane_max_it;       // iteration limit of one spot
     int refills;           // refill rounds run
+    unsigned long long bins_total;   // bins transported since the last reset
     int occ_mark;          // psi_in's occupancy list length when the injection opened
     int n_fin;             // lanes whose spot finished at this classification
     int fin[kMaxLanes];    // those lanes, ascending
@@ -121,6 +122,12 @@ struct Dev {
     int lutN;
     float lutEmin, lutEmax;
     const float *R, *logE, *logR;
+    float R_fine_on;      // lut_range(max(E_fine_on, lutEmin)), evaluated once on the device
+    // search tables (slot_of): the energy bin / R index where the searches
+    // of the slot's smallest value end
+    const int *e_slot, *r_slot;
+    uint32_t e_base, r_base;
+    int e_nslot, r_nslot;
     // per lane: Fermi-Eyges moments A(z), B(z), sigma_total(z) [B][Nz] of the
     // lane's beam (k1k6_pipeline.cu:1061-1206) and its initial sigma_x [B]
     float *feA, *feB, *feS, *sx0;
@@ -176,19 +183,29 @@ __device__ __forceinline__ int sub_bin(float off, float d, int n) {
 }
 
 // ---------------------------------------------------------------- LUT (device_lut.cuh:34-214)
-__device__ __forceinline__ int find_bin(const float* __restrict__ e, int N, float E) {
+// The searches of the LUT (device_find_bin_edges, the R inversion) start
+// from a table indexed by the top bits of the value's float pattern
+// (2^(23 - kSlotShift) slots per octave, monotone in the value): the
+// table holds the search result at the slot's smallest value, a lower bound
+// for every value in the slot, and a forward scan of a few entries ends at
+// exactly the binary search's result.
+constexpr int kSlotShift = 15;
+__device__ __forceinline__ int slot_of(float x, uint32_t base, int n) {
+    const int j = (int)(__float_as_uint(x) >> kSlotShift) - (int)base;
+    return max(0, min(j, n - 1));
+}
+// bin b of the energy edges with Ee[b] <= E < Ee[b+1], clamped to [0, N_E)
+__device__ __forceinline__ int find_ebin(const Dev& d, float E) {
+    const float* e = d.Ee;
     if (E <= e[0]) return 0;
-    if (E >= e[N]) return N - 1;
-    int lo = 0, hi = N;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (e[mid + 1] <= E) lo = mid + 1; else hi = mid;
-    }
-    return lo;
+    if (E >= e[d.N_E]) return d.N_E - 1;
+    int b = d.e_slot[slot_of(E, d.e_base, d.e_nslot)];
+    while (e[b + 1] <= E) ++b;   // stops at N_E - 1 at the latest: E < e[N_E]
+    return b;
 }
 __device__ __forceinline__ float lut_range(const Dev& d, float E) {
     float Ec = fmaxf(d.lutEmin, fminf(E, d.lutEmax));
-    int b = find_bin(d.Ee, d.lutN, Ec);
+    int b = find_ebin(d, Ec);
     if (b == d.lutN - 1 || Ec >= d.lutEmax) return d.R[d.lutN - 1];
     float le = sm2d_logf(Ec);
     float lr = d.logR[b] + (d.logR[b + 1] - d.logR[b]) * (le - d.logE[b]) / (d.logE[b + 1] - d.logE[b]);
@@ -196,11 +213,8 @@ __device__ __forceinline__ float lut_range(const Dev& d, float E) {
 }
 __device__ __forceinline__ float lut_energy_of_range(const Dev& d, float r) {
     if (r <= 0.0f) return d.lutEmin;
-    int lo = 0, hi = d.lutN;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (d.R[mid] < r) lo = mid + 1; else hi = mid;
-    }
+    int lo = d.r_slot[slot_of(r, d.r_base, d.r_nslot)];   // first index with R[lo] >= r
+    while (lo < d.lutN && d.R[lo] < r) ++lo;
     int b = max(0, min(lo, d.lutN - 2));
     float lr = sm2d_logf(r);
     float dl = d.logR[b + 1] - d.logR[b];
@@ -208,13 +222,15 @@ __device__ __forceinline__ float lut_energy_of_range(const Dev& d, float r) {
     float le = d.logE[b] + (d.logE[b + 1] - d.logE[b]) * (lr - d.logR[b]) / dl;
     return sm2d_expf(le);
 }
-__device__ __forceinline__ float lut_energy_loss(const Dev& d, float E, float s) {
-    float r = lut_range(d, E) - s;
+// energy lost over path s from E, whose range RE = lut_range(d, E)
+__device__ __forceinline__ float lut_energy_loss(const Dev& d, float E, float RE, float s) {
+    float r = RE - s;
     float En = (r <= 0.0f) ? d.lutEmin : lut_energy_of_range(d, r);
     return E - En;
 }
-__device__ __forceinline__ float fine_step_limit(const Dev& d, float E) {
-    float v = 0.01f * lut_range(d, E);
+// K3 step limit at E, whose range RE = lut_range(d, E)
+__device__ __forceinline__ float fine_step_limit(float E, float RE) {
+    float v = 0.01f * RE;
     float floor_ = E < 2.0f ? 0.1f : (E < 20.0f ? 0.25f : (E < 100.0f ? 0.5f : 1.0f));
     v = fmaxf(v, floor_);
     if (E < 0.5f) v = fminf(v, 0.05f);
@@ -278,7 +294,12 @@ __device__ __forceinline__ float nuclear_xs(float E) {
 }
 __device__ __forceinline__ float gauss_cdf(float x, float mu, float sigma) {
     if (sigma < 1e-10f) return (x >= mu) ? 1.0f : 0.0f;
-    float c = 0.5f * (1.0f + sm2d_erff((x - mu) / sigma * 0.70710678f));
+    const float dd = x - mu;
+    // beyond 8 sigma the argument of erf exceeds 4, where sm2d_erff is
+    // exactly +-1: the same 1 or 0 without the division and the series
+    if (dd > 8.0f * sigma) return 1.0f;
+    if (dd < -8.0f * sigma) return 0.0f;
+    float c = 0.5f * (1.0f + sm2d_erff(dd / sigma * 0.70710678f));
     return fminf(1.0f, fmaxf(0.0f, c));
 }
 

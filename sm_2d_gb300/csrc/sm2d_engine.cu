@@ -132,7 +132,7 @@ __device__ bool inject_sample(const Dev& d, const BeamArgs& b, float x_min, floa
     const float cont = (theta - tmin) / ((tmax - tmin) / (float)d.N_theta);
     int tb = (int)cont;
     float ft = cont - (float)tb;
-    int Eb = find_bin(d.Ee, d.N_E, E);
+    int Eb = find_ebin(d, E);
     const float lo = d.Ee[Eb], hi = d.Ee[Eb + 1];
     float fE = (hi - lo) > 1e-10f ? (E - lo) / (hi - lo) : 0.0f;
     if (tb >= d.N_theta - 1) { tb = d.N_theta - 1; ft = 0.0f; }
@@ -495,6 +495,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     gs->n_listed = halt ? 0 : min(nl, d.listed_cap);
     gs->n_items = halt ? 0 : ni;
     gs->n_bins = halt ? 0 : nb;
+    if (!halt) gs->bins_total += (unsigned long long)nb;
     gs->blocks_done = 0;
     if (use_cond) {
         cudaGraphSetConditional(cond, (!halt && gs->pass + 1 < gs->max_pass) ? 1u : 0u);
@@ -1075,6 +1076,12 @@ __global__ void k_dose(const double* __restrict__ edep, const int* __restrict__ 
     out[i] = acc;
 }
 
+// lut_range(E) of the device LUT, once (the fine-threshold range of K2)
+__global__ void k_eval_range(Dev d, float E, float* out) {
+    if (threadIdx.x || blockIdx.x) return;
+    *out = lut_range(d, E);
+}
+
 // ------------------------------------------------------------------ spot plan
 // Outcome of a lane's spot (sm2d_spot_result).
 __host__ __device__ inline void lane_result(const LaneState& L, sm2d_spot_result& r) {
@@ -1503,6 +1510,26 @@ static int stage_beams(Ctx& c, const sm2d_beam* beams, int n, int* max_n) {
     return 0;
 }
 
+// Search tables of slot_of: for each slot of float patterns between lo and
+// hi (top bits above kSlotShift), the result of `search` at the slot's
+// smallest value.
+template <class F>
+static std::vector<int> slot_table(float lo, float hi, uint32_t* base, F search) {
+    uint32_t ulo, uhi;
+    memcpy(&ulo, &lo, 4);
+    memcpy(&uhi, &hi, 4);
+    *base = ulo >> kSlotShift;
+    const uint32_t last = uhi >> kSlotShift;
+    std::vector<int> t(last - *base + 1);
+    for (uint32_t j = 0; j < t.size(); ++j) {
+        const uint32_t u = (*base + j) << kSlotShift;
+        float v;
+        memcpy(&v, &u, 4);
+        t[j] = search(v);
+    }
+    return t;
+}
+
 }  // namespace sm2d
 
 using namespace sm2d;
@@ -1587,6 +1614,28 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(R_d, float, N);
     A(lE_d, float, N);
     A(lR_d, float, N);
+    // search tables: the energy bin (binary search of device_find_bin_edges)
+    // and the R-LUT lower bound at each slot's smallest value
+    const std::vector<float>& Eh = c->Ee;
+    const std::vector<int> et = slot_table(Eh[0], Eh[N], &d.e_base, [&](float v) {
+        if (v <= Eh[0]) return 0;
+        if (v >= Eh[N]) return N - 1;
+        int lo = 0, hi = N;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (Eh[mid + 1] <= v) lo = mid + 1; else hi = mid;
+        }
+        return lo;
+    });
+    const std::vector<int> rt = slot_table(std::max(R[0], 1e-30f), std::max(R[N - 1], 1e-30f), &d.r_base,
+                                           [&](float v) { return (int)(std::lower_bound(R.begin(), R.end(), v) - R.begin()); });
+    d.e_nslot = (int)et.size();
+    d.r_nslot = (int)rt.size();
+    int *e_slot, *r_slot;
+    A(e_slot, int, et.size());
+    A(r_slot, int, rt.size());
+    d.e_slot = e_slot;
+    d.r_slot = r_slot;
     const size_t BN = (size_t)B * p->Nz;
     A(c->fe_dev, float, 3 * BN + B);
     d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d;
@@ -1648,7 +1697,9 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
               cudaMemcpyAsync(Ee_d, c->Ee.data(), sizeof(float) * (N + 1), cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(R_d, R.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(lE_d, lE.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-              cudaMemcpyAsync(lR_d, lR.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess;
+              cudaMemcpyAsync(lR_d, lR.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(e_slot, et.data(), sizeof(int) * et.size(), cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(r_slot, rt.data(), sizeof(int) * rt.size(), cudaMemcpyHostToDevice, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.bid, 0xFF, ns * 4, s) == cudaSuccess &&
          cudaMemsetAsync(d.val, 0, ns * c->L * 4, s) == cudaSuccess;
     for (int k = 0; k < 2 && ok; ++k) ok = cudaMemsetAsync(d.occ[k], 0, NcB * 4, s) == cudaSuccess;
@@ -1665,6 +1716,15 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
          cudaMemsetAsync(d.ccount, 0, c->ccount_n * sizeof(int), s) == cudaSuccess &&
          cudaMemsetAsync(d.bkt_ids, 0xFF, (size_t)4 * d.listed_cap * kKb * 4, s) == cudaSuccess;
     if (!ok) return bail(fail(SM2D_ERR_CUDA, "initial copies failed"));
+    {   // the fine-threshold range, evaluated by the device LUT itself
+        void* q1 = nullptr;
+        if ((rc = dalloc(*c, &q1, sizeof(float)))) return bail(rc);
+        float* rf = static_cast<float*>(q1);
+        k_eval_range<<<1, 1, 0, s>>>(d, fmaxf(p->E_fine_on, d.lutEmin), rf);
+        if (cudaMemcpyAsync(&d.R_fine_on, rf, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return bail(fail(SM2D_ERR_CUDA, "LUT setup"));
+    }
     // every lane starts with the problem's tables
     c->fe_host.assign(3 * BN + B, 0.0f);
     c->fe_E0.assign(B, -1.0f);
@@ -2167,12 +2227,13 @@ int sm2d_plan_results(sm2d_handle h, double* dose, sm2d_spot_result* results) {
     return 0;
 }
 
-int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills) {
+int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills, double* bins) {
     if (!h) return fail(SM2D_ERR_ARG, "null handle");
     int rc = sync_state(*h);
     if (rc) return rc;
     if (passes) *passes = h->gs_host->pass;
     if (refills) *refills = h->gs_host->refills;
+    if (bins) *bins = (double)h->gs_host->bins_total;
     return 0;
 }
 

@@ -55,7 +55,7 @@ struct EParts {
 // neighbouring bin centres.
 __device__ __forceinline__ EParts bin_energy(const Dev& d, float E, float w) {
     EParts p;
-    int k = find_bin(d.Ee, d.N_E, E);
+    int k = find_ebin(d, E);
     p.n = 1;
     p.bin[0] = p.bin[1] = k;
     p.frac[0] = 1.0f;
@@ -161,7 +161,7 @@ __device__ __forceinline__ EmitPlan plan_emission(const Dev& d, float theta, flo
         p.tw1 = f * f;
     }
     const float Ec = fmaxf(d.Ee[0], fminf(E, d.Ee[d.N_E]));
-    const int k = find_bin(d.Ee, d.N_E, Ec);
+    const int k = find_ebin(d, Ec);
     p.k = k;
     p.lo = -1;
     p.hi = -1;
@@ -294,7 +294,8 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
         float s = 0.0f;
         for (int i = 0; i < N; ++i) s += w[i];
         if (s > 1e-10f) {
-            for (int i = 0; i < N; ++i) w[i] /= s;
+            for (int i = 0; i < N; ++i)
+                if (w[i] != 0.0f) w[i] /= s;   // 0 / s is 0: skip the division
         } else {
             for (int i = 0; i < N; ++i) w[i] = (i == N / 2) ? 1.0f : 0.0f;
         }
@@ -305,7 +306,8 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
         for (int i = 0; i < N; ++i) w[i] = 0.0f;
         w[N / 2] = 1.0f;
     } else {
-        for (int i = 0; i < N; ++i) w[i] /= s;
+        for (int i = 0; i < N; ++i)
+            if (w[i] != 0.0f) w[i] /= s;
     }
     const int ixs = src % d.Nx, izs = (src / d.Nx) % d.Nz, tz = izs + 1;
     const EmitPlan pl = plan_emission(d, theta, E);
@@ -373,7 +375,8 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             for (int i = 0; i < Lay::NX; ++i) s += w[i];
             if (s > 1e-10f) {
 #pragma unroll
-                for (int i = 0; i < Lay::NX; ++i) w[i] /= s;
+                for (int i = 0; i < Lay::NX; ++i)
+                    if (w[i] != 0.0f) w[i] /= s;
             } else {
 #pragma unroll
                 for (int i = 0; i < Lay::NX; ++i) w[i] = (i == Lay::NX / 2) ? 1.0f : 0.0f;
@@ -415,6 +418,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             const double Ec_out = (double)e_center(d, max(0, min(Ebe, d.N_E - 1)));
 #pragma unroll
             for (int xs = 0; xs < Lay::NX; ++xs) {
+                if (w[xs] <= 0.0f) continue;   // its share would be 0
                 const float wf = (w[xs] / wsum) * wcf;
                 if (wf <= 0.0f) continue;
                 const float ws = wpart * wf;
@@ -563,8 +567,9 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, 
         const float sxp = (eta0 > 0) ? (hx - xc) / eta0 : 1e30f;
         const float sxm = (eta0 < 0) ? (-hx - xc) / eta0 : 1e30f;
         const float sb = fmaxf(fminf(fminf(szp, szm), fminf(sxp, sxm)), 0.0f);
-        step = fminf(fine_step_limit(d, E), sb * 1.001f);
-        const float mean_dE = lut_energy_loss(d, E, step);
+        const float RE = lut_range(d, E);
+        step = fminf(fine_step_limit(E, RE), sb * 1.001f);
+        const float mean_dE = lut_energy_loss(d, E, RE, step);
         if (d.straggle) {
             unsigned seed = ((unsigned)(lc * 7 + sslot * 13 + lidx * 17) ^ 0xDEECE66Du) ^ salt;
             const float sE = straggling_sigma(E, step, 1.0f);
@@ -597,12 +602,13 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, 
         float lim = fminf(d.step_coarse, fminf(dx, dz));
         float rs = lim;
         bool split = false;
+        const float RE = lut_range(d, E);
         if (E > d.E_fine_on + 1e-6f) {
-            const float rtf = lut_range(d, E) - lut_range(d, fmaxf(d.E_fine_on, d.lutEmin));
+            const float rtf = RE - d.R_fine_on;
             if (rtf > 0.0f && rtf < rs) { rs = rtf; lim = rs; split = true; }
         }
         step = lim;
-        dE = fminf(lut_energy_loss(d, E, rs), E);
+        dE = fminf(lut_energy_loss(d, E, RE, rs), E);
         E_new = E - dE;
         edep = dE * w;
         const float surv = sm2d_expf(-nuclear_xs(E) * rs);

@@ -159,7 +159,7 @@ def lib(build_if_needed: bool = True):
         L.sm2d_plan_load.argtypes = [P, P, I, I, I]
         L.sm2d_plan_run_async.argtypes = [P]
         L.sm2d_plan_results.argtypes = [P, P, P]
-        L.sm2d_plan_stats.argtypes = [P, C.POINTER(I), C.POINTER(I)]
+        L.sm2d_plan_stats.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(D)]
         _LIB = L
         return L
 
@@ -470,10 +470,10 @@ class Transport:
         return d, ([r[i].as_dict() for i in range(n)] if results else None)
 
     def plan_stats(self):
-        """(device passes, refill rounds) of the last plan."""
-        p, r = C.c_int(), C.c_int()
-        check(self._lib.sm2d_plan_stats(self.h, C.byref(p), C.byref(r)))
-        return p.value, r.value
+        """(device passes, refill rounds, transported bins) of the last plan."""
+        p, r, b = C.c_int(), C.c_int(), C.c_double()
+        check(self._lib.sm2d_plan_stats(self.h, C.byref(p), C.byref(r), C.byref(b)))
+        return p.value, r.value, b.value
 
     def batch_inject(self, beams):
         """Reset every lane and inject beams[i] into lane i (asynchronous)."""

@@ -61,7 +61,7 @@ def test_plan_equals_single_spots(singles):
     with sm.Transport(_cfg(3)) as many:   # 7 spots on 3 lanes: lanes refilled as their spots finish
         assert many.lanes == 3
         dose, res = many.batch_run(beams, 3000)
-        passes, refills = many.plan_stats()
+        passes, refills, _ = many.plan_stats()
         # a single spot afterwards is back on the problem's tables
         b = beams[0]
         many.reset()

@@ -1,6 +1,7 @@
 """The multi-rank host logic of bench.py on CPU with the gloo backend,
-world size 2: spots are sharded by rank with no overlap (replicas by spot,
-no data-path collective) and timings reduce to the slowest rank."""
+world size 2: each rank's plan holds its own spots, with no overlap
+(replicas by spot, no data-path collective), and timings reduce to the
+slowest rank."""
 import os
 import socket
 import sys
@@ -24,7 +25,9 @@ def _worker(rank, world, port, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        seeds = torch.tensor(bench.spot_seeds(rank, 8), dtype=torch.int64)
+        plan = bench.plan_spots("plan512", rank, 8)
+        seeds = torch.tensor([b["seed"] for b in plan], dtype=torch.int64)
+        assert [b["seed"] for b in plan] == bench.spot_seeds(rank, 8)
         gathered = [torch.zeros_like(seeds) for _ in range(world)]
         dist.all_gather(gathered, seeds)
         slowest = bench.max_over_ranks(10.0 * (rank + 1), dist, "cpu")
@@ -59,3 +62,9 @@ def test_single_process_needs_no_collective():
     import bench
     assert bench.max_over_ranks(3.5, None, "cpu") == 3.5
     assert bench.spot_seeds(0, 3) == [bench.BEAM["seed"] + i for i in range(3)]
+    # the plan is reproducible and spans the batching form's ranges
+    p1, p2 = bench.plan_spots("plan512", 0, 512), bench.plan_spots("plan512", 0, 512)
+    assert p1 == p2
+    E = [b["E0"] for b in p1]
+    assert min(E) >= 70.0 and max(E) <= 230.0 and all((e - 70.0) % 2.0 == 0.0 for e in E)
+    assert all(3.0 <= b["sigma_x"] <= 6.0 and -50.0 <= b["x0"] <= 50.0 for b in p1)
