@@ -111,7 +111,7 @@ def lane_bytes(cfg):
     psi = nc * 32 * (4 + 4 * L)
     per_cell = nc * (2 * 8 + 44 + 44 + 8 + 1 + 4 + 8)
     rows = nc * 2048 + (nc // 8) * 4 * (2048 + 128 + 4)
-    bins = nc * L // 4 * 16
+    bins = nc * L // 4 * 48   # bin list (16 B) + step records (32 B)
     return psi + per_cell + rows + bins
 
 

@@ -537,6 +537,7 @@ __global__ void __launch_bounds__(1024) k_order_lists(Dev d) {
 // holds the run's total.
 template <class T>
 __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
+    if (!__any_sync(kFull, v != T(0))) return v;   // all zero: the sums are zero
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
         const T n = __shfl_down_sync(kFull, v, 1 << i);
@@ -575,7 +576,7 @@ __global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 4 : 3) k_transpo
             const int slot = (int)(r.y & 31u), sslot = (int)((r.y >> 5) & 31u), lidx = (int)((r.y >> 10) & 0xFFu);
             const bool k3 = ((r.y >> 18) & 1u) != 0;
             const unsigned salt = d.salt ? (unsigned)d.ls[ln].iter * 0x9E3779B9u : 0u;
-            transport_bin<Lay, PASS>(d, par, k3, cell, ln, cell - ln * d.Nc, r.w, slot, sslot, lidx,
+            transport_bin<Lay, PASS>(d, i, par, k3, cell, ln, cell - ln * d.Nc, r.w, slot, sslot, lidx,
                                      __uint_as_float(r.z), salt, tag, t);
         }
         if (PASS != PASS_KEYS) {
@@ -1660,6 +1661,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     // hundred thousand); a pass that needs more stops with SM2D_ERR_ALLOC
     d.bins_cap = (int)std::min<size_t>((B == 1 ? Nc * c->L : NcB * c->L / 4), (size_t)INT_MAX);
     A(d.bins, uint4, d.bins_cap);
+    A(d.brec, uint4, 2 * (size_t)d.bins_cap);
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
     A(d.gs, IterGlobal, 1);
     A(d.ls, LaneState, B);

@@ -525,9 +525,13 @@ __device__ __forceinline__ int exit_face(float x, float z, float dx, float dz) {
 
 // One component of a listed cell gc of lane ln (lane-local index lc, which
 // the random seeds use): local bin lidx of psi_in slot `slot` (sslot: the slot number
-// the seeds use).  par selects the occupancy list of psi_out (par ^ 1).
+// the seeds use), entry bi of the bin list.  par selects the occupancy list
+// of psi_out (par ^ 1).  The claim pass stores the step's outcome (new angle,
+// energy, weight, raw position, lateral sigma, deposit, nuclear loss) in the
+// bin's record; the deposit pass reads it back instead of repeating the
+// physics, so both passes emit the same arithmetic's results.
 template <class Lay, int PASS>
-__device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, int lc, uint32_t bid, int slot,
+__device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, int ln, int lc, uint32_t bid, int slot,
                               int sslot, int lidx, float w, unsigned salt, uint32_t tag, Tally& t) {
     const float dx = d.dx, dz = d.dz;
     int tl, El, xs, zs;
@@ -554,10 +558,17 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, 
         t.e_cut += (double)(E * w);
         return;
     }
-    const float xc = sub_offset(xs, Lay::NX, dx), zc = sub_offset(zs, Lay::NZ, dz);
     const float hx = dx * 0.5f, hz = dz * 0.5f;
+    float theta_new, x_new, z_new, E_new, w_new, edep, w_rem = 0.0f, sigv;
+    float4* rec = reinterpret_cast<float4*>(d.brec + 2 * (size_t)bi);
+    if (PASS != PASS_KEYS) {
+        const float4 r0 = __ldcs(rec), r1 = __ldcs(rec + 1);
+        theta_new = r0.x; E_new = r0.y; w_new = r0.z; x_new = r0.w;
+        z_new = r1.x; sigv = r1.y; edep = r1.z; w_rem = r1.w;
+    } else {
+    const float xc = sub_offset(xs, Lay::NX, dx), zc = sub_offset(zs, Lay::NZ, dz);
     const int iz = lc / d.Nx;
-    float step, dE, w_new, w_rem = 0.0f, E_rem = 0.0f, sig_th, sig_x, E_new, edep;
+    float step, dE, sig_th, sig_x;
     unsigned ts;
     if (k3) {
         // K3_FineTransport body, k3_finetransport.cu:226-366
@@ -585,7 +596,6 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, 
             const float surv = sm2d_expf(-nuclear_xs(E) * step);
             w_new = w * surv;
             w_rem = w - w_new;
-            E_rem = w_rem * E;
         }
         const float sm = fmaxf(step, 0.0f);
         const float Ap = iz < d.Nz ? d.feA[(size_t)ln * d.Nz + iz] : 0.0f;
@@ -614,7 +624,6 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, 
         const float surv = sm2d_expf(-nuclear_xs(E) * rs);
         w_new = w * surv;
         w_rem = w - w_new;
-        E_rem = w_rem * E;
         if (split && E_new > d.E_fine_on) {
             const float ex = E_new - d.E_fine_on;
             if (ex > 0.0f && w_new > 0.0f) edep += ex * w_new;
@@ -639,15 +648,21 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, 
              ((unsigned)(lidx + 1) * 3266489917u) ^ (unsigned)(Ebin + 17) ^ (ps * 747796405u) ^ salt;
     }
     const float scat = sig_th <= 0.0f ? 0.0f : normal_draw(ts) * sig_th;
-    const float theta_new = fmaxf(d.th[0], fminf(theta + scat, d.th[d.N_theta]));
-    float x_new = xc + sm2d_sinf(theta_new) * step;
-    float z_new = zc + sm2d_cosf(theta_new) * step;
+    theta_new = fmaxf(d.th[0], fminf(theta + scat, d.th[d.N_theta]));
+    x_new = xc + sm2d_sinf(theta_new) * step;
+    z_new = zc + sm2d_cosf(theta_new) * step;
+    sigv = exit_face(x_new, z_new, dx, dz) >= 0
+               ? (k3 ? 0.001f : fmaxf(sm2d_sinf(fminf(sig_th, 1.57f)) * fmaxf(step, 0.0f) / 1.7320508f, 0.01f))
+               : sig_x;
+    __stcg(rec, make_float4(theta_new, E_new, w_new, x_new));
+    __stcg(rec + 1, make_float4(z_new, sigv, edep, w_rem));
+    }
     const int face = exit_face(x_new, z_new, dx, dz);
     x_new = fmaxf(-hx, fminf(x_new, hx));
     z_new = fmaxf(-hz, fminf(z_new, hz));
     t.edep += (double)edep;
     t.w_nuc += w_rem;
-    t.e_nuc += (double)E_rem;
+    t.e_nuc += (double)(w_rem * E);
     if (E_new <= 0.1f || ((d.esplit || d.floor_cutoff) && E_new <= e_center(d, 0))) {
         t.w_cut += w_new;
         t.e_cut += (double)(E_new * w_new);
@@ -656,11 +671,9 @@ __device__ void transport_bin(const Dev& d, int par, bool k3, int cell, int ln, 
     const int my_cls = k3 ? 2 : 1;
     const Src sc{cell, slot, lidx, k3 ? 1 : 0, tag};
     if (face >= 0) {
-        const float sig_tr = k3 ? 0.001f : fmaxf(sm2d_sinf(fminf(sig_th, 1.57f)) * fmaxf(step, 0.0f) / 1.7320508f, 0.01f);
-        emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, theta_new, E_new, w_new, x_new, z_new, sig_tr, t);
+        emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, theta_new, E_new, w_new, x_new, z_new, sigv, t);
     } else {
-        emit_stay<Lay, PASS>(d, sc, par, k3, cell, theta_new, E_new, w_new, x_new, z_new, k3 ? 0.001f : sig_x, sig_x,
-                             t);
+        emit_stay<Lay, PASS>(d, sc, par, k3, cell, theta_new, E_new, w_new, x_new, z_new, k3 ? 0.001f : sigv, sigv, t);
     }
 }
 
