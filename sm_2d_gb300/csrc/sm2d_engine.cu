@@ -551,7 +551,7 @@ __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
 // increments in the dl_* arrays (one atomic per cell run of a warp) and the
 // per-lane audit sums (staged per block in shared memory).
 template <class Lay, int PASS>
-__global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 4 : 3) k_transport(Dev d) {
+__global__ void __launch_bounds__(kThreads, 4) k_transport(Dev d) {
     __shared__ LaneSums<6> s_sum;   // drop_w, drop_e, Win, Ein, Wout, Eout
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
