@@ -245,6 +245,67 @@ int sm2d_range_lut(int N, const float* rep, float* R, float* S, float* logE, flo
 /* Fermi-Eyges A(z), B(z), sigma_total(z) (k1k6_pipeline.cu:1061-1176) */
 int sm2d_fermi_eyges(float E0, int Nz, float dz, float sigma_x0, float* A, float* B, float* sigma_total);
 
+/* ---- the INI front end (run_simulation's configuration file) ---- */
+/* One run as the reference's configuration file describes it: the problem
+ * and beam GPUTransportRunner::run builds from IncidentParticleConfig
+ * (src/include/core/config_loader.hpp:98-413, src/gpu/gpu_transport_runner.cpp:28-105)
+ * and run_simulation's output settings.  The grids are owned by the config
+ * (problem.theta_edges / E_edges point into them): release them with
+ * sm2d_run_config_free. */
+typedef struct sm2d_run_config {
+    sm2d_problem problem;
+    sm2d_beam beam;
+    int max_iterations;          /* transport.max_iterations, or grid.max_steps if 0 */
+    int log_level;
+    int fail_fast_on_audit;      /* parsed; the engine books audit failures instead  */
+    int normalize_dose, save_2d, save_pdd;
+    char output_dir[1024];       /* as written; relative paths are relative to the INI */
+    char dose_2d_file[256], pdd_file[256];
+    float* theta_edges_buf;
+    float* E_edges_buf;
+} sm2d_run_config;
+/* load_incident_particle_config + validate (config_loader.hpp:324-411,
+ * incident_particle_config.hpp:274-399); SM2D_ERR_ARG with the reference's
+ * message for an unreadable file or an invalid value */
+int sm2d_load_ini(const char* ini_path, sm2d_run_config* out);
+void sm2d_run_config_free(sm2d_run_config* config);
+/* run_simulation's main (run_simulation.cpp:116-188): one spot from the INI,
+ * dose_2d.txt and pdd.txt under its output_dir.  0 on success. */
+int sm2d_run_simulation(const char* ini_path);
+
+/* ---- depth-dose metrics and output files (host; dose[Nz][Nx] as
+ * sm2d_get_dose returns it) ---- */
+/* get_depth_dose (src/validation/deterministic_beam.cpp:224-236): pdd[Nz],
+ * the double sum over x of each row */
+int sm2d_depth_dose(const double* dose, int Nx, int Nz, double* pdd);
+/* find_bragg_peak_z (deterministic_beam.cpp:207-222): the row of the largest
+ * depth dose (the first of equals; 0 if none is positive) */
+int sm2d_bragg_peak_row(const double* dose, int Nx, int Nz);
+/* src/validation/bragg_peak.cpp: out[5] = peak depth, FWHM, R80, R20 and
+ * distal falloff R20 - R80, all in mm, from float row sums */
+int sm2d_bragg_metrics(const double* dose, int Nx, int Nz, float dz, float* out);
+/* save_dose_2d / save_pdd (run_simulation.cpp:31-114): the reference's
+ * dose_2d.txt and pdd.txt files, byte for byte, with the cell centres of its
+ * runner (x = (i + 0.5) dx - Nx dx / 2, z = j dz) */
+int sm2d_write_dose_2d(const char* path, const double* dose, int Nx, int Nz, float dx, float dz, int normalize);
+int sm2d_write_pdd(const char* path, const double* dose, int Nx, int Nz, float dz, int normalize);
+
+/* ---- debug dumps in the reference's CSV formats (host; built with
+ * SM2D_ENABLE_DEBUG_DUMPS there), from a host copy of psi (sm2d_get_psi_in)
+ * and the problem's grids ---- */
+/* debug_ps_raw_iter_NN_<stage>.csv: dump_phase_space_raw_to_csv
+ * (src/cuda/k1k6_pipeline.cu:195-291, precision 8) and the initial dump of
+ * src/cuda/gpu_transport_wrapper.cu:22-120 (iteration 0, precision 6) */
+int sm2d_write_ps_raw_csv(const char* path, const sm2d_problem* p, const uint32_t* bid, const float* val,
+                          int iteration, int precision);
+/* debug_cells_iter_NN_<stage>.csv: dump_nonzero_cells_to_csv (k1k6_pipeline.cu:29-193) */
+int sm2d_write_cells_csv(const char* path, const sm2d_problem* p, const uint32_t* bid, const float* val);
+/* debug_channels_totals_iter01.csv (k1k6_pipeline.cu:2125-2155) from the 17
+ * totals of iteration 1 in the file's order; sm2d_channel_totals computes
+ * them from a single-spot engine (cell sums in cell order, then its scalars) */
+int sm2d_write_channel_totals_csv(const char* path, const double* totals17);
+int sm2d_channel_totals(sm2d_handle h, int Nx, int Nz, double* totals17);
+
 /* ---- raw stage entries on caller-owned device memory (stream may be 0) ---- */
 int sm2d_k1_active_mask(const uint32_t* d_block_ids, const float* d_values, uint8_t* d_mask,
                         const uint8_t* d_mask_prev, int Nx, int Nz, int local_bins,

@@ -1,9 +1,10 @@
 """In-tree build of libsm2d.so: the sm_103a CUDA kernels + C ABI.
 
 nvcc compiles the two CUDA translation units (the engine and the stage
-entries) for sm_103a only, g++ compiles the host tables with
--ffp-contract=off (so an Arm host gives the x86 float results), and g++
-links the shared library against the CUDA runtime.  The compiles run in
+entries) for sm_103a only, g++ compiles the host tables, the output writers
+and the INI front end with -ffp-contract=off (so an Arm host gives the x86
+float results), g++ links the shared library against the CUDA runtime, and
+gcc builds the run_simulation command over it.  The compiles run in
 parallel.  Usage: python -m sm_2d_gb300.build
 """
 from __future__ import annotations
@@ -50,7 +51,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-    cpp_obj = os.path.join(OUT, "sm2d_tables.o")
+    cpp_units = ["sm2d_tables.cpp", "sm2d_output.cpp", "sm2d_config.cpp"]
+    cpp_objs = [os.path.join(OUT, u.replace(".cpp", ".o")) for u in cpp_units]
     cu_units = ["sm2d_engine.cu", "sm2d_stages.cu"]
     cu_objs = [os.path.join(OUT, u.replace(".cu", ".o")) for u in cu_units]
     # --fmad=false: every float operation rounds on its own, as the oracle's
@@ -62,8 +64,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if ptxas_info:
         for c in cu_cmds:
             c.insert(1, "-Xptxas=-v")
-    cpp_cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-c",
-               os.path.join(CSRC, "sm2d_tables.cpp"), "-o", cpp_obj]
+    cpp_cmds = [["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-c", os.path.join(CSRC, u), "-o", o]
+                for u, o in zip(cpp_units, cpp_objs)]
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -73,14 +75,19 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             raise RuntimeError("build step failed: " + " ".join(cmd))
         return r
 
-    with ThreadPoolExecutor(len(cu_cmds) + 1) as ex:
-        for f in [ex.submit(run, c) for c in cu_cmds] + [ex.submit(run, cpp_cmd)]:
+    with ThreadPoolExecutor(len(cu_cmds) + len(cpp_cmds)) as ex:
+        for f in [ex.submit(run, c) for c in cu_cmds + cpp_cmds]:
             f.result()
     tmp = LIB + ".tmp"
-    run(["g++", "-shared", "-o", tmp, *cu_objs, cpp_obj, "-L" + os.path.join(cuda, "lib64"),
+    run(["g++", "-shared", "-o", tmp, *cu_objs, *cpp_objs, "-L" + os.path.join(cuda, "lib64"),
          "-L" + os.path.join(cuda, "targets", "sbsa-linux", "lib"), "-L" + os.path.join(cuda, "targets", "x86_64-linux", "lib"),
          "-lcudart", "-Wl,-rpath," + os.path.join(cuda, "lib64")])
     os.replace(tmp, LIB)
+    # the run_simulation command over the library
+    exe = os.path.join(OUT, "run_simulation")
+    run(["gcc", "-O2", "-std=c11", *inc, os.path.join(CSRC, "sm2d_run_simulation.c"), "-o", exe + ".tmp",
+         "-L" + OUT, "-lsm2d", "-Wl,-rpath,$ORIGIN"])
+    os.replace(exe + ".tmp", exe)
     return LIB
 
 

@@ -2,6 +2,9 @@
 #pragma once
 
 namespace sm2d {
+// Records a formatted message for sm2d_last_error() and returns `code`.
+int fail(int code, const char* fmt, ...);
+
 void energy_grid_log(float E_min, float E_max, int N, float* edges, float* rep);
 int energy_grid_piecewise(int n_groups, const float* groups, float* edges, float* rep);
 void angular_grid(float lo, float hi, int N, float* edges, float* rep);

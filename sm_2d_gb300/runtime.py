@@ -54,6 +54,14 @@ class Beam(C.Structure):
                 ("sigma_E", C.c_float), ("n_samples", C.c_int), ("seed", C.c_uint)]
 
 
+class RunConfig(C.Structure):
+    """sm2d_run_config: one run as the reference's INI file describes it."""
+    _fields_ = [("problem", Problem), ("beam", Beam), ("max_iterations", C.c_int), ("log_level", C.c_int),
+                ("fail_fast_on_audit", C.c_int), ("normalize_dose", C.c_int), ("save_2d", C.c_int),
+                ("save_pdd", C.c_int), ("output_dir", C.c_char * 1024), ("dose_2d_file", C.c_char * 256),
+                ("pdd_file", C.c_char * 256), ("theta_edges_buf", C.c_void_p), ("E_edges_buf", C.c_void_p)]
+
+
 class Audit(C.Structure):
     _fields_ = [
         ("W_error", C.c_float), ("W_pass", C.c_int), ("E_error", C.c_float), ("E_pass", C.c_int),
@@ -156,6 +164,19 @@ def lib(build_if_needed: bool = True):
         L.sm2d_batch_results.argtypes = [P, P, I]
         L.sm2d_batch_dose.argtypes = [P, P, I]
         L.sm2d_batch_audit_history.argtypes = [P, I, P, I, C.POINTER(I)]
+        L.sm2d_load_ini.argtypes = [C.c_char_p, C.POINTER(RunConfig)]
+        L.sm2d_run_config_free.argtypes = [C.POINTER(RunConfig)]
+        L.sm2d_run_config_free.restype = None
+        L.sm2d_run_simulation.argtypes = [C.c_char_p]
+        L.sm2d_write_ps_raw_csv.argtypes = [C.c_char_p, C.POINTER(Problem), P, P, I, I]
+        L.sm2d_write_cells_csv.argtypes = [C.c_char_p, C.POINTER(Problem), P, P]
+        L.sm2d_write_channel_totals_csv.argtypes = [C.c_char_p, P]
+        L.sm2d_channel_totals.argtypes = [P, I, I, P]
+        L.sm2d_depth_dose.argtypes = [P, I, I, P]
+        L.sm2d_bragg_peak_row.argtypes = [P, I, I]
+        L.sm2d_bragg_metrics.argtypes = [P, I, I, F, P]
+        L.sm2d_write_dose_2d.argtypes = [C.c_char_p, P, I, I, F, F, I]
+        L.sm2d_write_pdd.argtypes = [C.c_char_p, P, I, I, F, I]
         L.sm2d_plan_load.argtypes = [P, P, I, I, I]
         L.sm2d_plan_run_async.argtypes = [P]
         L.sm2d_plan_results.argtypes = [P, P, P]
@@ -263,6 +284,25 @@ class Config:
             self.split_min_weight = 1e-7
         return self
 
+    def _problem(self):
+        """The sm2d_problem of this config and the edge arrays it points into
+        (keep them alive while the struct is used)."""
+        th = np.ascontiguousarray(self.theta_edges, np.float32)
+        E = np.ascontiguousarray(self.E_edges, np.float32)
+        p = Problem(Nx=self.Nx, Nz=self.Nz, dx=self.dx, dz=self.dz, x_min=self.x_min, z_min=self.z_min,
+                    N_theta=th.size - 1, theta_edges=th.ctypes.data, N_E=E.size - 1, E_edges=E.ctypes.data,
+                    E_min=self.E_min, E_max=self.E_max, E_fine_on=self.E_fine_on, E_fine_off=self.E_fine_off,
+                    weight_active_min=self.weight_active_min, step_coarse=self.step_coarse,
+                    sigma_x_initial=self.sigma_x_initial, E0=self.E0,
+                    enable_straggling=self.enable_straggling, enable_nuclear=self.enable_nuclear,
+                    seed_slot_mode=self.seed_slot_mode, energy_split=self.energy_split,
+                    use_buckets=self.use_buckets, max_iterations=self.max_iterations,
+                    prune_coarse=self.prune_coarse, prune_fine=self.prune_fine,
+                    split_min_weight=self.split_min_weight, stop_weight_fraction=self.stop_weight_fraction,
+                    floor_cutoff=self.floor_cutoff, seed_iteration_salt=self.seed_iteration_salt, lanes=self.lanes,
+                    **self.layout)
+        return p, (th, E)
+
     def oracle_config(self):
         """The same problem as a CPU-oracle configuration dict."""
         return dict(Nx=self.Nx, Nz=self.Nz, dx=self.dx, dz=self.dz, x_min=self.x_min, z_min=self.z_min,
@@ -300,21 +340,7 @@ class Transport:
 
     def __init__(self, cfg: Config):
         self.cfg = cfg
-        self._th = np.ascontiguousarray(cfg.theta_edges, np.float32)
-        self._E = np.ascontiguousarray(cfg.E_edges, np.float32)
-        p = Problem(Nx=cfg.Nx, Nz=cfg.Nz, dx=cfg.dx, dz=cfg.dz, x_min=cfg.x_min, z_min=cfg.z_min,
-                    N_theta=self._th.size - 1, theta_edges=self._th.ctypes.data,
-                    N_E=self._E.size - 1, E_edges=self._E.ctypes.data, E_min=cfg.E_min, E_max=cfg.E_max,
-                    E_fine_on=cfg.E_fine_on, E_fine_off=cfg.E_fine_off,
-                    weight_active_min=cfg.weight_active_min, step_coarse=cfg.step_coarse,
-                    sigma_x_initial=cfg.sigma_x_initial, E0=cfg.E0,
-                    enable_straggling=cfg.enable_straggling, enable_nuclear=cfg.enable_nuclear,
-                    seed_slot_mode=cfg.seed_slot_mode, energy_split=cfg.energy_split,
-                    use_buckets=cfg.use_buckets, max_iterations=cfg.max_iterations,
-                    prune_coarse=cfg.prune_coarse, prune_fine=cfg.prune_fine,
-                    split_min_weight=cfg.split_min_weight, stop_weight_fraction=cfg.stop_weight_fraction,
-                    floor_cutoff=cfg.floor_cutoff, seed_iteration_salt=cfg.seed_iteration_salt, lanes=cfg.lanes,
-                    **cfg.layout)
+        p, (self._th, self._E) = cfg._problem()
         h = C.c_void_p()
         self._lib = lib()
         check(self._lib.sm2d_create(C.byref(p), C.byref(h)))
@@ -407,6 +433,13 @@ class Transport:
         n = C.c_int()
         check(self._lib.sm2d_get_audit_history(self.h, C.cast(arr, C.c_void_p), n_max, C.byref(n)))
         return [arr[i].as_dict() for i in range(n.value)]
+
+    def channel_totals(self):
+        """The 17 channel totals of debug_channels_totals_iter01.csv
+        (sm2d_channel_totals; CHANNELS order)."""
+        out = np.zeros(17)
+        check(self._lib.sm2d_channel_totals(self.h, self.cfg.Nx, self.cfg.Nz, _p(out)))
+        return out
 
     def scalars(self):
         s = np.zeros(len(SCALAR_KEYS))
@@ -519,16 +552,113 @@ def math_eval(name: str, x) -> np.ndarray:
     return y
 
 
+def load_ini(path: str) -> tuple:
+    """The reference's INI file as (Config, Beam, dict of run settings)
+    (sm2d_load_ini: config_loader.hpp:324-411 and the runner's mapping)."""
+    rc = RunConfig()
+    check(lib().sm2d_load_ini(os.fsencode(path), C.byref(rc)))
+    try:
+        p = rc.problem
+        th = np.ctypeslib.as_array(C.cast(p.theta_edges, C.POINTER(C.c_float)), (p.N_theta + 1,)).copy()
+        ee = np.ctypeslib.as_array(C.cast(p.E_edges, C.POINTER(C.c_float)), (p.N_E + 1,)).copy()
+        layout = dict(nt_local=p.nt_local, ne_local=p.ne_local, nx_sub=p.nx_sub, nz_sub=p.nz_sub)
+        cfg = Config(Nx=p.Nx, Nz=p.Nz, dx=p.dx, dz=p.dz, theta_edges=th, E_edges=ee, E_min=p.E_min, E_max=p.E_max,
+                     x_min=p.x_min, z_min=p.z_min, layout=layout, E_fine_on=p.E_fine_on, E_fine_off=p.E_fine_off,
+                     weight_active_min=p.weight_active_min, step_coarse=p.step_coarse,
+                     sigma_x_initial=p.sigma_x_initial, E0=p.E0, max_iterations=p.max_iterations)
+        b = rc.beam
+        beam = Beam(b.x0, b.z0, b.theta0, b.E0, b.W_total, b.sigma_x, b.sigma_theta, b.sigma_E, b.n_samples, b.seed)
+        run = dict(max_iterations=rc.max_iterations, log_level=rc.log_level,
+                   fail_fast_on_audit=bool(rc.fail_fast_on_audit), normalize_dose=bool(rc.normalize_dose),
+                   save_2d=bool(rc.save_2d), save_pdd=bool(rc.save_pdd), output_dir=rc.output_dir.decode(),
+                   dose_2d_file=rc.dose_2d_file.decode(), pdd_file=rc.pdd_file.decode())
+    finally:
+        lib().sm2d_run_config_free(C.byref(rc))
+    return cfg, beam, run
+
+
+def run_simulation(path: str):
+    """run_simulation's main over the GPU engine (sm2d_run_simulation)."""
+    check(lib().sm2d_run_simulation(os.fsencode(path)))
+
+
+CHANNELS = ["EdepC", "AbsorbedWeight_cutoff", "AbsorbedEnergy_cutoff", "AbsorbedWeight_nuclear",
+            "AbsorbedEnergy_nuclear", "BoundaryLoss_weight", "BoundaryLoss_energy", "transport_dropped_weight",
+            "transport_dropped_energy", "transport_audit_residual_energy", "source_injected_weight",
+            "source_out_of_grid_weight", "source_slot_dropped_weight", "source_injected_energy",
+            "source_out_of_grid_energy", "source_slot_dropped_energy", "source_representation_loss_energy"]
+
+
+def write_ps_raw_csv(path: str, cfg: "Config", bid: np.ndarray, val: np.ndarray, iteration: int,
+                     precision: int = 8):
+    """debug_ps_raw_iter_NN_<stage>.csv of psi (bid [cells*32], val
+    [cells*32*L]) on cfg's grids (sm2d_write_ps_raw_csv)."""
+    p, keep = cfg._problem()
+    b = np.ascontiguousarray(bid, np.uint32)
+    v = np.ascontiguousarray(val, np.float32)
+    check(lib().sm2d_write_ps_raw_csv(os.fsencode(path), C.byref(p), _p(b), _p(v), int(iteration), int(precision)))
+
+
+def write_cells_csv(path: str, cfg: "Config", bid: np.ndarray, val: np.ndarray):
+    """debug_cells_iter_NN_<stage>.csv (sm2d_write_cells_csv)."""
+    p, keep = cfg._problem()
+    b = np.ascontiguousarray(bid, np.uint32)
+    v = np.ascontiguousarray(val, np.float32)
+    check(lib().sm2d_write_cells_csv(os.fsencode(path), C.byref(p), _p(b), _p(v)))
+
+
+def write_channel_totals_csv(path: str, totals):
+    """debug_channels_totals_iter01.csv from the 17 totals (CHANNELS order)."""
+    t = np.ascontiguousarray(totals, np.float64)
+    if t.shape != (17,):
+        raise ValueError("17 channel totals expected")
+    check(lib().sm2d_write_channel_totals_csv(os.fsencode(path), _p(t)))
+
+
+def _grid(dose_2d):
+    d = np.ascontiguousarray(dose_2d, np.float64)
+    if d.ndim != 2:
+        raise ValueError("dose grid must be [Nz, Nx]")
+    return d, d.shape[1], d.shape[0]
+
+
 def depth_dose(dose_2d: np.ndarray) -> np.ndarray:
-    """get_depth_dose (src/validation/deterministic_beam.cpp:227-236): sum over x."""
-    return np.asarray(dose_2d).sum(axis=1)
+    """get_depth_dose (src/validation/deterministic_beam.cpp:224-236): the
+    sum over x of each row, in column order (sm2d_depth_dose)."""
+    d, nx, nz = _grid(dose_2d)
+    out = np.zeros(nz)
+    check(lib().sm2d_depth_dose(_p(d), nx, nz, _p(out)))
+    return out
 
 
 def bragg_peak_row(dose_2d: np.ndarray) -> int:
-    """find_bragg_peak_z (deterministic_beam.cpp:207-225): first row of the maximum."""
-    pdd = depth_dose(dose_2d)
-    best, row = 0.0, 0
-    for j, v in enumerate(pdd):
-        if v > best:
-            best, row = v, j
-    return row
+    """find_bragg_peak_z (deterministic_beam.cpp:207-222): the first row of
+    the largest depth dose (sm2d_bragg_peak_row)."""
+    d, nx, nz = _grid(dose_2d)
+    r = lib().sm2d_bragg_peak_row(_p(d), nx, nz)
+    check(min(r, 0))
+    return r
+
+
+BRAGG_KEYS = ("peak_mm", "fwhm_mm", "r80_mm", "r20_mm", "distal_falloff_mm")
+
+
+def bragg_metrics(dose_2d: np.ndarray, dz: float) -> dict:
+    """Bragg-peak depth, FWHM, R80, R20 and distal falloff in mm
+    (src/validation/bragg_peak.cpp; sm2d_bragg_metrics)."""
+    d, nx, nz = _grid(dose_2d)
+    out = np.zeros(5, np.float32)
+    check(lib().sm2d_bragg_metrics(_p(d), nx, nz, float(dz), _p(out)))
+    return dict(zip(BRAGG_KEYS, (float(v) for v in out)))
+
+
+def write_dose_2d(path: str, dose_2d: np.ndarray, dx: float, dz: float, normalize: bool = True):
+    """The reference's dose_2d.txt (run_simulation.cpp:31-75; sm2d_write_dose_2d)."""
+    d, nx, nz = _grid(dose_2d)
+    check(lib().sm2d_write_dose_2d(os.fsencode(path), _p(d), nx, nz, float(dx), float(dz), 1 if normalize else 0))
+
+
+def write_pdd(path: str, dose_2d: np.ndarray, dz: float, normalize: bool = True):
+    """The reference's pdd.txt (run_simulation.cpp:80-114; sm2d_write_pdd)."""
+    d, nx, nz = _grid(dose_2d)
+    check(lib().sm2d_write_pdd(os.fsencode(path), _p(d), nx, nz, float(dz), 1 if normalize else 0))
