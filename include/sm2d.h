@@ -88,6 +88,12 @@ typedef struct sm2d_problem {
     /* engine shape */
     int lanes;                   /* spots transported together by sm2d_batch_run
                                     (0 or 1: one; the single-spot entries use lane 0) */
+    /* slab phantom (no counterpart in the reference, which transports water):
+     * density of each depth row [Nz] in g/cm^3, or NULL for water.  Energy
+     * loss, range limits, straggling, nuclear attenuation and the Highland
+     * thickness use the water-equivalent path rho * step; the Fermi-Eyges
+     * tables are integrated through the phantom. */
+    const float* density_z;
 } sm2d_problem;
 
 typedef struct sm2d_beam {
@@ -244,6 +250,9 @@ int sm2d_angular_grid(float theta_min, float theta_max, int N, float* edges, flo
 int sm2d_range_lut(int N, const float* rep, float* R, float* S, float* logE, float* logR, float* logS);
 /* Fermi-Eyges A(z), B(z), sigma_total(z) (k1k6_pipeline.cu:1061-1176) */
 int sm2d_fermi_eyges(float E0, int Nz, float dz, float sigma_x0, float* A, float* B, float* sigma_total);
+/* the same through a slab phantom (density_z[Nz], as in sm2d_problem) */
+int sm2d_fermi_eyges_density(float E0, int Nz, float dz, float sigma_x0, const float* density_z, float* A, float* B,
+                             float* sigma_total);
 
 /* ---- the INI front end (run_simulation's configuration file) ---- */
 /* One run as the reference's configuration file describes it: the problem

@@ -96,6 +96,8 @@ def _lib(fp64: bool):
         lib.orc_angular_grid.argtypes = [C.c_float, C.c_float, C.c_int, P, P]
         lib.orc_generate_rlut.argtypes = [C.c_int] + [P] * 6
         lib.orc_fe_precompute.argtypes = [C.c_float, C.c_int, C.c_float, C.c_float, P, P, P]
+        lib.orc_fe_precompute_density.argtypes = [C.c_float, C.c_int, C.c_float, C.c_float, P, P, P, P]
+        lib.orc_set_density.argtypes = [P, P]
         lib.orc_postprocess.argtypes = [P, P, C.c_float, C.c_int, C.c_int, C.c_float, P]
         lib.orc_math.argtypes = [C.c_int, P, P, C.c_int]
         _LIBS[key] = lib
@@ -142,10 +144,15 @@ def generate_rlut(rep):
     return dict(zip(["R", "S", "logE", "logR", "logS"], out))
 
 
-def fe_precompute(E0, Nz, dz, sigma_x0):
+def fe_precompute(E0, Nz, dz, sigma_x0, rho=None):
+    """Fermi-Eyges A, B, sigma_total; through a density per depth row when rho is given."""
     lib = _lib(False)
     A, B, S = (np.zeros(Nz, np.float32) for _ in range(3))
-    lib.orc_fe_precompute(E0, Nz, dz, sigma_x0, _p(A), _p(B), _p(S))
+    if rho is None:
+        lib.orc_fe_precompute(E0, Nz, dz, sigma_x0, _p(A), _p(B), _p(S))
+    else:
+        r = np.ascontiguousarray(rho, np.float32)
+        lib.orc_fe_precompute_density(E0, Nz, dz, sigma_x0, _p(r), _p(A), _p(B), _p(S))
     return A, B, S
 
 
@@ -201,6 +208,15 @@ class Oracle:
                n_samples=1, seed=42):
         self.lib.orc_inject(self.ctx, x0, z0, theta0, E0, W, sigma_x, sigma_theta, sigma_E,
                             int(n_samples), int(seed) & 0xFFFFFFFF)
+
+    def set_density(self, rho):
+        """Slab phantom: density per depth row (None: water)."""
+        if rho is None:
+            self.lib.orc_set_density(self.ctx, None)
+            return
+        self._rho = np.ascontiguousarray(rho, np.float32)
+        assert self._rho.size == self.Nz
+        self.lib.orc_set_density(self.ctx, _p(self._rho))
 
     def set_psi_in(self, bid, val):
         bid = np.ascontiguousarray(bid, np.uint32)

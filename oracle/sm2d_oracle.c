@@ -105,6 +105,9 @@ struct orc_ctx {
     real* E_edges;                /* [N_E+1] */
     rlut lut;
     float *fe_A, *fe_B, *fe_sigma;
+    /* density of each depth row (slab phantom; NULL: water) and the
+     * water-equivalent depth of each row's upper face */
+    float *rho, *wet;
     psi_buf buf[2];
     int in_idx;                   /* which buffer is psi_in */
     uint8_t *mask, *mask_prev;
@@ -299,8 +302,11 @@ static float highland_f(float E, float ds) {
     return (13.6f * 1.0f / (beta * p)) * sqrtf(t) * br;
 }
 
-/* Fermi-Eyges precompute of A(z), B(z), sigma_total(z): k1k6_pipeline.cu:1061-1176 */
-void orc_fe_precompute(float E0, int Nz, float dz, float sx0, float* A, float* B, float* sig) {
+/* Fermi-Eyges precompute of A(z), B(z), sigma_total(z): k1k6_pipeline.cu:1061-1176.
+ * With a density per row (rho, NULL: water) each row's energy loss and
+ * scattering thickness are its water-equivalent path rho dz. */
+void orc_fe_precompute_density(float E0, int Nz, float dz, float sx0, const float* rho, float* A, float* B,
+                               float* sig) {
     for (int i = 0; i < Nz; ++i) { A[i] = 0.0f; B[i] = 0.0f; sig[i] = sx0; }
     if (!(E0 > 0.0f)) {
         for (int i = 0; i < Nz; ++i) sig[i] = 0.0f;
@@ -319,11 +325,12 @@ void orc_fe_precompute(float E0, int Nz, float dz, float sx0, float* A, float* B
         A[iz] = Aa;
         B[iz] = Ba;
         if (Ec <= 0.5f) break;
-        float dE = host_energy_deposition(&h, Ec, dz);
+        const float rw = (rho ? rho[iz] : 1.0f) * dz;
+        float dE = host_energy_deposition(&h, Ec, rw);
         dE = fminf(dE, Ec - 0.1f);
         float Em = Ec - 0.5f * dE;
         if (Em < 0.5f) Em = 0.5f;
-        float s = highland_f(Em, dz);
+        float s = highland_f(Em, rw);
         float T = s * s / dz;
         float Ao = Aa;
         Aa = Ao + T * dz;
@@ -339,10 +346,11 @@ void orc_fe_precompute(float E0, int Nz, float dz, float sx0, float* A, float* B
             for (int j = iz + 1; j < Nz; ++j) sig[j] = sig[iz];
             break;
         }
-        float dE = host_energy_deposition(&h, Et, dz);
+        const float rw = (rho ? rho[iz] : 1.0f) * dz;
+        float dE = host_energy_deposition(&h, Et, rw);
         dE = fminf(dE, Et - 0.1f);
         float Em = fmaxf(0.5f, Et - 0.5f * dE);
-        float s = highland_f(Em, dz);
+        float s = highland_f(Em, rw);
         float T = s * s / dz;
         float dC = 2.0f * Bt * dz + At * dz * dz + T * dz * dz * dz / 3.0f;
         C += dC;
@@ -352,6 +360,10 @@ void orc_fe_precompute(float E0, int Nz, float dz, float sx0, float* A, float* B
         Et -= dE;
         if (Et < 0.1f) Et = 0.1f;
     }
+}
+
+void orc_fe_precompute(float E0, int Nz, float dz, float sx0, float* A, float* B, float* sig) {
+    orc_fe_precompute_density(E0, Nz, dz, sx0, NULL, A, B, sig);
 }
 
 /* Post-process lateral convolution: gpu_transport_wrapper.cu:551-616 */
@@ -560,11 +572,14 @@ static void spread_weights_subcell(real* w, real xm, real sigma, real dx, int N)
         for (int i = 0; i < N; ++i) w[i] = (i == N / 2) ? RL(1.0) : RL(0.0);
     }
 }
-static real scattering_T(real E, real ds) {
-    real th = highland(E, ds);
+/* scattering power per geometric mm in a medium of density rho: Highland
+ * angle of the water-equivalent thickness rho ds */
+static real scattering_T(real E, real ds, real rho) {
+    real th = highland(E, rho * ds);
     if (ds < RL(1e-6)) return RL(0.0);
     return th * th / ds;
 }
+static real rho_of(const orc_ctx* c, int iz) { return c->rho ? (real)c->rho[iz] : RL(1.0); }
 
 /* ------------------------------------------------------------------------- */
 /* slot tables: device_psic.cuh:163-292, device_bucket.cuh:61-128           */
@@ -1038,38 +1053,41 @@ static void k2_cell(orc_ctx* c, int cell) {
             real rstep = step_lim;
             int split = 0;
             real Efo = (real)c->cfg.E_fine_on;
+            const int iz = cell / Nx;
+            const real rho = rho_of(c, iz);
             if (E > Efo + RL(1e-6)) {
                 real Rc = lut_R(lut, E);
                 real Rf = lut_R(lut, r_max(Efo, (real)lut->Emin));
-                real rtf = Rc - Rf;
+                real rtf = (Rc - Rf) / rho;   /* geometric distance to the fine threshold */
                 if (rtf > RL(0.0) && rtf < rstep) {
                     rstep = rtf;
                     step_lim = rstep;
                     split = 1;
                 }
             }
-            real dE = lut_energy_deposition(lut, E, rstep);
+            real dE = lut_energy_deposition(lut, E, rho * rstep);
             dE = r_min(dE, E);
             real E_new = E - dE;
             real edep = dE * w;
             real w_rem, E_rem;
-            real w_new = nuclear_atten(w, E, rstep, &w_rem, &E_rem);
+            real w_new = nuclear_atten(w, E, rho * rstep, &w_rem, &E_rem);
             if (split && E_new > Efo) {
                 real ex = E_new - Efo;
                 if (ex > RL(0.0) && w_new > RL(0.0)) edep += ex * w_new;
                 E_new = Efo;
             }
-            int iz = cell / Nx;
             real path0 = r_max(RL(0.0), (real)iz * dz + (zc + RL(0.5) * dz));
+            /* scattering accumulated over the water-equivalent depth */
+            real path0w = c->rho ? r_max(RL(0.0), (real)c->wet[iz] + rho * (zc + RL(0.5) * dz)) : path0;
             real step_mm = r_max(rstep, RL(0.0));
             real sts = RL(0.0);
-            if (path0 > RL(0.0)) sts = highland(E, path0);
+            if (path0 > RL(0.0)) sts = highland(E, path0w);
             real A_old = sts * sts;
             real B_old = RL(0.5) * A_old * path0;
             real sx0 = (real)c->cfg.sigma_x_initial;
             real C_old = sx0 * sx0 + (A_old * path0 * path0) / RL(3.0);
             real E_mid = r_max(E - RL(0.5) * dE, (real)lut->Emin);
-            real T = scattering_T(E_mid, step_mm);
+            real T = scattering_T(E_mid, step_mm, rho);
             /* device_fermi_eyges_step */
             real A_new = A_old + T * step_mm;
             real C_new = C_old + RL(2.0) * B_old * step_mm + A_old * step_mm * step_mm
@@ -1158,13 +1176,15 @@ static void k3_cell(orc_ctx* c, int cell) {
             real sxm = (eta0 < 0) ? (-hx - xc) / eta0 : RL(1e30);
             real sb = r_min(r_min(szp, szm), r_min(sxp, sxm));
             sb = r_max(sb, RL(0.0));
-            real sphys = max_step(lut, E);
+            const int iz = cell / Nx;
+            const real rho = rho_of(c, iz);
+            real sphys = max_step(lut, E) / rho;   /* the water-equivalent limit as a geometric step */
             real step = r_min(sphys, sb * BOUNDARY_SAFETY);
-            real mean_dE = lut_energy_deposition(lut, E, step);
+            real mean_dE = lut_energy_deposition(lut, E, rho * step);
             real dE;
             if (c->cfg.enable_straggling) {
                 unsigned seed = ((unsigned)(cell * 7 + sslot * 13 + l * 17) ^ 0xDEECE66Du) ^ iter_salt(c);
-                real sE = straggling_sigma(E, step, RL(1.0));
+                real sE = straggling_sigma(E, step, rho);
                 if (sE <= RL(0.0)) dE = mean_dE;
                 else {
                     real z = gauss_sample(&seed);
@@ -1177,13 +1197,12 @@ static void k3_cell(orc_ctx* c, int cell) {
             real E_new = E - dE;
             real edep = dE * w;
             real w_rem = RL(0.0), E_rem = RL(0.0), w_new = w;
-            if (c->cfg.enable_nuclear) w_new = nuclear_atten(w, E, step, &w_rem, &E_rem);
-            int iz = cell / Nx;
+            if (c->cfg.enable_nuclear) w_new = nuclear_atten(w, E, rho * step, &w_rem, &E_rem);
             real step_mm = r_max(step, RL(0.0));
             real Ap = (c->fe_A && iz >= 0 && iz < Nz) ? (real)c->fe_A[iz] : RL(0.0);
             real Bp = (c->fe_B && iz >= 0 && iz < Nz) ? (real)c->fe_B[iz] : RL(0.0);
             real E_mid = r_max(E - RL(0.5) * dE, (real)lut->Emin);
-            real T = scattering_T(E_mid, step_mm);
+            real T = scattering_T(E_mid, step_mm, rho);
             real sig_th = r_sqrt(r_max(T * step_mm, RL(0.0)));
             real dC = RL(2.0) * Bp * step_mm + Ap * step_mm * step_mm + T * step_mm * step_mm * step_mm / RL(3.0);
             dC = r_max(dC, RL(0.0));
@@ -1718,6 +1737,7 @@ void orc_destroy(orc_ctx* c) {
     free(c->th_edges); free(c->E_edges);
     free(c->lut.R); free(c->lut.S); free(c->lut.logE); free(c->lut.logR); free(c->lut.logS);
     free(c->fe_A); free(c->fe_B); free(c->fe_sigma);
+    free(c->rho); free(c->wet);
     for (int b = 0; b < 2; ++b) { free(c->buf[b].bid); free(c->buf[b].val); free(c->buf[b].occ); }
     free(c->mask); free(c->mask_prev); free(c->active); free(c->coarse);
     free(c->edep); free(c->e_cut); free(c->e_nuc); free(c->e_bnd);
@@ -1736,6 +1756,26 @@ void orc_destroy(orc_ctx* c) {
 
 int orc_local_bins(const orc_ctx* c) { return c->L; }
 int orc_slots_per_cell(const orc_ctx* c) { return c->Kb; }
+
+/* Slab phantom: density of each depth row (NULL: water again).  Recomputes
+ * the Fermi-Eyges tables through the phantom. */
+void orc_set_density(orc_ctx* c, const float* rho) {
+    free(c->rho); free(c->wet);
+    c->rho = c->wet = NULL;
+    if (rho) {
+        const int Nz = c->cfg.Nz;
+        c->rho = (float*)malloc(sizeof(float) * Nz);
+        c->wet = (float*)malloc(sizeof(float) * Nz);
+        memcpy(c->rho, rho, sizeof(float) * Nz);
+        float acc = 0.0f;
+        for (int iz = 0; iz < Nz; ++iz) {
+            c->wet[iz] = acc;
+            acc += rho[iz] * c->cfg.dz;
+        }
+    }
+    orc_fe_precompute_density(c->cfg.E0, c->cfg.Nz, c->cfg.dz, c->cfg.sigma_x_initial, c->rho, c->fe_A, c->fe_B,
+                              c->fe_sigma);
+}
 
 void orc_set_psi_in(orc_ctx* c, const uint32_t* bid, const orc_real* val) {
     psi_buf* p = psi_in(c);

@@ -96,6 +96,9 @@ void orc_generate_rlut(int N_E, const float* rep, float* R, float* S,
                        float* logE, float* logR, float* logS);
 void orc_fe_precompute(float E0, int Nz, float dz, float sigma_x0,
                        float* A, float* B, float* sigma_total);
+/* the same through a density per depth row (rho[Nz]; NULL: water) */
+void orc_fe_precompute_density(float E0, int Nz, float dz, float sigma_x0, const float* rho,
+                               float* A, float* B, float* sigma_total);
 void orc_postprocess(const double* edep_in, const float* sigma_total, float sigma_x0,
                      int Nx, int Nz, float dx, double* edep_out);
 /* the transport's elementary functions (0 exp, 1 log, 2 sin, 3 cos, 4 erf)
@@ -115,6 +118,10 @@ void orc_inject(orc_ctx* c, float x0, float z0, float theta0, float E0, float W_
                 int n_samples, unsigned seed);
 /* overwrite psi_in directly (golden inputs); values are orc_real */
 void orc_set_psi_in(orc_ctx* c, const uint32_t* bid, const orc_real* val);
+/* slab phantom: the density of each depth row (rho[Nz]; NULL: water).  Energy
+ * loss, range limits, straggling, nuclear attenuation and scattering use the
+ * water-equivalent path rho * step; the Fermi-Eyges tables are recomputed. */
+void orc_set_density(orc_ctx* c, const float* rho);
 void orc_get_psi_in(const orc_ctx* c, uint32_t* bid, orc_real* val);
 
 /* one K1..K6 iteration; returns 1 if work was done, 0 if transport finished */

@@ -131,6 +131,9 @@ struct Dev {
     // per lane: Fermi-Eyges moments A(z), B(z), sigma_total(z) [B][Nz] of the
     // lane's beam (k1k6_pipeline.cu:1061-1206) and its initial sigma_x [B]
     float *feA, *feB, *feS, *sx0;
+    // slab phantom: density of each depth row and the water-equivalent depth
+    // of each row's upper face [Nz]; null for water
+    const float *rho, *wet;
     float E_fine_on, wmin, step_coarse;
     int b_on, b_off;
     int straggle, nuclear, seed_mode, esplit;
@@ -253,8 +256,10 @@ __device__ __forceinline__ float highland(float E, float ds) {
     float br = fmaxf(1.0f + 0.038f * sm2d_logf(t), 0.25f);
     return (13.6f * 1.0f / (beta * p)) * sqrtf(t) * br;
 }
-__device__ __forceinline__ float scatter_power(float E, float ds) {
-    float th = highland(E, ds);
+// scattering power per geometric mm in a medium of density rho: the
+// Highland angle of the water-equivalent thickness rho ds
+__device__ __forceinline__ float scatter_power(float E, float ds, float rho) {
+    float th = highland(E, rho * ds);
     if (ds < 1e-6f) return 0.0f;
     return th * th / ds;
 }

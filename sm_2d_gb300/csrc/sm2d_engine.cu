@@ -1230,6 +1230,7 @@ struct Ctx {
     // per-lane Fermi-Eyges tables: host copy [feA B*Nz | feB B*Nz | feS B*Nz |
     // sigma_x B] of fe_dev, and the (E0, sigma_x) each lane's tables are for
     std::vector<float> fe_host, fe_E0, fe_sx;
+    std::vector<float> rho_host;    // slab phantom: density per depth row (empty: water)
     float* fe_dev = nullptr;
     int fe_lo = 0, fe_hi = -1;      // lanes whose tables changed since the last upload
     int L = 0, layout = 0;  // 0: LayoutRef, 1: LayoutB128
@@ -1464,7 +1465,7 @@ static void set_lane_fe(Ctx& c, int ln, float E0, float sx) {
     const int Nz = c.d.Nz;
     const size_t BN = (size_t)c.B * Nz;
     float* A = c.fe_host.data() + (size_t)ln * Nz;
-    fermi_eyges_moments(E0, Nz, c.d.dz, sx, A, A + BN, A + 2 * BN);
+    fermi_eyges_moments(E0, Nz, c.d.dz, sx, A, A + BN, A + 2 * BN, c.rho_host.empty() ? nullptr : c.rho_host.data());
     c.fe_host[3 * BN + ln] = sx;
     c.fe_E0[ln] = E0;
     c.fe_sx[ln] = sx;
@@ -1556,6 +1557,10 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
                      p->nt_local, p->ne_local, p->nx_sub, p->nz_sub);
     if (p->N_theta / p->nt_local > 4095 || p->N_E / p->ne_local > 4095)
         return fail(SM2D_ERR_ARG, "grid exceeds the 12-bit block indices");
+    if (p->density_z)
+        for (int iz = 0; iz < p->Nz; ++iz)
+            if (!(p->density_z[iz] > 0.0f) || !std::isfinite(p->density_z[iz]))
+                return fail(SM2D_ERR_ARG, "density of row %d must be positive", iz);
     sm2d_ctx* c = new sm2d_ctx();
     c->p = *p;
     c->layout = layout;
@@ -1572,10 +1577,12 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     std::vector<float> rep(N), R(N), S(N), lE(N), lR(N), lS(N);
     for (int i = 0; i < N; ++i) rep[i] = std::sqrt(c->Ee[i] * c->Ee[i + 1]);
     range_lut(N, rep.data(), R.data(), S.data(), lE.data(), lR.data(), lS.data());
+    if (p->density_z) c->rho_host.assign(p->density_z, p->density_z + p->Nz);
     c->feA.resize(p->Nz);
     c->feB.resize(p->Nz);
     c->feS.resize(p->Nz);
-    fermi_eyges_moments(p->E0, p->Nz, p->dz, p->sigma_x_initial, c->feA.data(), c->feB.data(), c->feS.data());
+    fermi_eyges_moments(p->E0, p->Nz, p->dz, p->sigma_x_initial, c->feA.data(), c->feB.data(), c->feS.data(),
+                        p->density_z ? c->rho_host.data() : nullptr);
     Dev& d = c->d;
     d.Nx = p->Nx; d.Nz = p->Nz; d.Nc = p->Nx * p->Nz; d.B = B;
     d.dx = p->dx; d.dz = p->dz;
@@ -1637,6 +1644,21 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(r_slot, int, rt.size());
     d.e_slot = e_slot;
     d.r_slot = r_slot;
+    // slab phantom: density and water-equivalent depth of each row's upper face
+    std::vector<float> wet;
+    float *rho_d = nullptr, *wet_d = nullptr;
+    if (!c->rho_host.empty()) {
+        wet.resize(p->Nz);
+        float acc = 0.0f;
+        for (int iz = 0; iz < p->Nz; ++iz) {
+            wet[iz] = acc;
+            acc += c->rho_host[iz] * p->dz;
+        }
+        A(rho_d, float, p->Nz);
+        A(wet_d, float, p->Nz);
+    }
+    d.rho = rho_d;
+    d.wet = wet_d;
     const size_t BN = (size_t)B * p->Nz;
     A(c->fe_dev, float, 3 * BN + B);
     d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d;
@@ -1702,6 +1724,9 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
               cudaMemcpyAsync(lR_d, lR.data(), sizeof(float) * N, cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(e_slot, et.data(), sizeof(int) * et.size(), cudaMemcpyHostToDevice, s) == cudaSuccess &&
               cudaMemcpyAsync(r_slot, rt.data(), sizeof(int) * rt.size(), cudaMemcpyHostToDevice, s) == cudaSuccess;
+    if (ok && rho_d)
+        ok = cudaMemcpyAsync(rho_d, c->rho_host.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+             cudaMemcpyAsync(wet_d, wet.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.bid, 0xFF, ns * 4, s) == cudaSuccess &&
          cudaMemsetAsync(d.val, 0, ns * c->L * 4, s) == cudaSuccess;
     for (int k = 0; k < 2 && ok; ++k) ok = cudaMemsetAsync(d.occ[k], 0, NcB * 4, s) == cudaSuccess;
@@ -2171,7 +2196,8 @@ int sm2d_plan_load(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_i
         for (size_t k = t; k < uniq.size(); k += T) {
             const int i = uniq[k];
             float* f = c.plan_fe_host.data() + per * i;
-            fermi_eyges_moments(beams[i].E0, Nz, c.d.dz, beams[i].sigma_x, f, f + Nz, f + 2 * Nz);
+            fermi_eyges_moments(beams[i].E0, Nz, c.d.dz, beams[i].sigma_x, f, f + Nz, f + 2 * Nz,
+                                c.rho_host.empty() ? nullptr : c.rho_host.data());
             f[3 * Nz] = beams[i].sigma_x;
         }
     };

@@ -441,6 +441,12 @@ int sm2d_fermi_eyges(float E0, int Nz, float dz, float sx0, float* A, float* B, 
     return 0;
 }
 
+int sm2d_fermi_eyges_density(float E0, int Nz, float dz, float sx0, const float* rho, float* A, float* B, float* S) {
+    if (Nz <= 0 || !A || !B || !S || !rho) return fail(SM2D_ERR_ARG, "invalid argument");
+    fermi_eyges_moments(E0, Nz, dz, sx0, A, B, S, rho);
+    return 0;
+}
+
 // ---------------------------------------------------------------- raw stage entries
 int sm2d_k1_active_mask(const uint32_t* bid, const float* val, uint8_t* mask, const uint8_t* prev, int Nx, int Nz,
                         int L, int b_on, int b_off, float wmin, void* stream) {

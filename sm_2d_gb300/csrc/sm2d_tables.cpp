@@ -143,8 +143,9 @@ float highland_host(float E, float ds) {  // highland.hpp:59-80
 
 // Fermi-Eyges moments A(z), B(z) and the total lateral sigma(z) along the
 // central axis: k1k6_pipeline.cu:1061-1176 (A and B stay zero past the range,
-// sigma holds its last value).
-void fermi_eyges_moments(float E0, int Nz, float dz, float sigma_x0, float* A, float* B, float* sigma) {
+// sigma holds its last value); through a slab phantom, each row's energy
+// loss and scattering use its water-equivalent thickness.
+void fermi_eyges_moments(float E0, int Nz, float dz, float sigma_x0, float* A, float* B, float* sigma, const float* rho) {
     for (int i = 0; i < Nz; ++i) { A[i] = 0.0f; B[i] = 0.0f; sigma[i] = sigma_x0; }
     if (!(E0 > 0.0f)) {
         std::fill(sigma, sigma + Nz, 0.0f);
@@ -157,10 +158,11 @@ void fermi_eyges_moments(float E0, int Nz, float dz, float sigma_x0, float* A, f
             A[iz] = a;
             B[iz] = b;
             if (E <= 0.5f) break;
-            float dE = std::min(lut.energy_loss(E, dz), E - 0.1f);
+            const float rw = (rho ? rho[iz] : 1.0f) * dz;
+            float dE = std::min(lut.energy_loss(E, rw), E - 0.1f);
             float Em = E - 0.5f * dE;
             if (Em < 0.5f) Em = 0.5f;
-            const float th = highland_host(Em, dz);
+            const float th = highland_host(Em, rw);
             const float T = th * th / dz;
             const float a_prev = a;
             a = a_prev + T * dz;
@@ -176,9 +178,10 @@ void fermi_eyges_moments(float E0, int Nz, float dz, float sigma_x0, float* A, f
             for (int j = iz + 1; j < Nz; ++j) sigma[j] = sigma[iz];
             break;
         }
-        const float dE = std::min(lut.energy_loss(E, dz), E - 0.1f);
+        const float rw = (rho ? rho[iz] : 1.0f) * dz;
+        const float dE = std::min(lut.energy_loss(E, rw), E - 0.1f);
         const float Em = std::max(0.5f, E - 0.5f * dE);
-        const float th = highland_host(Em, dz);
+        const float th = highland_host(Em, rw);
         const float T = th * th / dz;
         C += 2.0f * b * dz + a * dz * dz + T * dz * dz * dz / 3.0f;
         const float a_prev = a;

@@ -568,6 +568,10 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
     } else {
     const float xc = sub_offset(xs, Lay::NX, dx), zc = sub_offset(zs, Lay::NZ, dz);
     const int iz = lc / d.Nx;
+    // slab phantom: paths below are geometric; energy loss, range limits,
+    // straggling, nuclear attenuation and scattering thickness take the
+    // water-equivalent path rho * step (rho = 1: the water arithmetic)
+    const float rho = d.rho ? d.rho[iz] : 1.0f;
     float step, dE, sig_th, sig_x;
     unsigned ts;
     if (k3) {
@@ -579,11 +583,11 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         const float sxm = (eta0 < 0) ? (-hx - xc) / eta0 : 1e30f;
         const float sb = fmaxf(fminf(fminf(szp, szm), fminf(sxp, sxm)), 0.0f);
         const float RE = lut_range(d, E);
-        step = fminf(fine_step_limit(E, RE), sb * 1.001f);
-        const float mean_dE = lut_energy_loss(d, E, RE, step);
+        step = fminf(fine_step_limit(E, RE) / rho, sb * 1.001f);
+        const float mean_dE = lut_energy_loss(d, E, RE, rho * step);
         if (d.straggle) {
             unsigned seed = ((unsigned)(lc * 7 + sslot * 13 + lidx * 17) ^ 0xDEECE66Du) ^ salt;
-            const float sE = straggling_sigma(E, step, 1.0f);
+            const float sE = straggling_sigma(E, step, rho);
             dE = sE <= 0.0f ? mean_dE : fmaxf(mean_dE + normal_draw(seed) * sE, 0.0f);
         } else {
             dE = mean_dE;
@@ -593,14 +597,14 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         edep = dE * w;
         w_new = w;
         if (d.nuclear) {
-            const float surv = sm2d_expf(-nuclear_xs(E) * step);
+            const float surv = sm2d_expf(-nuclear_xs(E) * (rho * step));
             w_new = w * surv;
             w_rem = w - w_new;
         }
         const float sm = fmaxf(step, 0.0f);
         const float Ap = iz < d.Nz ? d.feA[(size_t)ln * d.Nz + iz] : 0.0f;
         const float Bp = iz < d.Nz ? d.feB[(size_t)ln * d.Nz + iz] : 0.0f;
-        const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm);
+        const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm, rho);
         sig_th = sqrtf(fmaxf(T * sm, 0.0f));
         const float dC = fmaxf(2.0f * Bp * sm + Ap * sm * sm + T * sm * sm * sm / 3.0f, 0.0f);
         sig_x = fmaxf(sqrtf(dC), 0.01f);
@@ -614,14 +618,14 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         bool split = false;
         const float RE = lut_range(d, E);
         if (E > d.E_fine_on + 1e-6f) {
-            const float rtf = RE - d.R_fine_on;
+            const float rtf = (RE - d.R_fine_on) / rho;   // geometric distance to the fine threshold
             if (rtf > 0.0f && rtf < rs) { rs = rtf; lim = rs; split = true; }
         }
         step = lim;
-        dE = fminf(lut_energy_loss(d, E, RE, rs), E);
+        dE = fminf(lut_energy_loss(d, E, RE, rho * rs), E);
         E_new = E - dE;
         edep = dE * w;
-        const float surv = sm2d_expf(-nuclear_xs(E) * rs);
+        const float surv = sm2d_expf(-nuclear_xs(E) * (rho * rs));
         w_new = w * surv;
         w_rem = w - w_new;
         if (split && E_new > d.E_fine_on) {
@@ -630,13 +634,15 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
             E_new = d.E_fine_on;
         }
         const float p0 = fmaxf(0.0f, (float)iz * dz + (zc + 0.5f * dz));
+        // scattering accumulated over the water-equivalent depth
+        const float p0w = d.rho ? fmaxf(0.0f, d.wet[iz] + rho * (zc + 0.5f * dz)) : p0;
         const float sm = fmaxf(rs, 0.0f);
-        const float s0 = p0 > 0.0f ? highland(E, p0) : 0.0f;
+        const float s0 = p0 > 0.0f ? highland(E, p0w) : 0.0f;
         const float A0 = s0 * s0;
         const float B0 = 0.5f * A0 * p0;
         const float sx0 = d.sx0[ln];
         const float C0 = sx0 * sx0 + (A0 * p0 * p0) / 3.0f;
-        const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm);
+        const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm, rho);
         const float A1 = fmaxf(A0 + T * sm, 0.0f);
         const float C1 = fmaxf(C0 + 2.0f * B0 * sm + A0 * sm * sm + (1.0f / 3.0f) * T * sm * sm * sm, 0.0f);
         sig_th = sqrtf(fmaxf(A1 - A0, 0.0f));

@@ -44,7 +44,7 @@ class Problem(C.Structure):
         ("max_iterations", C.c_int),
         ("prune_coarse", C.c_float), ("prune_fine", C.c_float), ("split_min_weight", C.c_float),
         ("stop_weight_fraction", C.c_float), ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
-        ("lanes", C.c_int),
+        ("lanes", C.c_int), ("density_z", C.c_void_p),
     ]
 
 
@@ -152,6 +152,7 @@ def lib(build_if_needed: bool = True):
         L.sm2d_angular_grid.argtypes = [F, F, I, P, P]
         L.sm2d_range_lut.argtypes = [I] + [P] * 6
         L.sm2d_fermi_eyges.argtypes = [F, I, F, F, P, P, P]
+        L.sm2d_fermi_eyges_density.argtypes = [F, I, F, F, P, P, P, P]
         L.sm2d_k1_active_mask.argtypes = [P, P, P, P, I, I, I, I, I, F, P]
         L.sm2d_compact_lists.argtypes = [P, P, P, I, I, I, P, P, P, P, P]
         L.sm2d_k4_bucket_transfer.argtypes = [P, P, P, P, I, I, I, I, I, I, P, I, I, P, P]
@@ -227,9 +228,15 @@ def range_lut(rep):
     return dict(zip(["R", "S", "logE", "logR", "logS"], out))
 
 
-def fermi_eyges(E0, Nz, dz, sigma_x0):
+def fermi_eyges(E0, Nz, dz, sigma_x0, density_z=None):
+    """Fermi-Eyges A, B, sigma_total along depth; through a slab phantom when
+    density_z (g/cm^3 per depth row) is given."""
     A, B, S = (np.zeros(Nz, np.float32) for _ in range(3))
-    check(lib().sm2d_fermi_eyges(E0, Nz, dz, sigma_x0, _p(A), _p(B), _p(S)))
+    if density_z is None:
+        check(lib().sm2d_fermi_eyges(E0, Nz, dz, sigma_x0, _p(A), _p(B), _p(S)))
+    else:
+        r = np.ascontiguousarray(density_z, np.float32)
+        check(lib().sm2d_fermi_eyges_density(E0, Nz, dz, sigma_x0, _p(r), _p(A), _p(B), _p(S)))
     return A, B, S
 
 
@@ -271,6 +278,7 @@ class Config:
     floor_cutoff: int = 0
     seed_iteration_salt: int = 0
     lanes: int = 1          # spots transported together by Transport.batch_run
+    density_z: np.ndarray = None   # slab phantom: density per depth row (None: water)
 
     def production(self):
         """Options of a production run: deterministic rank-ordered seeds salted
@@ -289,6 +297,9 @@ class Config:
         (keep them alive while the struct is used)."""
         th = np.ascontiguousarray(self.theta_edges, np.float32)
         E = np.ascontiguousarray(self.E_edges, np.float32)
+        rho = None if self.density_z is None else np.ascontiguousarray(self.density_z, np.float32)
+        if rho is not None and rho.size != self.Nz:
+            raise ValueError("density_z needs one value per depth row")
         p = Problem(Nx=self.Nx, Nz=self.Nz, dx=self.dx, dz=self.dz, x_min=self.x_min, z_min=self.z_min,
                     N_theta=th.size - 1, theta_edges=th.ctypes.data, N_E=E.size - 1, E_edges=E.ctypes.data,
                     E_min=self.E_min, E_max=self.E_max, E_fine_on=self.E_fine_on, E_fine_off=self.E_fine_off,
@@ -300,8 +311,8 @@ class Config:
                     prune_coarse=self.prune_coarse, prune_fine=self.prune_fine,
                     split_min_weight=self.split_min_weight, stop_weight_fraction=self.stop_weight_fraction,
                     floor_cutoff=self.floor_cutoff, seed_iteration_salt=self.seed_iteration_salt, lanes=self.lanes,
-                    **self.layout)
-        return p, (th, E)
+                    density_z=None if rho is None else rho.ctypes.data, **self.layout)
+        return p, (th, E, rho)
 
     def oracle_config(self):
         """The same problem as a CPU-oracle configuration dict."""
@@ -340,7 +351,7 @@ class Transport:
 
     def __init__(self, cfg: Config):
         self.cfg = cfg
-        p, (self._th, self._E) = cfg._problem()
+        p, (self._th, self._E, self._rho) = cfg._problem()
         h = C.c_void_p()
         self._lib = lib()
         check(self._lib.sm2d_create(C.byref(p), C.byref(h)))
