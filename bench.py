@@ -45,14 +45,38 @@ METRIC = "spots/s on 1 GB300, surrogate+batched vs plain K1–K6, at ≤1% dose 
 BEAM = dict(x0=0.0, z0=0.0, theta0=0.0, E0=150.0, W=1.0, sigma_x=3.8, sigma_theta=0.002, sigma_E=1.5,
             n_samples=1000, seed=42)
 PLAN_SEED = 2024
+PHANTOM_SEED = 7
+C3_BEAM = dict(x0=0.0, z0=0.0, theta0=0.0, E0=230.0, W=1.0, sigma_x=5.0, sigma_theta=0.002, sigma_E=1.84,
+               n_samples=1000)
 MAX_IT = 4000
 
 
 SMALL = False   # --small: 100 x 200 cells and an 80 MeV beam, for profiler captures
 
 
-def make_config(grid: str):
+def slab_phantom(Nz, dz, seed=PHANTOM_SEED):
+    """The precision form's phantom: 6-10 slabs of 5-30 mm stacked from the
+    surface, densities drawn from {0.25 (lung-like), 1.0, 1.85 (bone-like)},
+    water below them; one density per depth row."""
+    rng = np.random.default_rng(seed)
+    rho = np.ones(Nz, np.float32)
+    z = 0.0
+    for _ in range(int(rng.integers(6, 11))):
+        t = float(rng.uniform(5.0, 30.0))
+        r = float(rng.choice([0.25, 1.0, 1.85]))
+        a, b = int(round(z / dz)), int(round((z + t) / dz))
+        rho[a:min(b, Nz)] = r
+        z += t
+    return rho
+
+
+def make_config(grid: str, workload: str = "plan512"):
     import sm_2d_gb300 as sm
+    if workload == "c3" and not SMALL:
+        cfg = sm.Config.reference_runner(300, 600, 0.5, 0.5, N_theta=36, sigma_x_initial=5.0, E0=230.0)
+        cfg.density_z = slab_phantom(600, 0.5)
+        cfg.max_iterations = MAX_IT
+        return cfg.production()
     if SMALL:
         cfg = sm.Config.reference_runner(100, 200, 0.5, 0.5, N_theta=36, sigma_x_initial=BEAM["sigma_x"],
                                          E0=BEAM["E0"])
@@ -82,6 +106,8 @@ def plan_spots(workload, rank, n):
     seeds = spot_seeds(rank, n)
     if workload == "c2" or SMALL:
         return [dict(BEAM, seed=s) for s in seeds]
+    if workload == "c3":
+        return [dict(C3_BEAM, seed=s) for s in seeds]
     rng = np.random.default_rng(PLAN_SEED + rank)
     out = []
     for s in seeds:
@@ -128,6 +154,11 @@ def workload_desc(workload, grid, n_spots):
         ph = "256 log E bins 0.1-250 MeV, 512 theta bins +-pi/2, 128 local bins (8x4x4x1), energy-split method"
     else:
         ph = "reference grids: 1029 piecewise E bins, 36 theta bins +-0.35 rad, 256 local bins (4x2x8x4)"
+    if workload == "c3":
+        return (f"{n_spots} spots of a 230 MeV Gaussian beam (sigma_x 5 mm, sigma_theta 2 mrad, sigma_E 0.8% E0, 1000 "
+                f"samples, sample seeds per spot) into a slab phantom 300x600 cells @0.5 mm (6-10 slabs of 5-30 mm, "
+                f"densities 0.25/1.0/1.85, seed {PHANTOM_SEED}); {ph}; full K1-K6 + audit per iteration + lateral dose "
+                "post-convolution; each spot until in-flight weight < 1e-6 W0")
     if workload == "c2":
         spots = (f"{n_spots} spots of a 150 MeV Gaussian beam (sigma_x 3.8 mm, sigma_theta 2 mrad, sigma_E 1.5 MeV, "
                  "1000 samples, sample seeds per spot)")
@@ -190,11 +221,13 @@ def cpu_spots_per_s(grid: str, workload: str, n_threads: int, n_spots: int):
     with the Fermi-Eyges tables of its own energy and width), n_threads at a
     time; returns (spots/s, wall seconds)."""
     from oracle import oracle as orc
-    cfg = make_config(grid)
+    cfg = make_config(grid, workload)
     oracles = []
     for b in plan_spots(workload, 0, n_spots):
         oc = dict(cfg.oracle_config(), E0=b["E0"], sigma_x_initial=b["sigma_x"])
         o = orc.Oracle(oc, cfg.theta_edges, cfg.E_edges)
+        if cfg.density_z is not None:
+            o.set_density(cfg.density_z)
         o.inject(**b)
         oracles.append(o)
     t0 = time.perf_counter()
@@ -252,7 +285,7 @@ def run_gpu_arm(args):
             dist.all_reduce(torch.zeros(1, device="cuda"))
             torch.cuda.synchronize()
 
-    cfg = make_config(args.grid)
+    cfg = make_config(args.grid, args.workload)
     cfg.lanes = args.lanes if args.lanes > 0 else auto_lanes(cfg, torch.cuda.mem_get_info()[0])
     t = sm.Transport(cfg)
     B = t.lanes
@@ -397,11 +430,13 @@ def main():
     ap.add_argument("--grid", default="reference", choices=["reference", "log"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--lanes", type=int, default=0, help="spots in flight (0: from free device memory)")
-    ap.add_argument("--workload", default="plan512", choices=["plan512", "c2"])
-    ap.add_argument("--spots", type=int, default=512, help="spots per step (the plan)")
+    ap.add_argument("--workload", default="plan512", choices=["plan512", "c2", "c3"])
+    ap.add_argument("--spots", type=int, default=0, help="spots per step, the plan (0: 512; 64 for c3)")
     ap.add_argument("--small", action="store_true",
                     help="100x200 cells, 80 MeV beam: a small case for profiler captures (not a bench line)")
     args = ap.parse_args()
+    if args.spots <= 0:
+        args.spots = 64 if args.workload == "c3" else 512
     if args.small:
         global SMALL
         SMALL = True
