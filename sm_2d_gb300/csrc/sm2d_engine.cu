@@ -1774,7 +1774,10 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    c->grid_cell = std::max(1, std::min((int)((NcB + kThreads / 32 - 1) / (kThreads / 32)), 4 * std::max(sms, 1)));
+    // warp-per-cell kernels: 8 blocks per SM (the selection kernels are
+    // latency-bound and gain from the warps in flight; finalize's last-block
+    // step grows with the grid beyond that)
+    c->grid_cell = std::max(1, std::min((int)((NcB + kThreads / 32 - 1) / (kThreads / 32)), 8 * std::max(sms, 1)));
     if ((rc = DISPATCH(*c, transport_grid, sms))) return bail(rc);
     if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "create sync"));
     *out = c;
