@@ -126,3 +126,27 @@ def test_batch_refuses_bad_beams():
         bad = [Beam(0.0, 0.0, 0.0, 40.0, 1.0, 1.5, 0.002, 0.4, 0, 1)]   # Gaussian without samples
         with pytest.raises(sm.Sm2dError):
             t.batch_run(bad, 100)
+
+
+def test_plan_edges(singles):
+    """An empty plan, fewer spots than lanes, dose asked of a plan loaded
+    without dose maps, and a larger plan after a smaller one (its buffers
+    grow)."""
+    beams = _beams()
+    with sm.Transport(_cfg(4)) as many:
+        many.plan_load([], 3000)
+        many.plan_run_async()
+        d, r = many.plan_results()
+        assert d.shape == (0, 70, 40) and r == []
+        dose, res = many.batch_run(beams[:2], 3000)          # 2 spots on 4 lanes
+        for i in range(2):
+            _check_spot(i, res[i], dose[i], singles[i])
+        many.plan_load(beams[:3], 3000, dose=False)
+        many.plan_run_async()
+        with pytest.raises(sm.Sm2dError, match="without dose"):
+            many.plan_results(dose=True)
+        _, res = many.plan_results(dose=False)
+        assert [r["iterations"] for r in res] == [s["n"] for s in singles[:3]]
+        dose, res = many.batch_run(beams, 3000)              # 7 spots: the plan buffers grow
+        for i in range(len(beams)):
+            _check_spot(i, res[i], dose[i], singles[i])
