@@ -150,3 +150,15 @@ def test_plan_edges(singles):
         dose, res = many.batch_run(beams, 3000)              # 7 spots: the plan buffers grow
         for i in range(len(beams)):
             _check_spot(i, res[i], dose[i], singles[i])
+
+
+def test_plan_in_bucket_mode_equals_direct_mode(singles):
+    """The reference's bucket structure (DeviceOutflowBucket + K4) gives the
+    same spots as the fused direct scatter, refills included."""
+    beams = _beams()
+    cfg = _cfg(3)
+    cfg.use_buckets = 1
+    with sm.Transport(cfg) as many:
+        dose, res = many.batch_run(beams, 3000)
+    for i in range(len(beams)):
+        _check_spot(i, res[i], dose[i], singles[i])
