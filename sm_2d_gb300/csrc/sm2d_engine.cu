@@ -374,6 +374,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
                 if (idx < d.listed_cap) {
                     d.listed[idx] = (uint32_t)c;
                     d.c2b[c] = 4 * idx;
+                    d.cell_bins[idx] = make_int2(base, nz);
                 }
                 atomicAdd(&s_cnt[ln][act ? 0 : 1], 1);
                 atomicAdd(&s_cnt[ln][2], __popc(um));
@@ -617,6 +618,52 @@ __global__ void __launch_bounds__(kThreads, 4) k_transport(Dev d) {
     }
 }
 
+// Per-cell tallies of the transported bins of listed cell idx (its
+// contiguous run of the bin list), by one warp: the psi_in weight and
+// bin-centre energy of every bin, and for the bins that took a step (past the
+// prune and cutoff checks) the deposit and the nuclear loss from their step
+// records.  One warp reduction per cell instead of one per 32 bins in the
+// deposit pass; the bucket selection runs it for each cell's first face.
+template <class Lay, int NS>
+__device__ __forceinline__ void tally_cell(const Dev& d, int idx, int lane, LaneSums<NS>& s_sum) {
+    const int2 r = d.cell_bins[idx];
+    const int c = (int)d.listed[idx];
+    const float4* rec = reinterpret_cast<const float4*>(d.brec);
+    double Wi = 0.0, Ei = 0.0, ed = 0.0, en = 0.0;
+    float wn = 0.0f;
+    for (int i = r.x + lane; i < r.x + r.y; i += 32) {
+        const uint4 b = __ldcg(d.bins + i);
+        const bool k3 = ((b.y >> 18) & 1u) != 0;
+        const int lidx = (int)((b.y >> 10) & 0xFFu);
+        const float w = __uint_as_float(b.z);
+        int tl, El, xs, zs;
+        Lay::dec(lidx, tl, El, xs, zs);
+        int Ebin = (int)((b.w >> 12) & 0xFFFu) * Lay::NE + El;
+        if (k3) Ebin = max(0, min(Ebin, d.N_E - 1));
+        const float E = d.Ee[Ebin] + 1.0f * ((d.Ee[Ebin + 1] - d.Ee[Ebin]) * 0.5f);
+        Wi += (double)w;
+        Ei += (double)w * (double)E;
+        if (w < (k3 ? d.prune_fine : d.prune_coarse) || E <= 0.1f) continue;
+        const float4 r1 = __ldcg(rec + 2 * (size_t)i + 1);   // z, sigma, deposit, nuclear weight
+        ed += (double)r1.z;
+        wn += r1.w;
+        en += (double)(r1.w * E);
+    }
+    Wi = warp_sum(Wi);
+    Ei = warp_sum(Ei);
+    ed = warp_sum(ed);
+    en = warp_sum(en);
+    wn = warp_sumf(wn);
+    if (lane == 0) {
+        if (ed != 0.0) atomicAdd(d.dl_edep + c, ed);
+        if (en != 0.0) atomicAdd(d.dl_enuc + c, en);
+        if (wn != 0.0f) atomicAdd(d.dl_wnuc + c, wn);
+        double* ls = s_sum.v[lane_of(d, c)];
+        atomicAdd(ls + 0, Wi);
+        atomicAdd(ls + 1, Ei);
+    }
+}
+
 // ------------------------------------------------------------------ slot selection
 // Selection of one claim-table row by one warp: the gathered ids ordered by
 // claim key; the first 32 become slots 0..31 (written to kept[]), the rest
@@ -682,20 +729,26 @@ __device__ int select_row(unsigned long long* row, int* count, uint32_t tag, Sel
 // Buckets of this pass (warp per listed cell and face): select the kept
 // ids, write them to the bucket (bucket mode: also clear its values), and
 // offer them to the psi_out row of the cell behind the face in bucket-slot
-// order, as K4 claims them.
+// order, as K4 claims them; and the per-cell tallies of the step records.
 template <class Lay, bool BUCKET>
 __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
     constexpr int NW = kThreads / 32;
     __shared__ SelScratch s_sel[NW];
+    __shared__ LaneSums<2> s_tal;   // Win, Ein of the cell tallies
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
     const int out = gs->parity ^ 1;
     const int n = 4 * gs->n_listed;
     const uint32_t tag = gs->ctag;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    s_tal.zero(d.B);
+    __syncthreads();
     for (int wi = blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
         const int face = wi & 3;
         const int src = (int)d.listed[wi >> 2];
+        // the warp of the cell's -z face (usually without emissions) takes
+        // the cell's tallies
+        if (face == FACE_ZM) tally_cell<Lay>(d, wi >> 2, lane, s_tal);
         uint32_t* kept = d.bkt_ids + (size_t)wi * kKb;
         const int nk = select_row(bucket_row(d, wi), d.ccount + (size_t)d.B * d.Nc + wi, tag, s_sel[wid], kept, lane);
         if (BUCKET) {
@@ -719,6 +772,8 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
                         &gs->cand_ovf);
         if (lane == 0) mark_occupied(d, out, dst);
     }
+    __syncthreads();
+    s_tal.flush(d, LANE_DOUBLE(Win));
 }
 
 // Occupied cells of psi_out (which = 1, a transport pass) or the cells an
@@ -1289,10 +1344,11 @@ static bool host_gaussian(const sm2d_beam& b) {   // gpu_transport_wrapper.cu:24
 template <class Lay>
 struct Impl {
     // One iteration: K1 classify, (ascending lists on request), the claim
-    // pass of K2/K3, bucket and psi_out slot selection, the deposit pass of
-    // K2/K3 with the fused K4 scatter or the bucket pair, K5 finalize.
-    // ev[0..7] bracket: classify, lists, claim pass, selection, deposit pass,
-    // K4 bucket move, finalize.
+    // pass of K2/K3, bucket and psi_out slot selection (with the per-cell
+    // tallies of the claim pass's step records), the deposit pass of K2/K3
+    // with the fused K4 scatter or the bucket pair, K5 finalize.  ev[0..7]
+    // bracket: classify, lists, claim pass, selection + tallies, deposit
+    // pass, K4 bucket move, finalize.
     static int launch_body(Ctx& c, bool timed, bool use_cond, bool lists) {
         const int gc = c.grid_cell, gt = c.grid_transport, gk = c.grid_keys;
         const bool bk = c.p.use_buckets != 0;
@@ -1683,6 +1739,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     // hundred thousand); a pass that needs more stops with SM2D_ERR_ALLOC
     d.bins_cap = (int)std::min<size_t>((B == 1 ? Nc * c->L : NcB * c->L / 4), (size_t)INT_MAX);
     A(d.bins, uint4, d.bins_cap);
+    A(d.cell_bins, int2, d.listed_cap);
     A(d.brec, uint4, 2 * (size_t)d.bins_cap);
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
     A(d.gs, IterGlobal, 1);

@@ -543,8 +543,10 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         Ebin = max(0, min(Ebin, d.N_E - 1));
     }
     const float E = d.Ee[Ebin] + 1.0f * ((d.Ee[Ebin + 1] - d.Ee[Ebin]) * 0.5f);
-    t.Win += (double)w;
-    t.Ein += (double)w * (double)E;
+    // the bins' weight and energy, the step's deposit and nuclear loss are
+    // summed per cell by the tally kernel from the bin list and the step
+    // records; the claim pass adds nothing either
+    (void)t;
     if (w < (k3 ? d.prune_fine : d.prune_coarse)) {   // prune (k3:175-184, k2:172-177)
         t.drop_w += (double)w;
         t.drop_e += (double)(E * w);
@@ -666,9 +668,8 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
     const int face = exit_face(x_new, z_new, dx, dz);
     x_new = fmaxf(-hx, fminf(x_new, hx));
     z_new = fmaxf(-hz, fminf(z_new, hz));
-    t.edep += (double)edep;
-    t.w_nuc += w_rem;
-    t.e_nuc += (double)(w_rem * E);
+    (void)edep;
+    (void)w_rem;
     if (E_new <= 0.1f || ((d.esplit || d.floor_cutoff) && E_new <= e_center(d, 0))) {
         t.w_cut += w_new;
         t.e_cut += (double)(E_new * w_new);
