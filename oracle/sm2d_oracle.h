@@ -102,7 +102,8 @@ void orc_fe_precompute_density(float E0, int Nz, float dz, float sigma_x0, const
 void orc_postprocess(const double* edep_in, const float* sigma_total, float sigma_x0,
                      int Nx, int Nz, float dx, double* edep_out);
 /* the transport's elementary functions (0 exp, 1 log, 2 sin, 3 cos, 4 erf)
- * as this build evaluates them, for comparison with the CUDA build */
+ * as the oracle evaluates them on the host, for comparison with the CUDA
+ * library's device results */
 void orc_math(int fn, const float* x, float* y, int n);
 
 /* ---- transport context ---- */
