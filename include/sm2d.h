@@ -15,6 +15,7 @@
  *                               (src/cuda/kernels/k3_finetransport.cuh:114-150)
  *   sm2d_inject                 inject_source_kernel / inject_gaussian_source_kernel and the
  *                               source accounting (src/cuda/gpu_transport_wrapper.cu:339-460)
+ *   sm2d_inject_quadrature      inject_source_kernel with its spreads (src/cuda/k1k6_pipeline.cu:300-427)
  *   sm2d_step                   one pass of the loop body (src/cuda/k1k6_pipeline.cu:1606-2038)
  *   sm2d_run                    run_k1k6_pipeline_transport(DevicePsiC*,...) (k1k6_pipeline.cuh:296)
  *   sm2d_get_dose               EdepC D2H + lateral post-convolution
@@ -145,6 +146,16 @@ int sm2d_local_bins(sm2d_handle h);
 
 /* source injection into psi_in (pencil or LCG Gaussian beam) */
 int sm2d_inject(sm2d_handle h, const sm2d_beam* beam);
+/* inject_source_kernel called with its spreads (src/cuda/k1k6_pipeline.cu:300-427):
+ * the quadrature source.  Uses x0, z0, theta0, E0, W_total, sigma_x and
+ * sigma_theta (sigma_E, n_samples and seed are ignored).  Without spreads
+ * (sigma_theta <= 1e-4, sigma_x <= 0.01) it injects the pencil; otherwise
+ * each cell centre within +-4 sigma_x of x0 takes a Gaussian weight
+ * normalised over those cells, on 7 angle nodes theta0 + a_k sigma_theta with
+ * weights w_k when sigma_theta > 1e-4.  Needs sigma_x > 0 on that path (the
+ * reference divides by sigma_x^2).  Accounting as the wrapper books a
+ * non-Gaussian source: W_total and E0 W_total injected. */
+int sm2d_inject_quadrature(sm2d_handle h, const sm2d_beam* beam);
 /* host <-> device phase space (psi_in): bid[Nx*Nz*32], val[Nx*Nz*32*L] */
 int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val);
 int sm2d_get_psi_in(sm2d_handle h, uint32_t* bid, float* val);

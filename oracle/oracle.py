@@ -80,6 +80,7 @@ def _lib(fp64: bool):
         lib.orc_local_bins.argtypes = [P]
         lib.orc_slots_per_cell.argtypes = [P]
         lib.orc_inject.argtypes = [P] + [C.c_float] * 8 + [C.c_int, C.c_uint]
+        lib.orc_inject_quadrature.argtypes = [P] + [C.c_float] * 7
         lib.orc_set_psi_in.argtypes = [P, P, P]
         lib.orc_get_psi_in.argtypes = [P, P, P]
         lib.orc_step.argtypes = [P]
@@ -208,6 +209,10 @@ class Oracle:
                n_samples=1, seed=42):
         self.lib.orc_inject(self.ctx, x0, z0, theta0, E0, W, sigma_x, sigma_theta, sigma_E,
                             int(n_samples), int(seed) & 0xFFFFFFFF)
+
+    def inject_quadrature(self, x0, z0, theta0, sigma_theta, E0, W, sigma_x):
+        """inject_source_kernel with its spreads (the quadrature source)."""
+        self.lib.orc_inject_quadrature(self.ctx, x0, z0, theta0, sigma_theta, E0, W, sigma_x)
 
     def set_density(self, rho):
         """Slab phantom: density per depth row (None: water)."""

@@ -1668,6 +1668,57 @@ void orc_inject(orc_ctx* c, float x0, float z0, float theta0, float E0, float W,
     c->src_rep_loss = loss;
 }
 
+/* inject_source_kernel with its spreads (k1k6_pipeline.cu:300-427), one
+ * thread, in its loop order: the 7 angle nodes (k1k6_pipeline.cu:316-318)
+ * when sigma_theta > 1e-4, and for each the cells within +-4 sigma_x of x0,
+ * weighted by the Gaussian at their centres over the float sum of those
+ * weights.  Without spreads it is the pencil branch.  Accounting as the
+ * wrapper books a non-Gaussian source (W and E0 W injected). */
+static const float kGhAbscissa[7] = {-2.65f, -1.67f, -0.82f, 0.0f, 0.82f, 1.67f, 2.65f};
+static const float kGhWeight[7] = {0.0105f, 0.0769f, 0.2448f, 0.3357f, 0.2448f, 0.0769f, 0.0105f};
+
+void orc_inject_quadrature(orc_ctx* c, float x0, float z0, float theta0, float sth, float E0, float W, float sx) {
+    int ang = sth > 0.0001f, spat = sx > 0.01f;
+    if (!ang && !spat) {
+        orc_inject(c, x0, z0, theta0, E0, W, 0.0f, 0.0f, 0.0f, 1, 0u);
+        return;
+    }
+    float dx = c->cfg.dx, dz = c->cfg.dz, x_min = c->cfg.x_min, z_min = c->cfg.z_min;
+    int Nx = c->cfg.Nx, Nz = c->cfg.Nz;
+    c->src_inj_w = W;
+    c->src_inj_e = (double)E0 * (double)W;
+    c->src_oog_w = c->src_slot_w = 0.0f;
+    c->src_oog_e = c->src_slot_e = 0.0;
+    float lo = x0 - 4.0f * sx, hi = x0 + 4.0f * sx;
+    int ix0 = (int)((lo - x_min) / dx), ix1 = (int)((hi - x_min) / dx) + 1;
+    if (ix0 < 0) ix0 = 0;
+    if (ix1 > Nx) ix1 = Nx;
+    real total = RL(0.0);
+    for (int ix = ix0; ix < ix1; ++ix) {
+        real d = ((real)x_min + ((real)ix + RL(0.5)) * (real)dx) - (real)x0;
+        total += r_exp(RL(-0.5) * d * d / ((real)sx * (real)sx)) * (real)dx;
+    }
+    if (total <= RL(0.0)) total = RL(1.0);
+    float zr = z0 - z_min;
+    int cz = (int)(zr / dz);
+    cz = cz < 0 ? 0 : (cz >= Nz ? Nz - 1 : cz);
+    for (int it = 0; it < (ang ? 7 : 1); ++it) {
+        real th = ang ? (real)theta0 + (real)kGhAbscissa[it] * (real)sth : (real)theta0;
+        real wt = ang ? (real)kGhWeight[it] : RL(1.0);
+        for (int ix = ix0; ix < ix1; ++ix) {
+            real d = ((real)x_min + ((real)ix + RL(0.5)) * (real)dx) - (real)x0;
+            real wx = (r_exp(RL(-0.5) * d * d / ((real)sx * (real)sx)) * (real)dx) / total;
+            inject_one(c, cz * Nx + ix, th, (real)E0, (real)W * wt * wx, (real)dx * RL(0.5),
+                       (real)zr - (real)cz * (real)dz);
+        }
+    }
+    double W_rep, E_rep;
+    psi_totals(c, psi_in(c), &W_rep, &E_rep);
+    double loss = c->src_inj_e - E_rep;
+    if (fabs(loss) < 1e-12) loss = 0.0;
+    c->src_rep_loss = loss;
+}
+
 /* ------------------------------------------------------------------------- */
 /* context lifecycle and accessors                                           */
 /* ------------------------------------------------------------------------- */

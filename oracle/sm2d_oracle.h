@@ -117,6 +117,10 @@ int  orc_slots_per_cell(const orc_ctx* c);
 void orc_inject(orc_ctx* c, float x0, float z0, float theta0, float E0, float W_total,
                 float sigma_x, float sigma_theta, float sigma_E,
                 int n_samples, unsigned seed);
+/* inject_source_kernel with its spreads: the quadrature source
+ * (k1k6_pipeline.cu:300-427) */
+void orc_inject_quadrature(orc_ctx* c, float x0, float z0, float theta0, float sigma_theta, float E0,
+                           float W_total, float sigma_x);
 /* overwrite psi_in directly (golden inputs); values are orc_real */
 void orc_set_psi_in(orc_ctx* c, const uint32_t* bid, const orc_real* val);
 /* slab phantom: the density of each depth row (rho[Nz]; NULL: water).  Energy

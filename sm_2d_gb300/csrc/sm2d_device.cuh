@@ -18,11 +18,14 @@ constexpr int kKb = 32;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kMaxLanes = 256;   // per-lane sums are staged in shared memory
 
-// One beam on the device (sm2d_beam).
+// One beam on the device (sm2d_beam).  kind 0: the runner's source (pencil
+// or LCG Gaussian, n samples); kind 1: the quadrature source, n samples over
+// the q_nx cells from q_ix0 (the host computes the cell range).
 struct BeamArgs {
     float x0, z0, theta0, E0, W, sx, sth, sE;
     int n;
     unsigned seed;
+    int kind, q_ix0, q_nx;
 };
 
 // Local-bin layout: lidx = t + NT*(e + NE*(x + NX*z))  (local_bins.hpp:62-78)

@@ -75,13 +75,22 @@ __device__ __forceinline__ float source_normal(unsigned& s) {
 }
 
 __device__ __forceinline__ bool beam_gaussian(const BeamArgs& b) {   // gpu_transport_wrapper.cu:246
-    return b.n > 1 || b.sx > 0.0f || b.sth > 0.0f;
+    return b.kind == 0 && (b.n > 1 || b.sx > 0.0f || b.sth > 0.0f);
 }
-__device__ __forceinline__ int beam_samples(const BeamArgs& b) { return beam_gaussian(b) ? max(b.n, 0) : 1; }
+__device__ __forceinline__ int beam_samples(const BeamArgs& b) {
+    return b.kind == 1 ? b.n : beam_gaussian(b) ? max(b.n, 0) : 1;
+}
+
+// The quadrature source's angular nodes and weights, the reference's own
+// 7-point table (k1k6_pipeline.cu:316-318).
+__constant__ float kGhAbscissa[7] = {-2.65f, -1.67f, -0.82f, 0.0f, 0.82f, 1.67f, 2.65f};
+__constant__ float kGhWeight[7] = {0.0105f, 0.0769f, 0.2448f, 0.3357f, 0.2448f, 0.0769f, 0.0105f};
 
 // One source sample: inject_source_kernel's pencil branch
-// (k1k6_pipeline.cu:325-343) or sample i of inject_gaussian_source_kernel
-// (k1k6_pipeline.cu:451-551), placed as device_psic_inject_source does
+// (k1k6_pipeline.cu:325-343), sample i of inject_gaussian_source_kernel
+// (k1k6_pipeline.cu:451-551) or sample i of inject_source_kernel's
+// distributed branch (k1k6_pipeline.cu:345-427: i = angle node * cells +
+// cell, the kernel's loop order), placed as device_psic_inject_source does
 // (device_psic.cuh:347-450: clamp into the cell, sub-cell bins, nearest
 // global bins).  Returns false when the sample leaves the grid.
 struct InjSample {
@@ -92,7 +101,30 @@ struct InjSample {
 template <class Lay>
 __device__ bool inject_sample(const Dev& d, const BeamArgs& b, float x_min, float z_min, int i, InjSample& o) {
     float theta, E, x, z;
-    if (!beam_gaussian(b)) {
+    if (b.kind == 1) {
+        // Gaussian weight of each cell centre over the cell range, normalised
+        // by their float sum in cell order; angle nodes when sigma_theta > 1e-4
+        const int it = i / b.q_nx, ix = b.q_ix0 + i % b.q_nx;
+        float total = 0.0f;
+        for (int k = b.q_ix0; k < b.q_ix0 + b.q_nx; ++k) {
+            const float dxb = (x_min + ((float)k + 0.5f) * d.dx) - b.x0;
+            total += sm2d_expf(-0.5f * dxb * dxb / (b.sx * b.sx)) * d.dx;
+        }
+        if (total <= 0.0f) total = 1.0f;
+        const float dxb = (x_min + ((float)ix + 0.5f) * d.dx) - b.x0;
+        const float w_x = (sm2d_expf(-0.5f * dxb * dxb / (b.sx * b.sx)) * d.dx) / total;
+        const bool ang = b.sth > 0.0001f;
+        theta = ang ? b.theta0 + kGhAbscissa[it] * b.sth : b.theta0;
+        const float w_t = ang ? kGhWeight[it] : 1.0f;
+        const float zr = b.z0 - z_min;
+        int cz = (int)(zr / d.dz);
+        cz = cz < 0 ? 0 : (cz >= d.Nz ? d.Nz - 1 : cz);
+        o.cell = cz * d.Nx + ix;
+        o.w = b.W * w_t * w_x;
+        E = b.E0;
+        x = d.dx * 0.5f;
+        z = zr - cz * d.dz;
+    } else if (!beam_gaussian(b)) {
         const float xr = b.x0 - x_min, zr = b.z0 - z_min;
         int cx = (int)(xr / d.dx), cz = (int)(zr / d.dz);
         cx = cx < 0 ? 0 : (cx >= d.Nx ? d.Nx - 1 : cx);
@@ -1886,6 +1918,55 @@ int sm2d_inject(sm2d_handle h, const sm2d_beam* b) {
     if (c.gs_host->occ_n[c.gs_host->parity] != 0)
         return fail(SM2D_ERR_STATE, "phase space not empty: call sm2d_reset before injecting");
     if ((rc = sm2d_inject_async(h, b))) return rc;
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+
+// inject_source_kernel with its spreads (k1k6_pipeline.cu:300-427).  Without
+// spreads (sigma_theta <= 1e-4 and sigma_x <= 0.01) it is the pencil branch;
+// otherwise the cells within +-4 sigma_x of x0 (clamped to the grid) take
+// Gaussian weights of their centres, normalised over those cells, on the 7
+// angle nodes when sigma_theta > 1e-4.  Source accounting as the wrapper
+// books a non-Gaussian source: W_total and E0 W_total injected.
+static int float_to_index(float v) {   // a float-to-int conversion that saturates
+    if (!(v == v)) return 0;
+    if (v >= 1e9f) return 1000000000;
+    if (v <= -1e9f) return -1000000000;
+    return (int)v;
+}
+
+int sm2d_inject_quadrature(sm2d_handle h, const sm2d_beam* b) {
+    if (!h || !b) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    const bool ang = b->sigma_theta > 0.0001f, spat = b->sigma_x > 0.01f;
+    if (!ang && !spat) {
+        sm2d_beam p = *b;
+        p.sigma_x = p.sigma_theta = p.sigma_E = 0.0f;
+        p.n_samples = 1;
+        return sm2d_inject(h, &p);
+    }
+    if (!(b->sigma_x > 0.0f) || !std::isfinite(b->sigma_x) || !std::isfinite(b->x0))
+        return fail(SM2D_ERR_ARG, "the quadrature source needs a finite sigma_x > 0 (its cell weights divide by sigma_x^2)");
+    int rc = sync_state(c);
+    if (rc) return rc;
+    if (c.gs_host->occ_n[c.gs_host->parity] != 0)
+        return fail(SM2D_ERR_STATE, "phase space not empty: call sm2d_reset before injecting");
+    // cells within +-4 sigma_x (k1k6_pipeline.cu:351-364)
+    const float lo = b->x0 - 4.0f * b->sigma_x, hi = b->x0 + 4.0f * b->sigma_x;
+    int ix0 = float_to_index((lo - c.p.x_min) / c.p.dx), ix1 = float_to_index((hi - c.p.x_min) / c.p.dx) + 1;
+    ix0 = std::max(ix0, 0);
+    ix1 = std::min(ix1, c.p.Nx);
+    BeamArgs a = beam_args(*b);
+    a.kind = 1;
+    a.q_ix0 = ix0;
+    a.q_nx = std::max(ix1 - ix0, 0);
+    a.n = (ang ? 7 : 1) * a.q_nx;
+    for (int ln = 0; ln < c.B; ++ln) c.beams_host[ln] = ln == 0 ? a : BeamArgs{};
+    CK(cudaMemcpyAsync(c.beams_dev, c.beams_host, sizeof(BeamArgs) * c.B, cudaMemcpyHostToDevice, c.s));
+    set_lane_fe(c, 0, c.p.E0, c.p.sigma_x_initial);
+    if ((rc = upload_lane_fe(c))) return rc;
+    if ((rc = DISPATCH(c, inject, std::max(a.n, 1), true, false))) return rc;
+    c.injected = true;
     CK(cudaStreamSynchronize(c.s));
     return 0;
 }

@@ -126,6 +126,7 @@ def lib(build_if_needed: bool = True):
         for n in ["sm2d_destroy", "sm2d_local_bins"]:
             getattr(L, n).argtypes = [P]
         L.sm2d_inject.argtypes = [P, C.POINTER(Beam)]
+        L.sm2d_inject_quadrature.argtypes = [P, C.POINTER(Beam)]
         L.sm2d_set_psi_in.argtypes = [P, P, P]
         L.sm2d_get_psi_in.argtypes = [P, P, P]
         L.sm2d_step.argtypes = [P, C.POINTER(I), C.POINTER(I)]
@@ -382,6 +383,13 @@ class Transport:
                sigma_E=0.0, n_samples=1, seed=42):
         b = Beam(x0, z0, theta0, E0, W, sigma_x, sigma_theta, sigma_E, int(n_samples), int(seed) & 0xFFFFFFFF)
         check(self._lib.sm2d_inject(self.h, C.byref(b)))
+
+    def inject_quadrature(self, x0=0.0, z0=0.0, theta0=0.0, sigma_theta=0.0, E0=150.0, W=1.0, sigma_x=0.0):
+        """inject_source_kernel called with its spreads (k1k6_pipeline.cu:300-427):
+        Gaussian cell weights over +-4 sigma_x, 7 angle nodes when
+        sigma_theta > 1e-4; the pencil without spreads."""
+        b = Beam(x0, z0, theta0, E0, W, sigma_x, sigma_theta, 0.0, 0, 0)
+        check(self._lib.sm2d_inject_quadrature(self.h, C.byref(b)))
 
     def set_psi_in(self, bid, val):
         bid = np.ascontiguousarray(bid, np.uint32)
