@@ -185,6 +185,19 @@ int sm2d_get_audit_history(sm2d_handle h, sm2d_audit* out, int max_entries, int*
  * since create) [16] bin-list overflows of this spot (non-zero: the run
  * stopped early; sm2d_run/sm2d_step return SM2D_ERR_ALLOC) */
 int sm2d_get_scalars(sm2d_handle h, double* out17);
+/* k2_get_debug_counters / k3_get_debug_counters / k4_get_debug_counters
+ * (src/cuda/kernels/k2_coarsetransport.cuh:101-112, k3_finetransport.cuh:78-89,
+ * k4_transfer.cuh:19-24) for stage 2, 3 or 4: [0] output-slot drops, [1]
+ * bucket drops, [2] pruned components; dropped components, weight and energy
+ * (after-step energy; bin centre for K4) since sm2d_reset or
+ * sm2d_reset_debug_counters, summed over lanes.  K4 counts the output slots
+ * the fused deposit or the bucket move could not resolve; K4 has no bucket or
+ * prune drops.  Their weights add up to the transport-drop channel, less
+ * what a stopping rule or an iteration limit books there at a spot's end. */
+int sm2d_get_debug_counters(sm2d_handle h, int stage, unsigned long long* counts3, double* weights3,
+                            double* energies3);
+/* k2/k3/k4_reset_debug_counters */
+int sm2d_reset_debug_counters(sm2d_handle h, int stage);
 int sm2d_get_fe(sm2d_handle h, float* A, float* B, float* sigma_total);
 /* EdepC after the lateral MCS post-convolution, [Nz][Nx] row-major */
 int sm2d_get_dose(sm2d_handle h, double* dose);

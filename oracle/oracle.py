@@ -81,6 +81,7 @@ def _lib(fp64: bool):
         lib.orc_slots_per_cell.argtypes = [P]
         lib.orc_inject.argtypes = [P] + [C.c_float] * 8 + [C.c_int, C.c_uint]
         lib.orc_inject_quadrature.argtypes = [P] + [C.c_float] * 7
+        lib.orc_get_drop_channels.argtypes = [P, P, P]
         lib.orc_set_psi_in.argtypes = [P, P, P]
         lib.orc_get_psi_in.argtypes = [P, P, P]
         lib.orc_step.argtypes = [P]
@@ -266,6 +267,14 @@ class Oracle:
         a = OrcAudit()
         self.lib.orc_get_audit(self.ctx, C.byref(a))
         return a.as_dict()
+
+    def drop_channels(self):
+        """{(stage, kind): (weight, energy)} of the drops since create, stage
+        2/3/4 (K2, K3, K4), kind slot/bucket/pruned."""
+        w, e = np.zeros(9), np.zeros(9)
+        self.lib.orc_get_drop_channels(self.ctx, _p(w), _p(e))
+        kinds = ("slot", "bucket", "pruned")
+        return {(2 + i // 3, kinds[i % 3]): (float(w[i]), float(e[i])) for i in range(9)}
 
     def scalars(self):
         s = np.zeros(14)

@@ -126,6 +126,8 @@ struct orc_ctx {
     double k2_slot_w, k2_slot_e, k2_bkt_w, k2_bkt_e, k2_prune_w, k2_prune_e;
     double k3_slot_w, k3_slot_e, k3_bkt_w, k3_bkt_e, k3_prune_w, k3_prune_e;
     double k4_slot_w, k4_slot_e;
+    /* the same, summed over the iterations since create: [K2, K3, K4][slot, bucket, prune] */
+    double cum_drop_w[3][3], cum_drop_e[3][3];
     /* run state */
     double transport_drop_w, transport_drop_e, audit_residual;
     float src_inj_w, src_oog_w, src_slot_w;
@@ -1539,6 +1541,19 @@ int orc_step(orc_ctx* c) {
     for (int cell = 0; cell < c->Nc; ++cell) if (po->occ[cell]) c->slots_out += (double)count_slots(c, po, cell);
     double dw = c->k2_slot_w + c->k2_bkt_w + c->k3_slot_w + c->k3_bkt_w + c->k4_slot_w + c->k2_prune_w + c->k3_prune_w;
     double de = c->k2_slot_e + c->k2_bkt_e + c->k3_slot_e + c->k3_bkt_e + c->k4_slot_e + c->k2_prune_e + c->k3_prune_e;
+    {
+        const double cw[3][3] = {{c->k2_slot_w, c->k2_bkt_w, c->k2_prune_w},
+                                 {c->k3_slot_w, c->k3_bkt_w, c->k3_prune_w},
+                                 {c->k4_slot_w, 0.0, 0.0}};
+        const double ce[3][3] = {{c->k2_slot_e, c->k2_bkt_e, c->k2_prune_e},
+                                 {c->k3_slot_e, c->k3_bkt_e, c->k3_prune_e},
+                                 {c->k4_slot_e, 0.0, 0.0}};
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                c->cum_drop_w[a][b] += cw[a][b];
+                c->cum_drop_e[a][b] += ce[a][b];
+            }
+    }
     c->transport_drop_w += dw;
     c->transport_drop_e += de;
     k5(c, (float)dw, de, c->iter == 1);
@@ -1722,6 +1737,14 @@ void orc_inject_quadrature(orc_ctx* c, float x0, float z0, float theta0, float s
 /* ------------------------------------------------------------------------- */
 /* context lifecycle and accessors                                           */
 /* ------------------------------------------------------------------------- */
+void orc_get_drop_channels(const orc_ctx* c, double* w9, double* e9) {
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            w9[3 * a + b] = c->cum_drop_w[a][b];
+            e9[3 * a + b] = c->cum_drop_e[a][b];
+        }
+}
+
 orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* th_edges, int N_E, const float* E_edges) {
     orc_ctx* c = (orc_ctx*)calloc(1, sizeof(orc_ctx));
     c->cfg = *cfg;

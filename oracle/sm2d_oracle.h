@@ -138,6 +138,10 @@ int  orc_get_lists(const orc_ctx* c, uint32_t* active, int* n_active,
 void orc_get_tallies(const orc_ctx* c, double* edep, float* w_cut, double* e_cut,
                      float* w_nuc, double* e_nuc, float* w_bnd, double* e_bnd);
 void orc_get_audit(const orc_ctx* c, orc_audit* out);
+/* the per-iteration drop channels of k2/k3/k4_get_debug_counters summed over
+ * the iterations since create: w9[3 * stage + kind], stage K2, K3, K4 and
+ * kind output slot, bucket, prune */
+void orc_get_drop_channels(const orc_ctx* c, double* w9, double* e9);
 /* scalars: [0]=transport_dropped_weight [1]=transport_dropped_energy
  * [2]=audit residual energy [3]=source_injected_weight [4]=source_injected_energy
  * [5]=source_out_of_grid_weight [6]=source_out_of_grid_energy

@@ -53,6 +53,16 @@ using LayoutB128 = Layout<8, 4, 4, 1>;   // 128 bins: 8 theta x 4 E x 4 x_sub
 
 // Iteration state shared by the lanes (one per engine), written only by
 // device code between host syncs.
+// Drop counters of k2/k3/k4_get_debug_counters (k2_coarsetransport.cuh:101-112,
+// k3_finetransport.cuh:78-89, k4_transfer.cuh:19-24): per stage (K2, K3, K4)
+// and kind (output slot, bucket, prune), the dropped components, their
+// weight and energy, since the last reset.
+enum { DROP_SLOT = 0, DROP_BUCKET = 1, DROP_PRUNE = 2 };
+struct DropCounters {
+    unsigned long long n[3][3];
+    double w[3][3], e[3][3];
+};
+
 struct IterGlobal {
     int parity;            // occupancy list `parity` lists psi_in, `parity ^ 1` psi_out
     int halt;              // this pass does no transport (no lane has work, or paused)
@@ -84,7 +94,16 @@ struct IterGlobal {
     const float* plan_fe;         // [plan_n][3 Nz + 1]: A(z), B(z), sigma_total(z), sigma_x
     double* plan_dose;            // [plan_n][Nc] convolved dose, or null
     sm2d_spot_result* plan_res;   // [plan_n]
+    DropCounters drops;           // cleared with the iteration state
 };
+
+// One dropped component (rare paths only): stage 0 K2, 1 K3, 2 K4.  Out of
+// line, so that the emission code inlined at many sites stays small.
+static __device__ __noinline__ void count_drop(IterGlobal* gs, int stage, int kind, double w, double e) {
+    atomicAdd(&gs->drops.n[stage][kind], 1ull);
+    atomicAdd(&gs->drops.w[stage][kind], w);
+    atomicAdd(&gs->drops.e[stage][kind], e);
+}
 
 // Per-lane (per-spot) state.
 struct LaneState {

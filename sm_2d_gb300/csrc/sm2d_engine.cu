@@ -657,12 +657,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_transport(Dev d) {
 // records.  One warp reduction per cell instead of one per 32 bins in the
 // deposit pass; the bucket selection runs it for each cell's first face.
 template <class Lay, int NS>
-__device__ __forceinline__ void tally_cell(const Dev& d, int idx, int lane, LaneSums<NS>& s_sum) {
+__device__ __forceinline__ void tally_cell(const Dev& d, int idx, int lane, LaneSums<NS>& s_sum, double* s_prune) {
     const int2 r = d.cell_bins[idx];
     const int c = (int)d.listed[idx];
     const float4* rec = reinterpret_cast<const float4*>(d.brec);
-    double Wi = 0.0, Ei = 0.0, ed = 0.0, en = 0.0;
+    double Wi = 0.0, Ei = 0.0, ed = 0.0, en = 0.0, pw = 0.0, pe = 0.0;
     float wn = 0.0f;
+    int pn = 0, k3c = 0;
     for (int i = r.x + lane; i < r.x + r.y; i += 32) {
         const uint4 b = __ldcg(d.bins + i);
         const bool k3 = ((b.y >> 18) & 1u) != 0;
@@ -675,7 +676,14 @@ __device__ __forceinline__ void tally_cell(const Dev& d, int idx, int lane, Lane
         const float E = d.Ee[Ebin] + 1.0f * ((d.Ee[Ebin + 1] - d.Ee[Ebin]) * 0.5f);
         Wi += (double)w;
         Ei += (double)w * (double)E;
-        if (w < (k3 ? d.prune_fine : d.prune_coarse) || E <= 0.1f) continue;
+        if (w < (k3 ? d.prune_fine : d.prune_coarse)) {   // the transport's prune drop
+            pw += (double)w;
+            pe += (double)(E * w);
+            ++pn;
+            k3c = k3;
+            continue;
+        }
+        if (E <= 0.1f) continue;
         const float4 r1 = __ldcg(rec + 2 * (size_t)i + 1);   // z, sigma, deposit, nuclear weight
         ed += (double)r1.z;
         wn += r1.w;
@@ -686,6 +694,17 @@ __device__ __forceinline__ void tally_cell(const Dev& d, int idx, int lane, Lane
     ed = warp_sum(ed);
     en = warp_sum(en);
     wn = warp_sumf(wn);
+    if (__any_sync(kFull, pn != 0)) {   // a cell is of one class: K2 or K3
+        const int st = __reduce_max_sync(kFull, (unsigned)k3c);
+        pw = warp_sum(pw);
+        pe = warp_sum(pe);
+        pn = (int)__reduce_add_sync(kFull, (unsigned)pn);
+        if (lane == 0) {
+            atomicAdd(s_prune + 3 * st, (double)pn);
+            atomicAdd(s_prune + 3 * st + 1, pw);
+            atomicAdd(s_prune + 3 * st + 2, pe);
+        }
+    }
     if (lane == 0) {
         if (ed != 0.0) atomicAdd(d.dl_edep + c, ed);
         if (en != 0.0) atomicAdd(d.dl_enuc + c, en);
@@ -767,6 +786,7 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
     constexpr int NW = kThreads / 32;
     __shared__ SelScratch s_sel[NW];
     __shared__ LaneSums<2> s_tal;   // Win, Ein of the cell tallies
+    __shared__ double s_prune[6];   // pruned components, weight, energy of K2 and K3
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
     const int out = gs->parity ^ 1;
@@ -774,13 +794,14 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
     const uint32_t tag = gs->ctag;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     s_tal.zero(d.B);
+    if (threadIdx.x < 6) s_prune[threadIdx.x] = 0.0;
     __syncthreads();
     for (int wi = blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
         const int face = wi & 3;
         const int src = (int)d.listed[wi >> 2];
         // the warp of the cell's -z face (usually without emissions) takes
         // the cell's tallies
-        if (face == FACE_ZM) tally_cell<Lay>(d, wi >> 2, lane, s_tal);
+        if (face == FACE_ZM) tally_cell<Lay>(d, wi >> 2, lane, s_tal, s_prune);
         uint32_t* kept = d.bkt_ids + (size_t)wi * kKb;
         const int nk = select_row(bucket_row(d, wi), d.ccount + (size_t)d.B * d.Nc + wi, tag, s_sel[wid], kept, lane);
         if (BUCKET) {
@@ -806,6 +827,12 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
     }
     __syncthreads();
     s_tal.flush(d, LANE_DOUBLE(Win));
+    if (threadIdx.x < 2 && s_prune[3 * threadIdx.x] != 0.0) {
+        const int st = threadIdx.x;
+        atomicAdd(&gs->drops.n[st][DROP_PRUNE], (unsigned long long)s_prune[3 * st]);
+        atomicAdd(&gs->drops.w[st][DROP_PRUNE], s_prune[3 * st + 1]);
+        atomicAdd(&gs->drops.e[st][DROP_PRUNE], s_prune[3 * st + 2]);
+    }
 }
 
 // Occupied cells of psi_out (which = 1, a transport pass) or the cells an
@@ -877,8 +904,10 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
                 const float w = v[l];
                 if (w <= 0.0f) continue;
                 if (os < 0) {
+                    const double e = (double)e_center(d, ebin_of<Lay>(d, bid, l)) * (double)w;
                     g[0] += (double)w;
-                    g[1] += (double)e_center(d, ebin_of<Lay>(d, bid, l)) * (double)w;
+                    g[1] += e;
+                    count_drop(d.gs, 2, DROP_SLOT, (double)w, e);
                     continue;
                 }
                 const int le = sel != bid ? remap_lidx<Lay>(l, bid, sel) : l;
@@ -2143,6 +2172,35 @@ int sm2d_get_scalars(sm2d_handle h, double* o) {
     o[7] = L.src_slot_w; o[8] = L.src_slot_e; o[9] = L.src_rep_loss;
     o[10] = L.iter; o[11] = L.cell_steps; o[12] = L.slots_in; o[13] = L.slots_out;
     o[14] = G.cand_ovf; o[15] = G.cand_miss; o[16] = G.bin_ovf;
+    return 0;
+}
+
+int sm2d_get_debug_counters(sm2d_handle h, int stage, unsigned long long* counts, double* weights,
+                            double* energies) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    if (stage < 2 || stage > 4) return fail(SM2D_ERR_ARG, "stage must be 2 (K2), 3 (K3) or 4 (K4)");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    const DropCounters& D = h->gs_host->drops;
+    for (int k = 0; k < 3; ++k) {
+        if (counts) counts[k] = D.n[stage - 2][k];
+        if (weights) weights[k] = D.w[stage - 2][k];
+        if (energies) energies[k] = D.e[stage - 2][k];
+    }
+    return 0;
+}
+
+int sm2d_reset_debug_counters(sm2d_handle h, int stage) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    if (stage < 2 || stage > 4) return fail(SM2D_ERR_ARG, "stage must be 2 (K2), 3 (K3) or 4 (K4)");
+    Ctx& c = *h;
+    char* base = reinterpret_cast<char*>(c.d.gs) + offsetof(IterGlobal, drops);
+    const int s = stage - 2;
+    CK(cudaMemsetAsync(base + offsetof(DropCounters, n) + sizeof(unsigned long long) * 3 * s, 0,
+                       sizeof(unsigned long long) * 3, c.s));
+    CK(cudaMemsetAsync(base + offsetof(DropCounters, w) + sizeof(double) * 3 * s, 0, sizeof(double) * 3, c.s));
+    CK(cudaMemsetAsync(base + offsetof(DropCounters, e) + sizeof(double) * 3 * s, 0, sizeof(double) * 3, c.s));
+    CK(cudaStreamSynchronize(c.s));
     return 0;
 }
 

@@ -36,10 +36,12 @@ struct Tally {                // per-lane accumulators of one work item
 };
 
 // The component being transported: its cell, psi_in slot and local bin give
-// the sequential claim order; k3 selects the batch.
+// the sequential claim order; k3 selects the batch; E is its energy after
+// the step (the energy its drops are booked with).
 struct Src {
     int cell, slot, lidx, k3;
     uint32_t tag;   // classification number of this pass
+    float E;
 };
 
 __device__ __forceinline__ float e_center(const Dev& d, int b) { return d.Ee[b] + 0.5f * (d.Ee[b + 1] - d.Ee[b]); }
@@ -204,38 +206,47 @@ __device__ __forceinline__ EParts plan_energy(const Dev& d, const EmitPlan& p, f
 template <class Lay, int PASS>
 __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int bcell, int face, int dcell, int col,
                                      int seq, uint32_t want, int lidx, float w, Tally& t) {
+    // a drop leaves through the single exit at the end: a bucket drop of the
+    // transport's stage, or an output-slot drop of the fused K4
+    int stage = src.k3;
     const int base = d.c2b[bcell];
-    if (base < 0) return w;
-    const int bf = base + face;
-    if (PASS == PASS_KEYS) {
-        cand_insert(bucket_row(d, bf), d.ccount + (size_t)d.B * d.Nc + bf, src.tag, want,
-                    bucket_key(col, src.slot, src.lidx, seq),
-                    &d.gs->cand_ovf);
-        return 0.0f;
+    if (base >= 0) {
+        const int bf = base + face;
+        if (PASS == PASS_KEYS) {
+            cand_insert(bucket_row(d, bf), d.ccount + (size_t)d.B * d.Nc + bf, src.tag, want,
+                        bucket_key(col, src.slot, src.lidx, seq),
+                        &d.gs->cand_ovf);
+            return 0.0f;
+        }
+        uint32_t selb;
+        const int kb = resolve(d, bucket_row(d, bf), d.bkt_ids + (size_t)bf * kKb, src.tag, want, selb);
+        if (kb >= 0) {
+            const int le = (selb == want) ? lidx : remap_lidx<Lay>(lidx, want, selb);
+            if (selb != want && d.esplit)   // split method: a re-binned part keeps its energy
+                t.edep += (double)((e_center(d, ebin_of<Lay>(d, want, lidx)) - e_center(d, ebin_of<Lay>(d, selb, le))) * w);
+            if (PASS == PASS_BUCKET) {
+                float* vals = bucket_vals(d.buckets + (size_t)bf * d.bucket_bytes);
+                atomicAdd(vals + (size_t)kb * Lay::L + le, w);
+                return 0.0f;
+            }
+            // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
+            uint32_t seld;
+            const int os = resolve(d, psi_row(d, dcell), d.bid + (size_t)dcell * kKb, src.tag, selb, seld);
+            if (os >= 0) {
+                const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
+                const int e2 = ebin_of<Lay>(d, seld, le2);
+                if (seld != selb && d.esplit)
+                    atomicAdd(d.dl_edep + bcell, (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, e2)) * w));
+                atomicAdd(d.val + ((size_t)dcell * kKb + os) * Lay::L + le2, w);
+                t.Wout += (double)w;
+                t.Eout += (double)w * (double)e_center(d, e2);
+                return 0.0f;
+            }
+            stage = 2;
+        }
     }
-    uint32_t selb;
-    const int kb = resolve(d, bucket_row(d, bf), d.bkt_ids + (size_t)bf * kKb, src.tag, want, selb);
-    if (kb < 0) return w;
-    const int le = (selb == want) ? lidx : remap_lidx<Lay>(lidx, want, selb);
-    if (selb != want && d.esplit)   // split method: a re-binned part keeps its energy
-        t.edep += (double)((e_center(d, ebin_of<Lay>(d, want, lidx)) - e_center(d, ebin_of<Lay>(d, selb, le))) * w);
-    if (PASS == PASS_BUCKET) {
-        float* vals = bucket_vals(d.buckets + (size_t)bf * d.bucket_bytes);
-        atomicAdd(vals + (size_t)kb * Lay::L + le, w);
-        return 0.0f;
-    }
-    // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
-    uint32_t seld;
-    const int os = resolve(d, psi_row(d, dcell), d.bid + (size_t)dcell * kKb, src.tag, selb, seld);
-    if (os < 0) return w;
-    const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
-    const int e2 = ebin_of<Lay>(d, seld, le2);
-    if (seld != selb && d.esplit)
-        atomicAdd(d.dl_edep + bcell, (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, e2)) * w));
-    atomicAdd(d.val + ((size_t)dcell * kKb + os) * Lay::L + le2, w);
-    t.Wout += (double)w;
-    t.Eout += (double)w * (double)e_center(d, e2);
-    return 0.0f;
+    if (PASS != PASS_KEYS) count_drop(d.gs, stage, stage == 2 ? DROP_SLOT : DROP_BUCKET, (double)w, (double)(src.E * w));
+    return w;
 }
 
 // Two-bin theta split around the nearest bin centre with frac^2 weight to
@@ -321,7 +332,11 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
         const int ecell = src + off;   // same row of the same lane
         // the bucket of another column exists only if that cell is listed
         // in the same pass (k1k6_pipeline.cu:800-847 maps one list at a time)
-        if (ecell != src && d.cls[ecell] != my_cls) { dropped += weight * wf; continue; }
+        if (ecell != src && d.cls[ecell] != my_cls) {
+            if (PASS != PASS_KEYS) count_drop(d.gs, sc.k3, DROP_BUCKET, (double)(weight * wf), (double)(E * (weight * wf)));
+            dropped += weight * wf;
+            continue;
+        }
         const int xt = off < 0 ? Lay::NX - 1 : (off > 0 ? 0 : Lay::NX / 2);
         dropped += emit_component<Lay, PASS>(d, sc, par, ecell, FACE_ZP, ecell + d.Nx, N - 1 - i, pl, weight * wf,
                                              xt, 0, t);
@@ -402,6 +417,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             if (os < 0) {
                 t.drop_w += (double)wpart;
                 t.drop_e += (double)(E_new * wpart);
+                count_drop(d.gs, sc.k3, DROP_SLOT, (double)wpart, (double)(E_new * wpart));
                 if (!d.esplit) return;
                 continue;
             }
@@ -549,7 +565,7 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
     (void)t;
     if (w < (k3 ? d.prune_fine : d.prune_coarse)) {   // prune (k3:175-184, k2:172-177)
         t.drop_w += (double)w;
-        t.drop_e += (double)(E * w);
+        t.drop_e += (double)(E * w);   // counted per cell by the tally (tally_cell)
         return;
     }
     const float tmin = d.th[0], tmax = d.th[d.N_theta];
@@ -676,7 +692,7 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         return;
     }
     const int my_cls = k3 ? 2 : 1;
-    const Src sc{cell, slot, lidx, k3 ? 1 : 0, tag};
+    const Src sc{cell, slot, lidx, k3 ? 1 : 0, tag, E_new};
     if (face >= 0) {
         emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, theta_new, E_new, w_new, x_new, z_new, sigv, t);
     } else {

@@ -127,6 +127,8 @@ def lib(build_if_needed: bool = True):
             getattr(L, n).argtypes = [P]
         L.sm2d_inject.argtypes = [P, C.POINTER(Beam)]
         L.sm2d_inject_quadrature.argtypes = [P, C.POINTER(Beam)]
+        L.sm2d_get_debug_counters.argtypes = [P, C.c_int, P, P, P]
+        L.sm2d_reset_debug_counters.argtypes = [P, C.c_int]
         L.sm2d_set_psi_in.argtypes = [P, P, P]
         L.sm2d_get_psi_in.argtypes = [P, P, P]
         L.sm2d_step.argtypes = [P, C.POINTER(I), C.POINTER(I)]
@@ -464,6 +466,18 @@ class Transport:
         s = np.zeros(len(SCALAR_KEYS))
         check(self._lib.sm2d_get_scalars(self.h, _p(s)))
         return dict(zip(SCALAR_KEYS, s.tolist()))
+
+    def debug_counters(self, stage):
+        """k{stage}_get_debug_counters for stage 2 (K2), 3 (K3) or 4 (K4):
+        {kind: (count, weight, energy)} for the output-slot, bucket and
+        prune drops since the last reset."""
+        n = np.zeros(3, np.uint64)
+        w, e = np.zeros(3), np.zeros(3)
+        check(self._lib.sm2d_get_debug_counters(self.h, int(stage), _p(n), _p(w), _p(e)))
+        return {k: (int(n[i]), float(w[i]), float(e[i])) for i, k in enumerate(("slot", "bucket", "pruned"))}
+
+    def reset_debug_counters(self, stage):
+        check(self._lib.sm2d_reset_debug_counters(self.h, int(stage)))
 
     def fe(self):
         A, B, S = (np.zeros(self.cfg.Nz, np.float32) for _ in range(3))
