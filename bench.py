@@ -141,9 +141,11 @@ def lane_bytes(cfg):
     return psi + per_cell + rows + bins
 
 
-def auto_lanes(cfg, free_bytes, cap=64):
-    """Lanes filling at most 60 % of the free device memory (at most `cap`)."""
-    return int(max(1, min(cap, 0.6 * free_bytes // lane_bytes(cfg))))
+def auto_lanes(cfg, free_bytes, cap=80):
+    """Lanes filling at most 85 % of the free device memory (at most `cap`).
+    On the 512-spot plan the rate grows with the lanes up to about 72 and is
+    flat beyond: 64 lanes 731, 72 lanes 752, 80 lanes 756 spots/s."""
+    return int(max(1, min(cap, 0.85 * free_bytes // lane_bytes(cfg))))
 
 
 def workload_desc(workload, grid, n_spots):
