@@ -582,9 +582,12 @@ __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
 // One thread per w > 0 bin of the listed cells.  PASS_KEYS gathers the
 // claim candidates; the deposit passes add the weights, book per-cell tally
 // increments in the dl_* arrays (one atomic per cell run of a warp) and the
-// per-lane audit sums (staged per block in shared memory).
+// per-lane audit sums (staged per block in shared memory).  Resident blocks
+// per SM: five for the claim pass (47 registers, no spills; 27.2 -> 24.1 ms
+// per wave of 80 spots against four), four for the deposit passes (five
+// would spill).
 template <class Lay, int PASS>
-__global__ void __launch_bounds__(kThreads, 4) k_transport(Dev d) {
+__global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 5 : 4) k_transport(Dev d) {
     __shared__ LaneSums<6> s_sum;   // drop_w, drop_e, Win, Ein, Wout, Eout
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
