@@ -582,13 +582,14 @@ __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
 // One thread per w > 0 bin of the listed cells.  PASS_KEYS gathers the
 // claim candidates; the deposit passes add the weights, book per-cell tally
 // increments in the dl_* arrays (one atomic per cell run of a warp) and the
-// per-lane audit sums (staged per block in shared memory).  Resident blocks
+// per-lane drop sums (staged per block in shared memory); psi_out's weight
+// and energy for the audit are summed by the finalize kernel.  Resident blocks
 // per SM: five for the claim pass (47 registers, no spills; 27.2 -> 24.1 ms
 // per wave of 80 spots against four), four for the deposit passes (five
 // would spill).
 template <class Lay, int PASS>
 __global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 5 : 4) k_transport(Dev d) {
-    __shared__ LaneSums<6> s_sum;   // drop_w, drop_e, Win, Ein, Wout, Eout
+    __shared__ LaneSums<2> s_sum;   // drop_w, drop_e
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
     const int par = gs->parity;
@@ -626,8 +627,7 @@ __global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 5 : 4) k_transpo
             const double edep = seg_sum(t.edep, same), ecut = seg_sum(t.e_cut, same), enuc = seg_sum(t.e_nuc, same),
                          ebnd = seg_sum(t.e_bnd, same);
             const float wcut = seg_sum(t.w_cut, same), wnuc = seg_sum(t.w_nuc, same), wbnd = seg_sum(t.w_bnd, same);
-            const double dw = seg_sum(t.drop_w, same), de = seg_sum(t.drop_e, same), wi = seg_sum(t.Win, same),
-                         ei = seg_sum(t.Ein, same), wo = seg_sum(t.Wout, same), eo = seg_sum(t.Eout, same);
+            const double dw = seg_sum(t.drop_w, same), de = seg_sum(t.drop_e, same);
             const int prev_cell = __shfl_up_sync(kFull, cell, 1);
             if (cell >= 0 && (lane == 0 || prev_cell != cell)) {
                 if (edep != 0.0) atomicAdd(d.dl_edep + cell, edep);
@@ -637,13 +637,11 @@ __global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 5 : 4) k_transpo
                 if (wcut != 0.0f) atomicAdd(d.dl_wcut + cell, wcut);
                 if (wnuc != 0.0f) atomicAdd(d.dl_wnuc + cell, wnuc);
                 if (wbnd != 0.0f) atomicAdd(d.dl_wbnd + cell, wbnd);
-                double* ls = s_sum.v[lane_of(d, cell)];
-                if (dw != 0.0) atomicAdd(ls + 0, dw);
-                if (de != 0.0) atomicAdd(ls + 1, de);
-                atomicAdd(ls + 2, wi);
-                atomicAdd(ls + 3, ei);
-                if (wo != 0.0) atomicAdd(ls + 4, wo);
-                if (eo != 0.0) atomicAdd(ls + 5, eo);
+                if (dw != 0.0 || de != 0.0) {
+                    double* ls = s_sum.v[lane_of(d, cell)];
+                    atomicAdd(ls + 0, dw);
+                    atomicAdd(ls + 1, de);
+                }
             }
         }
     }
@@ -869,7 +867,7 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
 // resolved to (lidx remap when it folded into a nearer id).
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
-    __shared__ LaneSums<6> s_sum;   // drop_w, drop_e, -, -, Wout, Eout
+    __shared__ LaneSums<2> s_sum;   // drop_w, drop_e
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
     const int n = 4 * gs->n_listed;
@@ -893,7 +891,7 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
         unsigned um = __ballot_sync(kFull, sb != kEmpty);
         const float* bv = bucket_vals(b);
         const uint32_t* kept = d.bid + (size_t)dst * kKb;
-        double g[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        double g[2] = {0.0, 0.0};
         while (um) {
             const int s = __ffs(um) - 1;
             um &= um - 1;
@@ -915,20 +913,19 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
                 }
                 const int le = sel != bid ? remap_lidx<Lay>(l, bid, sel) : l;
                 atomicAdd(o + le, w);
-                const int Eb = ebin_of<Lay>(d, sel, le);
                 if (sel != bid && d.esplit)
-                    eshift += (double)((e_center(d, ebin_of<Lay>(d, bid, l)) - e_center(d, Eb)) * w);
-                g[4] += (double)w;
-                g[5] += (double)w * (double)e_center(d, Eb);
+                    eshift += (double)((e_center(d, ebin_of<Lay>(d, bid, l)) - e_center(d, ebin_of<Lay>(d, sel, le))) * w);
             }
             eshift = warp_sum(eshift);
             if (lane == 0 && eshift != 0.0) atomicAdd(d.dl_edep + src, eshift);
         }
         double* ls = s_sum.v[lane_of(d, src)];
+        if (__any_sync(kFull, g[0] != 0.0 || g[1] != 0.0)) {
 #pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            const double x = warp_sum(g[k]);
-            if (lane == 0 && x != 0.0) atomicAdd(ls + k, x);
+            for (int k = 0; k < 2; ++k) {
+                const double x = warp_sum(g[k]);
+                if (lane == 0 && x != 0.0) atomicAdd(ls + k, x);
+            }
         }
     }
     __syncthreads();
@@ -1027,9 +1024,11 @@ __device__ __forceinline__ double fold_tally(const Dev& d, int c, int k) {
 // K5 audit of the iteration, warp per cell of psi_in's list (whose storage
 // the classify kernel already cleared); the last block writes each working
 // lane's audit record and swaps the occupancy lists (K6).
+template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
     constexpr int NW = kThreads / 32;
     __shared__ LaneSums<7> s_sum;   // Edep, Ecut, Enuc, Ebnd, Wcut, Wnuc, Wbnd
+    __shared__ float s_out[kMaxLanes][2];   // psi_out weight and bin-centre energy
     __shared__ int s_last;
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
@@ -1038,7 +1037,47 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nw = gridDim.x * NW;
     s_sum.zero(d.B);
+    for (int i = threadIdx.x; i < 2 * d.B; i += blockDim.x) (&s_out[0][0])[i] = 0.0f;
     __syncthreads();
+    // psi_out's weight and bin-centre energy per lane, from the values the
+    // deposit pass left (K5_ConservationAudit's psi_out sums,
+    // k5_audit.cu:22-167): warp per (occupied psi_out cell, slot), all of a
+    // slot's loads in flight at once as float4s.  A lane's float4s (4 q .. 4 q
+    // + 3 for q = lane + 32 k) lie in one energy bin of the slot's block
+    // (NT is a multiple of 4 and 128 / NT a multiple of NE), so one bin
+    // centre serves them.  Float sums per slot and per block (FP64 is a
+    // scarce pipe on this part), converted to double once per block; a slot's
+    // sum of at most 256 values keeps about 1e-7 of relative precision.
+    static_assert(Lay::NT % 4 == 0 && (128 / Lay::NT) % Lay::NE == 0 && Lay::L % 128 == 0,
+                  "a lane's float4s share one local energy bin");
+    const int nout = gs->occ_n[in ^ 1];
+    for (int wi = blockIdx.x * NW + wid; wi < nout * kKb; wi += nw) {
+        const int gc = d.occ_list[in ^ 1][wi / kKb];
+        const int s = wi % kKb;
+        const uint32_t bs = d.bid[(size_t)gc * kKb + s];
+        if (bs == kEmpty) continue;
+        const float4* v = reinterpret_cast<const float4*>(d.val + ((size_t)gc * kKb + s) * Lay::L);
+        float4 wv[Lay::L / 128];
+#pragma unroll
+        for (int k = 0; k < Lay::L / 128; ++k) wv[k] = __ldcg(v + lane + 32 * k);
+        const int Eb = max(0, min((int)((bs >> 12) & 0xFFFu) * Lay::NE + (4 * lane / Lay::NT) % Lay::NE, d.N_E - 1));
+        float W = 0.0f;
+#pragma unroll
+        for (int k = 0; k < Lay::L / 128; ++k) {
+            if (wv[k].x > 0.0f) W += wv[k].x;
+            if (wv[k].y > 0.0f) W += wv[k].y;
+            if (wv[k].z > 0.0f) W += wv[k].z;
+            if (wv[k].w > 0.0f) W += wv[k].w;
+        }
+        float E = W * e_center(d, Eb);
+        W = warp_sumf(W);
+        E = warp_sumf(E);
+        if (lane == 0 && W != 0.0f) {
+            float* ls = s_out[lane_of(d, gc)];
+            atomicAdd(ls + 0, W);
+            atomicAdd(ls + 1, E);
+        }
+    }
     for (int wi = blockIdx.x * NW + wid; wi < nocc; wi += nw) {
         const int c = d.occ_list[in][wi];
         const int cls = d.cls[c];
@@ -1054,6 +1093,10 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
     }
     __syncthreads();
     s_sum.flush(d, LANE_DOUBLE(Edep));
+    for (int i = threadIdx.x; i < 2 * d.B; i += blockDim.x) {
+        const float x = (&s_out[0][0])[i];
+        if (x != 0.0f) atomicAdd(reinterpret_cast<double*>(d.ls + i / 2) + LANE_DOUBLE(Wout) + i % 2, (double)x);
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(&gs->blocks_done, 1u) == gridDim.x - 1;
@@ -1366,6 +1409,8 @@ struct Ctx {
     cudaEvent_t ev[10] = {};   // 0..7 one iteration's stages, 8..9 a whole run
     float step_ms[7] = {};
     int grid_cell = 0, grid_transport = 0, grid_keys = 0;   // warp-per-cell kernels, deposit pass, claim pass
+    int grid_fin = 0;   // finalize: four blocks per SM (its per-block flushes of per-lane sums are atomics on a
+                        // few addresses; 13.2 ms per wave of 80 spots against 14.2 at eight, 14.8 at three)
     size_t ctab_words = 0;                   // claim-table size in 64-bit words
     size_t ccount_n = 0;
     bool injected = false;
@@ -1433,7 +1478,7 @@ struct Impl {
         CK(rec(5));
         if (bk) k_bucket_push<Lay><<<gc, kThreads, 0, c.s>>>(c.d);
         CK(rec(6));
-        k_finalize<<<gc, kThreads, 0, c.s>>>(c.d);
+        k_finalize<Lay><<<c.grid_fin, kThreads, 0, c.s>>>(c.d);
         CK(rec(7));
         CK(cudaGetLastError());
         return 0;
@@ -1899,6 +1944,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     // latency-bound and gain from the warps in flight; finalize's last-block
     // step grows with the grid beyond that)
     c->grid_cell = std::max(1, std::min((int)((NcB + kThreads / 32 - 1) / (kThreads / 32)), 8 * std::max(sms, 1)));
+    c->grid_fin = std::max(1, std::min(c->grid_cell, 4 * std::max(sms, 1)));
     if ((rc = DISPATCH(*c, transport_grid, sms))) return bail(rc);
     if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "create sync"));
     *out = c;

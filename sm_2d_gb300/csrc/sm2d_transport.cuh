@@ -31,8 +31,6 @@ struct Tally {                // per-lane accumulators of one work item
     double edep, e_cut, e_nuc, e_bnd;
     float w_cut, w_nuc, w_bnd;
     double drop_w, drop_e;    // slot / bucket / prune drops
-    double Win, Ein;          // psi_in weight and energy of the bins read
-    double Wout, Eout;        // weight and bin-centre energy deposited in psi_out
 };
 
 // The component being transported: its cell, psi_in slot and local bin give
@@ -234,12 +232,10 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
             const int os = resolve(d, psi_row(d, dcell), d.bid + (size_t)dcell * kKb, src.tag, selb, seld);
             if (os >= 0) {
                 const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
-                const int e2 = ebin_of<Lay>(d, seld, le2);
                 if (seld != selb && d.esplit)
-                    atomicAdd(d.dl_edep + bcell, (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, e2)) * w));
+                    atomicAdd(d.dl_edep + bcell,
+                              (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, ebin_of<Lay>(d, seld, le2))) * w));
                 atomicAdd(d.val + ((size_t)dcell * kKb + os) * Lay::L + le2, w);
-                t.Wout += (double)w;
-                t.Eout += (double)w * (double)e_center(d, e2);
                 return 0.0f;
             }
             stage = 2;
@@ -431,7 +427,6 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             else if (Ebe != Eb) t.edep += (double)((e_center(d, Eb) - e_center(d, Ebe)) * wpart * wcf);
             const int tl = tbe % Lay::NT, El = Ebe % Lay::NE;
             float* vs = vals + (size_t)os * Lay::L;
-            const double Ec_out = (double)e_center(d, max(0, min(Ebe, d.N_E - 1)));
 #pragma unroll
             for (int xs = 0; xs < Lay::NX; ++xs) {
                 if (w[xs] <= 0.0f) continue;   // its share would be 0
@@ -439,8 +434,6 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
                 if (wf <= 0.0f) continue;
                 const float ws = wpart * wf;
                 atomicAdd(vs + Lay::enc(tl, El, xs, zst), ws);
-                t.Wout += (double)ws;
-                t.Eout += (double)ws * Ec_out;
             }
         }
     }
