@@ -838,7 +838,10 @@ __global__ void __launch_bounds__(kThreads) k_select_buckets(Dev d) {
 
 // Occupied cells of psi_out (which = 1, a transport pass) or the cells an
 // injection put on psi_in's list (which = 0), warp per cell: select the kept
-// ids into the cell's slot ids.
+// ids into the cell's slot ids.  In a transport pass the warp then resolves
+// the kept ids of the four bucket rows that lead into the cell (the K4 step
+// of the fused deposit) to the cell's slots, once per pass instead of once
+// per emitted component.
 __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
     constexpr int NW = kThreads / 32;
     __shared__ SelScratch s_sel[NW];
@@ -854,7 +857,28 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
     for (int wi = (which ? 0 : gs->occ_mark) + blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
         const int gc = d.occ_list[k][wi];
         const int nk = select_row(psi_row(d, gc), d.ccount + gc, tag, s_sel[wid], d.bid + (size_t)gc * kKb, lane);
-        if (which && lane == 0) atomicAdd(&s_sum.v[lane_of(d, gc)][0], (double)nk);
+        if (!which) continue;
+        if (lane == 0) atomicAdd(&s_sum.v[lane_of(d, gc)][0], (double)nk);
+        const int ix = gc % d.Nx, iz = (gc / d.Nx) % d.Nz;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {   // the source cell whose face f leads here
+            int src = -1;
+            if (f == FACE_ZP && iz > 0) src = gc - d.Nx;
+            if (f == FACE_ZM && iz + 1 < d.Nz) src = gc + d.Nx;
+            if (f == FACE_XP && ix > 0) src = gc - 1;
+            if (f == FACE_XM && ix + 1 < d.Nx) src = gc + 1;
+            if (src < 0) continue;
+            const int base = d.c2b[src];
+            if (base < 0) continue;
+            const size_t e = (size_t)(base + f) * kKb + lane;
+            const uint32_t id = d.bkt_ids[e];
+            int os = -1;
+            if (id != kEmpty) {
+                uint32_t sel;
+                os = resolve(d, psi_row(d, gc), d.bid + (size_t)gc * kKb, tag, id, sel);
+            }
+            d.bkt_os[e] = (int8_t)os;
+        }
     }
     __syncthreads();
     if (which) s_sum.flush(d, LANE_DOUBLE(slots_out_it));
@@ -1862,6 +1886,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.ctab, unsigned long long, c->ctab_words);
     A(d.ccount, int, c->ccount_n);
     A(d.bkt_ids, uint32_t, (size_t)4 * d.listed_cap * kKb);
+    A(d.bkt_os, int8_t, (size_t)4 * d.listed_cap * kKb);
     A(c->beams_dev, BeamArgs, B);
     // lateral post-convolution kernels per lane and depth row: half widths
     // are at most Nx/2

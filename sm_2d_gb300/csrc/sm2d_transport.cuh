@@ -228,9 +228,10 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
                 return 0.0f;
             }
             // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
-            uint32_t seld;
-            const int os = resolve(d, psi_row(d, dcell), d.bid + (size_t)dcell * kKb, src.tag, selb, seld);
+            // slot that the selection resolved for it
+            const int os = d.bkt_os[(size_t)bf * kKb + kb];
             if (os >= 0) {
+                const uint32_t seld = d.bid[(size_t)dcell * kKb + os];
                 const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
                 if (seld != selb && d.esplit)
                     atomicAdd(d.dl_edep + bcell,
