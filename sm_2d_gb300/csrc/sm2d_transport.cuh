@@ -289,6 +289,22 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
     if (weight <= 0.0f) return 0.0f;
     constexpr int N = 11;
     sigma = fmaxf(sigma, 1e-6f);
+    {
+        // the centre column's edges xmin + 5 dx and xmin + 6 dx, as the loop
+        // below computes them: beyond 8 sigma on both sides every CDF value is
+        // exactly 0 left of the column and 1 right of it (gauss_cdf), so the
+        // weights are exactly (0, .., 1, .., 0) after both normalisations
+        const float xmin = xoff - 0.5f * (float)N * d.dx;
+        const float dl = (xmin + (float)(N / 2) * d.dx) - xoff, dr = (xmin + (float)(N / 2 + 1) * d.dx) - xoff;
+        if (dl < -8.0f * sigma && dr > 8.0f * sigma) {
+            if ((src / d.Nx) % d.Nz + 1 >= d.Nz) {
+                boundary_w += weight;
+                return 0.0f;
+            }
+            const EmitPlan pl = plan_emission(d, theta, E);
+            return emit_component<Lay, PASS>(d, sc, par, src, FACE_ZP, src + d.Nx, N / 2, pl, weight, Lay::NX / 2, 0, t);
+        }
+    }
     float w[N];
     {
         const float dx = d.dx;
