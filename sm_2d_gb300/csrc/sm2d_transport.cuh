@@ -387,10 +387,20 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
         mark_occupied(d, outp, cell);
     } else {
         float w[Lay::NX];
-        {
-            const float sg = fmaxf(sig_sub, 1e-6f);
-            const float dxs = dx / (float)Lay::NX;
-            const float xmin = -dx * 0.5f;
+        const float sg = fmaxf(sig_sub, 1e-6f);
+        const float dxs = dx / (float)Lay::NX;
+        const float xmin = -dx * 0.5f;
+        // the sub-bin k holding x_new, with its edges as the loop below
+        // computes them: beyond 8 sigma on both sides every CDF value is
+        // exactly 0 left of it and 1 right of it, so the weights are exactly
+        // the unit vector e_k and their sum 1 (any other k fails the test)
+        const int kc = max(0, min((int)floorf((x_new - xmin) / dxs), Lay::NX - 1));
+        const bool unit = ((xmin + (float)kc * dxs) - x_new < -8.0f * sg) &&
+                          ((xmin + (float)(kc + 1) * dxs) - x_new > 8.0f * sg);
+        if (unit) {
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) w[i] = (i == kc) ? 1.0f : 0.0f;
+        } else {
             float prev = gauss_cdf(xmin, x_new, sg);
 #pragma unroll
             for (int i = 0; i < Lay::NX; ++i) {
