@@ -145,6 +145,11 @@ struct Dev {
     float lutEmin, lutEmax;
     const float *R, *logE, *logR;
     float R_fine_on;      // lut_range(max(E_fine_on, lutEmin)), evaluated once on the device
+    // per energy bin, K2 at the bin-centre energy over the coarse step in a
+    // row of density 1 whose step does not split at the fine threshold:
+    // range, energy loss, nuclear survival, scattering power (the transport's
+    // own arithmetic, evaluated once on the device) [N_E]
+    const float4* k2tab;
     // search tables (slot_of): the energy bin / R index where the searches
     // of the slot's smallest value end
     const int *e_slot, *r_slot;

@@ -1269,6 +1269,21 @@ __global__ void k_eval_range(Dev d, float E, float* out) {
     *out = lut_range(d, E);
 }
 
+// K2's physics per energy bin at density 1 over the coarse step (Dev::k2tab):
+// the expressions of the K2 branch of transport_bin with rho = 1
+__global__ void k_k2_table(Dev d, float4* tab) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.N_E) return;
+    const float E = d.Ee[b] + 1.0f * ((d.Ee[b + 1] - d.Ee[b]) * 0.5f);
+    const float rs = fminf(d.step_coarse, fminf(d.dx, d.dz));
+    const float rho = 1.0f;
+    const float RE = lut_range(d, E);
+    const float dE = fminf(lut_energy_loss(d, E, RE, rho * rs), E);
+    const float surv = sm2d_expf(-nuclear_xs(E) * (rho * rs));
+    const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), fmaxf(rs, 0.0f), rho);
+    tab[b] = make_float4(RE, dE, surv, T);
+}
+
 // ------------------------------------------------------------------ spot plan
 // Outcome of a lane's spot (sm2d_spot_result).
 __host__ __device__ inline void lane_result(const LaneState& L, sm2d_spot_result& r) {
@@ -1942,6 +1957,12 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
         if (cudaMemcpyAsync(&d.R_fine_on, rf, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return bail(fail(SM2D_ERR_CUDA, "LUT setup"));
+        void* q2 = nullptr;
+        if ((rc = dalloc(*c, &q2, sizeof(float4) * (size_t)d.N_E))) return bail(rc);
+        k_k2_table<<<(d.N_E + 255) / 256, 256, 0, s>>>(d, static_cast<float4*>(q2));
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+            return bail(fail(SM2D_ERR_CUDA, "K2 table setup"));
+        d.k2tab = static_cast<const float4*>(q2);
     }
     // every lane starts with the problem's tables
     c->fe_host.assign(3 * BN + B, 0.0f);

@@ -654,16 +654,19 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         float lim = fminf(d.step_coarse, fminf(dx, dz));
         float rs = lim;
         bool split = false;
-        const float RE = lut_range(d, E);
+        const bool tab = d.k2tab && rho == 1.0f && Ebin < d.N_E;   // the table's values are this arithmetic's
+        const float4 q = tab ? __ldg(d.k2tab + Ebin) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float RE = tab ? q.x : lut_range(d, E);
         if (E > d.E_fine_on + 1e-6f) {
             const float rtf = (RE - d.R_fine_on) / rho;   // geometric distance to the fine threshold
             if (rtf > 0.0f && rtf < rs) { rs = rtf; lim = rs; split = true; }
         }
         step = lim;
-        dE = fminf(lut_energy_loss(d, E, RE, rho * rs), E);
+        const bool use = tab && !split;
+        dE = use ? q.y : fminf(lut_energy_loss(d, E, RE, rho * rs), E);
         E_new = E - dE;
         edep = dE * w;
-        const float surv = sm2d_expf(-nuclear_xs(E) * (rho * rs));
+        const float surv = use ? q.z : sm2d_expf(-nuclear_xs(E) * (rho * rs));
         w_new = w * surv;
         w_rem = w - w_new;
         if (split && E_new > d.E_fine_on) {
@@ -680,7 +683,7 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         const float B0 = 0.5f * A0 * p0;
         const float sx0 = d.sx0[ln];
         const float C0 = sx0 * sx0 + (A0 * p0 * p0) / 3.0f;
-        const float T = scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm, rho);
+        const float T = use ? q.w : scatter_power(fmaxf(E - 0.5f * dE, d.lutEmin), sm, rho);
         const float A1 = fmaxf(A0 + T * sm, 0.0f);
         const float C1 = fmaxf(C0 + 2.0f * B0 * sm + A0 * sm * sm + (1.0f / 3.0f) * T * sm * sm * sm, 0.0f);
         sig_th = sqrtf(fmaxf(A1 - A0, 0.0f));
