@@ -620,7 +620,7 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         const float sxp = (eta0 > 0) ? (hx - xc) / eta0 : 1e30f;
         const float sxm = (eta0 < 0) ? (-hx - xc) / eta0 : 1e30f;
         const float sb = fmaxf(fminf(fminf(szp, szm), fminf(sxp, sxm)), 0.0f);
-        const float RE = lut_range(d, E);
+        const float RE = d.k2tab ? __ldg(d.k2tab + Ebin).x : lut_range(d, E);   // Ebin is clamped here
         step = fminf(fine_step_limit(E, RE) / rho, sb * 1.001f);
         const float mean_dE = lut_energy_loss(d, E, RE, rho * step);
         if (d.straggle) {
@@ -654,9 +654,12 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         float lim = fminf(d.step_coarse, fminf(dx, dz));
         float rs = lim;
         bool split = false;
-        const bool tab = d.k2tab && rho == 1.0f && Ebin < d.N_E;   // the table's values are this arithmetic's
-        const float4 q = tab ? __ldg(d.k2tab + Ebin) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        const float RE = tab ? q.x : lut_range(d, E);
+        // the table's values are this arithmetic's: the range for any row, the
+        // rest for a density-1 row whose step does not split
+        const bool inr = d.k2tab && Ebin < d.N_E;
+        const bool tab = inr && rho == 1.0f;
+        const float4 q = inr ? __ldg(d.k2tab + Ebin) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float RE = inr ? q.x : lut_range(d, E);
         if (E > d.E_fine_on + 1e-6f) {
             const float rtf = (RE - d.R_fine_on) / rho;   // geometric distance to the fine threshold
             if (rtf > 0.0f && rtf < rs) { rs = rtf; lim = rs; split = true; }
