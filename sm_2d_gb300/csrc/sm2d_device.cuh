@@ -411,14 +411,15 @@ __device__ __forceinline__ void cand_insert(unsigned long long* row, int* count,
 }
 
 // Slot assigned to `bid` by the selection of this pass, -1 if not gathered.
+// An entry's id and slot words are read together (entries are 16-byte
+// aligned), one L2 round trip per probe.
 __device__ __forceinline__ int cand_find(const unsigned long long* row, uint32_t tag, uint32_t bid) {
     const unsigned long long tb = ((unsigned long long)tag << 32) | bid;
     const unsigned h = cand_hash(bid);
     for (int p = 0; p < kCand; ++p) {
-        const unsigned long long* e = row + 2 * ((h + p) & (kCand - 1));
-        const unsigned long long cur = __ldcg(e);
-        if (cur == tb) return (int)((uint32_t)__ldcg(e + 1) & 31u);
-        if ((uint32_t)(cur >> 32) != tag) return -1;
+        const ulonglong2 e = __ldcg(reinterpret_cast<const ulonglong2*>(row + 2 * ((h + p) & (kCand - 1))));
+        if (e.x == tb) return (int)((uint32_t)e.y & 31u);
+        if ((uint32_t)(e.x >> 32) != tag) return -1;
     }
     return -1;
 }
