@@ -202,8 +202,9 @@ struct Dev {
     unsigned long long* ctab;  // claim tables: B * Nc psi_out rows, then 4 * listed_cap bucket rows
     int* ccount;               // gathered ids per claim-table row
     uint32_t* bkt_ids;         // kept ids of each bucket row [4 * listed_cap][32]
-    int8_t* bkt_os;            // psi_out slot of each kept bucket id in the cell behind the face
-                               // (-1: none), resolved once per pass by the selection [4 * listed_cap][32]
+    uint2* bkt_os;             // psi_out slot of each kept bucket id in the cell behind the face
+                               // (x = slot or -1, y = the kept id there), resolved once per pass by
+                               // the selection [4 * listed_cap][32]
 };
 
 __device__ __forceinline__ int lane_of(const Dev& d, int gc) { return gc / d.Nc; }

@@ -873,11 +873,9 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
             const size_t e = (size_t)(base + f) * kKb + lane;
             const uint32_t id = d.bkt_ids[e];
             int os = -1;
-            if (id != kEmpty) {
-                uint32_t sel;
-                os = resolve(d, psi_row(d, gc), d.bid + (size_t)gc * kKb, tag, id, sel);
-            }
-            d.bkt_os[e] = (int8_t)os;
+            uint32_t sel = kEmpty;
+            if (id != kEmpty) os = resolve(d, psi_row(d, gc), d.bid + (size_t)gc * kKb, tag, id, sel);
+            d.bkt_os[e] = make_uint2((uint32_t)os, sel);
         }
     }
     __syncthreads();
@@ -1901,7 +1899,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.ctab, unsigned long long, c->ctab_words);
     A(d.ccount, int, c->ccount_n);
     A(d.bkt_ids, uint32_t, (size_t)4 * d.listed_cap * kKb);
-    A(d.bkt_os, int8_t, (size_t)4 * d.listed_cap * kKb);
+    A(d.bkt_os, uint2, (size_t)4 * d.listed_cap * kKb);
     A(c->beams_dev, BeamArgs, B);
     // lateral post-convolution kernels per lane and depth row: half widths
     // are at most Nx/2

@@ -229,9 +229,10 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
             }
             // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
             // slot that the selection resolved for it
-            const int os = d.bkt_os[(size_t)bf * kKb + kb];
+            const uint2 m = __ldcg(d.bkt_os + (size_t)bf * kKb + kb);
+            const int os = (int)m.x;
             if (os >= 0) {
-                const uint32_t seld = d.bid[(size_t)dcell * kKb + os];
+                const uint32_t seld = m.y;
                 const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
                 if (seld != selb && d.esplit)
                     atomicAdd(d.dl_edep + bcell,
