@@ -732,16 +732,19 @@ __device__ int select_row(unsigned long long* row, int* count, uint32_t tag, Sel
     const bool any = *(volatile int*)count > 0;
     int n = 0;
     if (any) {
+        // every entry's id and key words in one 16-byte load, all in flight
+        ulonglong2 e[kCand / 32];
+#pragma unroll
+        for (int q = 0; q < kCand / 32; ++q) e[q] = __ldcg(reinterpret_cast<const ulonglong2*>(row + 2 * (q * 32 + lane)));
 #pragma unroll
         for (int q = 0; q < kCand / 32; ++q) {
             const int i = q * 32 + lane;
-            const unsigned long long tb = __ldcg(row + 2 * i);
-            const bool cur = (uint32_t)(tb >> 32) == tag;
+            const bool cur = (uint32_t)(e[q].x >> 32) == tag;
             const unsigned m = __ballot_sync(kFull, cur);
             if (cur) {
                 const int p = n + __popc(m & lt);
-                sh.bid[p] = (uint32_t)tb;
-                sh.key[p] = (uint32_t)__ldcg(row + 2 * i + 1);
+                sh.bid[p] = (uint32_t)e[q].x;
+                sh.key[p] = (uint32_t)e[q].y;
                 sh.idx[p] = (uint8_t)i;
             }
             n += __popc(m);
