@@ -392,6 +392,57 @@ int sm2d_k5_conservation_audit_static(
  * oracle's build of the same header must agree bit for bit. */
 int sm2d_math_eval(int fn, const float* x, float* y, int n);
 
+/* ---- learned redistribution surrogate of the fine step ----
+ * Replaces the per-bin Highland-MCS / Vavilov-straggling / energy-loss
+ * redistribution of K3_FineTransport (src/cuda/kernels/k3_finetransport.cu:94-760
+ * with src/cuda/device/device_physics.cuh:50-437 and device_lut.cuh:145-168)
+ * by a 4 -> 128 -> 128 -> 32 MLP (ReLU, softmax): inputs (E [MeV], theta
+ * [rad], step [mm], density [g/cm^3]) as float4 rows, outputs 32 weights
+ * (8 theta x 4 E, index theta + 8 E) per row that sum to 1.  The tables of
+ * the method itself come from sm2d_redistribution_table: theta bins of width
+ * pi/512 centred on the incoming direction, E bins of width ln(2500)/256 in
+ * ln E below the incoming energy, end bins holding the tails.  bf16 weights,
+ * fp32 accumulation on the tcgen05 tensor cores, trained on the device
+ * (softmax cross-entropy, Adam).  Device arrays must be 16-byte aligned.
+ * The reference has no learned part; these entries have no counterpart. */
+typedef struct sm2d_mlp* sm2d_mlp_handle;
+int sm2d_mlp_param_count(void);   /* 22816 fp32: W1[128][16] W2[128][128] W3[32][128] b1 b2 b3 */
+/* max_batch: the largest training batch (rounded up to 128); stream: the
+ * cudaStream_t of every launch (NULL: the legacy stream).  Weights start
+ * He-uniform from a fixed seed. */
+int sm2d_mlp_create(int max_batch, void* stream, sm2d_mlp_handle* out);
+int sm2d_mlp_destroy(sm2d_mlp_handle m);
+/* host fp32 parameters in and out (setting them resets the Adam state) */
+int sm2d_mlp_set_params(sm2d_mlp_handle m, const float* host_params);
+int sm2d_mlp_get_params(sm2d_mlp_handle m, float* host_params);
+/* mean softmax cross-entropy of n <= max_batch rows against d_target
+ * [n][32] and its gradient (the fp32 parameter layout) into device arrays */
+int sm2d_mlp_gradients(sm2d_mlp_handle m, const float* d_feats, const float* d_target, int n, float* d_grads,
+                       float* d_loss);
+/* `steps` Adam steps over consecutive batches of the set (wrapping), cosine
+ * learning rate from lr0 to lr_min; per-step loss into d_loss_hist (or NULL) */
+int sm2d_mlp_train(sm2d_mlp_handle m, const float* d_feats, const float* d_target, int n_total, int batch, int steps,
+                   float lr0, float lr_min, float* d_loss_hist);
+/* surrogate tables of n rows into d_table [n][32] */
+int sm2d_mlp_forward(sm2d_mlp_handle m, const float* d_feats, int n, float* d_table);
+/* n training inputs: E log-uniform on [0.1, 250] MeV, theta on +-0.3 rad,
+ * step on [0.05, 2] mm, density on [0.2, 2.0] (hash of seed and row) */
+int sm2d_redistribution_features(int n, uint32_t seed, float* d_feats, void* stream);
+/* the method's own tables (the handle's R-LUT, the transport's physics) */
+int sm2d_redistribution_table(sm2d_handle h, const float* d_feats, int n, float* d_table);
+/* per input region (64 ln E x 8 step x 8 density) the largest absolute weight
+ * error of the surrogate rows against the plain rows; optional host copy of
+ * the 4096 errors (as float bits) */
+int sm2d_mlp_calibrate(sm2d_mlp_handle m, const float* d_feats, const float* d_plain, const float* d_surrogate, int n,
+                       float* host_region_err);
+/* surrogate tables, with the plain table of the handle's physics in the rows
+ * whose calibrated region error exceeds tol (d_fallback[i] = 1 there) */
+int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats, int n, float tol, float* d_table,
+                          int* d_fallback);
+/* table geometry and feature ranges: dtheta, dlnE, ln E_min, ln E_max,
+ * theta_max, step_min, step_max, density_min */
+int sm2d_mlp_geometry(float* out8);
+
 #ifdef __cplusplus
 }
 #endif

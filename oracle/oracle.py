@@ -102,6 +102,7 @@ def _lib(fp64: bool):
         lib.orc_set_density.argtypes = [P, P]
         lib.orc_postprocess.argtypes = [P, P, C.c_float, C.c_int, C.c_int, C.c_float, P]
         lib.orc_math.argtypes = [C.c_int, P, P, C.c_int]
+        lib.orc_redistribution_table.argtypes = [P, C.c_int, P, P]
         _LIBS[key] = lib
         return lib
 
@@ -284,6 +285,13 @@ class Oracle:
                 "source_out_of_grid_energy", "source_slot_dropped_weight", "source_slot_dropped_energy",
                 "source_representation_loss_energy", "iterations", "cell_steps", "slots_in", "slots_out"]
         return dict(zip(keys, s.tolist()))
+
+    def redistribution_table(self, feats):
+        """K3's 8 theta x 4 E redistribution of each (E, theta, step, density) row."""
+        f = np.ascontiguousarray(feats, np.float32).reshape(-1, 4)
+        out = np.zeros((f.shape[0], 32), np.float32)
+        self.lib.orc_redistribution_table(self.ctx, f.shape[0], _p(f), _p(out))
+        return out
 
     def fe(self):
         A, B, S = (np.zeros(self.Nz, np.float32) for _ in range(3))

@@ -151,6 +151,13 @@ void orc_get_drop_channels(const orc_ctx* c, double* w9, double* e9);
 void orc_get_scalars(const orc_ctx* c, double* out14);
 void orc_get_fe(const orc_ctx* c, float* A, float* B, float* sigma_total);
 
+/* K3's per-component redistribution over one step (the surrogate's
+ * targets): feats [n][4] = (E, theta, step, density), out [n][32] with
+ * out[t + 8 e] = w_theta[t] w_E[e]; theta bins of width pi/512 centred on
+ * the incoming direction, E bins of width ln(2500)/256 in ln E below the
+ * incoming energy, tails in the end bins.  Uses the context's R-LUT. */
+void orc_redistribution_table(const orc_ctx* c, int n, const float* feats, float* out);
+
 /* run several independent contexts on n_threads host threads */
 int  orc_run_many(orc_ctx** ctxs, int n, int max_iterations, int n_threads);
 

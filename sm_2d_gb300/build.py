@@ -1,7 +1,7 @@
 """In-tree build of libsm2d.so: the sm_103a CUDA kernels + C ABI.
 
-nvcc compiles the two CUDA translation units (the engine and the stage
-entries) for sm_103a only, g++ compiles the host tables, the output writers
+nvcc compiles the three CUDA translation units (the engine, the stage
+entries and the redistribution surrogate) for sm_103a only, g++ compiles the host tables, the output writers
 and the INI front end with -ffp-contract=off (so an Arm host gives the x86
 float results), g++ links the shared library against the CUDA runtime, and
 gcc builds the run_simulation command over it.  The compiles run in
@@ -53,7 +53,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     cpp_units = ["sm2d_tables.cpp", "sm2d_output.cpp", "sm2d_config.cpp"]
     cpp_objs = [os.path.join(OUT, u.replace(".cpp", ".o")) for u in cpp_units]
-    cu_units = ["sm2d_engine.cu", "sm2d_stages.cu"]
+    cu_units = ["sm2d_engine.cu", "sm2d_stages.cu", "sm2d_surrogate.cu"]
     cu_objs = [os.path.join(OUT, u.replace(".cu", ".o")) for u in cu_units]
     # --fmad=false: every float operation rounds on its own, as the oracle's
     # -ffp-contract=off build does, so that both transport passes (and the

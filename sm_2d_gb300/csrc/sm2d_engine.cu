@@ -1743,6 +1743,18 @@ using namespace sm2d;
 
 struct sm2d_ctx : sm2d::Ctx {};
 
+namespace sm2d {
+// The device view of a handle's grids and R-LUT and its stream, for the
+// redistribution tables of sm2d_surrogate.cu (the transport's own per-bin
+// physics evaluated outside a transport pass).
+int handle_dev(sm2d_handle h, Dev* d, cudaStream_t* s) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    *d = h->d;
+    *s = h->s;
+    return 0;
+}
+}  // namespace sm2d
+
 extern "C" {
 
 int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {

@@ -1,0 +1,162 @@
+"""Learned redistribution surrogate of the fine transport step (host side).
+
+``Surrogate`` owns one network (sm2d_mlp_* in libsm2d.so) and one transport
+handle on the 256-bin log energy grid (0.1-250 MeV) whose R-LUT and per-bin
+physics generate the method's own tables (sm2d_redistribution_table): the
+8 theta x 4 E redistribution of a component of energy E, angle theta, over a
+step of the given length in a medium of the given density, the quantity
+K3_FineTransport (src/cuda/kernels/k3_finetransport.cu:94-760) evaluates per
+bin from device_physics.cuh and device_lut.cuh.  Training, inference and the
+tables all run on the GPU; torch provides the device arrays.  There is no CPU
+path: without the library or a GPU every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .runtime import Config, Transport, check, lib
+
+N_PARAMS = 22816
+N_OUT = 32
+REGIONS = 64 * 8 * 8
+_READY = False
+
+
+def _lib():
+    global _READY
+    L = lib()
+    if not _READY:
+        P, I, F = C.c_void_p, C.c_int, C.c_float
+        L.sm2d_mlp_create.argtypes = [I, P, C.POINTER(P)]
+        L.sm2d_mlp_destroy.argtypes = [P]
+        L.sm2d_mlp_set_params.argtypes = [P, P]
+        L.sm2d_mlp_get_params.argtypes = [P, P]
+        L.sm2d_mlp_gradients.argtypes = [P, P, P, I, P, P]
+        L.sm2d_mlp_train.argtypes = [P, P, P, I, I, I, F, F, P]
+        L.sm2d_mlp_forward.argtypes = [P, P, I, P]
+        L.sm2d_redistribution_features.argtypes = [I, C.c_uint32, P, P]
+        L.sm2d_redistribution_table.argtypes = [P, P, I, P]
+        L.sm2d_mlp_calibrate.argtypes = [P, P, P, P, I, P]
+        L.sm2d_mlp_redistribute.argtypes = [P, P, P, I, F, P, P]
+        L.sm2d_mlp_geometry.argtypes = [P]
+        _READY = True
+    return L
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+class Surrogate:
+    """The network, its training set and the method's tables on cuda:0."""
+
+    def __init__(self, max_batch: int | None = None):
+        import torch
+
+        self.torch = torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("the redistribution surrogate needs a CUDA device")
+        self.L = _lib()
+        # the physics source: a small transport problem on the 256-bin log grid
+        self.t = Transport(Config.log_grid(4, 4, 0.5, 0.5, N_E=256, E_min=0.1, E_max=250.0, N_theta=512))
+        self.sms = torch.cuda.get_device_properties(0).multi_processor_count
+        self.batch = 128 * self.sms   # one 128-sample tile per SM
+        h = C.c_void_p()
+        check(self.L.sm2d_mlp_create(max(self.batch, max_batch or 0), self.t.stream(), C.byref(h)))
+        self.m = h
+
+    def close(self):
+        if getattr(self, "m", None):
+            self.L.sm2d_mlp_destroy(self.m)
+            self.m = None
+        if getattr(self, "t", None):
+            self.t.close()
+            self.t = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _sync(self):
+        self.torch.cuda.synchronize()
+
+    def features(self, n: int, seed: int):
+        """n inputs (E, theta, step, density) of the training distribution, [n][4] on the device."""
+        f = self.torch.empty((n, 4), dtype=self.torch.float32, device="cuda")
+        self._sync()
+        check(self.L.sm2d_redistribution_features(n, seed, _ptr(f), self.t.stream()))
+        self._sync()
+        return f
+
+    def plain(self, feats):
+        """The method's own tables of the rows of feats, [n][32] on the device."""
+        out = self.torch.empty((feats.shape[0], N_OUT), dtype=self.torch.float32, device="cuda")
+        self._sync()
+        check(self.L.sm2d_redistribution_table(self.t.h, _ptr(feats), feats.shape[0], _ptr(out)))
+        self._sync()
+        return out
+
+    def forward(self, feats):
+        out = self.torch.empty((feats.shape[0], N_OUT), dtype=self.torch.float32, device="cuda")
+        self._sync()
+        check(self.L.sm2d_mlp_forward(self.m, _ptr(feats), feats.shape[0], _ptr(out)))
+        self._sync()
+        return out
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(N_PARAMS, np.float32)
+        check(self.L.sm2d_mlp_get_params(self.m, p.ctypes.data_as(C.c_void_p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(self.L.sm2d_mlp_set_params(self.m, p.ctypes.data_as(C.c_void_p)))
+
+    def gradients(self, feats, target):
+        """(loss, gradient) of the mean cross-entropy of the rows; no update."""
+        g = self.torch.empty(N_PARAMS, dtype=self.torch.float32, device="cuda")
+        loss = self.torch.empty(1, dtype=self.torch.float32, device="cuda")
+        self._sync()
+        check(self.L.sm2d_mlp_gradients(self.m, _ptr(feats), _ptr(target), feats.shape[0], _ptr(g), _ptr(loss)))
+        self._sync()
+        return float(loss.item()), g.cpu().numpy()
+
+    def train(self, feats, target, steps: int, lr0: float = 2e-3, lr_min: float = 2e-5, batch: int | None = None):
+        """Adam steps over the set; returns the per-step loss."""
+        batch = batch or self.batch
+        hist = self.torch.zeros(max(steps, 1), dtype=self.torch.float32, device="cuda")
+        self._sync()
+        check(self.L.sm2d_mlp_train(self.m, _ptr(feats), _ptr(target), feats.shape[0], batch, steps, lr0, lr_min,
+                                    _ptr(hist)))
+        self._sync()
+        return hist[:steps].cpu().numpy()
+
+    def calibrate(self, feats, plain=None):
+        """Per-region largest weight error of the network against the method, as float [4096]."""
+        plain = self.plain(feats) if plain is None else plain
+        surr = self.forward(feats)
+        err = np.zeros(REGIONS, np.float32)
+        check(self.L.sm2d_mlp_calibrate(self.m, _ptr(feats), _ptr(plain), _ptr(surr), feats.shape[0],
+                                        err.ctypes.data_as(C.c_void_p)))
+        return err
+
+    def redistribute(self, feats, tol: float = 0.005):
+        """Network tables with the method's rows where the calibrated error exceeds tol."""
+        n = feats.shape[0]
+        out = self.torch.empty((n, N_OUT), dtype=self.torch.float32, device="cuda")
+        fb = self.torch.zeros(n, dtype=self.torch.int32, device="cuda")
+        self._sync()
+        check(self.L.sm2d_mlp_redistribute(self.m, self.t.h, _ptr(feats), n, tol, _ptr(out), _ptr(fb)))
+        self._sync()
+        return out, fb
+
+    @staticmethod
+    def geometry():
+        g = np.zeros(8, np.float32)
+        check(_lib().sm2d_mlp_geometry(g.ctypes.data_as(C.c_void_p)))
+        return dict(zip(["dtheta", "dlnE", "lnE_min", "lnE_max", "theta_max", "step_min", "step_max",
+                         "density_min"], g.tolist()))

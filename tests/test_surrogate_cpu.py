@@ -1,0 +1,114 @@
+"""CPU checks of the redistribution surrogate's oracle: the method's tables
+(C restatement of K3's per-bin physics) and the network's float64/bf16
+restatement, its gradient against finite differences, and the host helpers."""
+import numpy as np
+import pytest
+
+import sm_2d_gb300 as sm
+from oracle import oracle as orc
+from oracle import surrogate as so
+
+
+def table_oracle():
+    cfg = sm.Config.log_grid(4, 4, 0.5, 0.5, N_E=256, E_min=0.1, E_max=250.0, N_theta=512)
+    return orc.Oracle(cfg.oracle_config(), cfg.theta_edges, cfg.E_edges)
+
+
+def sample_features(n, seed):
+    r = np.random.default_rng(seed)
+    return np.stack([np.exp(r.uniform(np.log(0.1), np.log(250.0), n)), r.uniform(-0.3, 0.3, n),
+                     r.uniform(0.05, 2.0, n), r.uniform(0.2, 2.0, n)], axis=1).astype(np.float32)
+
+
+def test_tables_are_distributions():
+    o = table_oracle()
+    t = o.redistribution_table(sample_features(4000, 1))
+    assert t.shape == (4000, 32)
+    assert (t >= 0).all()
+    np.testing.assert_allclose(t.sum(axis=1), 1.0, atol=2e-6)
+
+
+def test_table_physics_limits():
+    o = table_oracle()
+    # 150 MeV over 0.1 mm of water: energy loss far below a bin, so all weight in
+    # E bin 0; sigma_theta well below a bin, so the two bins around the incoming
+    # direction (3 and 4) share it equally
+    t = o.redistribution_table(np.array([[150.0, 0.1, 0.1, 1.0]], np.float32))[0].reshape(4, 8)
+    assert t[1:].sum() < 1e-6
+    assert abs(t[0, 3] - 0.5) < 1e-3 and abs(t[0, 4] - 0.5) < 1e-3
+    # 1 MeV over 2 mm: the mean energy falls to the LUT floor (R(1 MeV) is about
+    # 0.02 mm), so most weight is in the lowest E bin; the straggling sigma of
+    # the step (Bohr, several MeV at this beta) puts the rest in the top bin,
+    # and the angle spreads into the end bins
+    t = o.redistribution_table(np.array([[1.0, 0.0, 2.0, 1.0]], np.float32))[0].reshape(4, 8)
+    assert t[3].sum() > 0.5 and t[1:3].sum() < 0.02
+    assert t[3, 0] > 0.05 and t[3, 7] > 0.05
+    # the incoming angle does not enter the relative bins
+    a = o.redistribution_table(np.array([[20.0, -0.2, 1.0, 1.5], [20.0, 0.25, 1.0, 1.5]], np.float32))
+    np.testing.assert_array_equal(a[0], a[1])
+
+
+def test_fp32_table_matches_fp64_method():
+    cfg = sm.Config.log_grid(4, 4, 0.5, 0.5, N_E=256, E_min=0.1, E_max=250.0, N_theta=512)
+    o32 = orc.Oracle(cfg.oracle_config(), cfg.theta_edges, cfg.E_edges)
+    o64 = orc.Oracle(cfg.oracle_config(), cfg.theta_edges, cfg.E_edges, fp64=True)
+    f = sample_features(3000, 2)
+    d = np.abs(o32.redistribution_table(f) - o64.redistribution_table(f))
+    assert d.max() < 2e-3, d.max()
+    assert d.mean() < 1e-5
+
+
+def test_gradient_matches_finite_differences():
+    r = np.random.default_rng(3)
+    f = sample_features(64, 4)
+    y = r.dirichlet(np.ones(32), 64)
+    p = so.init_params().astype(np.float64)
+    p[so.O_B1:] = r.normal(0, 0.1, so.N_PARAMS - so.O_B1)
+    g = so.grad_exact(p, f, y)
+    idx = np.concatenate([r.choice(np.arange(so.O_W1, so.O_W2).reshape(-1, 16)[:, :4].ravel(), 8),
+                          r.choice(np.arange(so.O_W2, so.O_W3), 8), r.choice(np.arange(so.O_W3, so.O_B1), 8),
+                          r.choice(np.arange(so.O_B1, so.N_PARAMS), 8)])
+    h = 1e-4   # smaller steps lose digits to cancellation in the float64 loss
+    for k in idx:
+        a, b = p.copy(), p.copy()
+        a[k] += h
+        b[k] -= h
+        fd = (so.loss_exact(a, f, y) - so.loss_exact(b, f, y)) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 + 1e-4 * abs(g[k]), (k, fd, g[k])
+
+
+def test_bf16_restatement_close_to_exact_gradient():
+    r = np.random.default_rng(5)
+    o = table_oracle()
+    f = sample_features(512, 6)
+    y = o.redistribution_table(f)
+    p = so.init_params()
+    loss, g = so.loss_and_grad(p, f, y)
+    ge = so.grad_exact(p, f, y)
+    assert abs(loss - so.loss_exact(p, f, y)) < 2e-2 * abs(loss)
+    for lo, hi in [(so.O_W2, so.O_W3), (so.O_W3, so.O_B1), (so.O_B2, so.O_B3), (so.O_B3, so.N_PARAMS)]:
+        rel = np.linalg.norm(g[lo:hi] - ge[lo:hi]) / np.linalg.norm(ge[lo:hi])
+        assert rel < 0.1, (lo, rel)
+
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, -2.5, 3.0e-3], np.float32)
+    b = so.bf16(x)
+    assert b[0] == 1.0 and b[1] == 1.0 and b[2] == np.float32(1.0 + 2 ** -6) and b[3] == -2.5
+    assert abs(b[4] - 3.0e-3) / 3.0e-3 < 2 ** -8
+
+
+def test_surrogate_geometry_exported():
+    g = sm.Surrogate.geometry()
+    assert abs(g["dtheta"] - np.pi / 512) < 1e-7
+    assert abs(g["dlnE"] - np.log(2500.0) / 256) < 1e-7
+    assert g["step_min"] == pytest.approx(0.05) and g["step_max"] == pytest.approx(2.0)
+
+
+def test_adam_restatement_first_step():
+    p = so.init_params()
+    r = np.random.default_rng(7)
+    g = (r.choice([-1.0, 1.0], so.N_PARAMS) * r.uniform(1e-3, 2e-3, so.N_PARAMS)).astype(np.float32)
+    q, m, v = so.adam(p, g, np.zeros_like(p), np.zeros_like(p), 1, 1e-3)
+    # the first bias-corrected Adam step moves each parameter by lr against its gradient's sign
+    np.testing.assert_allclose(q - p, -1e-3 * np.sign(g), rtol=1e-3, atol=1e-9)
