@@ -267,6 +267,88 @@ def run_reference_arm(args):
 
 
 # ---------------------------------------------------------------- GPU arm
+def surrogate_leg(n_train=1 << 21, steps=3000, n_eval=1 << 22, tol=0.01):
+    """The learned redistribution surrogate next to the method it replaces.
+
+    Trains the network on the method's own tables (K3 physics on the device),
+    calibrates the per-region fallback, and times on the library stream with
+    CUDA events, on n_eval fresh rows: the method's table kernel, the
+    network's tcgen05 inference kernel, and the network with fallback.  The
+    tensor roofline of the inference kernel counts the network's algorithmic
+    FLOPs, 2 (4*128 + 128*128 + 128*32) = 41,984 per row.
+    """
+    import torch
+    import sm_2d_gb300 as sm
+
+    s = sm.Surrogate()
+    L, m = s.L, s.m
+    stream = torch.cuda.ExternalStream(s.t.stream())
+    f = s.features(n_train, 101)
+    y = s.plain(f)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    hist = s.train(f, y, steps=steps)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    train_ms = ev[0].elapsed_time(ev[1])
+    s.calibrate(s.features(1 << 20, 102))
+    fe = s.features(n_eval, 103)
+    out = torch.empty((n_eval, 32), dtype=torch.float32, device="cuda")
+    ref = torch.empty_like(out)
+    fb = torch.zeros(n_eval, dtype=torch.int32, device="cuda")
+    P = C.c_void_p
+
+    def timed(fn, reps=10):
+        fn()
+        s.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        s.sync()
+        return e0.elapsed_time(e1) / reps
+
+    t_plain = timed(lambda: L.sm2d_redistribution_table(s.t.h, P(fe.data_ptr()), n_eval, P(ref.data_ptr())))
+    t_net = timed(lambda: L.sm2d_mlp_forward(m, P(fe.data_ptr()), n_eval, P(out.data_ptr())))
+    err = (out - ref).abs()
+    mean_err = float(err.mean())
+    t_fb = timed(lambda: L.sm2d_mlp_redistribute(m, s.t.h, P(fe.data_ptr()), n_eval, tol, P(out.data_ptr()),
+                                                 P(fb.data_ptr())))
+    row_err = (out - ref).abs().max(dim=1).values
+    fb_share = float(fb.float().mean())
+    flops = 41984.0 * n_eval
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, src = float(json.load(open(peaks_path))["bf16_tflops"]), "measured (cuBLAS bf16 burst)"
+    else:
+        peak, src = 1900.0, "fallback"
+    achieved = flops / (t_net * 1e-3) / 1e12
+    train_flops = 3.0 * 41984.0 * s.batch * steps
+    res = {
+        "network": "4-128-128-32 ReLU MLP, softmax, bf16 operands, fp32 accumulate (tcgen05)",
+        "training": {"samples": n_train, "steps": steps, "batch": s.batch, "ms": train_ms,
+                     "samples_per_s": s.batch * steps / (train_ms * 1e-3),
+                     "tflops": train_flops / (train_ms * 1e-3) / 1e12,
+                     "loss_first": float(hist[0]), "loss_last": float(np.mean(hist[-50:]))},
+        "rows": n_eval,
+        "plain_rows_per_s": n_eval / (t_plain * 1e-3),
+        "surrogate_rows_per_s": n_eval / (t_net * 1e-3),
+        "surrogate_with_fallback_rows_per_s": n_eval / (t_fb * 1e-3),
+        "surrogate_over_plain": t_plain / t_net,
+        "mean_abs_weight_error": mean_err,
+        "fallback_tol": tol, "fallback_share": fb_share,
+        "row_max_error_q99": float(torch.quantile(row_err[:1 << 20], 0.99)),
+        "row_max_error_max": float(row_err.max()),
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "peak_source": src, "kernel": "k_infer",
+                     "avg_launch_ms": t_net, "algorithmic_flops_per_launch": flops},
+    }
+    s.close()
+    return res
+
+
 def run_gpu_arm(args):
     import torch
     import sm_2d_gb300 as sm
@@ -399,6 +481,10 @@ def run_gpu_arm(args):
         cpu = {"value": v, "unit": "spots/s", "cores": n_threads, "kind": "port",
                "sample": f"the plan's first {n_threads} spots, one per host thread, full transport ({dt:.1f} s wall)"}
 
+    surrogate = None
+    if rank == 0 and not args.no_surrogate and not SMALL:
+        surrogate = surrogate_leg()
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "spots/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -415,7 +501,7 @@ def run_gpu_arm(args):
                 "e2e": {"value": e2e_value, "unit": "spots/s", "h2d_bytes_per_step": int(C.sizeof(Beam) * n),
                         "d2h_bytes_per_step": int(cfg.Nx * cfg.Nz * 8 * n)},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "gpu_launches": launches}
+                "gpu_launches": launches, "surrogate": surrogate}
         print(json.dumps(line))
     t.close()
     if dist:
@@ -431,6 +517,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", default="reference", choices=["reference", "log"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
     ap.add_argument("--lanes", type=int, default=0, help="spots in flight (0: from free device memory)")
     ap.add_argument("--workload", default="plan512", choices=["plan512", "c2", "c3"])
     ap.add_argument("--spots", type=int, default=0, help="spots per step, the plan (0: 512; 64 for c3)")

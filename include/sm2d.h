@@ -404,6 +404,9 @@ int sm2d_math_eval(int fn, const float* x, float* y, int n);
  * ln E below the incoming energy, end bins holding the tails.  bf16 weights,
  * fp32 accumulation on the tcgen05 tensor cores, trained on the device
  * (softmax cross-entropy, Adam).  Device arrays must be 16-byte aligned.
+ * gradients, train, forward and redistribute only enqueue work on the
+ * handle's stream; sm2d_mlp_sync waits for it and reports a device wait that
+ * gave up (SM2D_ERR_TIMEOUT).
  * The reference has no learned part; these entries have no counterpart. */
 typedef struct sm2d_mlp* sm2d_mlp_handle;
 int sm2d_mlp_param_count(void);   /* 22816 fp32: W1[128][16] W2[128][128] W3[32][128] b1 b2 b3 */
@@ -439,6 +442,8 @@ int sm2d_mlp_calibrate(sm2d_mlp_handle m, const float* d_feats, const float* d_p
  * whose calibrated region error exceeds tol (d_fallback[i] = 1 there) */
 int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats, int n, float tol, float* d_table,
                           int* d_fallback);
+/* wait for the handle's stream; SM2D_ERR_TIMEOUT if a kernel's bounded wait gave up */
+int sm2d_mlp_sync(sm2d_mlp_handle m);
 /* table geometry and feature ranges: dtheta, dlnE, ln E_min, ln E_max,
  * theta_max, step_min, step_max, density_min */
 int sm2d_mlp_geometry(float* out8);

@@ -143,6 +143,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 consecutive fp32 columns of this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
@@ -589,12 +605,16 @@ struct InferArgs {
 };
 
 // Persistent inference: weights resident, one 128-sample tile per round.
-__global__ void __launch_bounds__(128, 2) k_infer(InferArgs a) {
+// 256 threads: thread t serves row t % 128 (its TMEM lane); the two
+// warpgroups split the 128 columns of each hidden layer's epilogue, and the
+// first warpgroup does the softmax.
+constexpr int kInferThreads = 256;
+__global__ void __launch_bounds__(kInferThreads, 2) k_infer(InferArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t* bar_w = reinterpret_cast<uint64_t*>(sm + inf::BAR);
     uint64_t* bar_m = bar_w + 1;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + inf::BAR + 16);
-    const int tid = threadIdx.x, warp = tid >> 5, row = tid;
+    const int tid = threadIdx.x, warp = tid >> 5, row = tid & (kTile - 1), half = tid >> 7;
     uint32_t pm = 0;
     bool ok = true;
     if (tid == 0) {
@@ -612,22 +632,22 @@ __global__ void __launch_bounds__(128, 2) k_infer(InferArgs a) {
     }
     fence_after();
     const uint32_t tm = *tslot;
-    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+    const int c0 = half * (kHid / 2);
     ok = bar_wait(bar_w, 0);
     if (__syncthreads_or(!ok)) goto fail;
     for (int tile = blockIdx.x; tile * kTile < a.n; tile += gridDim.x) {
         const int i = tile * kTile + row;
         const bool live = i < a.n;
         float f[4] = {1.0f, 0.0f, 1.0f, 1.0f};
-        {
+        if (live) {
+            const float4 q = a.feats[i];
+            f[0] = q.x; f[1] = q.y; f[2] = q.z; f[3] = q.w;
+        }
+        if (half == 0) {
             float x[kIn];
-            if (live) {
-                const float4 q = a.feats[i];
-                f[0] = q.x; f[1] = q.y; f[2] = q.z; f[3] = q.w;
-                feature_row(f, x);
-            } else {
-                for (int k = 0; k < kIn; ++k) x[k] = 0.0f;
-            }
+            if (live) feature_row(f, x);
+            else for (int k = 0; k < kIn; ++k) x[k] = 0.0f;
             st_row16(sm + inf::X, row, 0, kIn, x);
         }
         fence_before();
@@ -642,12 +662,13 @@ __global__ void __launch_bounds__(128, 2) k_infer(InferArgs a) {
         pm ^= 1;
         if (__syncthreads_or(!ok)) goto fail;
         fence_after();
-        for (int c = 0; c < kHid; c += 16) {
-            float v[16];
-            tmem_ld16(tm + lane_base + c, v);
+        for (int c = c0; c < c0 + kHid / 2; c += 32) {
+            float v[32];
+            tmem_ld32(tm + lane_base + c, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + a.params[ob1 + c + j], 0.0f);
+            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + a.params[ob1 + c + j], 0.0f);
             st_row16(sm + inf::H, row, c, kHid, v);
+            st_row16(sm + inf::H, row, c + 16, kHid, v + 16);
         }
         fence_before();
         fence_async_smem();
@@ -663,12 +684,13 @@ __global__ void __launch_bounds__(128, 2) k_infer(InferArgs a) {
         pm ^= 1;
         if (__syncthreads_or(!ok)) goto fail;
         fence_after();
-        for (int c = 0; c < kHid; c += 16) {
-            float v[16];
-            tmem_ld16(tm + lane_base + 128 + c, v);
+        for (int c = c0; c < c0 + kHid / 2; c += 32) {
+            float v[32];
+            tmem_ld32(tm + lane_base + 128 + c, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + a.params[ob2 + c + j], 0.0f);
+            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + a.params[ob2 + c + j], 0.0f);
             st_row16(sm + inf::H, row, c, kHid, v);
+            st_row16(sm + inf::H, row, c + 16, kHid, v + 16);
         }
         fence_before();
         fence_async_smem();
@@ -684,10 +706,9 @@ __global__ void __launch_bounds__(128, 2) k_infer(InferArgs a) {
         pm ^= 1;
         if (__syncthreads_or(!ok)) goto fail;
         fence_after();
-        {
+        if (half == 0) {
             float z[kOut];
-            tmem_ld16(tm + lane_base + 0, z);
-            tmem_ld16(tm + lane_base + 16, z + 16);
+            tmem_ld32(tm + lane_base + 0, z);
             if (live) {
                 float m = -3.0e38f;
                 int am = 0;
@@ -906,8 +927,7 @@ int sm2d_mlp_gradients(sm2d_mlp_handle m, const float* d_feats, const float* d_t
     if (!aligned16(d_feats) || !aligned16(d_target)) return fail(SM2D_ERR_ARG, "inputs must be 16-byte aligned");
     int rc = launch_train(m, d_feats, d_target, n, 1.0f / (float)n);
     if (!rc) rc = launch_update(m, (n + kTile - 1) / kTile, d_grads, d_loss, 0, 0.0f);
-    if (rc) return rc;
-    return check_err(m);
+    return rc;
 }
 
 int sm2d_mlp_train(sm2d_mlp_handle m, const float* d_feats, const float* d_target, int n_total, int batch, int steps,
@@ -925,7 +945,7 @@ int sm2d_mlp_train(sm2d_mlp_handle m, const float* d_feats, const float* d_targe
         if (rc) return rc;
     }
     m->calibrated = 0;
-    return check_err(m);
+    return 0;
 }
 
 int sm2d_mlp_forward(sm2d_mlp_handle m, const float* d_feats, int n, float* d_table) {
@@ -940,9 +960,9 @@ int sm2d_mlp_forward(sm2d_mlp_handle m, const float* d_feats, int n, float* d_ta
     a.out = d_table;
     a.err = m->err;
     const int tiles = (n + kTile - 1) / kTile;
-    k_infer<<<std::min(tiles, 2 * m->sms), 128, inf::BYTES, m->s>>>(a);
+    k_infer<<<std::min(tiles, 2 * m->sms), kInferThreads, inf::BYTES, m->s>>>(a);
     CK(cudaGetLastError());
-    return check_err(m);
+    return 0;
 }
 
 int sm2d_redistribution_features(int n, uint32_t seed, float* d_feats, void* stream) {
@@ -999,8 +1019,13 @@ int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats
     a.fallback = d_fallback;
     a.err = m->err;
     const int tiles = (n + kTile - 1) / kTile;
-    k_infer<<<std::min(tiles, 2 * m->sms), 128, inf::BYTES, m->s>>>(a);
+    k_infer<<<std::min(tiles, 2 * m->sms), kInferThreads, inf::BYTES, m->s>>>(a);
     CK(cudaGetLastError());
+    return 0;
+}
+
+int sm2d_mlp_sync(sm2d_mlp_handle m) {
+    if (!m) return fail(SM2D_ERR_ARG, "null surrogate handle");
     return check_err(m);
 }
 

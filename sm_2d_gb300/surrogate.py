@@ -41,6 +41,7 @@ def _lib():
         L.sm2d_mlp_calibrate.argtypes = [P, P, P, P, I, P]
         L.sm2d_mlp_redistribute.argtypes = [P, P, P, I, F, P, P]
         L.sm2d_mlp_geometry.argtypes = [P]
+        L.sm2d_mlp_sync.argtypes = [P]
         _READY = True
     return L
 
@@ -84,6 +85,10 @@ class Surrogate:
     def _sync(self):
         self.torch.cuda.synchronize()
 
+    def sync(self):
+        """Wait for the handle's stream; raises if a kernel's bounded wait gave up."""
+        check(self.L.sm2d_mlp_sync(self.m))
+
     def features(self, n: int, seed: int):
         """n inputs (E, theta, step, density) of the training distribution, [n][4] on the device."""
         f = self.torch.empty((n, 4), dtype=self.torch.float32, device="cuda")
@@ -104,6 +109,7 @@ class Surrogate:
         out = self.torch.empty((feats.shape[0], N_OUT), dtype=self.torch.float32, device="cuda")
         self._sync()
         check(self.L.sm2d_mlp_forward(self.m, _ptr(feats), feats.shape[0], _ptr(out)))
+        self.sync()
         self._sync()
         return out
 
@@ -122,6 +128,7 @@ class Surrogate:
         loss = self.torch.empty(1, dtype=self.torch.float32, device="cuda")
         self._sync()
         check(self.L.sm2d_mlp_gradients(self.m, _ptr(feats), _ptr(target), feats.shape[0], _ptr(g), _ptr(loss)))
+        self.sync()
         self._sync()
         return float(loss.item()), g.cpu().numpy()
 
@@ -132,7 +139,7 @@ class Surrogate:
         self._sync()
         check(self.L.sm2d_mlp_train(self.m, _ptr(feats), _ptr(target), feats.shape[0], batch, steps, lr0, lr_min,
                                     _ptr(hist)))
-        self._sync()
+        self.sync()
         return hist[:steps].cpu().numpy()
 
     def calibrate(self, feats, plain=None):
@@ -151,6 +158,7 @@ class Surrogate:
         fb = self.torch.zeros(n, dtype=self.torch.int32, device="cuda")
         self._sync()
         check(self.L.sm2d_mlp_redistribute(self.m, self.t.h, _ptr(feats), n, tol, _ptr(out), _ptr(fb)))
+        self.sync()
         self._sync()
         return out, fb
 
@@ -160,3 +168,39 @@ class Surrogate:
         check(_lib().sm2d_mlp_geometry(g.ctypes.data_as(C.c_void_p)))
         return dict(zip(["dtheta", "dlnE", "lnE_min", "lnE_max", "theta_max", "step_min", "step_max",
                          "density_min"], g.tolist()))
+
+
+def main(argv=None):
+    """Train the surrogate on the method's tables and report its accuracy and speed.
+
+    python -m sm_2d_gb300.surrogate [--train N] [--steps S] [--rows R]
+    """
+    import argparse
+    import json
+
+    import torch
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=1 << 20, help="training rows")
+    ap.add_argument("--steps", type=int, default=1000, help="Adam steps")
+    ap.add_argument("--rows", type=int, default=1 << 20, help="rows of the inference pass")
+    a = ap.parse_args(argv)
+    with Surrogate() as s:
+        f = s.features(a.train, 1)
+        hist = s.train(f, s.plain(f), steps=a.steps)
+        fe = s.features(a.rows, 2)
+        ref = s.plain(fe)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream = torch.cuda.ExternalStream(s.t.stream())
+        e0.record(stream)
+        out = s.forward(fe)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        print(json.dumps({"loss_first": float(hist[0]), "loss_last": float(hist[-1]),
+                          "mean_abs_weight_error": float((out - ref).abs().mean()),
+                          "forward_ms": e0.elapsed_time(e1), "rows": a.rows}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
