@@ -296,9 +296,13 @@ namespace tr {   // training kernel
 constexpr int X = 0, XT = 4096, W1 = 8192, W2 = 12288, W3 = 45056, H1 = 53248, H1T = 86016, H2 = 118784,
               H2T = 151552, D3 = 184320, D3T = 192512, BAR = 200704, BYTES = BAR + 64;
 }
-namespace inf {  // inference kernel (H2 overwrites H1 once the second GEMM is done)
-constexpr int X = 0, W1 = 4096, W2 = 8192, W3 = 40960, H = 49152, BAR = 81920, BYTES = BAR + 64;
+namespace inf {  // inference kernel: weights shared by the CTA, then X and H of each warpgroup's tile
+constexpr int WG = 4;                                       // warpgroups (tiles in flight) per CTA
+constexpr int W1 = 0, W2 = 4096, W3 = 36864, TILE0 = 45056;
+constexpr int XB = 4096, TILE_BYTES = XB + 32768;           // X [128][16], H [128][128] (H2 over H1)
+constexpr int BAR = TILE0 + WG * TILE_BYTES, BYTES = BAR + 96;
 }
+static_assert(inf::BYTES <= 227 * 1024, "inference CTA exceeds shared memory");
 static_assert(tr::BYTES <= 227 * 1024, "training tile exceeds shared memory");
 
 // TMEM columns of the training kernel (512 allocated, one CTA per SM)
@@ -604,25 +608,40 @@ struct InferArgs {
     int* err;
 };
 
-// Persistent inference: weights resident, one 128-sample tile per round.
-// 256 threads: thread t serves row t % 128 (its TMEM lane); the two
-// warpgroups split the 128 columns of each hidden layer's epilogue, and the
-// first warpgroup does the softmax.
-constexpr int kInferThreads = 256;
-__global__ void __launch_bounds__(kInferThreads, 2) k_infer(InferArgs a) {
+// Persistent inference, one CTA per SM with the weights resident in shared
+// memory and four warpgroups, each running its own stream of 128-row tiles
+// with its own X/H buffers, 128 TMEM columns (the three layers reuse them),
+// MMA barrier and named barrier: one tile's GEMMs overlap the other tiles'
+// epilogues.  Thread t of a warpgroup serves row t (TMEM lane t).
+constexpr int kInferThreads = 128 * inf::WG;
+__device__ __forceinline__ void wg_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(g + 1) : "memory"); }
+// barrier of warpgroup g that returns, to all its threads, whether any passed v
+__device__ __forceinline__ bool wg_any(int g, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, %2, 128, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(g + 1)
+        : "memory");
+    return r != 0;
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
+    const int tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, row = tid & (kTile - 1);
     uint64_t* bar_w = reinterpret_cast<uint64_t*>(sm + inf::BAR);
-    uint64_t* bar_m = bar_w + 1;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + inf::BAR + 16);
-    const int tid = threadIdx.x, warp = tid >> 5, row = tid & (kTile - 1), half = tid >> 7;
-    uint32_t pm = 0;
-    bool ok = true;
+    uint64_t* bar_m = bar_w + 1 + g;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + inf::BAR + 48);
+    int* wfail = reinterpret_cast<int*>(sm + inf::BAR + 64);
+    unsigned char* X = sm + inf::TILE0 + g * inf::TILE_BYTES;
+    unsigned char* H = X + inf::XB;
     if (tid == 0) {
         bar_init(bar_w, 1);
-        bar_init(bar_m, 1);
+        for (int k = 0; k < inf::WG; ++k) bar_init(bar_w + 1 + k, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) tmem_alloc(tslot, 256);
+    if (tid < inf::WG) wfail[tid] = 0;
+    if (warp == 0) tmem_alloc(tslot, 512);
     __syncthreads();
     if (tid == 0) {
         bar_expect(bar_w, kHid * kIn * 2 + kHid * kHid * 2 + kOut * kHid * 2);
@@ -631,84 +650,84 @@ __global__ void __launch_bounds__(kInferThreads, 2) k_infer(InferArgs a) {
         bulk_g2s(sm + inf::W3, a.img + iW3, kOut * kHid * 2, bar_w);
     }
     fence_after();
-    const uint32_t tm = *tslot;
+    const uint32_t tm = *tslot + (uint32_t)(g * 128);
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-    const int c0 = half * (kHid / 2);
-    ok = bar_wait(bar_w, 0);
-    if (__syncthreads_or(!ok)) goto fail;
-    for (int tile = blockIdx.x; tile * kTile < a.n; tile += gridDim.x) {
+    uint32_t pm = 0;
+    bool ok = bar_wait(bar_w, 0);
+    if (wg_any(g, !ok)) goto fail;
+    for (int tile = blockIdx.x * inf::WG + g; tile * kTile < a.n; tile += gridDim.x * inf::WG) {
         const int i = tile * kTile + row;
         const bool live = i < a.n;
         float f[4] = {1.0f, 0.0f, 1.0f, 1.0f};
-        if (live) {
-            const float4 q = a.feats[i];
-            f[0] = q.x; f[1] = q.y; f[2] = q.z; f[3] = q.w;
-        }
-        if (half == 0) {
+        {
             float x[kIn];
-            if (live) feature_row(f, x);
-            else for (int k = 0; k < kIn; ++k) x[k] = 0.0f;
-            st_row16(sm + inf::X, row, 0, kIn, x);
+            if (live) {
+                const float4 q = a.feats[i];
+                f[0] = q.x; f[1] = q.y; f[2] = q.z; f[3] = q.w;
+                feature_row(f, x);
+            } else {
+                for (int k = 0; k < kIn; ++k) x[k] = 0.0f;
+            }
+            st_row16(X, row, 0, kIn, x);
         }
-        fence_before();
         fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
+        wg_sync(g);
+        if (row == 0) {
             fence_after();
-            mma(tm + 0, sdesc(su32(sm + inf::X), 256), sdesc(su32(sm + inf::W1), 256), idesc(128, 128), 0);
+            mma(tm, sdesc(su32(X), 256), sdesc(su32(sm + inf::W1), 256), idesc(128, 128), 0);
             mma_commit(bar_m);
         }
         ok = bar_wait(bar_m, pm);
         pm ^= 1;
-        if (__syncthreads_or(!ok)) goto fail;
+        if (wg_any(g, !ok)) goto fail;
         fence_after();
-        for (int c = c0; c < c0 + kHid / 2; c += 32) {
+        for (int c = 0; c < kHid; c += 32) {
             float v[32];
             tmem_ld32(tm + lane_base + c, v);
 #pragma unroll
             for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + a.params[ob1 + c + j], 0.0f);
-            st_row16(sm + inf::H, row, c, kHid, v);
-            st_row16(sm + inf::H, row, c + 16, kHid, v + 16);
+            st_row16(H, row, c, kHid, v);
+            st_row16(H, row, c + 16, kHid, v + 16);
         }
         fence_before();
         fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
+        wg_sync(g);
+        if (row == 0) {
             fence_after();
             for (int k = 0; k < kHid / 16; ++k)
-                mma(tm + 128, sdesc(su32(sm + inf::H) + 256 * k, 2048), sdesc(su32(sm + inf::W2) + 256 * k, 2048),
-                    idesc(128, 128), k > 0);
+                mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W2) + 256 * k, 2048), idesc(128, 128),
+                    k > 0);
             mma_commit(bar_m);
         }
         ok = bar_wait(bar_m, pm);
         pm ^= 1;
-        if (__syncthreads_or(!ok)) goto fail;
+        if (wg_any(g, !ok)) goto fail;
         fence_after();
-        for (int c = c0; c < c0 + kHid / 2; c += 32) {
+        for (int c = 0; c < kHid; c += 32) {
             float v[32];
-            tmem_ld32(tm + lane_base + 128 + c, v);
+            tmem_ld32(tm + lane_base + c, v);
 #pragma unroll
             for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + a.params[ob2 + c + j], 0.0f);
-            st_row16(sm + inf::H, row, c, kHid, v);
-            st_row16(sm + inf::H, row, c + 16, kHid, v + 16);
+            st_row16(H, row, c, kHid, v);
+            st_row16(H, row, c + 16, kHid, v + 16);
         }
         fence_before();
         fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
+        wg_sync(g);
+        if (row == 0) {
             fence_after();
             for (int k = 0; k < kHid / 16; ++k)
-                mma(tm + 0, sdesc(su32(sm + inf::H) + 256 * k, 2048), sdesc(su32(sm + inf::W3) + 256 * k, 2048),
-                    idesc(128, kOut), k > 0);
+                mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W3) + 256 * k, 2048), idesc(128, kOut),
+                    k > 0);
             mma_commit(bar_m);
         }
         ok = bar_wait(bar_m, pm);
         pm ^= 1;
-        if (__syncthreads_or(!ok)) goto fail;
+        if (wg_any(g, !ok)) goto fail;
         fence_after();
-        if (half == 0) {
+        {
             float z[kOut];
-            tmem_ld32(tm + lane_base + 0, z);
+            tmem_ld32(tm + lane_base, z);
             if (live) {
                 float m = -3.0e38f;
                 int am = 0;
@@ -733,20 +752,21 @@ __global__ void __launch_bounds__(kInferThreads, 2) k_infer(InferArgs a) {
             }
         }
         fence_before();
-        __syncthreads();
+        wg_sync(g);   // TMEM and X are reused by the next tile
     }
-    if (warp == 0) {
-        fence_after();
-        tmem_free(tm, 256);
-    }
-    return;
+    goto done;
 fail:
-    if (tid == 0) atomicExch(a.err, 1);
+    if (row == 0) wfail[g] = 1;
+done:
     fence_before();
     __syncthreads();
+    if (tid == 0) {
+        for (int k = 0; k < inf::WG; ++k)
+            if (wfail[k]) atomicExch(a.err, 1);
+    }
     if (warp == 0) {
         fence_after();
-        tmem_free(tm, 256);
+        tmem_free(*tslot, 512);
     }
 }
 
@@ -960,7 +980,7 @@ int sm2d_mlp_forward(sm2d_mlp_handle m, const float* d_feats, int n, float* d_ta
     a.out = d_table;
     a.err = m->err;
     const int tiles = (n + kTile - 1) / kTile;
-    k_infer<<<std::min(tiles, 2 * m->sms), kInferThreads, inf::BYTES, m->s>>>(a);
+    k_infer<<<std::min((tiles + inf::WG - 1) / inf::WG, m->sms), kInferThreads, inf::BYTES, m->s>>>(a);
     CK(cudaGetLastError());
     return 0;
 }
@@ -1019,7 +1039,7 @@ int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats
     a.fallback = d_fallback;
     a.err = m->err;
     const int tiles = (n + kTile - 1) / kTile;
-    k_infer<<<std::min(tiles, 2 * m->sms), kInferThreads, inf::BYTES, m->s>>>(a);
+    k_infer<<<std::min((tiles + inf::WG - 1) / inf::WG, m->sms), kInferThreads, inf::BYTES, m->s>>>(a);
     CK(cudaGetLastError());
     return 0;
 }

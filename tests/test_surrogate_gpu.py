@@ -19,10 +19,12 @@ from oracle import surrogate as so
 
 pytestmark = pytest.mark.gpu
 
-# forward tables: most rows agree to ~1e-8; a hidden activation that lands on a
-# bf16 rounding tie rounds differently on the two sides and moves that row by
-# up to ~5e-3, so the bound is on the share of such rows and on their size
-FWD_ROW_ATOL, FWD_MAX_SHARE, FWD_ATOL = 1e-5, 0.01, 1e-2
+# forward tables: the hidden activations are rounded to bf16 on both sides, but
+# from sums accumulated in different orders (fp32 tensor core, float64 here);
+# a sum within that difference of a bf16 rounding boundary rounds the other
+# way and moves its row by 1e-5..1e-4 (about 2 % of rows), exceptionally by a
+# few 1e-3.  Bounds: the median row, the share of rows above 1e-3, the worst row.
+FWD_MEDIAN, FWD_ROW_ATOL, FWD_MAX_SHARE, FWD_ATOL = 1e-6, 1e-3, 0.01, 1e-2
 GRAD_RTOL = 2e-2    # relative L2 error of each parameter block's gradient
 
 
@@ -65,6 +67,7 @@ def test_forward_matches_oracle(surr):
     t = surr.forward(f).cpu().numpy()
     ref, _ = so.forward(p, f.cpu().numpy())
     d = np.abs(t - ref).max(axis=1)
+    assert np.median(d) <= FWD_MEDIAN, np.median(d)
     assert np.mean(d > FWD_ROW_ATOL) < FWD_MAX_SHARE and d.max() <= FWD_ATOL, (np.mean(d > FWD_ROW_ATOL), d.max())
     np.testing.assert_allclose(t.sum(axis=1), 1.0, atol=1e-6)
 
