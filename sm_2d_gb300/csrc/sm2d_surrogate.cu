@@ -300,7 +300,8 @@ namespace inf {  // inference kernel: weights shared by the CTA, then X and H of
 constexpr int WG = 4;                                       // warpgroups (tiles in flight) per CTA
 constexpr int W1 = 0, W2 = 4096, W3 = 36864, TILE0 = 45056;
 constexpr int XB = 4096, TILE_BYTES = XB + 32768;           // X [128][16], H [128][128] (H2 over H1)
-constexpr int BAR = TILE0 + WG * TILE_BYTES, BYTES = BAR + 96;
+constexpr int BIAS = TILE0 + WG * TILE_BYTES;                // b1, b2, b3 as fp32
+constexpr int BAR = BIAS + (2 * kHid + kOut) * 4, BYTES = BAR + 96;
 }
 static_assert(inf::BYTES <= 227 * 1024, "inference CTA exceeds shared memory");
 static_assert(tr::BYTES <= 227 * 1024, "training tile exceeds shared memory");
@@ -640,7 +641,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
         for (int k = 0; k < inf::WG; ++k) bar_init(bar_w + 1 + k, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    float* bias = reinterpret_cast<float*>(sm + inf::BIAS);
     if (tid < inf::WG) wfail[tid] = 0;
+    for (int k = tid; k < 2 * kHid + kOut; k += kInferThreads) bias[k] = a.params[ob1 + k];
     if (warp == 0) tmem_alloc(tslot, 512);
     __syncthreads();
     if (tid == 0) {
@@ -685,7 +688,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
             float v[32];
             tmem_ld32(tm + lane_base + c, v);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + a.params[ob1 + c + j], 0.0f);
+            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + bias[c + j], 0.0f);
             st_row16(H, row, c, kHid, v);
             st_row16(H, row, c + 16, kHid, v + 16);
         }
@@ -707,7 +710,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
             float v[32];
             tmem_ld32(tm + lane_base + c, v);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + a.params[ob2 + c + j], 0.0f);
+            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + bias[kHid + c + j], 0.0f);
             st_row16(H, row, c, kHid, v);
             st_row16(H, row, c + 16, kHid, v + 16);
         }
@@ -731,16 +734,21 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
             if (live) {
                 float m = -3.0e38f;
                 int am = 0;
+#pragma unroll
                 for (int k = 0; k < kOut; ++k) {
-                    z[k] += a.params[ob3 + k];
+                    z[k] += bias[2 * kHid + k];
                     if (z[k] > m) { m = z[k]; am = k; }
                 }
                 float s = 0.0f;
-                for (int k = 0; k < kOut; ++k) { z[k] = sm2d_expf(z[k] - m); s += z[k]; }
+#pragma unroll
+                for (int k = 0; k < kOut; ++k) { z[k] = __expf(z[k] - m); s += z[k]; }
                 const float inv = 1.0f / s;
                 float t = 0.0f;
+#pragma unroll
                 for (int k = 0; k < kOut; ++k) { z[k] *= inv; if (k != am) t += z[k]; }
-                z[am] = 1.0f - t;   // the row sums to 1: the component's weight is conserved
+#pragma unroll
+                for (int k = 0; k < kOut; ++k)
+                    if (k == am) z[k] = 1.0f - t;   // the row sums to 1: the component's weight is conserved
                 int fb = 0;
                 if (a.err_bits && __int_as_float(a.err_bits[region_of(f)]) > a.tol) {
                     plain_table(a.dev, f, z);
@@ -748,6 +756,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
                 }
                 if (a.fallback) a.fallback[i] = fb;
                 float4* o = reinterpret_cast<float4*>(a.out + (size_t)i * kOut);
+#pragma unroll
                 for (int q = 0; q < 8; ++q) o[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
             }
         }
