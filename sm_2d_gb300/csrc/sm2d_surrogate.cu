@@ -163,6 +163,24 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
 }
+// relu of two values rounded to a bf16 pair (a in the low half) in one instruction
+__device__ __forceinline__ uint32_t pack2_relu(float a, float b) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
+// relu(v + bias) of 32 values as bf16 into row r, columns c..c+31 of a K-major operand
+__device__ __forceinline__ void st_row32_relu(unsigned char* base, int r, int c, int K, const float* v,
+                                              const float* bias) {
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        const float* x = v + 8 * h;
+        const float* b = bias + 8 * h;
+        const uint4 q = make_uint4(pack2_relu(x[0] + b[0], x[1] + b[1]), pack2_relu(x[2] + b[2], x[3] + b[3]),
+                                   pack2_relu(x[4] + b[4], x[5] + b[5]), pack2_relu(x[6] + b[6], x[7] + b[7]));
+        *reinterpret_cast<uint4*>(base + 2 * core_off(r, c + 8 * h, K)) = q;
+    }
+}
 // 16 values as bf16 into row r, columns c..c+15 (c a multiple of 8) of a K-major operand
 __device__ __forceinline__ void st_row16(unsigned char* base, int r, int c, int K, const float* v) {
     uint4 a = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
@@ -687,10 +705,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
         for (int c = 0; c < kHid; c += 32) {
             float v[32];
             tmem_ld32(tm + lane_base + c, v);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + bias[c + j], 0.0f);
-            st_row16(H, row, c, kHid, v);
-            st_row16(H, row, c + 16, kHid, v + 16);
+            st_row32_relu(H, row, c, kHid, v, bias + c);
         }
         fence_before();
         fence_async_smem();
@@ -709,10 +724,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
         for (int c = 0; c < kHid; c += 32) {
             float v[32];
             tmem_ld32(tm + lane_base + c, v);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + bias[kHid + c + j], 0.0f);
-            st_row16(H, row, c, kHid, v);
-            st_row16(H, row, c + 16, kHid, v + 16);
+            st_row32_relu(H, row, c, kHid, v, bias + kHid + c);
         }
         fence_before();
         fence_async_smem();
