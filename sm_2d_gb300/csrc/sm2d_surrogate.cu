@@ -51,7 +51,14 @@ constexpr int oW1 = 0, oW2 = oW1 + kHid * kIn, oW3 = oW2 + kHid * kHid, ob1 = oW
               ob3 = ob2 + kHid, kParams = ob3 + kOut;
 // bf16 weight images in the core-matrix layout (bytes)
 constexpr int iW1 = 0, iW2 = iW1 + kHid * kIn * 2, iW2T = iW2 + kHid * kHid * 2, iW3 = iW2T + kHid * kHid * 2,
-              iW3T = iW3 + kOut * kHid * 2, kImgBytes = iW3T + kOut * kHid * 2;
+              iW3T = iW3 + kOut * kHid * 2, iB2X = iW3T + kOut * kHid * 2, iB3X = iB2X + kHid * 16 * 2,
+              kImgBytes = iB3X + kOut * 16 * 2;
+// Inference adds the biases on the tensor cores: each bias is a bf16 pair
+// (value, rounding remainder) in K columns 8-9 of the W1 image and 0-1 of the
+// B2X [128][16] and B3X [32][16] images, multiplied by constant-one input
+// columns.  The training kernel's inputs hold zeros there and it adds the
+// fp32 biases itself.
+constexpr int kBiasCol = 8;
 // table geometry: theta bins of the 512-bin grid over [-pi/2, pi/2], energy bins
 // of the 256-bin log grid over [0.1, 250] MeV
 constexpr float kDth = 3.14159265358979323846f / 512.0f;
@@ -169,15 +176,13 @@ __device__ __forceinline__ uint32_t pack2_relu(float a, float b) {
     asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
     return d;
 }
-// relu(v + bias) of 32 values as bf16 into row r, columns c..c+31 of a K-major operand
-__device__ __forceinline__ void st_row32_relu(unsigned char* base, int r, int c, int K, const float* v,
-                                              const float* bias) {
+// relu of 32 values as bf16 into row r, columns c..c+31 of a K-major operand
+__device__ __forceinline__ void st_row32_relu(unsigned char* base, int r, int c, int K, const float* v) {
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
         const float* x = v + 8 * h;
-        const float* b = bias + 8 * h;
-        const uint4 q = make_uint4(pack2_relu(x[0] + b[0], x[1] + b[1]), pack2_relu(x[2] + b[2], x[3] + b[3]),
-                                   pack2_relu(x[4] + b[4], x[5] + b[5]), pack2_relu(x[6] + b[6], x[7] + b[7]));
+        const uint4 q = make_uint4(pack2_relu(x[0], x[1]), pack2_relu(x[2], x[3]), pack2_relu(x[4], x[5]),
+                                   pack2_relu(x[6], x[7]));
         *reinterpret_cast<uint4*>(base + 2 * core_off(r, c + 8 * h, K)) = q;
     }
 }
@@ -316,10 +321,9 @@ constexpr int X = 0, XT = 4096, W1 = 8192, W2 = 12288, W3 = 45056, H1 = 53248, H
 }
 namespace inf {  // inference kernel: weights shared by the CTA, then X and H of each warpgroup's tile
 constexpr int WG = 4;                                       // warpgroups (tiles in flight) per CTA
-constexpr int W1 = 0, W2 = 4096, W3 = 36864, TILE0 = 45056;
+constexpr int W1 = 0, W2 = 4096, W3 = 36864, ONES = 45056, B2X = 49152, B3X = 53248, TILE0 = 54272;
 constexpr int XB = 4096, TILE_BYTES = XB + 32768;           // X [128][16], H [128][128] (H2 over H1)
-constexpr int BIAS = TILE0 + WG * TILE_BYTES;                // b1, b2, b3 as fp32
-constexpr int BAR = BIAS + (2 * kHid + kOut) * 4, BYTES = BAR + 96;
+constexpr int BAR = TILE0 + WG * TILE_BYTES, BYTES = BAR + 96;
 }
 static_assert(inf::BYTES <= 227 * 1024, "inference CTA exceeds shared memory");
 static_assert(tr::BYTES <= 227 * 1024, "training tile exceeds shared memory");
@@ -659,16 +663,21 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
         for (int k = 0; k < inf::WG; ++k) bar_init(bar_w + 1 + k, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    float* bias = reinterpret_cast<float*>(sm + inf::BIAS);
     if (tid < inf::WG) wfail[tid] = 0;
-    for (int k = tid; k < 2 * kHid + kOut; k += kInferThreads) bias[k] = a.params[ob1 + k];
+    if (tid < kTile) {   // the constant-one operand of the bias products: columns 0-1 of [128][16]
+        float o[kIn] = {1.0f, 1.0f};
+        st_row16(sm + inf::ONES, tid, 0, kIn, o);
+    }
+    fence_async_smem();
     if (warp == 0) tmem_alloc(tslot, 512);
     __syncthreads();
     if (tid == 0) {
-        bar_expect(bar_w, kHid * kIn * 2 + kHid * kHid * 2 + kOut * kHid * 2);
+        bar_expect(bar_w, kHid * kIn * 2 + kHid * kHid * 2 + kOut * kHid * 2 + kHid * 16 * 2 + kOut * 16 * 2);
         bulk_g2s(sm + inf::W1, a.img + iW1, kHid * kIn * 2, bar_w);
         bulk_g2s(sm + inf::W2, a.img + iW2, kHid * kHid * 2, bar_w);
         bulk_g2s(sm + inf::W3, a.img + iW3, kOut * kHid * 2, bar_w);
+        bulk_g2s(sm + inf::B2X, a.img + iB2X, kHid * 16 * 2, bar_w);
+        bulk_g2s(sm + inf::B3X, a.img + iB3X, kOut * 16 * 2, bar_w);
     }
     fence_after();
     const uint32_t tm = *tslot + (uint32_t)(g * 128);
@@ -689,6 +698,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
             } else {
                 for (int k = 0; k < kIn; ++k) x[k] = 0.0f;
             }
+            x[kBiasCol] = 1.0f;       // picks up b1 (hi, lo) from the W1 image
+            x[kBiasCol + 1] = 1.0f;
             st_row16(X, row, 0, kIn, x);
         }
         fence_async_smem();
@@ -705,7 +716,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
         for (int c = 0; c < kHid; c += 32) {
             float v[32];
             tmem_ld32(tm + lane_base + c, v);
-            st_row32_relu(H, row, c, kHid, v, bias + c);
+            st_row32_relu(H, row, c, kHid, v);
         }
         fence_before();
         fence_async_smem();
@@ -715,6 +726,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
             for (int k = 0; k < kHid / 16; ++k)
                 mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W2) + 256 * k, 2048), idesc(128, 128),
                     k > 0);
+            mma(tm, sdesc(su32(sm + inf::ONES), 256), sdesc(su32(sm + inf::B2X), 256), idesc(128, 128), 1);   // + b2
             mma_commit(bar_m);
         }
         ok = bar_wait(bar_m, pm);
@@ -724,7 +736,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
         for (int c = 0; c < kHid; c += 32) {
             float v[32];
             tmem_ld32(tm + lane_base + c, v);
-            st_row32_relu(H, row, c, kHid, v, bias + kHid + c);
+            st_row32_relu(H, row, c, kHid, v);
         }
         fence_before();
         fence_async_smem();
@@ -734,6 +746,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
             for (int k = 0; k < kHid / 16; ++k)
                 mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W3) + 256 * k, 2048), idesc(128, kOut),
                     k > 0);
+            mma(tm, sdesc(su32(sm + inf::ONES), 256), sdesc(su32(sm + inf::B3X), 256), idesc(128, kOut), 1);   // + b3
             mma_commit(bar_m);
         }
         ok = bar_wait(bar_m, pm);
@@ -748,7 +761,6 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
                 int am = 0;
 #pragma unroll
                 for (int k = 0; k < kOut; ++k) {
-                    z[k] += bias[2 * kHid + k];
                     if (z[k] > m) { m = z[k]; am = k; }
                 }
                 float s = 0.0f;
@@ -822,7 +834,7 @@ __global__ void k_update(float* params, float* m1, float* m2, const float* parti
     const __nv_bfloat16 h = __float2bfloat16_rn(w);
     if (p < oW2) {
         const int o = p / kIn, k = p % kIn;
-        im[iW1 / 2 + core_off(o, k, kIn)] = h;
+        if (k < kBiasCol) im[iW1 / 2 + core_off(o, k, kIn)] = h;
     } else if (p < oW3) {
         const int q = p - oW2, o = q / kHid, k = q % kHid;
         im[iW2 / 2 + core_off(o, k, kHid)] = h;
@@ -831,6 +843,21 @@ __global__ void k_update(float* params, float* m1, float* m2, const float* parti
         const int q = p - oW3, o = q / kHid, k = q % kHid;
         im[iW3 / 2 + core_off(o, k, kHid)] = h;
         im[iW3T / 2 + core_off(k, o, kOut)] = h;
+    } else {   // a bias: its (value, remainder) bf16 pair for the inference kernel's bias products
+        const __nv_bfloat16 lo = __float2bfloat16_rn(w - __bfloat162float(h));
+        if (p < ob2) {
+            const int o = p - ob1;
+            im[iW1 / 2 + core_off(o, kBiasCol, kIn)] = h;
+            im[iW1 / 2 + core_off(o, kBiasCol + 1, kIn)] = lo;
+        } else if (p < ob3) {
+            const int o = p - ob2;
+            im[iB2X / 2 + core_off(o, 0, 16)] = h;
+            im[iB2X / 2 + core_off(o, 1, 16)] = lo;
+        } else {
+            const int o = p - ob3;
+            im[iB3X / 2 + core_off(o, 0, 16)] = h;
+            im[iB3X / 2 + core_off(o, 1, 16)] = lo;
+        }
     }
 }
 
