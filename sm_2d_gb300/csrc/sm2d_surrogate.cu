@@ -683,16 +683,26 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
     const uint32_t tm = *tslot + (uint32_t)(g * 128);
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
     uint32_t pm = 0;
+    // this warpgroup's first row, loaded ahead; each tile loads the next tile's row
+    float4 qn = make_float4(1.0f, 0.0f, 1.0f, 1.0f);
+    {
+        const int i0 = (blockIdx.x * inf::WG + g) * kTile + row;
+        if (i0 < a.n) qn = a.feats[i0];
+    }
     bool ok = bar_wait(bar_w, 0);
     if (wg_any(g, !ok)) goto fail;
     for (int tile = blockIdx.x * inf::WG + g; tile * kTile < a.n; tile += gridDim.x * inf::WG) {
         const int i = tile * kTile + row;
         const bool live = i < a.n;
         float f[4] = {1.0f, 0.0f, 1.0f, 1.0f};
+        const float4 q = qn;
+        {
+            const long long inext = (long long)(tile + gridDim.x * inf::WG) * kTile + row;
+            if (inext < a.n) qn = a.feats[inext];
+        }
         {
             float x[kIn];
             if (live) {
-                const float4 q = a.feats[i];
                 f[0] = q.x; f[1] = q.y; f[2] = q.z; f[3] = q.w;
                 feature_row(f, x);
             } else {
