@@ -69,6 +69,7 @@ constexpr float kThMax = 0.3f, kDsMin = 0.05f, kDsMax = 2.0f, kRhoMin = 0.2f, kR
 // calibration regions: ln E x step x density
 constexpr int kRegE = 64, kRegS = 8, kRegR = 8, kRegions = kRegE * kRegS * kRegR;
 constexpr long long kSpinCycles = 2000000000LL;   // about one second at the SM clock
+constexpr int kMaxRows = 1 << 30;                  // rows per call (tile indices stay within int)
 
 // element offset of (row r, column k) of a K-major bf16 operand with K columns
 __host__ __device__ constexpr int core_off(int r, int k, int K) {
@@ -930,14 +931,17 @@ extern "C" {
 int sm2d_mlp_param_count(void) { return kParams; }
 
 int sm2d_mlp_create(int max_batch, void* stream, sm2d_mlp_handle* out) {
-    if (!out || max_batch <= 0) return fail(SM2D_ERR_ARG, "sm2d_mlp_create: bad argument");
+    if (!out || max_batch <= 0 || max_batch > kMaxRows) return fail(SM2D_ERR_ARG, "sm2d_mlp_create: bad argument");
     *out = nullptr;
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, tr::BYTES));
+    CK(cudaFuncSetAttribute(k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, inf::BYTES));
     sm2d_mlp* m = new sm2d_mlp();
     m->max_batch = (max_batch + kTile - 1) / kTile * kTile;
     m->s = (cudaStream_t)stream;
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, dev));
+    m->sms = sms;
     const int tiles = m->max_batch / kTile;
     int rc = 0;
     if (!rc) rc = mlp_alloc((void**)&m->params, sizeof(float) * kParams);
@@ -948,14 +952,13 @@ int sm2d_mlp_create(int max_batch, void* stream, sm2d_mlp_handle* out) {
     if (!rc) rc = mlp_alloc((void**)&m->img, kImgBytes);
     if (!rc) rc = mlp_alloc((void**)&m->err, sizeof(int));
     if (!rc) rc = mlp_alloc((void**)&m->err_bits, sizeof(int) * kRegions);
+    if (!rc && cudaMemsetAsync(m->err, 0, sizeof(int), m->s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "cudaMemsetAsync");
+    if (!rc && cudaMemsetAsync(m->err_bits, 0, sizeof(int) * kRegions, m->s) != cudaSuccess)
+        rc = fail(SM2D_ERR_CUDA, "cudaMemsetAsync");
     if (rc) {
         sm2d_mlp_destroy(m);
         return rc;
     }
-    CK(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, tr::BYTES));
-    CK(cudaFuncSetAttribute(k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, inf::BYTES));
-    CK(cudaMemsetAsync(m->err, 0, sizeof(int), m->s));
-    CK(cudaMemsetAsync(m->err_bits, 0, sizeof(int) * kRegions, m->s));
     // initial weights: uniform +-sqrt(6 / fan_in) (He), zero biases, fixed seed
     std::vector<float> p(kParams, 0.0f);
     uint32_t st = 12345u;
@@ -963,8 +966,13 @@ int sm2d_mlp_create(int max_batch, void* stream, sm2d_mlp_handle* out) {
     for (int k = oW1; k < oW2; ++k) p[k] = (2.0f * u() - 1.0f) * sqrtf(6.0f / 8.0f);
     for (int k = oW2; k < oW3; ++k) p[k] = (2.0f * u() - 1.0f) * sqrtf(6.0f / kHid);
     for (int k = oW3; k < ob1; ++k) p[k] = (2.0f * u() - 1.0f) * sqrtf(1.0f / kHid);
+    const int rc2 = sm2d_mlp_set_params(m, p.data());
+    if (rc2) {
+        sm2d_mlp_destroy(m);
+        return rc2;
+    }
     *out = m;
-    return sm2d_mlp_set_params(m, p.data());
+    return 0;
 }
 
 int sm2d_mlp_destroy(sm2d_mlp_handle m) {
@@ -1012,7 +1020,7 @@ int sm2d_mlp_train(sm2d_mlp_handle m, const float* d_feats, const float* d_targe
                    float lr0, float lr_min, float* d_loss_hist) {
     if (!m || !d_feats || !d_target) return fail(SM2D_ERR_ARG, "null argument");
     if (batch <= 0 || batch > m->max_batch || batch % kTile) return fail(SM2D_ERR_ARG, "batch %d: a multiple of %d up to %d", batch, kTile, m->max_batch);
-    if (n_total < batch || steps < 0) return fail(SM2D_ERR_ARG, "training set smaller than a batch");
+    if (n_total < batch || n_total > kMaxRows || steps < 0) return fail(SM2D_ERR_ARG, "training set of %d rows", n_total);
     if (!aligned16(d_feats) || !aligned16(d_target)) return fail(SM2D_ERR_ARG, "inputs must be 16-byte aligned");
     const int per_epoch = n_total / batch;
     for (int s = 0; s < steps; ++s) {
@@ -1028,7 +1036,7 @@ int sm2d_mlp_train(sm2d_mlp_handle m, const float* d_feats, const float* d_targe
 
 int sm2d_mlp_forward(sm2d_mlp_handle m, const float* d_feats, int n, float* d_table) {
     if (!m || !d_feats || !d_table) return fail(SM2D_ERR_ARG, "null argument");
-    if (n <= 0) return fail(SM2D_ERR_ARG, "no samples");
+    if (n <= 0 || n > kMaxRows) return fail(SM2D_ERR_ARG, "rows %d outside 1..%d", n, kMaxRows);
     if (!aligned16(d_feats) || !aligned16(d_table)) return fail(SM2D_ERR_ARG, "arrays must be 16-byte aligned");
     InferArgs a{};
     a.feats = reinterpret_cast<const float4*>(d_feats);
@@ -1044,14 +1052,14 @@ int sm2d_mlp_forward(sm2d_mlp_handle m, const float* d_feats, int n, float* d_ta
 }
 
 int sm2d_redistribution_features(int n, uint32_t seed, float* d_feats, void* stream) {
-    if (n <= 0 || !d_feats || !aligned16(d_feats)) return fail(SM2D_ERR_ARG, "bad argument");
+    if (n <= 0 || n > kMaxRows || !d_feats || !aligned16(d_feats)) return fail(SM2D_ERR_ARG, "bad argument");
     k_features<<<std::min((n + 255) / 256, 4096), 256, 0, (cudaStream_t)stream>>>(n, seed, reinterpret_cast<float4*>(d_feats));
     CK(cudaGetLastError());
     return 0;
 }
 
 int sm2d_redistribution_table(sm2d_handle h, const float* d_feats, int n, float* d_table) {
-    if (!d_feats || !d_table || n <= 0) return fail(SM2D_ERR_ARG, "bad argument");
+    if (!d_feats || !d_table || n <= 0 || n > kMaxRows) return fail(SM2D_ERR_ARG, "bad argument");
     if (!aligned16(d_feats) || !aligned16(d_table)) return fail(SM2D_ERR_ARG, "arrays must be 16-byte aligned");
     Dev d;
     cudaStream_t s;
@@ -1065,7 +1073,7 @@ int sm2d_redistribution_table(sm2d_handle h, const float* d_feats, int n, float*
 
 int sm2d_mlp_calibrate(sm2d_mlp_handle m, const float* d_feats, const float* d_plain, const float* d_surrogate, int n,
                        float* host_region_err) {
-    if (!m || !d_feats || !d_plain || !d_surrogate || n <= 0) return fail(SM2D_ERR_ARG, "bad argument");
+    if (!m || !d_feats || !d_plain || !d_surrogate || n <= 0 || n > kMaxRows) return fail(SM2D_ERR_ARG, "bad argument");
     CK(cudaMemsetAsync(m->err_bits, 0, sizeof(int) * kRegions, m->s));
     k_calibrate<<<std::min((n + 255) / 256, 8192), 256, 0, m->s>>>(n, reinterpret_cast<const float4*>(d_feats), d_plain,
                                                                   d_surrogate, m->err_bits);
@@ -1080,7 +1088,7 @@ int sm2d_mlp_calibrate(sm2d_mlp_handle m, const float* d_feats, const float* d_p
 int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats, int n, float tol, float* d_table,
                           int* d_fallback) {
     if (!m || !d_feats || !d_table) return fail(SM2D_ERR_ARG, "null argument");
-    if (n <= 0) return fail(SM2D_ERR_ARG, "no samples");
+    if (n <= 0 || n > kMaxRows) return fail(SM2D_ERR_ARG, "rows %d outside 1..%d", n, kMaxRows);
     if (!m->calibrated) return fail(SM2D_ERR_STATE, "sm2d_mlp_redistribute before sm2d_mlp_calibrate");
     if (!aligned16(d_feats) || !aligned16(d_table)) return fail(SM2D_ERR_ARG, "arrays must be 16-byte aligned");
     InferArgs a{};

@@ -112,3 +112,19 @@ def test_adam_restatement_first_step():
     q, m, v = so.adam(p, g, np.zeros_like(p), np.zeros_like(p), 1, 1e-3)
     # the first bias-corrected Adam step moves each parameter by lr against its gradient's sign
     np.testing.assert_allclose(q - p, -1e-3 * np.sign(g), rtol=1e-3, atol=1e-9)
+
+
+def test_surrogate_entries_refuse_bad_arguments_without_a_gpu():
+    # argument checks come before any CUDA call, so they answer on a host without a GPU
+    import ctypes as C
+    from sm_2d_gb300 import surrogate as sg
+    L = sg._lib()
+    h = C.c_void_p()
+    assert L.sm2d_mlp_create(0, None, C.byref(h)) == -1 and not h.value
+    assert L.sm2d_mlp_create(1 << 31 - 1, None, None) == -1
+    assert L.sm2d_redistribution_features(0, 1, None, None) == -1
+    assert L.sm2d_redistribution_table(None, None, 10, None) == -1
+    assert L.sm2d_mlp_forward(None, None, 10, None) == -1
+    assert L.sm2d_mlp_sync(None) == -1
+    assert L.sm2d_mlp_destroy(None) == -1
+    assert b"null" in L.sm2d_last_error()
