@@ -267,7 +267,7 @@ def run_reference_arm(args):
 
 
 # ---------------------------------------------------------------- GPU arm
-def surrogate_leg(n_train=1 << 21, steps=3000, n_eval=1 << 22, tol=0.01):
+def surrogate_leg(n_train=1 << 21, steps=10000, n_eval=1 << 22, tol=0.01):
     """The learned redistribution surrogate next to the method it replaces.
 
     Trains the network on the method's own tables (K3 physics on the device),
