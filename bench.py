@@ -310,12 +310,13 @@ def surrogate_leg(n_train=1 << 21, steps=10000, n_eval=1 << 22, tol=0.01):
         s.sync()
         return e0.elapsed_time(e1) / reps
 
-    t_plain = timed(lambda: L.sm2d_redistribution_table(s.t.h, P(fe.data_ptr()), n_eval, P(ref.data_ptr())))
-    t_net = timed(lambda: L.sm2d_mlp_forward(m, P(fe.data_ptr()), n_eval, P(out.data_ptr())))
+    ck = sm.runtime.check   # a refused or failed launch raises instead of timing nothing
+    t_plain = timed(lambda: ck(L.sm2d_redistribution_table(s.t.h, P(fe.data_ptr()), n_eval, P(ref.data_ptr()))))
+    t_net = timed(lambda: ck(L.sm2d_mlp_forward(m, P(fe.data_ptr()), n_eval, P(out.data_ptr()))))
     err = (out - ref).abs()
     mean_err = float(err.mean())
-    t_fb = timed(lambda: L.sm2d_mlp_redistribute(m, s.t.h, P(fe.data_ptr()), n_eval, tol, P(out.data_ptr()),
-                                                 P(fb.data_ptr())))
+    t_fb = timed(lambda: ck(L.sm2d_mlp_redistribute(m, s.t.h, P(fe.data_ptr()), n_eval, tol, P(out.data_ptr()),
+                                                    P(fb.data_ptr()))))
     row_err = (out - ref).abs().max(dim=1).values
     fb_share = float(fb.float().mean())
     flops = 41984.0 * n_eval

@@ -331,6 +331,9 @@ static_assert(tr::BYTES <= 227 * 1024, "training tile exceeds shared memory");
 
 // TMEM columns of the training kernel (512 allocated, one CTA per SM)
 constexpr uint32_t cZ1 = 0, cZ2 = 128, cZ3 = 256, cW3T = 320, cH2g = 384, cW2g = 0, cH1g = 128, cW1g = 256;
+static_assert(cH2g + kHid <= 512 && cW3T + kOut <= cH2g && cZ3 + kOut <= cW3T && cW1g + kIn <= cW3T,
+              "training kernel's TMEM plan overlaps or exceeds 512 columns");
+static_assert(inf::WG * 128 <= 512, "inference warpgroups need 128 TMEM columns each");
 
 struct TrainArgs {
     const float4* feats;
