@@ -128,3 +128,17 @@ def test_surrogate_entries_refuse_bad_arguments_without_a_gpu():
     assert L.sm2d_mlp_sync(None) == -1
     assert L.sm2d_mlp_destroy(None) == -1
     assert b"null" in L.sm2d_last_error()
+
+
+def test_bf16_input_pairs_carry_sixteen_bits():
+    # each scaled input reaches the first GEMM as bf16(u) and bf16(128 (u - bf16(u))):
+    # together they restore u to about 2^-16 of its range
+    f = sample_features(20000, 8)
+    x = so.features(f)
+    u = np.stack([2.0 * (np.log(f[:, 0].astype(np.float64)) - so.LN_EMIN) / (so.LN_EMAX - so.LN_EMIN) - 1.0,
+                  f[:, 1] / so.TH_MAX, 2.0 * (f[:, 2] - so.DS_MIN) / (so.DS_MAX - so.DS_MIN) - 1.0,
+                  2.0 * (f[:, 3] - so.RHO_MIN) / (so.RHO_MAX - so.RHO_MIN) - 1.0], axis=1)
+    rebuilt = x[:, :4].astype(np.float64) + x[:, 4:8].astype(np.float64) / 128.0
+    assert np.abs(rebuilt - u).max() < 2.0 ** -15
+    assert np.abs(x[:, :4] - u).max() > 2.0 ** -10     # bf16 alone would lose them
+    assert (x[:, 8:] == 0).all()
