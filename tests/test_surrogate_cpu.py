@@ -121,7 +121,7 @@ def test_surrogate_entries_refuse_bad_arguments_without_a_gpu():
     L = sg._lib()
     h = C.c_void_p()
     assert L.sm2d_mlp_create(0, None, C.byref(h)) == -1 and not h.value
-    assert L.sm2d_mlp_create(1 << 31 - 1, None, None) == -1
+    assert L.sm2d_mlp_create((1 << 30) + 1, None, C.byref(h)) == -1 and not h.value   # above the row limit
     assert L.sm2d_redistribution_features(0, 1, None, None) == -1
     assert L.sm2d_redistribution_table(None, None, 10, None) == -1
     assert L.sm2d_mlp_forward(None, None, 10, None) == -1
