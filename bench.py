@@ -93,6 +93,39 @@ def make_config(grid: str, workload: str = "plan512"):
     return cfg.production()
 
 
+def oracle_problem(grid: str, workload: str = "plan512"):
+    """The problem of make_config as the CPU oracle takes it, built from the
+    oracle's own grid tables (the reference arm loads no part of the GPU
+    library): (oracle config dict, theta edges, E edges, density per row or
+    None).  The production options are those of Config.production()."""
+    from oracle import oracle as orc
+    groups = [(0.1, 2.0, 0.1), (2.0, 20.0, 0.2), (20.0, 100.0, 0.25), (100.0, 250.0, 0.25)]
+    rho = None
+    if workload == "c3" and not SMALL:
+        Nx, Nz, sx, E0 = 300, 600, 5.0, 230.0
+        rho = slab_phantom(600, 0.5)
+    elif SMALL:
+        Nx, Nz, sx, E0 = 100, 200, BEAM["sigma_x"], BEAM["E0"]
+    else:
+        Nx, Nz, sx, E0 = 200, 400, BEAM["sigma_x"], BEAM["E0"]
+    if grid == "log" and workload != "c3" and not SMALL:
+        th, _ = orc.angular_grid(np.float32(-np.pi / 2), np.float32(np.pi / 2), 512)
+        ee, _ = orc.energy_grid_log(0.1, 250.0, 256)
+        layout = dict(nt_local=8, ne_local=4, nx_sub=4, nz_sub=1)
+        split = 1
+    else:
+        th, _ = orc.angular_grid(-0.35, 0.35, 36)
+        ee, _ = orc.energy_grid_piecewise(groups)
+        layout = dict(nt_local=4, ne_local=2, nx_sub=8, nz_sub=4)
+        split = 0
+    cfg = dict(Nx=Nx, Nz=Nz, dx=0.5, dz=0.5, x_min=-(Nx * 0.5) / 2.0, z_min=0.0, E_fine_on=10.0, E_fine_off=11.0,
+               weight_active_min=1e-12, step_coarse=5.0, sigma_x_initial=sx, E0=E0, enable_straggling=1,
+               enable_nuclear=1, seed_slot_mode=1, energy_split=split, grid_E_min=0.1, grid_E_max=250.0,
+               prune_coarse=0.0, prune_fine=0.0, split_min_weight=1e-7 if split else 0.0,
+               stop_weight_fraction=1e-6, floor_cutoff=1, seed_iteration_salt=1, **layout)
+    return cfg, th, ee, rho
+
+
 def spot_seeds(rank, n):
     """Sample seeds of a plan of n spots on `rank`: disjoint across ranks
     (replicas by spot), consecutive within a plan."""
@@ -136,7 +169,7 @@ def lane_bytes(cfg):
     L = cfg.layout["nt_local"] * cfg.layout["ne_local"] * cfg.layout["nx_sub"] * cfg.layout["nz_sub"]
     psi = nc * 32 * (4 + 4 * L)
     per_cell = nc * (2 * 8 + 44 + 44 + 8 + 1 + 4 + 8)
-    rows = nc * 2048 + (nc // 8) * 4 * (2048 + 128 + 4)
+    rows = nc * 4096 + (nc // 8) * 4 * (4096 + 128 + 4)
     bins = nc * L // 4 * 48   # bin list (16 B) + step records (32 B)
     return psi + per_cell + rows + bins
 
@@ -223,13 +256,12 @@ def cpu_spots_per_s(grid: str, workload: str, n_threads: int, n_spots: int):
     with the Fermi-Eyges tables of its own energy and width), n_threads at a
     time; returns (spots/s, wall seconds)."""
     from oracle import oracle as orc
-    cfg = make_config(grid, workload)
+    ocfg, th, ee, rho = oracle_problem(grid, workload)
     oracles = []
     for b in plan_spots(workload, 0, n_spots):
-        oc = dict(cfg.oracle_config(), E0=b["E0"], sigma_x_initial=b["sigma_x"])
-        o = orc.Oracle(oc, cfg.theta_edges, cfg.E_edges)
-        if cfg.density_z is not None:
-            o.set_density(cfg.density_z)
+        o = orc.Oracle(dict(ocfg, E0=b["E0"], sigma_x_initial=b["sigma_x"]), th, ee)
+        if rho is not None:
+            o.set_density(rho)
         o.inject(**b)
         oracles.append(o)
     t0 = time.perf_counter()
@@ -447,7 +479,7 @@ def run_gpu_arm(args):
     # ---- per-kernel device time: eager replay of one wave of the plan's first
     # `lanes` spots with CUDA events around every launch on the library stream
     t.batch_inject(beams[:B])
-    n_it, ms, n_launch = t.run_profiled(MAX_IT)
+    n_it, ms, n_launch, wave_passes = t.run_profiled(MAX_IT)
     prs = t.batch_results(min(B, n))
     L = t.L
     slot_bytes = 4 + 4 * L
@@ -459,6 +491,7 @@ def run_gpu_arm(args):
     else:
         peak, peak_src = 6800.0, "fallback"
     achieved = alg_bytes / (ms["transport"] / 1e3) / 1e9 if ms["transport"] > 0 else 0.0
+    plan_passes = passes
     traffic = None
     tp = os.path.join(ROOT, "profiles", f"k_transport_traffic_{args.workload}.json")
     if os.path.exists(tp) and not SMALL and args.grid == "reference":
@@ -469,11 +502,13 @@ def run_gpu_arm(args):
     step_total = sum(ms.values())
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_src, "kernel": "k_transport (deposit pass)",
-                "algorithmic_bytes_per_launch": alg_bytes / max(n_it, 1),
-                "avg_launch_ms": ms["transport"] / max(n_it, 1),
+                "algorithmic_bytes_per_launch": alg_bytes / max(wave_passes, 1),
+                "avg_launch_ms": ms["transport"] / max(wave_passes, 1),
+                "launches_timed": wave_passes, "launches_per_step": plan_passes,
                 "stage_share": {k: v / step_total for k, v in ms.items()} if step_total else {},
-                "note": "per-launch times from an eager replay of one wave (the plan's first lanes' spots) with "
-                        "CUDA events around each kernel on the library stream"}
+                "note": "per-launch times from an eager replay of one wave (the plan's first lanes' spots, "
+                        "launches_timed passes) with CUDA events around each kernel on the library stream; one "
+                        "deposit launch per pass, launches_per_step passes per plan"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

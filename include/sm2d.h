@@ -219,8 +219,11 @@ int sm2d_run_async(sm2d_handle h, int max_iterations);
 int sm2d_dose_async(sm2d_handle h, double* host_dose);
 /* replay up to n_iterations eagerly with CUDA events around every kernel;
  * ms7 receives the summed device time of the seven stages listed at
- * sm2d_get_step_timing, *launches the number of kernel launches */
-int sm2d_run_profiled(sm2d_handle h, int n_iterations, int* iterations_done, float* ms7, int* launches);
+ * sm2d_get_step_timing over the *passes passes that transported (a wave of
+ * lanes runs as many passes as its longest spot needs; *iterations_done is
+ * lane 0's count), *launches the number of kernel launches */
+int sm2d_run_profiled(sm2d_handle h, int n_iterations, int* iterations_done, float* ms7, int* launches,
+                      int* passes);
 
 /* ---- batched spots (no counterpart in the reference: its runner transports
  * one spot per call; a plan is a loop over such calls) ---- */
@@ -439,10 +442,13 @@ int sm2d_redistribution_table(sm2d_handle h, const float* d_feats, int n, float*
 int sm2d_mlp_calibrate(sm2d_mlp_handle m, const float* d_feats, const float* d_plain, const float* d_surrogate, int n,
                        float* host_region_err);
 /* surrogate tables, with the plain table of the handle's physics in the rows
- * whose calibrated region error exceeds tol (d_fallback[i] = 1 there) */
+ * whose calibrated region error exceeds tol (d_fallback[i] = 1 there).  The
+ * work runs on the surrogate's stream after the work already enqueued on h's
+ * stream (an event orders the two streams). */
 int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats, int n, float tol, float* d_table,
                           int* d_fallback);
-/* wait for the handle's stream; SM2D_ERR_TIMEOUT if a kernel's bounded wait gave up */
+/* wait for the handle's stream; SM2D_ERR_TIMEOUT if a kernel's bounded wait
+ * gave up since the last sync (the flag is cleared once reported) */
 int sm2d_mlp_sync(sm2d_mlp_handle m);
 /* table geometry and feature ranges: dtheta, dlnE, ln E_min, ln E_max,
  * theta_max, step_min, step_max, density_min */

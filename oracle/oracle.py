@@ -103,6 +103,8 @@ def _lib(fp64: bool):
         lib.orc_postprocess.argtypes = [P, P, C.c_float, C.c_int, C.c_int, C.c_float, P]
         lib.orc_math.argtypes = [C.c_int, P, P, C.c_int]
         lib.orc_redistribution_table.argtypes = [P, C.c_int, P, P]
+        lib.orc_track_claims.argtypes = [P, C.c_int]
+        lib.orc_claim_demand.argtypes = [P]
         _LIBS[key] = lib
         return lib
 
@@ -292,6 +294,15 @@ class Oracle:
         out = np.zeros((f.shape[0], 32), np.float32)
         self.lib.orc_redistribution_table(self.ctx, f.shape[0], _p(f), _p(out))
         return out
+
+    def track_claims(self, on=True):
+        """Record the distinct block ids aimed at each container per iteration."""
+        self.lib.orc_track_claims(self.ctx, 1 if on else 0)
+
+    def claim_demand(self):
+        """Largest number of distinct block ids aimed at one container (psi_out
+        cell or bucket) in one iteration while tracking was on."""
+        return self.lib.orc_claim_demand(self.ctx)
 
     def fe(self):
         A, B, S = (np.zeros(self.Nz, np.float32) for _ in range(3))

@@ -4,7 +4,9 @@
 # oracle/_ref/ref_writer_probe from its output writers.  Runs
 # only where the reference tree is mounted; the output never leaves oracle/_ref.
 set -e
-REF=${SM2D_REFERENCE:-/root/reference}
+# SM2D_REFERENCE names the root of the reference tree (its src/ and run_simulation.cpp).
+[ -n "$SM2D_REFERENCE" ] || { echo "set SM2D_REFERENCE to the reference tree" >&2; exit 2; }
+REF=$SM2D_REFERENCE
 HERE=$(cd "$(dirname "$0")" && pwd)
 [ -d "$REF/src" ] || { echo "reference tree not found at $REF" >&2; exit 1; }
 mkdir -p "$HERE/_ref"

@@ -136,6 +136,14 @@ struct orc_ctx {
     int finished;
     double cell_steps, slots_in, slots_out;
     orc_audit audit;
+    /* claim-demand diagnostic (off unless orc_track_claims enabled it):
+     * distinct block ids aimed at each container (psi_out cell or bucket)
+     * within one iteration, and the largest such count seen */
+    int track_claims;
+    struct claim_key { const uint32_t* ids; uint32_t want; } *ck;
+    struct claim_cnt { const uint32_t* ids; int n; } *cc;
+    size_t ck_cap, cc_cap, ck_n, cc_n;
+    int claim_demand_max, claim_batch;
 };
 
 static inline psi_buf* psi_in(orc_ctx* c) { return &c->buf[c->in_idx]; }
@@ -627,6 +635,65 @@ static int remap_lidx(const orc_ctx* c, int l, uint32_t src, uint32_t dst) {
 static int slot_with_fallback(uint32_t* ids, int n, uint32_t want, uint32_t* sel) {
     return slot_with_fallback_n(ids, n, n, want, sel);
 }
+/* ---- claim-demand diagnostic: open-addressing sets, cleared per iteration */
+static size_t ck_hash(const void* p, uint32_t w) {
+    uint64_t h = (uint64_t)(uintptr_t)p * 0x9E3779B97F4A7C15ull ^ (uint64_t)w * 0xC2B2AE3D27D4EB4Full;
+    return (size_t)(h ^ (h >> 29));
+}
+static void claims_reset(orc_ctx* c) {
+    if (c->ck) memset(c->ck, 0, sizeof(*c->ck) * c->ck_cap);
+    if (c->cc) memset(c->cc, 0, sizeof(*c->cc) * c->cc_cap);
+    c->ck_n = c->cc_n = 0;
+}
+static void claims_grow(orc_ctx* c) {
+    size_t ncap = c->ck_cap ? 2 * c->ck_cap : (1u << 16);
+    struct claim_key* old = c->ck;
+    size_t ocap = c->ck_cap;
+    c->ck = calloc(ncap, sizeof(*c->ck));
+    c->ck_cap = ncap;
+    for (size_t i = 0; i < ocap; ++i)
+        if (old[i].ids) {
+            size_t h = ck_hash(old[i].ids, old[i].want) & (ncap - 1);
+            while (c->ck[h].ids) h = (h + 1) & (ncap - 1);
+            c->ck[h] = old[i];
+        }
+    free(old);
+    struct claim_cnt* oc = c->cc;
+    size_t occ = c->cc_cap;
+    c->cc = calloc(ncap, sizeof(*c->cc));
+    c->cc_cap = ncap;
+    for (size_t i = 0; i < occ; ++i)
+        if (oc[i].ids) {
+            size_t h = ck_hash(oc[i].ids, 0) & (ncap - 1);
+            while (c->cc[h].ids) h = (h + 1) & (ncap - 1);
+            c->cc[h] = oc[i];
+        }
+    free(oc);
+}
+static void claims_note(orc_ctx* c, const uint32_t* ids, uint32_t want) {
+    if (!c->track_claims) return;
+    /* a bucket's storage is reused by the next batch of the iteration: key
+     * bucket claims by batch as well */
+    const psi_buf* po = &c->buf[1 - c->in_idx];
+    if (ids < po->bid || ids >= po->bid + (size_t)c->Nc * c->Kb)
+        ids = (const uint32_t*)((uintptr_t)ids ^ ((uintptr_t)c->claim_batch << 56));
+    if (2 * (c->ck_n + 1) > c->ck_cap) claims_grow(c);
+    size_t m = c->ck_cap - 1, h = ck_hash(ids, want) & m;
+    while (c->ck[h].ids) {
+        if (c->ck[h].ids == ids && c->ck[h].want == want) return;
+        h = (h + 1) & m;
+    }
+    c->ck[h].ids = ids;
+    c->ck[h].want = want;
+    c->ck_n++;
+    h = ck_hash(ids, 0) & m;
+    while (c->cc[h].ids && c->cc[h].ids != ids) h = (h + 1) & m;
+    if (!c->cc[h].ids) { c->cc[h].ids = ids; c->cc_n++; }
+    if (++c->cc[h].n > c->claim_demand_max) c->claim_demand_max = c->cc[h].n;
+}
+void orc_track_claims(orc_ctx* c, int on) { c->track_claims = on; }
+int orc_claim_demand(const orc_ctx* c) { return c->claim_demand_max; }
+
 /* number of slots a deposit of weight w may claim */
 static inline int claimable(const orc_ctx* c, int n, double w) {
     return (c->cfg.claim_reserve_weight > 0.0f && w < (double)c->cfg.claim_reserve_weight) ? n - 8 : n;
@@ -635,6 +702,7 @@ static inline int claimable(const orc_ctx* c, int n, double w) {
  * claim among the first 24 slots and are dropped (not merged) when those
  * are taken; heavy ones use all 32 and the nearest-block fallback */
 static int claim_w(const orc_ctx* c, uint32_t* ids, int n, uint32_t want, uint32_t* sel, double w) {
+    claims_note((orc_ctx*)c, ids, want);
     int nc = claimable(c, n, w);
     if (nc < n) {
         *sel = want;
@@ -1468,6 +1536,7 @@ static void psi_clear(orc_ctx* c, psi_buf* p) {
 }
 
 static void prepare_buckets(orc_ctx* c, const uint32_t* list, int n) {
+    c->claim_batch++;
     for (int i = 0; i < c->Nc; ++i) c->cell_to_bucket[i] = -1;
     if (n * 4 > c->n_buckets_cap) {
         for (int i = 0; i < c->n_buckets_cap; ++i) {
@@ -1520,6 +1589,7 @@ int orc_step(orc_ctx* c) {
         return 0;
     }
     psi_clear(c, psi_out(c));
+    if (c->track_claims) claims_reset(c);
     c->k2_slot_w = c->k2_slot_e = c->k2_bkt_w = c->k2_bkt_e = c->k2_prune_w = c->k2_prune_e = 0.0;
     c->k3_slot_w = c->k3_slot_e = c->k3_bkt_w = c->k3_bkt_e = c->k3_prune_w = c->k3_prune_e = 0.0;
     c->k4_slot_w = c->k4_slot_e = 0.0;
@@ -1825,6 +1895,8 @@ void orc_destroy(orc_ctx* c) {
     }
     free(c->buckets);
     free(c->cell_to_bucket);
+    free(c->ck);
+    free(c->cc);
     free(c);
 }
 

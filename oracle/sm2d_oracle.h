@@ -158,6 +158,12 @@ void orc_get_fe(const orc_ctx* c, float* A, float* B, float* sigma_total);
  * incoming energy, tails in the end bins.  Uses the context's R-LUT. */
 void orc_redistribution_table(const orc_ctx* c, int n, const float* feats, float* out);
 
+/* claim-demand diagnostic: with tracking on, the largest number of distinct
+ * block ids aimed at one container (a psi_out cell, or one bucket of one
+ * batch) within one iteration since tracking began */
+void orc_track_claims(orc_ctx* c, int on);
+int  orc_claim_demand(const orc_ctx* c);
+
 /* run several independent contexts on n_threads host threads */
 int  orc_run_many(orc_ctx** ctxs, int n, int max_iterations, int n_threads);
 

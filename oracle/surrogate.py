@@ -4,7 +4,10 @@ infrastructure: only tests/, the smoke check and bench.py's checks import it).
 The network is 4 -> 128 -> 128 -> 32 with ReLU and a softmax.  Each input row
 (E [MeV], theta [rad], step [mm], density [g/cm^3]) is scaled to [-1, 1] and
 fed as 16 values: the bf16 rounding of each scaled feature, 128 x its
-rounding remainder (also rounded to bf16), then zeros.  The GPU kernels hold
+rounding remainder (also rounded to bf16), then zeros.  The weights of the
+remainder columns 4-7 are tied to columns 0-3: bf16(W1[:, i]) / 128 (their
+own parameters stay zero), so the first layer forms bf16(W1[:, i]) times the
+input to about 16 bits.  The GPU kernels hold
 every GEMM operand in bf16 (inputs, weights, hidden activations, loss
 gradients) and accumulate in fp32; this module rounds the same operands to
 bf16 (round to nearest even) and does the rest in float64, so the two differ
@@ -41,6 +44,24 @@ def unpack(params):
             p[O_B1:O_B2], p[O_B2:O_B3], p[O_B3:N_PARAMS])
 
 
+def w1_image(W1):
+    """The first layer's bf16 weights as the GPU image holds them: columns 4-7
+    are bf16(W1[:, 0:4]) / 128 (exact, a power of two)."""
+    w = bf16(W1).copy()
+    w[:, 4:8] = w[:, 0:4] / np.float32(128.0)
+    return w
+
+
+def tie_w1_grad(g):
+    """Gradient of the tied parameterisation: d/dW1[:, i] gains 1/128 of the
+    remainder column's gradient; columns 4-7 have none."""
+    g = np.array(g, np.float64, copy=True)
+    w = g[O_W1:O_W2].reshape(HID, IN)
+    w[:, 0:4] += w[:, 4:8] / 128.0
+    w[:, 4:8] = 0.0
+    return g
+
+
 def features(feats):
     """[n][4] physical inputs -> [n][16] network inputs (bf16 hi/lo pairs)."""
     f = np.asarray(feats, np.float32).reshape(-1, 4)
@@ -59,7 +80,7 @@ def forward(params, feats):
     """Softmax tables [n][32] and the intermediates of the backward pass."""
     W1, W2, W3, b1, b2, b3 = unpack(params)
     x = features(feats).astype(np.float64)
-    h1 = bf16(np.maximum(x @ bf16(W1).T.astype(np.float64) + b1, 0.0).astype(np.float32)).astype(np.float64)
+    h1 = bf16(np.maximum(x @ w1_image(W1).T.astype(np.float64) + b1, 0.0).astype(np.float32)).astype(np.float64)
     h2 = bf16(np.maximum(h1 @ bf16(W2).T.astype(np.float64) + b2, 0.0).astype(np.float32)).astype(np.float64)
     z = h2 @ bf16(W3).T.astype(np.float64) + b3
     z = z - z.max(axis=1, keepdims=True)
@@ -88,7 +109,7 @@ def loss_and_grad(params, feats, target):
     d1 = bf16(np.where(h1 > 0, dh1, 0.0).astype(np.float32)).astype(np.float64)
     g[O_W1:O_W2] = (d1.T @ x).ravel()
     g[O_B1:O_B2] = d1.sum(axis=0)
-    return loss, g
+    return loss, tie_w1_grad(g)
 
 
 def loss_exact(params, feats, target):
@@ -161,6 +182,7 @@ def init_params(seed=12345):
 
     for k in range(O_W1, O_W2):
         p[k] = (np.float32(2.0) * u() - np.float32(1.0)) * np.float32(np.sqrt(np.float32(6.0 / 8.0)))
+    p[O_W1:O_W2].reshape(HID, IN)[:, 4:8] = 0.0   # tied to columns 0-3
     for k in range(O_W2, O_W3):
         p[k] = (np.float32(2.0) * u() - np.float32(1.0)) * np.float32(np.sqrt(np.float32(6.0 / HID)))
     for k in range(O_W3, O_B1):

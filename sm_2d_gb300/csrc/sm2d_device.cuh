@@ -386,8 +386,12 @@ __device__ __forceinline__ int claim_slot(uint32_t* ids, uint32_t want, uint32_t
 // earlier passes read as free and the rows are never cleared (a wipe runs
 // when the pass number nears its 32-bit limit).  Injection uses the same
 // tables with the sample index as key: the reference's source kernels claim
-// in sample order when run one sample at a time.
-constexpr int kCandLog = 7, kCand = 1 << kCandLog;
+// in sample order when run one sample at a time.  A row holds 256 ids: the
+// oracle counts up to 115 distinct ids aimed at one container in one
+// iteration on the reference grids and up to 181 on the 512-theta log grid;
+// an id that finds no free entry is counted (cand_ovf), and a run that
+// counts any is not an exact restatement of the sequential claims.
+constexpr int kCandLog = 8, kCand = 1 << kCandLog;
 
 __device__ __forceinline__ unsigned cand_hash(uint32_t bid) { return (bid * 0x9E3779B1u) >> (32 - kCandLog); }
 

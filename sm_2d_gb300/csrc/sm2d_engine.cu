@@ -2358,7 +2358,7 @@ int sm2d_dose_async(sm2d_handle h, double* host_dose) {
     return 0;
 }
 
-int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* launches) {
+int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* launches, int* passes) {
     if (!h || !ms7 || n <= 0) return fail(SM2D_ERR_ARG, "invalid argument");
     Ctx& c = *h;
     if (!c.injected) return fail(SM2D_ERR_STATE, "no phase space");
@@ -2401,6 +2401,7 @@ int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* la
         }
     if (done_iters) *done_iters = c.ls_host[0].iter - start;
     if (launches) *launches = launched * (c.p.use_buckets ? 7 : 6);
+    if (passes) *passes = done;
     return 0;
 }
 

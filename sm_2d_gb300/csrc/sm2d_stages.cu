@@ -392,6 +392,16 @@ static int k5_static_scratch(double** out) {
     return 0;
 }
 
+// Both K5 entries index a slot's local bins as (l / nt_local) % N_E_local
+// over `local_bins` values: refuse layouts that would divide by zero or read
+// past a slot.
+static int k5_check_layout(int L, int nt_local, int N_E_local, int N_E) {
+    if (L != 128 && L != 256) return fail(SM2D_ERR_LAYOUT, "local_bins must be 256 or 128, got %d", L);
+    if (nt_local <= 0 || N_E_local <= 0 || N_E <= 0 || L % (nt_local * N_E_local) != 0)
+        return fail(SM2D_ERR_ARG, "invalid layout: nt_local %d, N_E_local %d, N_E %d", nt_local, N_E_local, N_E);
+    return 0;
+}
+
 // ------------------------------------------------------------------ diagnostics
 __global__ void k_math_eval(int fn, const float* __restrict__ x, float* __restrict__ y, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -500,11 +510,20 @@ int sm2d_k5_conservation_audit(const uint32_t* bid_in, const float* val_in, cons
                                int N_cells, void* stream) {
     if (!bid_in || !val_in || !bid_out || !val_out || !EdepC || !Ee || !d_report || N_cells <= 0)
         return fail(SM2D_ERR_ARG, "invalid argument");
+    int rc = k5_check_layout(L, nt_local, N_E_local, N_E);
+    if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    // accumulator of the device current at the call, allocated on first use
+    // of that device and kept until exit
+    constexpr int kMaxDevices = 64;
     static std::mutex mu;
+    static double* acc_of[kMaxDevices] = {};
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(SM2D_ERR_ARG, "device index %d out of range", dev);
     std::lock_guard<std::mutex> lock(mu);
-    static double* acc = nullptr;
-    if (!acc) CK(cudaMalloc(&acc, 12 * sizeof(double)));
+    if (!acc_of[dev]) CK(cudaMalloc(&acc_of[dev], 12 * sizeof(double)));
+    double* acc = acc_of[dev];
     CK(cudaMemsetAsync(acc, 0, 12 * sizeof(double), s));
     RawK5 a{bid_in, bid_out, val_in, val_out, EdepC, e_nuc, e_bnd, e_cut, p_edep, p_e_nuc, p_e_bnd, p_e_cut,
             w_cut, w_nuc, w_bnd, p_w_cut, p_w_nuc, p_w_bnd, Ee, N_E, nt_local, N_E_local, L, N_cells};
@@ -524,11 +543,13 @@ int sm2d_k5_conservation_audit_static(
     int L, sm2d_audit* d_report, int N_cells, void* stream) {
     if (!bid_in || !val_in || !bid_out || !val_out || !EdepC || !Ee || !d_report || N_cells <= 0)
         return fail(SM2D_ERR_ARG, "invalid argument");
+    int rc = k5_check_layout(L, nt_local, N_E_local, N_E);
+    if (rc) return rc;
     if (N_cells > kK5StaticMaxCells)
         return fail(SM2D_ERR_ARG, "N_cells %d exceeds the static scratch limit of %d cells", N_cells,
                     kK5StaticMaxCells);
     double* scratch = nullptr;
-    int rc = k5_static_scratch(&scratch);
+    rc = k5_static_scratch(&scratch);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     // the completion counter must start at zero

@@ -43,6 +43,7 @@ int handle_dev(sm2d_handle h, Dev* d, cudaStream_t* s);
 namespace mlp {
 
 constexpr int kIn = 16;     // input width of the first GEMM: 4 features as bf16 hi/lo pairs, zero padded
+constexpr int kPair = 4;    // input columns 0-3: bf16(u); 4-7: 128 (u - bf16(u)), weighted by W1[:, 0:4] / 128
 constexpr int kHid = 128;
 constexpr int kOut = 32;    // 8 theta x 4 E
 constexpr int kTile = 128;  // samples per CTA tile (the MMA's M)
@@ -222,8 +223,10 @@ __device__ __forceinline__ float row_sum(const unsigned char* base, int r, int K
 // ------------------------------------------------------------------ features and the plain table
 // Network inputs of one sample (E [MeV], theta [rad], step [mm], density
 // [g/cm^3]): each scaled to [-1, 1] and written as a bf16 pair (hi, 128 x
-// the rounding remainder), so the first GEMM sees the fp32 inputs to about
-// 16 bits.
+// the rounding remainder).  The W1 image multiplies the remainder column of
+// input i by bf16(W1[o][i]) / 128 (exact: a power of two), so the first GEMM
+// forms bf16(W1[o][i]) (hi + remainder) and sees the fp32 input to about 16
+// bits.
 __host__ __device__ inline void feature_row(const float* f, float* x16) {
     const float u[4] = {2.0f * (sm2d_logf(fmaxf(f[0], 1e-6f)) - kLnEmin) / (kLnEmax - kLnEmin) - 1.0f,
                         f[1] / kThMax, 2.0f * (f[2] - kDsMin) / (kDsMax - kDsMin) - 1.0f,
@@ -829,10 +832,24 @@ __global__ void k_update(float* params, float* m1, float* m2, const float* parti
         *loss_out = l;
     }
     if (p >= kParams) return;
+    // W1 columns kPair..2 kPair-1 multiply the inputs' rounding remainders
+    // (scaled by 128): they are tied to columns 0..kPair-1 (the image holds
+    // bf16(W1[o][i]) / 128 there) and their own parameters stay zero
+    const bool tied = p < oW2 && (p % kIn) >= kPair && (p % kIn) < 2 * kPair;
+    if (tied) {
+        if (mode == 0) grad_out[p] = 0.0f;
+        else params[p] = 0.0f;
+        return;
+    }
     float w = params[p];
     if (mode != 2) {
         float g = 0.0f;
         for (int c = 0; c < n_part; ++c) g += partial[(size_t)c * kParams + p];
+        if (p < oW2 && (p % kIn) < kPair) {   // plus the tied column's gradient, d(w / 128) / dw = 1 / 128
+            float gt = 0.0f;
+            for (int c = 0; c < n_part; ++c) gt += partial[(size_t)c * kParams + p + kPair];
+            g += gt * (1.0f / 128.0f);
+        }
         if (mode == 0) {
             grad_out[p] = g;
             return;
@@ -848,7 +865,10 @@ __global__ void k_update(float* params, float* m1, float* m2, const float* parti
     const __nv_bfloat16 h = __float2bfloat16_rn(w);
     if (p < oW2) {
         const int o = p / kIn, k = p % kIn;
-        if (k < kBiasCol) im[iW1 / 2 + core_off(o, k, kIn)] = h;
+        if (k < kPair) {
+            im[iW1 / 2 + core_off(o, k, kIn)] = h;
+            im[iW1 / 2 + core_off(o, k + kPair, kIn)] = __float2bfloat16_rn(__bfloat162float(h) * (1.0f / 128.0f));
+        }
     } else if (p < oW3) {
         const int q = p - oW2, o = q / kHid, k = q % kHid;
         im[iW2 / 2 + core_off(o, k, kHid)] = h;
@@ -889,6 +909,7 @@ struct sm2d_mlp {
     int* err = nullptr;
     int* err_bits = nullptr;   // calibration [kRegions]
     int calibrated = 0;
+    cudaEvent_t order = nullptr;   // orders a transport handle's stream before this handle's work
     int t = 0;                 // Adam steps taken
     int sms = 0;
 };
@@ -903,7 +924,12 @@ int check_err(sm2d_mlp* m) {
     int e = 0;
     CK(cudaMemcpyAsync(&e, m->err, sizeof(int), cudaMemcpyDeviceToHost, m->s));
     CK(cudaStreamSynchronize(m->s));
-    if (e) return fail(SM2D_ERR_TIMEOUT, "surrogate kernel: a bounded mbarrier wait gave up");
+    if (e) {
+        // reported once: clear the flag so that later calls start clean
+        CK(cudaMemsetAsync(m->err, 0, sizeof(int), m->s));
+        CK(cudaStreamSynchronize(m->s));
+        return fail(SM2D_ERR_TIMEOUT, "surrogate kernel: a bounded mbarrier wait gave up");
+    }
     return 0;
 }
 int launch_train(sm2d_mlp* m, const float* feats, const float* target, int n, float scale) {
@@ -955,6 +981,8 @@ int sm2d_mlp_create(int max_batch, void* stream, sm2d_mlp_handle* out) {
     if (!rc) rc = mlp_alloc((void**)&m->img, kImgBytes);
     if (!rc) rc = mlp_alloc((void**)&m->err, sizeof(int));
     if (!rc) rc = mlp_alloc((void**)&m->err_bits, sizeof(int) * kRegions);
+    if (!rc && cudaEventCreateWithFlags(&m->order, cudaEventDisableTiming) != cudaSuccess)
+        rc = fail(SM2D_ERR_CUDA, "cudaEventCreate");
     if (!rc && cudaMemsetAsync(m->err, 0, sizeof(int), m->s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "cudaMemsetAsync");
     if (!rc && cudaMemsetAsync(m->err_bits, 0, sizeof(int) * kRegions, m->s) != cudaSuccess)
         rc = fail(SM2D_ERR_CUDA, "cudaMemsetAsync");
@@ -967,6 +995,8 @@ int sm2d_mlp_create(int max_batch, void* stream, sm2d_mlp_handle* out) {
     uint32_t st = 12345u;
     auto u = [&st]() { st = 1664525u * st + 1013904223u; return ((st >> 8) + 0.5f) * (1.0f / 16777216.0f); };
     for (int k = oW1; k < oW2; ++k) p[k] = (2.0f * u() - 1.0f) * sqrtf(6.0f / 8.0f);
+    for (int o = 0; o < kHid; ++o)   // the remainder columns are tied to columns 0-3
+        for (int k = kPair; k < 2 * kPair; ++k) p[oW1 + o * kIn + k] = 0.0f;
     for (int k = oW2; k < oW3; ++k) p[k] = (2.0f * u() - 1.0f) * sqrtf(6.0f / kHid);
     for (int k = oW3; k < ob1; ++k) p[k] = (2.0f * u() - 1.0f) * sqrtf(1.0f / kHid);
     const int rc2 = sm2d_mlp_set_params(m, p.data());
@@ -984,6 +1014,7 @@ int sm2d_mlp_destroy(sm2d_mlp_handle m) {
     void* ps[] = {m->params, m->m1, m->m2, m->partial, m->ploss, m->img, m->err, m->err_bits};
     for (void* q : ps)
         if (q) cudaFree(q);
+    if (m->order) cudaEventDestroy(m->order);
     delete m;
     return 0;
 }
@@ -1107,6 +1138,11 @@ int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats
     a.tol = tol;
     a.fallback = d_fallback;
     a.err = m->err;
+    // the fallback rows read h's device tables: order h's stream first
+    if (s != m->s) {
+        CK(cudaEventRecord(m->order, s));
+        CK(cudaStreamWaitEvent(m->s, m->order, 0));
+    }
     const int tiles = (n + kTile - 1) / kTile;
     k_infer<<<std::min((tiles + inf::WG - 1) / inf::WG, m->sms), kInferThreads, inf::BYTES, m->s>>>(a);
     CK(cudaGetLastError());

@@ -149,7 +149,7 @@ def lib(build_if_needed: bool = True):
         L.sm2d_inject_async.argtypes = [P, C.POINTER(Beam)]
         L.sm2d_run_async.argtypes = [P, I]
         L.sm2d_dose_async.argtypes = [P, P]
-        L.sm2d_run_profiled.argtypes = [P, I, C.POINTER(I), P, C.POINTER(I)]
+        L.sm2d_run_profiled.argtypes = [P, I, C.POINTER(I), P, C.POINTER(I), C.POINTER(I)]
         L.sm2d_energy_grid_log.argtypes = [F, F, I, P, P]
         L.sm2d_energy_grid_piecewise.argtypes = [I, P, P, P]
         L.sm2d_angular_grid.argtypes = [F, F, I, P, P]
@@ -563,10 +563,13 @@ class Transport:
         return d
 
     def run_profiled(self, n_iterations):
-        n, launches = C.c_int(), C.c_int()
+        """Eager replay with CUDA events around every kernel: (lane 0's
+        iterations, {stage: summed ms}, kernel launches, passes timed)."""
+        n, launches, passes = C.c_int(), C.c_int(), C.c_int()
         ms = np.zeros(len(STAGES), np.float32)
-        check(self._lib.sm2d_run_profiled(self.h, int(n_iterations), C.byref(n), _p(ms), C.byref(launches)))
-        return n.value, dict(zip(STAGES, ms.tolist())), launches.value
+        check(self._lib.sm2d_run_profiled(self.h, int(n_iterations), C.byref(n), _p(ms), C.byref(launches),
+                                          C.byref(passes)))
+        return n.value, dict(zip(STAGES, ms.tolist())), launches.value, passes.value
 
     def step_timing(self):
         t = np.zeros(len(STAGES), np.float32)

@@ -18,8 +18,8 @@ Two sources, both produced by the reference itself:
    dose grids (``dose.bin``): dose_2d.txt and pdd.txt with and without
    normalisation, and the metrics.
 
-Run from the repository root in a container where the reference tree is
-mounted:  python tests/golden/make_golden.py
+Run from the repository root where the reference tree is mounted:
+SM2D_REFERENCE=<reference root> python tests/golden/make_golden.py
 """
 import configparser
 import json
@@ -28,7 +28,7 @@ import shutil
 import subprocess
 import sys
 
-REF = os.environ.get("SM2D_REFERENCE", "/root/reference")
+REF = os.environ.get("SM2D_REFERENCE", "")   # root of the reference tree (required)
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
@@ -89,6 +89,8 @@ def writer_cases():
 
 
 if __name__ == "__main__":
+    if not REF:
+        sys.exit("set SM2D_REFERENCE to the root of the reference tree")
     if not os.path.isdir(REF):
         sys.exit(f"reference tree not found at {REF}")
     one_step_cases()

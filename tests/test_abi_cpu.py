@@ -60,3 +60,24 @@ def test_bucket_layout_size():
     # DeviceOutflowBucket: 32 ids, 32 counts, 32 x L floats, 3 moments
     assert sm.lib().sm2d_bucket_bytes(256) == 32972
     assert sm.lib().sm2d_bucket_bytes(128) == 16588
+
+
+def _k5_args(nt_local, n_e_local, n_e, local_bins, n_cells=16):
+    import ctypes as C
+    P = C.c_void_p
+    return ([P(16)] * 18 + [C.c_float(0), C.c_float(0), C.c_double(0), C.c_double(0), C.c_float(0),
+                            C.c_double(0), C.c_int(1), P(16), C.c_int(n_e), C.c_int(nt_local), C.c_int(n_e_local),
+                            C.c_int(local_bins), P(16), C.c_int(n_cells), P(None)])
+
+
+@pytest.mark.parametrize("entry", ["sm2d_k5_conservation_audit", "sm2d_k5_conservation_audit_static"])
+def test_k5_entries_refuse_bad_layouts(entry):
+    """Both K5 entries refuse a local-bin count other than 128/256 and
+    non-positive layout counts before touching the device (the kernel divides
+    by nt_local and N_E_local and reads local_bins values per slot)."""
+    fn = getattr(sm.lib(), entry)
+    assert fn(*_k5_args(4, 2, 1029, 100)) == -6     # SM2D_ERR_LAYOUT
+    assert fn(*_k5_args(0, 2, 1029, 256)) == -1     # SM2D_ERR_ARG
+    assert fn(*_k5_args(4, 0, 1029, 256)) == -1
+    assert fn(*_k5_args(4, 2, 0, 256)) == -1
+    assert fn(*_k5_args(3, 2, 1029, 256)) == -1     # 256 local bins are not a whole number of (3 x 2) groups

@@ -42,3 +42,26 @@ def test_lanes_follow_free_memory(workload):
     free = 280 * 2 ** 30
     n = bench.auto_lanes(cfg, free)
     assert n * per <= 0.85 * free < (n + 1) * per or n == 80
+
+
+@pytest.mark.parametrize("grid,workload", [("reference", "plan512"), ("log", "plan512"), ("reference", "c3")])
+def test_reference_arm_problem_equals_the_gpu_arm_problem(grid, workload):
+    """The reference arm builds its oracle problem from the oracle's own grid
+    tables; it must be the problem the GPU arm transports."""
+    cfg = bench.make_config(grid, workload)
+    ocfg, th, ee, rho = bench.oracle_problem(grid, workload)
+    want = cfg.oracle_config()
+    assert set(want) <= set(ocfg)
+    for k, v in want.items():
+        assert ocfg[k] == pytest.approx(v, rel=0, abs=0), k
+    assert (th == cfg.theta_edges).all() and (ee == cfg.E_edges).all()
+    assert (rho is None) == (cfg.density_z is None)
+    if rho is not None:
+        assert (rho == cfg.density_z).all()
+
+
+def test_reference_arm_does_not_load_the_gpu_library():
+    code = ("import sys, bench; bench.cpu_spots_per_s('reference', 'plan512', 1, 1); "
+            "assert 'sm_2d_gb300' not in sys.modules, sorted(m for m in sys.modules if 'sm_2d' in m)")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]

@@ -260,7 +260,8 @@ def test_async_spot_pipeline_matches_blocking_api():
             assert np.abs(out.reshape(cfg.Nz, cfg.Nx) - dose_ref).max() <= 1e-5 * dose_ref.max()
         t.reset()
         t.inject_async(b)
-        n_it, ms, launches = t.run_profiled(3000)
+        n_it, ms, launches, passes = t.run_profiled(3000)
         per = 7 if cfg.use_buckets else 6
         assert n_it == n_ref and per * (n_it + 1) <= launches <= per * (n_it + 16)
+        assert passes == n_it   # one lane: a pass per iteration
         assert ms["transport"] > 0 and all(v >= 0 for v in ms.values())

@@ -142,3 +142,53 @@ def test_bf16_input_pairs_carry_sixteen_bits():
     assert np.abs(rebuilt - u).max() < 2.0 ** -15
     assert np.abs(x[:, :4] - u).max() > 2.0 ** -10     # bf16 alone would lose them
     assert (x[:, 8:] == 0).all()
+
+
+def test_first_layer_sees_inputs_to_sixteen_bits():
+    """With the remainder columns tied to bf16(W1[:, i]) / 128, the first
+    GEMM forms bf16(W1) u with u to about 2^-16, and an input moved by less
+    than a bf16 step moves the hidden pre-activations by about W1 times that
+    step, not by the sawtooth of an independent remainder weight."""
+    r = np.random.default_rng(9)
+    p = so.init_params()
+    W1 = so.unpack(p)[0]
+    assert (W1[:, 4:8] == 0).all()          # the tied parameters stay zero
+    f = sample_features(4000, 10)
+    u = np.stack([2.0 * (np.log(f[:, 0].astype(np.float64)) - so.LN_EMIN) / (so.LN_EMAX - so.LN_EMIN) - 1.0,
+                  f[:, 1] / so.TH_MAX, 2.0 * (f[:, 2] - so.DS_MIN) / (so.DS_MAX - so.DS_MIN) - 1.0,
+                  2.0 * (f[:, 3] - so.RHO_MIN) / (so.RHO_MAX - so.RHO_MIN) - 1.0], axis=1)
+    wimg = so.w1_image(W1).astype(np.float64)
+    pre = so.features(f).astype(np.float64) @ wimg.T
+    exact = u @ so.bf16(W1[:, :4]).astype(np.float64).T
+    scale = np.abs(so.bf16(W1[:, :4])).sum(axis=1).max()
+    assert np.abs(pre - exact).max() < scale * 2.0 ** -15
+    # a theta moved by 1/4 of a bf16 step of its scaled value
+    g = f.copy()
+    g[:, 1] = (f[:, 1].astype(np.float64) + 0.25 * 2.0 ** -9 * so.TH_MAX).astype(np.float32)
+    d = so.features(g).astype(np.float64) @ wimg.T - pre
+    step = (g[:, 1].astype(np.float64) - f[:, 1]) / so.TH_MAX
+    want = step[:, None] * so.bf16(W1[:, 1]).astype(np.float64)[None, :]
+    assert np.abs(d - want).max() < scale * 2.0 ** -14
+    del r
+
+
+def test_tied_gradient_is_the_sum_of_both_columns():
+    r = np.random.default_rng(11)
+    f = sample_features(256, 12)
+    y = r.dirichlet(np.ones(32), 256)
+    p = so.init_params()
+    _, g = so.loss_and_grad(p, f, y)
+    g1 = g[so.O_W1:so.O_W2].reshape(so.HID, so.IN)
+    assert (g1[:, 4:8] == 0).all()
+    # finite differences of the bf16 restatement through a weight of column 0:
+    # moving W1[o, 0] moves both image columns 0 and 4
+    o = int(np.argmax(np.abs(g1[:, 0])))
+    k = so.O_W1 + o * so.IN
+    h = 2.0 ** -4 * max(abs(float(p[k])), 0.05)
+    a, b = p.copy(), p.copy()
+    a[k] += h
+    b[k] -= h
+    la, _ = so.loss_and_grad(a, f, y)
+    lb, _ = so.loss_and_grad(b, f, y)
+    fd = (la - lb) / (2 * h)
+    assert abs(fd - g1[o, 0]) <= 0.05 * abs(g1[o, 0]) + 1e-6, (fd, g1[o, 0])
