@@ -153,6 +153,94 @@ def plan_spots(workload, rank, n):
     return out
 
 
+def plan_sample(workload, n, k=8):
+    """Indices of k spots of the plan spread over its energies (lowest and
+    highest included): the accuracy sample."""
+    spots = plan_spots(workload, 0, n)
+    order = sorted(range(len(spots)), key=lambda i: (spots[i]["E0"], i))
+    return sorted({order[int(round(j * (len(order) - 1) / (k - 1)))] for j in range(min(k, len(order)))})
+
+
+def accuracy_leg(grid, workload, spots, idx, dose, results, n_threads):
+    """Errors of the GPU's post-convolved dose maps on the sample spots `idx`
+    against the FP32 oracle (the same method and arithmetic) and the FP64
+    oracle (the same method in double precision), and the plan's audit
+    failure rates.  Dose error: max over cells |d - d_oracle| / max d_oracle,
+    the largest over the sample; depth-dose error the same over the PDD."""
+    from oracle import oracle as orc
+    ocfg, th, ee, rho = oracle_problem(grid, workload)
+    Nx, Nz, dx = ocfg["Nx"], ocfg["Nz"], ocfg["dx"]
+    out = {"spots": [int(i) for i in idx], "energies_mev": [float(spots[i]["E0"]) for i in idx]}
+    for fp64 in (False, True):
+        os_ = []
+        for i in idx:
+            b = spots[i]
+            o = orc.Oracle(dict(ocfg, E0=b["E0"], sigma_x_initial=b["sigma_x"]), th, ee, fp64=fp64)
+            if rho is not None:
+                o.set_density(rho)
+            o.inject(**b)
+            os_.append(o)
+        t0 = time.perf_counter()
+        orc.run_many(os_, MAX_IT, n_threads)
+        wall = time.perf_counter() - t0
+        derr, perr, same_peak, same_iters = [], [], 0, 0
+        for o, i in zip(os_, idx):
+            ref = orc.postprocess(o.tallies()["edep"], o.fe()[2], o.cfg["sigma_x_initial"], Nx, Nz, dx)
+            d = dose[i]
+            derr.append(float(np.abs(d - ref).max() / ref.max()))
+            pg, pr = d.sum(axis=1), ref.sum(axis=1)
+            perr.append(float(np.abs(pg - pr).max() / pr.max()))
+            same_peak += int(np.argmax(pg) == np.argmax(pr))
+            same_iters += int(o.scalars()["iterations"] == results[i]["iterations"])
+            o.close()
+        out["fp64" if fp64 else "fp32"] = {
+            "max_dose_error": max(derr), "max_pdd_error": max(perr), "dose_error_per_spot": derr,
+            "bragg_row_equal": f"{same_peak}/{len(idx)}", "iterations_equal": f"{same_iters}/{len(idx)}",
+            "oracle_wall_s": wall}
+    its = sum(r["iterations"] for r in results)
+    out["weight_audit_failure_rate"] = sum(r["weight_audit_failures"] for r in results) / max(its, 1)
+    out["energy_audit_failure_rate"] = sum(r["energy_audit_failures"] for r in results) / max(its, 1)
+    out["note"] = ("dose errors relative to the oracle's maximum cell dose; audit rates are failed K5 checks "
+                   "(W < 1e-6, E < 1e-5 relative) per spot-iteration over the whole plan")
+    return out
+
+
+def plan_rate(grid, workload, n_spots, lanes, steps, warmup):
+    """spots/s of a plan of n_spots on an engine of `lanes` lanes (0: from free
+    memory), device-resident, CUDA events on the library stream."""
+    import torch
+    import sm_2d_gb300 as sm
+    from sm_2d_gb300.runtime import Beam
+    cfg = make_config(grid, workload)
+    cfg.lanes = lanes if lanes > 0 else auto_lanes(cfg, torch.cuda.mem_get_info()[0])
+    spots = plan_spots(workload, 0, n_spots)
+    beams = [Beam(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
+                  b["n_samples"], b["seed"]) for b in spots]
+    with sm.Transport(cfg) as t:
+        ext = torch.cuda.ExternalStream(t.stream())
+        t.plan_load(beams, MAX_IT, dose=False)
+        for _ in range(warmup):
+            t.plan_run_async()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            t.plan_run_async()
+            e1.record(ext)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        _, rs = t.plan_results(dose=False)
+        passes, _, _ = t.plan_stats()
+        sc = t.scalars()
+        lanes_used = t.lanes
+    return {"value": n_spots * steps / (sum(ms) / 1e3), "unit": "spots/s", "lanes": lanes_used, "spots": n_spots,
+            "ms_per_step": float(np.mean(ms)), "passes_per_step": passes,
+            "iterations_per_spot": float(np.mean([r["iterations"] for r in rs])),
+            "unfinished_spots": sum(1 for r in rs if not r["finished"]),
+            "claim_table_overflows": sc["claim_table_overflows"]}
+
+
 def max_over_ranks(x, dist, device):
     """The largest of a per-rank value (timings take the slowest rank)."""
     if dist is None:
@@ -510,6 +598,28 @@ def run_gpu_arm(args):
                         "launches_timed passes) with CUDA events around each kernel on the library stream; one "
                         "deposit launch per pass, launches_per_step passes per plan"}
 
+    plan_scalars = t.scalars()
+    accuracy = None
+    if rank == 0 and not args.no_accuracy and not SMALL:
+        dose_all, rs_all = t.plan_results(dose=True)
+        accuracy = accuracy_leg(args.grid, args.workload, spots, plan_sample(args.workload, n), dose_all, rs_all,
+                                os.cpu_count() or 1)
+        del dose_all
+    t.close()
+    del flush
+    torch.cuda.empty_cache()
+
+    # context figures on the same box: the plan on the 256 log-E / 512 theta /
+    # 128-local-bin grid (energy-split method), and the plain engine with one
+    # lane (one spot at a time, as the reference runner transports them)
+    extra = {}
+    if rank == 0 and not args.no_context and not SMALL and args.workload == "plan512":
+        if args.grid == "reference":
+            extra["grid_log"] = plan_rate("log", args.workload, n, 0, 2, 1)
+        extra["single_lane"] = plan_rate(args.grid, args.workload, 24, 1, 2, 1)
+        extra["single_lane"]["note"] = ("the first 24 spots of the plan on an engine of one lane (one spot in "
+                                        "flight, refilled on the device)")
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         n_threads = os.cpu_count() or 1
@@ -537,9 +647,9 @@ def run_gpu_arm(args):
                 "e2e": {"value": e2e_value, "unit": "spots/s", "h2d_bytes_per_step": int(C.sizeof(Beam) * n),
                         "d2h_bytes_per_step": int(cfg.Nx * cfg.Nz * 8 * n)},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "gpu_launches": launches, "surrogate": surrogate}
+                "gpu_launches": launches, "accuracy": accuracy,
+                "claim_table_overflows": plan_scalars["claim_table_overflows"], **extra, "surrogate": surrogate}
         print(json.dumps(line))
-    t.close()
     if dist:
         dist.destroy_process_group()
     return 0
@@ -554,6 +664,8 @@ def main():
     ap.add_argument("--grid", default="reference", choices=["reference", "log"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the dose-error leg against the oracles")
+    ap.add_argument("--no-context", action="store_true", help="skip the log-grid and single-lane context figures")
     ap.add_argument("--lanes", type=int, default=0, help="spots in flight (0: from free device memory)")
     ap.add_argument("--workload", default="plan512", choices=["plan512", "c2", "c3"])
     ap.add_argument("--spots", type=int, default=0, help="spots per step, the plan (0: 512; 64 for c3)")

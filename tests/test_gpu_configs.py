@@ -114,11 +114,10 @@ def test_c2_production_beam(grid, oracle_mod):
 
 def _plan_sample(k=8):
     """k spots of the 512-spot plan spread over its energies, the highest
-    (a spot that leaves the 200 mm domain distally) and the lowest included."""
+    (a spot that leaves the 200 mm domain distally) and the lowest included:
+    the benchmark's accuracy sample."""
     spots = bench.plan_spots("plan512", 0, 512)
-    order = sorted(range(len(spots)), key=lambda i: spots[i]["E0"])
-    pick = sorted({order[int(round(j * (len(order) - 1) / (k - 1)))] for j in range(k)})
-    return [spots[i] for i in pick]
+    return [spots[i] for i in bench.plan_sample("plan512", 512, k)]
 
 
 def test_plan_spots_equal_oracle_single_spots(oracle_mod):
