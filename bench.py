@@ -70,7 +70,19 @@ def slab_phantom(Nz, dz, seed=PHANTOM_SEED):
     return rho
 
 
-def make_config(grid: str, workload: str = "plan512"):
+def make_config(grid: str, workload: str = "plan512", method: str = "sampled"):
+    """The engine configuration of a workload.  method "expect": the
+    expectation form (redistribution weights instead of hashed MCS and
+    straggling draws; energy split)."""
+    cfg = _make_config(grid, workload)
+    if method == "expect":
+        cfg.energy_split = 1
+        cfg.expectation = 1
+        cfg.production()
+    return cfg
+
+
+def _make_config(grid: str, workload: str = "plan512"):
     import sm_2d_gb300 as sm
     if workload == "c3" and not SMALL:
         cfg = sm.Config.reference_runner(300, 600, 0.5, 0.5, N_theta=36, sigma_x_initial=5.0, E0=230.0)
@@ -93,7 +105,7 @@ def make_config(grid: str, workload: str = "plan512"):
     return cfg.production()
 
 
-def oracle_problem(grid: str, workload: str = "plan512"):
+def oracle_problem(grid: str, workload: str = "plan512", method: str = "sampled"):
     """The problem of make_config as the CPU oracle takes it, built from the
     oracle's own grid tables (the reference arm loads no part of the GPU
     library): (oracle config dict, theta edges, E edges, density per row or
@@ -118,11 +130,13 @@ def oracle_problem(grid: str, workload: str = "plan512"):
         ee, _ = orc.energy_grid_piecewise(groups)
         layout = dict(nt_local=4, ne_local=2, nx_sub=8, nz_sub=4)
         split = 0
+    expect = 1 if method == "expect" else 0
+    split = 1 if expect else split
     cfg = dict(Nx=Nx, Nz=Nz, dx=0.5, dz=0.5, x_min=-(Nx * 0.5) / 2.0, z_min=0.0, E_fine_on=10.0, E_fine_off=11.0,
                weight_active_min=1e-12, step_coarse=5.0, sigma_x_initial=sx, E0=E0, enable_straggling=1,
                enable_nuclear=1, seed_slot_mode=1, energy_split=split, grid_E_min=0.1, grid_E_max=250.0,
                prune_coarse=0.0, prune_fine=0.0, split_min_weight=1e-7 if split else 0.0,
-               stop_weight_fraction=1e-6, floor_cutoff=1, seed_iteration_salt=1, **layout)
+               stop_weight_fraction=1e-6, floor_cutoff=1, seed_iteration_salt=1, expectation=expect, **layout)
     return cfg, th, ee, rho
 
 
@@ -161,14 +175,14 @@ def plan_sample(workload, n, k=8):
     return sorted({order[int(round(j * (len(order) - 1) / (k - 1)))] for j in range(min(k, len(order)))})
 
 
-def accuracy_leg(grid, workload, spots, idx, dose, results, n_threads):
+def accuracy_leg(grid, workload, spots, idx, dose, results, n_threads, method="sampled"):
     """Errors of the GPU's post-convolved dose maps on the sample spots `idx`
     against the FP32 oracle (the same method and arithmetic) and the FP64
     oracle (the same method in double precision), and the plan's audit
     failure rates.  Dose error: max over cells |d - d_oracle| / max d_oracle,
     the largest over the sample; depth-dose error the same over the PDD."""
     from oracle import oracle as orc
-    ocfg, th, ee, rho = oracle_problem(grid, workload)
+    ocfg, th, ee, rho = oracle_problem(grid, workload, method)
     Nx, Nz, dx = ocfg["Nx"], ocfg["Nz"], ocfg["dx"]
     out = {"spots": [int(i) for i in idx], "energies_mev": [float(spots[i]["E0"]) for i in idx]}
     for fp64 in (False, True):
@@ -205,20 +219,21 @@ def accuracy_leg(grid, workload, spots, idx, dose, results, n_threads):
     return out
 
 
-def plan_rate(grid, workload, n_spots, lanes, steps, warmup):
+def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", accuracy=False):
     """spots/s of a plan of n_spots on an engine of `lanes` lanes (0: from free
-    memory), device-resident, CUDA events on the library stream."""
+    memory), device-resident, CUDA events on the library stream; with
+    accuracy, also the dose errors of the accuracy sample (accuracy_leg)."""
     import torch
     import sm_2d_gb300 as sm
     from sm_2d_gb300.runtime import Beam
-    cfg = make_config(grid, workload)
+    cfg = make_config(grid, workload, method)
     cfg.lanes = lanes if lanes > 0 else auto_lanes(cfg, torch.cuda.mem_get_info()[0])
     spots = plan_spots(workload, 0, n_spots)
     beams = [Beam(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
                   b["n_samples"], b["seed"]) for b in spots]
     with sm.Transport(cfg) as t:
         ext = torch.cuda.ExternalStream(t.stream())
-        t.plan_load(beams, MAX_IT, dose=False)
+        t.plan_load(beams, MAX_IT, dose=accuracy)
         for _ in range(warmup):
             t.plan_run_async()
         torch.cuda.synchronize()
@@ -230,15 +245,19 @@ def plan_rate(grid, workload, n_spots, lanes, steps, warmup):
             e1.record(ext)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
-        _, rs = t.plan_results(dose=False)
-        passes, _, _ = t.plan_stats()
+        dose, rs = t.plan_results(dose=accuracy)
+        passes, _, bins = t.plan_stats()
         sc = t.scalars()
         lanes_used = t.lanes
-    return {"value": n_spots * steps / (sum(ms) / 1e3), "unit": "spots/s", "lanes": lanes_used, "spots": n_spots,
-            "ms_per_step": float(np.mean(ms)), "passes_per_step": passes,
-            "iterations_per_spot": float(np.mean([r["iterations"] for r in rs])),
-            "unfinished_spots": sum(1 for r in rs if not r["finished"]),
-            "claim_table_overflows": sc["claim_table_overflows"]}
+    out = {"value": n_spots * steps / (sum(ms) / 1e3), "unit": "spots/s", "lanes": lanes_used, "spots": n_spots,
+           "ms_per_step": float(np.mean(ms)), "passes_per_step": passes, "bins_per_step": bins,
+           "iterations_per_spot": float(np.mean([r["iterations"] for r in rs])),
+           "unfinished_spots": sum(1 for r in rs if not r["finished"]),
+           "claim_table_overflows": sc["claim_table_overflows"]}
+    if accuracy:
+        out["accuracy"] = accuracy_leg(grid, workload, spots, plan_sample(workload, n_spots), dose, rs,
+                                       os.cpu_count() or 1, method)
+    return out
 
 
 def max_over_ranks(x, dist, device):
@@ -258,7 +277,7 @@ def lane_bytes(cfg):
     psi = nc * 32 * (4 + 4 * L)
     per_cell = nc * (2 * 8 + 44 + 44 + 8 + 1 + 4 + 8)
     rows = nc * 4096 + (nc // 8) * 4 * (4096 + 128 + 4)
-    bins = nc * L // 4 * 48   # bin list (16 B) + step records (32 B)
+    bins = nc * L // 4 * (56 if getattr(cfg, "expectation", 0) else 48)   # bin list (16 B) + step records (32 B, 40 B)
     return psi + per_cell + rows + bins
 
 
@@ -619,6 +638,10 @@ def run_gpu_arm(args):
         extra["single_lane"] = plan_rate(args.grid, args.workload, 24, 1, 2, 1)
         extra["single_lane"]["note"] = ("the first 24 spots of the plan on an engine of one lane (one spot in "
                                         "flight, refilled on the device)")
+        extra["expectation"] = plan_rate(args.grid, args.workload, n, 0, 2, 1, "expect", accuracy=True)
+        extra["expectation"]["method"] = ("expectation form: K2/K3 emit the expected re-binning of their MCS angle "
+                                          "and straggling loss (up to 15 theta x 4 E children per component) "
+                                          "instead of one hashed draw; energy split")
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -95,6 +95,16 @@ typedef struct sm2d_problem {
      * thickness use the water-equivalent path rho * step; the Fermi-Eyges
      * tables are integrated through the phantom. */
     const float* density_z;
+    /* expectation form (no counterpart in the reference, whose K2/K3 draw one
+     * hashed MCS angle and one straggling loss per bin and step): 1 emits
+     * the expected result of the reference's re-binning of those draws
+     * instead -- up to 15 angle bins (frac^2 split of a Gaussian angle) times
+     * 4 energy bins (mean-preserving split of a Gaussian energy) per
+     * component, the 8 theta x 4 E redistribution table of sm2d_redist.h.
+     * Needs energy_split = 1 and the direct scatter (use_buckets = 0); the
+     * result no longer depends on random seeds or on arithmetic rounding
+     * through them. */
+    int expectation;
 } sm2d_problem;
 
 typedef struct sm2d_beam {

@@ -35,7 +35,7 @@ class OrcConfig(C.Structure):
         ("prune_coarse", C.c_float), ("prune_fine", C.c_float),
         ("split_min_weight", C.c_float), ("stop_weight_fraction", C.c_float),
         ("claim_reserve_weight", C.c_float), ("slots_per_cell", C.c_int),
-        ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
+        ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int), ("expectation", C.c_int),
     ]
 
 
@@ -69,7 +69,8 @@ def _lib(fp64: bool):
             return _LIBS[key]
         path = os.path.join(BUILD, f"liborc{key}.so")
         srcs = [os.path.join(HERE, "sm2d_oracle.c"), os.path.join(HERE, "sm2d_oracle.h"),
-                os.path.join(HERE, "..", "sm_2d_gb300", "csrc", "sm2d_math.h")]
+                os.path.join(HERE, "..", "sm_2d_gb300", "csrc", "sm2d_math.h"),
+                os.path.join(HERE, "..", "sm_2d_gb300", "csrc", "sm2d_redist.h")]
         if not os.path.exists(path) or os.path.getmtime(path) < max(os.path.getmtime(f) for f in srcs):
             build()
         lib = C.CDLL(path)
@@ -104,6 +105,7 @@ def _lib(fp64: bool):
         lib.orc_math.argtypes = [C.c_int, P, P, C.c_int]
         lib.orc_redistribution_table.argtypes = [P, C.c_int, P, P]
         lib.orc_track_claims.argtypes = [P, C.c_int]
+        lib.orc_redist_masses.argtypes = [C.c_double, C.c_double, C.c_double, P, C.c_int, P, P]
         lib.orc_claim_demand.argtypes = [P]
         _LIBS[key] = lib
         return lib
@@ -182,7 +184,7 @@ class Oracle:
         defaults = dict(x_min=0.0, z_min=0.0, E_fine_on=10.0, E_fine_off=11.0,
                         weight_active_min=1e-12, step_coarse=5.0, sigma_x_initial=0.0, E0=0.0,
                         enable_straggling=1, enable_nuclear=1, seed_slot_mode=0, energy_split=0,
-                        grid_E_min=0.0, grid_E_max=0.0, prune_coarse=0.0, prune_fine=0.0, split_min_weight=0.0, stop_weight_fraction=0.0, claim_reserve_weight=0.0, slots_per_cell=32, floor_cutoff=0, seed_iteration_salt=0)
+                        grid_E_min=0.0, grid_E_max=0.0, prune_coarse=0.0, prune_fine=0.0, split_min_weight=0.0, stop_weight_fraction=0.0, claim_reserve_weight=0.0, slots_per_cell=32, floor_cutoff=0, seed_iteration_salt=0, expectation=0)
         defaults.update(cfg)
         for name, _ in OrcConfig._fields_:
             setattr(c, name, defaults[name])
@@ -328,6 +330,16 @@ def psi_rows(bid, val, L, thresh=1e-12, Kb=KB):
     cells, slots, lidx = np.nonzero((v > thresh) & (b[:, :, None] != EMPTY))
     return dict(cell=cells, slot=slots, bid=b[cells, slots], lidx=lidx,
                 weight=v[cells, slots, lidx])
+
+
+def redist_masses(s, Em, sE, cen, fp64=False):
+    """The expectation form's masses (sm2d_redist.h): angular Mt[8] for
+    s = sigma_theta / dtheta, energy Me[4] for E' ~ N(Em, sE^2) over the
+    descending centres cen (1 to 4 of them)."""
+    cen = np.ascontiguousarray(cen, np.float64)
+    Mt, Me = np.zeros(8), np.zeros(4)
+    _lib(fp64).orc_redist_masses(float(s), float(Em), float(sE), _p(cen), cen.size - 1, _p(Mt), _p(Me))
+    return Mt, Me
 
 
 MATH_FUNCS = ("exp", "log", "sin", "cos", "erf")

@@ -12,6 +12,10 @@
  */
 #include "sm2d_oracle.h"
 #include "sm2d_math.h"
+#ifdef ORC_FP64
+#define SM2D_RD_DOUBLE
+#endif
+#include "sm2d_redist.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -692,6 +696,15 @@ static void claims_note(orc_ctx* c, const uint32_t* ids, uint32_t want) {
     if (++c->cc[h].n > c->claim_demand_max) c->claim_demand_max = c->cc[h].n;
 }
 void orc_track_claims(orc_ctx* c, int on) { c->track_claims = on; }
+/* the expectation form's masses (sm2d_redist.h) in this build's precision */
+void orc_redist_masses(double s, double Em, double sE, const double* cen, int emax, double* Mt, double* Me) {
+    real c4[SM2D_RD_NE] = {0}, mt[SM2D_RD_NT], me[SM2D_RD_NE];
+    for (int e = 0; e <= emax && e < SM2D_RD_NE; ++e) c4[e] = (real)cen[e];
+    sm2d_rd_theta((real)s, mt);
+    sm2d_rd_energy((real)Em, (real)sE, c4, emax, me);
+    for (int t = 0; t < SM2D_RD_NT; ++t) Mt[t] = (double)mt[t];
+    for (int e = 0; e < SM2D_RD_NE; ++e) Me[e] = (double)me[e];
+}
 int orc_claim_demand(const orc_ctx* c) { return c->claim_demand_max; }
 
 /* number of slots a deposit of weight w may claim */
@@ -759,6 +772,36 @@ static eparts bin_energy(const orc_ctx* c, real E, real w) {
     return p;
 }
 
+/* expectation form: the children of one component (sm2d_redist.h); c and j
+ * are its incoming angle and energy bins */
+typedef struct kids {
+    int c, j, emax;
+    real Mt[SM2D_RD_NT], Me[SM2D_RD_NE];
+    real Erep;
+} kids;
+/* energy window: its top is the second centre above the step's mean energy
+ * Em, at most the incoming bin jin */
+static void make_kids(const orc_ctx* c, int tb, int jin, real s, real Em, real sE, real w, kids* k) {
+    real Ec = r_max(c->E_edges[0], r_min(Em, c->E_edges[c->N_E]));
+    int b = find_bin_edges(c->E_edges, c->N_E, Ec);
+    int up = Ec >= e_center(c, b) ? b + 1 : b;
+    int Eb = up + 1 < jin ? up + 1 : jin;
+    k->c = tb;
+    k->j = Eb;
+    k->emax = Eb < SM2D_RD_NE - 1 ? Eb : SM2D_RD_NE - 1;
+    real cen[SM2D_RD_NE];
+    for (int e = 0; e <= k->emax; ++e) cen[e] = e_center(c, Eb - e);
+    sm2d_rd_theta(s, k->Mt);
+    sm2d_rd_energy(Em, sE, cen, k->emax, k->Me);
+    k->Erep = sm2d_rd_fold(w, (real)c->cfg.split_min_weight, k->Mt, k->Me, cen, k->emax);
+}
+static inline int kid_tbin(const orc_ctx* c, const kids* k, int kk) {
+    int tb = k->c + sm2d_rd_kid_side(kk) * sm2d_rd_kid_t(kk);
+    if (tb < 0) tb = 0;
+    if (tb > c->N_theta - 1) tb = c->N_theta - 1;
+    return tb;
+}
+
 /* ------------------------------------------------------------------------- */
 /* bucket emission: device_bucket.cuh:431-533 (4-D, theta 2-bin split)       */
 /* ------------------------------------------------------------------------- */
@@ -768,6 +811,32 @@ static inline int ebin_of(const orc_ctx* c, uint32_t bid, int l) {
 }
 /* The split method keeps energy when a saturated slot table re-bins a part
  * into another block: the shift (intended - stored centre) * w goes to *eshift. */
+/* the children of a component (expectation form), in child order */
+static real emit_kids_to_bucket(orc_ctx* c, bucket* bk, const kids* kd, real weight, int xs, int zs, double* eshift) {
+    if (weight <= RL(0.0)) return RL(0.0);
+    real dropped = RL(0.0);
+    for (int e = 0; e <= kd->emax; ++e) {
+        if (kd->Me[e] <= RL(0.0)) continue;
+        int Eb = kd->j - e;
+        int El = Eb % c->cfg.ne_local;
+        uint32_t bE = (uint32_t)(Eb / c->cfg.ne_local);
+        for (int k = 0; k < SM2D_RD_KIDS; ++k) {
+            if (kd->Mt[sm2d_rd_kid_t(k)] <= RL(0.0)) continue;
+            real wk = sm2d_rd_kid_w(weight, kd->Mt, kd->Me, k, e);
+            int tbin = kid_tbin(c, kd, k);
+            uint32_t want = enc_block((uint32_t)(tbin / c->cfg.nt_local), bE);
+            int l = enc_lidx(c, tbin % c->cfg.nt_local, El, xs, zs);
+            uint32_t sel;
+            int s = claim_w(c, bk->bid, c->Kb, want, &sel, (double)wk);
+            if (s < 0) { dropped += wk; continue; }
+            int le = (sel == want) ? l : remap_lidx(c, l, want, sel);
+            if (sel != want && eshift) *eshift += (double)((e_center(c, Eb) - e_center(c, ebin_of(c, sel, le))) * wk);
+            bk->val[(size_t)s * c->L + le] += wk;
+            bk->count[s]++;
+        }
+    }
+    return dropped;
+}
 static real emit_to_bucket(orc_ctx* c, bucket* bk, real theta, real E, real weight, int xs, int zs, double* eshift) {
     if (weight <= RL(0.0)) return RL(0.0);
     real tmin = c->th_edges[0], tmax = c->th_edges[c->N_theta];
@@ -847,7 +916,7 @@ static int neighbor(int cell, int face, int Nx, int Nz) {
 }
 
 /* +z emission with N-cell lateral Gaussian split: device_bucket.cuh:857-987 */
-static real emit_lateral_spread(orc_ctx* c, int src, int tz, real theta, real E, real weight,
+static real emit_lateral_spread(orc_ctx* c, int src, int tz, real theta, real E, const kids* kd, real weight,
                                 real xoff, real sigma, real* boundary_w, double* eshift) {
     if (weight <= RL(0.0)) return RL(0.0);
     real dropped = RL(0.0);
@@ -875,7 +944,8 @@ static real emit_lateral_spread(orc_ctx* c, int src, int tz, real theta, real E,
         int bi = bucket_index(c, emit_cell, FACE_ZP);
         if (bi < 0) { dropped += weight * wf; continue; }
         int xt = off < 0 ? c->cfg.nx_sub - 1 : (off > 0 ? 0 : c->cfg.nx_sub / 2);
-        dropped += emit_to_bucket(c, &c->buckets[bi], theta, E, weight * wf, xt, 0, eshift);
+        dropped += kd ? emit_kids_to_bucket(c, &c->buckets[bi], kd, weight * wf, xt, 0, eshift)
+                      : emit_to_bucket(c, &c->buckets[bi], theta, E, weight * wf, xt, 0, eshift);
     }
     return dropped;
 }
@@ -1021,8 +1091,110 @@ static int emit_stay(orc_ctx* c, int k3, int cell, real theta_new, real E_new, r
     return 1;
 }
 
-/* Crossing a face: k2_coarsetransport.cu:363-459, k3_finetransport.cu:380-503 */
-static void emit_cross(orc_ctx* c, int k3, int cell, int face, real theta_new, real E_new, real w_new,
+/* Expectation form of emit_stay: the children stay in the cell, each spread
+ * over the x sub-bins; the Gaussian tails past the cell edges go to the
+ * lateral buckets as children; the mean energy minus the children's
+ * represented energy is folded into the deposit. */
+static void emit_stay_kids(orc_ctx* c, int k3, int cell, const kids* kd, real E_new, real w_new,
+                           real x_new, real z_new, real sig_sub, real sig_cell, tally* t) {
+    psi_buf* po = psi_out(c);
+    const int Nx = c->cfg.Nx;
+    const real dx = (real)c->cfg.dx, dz = (real)c->cfg.dz;
+    int nxs = c->cfg.nx_sub;
+    real w[64];
+    spread_weights_subcell(w, x_new, sig_sub, dx, nxs);
+    int ix = cell % Nx;
+    int zst = sub_bin(z_new, dz, c->cfg.nz_sub);
+    real lb = -dx * RL(0.5), rb = dx * RL(0.5);
+    real win = gcdf(rb, x_new, sig_cell) - gcdf(lb, x_new, sig_cell);
+    real wcf = r_min(RL(1.0), r_max(RL(0.0), win));
+    real wsum = 0;
+    for (int i = 0; i < nxs; ++i) { w[i] = r_max(RL(0.0), w[i]); wsum += w[i]; }
+    if (wsum < RL(1e-12)) {
+        for (int i = 0; i < nxs; ++i) w[i] = RL(0.0);
+        w[nxs / 2] = RL(1.0);
+        wsum = RL(1.0);
+    }
+    for (int e = 0; e <= kd->emax; ++e) {
+        if (kd->Me[e] <= RL(0.0)) continue;
+        int Eb = kd->j - e;
+        for (int k = 0; k < SM2D_RD_KIDS; ++k) {
+            if (kd->Mt[sm2d_rd_kid_t(k)] <= RL(0.0)) continue;
+            real wk = sm2d_rd_kid_w(w_new, kd->Mt, kd->Me, k, e);
+            int tbn = kid_tbin(c, kd, k);
+            uint32_t want = ((uint32_t)(Eb / c->cfg.ne_local) << 12) | ((uint32_t)(tbn / c->cfg.nt_local) & 0xFFFu);
+            uint32_t sel;
+            int os = psi_slot(c, po, cell, want, &sel, (double)wk);
+            if (os < 0) {
+                double *cw = k3 ? &c->k3_slot_w : &c->k2_slot_w, *ce = k3 ? &c->k3_slot_e : &c->k2_slot_e;
+                *cw += (double)wk;
+                *ce += (double)(E_new * wk);
+                continue;
+            }
+            int tbe = tbn, Ebe = Eb;
+            if (sel != want) {
+                int t0 = (int)(sel & 0xFFFu) * c->cfg.nt_local, e0 = (int)((sel >> 12) & 0xFFFu) * c->cfg.ne_local;
+                if (tbe < t0) tbe = t0;
+                if (tbe > t0 + c->cfg.nt_local - 1) tbe = t0 + c->cfg.nt_local - 1;
+                if (Ebe < e0) Ebe = e0;
+                if (Ebe > e0 + c->cfg.ne_local - 1) Ebe = e0 + c->cfg.ne_local - 1;
+            }
+            if (Ebe != Eb) t->edep += (double)((e_center(c, Eb) - e_center(c, Ebe)) * wk * wcf);
+            int tl = tbe % c->cfg.nt_local, El = Ebe % c->cfg.ne_local;
+            for (int xs = 0; xs < nxs; ++xs) {
+                real wf = (w[xs] / wsum) * wcf;
+                if (wf <= RL(0.0)) continue;
+                int l = enc_lidx(c, tl, El, xs, zst);
+                po->val[((size_t)cell * c->Kb + os) * c->L + l] += wk * wf;
+            }
+        }
+    }
+    real wl = RL(0.0), wr = RL(0.0);
+    if (wcf < RL(1.0) - RL(1e-6)) {
+        real wlr = r_max(RL(0.0), gcdf(lb, x_new, sig_cell));
+        real wrr = r_max(RL(0.0), RL(1.0) - gcdf(rb, x_new, sig_cell));
+        real tt = r_max(RL(0.0), RL(1.0) - wcf);
+        real ts = wlr + wrr;
+        if (tt > RL(0.0) && ts > RL(1e-12)) {
+            real sc = tt / ts;
+            wl = wlr * sc;
+            wr = wrr * sc;
+        }
+        double *bw = k3 ? &c->k3_bkt_w : &c->k2_bkt_w, *be = k3 ? &c->k3_bkt_e : &c->k2_bkt_e;
+        if (wl > RL(0.0)) {
+            real ws = w_new * wl;
+            if (ix > 0) {
+                real d = emit_kids_to_bucket(c, &c->buckets[bucket_index(c, cell, FACE_XM)], kd, ws, nxs - 1, zst,
+                                             &t->edep);
+                if (d > RL(0.0)) { *bw += (double)d; *be += (double)(E_new * d); }
+            } else {
+                t->w_bnd += (float)ws;
+                t->e_bnd += (double)(E_new * ws);
+            }
+        }
+        if (wr > RL(0.0)) {
+            real ws = w_new * wr;
+            if (ix < Nx - 1) {
+                real d = emit_kids_to_bucket(c, &c->buckets[bucket_index(c, cell, FACE_XP)], kd, ws, 0, zst, &t->edep);
+                if (d > RL(0.0)) { *bw += (double)d; *be += (double)(E_new * d); }
+            } else {
+                t->w_bnd += (float)ws;
+                t->e_bnd += (double)(E_new * ws);
+            }
+        }
+    }
+    real rf = wcf;
+    if (ix > 0) rf += wl;
+    if (ix < Nx - 1) rf += wr;
+    rf = r_min(RL(1.0), r_max(RL(0.0), rf));
+    real rw = w_new * rf;
+    if (rw > RL(0.0)) t->edep += (double)((E_new - kd->Erep) * rw);
+}
+
+/* Crossing a face: k2_coarsetransport.cu:363-459, k3_finetransport.cu:380-503;
+ * kd: the component's children in the expectation form (NULL: re-bin the
+ * sampled angle and energy) */
+static void emit_cross(orc_ctx* c, int k3, int cell, int face, real theta_new, real E_new, const kids* kd, real w_new,
                        real x_new, real z_new, real sig_tr, tally* t) {
     const int Nx = c->cfg.Nx, Nz = c->cfg.Nz;
     const real dx = (real)c->cfg.dx, dz = (real)c->cfg.dz;
@@ -1033,13 +1205,12 @@ static void emit_cross(orc_ctx* c, int k3, int cell, int face, real theta_new, r
         t->e_bnd += (double)(E_new * w_new);
         return;
     }
-    eparts ep = bin_energy(c, E_new, w_new);
-    real E_emit_tr = ep.Erep;
+    real E_emit_tr = kd ? kd->Erep : bin_energy(c, E_new, w_new).Erep;
     int fold = k3 || c->cfg.energy_split;
     if (face == FACE_ZP) {
         int tz = cell / Nx + 1;
         real lbw = RL(0.0);
-        real d = emit_lateral_spread(c, cell, tz, theta_new, E_new, w_new, x_new, sig_tr, &lbw, &t->edep);
+        real d = emit_lateral_spread(c, cell, tz, theta_new, E_new, kd, w_new, x_new, sig_tr, &lbw, &t->edep);
         if (lbw > RL(0.0)) {
             t->w_bnd += (float)lbw;
             t->e_bnd += (double)(E_new * lbw);
@@ -1063,7 +1234,8 @@ static void emit_cross(orc_ctx* c, int k3, int cell, int face, real theta_new, r
         *be += (double)(E_new * w_new);
         return;
     }
-    real d = emit_to_bucket(c, &c->buckets[bi], theta_new, E_new, w_new, xsn, zsn, &t->edep);
+    real d = kd ? emit_kids_to_bucket(c, &c->buckets[bi], kd, w_new, xsn, zsn, &t->edep)
+                : emit_to_bucket(c, &c->buckets[bi], theta_new, E_new, w_new, xsn, zsn, &t->edep);
     if (d > RL(0.0)) { *bw += (double)d; *be += (double)(E_new * d); }
     if (fold) {
         real tw = r_max(RL(0.0), w_new - d);
@@ -1173,7 +1345,9 @@ static void k2_cell(orc_ctx* c, int cell) {
             unsigned pseed = (unsigned)r_min(path0 * RL(1000.0), RL(4294967295.0));
             unsigned ts = ((unsigned)(cell + 1) * SEED_A) ^ ((unsigned)(sslot + 1) * SEED_B) ^
                           ((unsigned)(l + 1) * SEED_C) ^ (unsigned)(Ebin + 17) ^ (pseed * 747796405u) ^ iter_salt(c);
-            real scat = (sig_th <= RL(0.0)) ? RL(0.0) : gauss_sample(&ts) * sig_th;
+            /* expectation form: the MCS distribution instead of a draw, the
+             * step along the incoming angle */
+            real scat = c->cfg.expectation ? RL(0.0) : ((sig_th <= RL(0.0)) ? RL(0.0) : gauss_sample(&ts) * sig_th);
             real theta_new = theta + scat;
             theta_new = r_max(c->th_edges[0], r_min(theta_new, c->th_edges[c->N_theta]));
             real mu = r_cos(theta_new), eta = r_sin(theta_new);
@@ -1190,7 +1364,16 @@ static void k2_cell(orc_ctx* c, int cell) {
                 t.e_cut += (double)(E_new * w_new);
                 continue;
             }
-            if (face >= 0) emit_cross(c, 0, cell, face, theta_new, E_new, w_new, x_new, z_new, sig_tr, &t);
+            if (c->cfg.expectation) {
+                kids kd;
+                int tc = tbin < 0 ? 0 : (tbin > c->N_theta - 1 ? c->N_theta - 1 : tbin);
+                int ec = Ebin < 0 ? 0 : (Ebin > c->N_E - 1 ? c->N_E - 1 : Ebin);
+                make_kids(c, tc, ec, sig_th / dth, E_new, RL(0.0), w_new, &kd);
+                if (face >= 0) emit_cross(c, 0, cell, face, theta_new, E_new, &kd, w_new, x_new, z_new, sig_tr, &t);
+                else emit_stay_kids(c, 0, cell, &kd, E_new, w_new, x_new, z_new, sig_x, sig_x, &t);
+                continue;
+            }
+            if (face >= 0) emit_cross(c, 0, cell, face, theta_new, E_new, NULL, w_new, x_new, z_new, sig_tr, &t);
             else emit_stay(c, 0, cell, theta_new, E_new, w_new, x_new, z_new, sig_x, sig_x, &t);
         }
     }
@@ -1251,8 +1434,11 @@ static void k3_cell(orc_ctx* c, int cell) {
             real sphys = max_step(lut, E) / rho;   /* the water-equivalent limit as a geometric step */
             real step = r_min(sphys, sb * BOUNDARY_SAFETY);
             real mean_dE = lut_energy_deposition(lut, E, rho * step);
-            real dE;
-            if (c->cfg.enable_straggling) {
+            real dE, sE = RL(0.0);
+            if (c->cfg.expectation) {   /* the straggling distribution instead of a draw */
+                dE = mean_dE;
+                if (c->cfg.enable_straggling) sE = straggling_sigma(E, step, rho);
+            } else if (c->cfg.enable_straggling) {
                 unsigned seed = ((unsigned)(cell * 7 + sslot * 13 + l * 17) ^ 0xDEECE66Du) ^ iter_salt(c);
                 real sE = straggling_sigma(E, step, rho);
                 if (sE <= RL(0.0)) dE = mean_dE;
@@ -1280,7 +1466,7 @@ static void k3_cell(orc_ctx* c, int cell) {
             unsigned pseed = (unsigned)r_min((real)iz * dz * RL(1000.0), RL(4294967295.0));
             unsigned ts = ((unsigned)(cell + 1) * SEED_A) ^ ((unsigned)(sslot + 1) * SEED_B) ^
                           ((unsigned)(l + 1) * SEED_C) ^ (unsigned)(Ebin + 17) ^ (pseed * 747796405u) ^ iter_salt(c);
-            real scat = (sig_th <= RL(0.0)) ? RL(0.0) : gauss_sample(&ts) * sig_th;
+            real scat = c->cfg.expectation ? RL(0.0) : ((sig_th <= RL(0.0)) ? RL(0.0) : gauss_sample(&ts) * sig_th);
             real theta_new = theta + scat;
             theta_new = r_max(c->th_edges[0], r_min(theta_new, c->th_edges[c->N_theta]));
             real mu = r_cos(theta_new), eta = r_sin(theta_new);
@@ -1297,7 +1483,15 @@ static void k3_cell(orc_ctx* c, int cell) {
                 t.e_cut += (double)(E_new * w_new);
                 continue;
             }
-            if (face >= 0) emit_cross(c, 1, cell, face, theta_new, E_new, w_new, x_new, z_new, K3_SIGMA_TRANSPORT, &t);
+            if (c->cfg.expectation) {
+                kids kd;
+                make_kids(c, tbin, Ebin, sig_th / dth, E_new, sE, w_new, &kd);
+                if (face >= 0)
+                    emit_cross(c, 1, cell, face, theta_new, E_new, &kd, w_new, x_new, z_new, K3_SIGMA_TRANSPORT, &t);
+                else emit_stay_kids(c, 1, cell, &kd, E_new, w_new, x_new, z_new, K3_SIGMA_TRANSPORT, sig_x, &t);
+                continue;
+            }
+            if (face >= 0) emit_cross(c, 1, cell, face, theta_new, E_new, NULL, w_new, x_new, z_new, K3_SIGMA_TRANSPORT, &t);
             else emit_stay(c, 1, cell, theta_new, E_new, w_new, x_new, z_new, K3_SIGMA_TRANSPORT, sig_x, &t);
         }
     }

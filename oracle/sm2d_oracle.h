@@ -74,6 +74,10 @@ typedef struct orc_config {
      * ((iter-1) * 0x9E3779B9, so the first iteration is unchanged); the
      * reference re-draws the same numbers for a bin every iteration */
     int seed_iteration_salt;
+    /* 1: expectation form -- K2/K3 emit the expected result of re-binning
+     * their MCS angle and straggling loss (sm2d_redist.h) instead of one
+     * hashed draw of each; needs energy_split = 1 */
+    int expectation;
 } orc_config;
 
 typedef struct orc_audit {       /* AuditReport, k5_audit.cuh:5-27 */
@@ -162,6 +166,10 @@ void orc_redistribution_table(const orc_ctx* c, int n, const float* feats, float
  * block ids aimed at one container (a psi_out cell, or one bucket of one
  * batch) within one iteration since tracking began */
 void orc_track_claims(orc_ctx* c, int on);
+/* the expectation form's angular masses Mt[8] for s = sigma_theta / dtheta
+ * and energy masses Me[4] for a Gaussian (Em, sE) over the centres cen[0..emax]
+ * (sm2d_redist.h), evaluated in this build's precision */
+void orc_redist_masses(double s, double Em, double sE, const double* cen, int emax, double* Mt, double* Me);
 int  orc_claim_demand(const orc_ctx* c);
 
 /* run several independent contexts on n_threads host threads */

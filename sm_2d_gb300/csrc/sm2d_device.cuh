@@ -189,6 +189,8 @@ struct Dev {
     uint4* bins;          // w > 0 bins of the listed cells, grouped by cell:
                           // {gc, slot | seed slot << 5 | lidx << 10 | K3 << 18, w bits, block id}
     uint4* brec;          // per bin, two uint4: the step's outcome from the claim pass
+    float2* brec2;        // expectation form, per bin: sigma_theta / dtheta, straggling sigma
+    int expect;           // 1: expectation form (redistribution weights instead of draws)
     int2* cell_bins;      // per listed cell: its first bin and bin count in the bin list
     int bins_cap;
     uint32_t *active, *coarse;   // ascending lists of lane 0 (built on request by k_order_lists)

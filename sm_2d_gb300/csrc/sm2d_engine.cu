@@ -587,7 +587,7 @@ __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
 // per SM: five for the claim pass (47 registers, no spills; 27.2 -> 24.1 ms
 // per wave of 80 spots against four), four for the deposit passes (five
 // would spill).
-template <class Lay, int PASS>
+template <class Lay, int PASS, bool EXP = false>
 __global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 5 : 4) k_transport(Dev d) {
     __shared__ LaneSums<2> s_sum;   // drop_w, drop_e
     IterGlobal* gs = d.gs;
@@ -613,8 +613,8 @@ __global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 5 : 4) k_transpo
             const int slot = (int)(r.y & 31u), sslot = (int)((r.y >> 5) & 31u), lidx = (int)((r.y >> 10) & 0xFFu);
             const bool k3 = ((r.y >> 18) & 1u) != 0;
             const unsigned salt = d.salt ? (unsigned)d.ls[ln].iter * 0x9E3779B9u : 0u;
-            transport_bin<Lay, PASS>(d, i, par, k3, cell, ln, cell - ln * d.Nc, r.w, slot, sslot, lidx,
-                                     __uint_as_float(r.z), salt, tag, t);
+            transport_bin<Lay, PASS, EXP>(d, i, par, k3, cell, ln, cell - ln * d.Nc, r.w, slot, sslot, lidx,
+                                          __uint_as_float(r.z), salt, tag, t);
         }
         if (PASS != PASS_KEYS) {
             unsigned same[5];
@@ -1507,13 +1507,17 @@ struct Impl {
         CK(rec(1));
         if (lists) k_order_lists<<<1, 1024, 0, c.s>>>(c.d);
         CK(rec(2));
-        k_transport<Lay, PASS_KEYS><<<gk, kThreads, 0, c.s>>>(c.d);
+        // the expectation form (direct scatter only) has kernels of its own,
+        // so the sampled form's keep their registers
+        if (c.d.expect) k_transport<Lay, PASS_KEYS, true><<<gk, kThreads, 0, c.s>>>(c.d);
+        else k_transport<Lay, PASS_KEYS><<<gk, kThreads, 0, c.s>>>(c.d);
         CK(rec(3));
         if (bk) k_select_buckets<Lay, true><<<gc, kThreads, 0, c.s>>>(c.d);
         else k_select_buckets<Lay, false><<<gc, kThreads, 0, c.s>>>(c.d);
         k_select_psi<<<gc, kThreads, 0, c.s>>>(c.d, 1);
         CK(rec(4));
         if (bk) k_transport<Lay, PASS_BUCKET><<<gt, kThreads, 0, c.s>>>(c.d);
+        else if (c.d.expect) k_transport<Lay, PASS_DIRECT, true><<<gt, kThreads, 0, c.s>>>(c.d);
         else k_transport<Lay, PASS_DIRECT><<<gt, kThreads, 0, c.s>>>(c.d);
         CK(rec(5));
         if (bk) k_bucket_push<Lay><<<gc, kThreads, 0, c.s>>>(c.d);
@@ -1527,11 +1531,13 @@ struct Impl {
     // kernels stride over the bin list)
     static int transport_grid(Ctx& c, int sms) {
         int per_sm = 0, per_sm_keys = 0;
-        cudaError_t e = c.p.use_buckets
-                            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_BUCKET>, kThreads, 0)
+        cudaError_t e =
+            c.p.use_buckets ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_BUCKET>, kThreads, 0)
+            : c.d.expect    ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_DIRECT, true>, kThreads, 0)
                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<Lay, PASS_DIRECT>, kThreads, 0);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_keys, k_transport<Lay, PASS_KEYS>, kThreads, 0);
+            e = c.d.expect ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_keys, k_transport<Lay, PASS_KEYS, true>, kThreads, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_keys, k_transport<Lay, PASS_KEYS>, kThreads, 0);
         if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
         const long long blocks_for_cap = ((long long)c.d.bins_cap + kThreads - 1) / kThreads;
         const long long s = std::max(sms, 1);
@@ -1778,6 +1784,10 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
         for (int iz = 0; iz < p->Nz; ++iz)
             if (!(p->density_z[iz] > 0.0f) || !std::isfinite(p->density_z[iz]))
                 return fail(SM2D_ERR_ARG, "density of row %d must be positive", iz);
+    if (p->expectation && !p->energy_split)
+        return fail(SM2D_ERR_ARG, "the expectation form needs the energy split (energy_split = 1)");
+    if (p->expectation && p->use_buckets)
+        return fail(SM2D_ERR_ARG, "the expectation form runs the direct neighbour scatter (use_buckets = 0)");
     sm2d_ctx* c = new sm2d_ctx();
     c->p = *p;
     c->layout = layout;
@@ -1827,6 +1837,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     d.stop_frac = p->stop_weight_fraction;
     d.floor_cutoff = p->floor_cutoff;
     d.salt = p->seed_iteration_salt;
+    d.expect = p->expectation ? 1 : 0;
     const size_t Nc = (size_t)d.Nc, NcB = Nc * B, ns = NcB * kKb;
     void* q;
     int rc;
@@ -1902,6 +1913,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.bins, uint4, d.bins_cap);
     A(d.cell_bins, int2, d.listed_cap);
     A(d.brec, uint4, 2 * (size_t)d.bins_cap);
+    if (d.expect) A(d.brec2, float2, (size_t)d.bins_cap);
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
     A(d.gs, IterGlobal, 1);
     A(d.ls, LaneState, B);

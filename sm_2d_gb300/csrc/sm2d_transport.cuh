@@ -21,6 +21,7 @@
 //     cell and face; the bucket move kernel then runs K4_BucketTransfer.
 #pragma once
 #include "sm2d_device.cuh"
+#include "sm2d_redist.h"
 
 namespace sm2d {
 
@@ -86,17 +87,19 @@ __device__ __forceinline__ unsigned long long* psi_row(const Dev& d, int cell) {
 __device__ __forceinline__ unsigned long long* bucket_row(const Dev& d, int bf) {
     return d.ctab + ((size_t)d.B * d.Nc + bf) * (2 * kCand);
 }
-// claim keys: psi_out rows [batch:1][part:3][slot:5][lidx:8][part index:1]
+// claim keys: psi_out rows [batch:1][part:3][slot:5][lidx:8][part index:6]
 // (part 0 in-cell deposit, 1 + f the K4 transfer of face f by bucket slot);
-// bucket rows [emitting column 0..10:4][slot:5][lidx:8][emission index:2]
+// bucket rows [emitting column 0..10:4][slot:5][lidx:8][emission index:6].
+// The emission index is the energy part (sampled form) or the child
+// 16 e + k of the expectation form, in the order the oracle emits them.
 __device__ __forceinline__ uint32_t stay_key(int k3, int slot, int lidx, int ei) {
-    return ((uint32_t)k3 << 17) | ((uint32_t)slot << 9) | ((uint32_t)lidx << 1) | (uint32_t)ei;
+    return ((uint32_t)k3 << 22) | ((uint32_t)slot << 14) | ((uint32_t)lidx << 6) | (uint32_t)ei;
 }
 __device__ __forceinline__ uint32_t k4_key(int k3, int face, int kslot) {
-    return ((uint32_t)k3 << 17) | ((uint32_t)(1 + face) << 14) | (uint32_t)kslot;
+    return ((uint32_t)k3 << 22) | ((uint32_t)(1 + face) << 19) | (uint32_t)kslot;
 }
 __device__ __forceinline__ uint32_t bucket_key(int col, int slot, int lidx, int seq) {
-    return ((uint32_t)col << 15) | ((uint32_t)slot << 10) | ((uint32_t)lidx << 2) | (uint32_t)seq;
+    return ((uint32_t)col << 19) | ((uint32_t)slot << 14) | ((uint32_t)lidx << 6) | (uint32_t)seq;
 }
 template <class Lay>
 __device__ __forceinline__ int ebin_of(const Dev& d, uint32_t bid, int l) {
@@ -281,11 +284,79 @@ __device__ float emit_component(const Dev& d, const Src& src, int par, int bcell
     return dropped;
 }
 
+// Expectation form: the children of one component (sm2d_redist.h).  c is
+// its incoming angle bin; j the top of its energy window: the second centre
+// above the step's mean energy Em, at most the incoming bin jin (a step
+// gains no energy).  Child k of energy offset e goes to angle bin c - t or
+// c + t (t = (k + 1) / 2) and energy bin j - e.
+struct Kids {
+    int c, j, emax;
+    float Mt[SM2D_RD_NT], Me[SM2D_RD_NE];
+    float Erep;   // represented energy of the children
+};
+__device__ __forceinline__ int kid_window_top(const Dev& d, int jin, float Em) {
+    const float Ec = fmaxf(d.Ee[0], fminf(Em, d.Ee[d.N_E]));
+    const int b = find_ebin(d, Ec);
+    const int up = Ec >= e_center(d, b) ? b + 1 : b;   // the lowest centre at or above Em
+    return min(jin, up + 1);
+}
+__device__ __forceinline__ void make_kids(const Dev& d, int c, int jin, float s, float Em, float sE, float w, Kids& k) {
+    const int j = kid_window_top(d, jin, Em);
+    k.c = c;
+    k.j = j;
+    k.emax = min(SM2D_RD_NE - 1, j);
+    float cen[SM2D_RD_NE];
+    for (int e = 0; e <= k.emax; ++e) cen[e] = e_center(d, j - e);
+    sm2d_rd_theta(s, k.Mt);
+    sm2d_rd_energy(Em, sE, cen, k.emax, k.Me);
+    k.Erep = sm2d_rd_fold(w, d.split_min_w, k.Mt, k.Me, cen, k.emax);
+}
+__device__ __forceinline__ int kid_tbin(const Dev& d, const Kids& k, int kk) {
+    return max(0, min(k.c + sm2d_rd_kid_side(kk) * sm2d_rd_kid_t(kk), d.N_theta - 1));
+}
+// the children of a component of weight `weight` into one container, in
+// child order (the claim key's emission index is the child number)
+template <class Lay, int PASS>
+__device__ float emit_component(const Dev& d, const Src& src, int par, int bcell, int face, int dcell, int col,
+                                const Kids& kd, float weight, int xs, int zs, Tally& t) {
+    if (weight <= 0.0f) return 0.0f;
+    float dropped = 0.0f;
+    for (int e = 0; e <= kd.emax; ++e) {
+        if (kd.Me[e] <= 0.0f) continue;
+        const int Eb = kd.j - e;
+        const int El = Eb % Lay::NE;
+        const uint32_t bE = (uint32_t)(Eb / Lay::NE);
+        for (int k = 0; k < SM2D_RD_KIDS; ++k) {
+            if (kd.Mt[sm2d_rd_kid_t(k)] <= 0.0f) continue;
+            const float wk = sm2d_rd_kid_w(weight, kd.Mt, kd.Me, k, e);
+            if (PASS != PASS_KEYS && wk <= 0.0f) continue;
+            const int tb = kid_tbin(d, kd, k);
+            const uint32_t want = make_bid((uint32_t)(tb / Lay::NT), bE);
+            const int l = Lay::enc(tb % Lay::NT, El, xs, zs);
+            dropped += put<Lay, PASS>(d, src, par, bcell, face, dcell, col, 16 * e + k, want, l, wk, t);
+        }
+    }
+    return dropped;
+}
+// The sampled form plans a component where it is emitted (plan_emission of
+// its new angle and energy); the expectation form's children are planned
+// once per component.
+struct AngleEnergy {
+    float theta, E;
+};
+__device__ __forceinline__ EmitPlan plan_of(const Dev& d, const AngleEnergy& a) { return plan_emission(d, a.theta, a.E); }
+__device__ __forceinline__ const Kids& plan_of(const Dev&, const Kids& k) { return k; }
+// energy of the re-binned parts of a planned component
+__device__ __forceinline__ float plan_erep(const Dev& d, const AngleEnergy&, float E, float w) {
+    return bin_energy(d, E, w).Erep;
+}
+__device__ __forceinline__ float plan_erep(const Dev&, const Kids& k, float, float) { return k.Erep; }
+
 // +z crossing with the N-cell lateral Gaussian split: the share of column
 // ix+k goes through the +z bucket of cell (ix+k, iz) to cell (ix+k, iz+1)
 // (device_bucket.cuh:857-987).
-template <class Lay, int PASS>
-__device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int my_cls, float theta, float E,
+template <class Lay, int PASS, class Plan>
+__device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int my_cls, const Plan& pl, float E,
                               float weight, float xoff, float sigma, float& boundary_w, Tally& t) {
     if (weight <= 0.0f) return 0.0f;
     constexpr int N = 11;
@@ -302,8 +373,8 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
                 boundary_w += weight;
                 return 0.0f;
             }
-            const EmitPlan pl = plan_emission(d, theta, E);
-            return emit_component<Lay, PASS>(d, sc, par, src, FACE_ZP, src + d.Nx, N / 2, pl, weight, Lay::NX / 2, 0, t);
+            const auto& pk = plan_of(d, pl);
+            return emit_component<Lay, PASS>(d, sc, par, src, FACE_ZP, src + d.Nx, N / 2, pk, weight, Lay::NX / 2, 0, t);
         }
     }
     float w[N];
@@ -335,7 +406,7 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
             if (w[i] != 0.0f) w[i] /= s;
     }
     const int ixs = src % d.Nx, izs = (src / d.Nx) % d.Nz, tz = izs + 1;
-    const EmitPlan pl = plan_emission(d, theta, E);
+    const auto& pk = plan_of(d, pl);
     float dropped = 0.0f;
     for (int i = 0; i < N; ++i) {
         const float wf = w[i];
@@ -352,7 +423,7 @@ __device__ float emit_forward(const Dev& d, const Src& sc, int par, int src, int
             continue;
         }
         const int xt = off < 0 ? Lay::NX - 1 : (off > 0 ? 0 : Lay::NX / 2);
-        dropped += emit_component<Lay, PASS>(d, sc, par, ecell, FACE_ZP, ecell + d.Nx, N - 1 - i, pl, weight * wf,
+        dropped += emit_component<Lay, PASS>(d, sc, par, ecell, FACE_ZP, ecell + d.Nx, N - 1 - i, pk, weight * wf,
                                              xt, 0, t);
     }
     return dropped;
@@ -509,10 +580,159 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
     }
 }
 
-// Component crosses `face` (k2_coarsetransport.cu:363-459, k3_finetransport.cu:380-503).
+// Expectation form of emit_stay: the component's children stay in the cell,
+// each spread over the x sub-bins as emit_stay spreads a component; the
+// Gaussian tails past the cell edges go to the lateral neighbours as
+// children; the difference between the step's mean energy and the
+// children's represented energy is folded into the deposit.
 template <class Lay, int PASS>
+__device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, const Kids& kd, float E_new,
+                               float w_new, float x_new, float z_new, float sig_sub, float sig_cell, Tally& t) {
+    const float dx = d.dx, dz = d.dz;
+    const int ix = cell % d.Nx;
+    const int zst = sub_bin(z_new, dz, Lay::NZ);
+    const float lb = -dx * 0.5f, rb = dx * 0.5f;
+    const float win = gauss_cdf(rb, x_new, sig_cell) - gauss_cdf(lb, x_new, sig_cell);
+    const float wcf = fminf(1.0f, fmaxf(0.0f, win));
+    if (PASS == PASS_KEYS) {
+        for (int e = 0; e <= kd.emax; ++e) {
+            if (kd.Me[e] <= 0.0f) continue;
+            const uint32_t bE = (uint32_t)((kd.j - e) / Lay::NE);
+            for (int k = 0; k < SM2D_RD_KIDS; ++k) {
+                if (kd.Mt[sm2d_rd_kid_t(k)] <= 0.0f) continue;
+                const uint32_t want = make_bid((uint32_t)(kid_tbin(d, kd, k) / Lay::NT), bE);
+                cand_insert(psi_row(d, cell), d.ccount + cell, sc.tag, want, stay_key(sc.k3, sc.slot, sc.lidx, 16 * e + k),
+                            &d.gs->cand_ovf);
+            }
+        }
+        mark_occupied(d, par ^ 1, cell);
+    } else {
+        float w[Lay::NX];
+        const float sg = fmaxf(sig_sub, 1e-6f);
+        const float dxs = dx / (float)Lay::NX;
+        const float xmin = -dx * 0.5f;
+        const int kc = max(0, min((int)floorf((x_new - xmin) / dxs), Lay::NX - 1));
+        const bool unit = ((xmin + (float)kc * dxs) - x_new < -8.0f * sg) &&
+                          ((xmin + (float)(kc + 1) * dxs) - x_new > 8.0f * sg);
+        if (unit) {
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) w[i] = (i == kc) ? 1.0f : 0.0f;
+        } else {
+            float prev = gauss_cdf(xmin, x_new, sg);
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) {
+                float cur = gauss_cdf(xmin + (float)(i + 1) * dxs, x_new, sg);
+                w[i] = cur - prev;
+                prev = cur;
+            }
+            float s = 0.0f;
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) s += w[i];
+            if (s > 1e-10f) {
+#pragma unroll
+                for (int i = 0; i < Lay::NX; ++i)
+                    if (w[i] != 0.0f) w[i] /= s;
+            } else {
+#pragma unroll
+                for (int i = 0; i < Lay::NX; ++i) w[i] = (i == Lay::NX / 2) ? 1.0f : 0.0f;
+            }
+        }
+        float wsum = 0.0f;
+#pragma unroll
+        for (int i = 0; i < Lay::NX; ++i) { w[i] = fmaxf(0.0f, w[i]); wsum += w[i]; }
+        if (wsum < 1e-12f) {
+#pragma unroll
+            for (int i = 0; i < Lay::NX; ++i) w[i] = 0.0f;
+            w[Lay::NX / 2] = 1.0f;
+            wsum = 1.0f;
+        }
+        const uint32_t* kept = d.bid + (size_t)cell * kKb;
+        float* vals = d.val + (size_t)cell * kKb * Lay::L;
+        for (int e = 0; e <= kd.emax; ++e) {
+            if (kd.Me[e] <= 0.0f) continue;
+            const int Eb = kd.j - e;
+            const uint32_t bE = (uint32_t)(Eb / Lay::NE);
+            for (int k = 0; k < SM2D_RD_KIDS; ++k) {
+                if (kd.Mt[sm2d_rd_kid_t(k)] <= 0.0f) continue;
+                const float wk = sm2d_rd_kid_w(w_new, kd.Mt, kd.Me, k, e);
+                if (wk <= 0.0f) continue;
+                const int tbn = kid_tbin(d, kd, k);
+                const uint32_t want = make_bid((uint32_t)(tbn / Lay::NT), bE);
+                uint32_t sel;
+                const int os = resolve(d, psi_row(d, cell), kept, sc.tag, want, sel);
+                if (os < 0) {
+                    t.drop_w += (double)wk;
+                    t.drop_e += (double)(E_new * wk);
+                    count_drop(d.gs, sc.k3, DROP_SLOT, (double)wk, (double)(E_new * wk));
+                    continue;
+                }
+                int tbe = tbn, Ebe = Eb;
+                if (sel != want) {
+                    const int t0 = (int)(sel & 0xFFFu) * Lay::NT, e0 = (int)((sel >> 12) & 0xFFFu) * Lay::NE;
+                    tbe = max(t0, min(tbe, t0 + Lay::NT - 1));
+                    Ebe = max(e0, min(Ebe, e0 + Lay::NE - 1));
+                }
+                if (Ebe != Eb) t.edep += (double)((e_center(d, Eb) - e_center(d, Ebe)) * wk * wcf);
+                const int tl = tbe % Lay::NT, El = Ebe % Lay::NE;
+                float* vs = vals + (size_t)os * Lay::L;
+#pragma unroll
+                for (int xs = 0; xs < Lay::NX; ++xs) {
+                    if (w[xs] <= 0.0f) continue;
+                    const float wf = (w[xs] / wsum) * wcf;
+                    if (wf <= 0.0f) continue;
+                    atomicAdd(vs + Lay::enc(tl, El, xs, zst), wk * wf);
+                }
+            }
+        }
+    }
+    float wl = 0.0f, wr = 0.0f;
+    if (wcf < 1.0f - 1e-6f) {
+        const float wlr = fmaxf(0.0f, gauss_cdf(lb, x_new, sig_cell));
+        const float wrr = fmaxf(0.0f, 1.0f - gauss_cdf(rb, x_new, sig_cell));
+        const float tt = fmaxf(0.0f, 1.0f - wcf);
+        const float ts = wlr + wrr;
+        if (tt > 0.0f && ts > 1e-12f) {
+            const float sc_ = tt / ts;
+            wl = wlr * sc_;
+            wr = wrr * sc_;
+        }
+        if (wl > 0.0f) {
+            const float ws = w_new * wl;
+            if (ix > 0) {
+                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XM, cell - 1, 5, kd, ws, Lay::NX - 1,
+                                                           zst, t);
+                if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
+            } else {
+                t.w_bnd += ws;
+                t.e_bnd += (double)(E_new * ws);
+            }
+        }
+        if (wr > 0.0f) {
+            const float ws = w_new * wr;
+            if (ix < d.Nx - 1) {
+                const float dr = emit_component<Lay, PASS>(d, sc, par, cell, FACE_XP, cell + 1, 5, kd, ws, 0, zst, t);
+                if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
+            } else {
+                t.w_bnd += ws;
+                t.e_bnd += (double)(E_new * ws);
+            }
+        }
+    }
+    if (PASS != PASS_KEYS) {
+        float rf = wcf;
+        if (ix > 0) rf += wl;
+        if (ix < d.Nx - 1) rf += wr;
+        rf = fminf(1.0f, fmaxf(0.0f, rf));
+        const float rw = w_new * rf;
+        if (rw > 0.0f) t.edep += (double)((E_new - kd.Erep) * rw);
+    }
+}
+
+// Component crosses `face` (k2_coarsetransport.cu:363-459, k3_finetransport.cu:380-503);
+// pl: plan_emission of its new angle and energy, or its children (expectation form).
+template <class Lay, int PASS, class Plan>
 __device__ void emit_cross(const Dev& d, const Src& sc, int par, bool k3, int cell, int my_cls, int face,
-                           float theta_new, float E_new, float w_new, float x_new, float z_new, float sig_tr, Tally& t) {
+                           const Plan& pl, float E_new, float w_new, float x_new, float z_new, float sig_tr, Tally& t) {
     const int ix = cell % d.Nx, iz = (cell / d.Nx) % d.Nz;
     int nb = -1;
     if (face == FACE_ZP) nb = iz + 1 < d.Nz ? cell + d.Nx : -1;
@@ -524,12 +744,11 @@ __device__ void emit_cross(const Dev& d, const Src& sc, int par, bool k3, int ce
         t.e_bnd += (double)(E_new * w_new);
         return;
     }
-    const float E_emit = bin_energy(d, E_new, w_new).Erep;
+    const float E_emit = plan_erep(d, pl, E_new, w_new);
     const bool fold = PASS != PASS_KEYS && (k3 || d.esplit);
     if (face == FACE_ZP) {
         float lbw = 0.0f;
-        const float dr =
-            emit_forward<Lay, PASS>(d, sc, par, cell, my_cls, theta_new, E_new, w_new, x_new, sig_tr, lbw, t);
+        const float dr = emit_forward<Lay, PASS>(d, sc, par, cell, my_cls, pl, E_new, w_new, x_new, sig_tr, lbw, t);
         if (lbw > 0.0f) { t.w_bnd += lbw; t.e_bnd += (double)(E_new * lbw); }
         if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
         if (fold) {
@@ -542,8 +761,7 @@ __device__ void emit_cross(const Dev& d, const Src& sc, int par, bool k3, int ce
     const float xo = face == FACE_XP ? -dx * 0.5f : (face == FACE_XM ? dx * 0.5f : x_new);
     const int xsn = sub_bin(xo, dx, Lay::NX);
     const int zsn = face == FACE_ZM ? Lay::NZ - 1 : sub_bin(z_new, dz, Lay::NZ);
-    const float dr =
-        emit_component<Lay, PASS>(d, sc, par, cell, face, nb, 5, plan_emission(d, theta_new, E_new), w_new, xsn, zsn, t);
+    const float dr = emit_component<Lay, PASS>(d, sc, par, cell, face, nb, 5, plan_of(d, pl), w_new, xsn, zsn, t);
     if (dr > 0.0f) { t.drop_w += (double)dr; t.drop_e += (double)(E_new * dr); }
     if (fold) {
         const float tw = fmaxf(0.0f, w_new - dr);
@@ -567,7 +785,7 @@ __device__ __forceinline__ int exit_face(float x, float z, float dx, float dz) {
 // energy, weight, raw position, lateral sigma, deposit, nuclear loss) in the
 // bin's record; the deposit pass reads it back instead of repeating the
 // physics, so both passes emit the same arithmetic's results.
-template <class Lay, int PASS>
+template <class Lay, int PASS, bool EXP>
 __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, int ln, int lc, uint32_t bid, int slot,
                               int sslot, int lidx, float w, unsigned salt, uint32_t tag, Tally& t) {
     const float dx = d.dx, dz = d.dz;
@@ -599,11 +817,17 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
     }
     const float hx = dx * 0.5f, hz = dz * 0.5f;
     float theta_new, x_new, z_new, E_new, w_new, edep, w_rem = 0.0f, sigv;
+    float s_th = 0.0f, s_E = 0.0f;   // expectation form: sigma_theta / dtheta, straggling sigma
     float4* rec = reinterpret_cast<float4*>(d.brec + 2 * (size_t)bi);
     if (PASS != PASS_KEYS) {
         const float4 r0 = __ldcs(rec), r1 = __ldcs(rec + 1);
         theta_new = r0.x; E_new = r0.y; w_new = r0.z; x_new = r0.w;
         z_new = r1.x; sigv = r1.y; edep = r1.z; w_rem = r1.w;
+        if (EXP) {
+            const float2 r2 = __ldcs(d.brec2 + bi);
+            s_th = r2.x;
+            s_E = r2.y;
+        }
     } else {
     const float xc = sub_offset(xs, Lay::NX, dx), zc = sub_offset(zs, Lay::NZ, dz);
     const int iz = lc / d.Nx;
@@ -624,7 +848,10 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         const float RE = d.k2tab ? __ldg(d.k2tab + Ebin).x : lut_range(d, E);   // Ebin is clamped here
         step = fminf(fine_step_limit(E, RE) / rho, sb * 1.001f);
         const float mean_dE = lut_energy_loss(d, E, RE, rho * step);
-        if (d.straggle) {
+        if (EXP) {   // the straggling distribution instead of a draw
+            dE = mean_dE;
+            s_E = d.straggle ? straggling_sigma(E, step, rho) : 0.0f;
+        } else if (d.straggle) {
             unsigned seed = ((unsigned)(lc * 7 + sslot * 13 + lidx * 17) ^ 0xDEECE66Du) ^ salt;
             const float sE = straggling_sigma(E, step, rho);
             dE = sE <= 0.0f ? mean_dE : fmaxf(mean_dE + normal_draw(seed) * sE, 0.0f);
@@ -698,7 +925,9 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
         ts = ((unsigned)(lc + 1) * 2654435761u) ^ ((unsigned)(sslot + 1) * 2246822519u) ^
              ((unsigned)(lidx + 1) * 3266489917u) ^ (unsigned)(Ebin + 17) ^ (ps * 747796405u) ^ salt;
     }
-    const float scat = sig_th <= 0.0f ? 0.0f : normal_draw(ts) * sig_th;
+    float scat = 0.0f;
+    if (EXP) s_th = sig_th / dth;   // the MCS distribution instead of a draw: geometry along theta
+    else scat = sig_th <= 0.0f ? 0.0f : normal_draw(ts) * sig_th;
     theta_new = fmaxf(d.th[0], fminf(theta + scat, d.th[d.N_theta]));
     x_new = xc + sm2d_sinf(theta_new) * step;
     z_new = zc + sm2d_cosf(theta_new) * step;
@@ -707,6 +936,7 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
                : sig_x;
     __stcg(rec, make_float4(theta_new, E_new, w_new, x_new));
     __stcg(rec + 1, make_float4(z_new, sigv, edep, w_rem));
+    if (EXP) __stcg(d.brec2 + bi, make_float2(s_th, s_E));
     }
     const int face = exit_face(x_new, z_new, dx, dz);
     x_new = fmaxf(-hx, fminf(x_new, hx));
@@ -720,8 +950,18 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
     }
     const int my_cls = k3 ? 2 : 1;
     const Src sc{cell, slot, lidx, k3 ? 1 : 0, tag, E_new};
+    if (EXP) {
+        Kids kd;
+        make_kids(d, max(0, min(tbin, d.N_theta - 1)), max(0, min(Ebin, d.N_E - 1)), s_th, E_new, s_E, w_new, kd);
+        if (face >= 0)
+            emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, kd, E_new, w_new, x_new, z_new, sigv, t);
+        else
+            emit_stay_kids<Lay, PASS>(d, sc, par, cell, kd, E_new, w_new, x_new, z_new, k3 ? 0.001f : sigv, sigv, t);
+        return;
+    }
     if (face >= 0) {
-        emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, theta_new, E_new, w_new, x_new, z_new, sigv, t);
+        emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, AngleEnergy{theta_new, E_new}, E_new, w_new, x_new,
+                              z_new, sigv, t);
     } else {
         emit_stay<Lay, PASS>(d, sc, par, k3, cell, theta_new, E_new, w_new, x_new, z_new, k3 ? 0.001f : sigv, sigv, t);
     }

@@ -44,7 +44,7 @@ class Problem(C.Structure):
         ("max_iterations", C.c_int),
         ("prune_coarse", C.c_float), ("prune_fine", C.c_float), ("split_min_weight", C.c_float),
         ("stop_weight_fraction", C.c_float), ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
-        ("lanes", C.c_int), ("density_z", C.c_void_p),
+        ("lanes", C.c_int), ("density_z", C.c_void_p), ("expectation", C.c_int),
     ]
 
 
@@ -282,6 +282,7 @@ class Config:
     seed_iteration_salt: int = 0
     lanes: int = 1          # spots transported together by Transport.batch_run
     density_z: np.ndarray = None   # slab phantom: density per depth row (None: water)
+    expectation: int = 0    # 1: expectation form (redistribution weights instead of MCS/straggling draws)
 
     def production(self):
         """Options of a production run: deterministic rank-ordered seeds salted
@@ -314,7 +315,8 @@ class Config:
                     prune_coarse=self.prune_coarse, prune_fine=self.prune_fine,
                     split_min_weight=self.split_min_weight, stop_weight_fraction=self.stop_weight_fraction,
                     floor_cutoff=self.floor_cutoff, seed_iteration_salt=self.seed_iteration_salt, lanes=self.lanes,
-                    density_z=None if rho is None else rho.ctypes.data, **self.layout)
+                    density_z=None if rho is None else rho.ctypes.data, expectation=self.expectation,
+                    **self.layout)
         return p, (th, E, rho)
 
     def oracle_config(self):
@@ -328,7 +330,7 @@ class Config:
                     grid_E_min=self.E_min, grid_E_max=self.E_max, prune_coarse=self.prune_coarse,
                     prune_fine=self.prune_fine, split_min_weight=self.split_min_weight,
                     stop_weight_fraction=self.stop_weight_fraction, floor_cutoff=self.floor_cutoff,
-                    seed_iteration_salt=self.seed_iteration_salt, **self.layout)
+                    seed_iteration_salt=self.seed_iteration_salt, expectation=self.expectation, **self.layout)
 
     @staticmethod
     def reference_runner(Nx, Nz, dx, dz, N_theta=36, E_fine_on=10.0, E_fine_off=11.0, **kw):
