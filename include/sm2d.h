@@ -406,20 +406,24 @@ int sm2d_k5_conservation_audit_static(
 int sm2d_math_eval(int fn, const float* x, float* y, int n);
 
 /* ---- learned redistribution surrogate of the fine step ----
- * Replaces the per-bin Highland-MCS / Vavilov-straggling / energy-loss
- * redistribution of K3_FineTransport (src/cuda/kernels/k3_finetransport.cu:94-760
- * with src/cuda/device/device_physics.cuh:50-437 and device_lut.cuh:145-168)
- * by a 4 -> 128 -> 128 -> 32 MLP (ReLU, softmax): inputs (E [MeV], theta
- * [rad], step [mm], density [g/cm^3]) as float4 rows, outputs 32 weights
- * (8 theta x 4 E, index theta + 8 E) per row that sum to 1.  The tables of
- * the method itself come from sm2d_redistribution_table: theta bins of width
- * pi/512 centred on the incoming direction, E bins of width ln(2500)/256 in
- * ln E below the incoming energy, end bins holding the tails.  bf16 weights,
- * fp32 accumulation on the tcgen05 tensor cores, trained on the device
- * (softmax cross-entropy, Adam).  Device arrays must be 16-byte aligned.
- * gradients, train, forward and redistribute only enqueue work on the
- * handle's stream; sm2d_mlp_sync waits for it and reports a device wait that
- * gave up (SM2D_ERR_TIMEOUT).
+ * Replaces the closed-form redistribution weights of K3_FineTransport's
+ * expectation form (the per-bin Highland-MCS / Vavilov-straggling /
+ * energy-split re-binning of src/cuda/kernels/k3_finetransport.cu:263-366,
+ * evaluated as expectations in sm2d_redist.h) by a 4 -> 128 -> 128 -> 32 MLP
+ * (ReLU, softmax).  Inputs are float4 rows (s, u, r, cap): s = sigma_theta /
+ * dtheta (the step's MCS angle in angle bins, 0..8), u in [0, 1) (where the
+ * step's mean energy lies between the two energy-bin centres around it),
+ * r = sigma_E / spacing of those centres (straggling in bins, 0..4), cap
+ * (1: the energy window's top is the incoming bin; 0: the second centre above
+ * the mean).  Outputs are 32 weights per row, index t + 8 e: angular
+ * distance t = 0..7 bins (t >= 1 split between both sides) times energy
+ * offset e = 0..3 below the window's top; they sum to 1.  The method's own
+ * tables come from sm2d_redistribution_table (the closed forms on centres of
+ * uniform spacing).  bf16 weights, fp32 accumulation on the tcgen05 tensor
+ * cores, trained on the device (softmax cross-entropy, Adam).  Device arrays
+ * must be 16-byte aligned.  gradients, train, forward and redistribute only
+ * enqueue work on the handle's stream; sm2d_mlp_sync waits for it and reports
+ * a device wait that gave up (SM2D_ERR_TIMEOUT).
  * The reference has no learned part; these entries have no counterpart. */
 typedef struct sm2d_mlp* sm2d_mlp_handle;
 int sm2d_mlp_param_count(void);   /* 22816 fp32: W1[128][16] W2[128][128] W3[32][128] b1 b2 b3 */
@@ -441,14 +445,15 @@ int sm2d_mlp_train(sm2d_mlp_handle m, const float* d_feats, const float* d_targe
                    float lr0, float lr_min, float* d_loss_hist);
 /* surrogate tables of n rows into d_table [n][32] */
 int sm2d_mlp_forward(sm2d_mlp_handle m, const float* d_feats, int n, float* d_table);
-/* n training inputs: E log-uniform on [0.1, 250] MeV, theta on +-0.3 rad,
- * step on [0.05, 2] mm, density on [0.2, 2.0] (hash of seed and row) */
+/* n training inputs (hash of seed and row): s = 8 a^2, u uniform on [0, 1),
+ * r = 4 c^2 (a, c uniform on [0, 1)), cap 0 or 1 */
 int sm2d_redistribution_features(int n, uint32_t seed, float* d_feats, void* stream);
-/* the method's own tables (the handle's R-LUT, the transport's physics) */
+/* the method's own tables (the closed forms of sm2d_redist.h); the work runs
+ * on h's stream */
 int sm2d_redistribution_table(sm2d_handle h, const float* d_feats, int n, float* d_table);
-/* per input region (64 ln E x 8 step x 8 density) the largest absolute weight
- * error of the surrogate rows against the plain rows; optional host copy of
- * the 4096 errors (as float bits) */
+/* per input region (16 sqrt(s/8) x 16 u x 8 sqrt(r/4) x 2 cap) the largest
+ * absolute weight error of the surrogate rows against the plain rows;
+ * optional host copy of the 4096 errors (as float bits) */
 int sm2d_mlp_calibrate(sm2d_mlp_handle m, const float* d_feats, const float* d_plain, const float* d_surrogate, int n,
                        float* host_region_err);
 /* surrogate tables, with the plain table of the handle's physics in the rows
@@ -460,8 +465,8 @@ int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats
 /* wait for the handle's stream; SM2D_ERR_TIMEOUT if a kernel's bounded wait
  * gave up since the last sync (the flag is cleared once reported) */
 int sm2d_mlp_sync(sm2d_mlp_handle m);
-/* table geometry and feature ranges: dtheta, dlnE, ln E_min, ln E_max,
- * theta_max, step_min, step_max, density_min */
+/* feature ranges and calibration regions: s_max, u_max, r_max, cap_max,
+ * regions along s, u, r and cap */
 int sm2d_mlp_geometry(float* out8);
 
 #ifdef __cplusplus

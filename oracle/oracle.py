@@ -291,7 +291,8 @@ class Oracle:
         return dict(zip(keys, s.tolist()))
 
     def redistribution_table(self, feats):
-        """K3's 8 theta x 4 E redistribution of each (E, theta, step, density) row."""
+        """The expectation form's 8 theta x 4 E redistribution of each feature
+        row (s, u, r, cap) (redistribution_table below; the context is not used)."""
         f = np.ascontiguousarray(feats, np.float32).reshape(-1, 4)
         out = np.zeros((f.shape[0], 32), np.float32)
         self.lib.orc_redistribution_table(self.ctx, f.shape[0], _p(f), _p(out))
@@ -330,6 +331,15 @@ def psi_rows(bid, val, L, thresh=1e-12, Kb=KB):
     cells, slots, lidx = np.nonzero((v > thresh) & (b[:, :, None] != EMPTY))
     return dict(cell=cells, slot=slots, bid=b[cells, slots], lidx=lidx,
                 weight=v[cells, slots, lidx])
+
+
+def redistribution_table(feats, fp64=False):
+    """The surrogate's targets: the expectation form's 8 theta x 4 E table of
+    each feature row (s, u, r, cap), on centres of uniform spacing."""
+    f = np.ascontiguousarray(feats, np.float32).reshape(-1, 4)
+    out = np.zeros((f.shape[0], 32), np.float32)
+    _lib(fp64).orc_redistribution_table(None, f.shape[0], _p(f), _p(out))
+    return out
 
 
 def redist_masses(s, Em, sE, cen, fp64=False):

@@ -2102,27 +2102,15 @@ void orc_destroy(orc_ctx* c) {
  * centred on the incoming direction and 4 log-energy bins below the incoming
  * energy, tails folded into the end bins. */
 void orc_redistribution_table(const orc_ctx* c, int n, const float* feats, float* out) {
-    const real dth = RL(3.14159265358979323846) / RL(512.0);
-    const real dlne = RL(7.82404601085629) / RL(256.0);
+    (void)c;
+    const real cap1[4] = {RL(1.0), RL(0.0), RL(-1.0), RL(-2.0)}, cap0[4] = {RL(2.0), RL(1.0), RL(0.0), RL(-1.0)};
     for (int i = 0; i < n; ++i) {
-        const real E = feats[4 * i], ds = feats[4 * i + 2], rho = feats[4 * i + 3];
-        const real Em = E - lut_energy_deposition(&c->lut, E, rho * ds);
-        const real sE = straggling_sigma(E, ds, rho);
-        const real sT = highland(E, rho * ds);
-        real wt[8], we[4], prev = RL(0.0);
-        for (int t = 0; t < 8; ++t) {
-            const real cdf = (t == 7) ? RL(1.0) : gcdf((real)(t - 3) * dth, RL(0.0), sT);
-            wt[t] = cdf - prev;
-            prev = cdf;
-        }
-        prev = RL(0.0);   /* P(E_out > E e^{-(e+1) dlnE}): the weight of bins 0..e */
-        for (int e = 0; e < 4; ++e) {
-            const real g = (e == 3) ? RL(1.0) : RL(1.0) - gcdf(E * r_exp(-(real)(e + 1) * dlne), Em, sE);
-            we[e] = g - prev;
-            prev = g;
-        }
-        for (int e = 0; e < 4; ++e)
-            for (int t = 0; t < 8; ++t) out[32 * (size_t)i + t + 8 * e] = (float)(wt[t] * we[e]);
+        const real s = feats[4 * i], u = feats[4 * i + 1], r = feats[4 * i + 2], cap = feats[4 * i + 3];
+        real Mt[SM2D_RD_NT], Me[SM2D_RD_NE];
+        sm2d_rd_theta(r_max(s, RL(0.0)), Mt);
+        sm2d_rd_energy(u, r_max(r, RL(0.0)), cap > RL(0.5) ? cap1 : cap0, SM2D_RD_NE - 1, Me);
+        for (int e = 0; e < SM2D_RD_NE; ++e)
+            for (int t = 0; t < SM2D_RD_NT; ++t) out[32 * (size_t)i + t + 8 * e] = (float)(Mt[t] * Me[e]);
     }
 }
 

@@ -155,11 +155,12 @@ void orc_get_drop_channels(const orc_ctx* c, double* w9, double* e9);
 void orc_get_scalars(const orc_ctx* c, double* out14);
 void orc_get_fe(const orc_ctx* c, float* A, float* B, float* sigma_total);
 
-/* K3's per-component redistribution over one step (the surrogate's
- * targets): feats [n][4] = (E, theta, step, density), out [n][32] with
- * out[t + 8 e] = w_theta[t] w_E[e]; theta bins of width pi/512 centred on
- * the incoming direction, E bins of width ln(2500)/256 in ln E below the
- * incoming energy, tails in the end bins.  Uses the context's R-LUT. */
+/* The surrogate's targets: the expectation form's redistribution table of
+ * each feature row (s, u, r, cap) -- s = sigma_theta / dtheta, u the mean
+ * energy's position between the centres around it, r = sigma_E / their
+ * spacing, cap 1 when the energy window's top is the incoming bin -- on
+ * centres of uniform spacing: out[t + 8 e] = Mt[t] Me[e] (sm2d_redist.h).
+ * The context is not used. */
 void orc_redistribution_table(const orc_ctx* c, int n, const float* feats, float* out);
 
 /* claim-demand diagnostic: with tracking on, the largest number of distinct

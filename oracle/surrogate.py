@@ -2,7 +2,8 @@
 infrastructure: only tests/, the smoke check and bench.py's checks import it).
 
 The network is 4 -> 128 -> 128 -> 32 with ReLU and a softmax.  Each input row
-(E [MeV], theta [rad], step [mm], density [g/cm^3]) is scaled to [-1, 1] and
+(s, u, r, cap) -- s = sigma_theta / dtheta in [0, 8], u in [0, 1), r =
+sigma_E / centre spacing in [0, 4], cap 0 or 1 -- is scaled to [-1, 1] and
 fed as 16 values: the bf16 rounding of each scaled feature, 128 x its
 rounding remainder (also rounded to bf16), then zeros.  The weights of the
 remainder columns 4-7 are tied to columns 0-3: bf16(W1[:, i]) / 128 (their
@@ -26,8 +27,14 @@ O_B1 = O_W3 + OUT * HID
 O_B2 = O_B1 + HID
 O_B3 = O_B2 + HID
 N_PARAMS = O_B3 + OUT
-LN_EMIN, LN_EMAX = -2.302585093, 5.521460918
-TH_MAX, DS_MIN, DS_MAX, RHO_MIN, RHO_MAX = 0.3, 0.05, 2.0, 0.2, 2.0
+S_MAX, R_MAX = 8.0, 4.0
+
+
+def scaled(feats):
+    """[n][4] feature rows -> the scaled inputs in [-1, 1] (float64)."""
+    f = np.asarray(feats, np.float64).reshape(-1, 4)
+    return np.stack([2.0 * np.clip(f[:, 0], 0.0, S_MAX) / S_MAX - 1.0, 2.0 * f[:, 1] - 1.0,
+                     2.0 * np.clip(f[:, 2], 0.0, R_MAX) / R_MAX - 1.0, 2.0 * f[:, 3] - 1.0], axis=1)
 
 
 def bf16(x):
@@ -65,9 +72,11 @@ def tie_w1_grad(g):
 def features(feats):
     """[n][4] physical inputs -> [n][16] network inputs (bf16 hi/lo pairs)."""
     f = np.asarray(feats, np.float32).reshape(-1, 4)
-    u = np.stack([2.0 * (np.log(np.maximum(f[:, 0].astype(np.float64), 1e-6)) - LN_EMIN) / (LN_EMAX - LN_EMIN) - 1.0,
-                  f[:, 1] / TH_MAX, 2.0 * (f[:, 2] - DS_MIN) / (DS_MAX - DS_MIN) - 1.0,
-                  2.0 * (f[:, 3] - RHO_MIN) / (RHO_MAX - RHO_MIN) - 1.0], axis=1).astype(np.float32)
+    s = np.minimum(np.maximum(f[:, 0], np.float32(0.0)), np.float32(S_MAX))
+    r = np.minimum(np.maximum(f[:, 2], np.float32(0.0)), np.float32(R_MAX))
+    u = np.stack([np.float32(2.0) * s / np.float32(S_MAX) - np.float32(1.0), np.float32(2.0) * f[:, 1] - np.float32(1.0),
+                  np.float32(2.0) * r / np.float32(R_MAX) - np.float32(1.0),
+                  np.float32(2.0) * f[:, 3] - np.float32(1.0)], axis=1).astype(np.float32)
     hi = bf16(u)
     lo = bf16((u - hi) * np.float32(128.0))
     x = np.zeros((f.shape[0], IN), np.float32)
@@ -116,11 +125,8 @@ def loss_exact(params, feats, target):
     """The same loss without any bf16 rounding (float64 throughout), for finite differences."""
     W1, W2, W3, b1, b2, b3 = [np.asarray(a, np.float64) for a in unpack(params)]
     f = np.asarray(feats, np.float64).reshape(-1, 4)
-    u = np.stack([2.0 * (np.log(f[:, 0]) - LN_EMIN) / (LN_EMAX - LN_EMIN) - 1.0, f[:, 1] / TH_MAX,
-                  2.0 * (f[:, 2] - DS_MIN) / (DS_MAX - DS_MIN) - 1.0,
-                  2.0 * (f[:, 3] - RHO_MIN) / (RHO_MAX - RHO_MIN) - 1.0], axis=1)
     x = np.zeros((f.shape[0], IN))
-    x[:, :4] = u
+    x[:, :4] = scaled(f)
     h1 = np.maximum(x @ W1.T + b1, 0.0)
     h2 = np.maximum(h1 @ W2.T + b2, 0.0)
     z = h2 @ W3.T + b3
@@ -135,11 +141,8 @@ def grad_exact(params, feats, target):
     f = np.asarray(feats, np.float64).reshape(-1, 4)
     y = np.asarray(target, np.float64)
     n = f.shape[0]
-    u = np.stack([2.0 * (np.log(f[:, 0]) - LN_EMIN) / (LN_EMAX - LN_EMIN) - 1.0, f[:, 1] / TH_MAX,
-                  2.0 * (f[:, 2] - DS_MIN) / (DS_MAX - DS_MIN) - 1.0,
-                  2.0 * (f[:, 3] - RHO_MIN) / (RHO_MAX - RHO_MIN) - 1.0], axis=1)
     x = np.zeros((n, IN))
-    x[:, :4] = u
+    x[:, :4] = scaled(f)
     h1 = np.maximum(x @ W1.T + b1, 0.0)
     h2 = np.maximum(h1 @ W2.T + b2, 0.0)
     z = h2 @ W3.T + b3

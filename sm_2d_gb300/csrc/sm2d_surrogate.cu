@@ -35,6 +35,7 @@
 
 #include "sm2d.h"
 #include "sm2d_common.cuh"
+#include "sm2d_redist.h"
 
 namespace sm2d {
 
@@ -60,15 +61,16 @@ constexpr int iW1 = 0, iW2 = iW1 + kHid * kIn * 2, iW2T = iW2 + kHid * kHid * 2,
 // columns.  The training kernel's inputs hold zeros there and it adds the
 // fp32 biases itself.
 constexpr int kBiasCol = 8;
-// table geometry: theta bins of the 512-bin grid over [-pi/2, pi/2], energy bins
-// of the 256-bin log grid over [0.1, 250] MeV
-constexpr float kDth = 3.14159265358979323846f / 512.0f;
-constexpr float kDlnE = 7.82404601085629f / 256.0f;   // ln(2500) / 256
-// feature ranges of the training set
-constexpr float kLnEmin = -2.302585093f, kLnEmax = 5.521460918f;   // ln 0.1, ln 250
-constexpr float kThMax = 0.3f, kDsMin = 0.05f, kDsMax = 2.0f, kRhoMin = 0.2f, kRhoMax = 2.0f;
-// calibration regions: ln E x step x density
-constexpr int kRegE = 64, kRegS = 8, kRegR = 8, kRegions = kRegE * kRegS * kRegR;
+// Input space: the expectation form's redistribution of one fine-step
+// component depends on its physics only through four numbers (features
+// f = (s, u, r, cap)): s = sigma_theta / dtheta, the MCS angle in angle bins;
+// u in [0, 1), where the step's mean energy lies between the two energy-bin
+// centres around it (spacing D); r = sigma_E / D, the straggling in bins;
+// cap = 1 when the energy window's top is the incoming bin (the mean lies in
+// the first interval below it), 0 when it is the second centre above the mean.
+constexpr float kSMax = 8.0f, kRMax = 4.0f;
+// calibration regions: sqrt(s / 8) x u x sqrt(r / 4) x cap
+constexpr int kRegS = 16, kRegU = 16, kRegR = 8, kRegC = 2, kRegions = kRegS * kRegU * kRegR * kRegC;
 constexpr long long kSpinCycles = 2000000000LL;   // about one second at the SM clock
 constexpr int kMaxRows = 1 << 30;                  // rows per call (tile indices stay within int)
 
@@ -221,16 +223,14 @@ __device__ __forceinline__ float row_sum(const unsigned char* base, int r, int K
 }
 
 // ------------------------------------------------------------------ features and the plain table
-// Network inputs of one sample (E [MeV], theta [rad], step [mm], density
-// [g/cm^3]): each scaled to [-1, 1] and written as a bf16 pair (hi, 128 x
-// the rounding remainder).  The W1 image multiplies the remainder column of
-// input i by bf16(W1[o][i]) / 128 (exact: a power of two), so the first GEMM
-// forms bf16(W1[o][i]) (hi + remainder) and sees the fp32 input to about 16
-// bits.
+// Network inputs of one sample: each feature scaled to [-1, 1] and written as
+// a bf16 pair (hi, 128 x the rounding remainder).  The W1 image multiplies
+// the remainder column of input i by bf16(W1[o][i]) / 128 (exact: a power of
+// two), so the first GEMM forms bf16(W1[o][i]) (hi + remainder) and sees the
+// fp32 input to about 16 bits.
 __host__ __device__ inline void feature_row(const float* f, float* x16) {
-    const float u[4] = {2.0f * (sm2d_logf(fmaxf(f[0], 1e-6f)) - kLnEmin) / (kLnEmax - kLnEmin) - 1.0f,
-                        f[1] / kThMax, 2.0f * (f[2] - kDsMin) / (kDsMax - kDsMin) - 1.0f,
-                        2.0f * (f[3] - kRhoMin) / (kRhoMax - kRhoMin) - 1.0f};
+    const float u[4] = {2.0f * fminf(fmaxf(f[0], 0.0f), kSMax) / kSMax - 1.0f, 2.0f * f[1] - 1.0f,
+                        2.0f * fminf(fmaxf(f[2], 0.0f), kRMax) / kRMax - 1.0f, 2.0f * f[3] - 1.0f};
     for (int i = 0; i < 4; ++i) {
 #ifdef __CUDA_ARCH__
         const float hi = __bfloat162float(__float2bfloat16_rn(u[i]));
@@ -243,43 +243,25 @@ __host__ __device__ inline void feature_row(const float* f, float* x16) {
     for (int i = 8; i < kIn; ++i) x16[i] = 0.0f;
 }
 __device__ __forceinline__ int region_of(const float* f) {
-    const float a = (sm2d_logf(fmaxf(f[0], 1e-6f)) - kLnEmin) / (kLnEmax - kLnEmin);
-    const float b = (f[2] - kDsMin) / (kDsMax - kDsMin);
-    const float c = (f[3] - kRhoMin) / (kRhoMax - kRhoMin);
-    const int ia = min(kRegE - 1, max(0, (int)(a * kRegE)));
-    const int ib = min(kRegS - 1, max(0, (int)(b * kRegS)));
-    const int ic = min(kRegR - 1, max(0, (int)(c * kRegR)));
-    return (ia * kRegS + ib) * kRegR + ic;
+    const int ia = min(kRegS - 1, max(0, (int)(sqrtf(fmaxf(f[0], 0.0f) / kSMax) * kRegS)));
+    const int ib = min(kRegU - 1, max(0, (int)(f[1] * kRegU)));
+    const int ic = min(kRegR - 1, max(0, (int)(sqrtf(fmaxf(f[2], 0.0f) / kRMax) * kRegR)));
+    const int id = f[3] > 0.5f ? 1 : 0;
+    return ((ia * kRegU + ib) * kRegR + ic) * kRegC + id;
 }
 
-// The K3 redistribution of one component (sm2d_device.cuh arithmetic of the
-// fine step): mean energy loss over the water-equivalent path rho ds from the
-// R-LUT, Vavilov/Bohr straggling sigma, Highland angle of the thickness rho
-// ds.  theta: 8 bins of the grid's width centred on the incoming direction,
-// tails folded into the end bins.  E: 4 log bins of the grid's width below
-// the incoming energy (bin 0 holds everything above E e^-dlnE, bin 3
-// everything below E e^-3dlnE).  out[t + 8 e] = w_theta[t] w_E[e].
-__device__ void plain_table(const Dev& d, const float* f, float* out) {
-    const float E = f[0], ds = f[2], rho = f[3];
-    const float RE = lut_range(d, E);
-    const float Em = E - lut_energy_loss(d, E, RE, rho * ds);
-    const float sE = straggling_sigma(E, ds, rho);
-    const float sT = highland(E, rho * ds);
-    float wt[8], we[4];
-    float prev = 0.0f;
-    for (int t = 0; t < 8; ++t) {
-        const float c = (t == 7) ? 1.0f : gauss_cdf((float)(t - 3) * kDth, 0.0f, sT);
-        wt[t] = c - prev;
-        prev = c;
-    }
-    prev = 0.0f;   // P(E_out > E e^{-(e+1) dlnE}): the weight of bins 0..e
-    for (int e = 0; e < 4; ++e) {
-        const float g = (e == 3) ? 1.0f : 1.0f - gauss_cdf(E * sm2d_expf(-(float)(e + 1) * kDlnE), Em, sE);
-        we[e] = g - prev;
-        prev = g;
-    }
-    for (int e = 0; e < 4; ++e)
-        for (int t = 0; t < 8; ++t) out[t + 8 * e] = wt[t] * we[e];
+// The expectation form's redistribution of one component (sm2d_redist.h),
+// out[t + 8 e] = Mt[t] Me[e], on centres of uniform spacing: in units of the
+// spacing, the mean energy u lies between centres 0 and 1; the window is
+// (1, 0, -1, -2) when its top is capped at the incoming bin, (2, 1, 0, -1)
+// otherwise.  The transport evaluates the same masses on the grid's centres.
+__host__ __device__ inline void plain_table(const float* f, float* out) {
+    float Mt[SM2D_RD_NT], Me[SM2D_RD_NE];
+    const float cap1[4] = {1.0f, 0.0f, -1.0f, -2.0f}, cap0[4] = {2.0f, 1.0f, 0.0f, -1.0f};
+    sm2d_rd_theta(fmaxf(f[0], 0.0f), Mt);
+    sm2d_rd_energy(f[1], fmaxf(f[2], 0.0f), f[3] > 0.5f ? cap1 : cap0, SM2D_RD_NE - 1, Me);
+    for (int e = 0; e < SM2D_RD_NE; ++e)
+        for (int t = 0; t < SM2D_RD_NT; ++t) out[t + 8 * e] = Mt[t] * Me[e];
 }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
@@ -289,21 +271,20 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
 __device__ __forceinline__ float unit(uint32_t seed, uint32_t i, uint32_t k) {
     return ((float)(hash32(seed * 0x9E3779B9u ^ hash32(4u * i + k)) >> 8) + 0.5f) * (1.0f / 16777216.0f);
 }
-// training-set inputs: E log-uniform on [0.1, 250], theta uniform on +-0.3,
-// step uniform on [0.05, 2] mm, density uniform on [0.2, 2.0]
+// training-set inputs: s = 8 a^2, u uniform, r = 4 c^2 (more samples at
+// the small spreads that dominate), cap 0 or 1
 __global__ void k_features(int n, uint32_t seed, float4* f) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float a = unit(seed, i, 0), b = unit(seed, i, 1), c = unit(seed, i, 2), e = unit(seed, i, 3);
-        f[i] = make_float4(sm2d_expf(kLnEmin + a * (kLnEmax - kLnEmin)), kThMax * (2.0f * b - 1.0f),
-                           kDsMin + c * (kDsMax - kDsMin), kRhoMin + e * (kRhoMax - kRhoMin));
+        f[i] = make_float4(kSMax * a * a, b, kRMax * c * c, e < 0.5f ? 0.0f : 1.0f);
     }
 }
-__global__ void k_plain(Dev d, int n, const float4* f, float4* out) {
+__global__ void k_plain(int n, const float4* f, float4* out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 q = f[i];
         const float fi[4] = {q.x, q.y, q.z, q.w};
         float t[kOut];
-        plain_table(d, fi, t);
+        plain_table(fi, t);
         for (int j = 0; j < kOut / 4; ++j) out[(size_t)i * 8 + j] = make_float4(t[4 * j], t[4 * j + 1], t[4 * j + 2], t[4 * j + 3]);
     }
 }
@@ -792,7 +773,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
                     if (k == am) z[k] = 1.0f - t;   // the row sums to 1: the component's weight is conserved
                 int fb = 0;
                 if (a.err_bits && __int_as_float(a.err_bits[region_of(f)]) > a.tol) {
-                    plain_table(a.dev, f, z);
+                    plain_table(f, z);
                     fb = 1;
                 }
                 if (a.fallback) a.fallback[i] = fb;
@@ -1099,7 +1080,8 @@ int sm2d_redistribution_table(sm2d_handle h, const float* d_feats, int n, float*
     cudaStream_t s;
     int rc = handle_dev(h, &d, &s);
     if (rc) return rc;
-    k_plain<<<std::min((n + 255) / 256, 8192), 256, 0, s>>>(d, n, reinterpret_cast<const float4*>(d_feats),
+    (void)d;
+    k_plain<<<std::min((n + 255) / 256, 8192), 256, 0, s>>>(n, reinterpret_cast<const float4*>(d_feats),
                                                            reinterpret_cast<float4*>(d_table));
     CK(cudaGetLastError());
     return 0;
@@ -1156,7 +1138,7 @@ int sm2d_mlp_sync(sm2d_mlp_handle m) {
 
 int sm2d_mlp_geometry(float* out8) {
     if (!out8) return fail(SM2D_ERR_ARG, "null argument");
-    const float g[8] = {kDth, kDlnE, kLnEmin, kLnEmax, kThMax, kDsMin, kDsMax, kRhoMin};
+    const float g[8] = {kSMax, 1.0f, kRMax, 1.0f, (float)kRegS, (float)kRegU, (float)kRegR, (float)kRegC};
     memcpy(out8, g, sizeof g);
     return 0;
 }

@@ -1,14 +1,17 @@
 """Learned redistribution surrogate of the fine transport step (host side).
 
-``Surrogate`` owns one network (sm2d_mlp_* in libsm2d.so) and one transport
-handle on the 256-bin log energy grid (0.1-250 MeV) whose R-LUT and per-bin
-physics generate the method's own tables (sm2d_redistribution_table): the
-8 theta x 4 E redistribution of a component of energy E, angle theta, over a
-step of the given length in a medium of the given density, the quantity
-K3_FineTransport (src/cuda/kernels/k3_finetransport.cu:94-760) evaluates per
-bin from device_physics.cuh and device_lut.cuh.  Training, inference and the
-tables all run on the GPU; torch provides the device arrays.  There is no CPU
-path: without the library or a GPU every call raises.
+``Surrogate`` owns one network (sm2d_mlp_* in libsm2d.so) and one small
+transport handle whose stream runs its work.  The network predicts the
+expectation form's redistribution weights of one fine-step component -- the
+8 theta x 4 E table of the expected Highland-MCS / Vavilov-straggling /
+energy-split re-binning that K3_FineTransport (src/cuda/kernels/
+k3_finetransport.cu:263-366) samples once per bin -- from four numbers:
+s = sigma_theta / dtheta, u (the mean energy's position between the energy
+centres around it), r = sigma_E / their spacing, and cap (the energy window's
+top is the incoming bin).  sm2d_redistribution_table evaluates the method's
+own closed forms.  Training, inference and the tables run on the GPU; torch
+provides the device arrays.  There is no CPU path: without the library or a
+GPU every call raises.
 """
 from __future__ import annotations
 
@@ -60,8 +63,8 @@ class Surrogate:
         if not torch.cuda.is_available():
             raise RuntimeError("the redistribution surrogate needs a CUDA device")
         self.L = _lib()
-        # the physics source: a small transport problem on the 256-bin log grid
-        self.t = Transport(Config.log_grid(4, 4, 0.5, 0.5, N_E=256, E_min=0.1, E_max=250.0, N_theta=512))
+        # a small transport handle: its stream runs the surrogate's work
+        self.t = Transport(Config.reference_runner(4, 4, 0.5, 0.5))
         self.sms = torch.cuda.get_device_properties(0).multi_processor_count
         self.batch = 128 * self.sms   # one 128-sample tile per SM
         h = C.c_void_p()
@@ -90,7 +93,7 @@ class Surrogate:
         check(self.L.sm2d_mlp_sync(self.m))
 
     def features(self, n: int, seed: int):
-        """n inputs (E, theta, step, density) of the training distribution, [n][4] on the device."""
+        """n inputs (s, u, r, cap) of the training distribution, [n][4] on the device."""
         f = self.torch.empty((n, 4), dtype=self.torch.float32, device="cuda")
         self._sync()
         check(self.L.sm2d_redistribution_features(n, seed, _ptr(f), self.t.stream()))
@@ -166,8 +169,8 @@ class Surrogate:
     def geometry():
         g = np.zeros(8, np.float32)
         check(_lib().sm2d_mlp_geometry(g.ctypes.data_as(C.c_void_p)))
-        return dict(zip(["dtheta", "dlnE", "lnE_min", "lnE_max", "theta_max", "step_min", "step_max",
-                         "density_min"], g.tolist()))
+        return dict(zip(["s_max", "u_max", "r_max", "cap_max", "regions_s", "regions_u", "regions_r",
+                         "regions_cap"], g.tolist()))
 
 
 def main(argv=None):

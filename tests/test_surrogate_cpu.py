@@ -1,6 +1,7 @@
 """CPU checks of the redistribution surrogate's oracle: the method's tables
-(C restatement of K3's per-bin physics) and the network's float64/bf16
-restatement, its gradient against finite differences, and the host helpers."""
+(the expectation form's closed forms, sm2d_redist.h, restated in the C
+oracle) and the network's float64/bf16 restatement, its gradient against
+finite differences, and the host helpers."""
 import numpy as np
 import pytest
 
@@ -9,53 +10,48 @@ from oracle import oracle as orc
 from oracle import surrogate as so
 
 
-def table_oracle():
-    cfg = sm.Config.log_grid(4, 4, 0.5, 0.5, N_E=256, E_min=0.1, E_max=250.0, N_theta=512)
-    return orc.Oracle(cfg.oracle_config(), cfg.theta_edges, cfg.E_edges)
-
-
 def sample_features(n, seed):
+    """(s, u, r, cap) rows of the training distribution."""
     r = np.random.default_rng(seed)
-    return np.stack([np.exp(r.uniform(np.log(0.1), np.log(250.0), n)), r.uniform(-0.3, 0.3, n),
-                     r.uniform(0.05, 2.0, n), r.uniform(0.2, 2.0, n)], axis=1).astype(np.float32)
+    return np.stack([8.0 * r.uniform(0, 1, n) ** 2, r.uniform(0, 1, n), 4.0 * r.uniform(0, 1, n) ** 2,
+                     (r.uniform(0, 1, n) < 0.5).astype(np.float64)], axis=1).astype(np.float32)
 
 
 def test_tables_are_distributions():
-    o = table_oracle()
-    t = o.redistribution_table(sample_features(4000, 1))
+    t = orc.redistribution_table(sample_features(4000, 1))
     assert t.shape == (4000, 32)
     assert (t >= 0).all()
     np.testing.assert_allclose(t.sum(axis=1), 1.0, atol=2e-6)
 
 
-def test_table_physics_limits():
-    o = table_oracle()
-    # 150 MeV over 0.1 mm of water: energy loss far below a bin, so all weight in
-    # E bin 0; sigma_theta well below a bin, so the two bins around the incoming
-    # direction (3 and 4) share it equally
-    t = o.redistribution_table(np.array([[150.0, 0.1, 0.1, 1.0]], np.float32))[0].reshape(4, 8)
-    assert t[1:].sum() < 1e-6
-    assert abs(t[0, 3] - 0.5) < 1e-3 and abs(t[0, 4] - 0.5) < 1e-3
-    # 1 MeV over 2 mm: the mean energy falls to the LUT floor (R(1 MeV) is about
-    # 0.02 mm), so most weight is in the lowest E bin; the straggling sigma of
-    # the step (Bohr, several MeV at this beta) puts the rest in the top bin,
-    # and the angle spreads into the end bins
-    t = o.redistribution_table(np.array([[1.0, 0.0, 2.0, 1.0]], np.float32))[0].reshape(4, 8)
-    assert t[3].sum() > 0.5 and t[1:3].sum() < 0.02
-    assert t[3, 0] > 0.05 and t[3, 7] > 0.05
-    # the incoming angle does not enter the relative bins
-    a = o.redistribution_table(np.array([[20.0, -0.2, 1.0, 1.5], [20.0, 0.25, 1.0, 1.5]], np.float32))
-    np.testing.assert_array_equal(a[0], a[1])
+def test_table_limits():
+    # no spreads: the angle stays, the energy splits between the centres
+    # around the mean (window capped at the incoming bin: centres 1, 0, -1, -2)
+    t = orc.redistribution_table(np.array([[0.0, 0.5, 0.0, 1.0]], np.float32))[0].reshape(4, 8)
+    assert t[:, 1:].sum() == 0.0
+    np.testing.assert_allclose(t[:, 0], [0.5, 0.5, 0.0, 0.0], atol=1e-7)
+    # window not capped (centres 2, 1, 0, -1): u = 0.25 gives 0.25 to e = 1
+    t = orc.redistribution_table(np.array([[0.0, 0.25, 0.0, 0.0]], np.float32))[0].reshape(4, 8)
+    np.testing.assert_allclose(t[:, 0], [0.0, 0.25, 0.75, 0.0], atol=1e-7)
+    # the energy split keeps the mean; straggling spreads it
+    for u, r in [(0.3, 0.2), (0.7, 0.5)]:
+        t = orc.redistribution_table(np.array([[1.0, u, r, 0.0]], np.float32), fp64=True)[0].reshape(4, 8)
+        me = t.sum(axis=1)
+        assert abs((me * np.array([2.0, 1.0, 0.0, -1.0])).sum() - u) < 5e-3
+    # a small angle spread sends s^2 to the neighbours, a large one spreads far
+    t = orc.redistribution_table(np.array([[0.1, 0.5, 0.0, 1.0]], np.float32), fp64=True)[0].reshape(4, 8)
+    assert abs(t[:, 1].sum() - 0.01) < 1e-6
+    t = orc.redistribution_table(np.array([[4.0, 0.5, 0.0, 1.0]], np.float32))[0].reshape(4, 8)
+    assert t[:, 4:].sum() > 0.3
 
 
 def test_fp32_table_matches_fp64_method():
-    cfg = sm.Config.log_grid(4, 4, 0.5, 0.5, N_E=256, E_min=0.1, E_max=250.0, N_theta=512)
-    o32 = orc.Oracle(cfg.oracle_config(), cfg.theta_edges, cfg.E_edges)
-    o64 = orc.Oracle(cfg.oracle_config(), cfg.theta_edges, cfg.E_edges, fp64=True)
     f = sample_features(3000, 2)
-    d = np.abs(o32.redistribution_table(f) - o64.redistribution_table(f))
-    assert d.max() < 2e-3, d.max()
-    assert d.mean() < 1e-5
+    d = np.abs(orc.redistribution_table(f) - orc.redistribution_table(f, fp64=True))
+    # the angular masses are differences of normal CDF values: in float they
+    # cancel to a few 1e-5 absolute (1e-6 on average) at the widest spreads
+    assert d.max() < 5e-5
+    assert d.mean() < 1e-6
 
 
 def test_gradient_matches_finite_differences():
@@ -78,10 +74,8 @@ def test_gradient_matches_finite_differences():
 
 
 def test_bf16_restatement_close_to_exact_gradient():
-    r = np.random.default_rng(5)
-    o = table_oracle()
     f = sample_features(512, 6)
-    y = o.redistribution_table(f)
+    y = orc.redistribution_table(f)
     p = so.init_params()
     loss, g = so.loss_and_grad(p, f, y)
     ge = so.grad_exact(p, f, y)
@@ -100,9 +94,8 @@ def test_bf16_rounding_is_nearest_even():
 
 def test_surrogate_geometry_exported():
     g = sm.Surrogate.geometry()
-    assert abs(g["dtheta"] - np.pi / 512) < 1e-7
-    assert abs(g["dlnE"] - np.log(2500.0) / 256) < 1e-7
-    assert g["step_min"] == pytest.approx(0.05) and g["step_max"] == pytest.approx(2.0)
+    assert g["s_max"] == 8.0 and g["r_max"] == 4.0 and g["u_max"] == 1.0 and g["cap_max"] == 1.0
+    assert g["regions_s"] * g["regions_u"] * g["regions_r"] * g["regions_cap"] == 4096
 
 
 def test_adam_restatement_first_step():
@@ -135,9 +128,7 @@ def test_bf16_input_pairs_carry_sixteen_bits():
     # together they restore u to about 2^-16 of its range
     f = sample_features(20000, 8)
     x = so.features(f)
-    u = np.stack([2.0 * (np.log(f[:, 0].astype(np.float64)) - so.LN_EMIN) / (so.LN_EMAX - so.LN_EMIN) - 1.0,
-                  f[:, 1] / so.TH_MAX, 2.0 * (f[:, 2] - so.DS_MIN) / (so.DS_MAX - so.DS_MIN) - 1.0,
-                  2.0 * (f[:, 3] - so.RHO_MIN) / (so.RHO_MAX - so.RHO_MIN) - 1.0], axis=1)
+    u = so.scaled(f)
     rebuilt = x[:, :4].astype(np.float64) + x[:, 4:8].astype(np.float64) / 128.0
     assert np.abs(rebuilt - u).max() < 2.0 ** -15
     assert np.abs(x[:, :4] - u).max() > 2.0 ** -10     # bf16 alone would lose them
@@ -154,19 +145,17 @@ def test_first_layer_sees_inputs_to_sixteen_bits():
     W1 = so.unpack(p)[0]
     assert (W1[:, 4:8] == 0).all()          # the tied parameters stay zero
     f = sample_features(4000, 10)
-    u = np.stack([2.0 * (np.log(f[:, 0].astype(np.float64)) - so.LN_EMIN) / (so.LN_EMAX - so.LN_EMIN) - 1.0,
-                  f[:, 1] / so.TH_MAX, 2.0 * (f[:, 2] - so.DS_MIN) / (so.DS_MAX - so.DS_MIN) - 1.0,
-                  2.0 * (f[:, 3] - so.RHO_MIN) / (so.RHO_MAX - so.RHO_MIN) - 1.0], axis=1)
+    u = so.scaled(f)
     wimg = so.w1_image(W1).astype(np.float64)
     pre = so.features(f).astype(np.float64) @ wimg.T
     exact = u @ so.bf16(W1[:, :4]).astype(np.float64).T
     scale = np.abs(so.bf16(W1[:, :4])).sum(axis=1).max()
     assert np.abs(pre - exact).max() < scale * 2.0 ** -15
-    # a theta moved by 1/4 of a bf16 step of its scaled value
+    # u moved by 1/4 of a bf16 step of its scaled value 2 u - 1
     g = f.copy()
-    g[:, 1] = (f[:, 1].astype(np.float64) + 0.25 * 2.0 ** -9 * so.TH_MAX).astype(np.float32)
+    g[:, 1] = (f[:, 1].astype(np.float64) + 0.25 * 2.0 ** -10).astype(np.float32)
     d = so.features(g).astype(np.float64) @ wimg.T - pre
-    step = (g[:, 1].astype(np.float64) - f[:, 1]) / so.TH_MAX
+    step = 2.0 * (g[:, 1].astype(np.float64) - f[:, 1])
     want = step[:, None] * so.bf16(W1[:, 1]).astype(np.float64)[None, :]
     assert np.abs(d - want).max() < scale * 2.0 ** -14
     del r
