@@ -219,10 +219,13 @@ def accuracy_leg(grid, workload, spots, idx, dose, results, n_threads, method="s
     return out
 
 
-def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", accuracy=False):
+def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", accuracy=False, surrogate=None,
+              tol=0.005):
     """spots/s of a plan of n_spots on an engine of `lanes` lanes (0: from free
     memory), device-resident, CUDA events on the library stream; with
-    accuracy, also the dose errors of the accuracy sample (accuracy_leg)."""
+    accuracy, also the dose errors of the accuracy sample (accuracy_leg);
+    with a calibrated surrogate (expectation form), K3's redistribution
+    weights come from the network with the per-row fallback at tol."""
     import torch
     import sm_2d_gb300 as sm
     from sm_2d_gb300.runtime import Beam
@@ -232,6 +235,8 @@ def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", a
     beams = [Beam(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
                   b["n_samples"], b["seed"]) for b in spots]
     with sm.Transport(cfg) as t:
+        if surrogate is not None:
+            t.set_surrogate(surrogate, tol=tol)
         ext = torch.cuda.ExternalStream(t.stream())
         t.plan_load(beams, MAX_IT, dose=accuracy)
         for _ in range(warmup):
@@ -249,11 +254,18 @@ def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", a
         passes, _, bins = t.plan_stats()
         sc = t.scalars()
         lanes_used = t.lanes
+        sst = t.surrogate_stats() if surrogate is not None else None
     out = {"value": n_spots * steps / (sum(ms) / 1e3), "unit": "spots/s", "lanes": lanes_used, "spots": n_spots,
            "ms_per_step": float(np.mean(ms)), "passes_per_step": passes, "bins_per_step": bins,
            "iterations_per_spot": float(np.mean([r["iterations"] for r in rs])),
            "unfinished_spots": sum(1 for r in rs if not r["finished"]),
            "claim_table_overflows": sc["claim_table_overflows"]}
+    if sst is not None:
+        # rows of the last plan (the stats count since the plan's start)
+        out["surrogate_rows_per_step"] = sst["rows"]
+        out["fallback_share"] = sst["fallback_rows"] / max(sst["rows"], 1)
+        out["rows_beyond_capacity"] = sst["overflow_bins"]
+        out["fallback_tol"] = tol
     if accuracy:
         out["accuracy"] = accuracy_leg(grid, workload, spots, plan_sample(workload, n_spots), dose, rs,
                                        os.cpu_count() or 1, method)
@@ -406,7 +418,7 @@ def run_reference_arm(args):
 
 
 # ---------------------------------------------------------------- GPU arm
-def surrogate_leg(n_train=1 << 21, steps=10000, n_eval=1 << 22, tol=0.01):
+def surrogate_leg(n_train=1 << 21, steps=10000, n_eval=1 << 22, tol=0.005):
     """The learned redistribution surrogate next to the method it replaces.
 
     Trains the network on the method's own tables (K3 physics on the device),
@@ -485,8 +497,7 @@ def surrogate_leg(n_train=1 << 21, steps=10000, n_eval=1 << 22, tol=0.01):
                      "frac": achieved / peak, "peak_source": src, "kernel": "k_infer",
                      "avg_launch_ms": t_net, "algorithmic_flops_per_launch": flops},
     }
-    s.close()
-    return res
+    return res, s
 
 
 def run_gpu_arm(args):
@@ -652,7 +663,19 @@ def run_gpu_arm(args):
 
     surrogate = None
     if rank == 0 and not args.no_surrogate and not SMALL:
-        surrogate = surrogate_leg()
+        surrogate, net = surrogate_leg()
+        if args.workload == "plan512" and not args.no_context:
+            # surrogate + batched: the plan in the expectation form with K3's
+            # redistribution weights from the network (fallback at 0.5 %)
+            st = plan_rate(args.grid, args.workload, n, 0, 2, 1, "expect", accuracy=True, surrogate=net, tol=0.005)
+            st["method"] = ("expectation form with the learned surrogate: K3 bins whose energy window has uniformly "
+                            "spaced centres take their 8 theta x 4 E weights from the network; rows whose calibrated "
+                            "region error exceeds the tolerance keep the closed forms")
+            st["over_plain"] = st["value"] / value
+            if "expectation" in extra:
+                st["over_expectation_form"] = st["value"] / extra["expectation"]["value"]
+            surrogate["transport"] = st
+        net.close()
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "spots/s", "n_gpus": world, "steps": args.steps,

@@ -468,6 +468,26 @@ int sm2d_mlp_sync(sm2d_mlp_handle m);
 /* feature ranges and calibration regions: s_max, u_max, r_max, cap_max,
  * regions along s, u, r and cap */
 int sm2d_mlp_geometry(float* out8);
+/* The surrogate inside the transport of an expectation-form handle: every K3
+ * bin that stays above the cutoff and whose energy window has four centres
+ * of uniform spacing takes its children's weights from network m instead of
+ * the closed forms of k3_finetransport.cu:263-366 (sm2d_redist.h).  The
+ * claim pass writes the bin's feature row and defers its claims; the network
+ * runs on the transport's stream inside the device loop; the rows' claims and
+ * the deposit pass then use the row's table (network weights below 2^-12 are
+ * zero and the rest sum to 1, so the weight is conserved; the energy the
+ * table does not represent goes to the deposit).  A row whose calibrated
+ * region error (sm2d_mlp_calibrate) exceeds tol falls back to the closed
+ * forms.  max_rows: surrogate rows per pass (0: min(bin list, 4 Mi)); bins
+ * beyond it keep the closed forms.  method_tables = 1 gives every row the
+ * plain table of its features instead of the network's (the table path with
+ * the method's own numbers; no calibration needed).  m = NULL detaches.  m
+ * must stay alive while attached and run on the device of h.  A bounded wait
+ * of the network that gives up sets m's error flag (sm2d_mlp_sync). */
+int sm2d_set_surrogate(sm2d_handle h, sm2d_mlp_handle m, float tol, int max_rows, int method_tables);
+/* since the last reset: [0] surrogate rows served, [1] rows that fell back
+ * to the closed forms, [2] K3 bins beyond max_rows */
+int sm2d_surrogate_stats(sm2d_handle h, double* out3);
 
 #ifdef __cplusplus
 }

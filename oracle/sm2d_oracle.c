@@ -778,6 +778,8 @@ typedef struct kids {
     int c, j, emax;
     real Mt[SM2D_RD_NT], Me[SM2D_RD_NE];
     real Erep;
+    int tab;                               /* 1: the weights are the table T */
+    real T[SM2D_RD_NT * SM2D_RD_NE];       /* T[t + 8 e] */
 } kids;
 /* energy window: its top is the second centre above the step's mean energy
  * Em, at most the incoming bin jin */
@@ -788,12 +790,86 @@ static void make_kids(const orc_ctx* c, int tb, int jin, real s, real Em, real s
     int Eb = up + 1 < jin ? up + 1 : jin;
     k->c = tb;
     k->j = Eb;
+    k->tab = 0;
     k->emax = Eb < SM2D_RD_NE - 1 ? Eb : SM2D_RD_NE - 1;
     real cen[SM2D_RD_NE];
     for (int e = 0; e <= k->emax; ++e) cen[e] = e_center(c, Eb - e);
     sm2d_rd_theta(s, k->Mt);
     sm2d_rd_energy(Em, sE, cen, k->emax, k->Me);
     k->Erep = sm2d_rd_fold(w, (real)c->cfg.split_min_weight, k->Mt, k->Me, cen, k->emax);
+}
+/* The surrogate's features of a component (the GPU's surr_features): s =
+ * sigma_theta / dtheta; u, where Em lies between the centres around it; r =
+ * sigma_E / their spacing; cap = 1 when the window's top is the incoming
+ * bin.  0: outside the table's domain (a window of fewer than four centres or
+ * of uneven spacing), which keeps the closed forms. */
+static int surr_features(const orc_ctx* c, int jin, real s, real Em, real sE, real* f) {
+    real Ec = r_max(c->E_edges[0], r_min(Em, c->E_edges[c->N_E]));
+    int b = find_bin_edges(c->E_edges, c->N_E, Ec);
+    int up = Ec >= e_center(c, b) ? b + 1 : b;
+    int jt = up + 1 < jin ? up + 1 : jin;
+    if (up < 1 || up > c->N_E - 1 || jt < SM2D_RD_NE - 1) return 0;
+    real ch = e_center(c, up), cl = e_center(c, up - 1), D = ch - cl;
+    for (int e = 0; e < SM2D_RD_NE - 1; ++e) {
+        real de = e_center(c, jt - e) - e_center(c, jt - e - 1);
+        if (r_fabs(de - D) > RL(1e-3) * D) return 0;
+    }
+    f[0] = s;
+    f[1] = r_min(r_max((Em - cl) / D, RL(0.0)), (real)0.99999994f);
+    f[2] = sE / D;
+    f[3] = jt == up ? RL(1.0) : RL(0.0);
+    return 1;
+}
+/* the plain table of a feature row (the GPU's plain_table) */
+static void plain_table(const real* f, real* out) {
+    const real cap1[4] = {RL(1.0), RL(0.0), RL(-1.0), RL(-2.0)}, cap0[4] = {RL(2.0), RL(1.0), RL(0.0), RL(-1.0)};
+    real Mt[SM2D_RD_NT], Me[SM2D_RD_NE];
+    sm2d_rd_theta(r_max(f[0], RL(0.0)), Mt);
+    sm2d_rd_energy(f[1], r_max(f[2], RL(0.0)), f[3] > RL(0.5) ? cap1 : cap0, SM2D_RD_NE - 1, Me);
+    for (int e = 0; e < SM2D_RD_NE; ++e)
+        for (int t = 0; t < SM2D_RD_NT; ++t) out[t + 8 * e] = Mt[t] * Me[e];
+}
+/* children from a table row (the GPU's make_kids_t): the window is complete
+ * (emax 3); as in the closed forms (sm2d_rd_fold), an angular distance whose
+ * total mass over the energy offsets is light folds into the centre angle;
+ * the represented energy counts each offset's whole mass */
+static void make_kids_tab(const orc_ctx* c, int tb, int jin, real Em, real w, const real* row, kids* k) {
+    real Ec = r_max(c->E_edges[0], r_min(Em, c->E_edges[c->N_E]));
+    int b = find_bin_edges(c->E_edges, c->N_E, Ec);
+    int up = Ec >= e_center(c, b) ? b + 1 : b;
+    int j = up + 1 < jin ? up + 1 : jin;
+    k->c = tb;
+    k->j = j;
+    k->tab = 1;
+    k->emax = SM2D_RD_NE - 1;
+    for (int i = 0; i < SM2D_RD_NT * SM2D_RD_NE; ++i) k->T[i] = r_max(row[i], RL(0.0));
+    real Er = RL(0.0);
+    for (int e = 0; e < SM2D_RD_NE; ++e) {
+        real me = RL(0.0);
+        for (int t = 0; t < SM2D_RD_NT; ++t) me = me + k->T[t + 8 * e];
+        Er = Er + me * e_center(c, j - e);
+    }
+    k->Erep = Er;
+    const real minw = (real)c->cfg.split_min_weight;
+    for (int t = 1; t < SM2D_RD_NT; ++t) {
+        real mt = RL(0.0);
+        for (int e = 0; e < SM2D_RD_NE; ++e) mt = mt + k->T[t + 8 * e];
+        if (mt > RL(0.0) && w * mt < minw) {
+            for (int e = 0; e < SM2D_RD_NE; ++e) {
+                k->T[8 * e] = k->T[8 * e] + k->T[t + 8 * e];
+                k->T[t + 8 * e] = RL(0.0);
+            }
+        }
+    }
+}
+static inline int kid_live(const kids* k, int t, int e) {
+    return k->tab ? k->T[t + 8 * e] > RL(0.0) : (k->Me[e] > RL(0.0) && k->Mt[t] > RL(0.0));
+}
+static inline real kid_weight(const kids* k, real w, int kk, int e) {
+    if (!k->tab) return sm2d_rd_kid_w(w, k->Mt, k->Me, kk, e);
+    const int t = sm2d_rd_kid_t(kk);
+    const real m = k->T[t + 8 * e];
+    return w * (t == 0 ? m : m * RL(0.5));
 }
 static inline int kid_tbin(const orc_ctx* c, const kids* k, int kk) {
     int tb = k->c + sm2d_rd_kid_side(kk) * sm2d_rd_kid_t(kk);
@@ -816,13 +892,12 @@ static real emit_kids_to_bucket(orc_ctx* c, bucket* bk, const kids* kd, real wei
     if (weight <= RL(0.0)) return RL(0.0);
     real dropped = RL(0.0);
     for (int e = 0; e <= kd->emax; ++e) {
-        if (kd->Me[e] <= RL(0.0)) continue;
         int Eb = kd->j - e;
         int El = Eb % c->cfg.ne_local;
         uint32_t bE = (uint32_t)(Eb / c->cfg.ne_local);
         for (int k = 0; k < SM2D_RD_KIDS; ++k) {
-            if (kd->Mt[sm2d_rd_kid_t(k)] <= RL(0.0)) continue;
-            real wk = sm2d_rd_kid_w(weight, kd->Mt, kd->Me, k, e);
+            if (!kid_live(kd, sm2d_rd_kid_t(k), e)) continue;
+            real wk = kid_weight(kd, weight, k, e);
             int tbin = kid_tbin(c, kd, k);
             uint32_t want = enc_block((uint32_t)(tbin / c->cfg.nt_local), bE);
             int l = enc_lidx(c, tbin % c->cfg.nt_local, El, xs, zs);
@@ -1116,11 +1191,10 @@ static void emit_stay_kids(orc_ctx* c, int k3, int cell, const kids* kd, real E_
         wsum = RL(1.0);
     }
     for (int e = 0; e <= kd->emax; ++e) {
-        if (kd->Me[e] <= RL(0.0)) continue;
         int Eb = kd->j - e;
         for (int k = 0; k < SM2D_RD_KIDS; ++k) {
-            if (kd->Mt[sm2d_rd_kid_t(k)] <= RL(0.0)) continue;
-            real wk = sm2d_rd_kid_w(w_new, kd->Mt, kd->Me, k, e);
+            if (!kid_live(kd, sm2d_rd_kid_t(k), e)) continue;
+            real wk = kid_weight(kd, w_new, k, e);
             int tbn = kid_tbin(c, kd, k);
             uint32_t want = ((uint32_t)(Eb / c->cfg.ne_local) << 12) | ((uint32_t)(tbn / c->cfg.nt_local) & 0xFFFu);
             uint32_t sel;
@@ -1485,7 +1559,13 @@ static void k3_cell(orc_ctx* c, int cell) {
             }
             if (c->cfg.expectation) {
                 kids kd;
-                make_kids(c, tbin, Ebin, sig_th / dth, E_new, sE, w_new, &kd);
+                real f[4], row[SM2D_RD_NT * SM2D_RD_NE];
+                if (c->cfg.surrogate_tables && surr_features(c, Ebin, sig_th / dth, E_new, sE, f)) {
+                    plain_table(f, row);   /* the table path with the method's own table */
+                    make_kids_tab(c, tbin, Ebin, E_new, w_new, row, &kd);
+                } else {
+                    make_kids(c, tbin, Ebin, sig_th / dth, E_new, sE, w_new, &kd);
+                }
                 if (face >= 0)
                     emit_cross(c, 1, cell, face, theta_new, E_new, &kd, w_new, x_new, z_new, K3_SIGMA_TRANSPORT, &t);
                 else emit_stay_kids(c, 1, cell, &kd, E_new, w_new, x_new, z_new, K3_SIGMA_TRANSPORT, sig_x, &t);

@@ -78,6 +78,11 @@ typedef struct orc_config {
      * their MCS angle and straggling loss (sm2d_redist.h) instead of one
      * hashed draw of each; needs energy_split = 1 */
     int expectation;
+    /* expectation form with the surrogate's table path (the GPU's
+     * sm2d_set_surrogate with method_tables = 1): a K3 component whose energy
+     * window has four centres of uniform spacing takes the plain table of its
+     * features (s, u, r, cap) as its children's weights; 0 = closed forms */
+    int surrogate_tables;
 } orc_config;
 
 typedef struct orc_audit {       /* AuditReport, k5_audit.cuh:5-27 */

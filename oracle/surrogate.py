@@ -98,6 +98,22 @@ def forward(params, feats):
     return p, (x, h1, h2, z)
 
 
+FLOOR = 1.0 / 4096.0   # inference: weights below 2^-12 are zero
+
+
+def table(params, feats):
+    """The inference kernel's tables [n][32]: the softmax with weights below
+    FLOOR set to zero and the largest weight taking 1 - the others (each row
+    sums to 1)."""
+    p, _ = forward(params, feats)
+    p = np.where(p < FLOOR, 0.0, p)
+    am = p.argmax(axis=1)
+    rows = np.arange(p.shape[0])
+    p[rows, am] = 0.0
+    p[rows, am] = 1.0 - p.sum(axis=1)
+    return p
+
+
 def loss_and_grad(params, feats, target):
     """Mean cross-entropy and its gradient in the fp32 parameter layout."""
     W1, W2, W3, b1, b2, b3 = unpack(params)

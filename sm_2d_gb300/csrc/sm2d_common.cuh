@@ -23,6 +23,12 @@ int fail(int code, const char* fmt, ...);
 
 constexpr int kThreads = 256;
 
+// The learned surrogate's network over a transport's surrogate rows
+// (sm2d_surrogate.cu), enqueued on stream s.
+int mlp_transport_rows(sm2d_mlp_handle m, cudaStream_t s, const float4* feats, const int* n_dev, int cap, float tol,
+                       int method_tables, float* table, int* fb);
+int mlp_calibrated(sm2d_mlp_handle m);
+
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
     return v;

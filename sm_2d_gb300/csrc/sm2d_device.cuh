@@ -78,6 +78,10 @@ struct IterGlobal {
     int cand_ovf;          // claim-table inserts that found no free entry (cumulative)
     int cand_miss;         // deposits whose block id was not gathered (cumulative)
     int wipe;              // claim tables are cleared before the next pass
+    int k3_rows;           // surrogate rows asked for by this pass's claim pass (may pass k3_cap)
+    int k3_ovf;            // K3 bins past the rows' capacity (closed forms; cumulative)
+    unsigned long long k3_total;   // surrogate rows served by earlier passes since the last reset
+    unsigned long long k3_fb;      // of those, rows that fell back to the closed forms
     uint32_t ctag;         // claim pass number: the tag of claim-table entries
     unsigned long long gen;  // K1 classifications done since create (never reset)
     // spot plan (sm2d_batch_run): lanes that finish take the plan's next
@@ -189,8 +193,20 @@ struct Dev {
     uint4* bins;          // w > 0 bins of the listed cells, grouped by cell:
                           // {gc, slot | seed slot << 5 | lidx << 10 | K3 << 18, w bits, block id}
     uint4* brec;          // per bin, two uint4: the step's outcome from the claim pass
-    float2* brec2;        // expectation form, per bin: sigma_theta / dtheta, straggling sigma
+    float4* brec2;        // expectation form, per bin: sigma_theta / dtheta, straggling sigma,
+                          // the bin's row of the surrogate's tables (int bits, -1: none)
     int expect;           // 1: expectation form (redistribution weights instead of draws)
+    // expectation form with the learned surrogate: the claim pass gives each
+    // K3 bin inside the network's domain a row (its feature row (s, u, r,
+    // cap) and its bin-list entry) and leaves its claims for later; the
+    // network fills the rows' tables [32] and fallback flags; the rows' claim
+    // pass and the deposit pass then emit from the table, or from the closed
+    // forms where the row fell back [k3_cap]
+    int surr, k3_cap;
+    float4* kfeat;
+    int* kbin;
+    float* ktab;
+    int* kfb;
     int2* cell_bins;      // per listed cell: its first bin and bin count in the bin list
     int bins_cap;
     uint32_t *active, *coarse;   // ascending lists of lane 0 (built on request by k_order_lists)

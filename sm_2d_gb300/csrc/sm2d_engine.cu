@@ -528,11 +528,41 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     gs->n_listed = halt ? 0 : min(nl, d.listed_cap);
     gs->n_items = halt ? 0 : ni;
     gs->n_bins = halt ? 0 : nb;
+    gs->k3_total += (unsigned long long)min(max(v->k3_rows, 0), d.k3_cap);   // the last pass's surrogate rows
+    gs->k3_rows = 0;
     if (!halt) gs->bins_total += (unsigned long long)nb;
     gs->blocks_done = 0;
     if (use_cond) {
         cudaGraphSetConditional(cond, (!halt && gs->pass + 1 < gs->max_pass) ? 1u : 0u);
         cudaGraphSetConditional(rcond, (!halt && nf > 0) ? 1u : 0u);
+    }
+}
+
+// The claims of the bins that took a surrogate row in the claim pass, from
+// the network's table of each row (or the closed forms where the row fell
+// back), thread per row.  The claim keys are the bins' own sequential keys,
+// so the claim tables end as if the claim pass had emitted them.
+template <class Lay>
+__global__ void __launch_bounds__(kThreads) k_surr_keys(Dev d) {
+    IterGlobal* gs = d.gs;
+    if (gs->halt) return;
+    const int par = gs->parity;
+    const int n = min(gs->k3_rows, d.k3_cap);
+    const uint32_t tag = gs->ctag;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+        const unsigned am = __activemask();
+        const unsigned fbm = __ballot_sync(am, __ldcg(d.kfb + row) != 0);
+        if ((threadIdx.x & 31) == __ffs(am) - 1 && fbm) atomicAdd(&gs->k3_fb, (unsigned long long)__popc(fbm));
+        const int i = __ldcg(d.kbin + row);
+        const uint4 r = __ldcg(d.bins + i);
+        const int cell = (int)r.x;
+        const int ln = lane_of(d, cell);
+        const int slot = (int)(r.y & 31u), sslot = (int)((r.y >> 5) & 31u), lidx = (int)((r.y >> 10) & 0xFFu);
+        const bool k3 = ((r.y >> 18) & 1u) != 0;
+        const unsigned salt = d.salt ? (unsigned)d.ls[ln].iter * 0x9E3779B9u : 0u;
+        Tally t{};
+        transport_bin<Lay, PASS_KEYS, true>(d, i, par, k3, cell, ln, cell - ln * d.Nc, r.w, slot, sslot, lidx,
+                                            __uint_as_float(r.z), salt, tag, t, true);
     }
 }
 
@@ -1473,6 +1503,12 @@ struct Ctx {
     double* plan_dose_dev = nullptr;
     std::vector<BeamArgs> plan_beams_host;
     std::vector<float> plan_fe_host;
+    // the learned surrogate in the expectation form's K3 (sm2d_set_surrogate)
+    sm2d_mlp_handle mlp = nullptr;
+    float mlp_tol = 0.0f;
+    int mlp_method = 0;
+    size_t k3_alloc = 0;   // rows of the buffers below
+    int grid_rows = 0;
 };
 
 static int dalloc(Ctx& c, void** p, size_t bytes) {
@@ -1511,6 +1547,12 @@ struct Impl {
         // so the sampled form's keep their registers
         if (c.d.expect) k_transport<Lay, PASS_KEYS, true><<<gk, kThreads, 0, c.s>>>(c.d);
         else k_transport<Lay, PASS_KEYS><<<gk, kThreads, 0, c.s>>>(c.d);
+        if (c.d.surr) {   // the network over the claim pass's surrogate rows, then their claims
+            const int rc = mlp_transport_rows(c.mlp, c.s, c.d.kfeat, &c.d.gs->k3_rows, c.d.k3_cap, c.mlp_tol,
+                                              c.mlp_method, c.d.ktab, c.d.kfb);
+            if (rc) return rc;
+            k_surr_keys<Lay><<<c.grid_rows, kThreads, 0, c.s>>>(c.d);
+        }
         CK(rec(3));
         if (bk) k_select_buckets<Lay, true><<<gc, kThreads, 0, c.s>>>(c.d);
         else k_select_buckets<Lay, false><<<gc, kThreads, 0, c.s>>>(c.d);
@@ -1543,6 +1585,15 @@ struct Impl {
         const long long s = std::max(sms, 1);
         c.grid_transport = (int)std::max(1LL, std::min((long long)std::max(per_sm, 1) * s, blocks_for_cap));
         c.grid_keys = (int)std::max(1LL, std::min((long long)std::max(per_sm_keys, 1) * s, blocks_for_cap));
+        return 0;
+    }
+    // grid of the surrogate rows' claim pass: every resident block once
+    static int rows_grid(Ctx& c, int sms) {
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_surr_keys<Lay>, kThreads, 0);
+        if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+        const long long blocks_for_cap = ((long long)c.d.k3_cap + kThreads - 1) / kThreads;
+        c.grid_rows = (int)std::max(1LL, std::min((long long)std::max(per_sm, 1) * std::max(sms, 1), blocks_for_cap));
         return 0;
     }
     static int clear_all(Ctx& c, int) {
@@ -1913,7 +1964,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.bins, uint4, d.bins_cap);
     A(d.cell_bins, int2, d.listed_cap);
     A(d.brec, uint4, 2 * (size_t)d.bins_cap);
-    if (d.expect) A(d.brec2, float2, (size_t)d.bins_cap);
+    if (d.expect) A(d.brec2, float4, (size_t)d.bins_cap);
     A(d.active, uint32_t, Nc); A(d.coarse, uint32_t, Nc);
     A(d.gs, IterGlobal, 1);
     A(d.ls, LaneState, B);
@@ -2412,7 +2463,7 @@ int sm2d_run_profiled(sm2d_handle h, int n, int* done_iters, float* ms7, int* la
             ms7[k] += t;
         }
     if (done_iters) *done_iters = c.ls_host[0].iter - start;
-    if (launches) *launches = launched * (c.p.use_buckets ? 7 : 6);
+    if (launches) *launches = launched * ((c.p.use_buckets ? 7 : 6) + (c.d.surr ? 2 : 0));
     if (passes) *passes = done;
     return 0;
 }
@@ -2582,6 +2633,69 @@ int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills, double* bins) {
     if (passes) *passes = h->gs_host->pass;
     if (refills) *refills = h->gs_host->refills;
     if (bins) *bins = (double)h->gs_host->bins_total;
+    return 0;
+}
+
+// ---------------------------------------------------------------- learned surrogate in the fine step
+int sm2d_set_surrogate(sm2d_handle h, sm2d_mlp_handle m, float tol, int max_rows, int method_tables) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    if (m && !c.d.expect) return fail(SM2D_ERR_ARG, "the surrogate replaces the expectation form's tables (expectation = 1)");
+    if (m && !method_tables && !mlp_calibrated(m))
+        return fail(SM2D_ERR_STATE, "sm2d_set_surrogate before sm2d_mlp_calibrate");
+    if (m && !(tol >= 0.0f)) return fail(SM2D_ERR_ARG, "tolerance %g", (double)tol);
+    if (max_rows < 0) return fail(SM2D_ERR_ARG, "max_rows %d", max_rows);
+    CK(cudaStreamSynchronize(c.s));
+    if (m) {
+        int rc = sm2d_mlp_sync(m);   // the network's weights are written on its own stream
+        if (rc) return rc;
+        const size_t rows = max_rows > 0 ? (size_t)max_rows : (size_t)std::min(c.d.bins_cap, 1 << 22);
+        if (rows > (size_t)c.d.bins_cap)
+            return fail(SM2D_ERR_ARG, "max_rows %d above the bin list's %d", max_rows, c.d.bins_cap);
+        if (rows > c.k3_alloc) {
+            float4* f = nullptr;
+            int* b = nullptr;
+            float* t = nullptr;
+            int* fb = nullptr;
+            if ((rc = dalloc(c, (void**)&f, sizeof(float4) * rows))) return rc;
+            if ((rc = dalloc(c, (void**)&b, sizeof(int) * rows))) return rc;
+            if ((rc = dalloc(c, (void**)&t, sizeof(float) * 32 * rows))) return rc;
+            if ((rc = dalloc(c, (void**)&fb, sizeof(int) * rows))) return rc;
+            c.d.kfeat = f;
+            c.d.kbin = b;
+            c.d.ktab = t;
+            c.d.kfb = fb;
+            c.k3_alloc = rows;
+        }
+        c.d.k3_cap = (int)rows;
+        c.d.surr = 1;
+        c.mlp = m;
+        c.mlp_tol = tol;
+        c.mlp_method = method_tables ? 1 : 0;
+        int dev = 0, sms = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        if ((rc = DISPATCH(c, rows_grid, sms))) return rc;
+    } else {
+        c.d.surr = 0;
+        c.d.k3_cap = 0;
+        c.mlp = nullptr;
+    }
+    // the device loop is captured again with the new pass
+    if (c.exec) cudaGraphExecDestroy(c.exec);
+    if (c.graph) cudaGraphDestroy(c.graph);
+    c.exec = nullptr;
+    c.graph = nullptr;
+    return 0;
+}
+
+int sm2d_surrogate_stats(sm2d_handle h, double* out3) {
+    if (!h || !out3) return fail(SM2D_ERR_ARG, "null argument");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    out3[0] = (double)h->gs_host->k3_total + (double)std::min(std::max(h->gs_host->k3_rows, 0), h->d.k3_cap);
+    out3[1] = (double)h->gs_host->k3_fb;
+    out3[2] = (double)h->gs_host->k3_ovf;
     return 0;
 }
 

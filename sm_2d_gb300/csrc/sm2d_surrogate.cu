@@ -69,6 +69,7 @@ constexpr int kBiasCol = 8;
 // cap = 1 when the energy window's top is the incoming bin (the mean lies in
 // the first interval below it), 0 when it is the second centre above the mean.
 constexpr float kSMax = 8.0f, kRMax = 4.0f;
+constexpr float kFloor = 1.0f / 4096.0f;   // network weights below this are zero (2^-12)
 // calibration regions: sqrt(s / 8) x u x sqrt(r / 4) x cap
 constexpr int kRegS = 16, kRegU = 16, kRegR = 8, kRegC = 2, kRegions = kRegS * kRegU * kRegR * kRegC;
 constexpr long long kSpinCycles = 2000000000LL;   // about one second at the SM clock
@@ -606,16 +607,26 @@ fail:
     }
 }
 
+// What the inference kernel writes for a row whose calibrated region error
+// exceeds the tolerance, and where the rows come from.
+enum {
+    INFER_TABLES = 0,      // the plain table in place of the network's row (fallback flag 1)
+    INFER_TRANSPORT = 1,   // the transport's rows: fallback flag 1, row left unwritten (the
+                           // transport evaluates the closed forms on its own grid)
+    INFER_METHOD = 2       // the transport's rows, every row the plain table (flag 0): the
+                           // table path of the transport with the method's own numbers
+};
 struct InferArgs {
     const float4* feats;
-    int n;
+    int n;                     // rows (with n_dev: the capacity)
+    const int* n_dev;          // device row count (null: n rows)
     const unsigned char* img;
     const float* params;
     float* out;                // [n][32]
     const int* err_bits;       // calibrated region errors (null: no fallback)
     float tol;
     int* fallback;             // per sample: 1 where the plain table was used (may be null)
-    Dev dev;                   // physics of the fallback
+    int mode;                  // INFER_*
     int* err;
 };
 
@@ -671,22 +682,24 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
     const uint32_t tm = *tslot + (uint32_t)(g * 128);
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
     uint32_t pm = 0;
+    // rows: a count the transport's claim pass left on the device, or n
+    const int n = a.n_dev ? min(max(__ldcg(a.n_dev), 0), a.n) : a.n;
     // this warpgroup's first row, loaded ahead; each tile loads the next tile's row
     float4 qn = make_float4(1.0f, 0.0f, 1.0f, 1.0f);
     {
         const int i0 = (blockIdx.x * inf::WG + g) * kTile + row;
-        if (i0 < a.n) qn = a.feats[i0];
+        if (i0 < n) qn = __ldcg(a.feats + i0);
     }
     bool ok = bar_wait(bar_w, 0);
     if (wg_any(g, !ok)) goto fail;
-    for (int tile = blockIdx.x * inf::WG + g; tile * kTile < a.n; tile += gridDim.x * inf::WG) {
+    for (int tile = blockIdx.x * inf::WG + g; tile * kTile < n; tile += gridDim.x * inf::WG) {
         const int i = tile * kTile + row;
-        const bool live = i < a.n;
+        const bool live = i < n;
         float f[4] = {1.0f, 0.0f, 1.0f, 1.0f};
         const float4 q = qn;
         {
             const long long inext = (long long)(tile + gridDim.x * inf::WG) * kTile + row;
-            if (inext < a.n) qn = a.feats[inext];
+            if (inext < n) qn = __ldcg(a.feats + inext);
         }
         {
             float x[kIn];
@@ -766,20 +779,30 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
                 for (int k = 0; k < kOut; ++k) { z[k] = __expf(z[k] - m); s += z[k]; }
                 const float inv = 1.0f / s;
                 float t = 0.0f;
+                // weights below the floor are zero (a component's children
+                // stay as few as the closed forms give), the rest sum to 1
 #pragma unroll
-                for (int k = 0; k < kOut; ++k) { z[k] *= inv; if (k != am) t += z[k]; }
+                for (int k = 0; k < kOut; ++k) {
+                    z[k] *= inv;
+                    if (z[k] < kFloor) z[k] = 0.0f;
+                    if (k != am) t += z[k];
+                }
 #pragma unroll
                 for (int k = 0; k < kOut; ++k)
                     if (k == am) z[k] = 1.0f - t;   // the row sums to 1: the component's weight is conserved
                 int fb = 0;
-                if (a.err_bits && __int_as_float(a.err_bits[region_of(f)]) > a.tol) {
+                if (a.mode == INFER_METHOD) {
                     plain_table(f, z);
+                } else if (a.err_bits && __int_as_float(a.err_bits[region_of(f)]) > a.tol) {
+                    if (a.mode == INFER_TABLES) plain_table(f, z);
                     fb = 1;
                 }
                 if (a.fallback) a.fallback[i] = fb;
-                float4* o = reinterpret_cast<float4*>(a.out + (size_t)i * kOut);
+                if (!(fb && a.mode == INFER_TRANSPORT)) {
+                    float4* o = reinterpret_cast<float4*>(a.out + (size_t)i * kOut);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) o[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+                    for (int q = 0; q < 8; ++q) o[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+                }
             }
         }
         fence_before();
@@ -1108,8 +1131,9 @@ int sm2d_mlp_redistribute(sm2d_mlp_handle m, sm2d_handle h, const float* d_feats
     if (!m->calibrated) return fail(SM2D_ERR_STATE, "sm2d_mlp_redistribute before sm2d_mlp_calibrate");
     if (!aligned16(d_feats) || !aligned16(d_table)) return fail(SM2D_ERR_ARG, "arrays must be 16-byte aligned");
     InferArgs a{};
+    Dev dev;
     cudaStream_t s;
-    int rc = handle_dev(h, &a.dev, &s);
+    int rc = handle_dev(h, &dev, &s);
     if (rc) return rc;
     a.feats = reinterpret_cast<const float4*>(d_feats);
     a.n = n;
@@ -1144,3 +1168,32 @@ int sm2d_mlp_geometry(float* out8) {
 }
 
 }  // extern "C"
+
+namespace sm2d {
+// The network over the transport's surrogate rows, enqueued on the
+// transport's stream (the engine captures it into its device loop): rows
+// 0 .. min(*n_dev, cap) of feats, their tables into table [cap][32] and
+// fallback flags into fb [cap].  method_tables: every row gets the plain
+// table instead (the table path with the method's own numbers).  A bounded
+// wait that gives up sets the surrogate handle's error flag (sm2d_mlp_sync).
+int mlp_transport_rows(sm2d_mlp_handle m, cudaStream_t s, const float4* feats, const int* n_dev, int cap, float tol,
+                       int method_tables, float* table, int* fb) {
+    InferArgs a{};
+    a.feats = feats;
+    a.n = cap;
+    a.n_dev = n_dev;
+    a.img = m->img;
+    a.params = m->params;
+    a.out = table;
+    a.err_bits = m->err_bits;
+    a.tol = tol;
+    a.fallback = fb;
+    a.mode = method_tables ? INFER_METHOD : INFER_TRANSPORT;
+    a.err = m->err;
+    const int tiles = (cap + kTile - 1) / kTile;
+    k_infer<<<std::max(1, std::min((tiles + inf::WG - 1) / inf::WG, m->sms)), kInferThreads, inf::BYTES, s>>>(a);
+    CK(cudaGetLastError());
+    return 0;
+}
+int mlp_calibrated(sm2d_mlp_handle m) { return m && m->calibrated; }
+}  // namespace sm2d

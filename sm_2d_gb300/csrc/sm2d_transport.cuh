@@ -300,6 +300,25 @@ __device__ __forceinline__ int kid_window_top(const Dev& d, int jin, float Em) {
     const int up = Ec >= e_center(d, b) ? b + 1 : b;   // the lowest centre at or above Em
     return min(jin, up + 1);
 }
+// The learned surrogate's features of a component (sm2d_surrogate.cu):
+// s = sigma_theta / dtheta; u, where the mean energy Em lies between the
+// centres around it; r = sigma_E / their spacing; cap = 1 when the window's
+// top is the incoming bin.  cap = -1 marks a component outside the network's
+// domain (a window of fewer than four centres or of uneven spacing), which
+// keeps the closed forms.
+__device__ __forceinline__ float4 surr_features(const Dev& d, int jin, float s, float Em, float sE) {
+    const float Ec = fmaxf(d.Ee[0], fminf(Em, d.Ee[d.N_E]));
+    const int b = find_ebin(d, Ec);
+    const int up = Ec >= e_center(d, b) ? b + 1 : b;   // the lowest centre at or above Em
+    const int jt = min(jin, up + 1);
+    if (up < 1 || up > d.N_E - 1 || jt < SM2D_RD_NE - 1) return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    const float ch = e_center(d, up), cl = e_center(d, up - 1), D = ch - cl;
+    for (int e = 0; e < SM2D_RD_NE - 1; ++e) {
+        const float de = e_center(d, jt - e) - e_center(d, jt - e - 1);
+        if (fabsf(de - D) > 1e-3f * D) return make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    }
+    return make_float4(s, fminf(fmaxf((Em - cl) / D, 0.0f), 0.99999994f), sE / D, jt == up ? 1.0f : 0.0f);
+}
 __device__ __forceinline__ void make_kids(const Dev& d, int c, int jin, float s, float Em, float sE, float w, Kids& k) {
     const int j = kid_window_top(d, jin, Em);
     k.c = c;
@@ -311,24 +330,82 @@ __device__ __forceinline__ void make_kids(const Dev& d, int c, int jin, float s,
     sm2d_rd_energy(Em, sE, cen, k.emax, k.Me);
     k.Erep = sm2d_rd_fold(w, d.split_min_w, k.Mt, k.Me, cen, k.emax);
 }
-__device__ __forceinline__ int kid_tbin(const Dev& d, const Kids& k, int kk) {
+// The children from the learned surrogate's table of the component (its
+// row of the network's output, T[t + 8 e]; the window is complete, emax 3).
+// As in the closed forms (sm2d_rd_fold), an angular distance whose total
+// mass (over the energy offsets) is light folds into the centre angle, and
+// the represented energy counts each offset's whole mass.
+struct KidsT {
+    int c, j;
+    float T[SM2D_RD_NT * SM2D_RD_NE];
+    float Erep;
+};
+__device__ __forceinline__ void make_kids_t(const Dev& d, int c, int jin, float Em, float w, const float* row,
+                                            KidsT& k) {
+    const int j = kid_window_top(d, jin, Em);
+    k.c = c;
+    k.j = j;
+    const float4* r4 = reinterpret_cast<const float4*>(row);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const float4 v = __ldcg(r4 + q);
+        k.T[4 * q] = fmaxf(v.x, 0.0f); k.T[4 * q + 1] = fmaxf(v.y, 0.0f);
+        k.T[4 * q + 2] = fmaxf(v.z, 0.0f); k.T[4 * q + 3] = fmaxf(v.w, 0.0f);
+    }
+    float Er = 0.0f;
+#pragma unroll
+    for (int e = 0; e < SM2D_RD_NE; ++e) {
+        float me = 0.0f;
+#pragma unroll
+        for (int t = 0; t < SM2D_RD_NT; ++t) me += k.T[t + 8 * e];
+        Er += me * e_center(d, j - e);
+    }
+    k.Erep = Er;
+#pragma unroll
+    for (int t = 1; t < SM2D_RD_NT; ++t) {
+        float mt = 0.0f;
+#pragma unroll
+        for (int e = 0; e < SM2D_RD_NE; ++e) mt += k.T[t + 8 * e];
+        if (mt > 0.0f && w * mt < d.split_min_w) {
+#pragma unroll
+            for (int e = 0; e < SM2D_RD_NE; ++e) {
+                k.T[8 * e] += k.T[t + 8 * e];
+                k.T[t + 8 * e] = 0.0f;
+            }
+        }
+    }
+}
+// accessors shared by both kinds of children
+__device__ __forceinline__ int kid_emax(const Kids& k) { return k.emax; }
+__device__ __forceinline__ int kid_emax(const KidsT&) { return SM2D_RD_NE - 1; }
+__device__ __forceinline__ bool kid_live(const Kids& k, int t, int e) { return k.Me[e] > 0.0f && k.Mt[t] > 0.0f; }
+__device__ __forceinline__ bool kid_live(const KidsT& k, int t, int e) { return k.T[t + 8 * e] > 0.0f; }
+__device__ __forceinline__ float kid_weight(const Kids& k, float w, int kk, int e) {
+    return sm2d_rd_kid_w(w, k.Mt, k.Me, kk, e);
+}
+__device__ __forceinline__ float kid_weight(const KidsT& k, float w, int kk, int e) {
+    const int t = sm2d_rd_kid_t(kk);
+    const float m = k.T[t + 8 * e];
+    return w * (t == 0 ? m : m * 0.5f);
+}
+template <class K>
+__device__ __forceinline__ int kid_tbin(const Dev& d, const K& k, int kk) {
     return max(0, min(k.c + sm2d_rd_kid_side(kk) * sm2d_rd_kid_t(kk), d.N_theta - 1));
 }
 // the children of a component of weight `weight` into one container, in
 // child order (the claim key's emission index is the child number)
-template <class Lay, int PASS>
+template <class Lay, int PASS, class K>
 __device__ float emit_component(const Dev& d, const Src& src, int par, int bcell, int face, int dcell, int col,
-                                const Kids& kd, float weight, int xs, int zs, Tally& t) {
+                                const K& kd, float weight, int xs, int zs, Tally& t) {
     if (weight <= 0.0f) return 0.0f;
     float dropped = 0.0f;
-    for (int e = 0; e <= kd.emax; ++e) {
-        if (kd.Me[e] <= 0.0f) continue;
+    for (int e = 0; e <= kid_emax(kd); ++e) {
         const int Eb = kd.j - e;
         const int El = Eb % Lay::NE;
         const uint32_t bE = (uint32_t)(Eb / Lay::NE);
         for (int k = 0; k < SM2D_RD_KIDS; ++k) {
-            if (kd.Mt[sm2d_rd_kid_t(k)] <= 0.0f) continue;
-            const float wk = sm2d_rd_kid_w(weight, kd.Mt, kd.Me, k, e);
+            if (!kid_live(kd, sm2d_rd_kid_t(k), e)) continue;
+            const float wk = kid_weight(kd, weight, k, e);
             if (PASS != PASS_KEYS && wk <= 0.0f) continue;
             const int tb = kid_tbin(d, kd, k);
             const uint32_t want = make_bid((uint32_t)(tb / Lay::NT), bE);
@@ -346,11 +423,13 @@ struct AngleEnergy {
 };
 __device__ __forceinline__ EmitPlan plan_of(const Dev& d, const AngleEnergy& a) { return plan_emission(d, a.theta, a.E); }
 __device__ __forceinline__ const Kids& plan_of(const Dev&, const Kids& k) { return k; }
+__device__ __forceinline__ const KidsT& plan_of(const Dev&, const KidsT& k) { return k; }
 // energy of the re-binned parts of a planned component
 __device__ __forceinline__ float plan_erep(const Dev& d, const AngleEnergy&, float E, float w) {
     return bin_energy(d, E, w).Erep;
 }
 __device__ __forceinline__ float plan_erep(const Dev&, const Kids& k, float, float) { return k.Erep; }
+__device__ __forceinline__ float plan_erep(const Dev&, const KidsT& k, float, float) { return k.Erep; }
 
 // +z crossing with the N-cell lateral Gaussian split: the share of column
 // ix+k goes through the +z bucket of cell (ix+k, iz) to cell (ix+k, iz+1)
@@ -585,8 +664,8 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
 // Gaussian tails past the cell edges go to the lateral neighbours as
 // children; the difference between the step's mean energy and the
 // children's represented energy is folded into the deposit.
-template <class Lay, int PASS>
-__device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, const Kids& kd, float E_new,
+template <class Lay, int PASS, class K>
+__device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, const K& kd, float E_new,
                                float w_new, float x_new, float z_new, float sig_sub, float sig_cell, Tally& t) {
     const float dx = d.dx, dz = d.dz;
     const int ix = cell % d.Nx;
@@ -595,11 +674,10 @@ __device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, c
     const float win = gauss_cdf(rb, x_new, sig_cell) - gauss_cdf(lb, x_new, sig_cell);
     const float wcf = fminf(1.0f, fmaxf(0.0f, win));
     if (PASS == PASS_KEYS) {
-        for (int e = 0; e <= kd.emax; ++e) {
-            if (kd.Me[e] <= 0.0f) continue;
+        for (int e = 0; e <= kid_emax(kd); ++e) {
             const uint32_t bE = (uint32_t)((kd.j - e) / Lay::NE);
             for (int k = 0; k < SM2D_RD_KIDS; ++k) {
-                if (kd.Mt[sm2d_rd_kid_t(k)] <= 0.0f) continue;
+                if (!kid_live(kd, sm2d_rd_kid_t(k), e)) continue;
                 const uint32_t want = make_bid((uint32_t)(kid_tbin(d, kd, k) / Lay::NT), bE);
                 cand_insert(psi_row(d, cell), d.ccount + cell, sc.tag, want, stay_key(sc.k3, sc.slot, sc.lidx, 16 * e + k),
                             &d.gs->cand_ovf);
@@ -648,13 +726,12 @@ __device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, c
         }
         const uint32_t* kept = d.bid + (size_t)cell * kKb;
         float* vals = d.val + (size_t)cell * kKb * Lay::L;
-        for (int e = 0; e <= kd.emax; ++e) {
-            if (kd.Me[e] <= 0.0f) continue;
+        for (int e = 0; e <= kid_emax(kd); ++e) {
             const int Eb = kd.j - e;
             const uint32_t bE = (uint32_t)(Eb / Lay::NE);
             for (int k = 0; k < SM2D_RD_KIDS; ++k) {
-                if (kd.Mt[sm2d_rd_kid_t(k)] <= 0.0f) continue;
-                const float wk = sm2d_rd_kid_w(w_new, kd.Mt, kd.Me, k, e);
+                if (!kid_live(kd, sm2d_rd_kid_t(k), e)) continue;
+                const float wk = kid_weight(kd, w_new, k, e);
                 if (wk <= 0.0f) continue;
                 const int tbn = kid_tbin(d, kd, k);
                 const uint32_t want = make_bid((uint32_t)(tbn / Lay::NT), bE);
@@ -785,9 +862,17 @@ __device__ __forceinline__ int exit_face(float x, float z, float dx, float dz) {
 // energy, weight, raw position, lateral sigma, deposit, nuclear loss) in the
 // bin's record; the deposit pass reads it back instead of repeating the
 // physics, so both passes emit the same arithmetic's results.
+//
+// With the learned surrogate (expectation form, d.surr): the claim pass gives
+// a K3 bin inside the network's domain a row of the surrogate's tables and
+// emits no claims for it; after the network has run, the rows' claim pass
+// (from_rec: the step's outcome from the record) and the deposit pass emit
+// the bin's children from its row's table, or from the closed forms where
+// the row fell back.
 template <class Lay, int PASS, bool EXP>
 __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, int ln, int lc, uint32_t bid, int slot,
-                              int sslot, int lidx, float w, unsigned salt, uint32_t tag, Tally& t) {
+                              int sslot, int lidx, float w, unsigned salt, uint32_t tag, Tally& t,
+                              bool from_rec = false) {
     const float dx = d.dx, dz = d.dz;
     int tl, El, xs, zs;
     Lay::dec(lidx, tl, El, xs, zs);
@@ -819,14 +904,16 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
     float theta_new, x_new, z_new, E_new, w_new, edep, w_rem = 0.0f, sigv;
     float s_th = 0.0f, s_E = 0.0f;   // expectation form: sigma_theta / dtheta, straggling sigma
     float4* rec = reinterpret_cast<float4*>(d.brec + 2 * (size_t)bi);
-    if (PASS != PASS_KEYS) {
+    int srow = -1;   // the bin's row of the surrogate's tables
+    if (PASS != PASS_KEYS || (EXP && from_rec)) {
         const float4 r0 = __ldcs(rec), r1 = __ldcs(rec + 1);
         theta_new = r0.x; E_new = r0.y; w_new = r0.z; x_new = r0.w;
         z_new = r1.x; sigv = r1.y; edep = r1.z; w_rem = r1.w;
         if (EXP) {
-            const float2 r2 = __ldcs(d.brec2 + bi);
+            const float4 r2 = __ldcs(d.brec2 + bi);
             s_th = r2.x;
             s_E = r2.y;
+            srow = __float_as_int(r2.z);
         }
     } else {
     const float xc = sub_offset(xs, Lay::NX, dx), zc = sub_offset(zs, Lay::NZ, dz);
@@ -936,7 +1023,25 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
                : sig_x;
     __stcg(rec, make_float4(theta_new, E_new, w_new, x_new));
     __stcg(rec + 1, make_float4(z_new, sigv, edep, w_rem));
-    if (EXP) __stcg(d.brec2 + bi, make_float2(s_th, s_E));
+    if (EXP) {
+        // a K3 bin that stays above the cutoff with features inside the
+        // network's domain gets a row of the surrogate's tables
+        float4 q = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        if (d.surr && k3 && E_new > 0.1f && E_new > e_center(d, 0))
+            q = surr_features(d, max(0, min(Ebin, d.N_E - 1)), s_th, E_new, s_E);
+        if (q.w >= 0.0f) {
+            const int row = atomicAdd(&d.gs->k3_rows, 1);
+            if (row < d.k3_cap) {
+                d.kfeat[row] = q;
+                d.kbin[row] = bi;
+                srow = row;
+            } else {
+                atomicAdd(&d.gs->k3_ovf, 1);
+            }
+        }
+        __stcg(d.brec2 + bi, make_float4(s_th, s_E, __int_as_float(srow), 0.0f));
+        if (srow >= 0) return;   // its claims follow the network (the rows' claim pass)
+    }
     }
     const int face = exit_face(x_new, z_new, dx, dz);
     x_new = fmaxf(-hx, fminf(x_new, hx));
@@ -951,8 +1056,21 @@ __device__ void transport_bin(const Dev& d, int bi, int par, bool k3, int cell, 
     const int my_cls = k3 ? 2 : 1;
     const Src sc{cell, slot, lidx, k3 ? 1 : 0, tag, E_new};
     if (EXP) {
+        const int c0 = max(0, min(tbin, d.N_theta - 1)), j0 = max(0, min(Ebin, d.N_E - 1));
+        // the surrogate's table where the network served the bin's row (the
+        // rows' claim pass and the deposit pass), else the closed forms
+        if (srow >= 0 && __ldcg(d.kfb + srow) == 0) {
+            KidsT kt;
+            make_kids_t(d, c0, j0, E_new, w_new, d.ktab + (size_t)srow * (SM2D_RD_NT * SM2D_RD_NE), kt);
+            if (face >= 0)
+                emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, kt, E_new, w_new, x_new, z_new, sigv, t);
+            else
+                emit_stay_kids<Lay, PASS>(d, sc, par, cell, kt, E_new, w_new, x_new, z_new, k3 ? 0.001f : sigv, sigv,
+                                          t);
+            return;
+        }
         Kids kd;
-        make_kids(d, max(0, min(tbin, d.N_theta - 1)), max(0, min(Ebin, d.N_E - 1)), s_th, E_new, s_E, w_new, kd);
+        make_kids(d, c0, j0, s_th, E_new, s_E, w_new, kd);
         if (face >= 0)
             emit_cross<Lay, PASS>(d, sc, par, k3, cell, my_cls, face, kd, E_new, w_new, x_new, z_new, sigv, t);
         else

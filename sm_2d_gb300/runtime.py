@@ -185,6 +185,8 @@ def lib(build_if_needed: bool = True):
         L.sm2d_plan_run_async.argtypes = [P]
         L.sm2d_plan_results.argtypes = [P, P, P]
         L.sm2d_plan_stats.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(D)]
+        L.sm2d_set_surrogate.argtypes = [P, P, F, I, I]
+        L.sm2d_surrogate_stats.argtypes = [P, P]
         _LIB = L
         return L
 
@@ -381,6 +383,22 @@ class Transport:
 
     def __exit__(self, *a):
         self.close()
+
+    # -- learned surrogate in the fine step (expectation form)
+    def set_surrogate(self, surrogate, tol=0.005, max_rows=0, method_tables=False):
+        """K3 bins inside the network's domain take their redistribution
+        weights from `surrogate` (a calibrated surrogate.Surrogate), with the
+        closed forms where the calibrated error exceeds tol; method_tables:
+        the plain table of each row instead of the network's; None detaches."""
+        m = surrogate.m if surrogate is not None else None
+        check(self._lib.sm2d_set_surrogate(self.h, m, float(tol), int(max_rows), 1 if method_tables else 0))
+        self._surrogate = surrogate   # the network must outlive its use here
+
+    def surrogate_stats(self):
+        """rows served, rows that fell back, K3 bins beyond the row capacity (since the last reset)"""
+        o = np.zeros(3)
+        check(self._lib.sm2d_surrogate_stats(self.h, _p(o)))
+        return dict(rows=int(o[0]), fallback_rows=int(o[1]), overflow_bins=int(o[2]))
 
     # -- source and phase space
     def inject(self, x0=0.0, z0=0.0, theta0=0.0, E0=150.0, W=1.0, sigma_x=0.0, sigma_theta=0.0,

@@ -76,10 +76,10 @@ def test_energy_masses_match_integration(Em, sE):
     assert abs((Me * np.array(cen)).sum() - 9.58) < 1e-12
 
 
-def _run(fp64, E0=40.0, Nx=40, Nz=80, expect=1):
+def _run(fp64, E0=40.0, Nx=40, Nz=80, expect=1, tables=0):
     cfg = sm.Config.reference_runner(Nx, Nz, 0.5, 0.5, sigma_x_initial=1.5, E0=E0, energy_split=1).production()
     cfg.expectation = expect
-    o = orc.Oracle(cfg.oracle_config(), cfg.theta_edges, cfg.E_edges, fp64=fp64)
+    o = orc.Oracle(dict(cfg.oracle_config(), surrogate_tables=tables), cfg.theta_edges, cfg.E_edges, fp64=fp64)
     o.inject(x0=0.0, z0=0.0, theta0=0.0, E0=E0, W=1.0, sigma_x=1.5, sigma_theta=0.002, sigma_E=0.01 * E0,
              n_samples=400, seed=11)
     fails = 0
@@ -134,3 +134,15 @@ def test_expectation_needs_the_energy_split():
     cfg.expectation = 1
     with pytest.raises(sm.Sm2dError, match="energy split"):
         sm.Transport(cfg)
+
+
+def test_table_path_with_the_method_tables_equals_the_closed_forms():
+    """K3 components whose energy window has uniformly spaced centres take
+    their children's weights from a 32-entry table (the learned surrogate's
+    path); given the plain table of their features, the run equals the closed
+    forms up to float rounding (the table's energy masses are evaluated in
+    units of the centre spacing)."""
+    a, b = _run(False), _run(False, tables=1)
+    assert a["n"] == b["n"]
+    assert np.abs(a["dose"] - b["dose"]).max() / a["dose"].max() < 1e-5
+    assert abs(b["balance"]) < 1e-6 and b["fails"] == 0

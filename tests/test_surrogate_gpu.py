@@ -23,7 +23,9 @@ pytestmark = pytest.mark.gpu
 # from sums accumulated in different orders (fp32 tensor core, float64 here);
 # a sum within that difference of a bf16 rounding boundary rounds the other
 # way and moves its row by 1e-5..1e-4 (about 2 % of rows), exceptionally by a
-# few 1e-3.  Bounds: the median row, the share of rows above 1e-3, the worst row.
+# few 1e-3; a weight within that difference of the 2^-12 floor is zero on one
+# side only (a move of 2.4e-4).  Bounds: the median row, the share of rows
+# above 1e-3, the worst row.
 FWD_MEDIAN, FWD_ROW_ATOL, FWD_MAX_SHARE, FWD_ATOL = 1e-6, 1e-3, 0.01, 1e-2
 GRAD_RTOL = 2e-2    # relative L2 error of each parameter block's gradient
 
@@ -58,7 +60,7 @@ def test_forward_matches_oracle(surr):
     surr.set_params(p)
     f = surr.features(3000, 21)   # not a multiple of the 128-row tile
     t = surr.forward(f).cpu().numpy()
-    ref, _ = so.forward(p, f.cpu().numpy())
+    ref = so.table(p, f.cpu().numpy())
     d = np.abs(t - ref).max(axis=1)
     assert np.median(d) <= FWD_MEDIAN, np.median(d)
     assert np.mean(d > FWD_ROW_ATOL) < FWD_MAX_SHARE and d.max() <= FWD_ATOL, (np.mean(d > FWD_ROW_ATOL), d.max())
