@@ -169,6 +169,16 @@ int sm2d_inject_quadrature(sm2d_handle h, const sm2d_beam* beam);
 /* host <-> device phase space (psi_in): bid[Nx*Nz*32], val[Nx*Nz*32*L] */
 int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val);
 int sm2d_get_psi_in(sm2d_handle h, uint32_t* bid, float* val);
+/* the same on device arrays of the caller (DevicePsiC::block_id / value,
+ * src/cuda/device/device_psic.cuh:39-55; single-lane engines) */
+int sm2d_set_psi_in_device(sm2d_handle h, const uint32_t* d_bid, const float* d_val);
+int sm2d_get_psi_in_device(sm2d_handle h, uint32_t* d_bid, float* d_val);
+/* source accounting of a phase space set by the caller (the
+ * K1K6PipelineState::source_* fields, src/cuda/k1k6_pipeline.cuh:190-197, that
+ * the first iteration's audit lifts): [0] injected weight, [1] out-of-grid
+ * weight, [2] slot-dropped weight, [3] injected energy, [4] out-of-grid
+ * energy, [5] slot-dropped energy, [6] representation loss energy */
+int sm2d_set_source_accounting(sm2d_handle h, const double* v7);
 
 /* one K1..K6 iteration; *n_active/*n_coarse are the listed cells (0,0 = done) */
 int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse);

@@ -108,6 +108,7 @@ def _lib(fp64: bool):
         lib.orc_track_claims.argtypes = [P, C.c_int]
         lib.orc_redist_masses.argtypes = [C.c_double, C.c_double, C.c_double, P, C.c_int, P, P]
         lib.orc_claim_demand.argtypes = [P]
+        lib.orc_k4_raw.argtypes = [P, C.c_int, P, P, P, P, P, P]
         _LIBS[key] = lib
         return lib
 
@@ -299,6 +300,19 @@ class Oracle:
         out = np.zeros((f.shape[0], 32), np.float32)
         self.lib.orc_redistribution_table(self.ctx, f.shape[0], _p(f), _p(out))
         return out
+
+    def k4_raw(self, bkt_bid, bkt_val, c2b, out_bid, out_val):
+        """K4 on caller arrays: buckets [nb][Kb] ids and [nb][Kb][L] values,
+        c2b [Nc]; returns the updated psi_out ids and values and the dropped
+        (weight, energy)."""
+        bb = np.ascontiguousarray(bkt_bid, np.uint32)
+        bv = np.ascontiguousarray(bkt_val, self.dtype)
+        cb = np.ascontiguousarray(c2b, np.int32)
+        ob = np.array(out_bid, np.uint32, copy=True)
+        ov = np.array(out_val, self.dtype, copy=True)
+        drop = np.zeros(2)
+        self.lib.orc_k4_raw(self.ctx, bb.shape[0], _p(bb), _p(bv), _p(cb), _p(ob), _p(ov), _p(drop))
+        return ob, ov, (float(drop[0]), float(drop[1]))
 
     def track_claims(self, on=True):
         """Record the distinct block ids aimed at each container per iteration."""

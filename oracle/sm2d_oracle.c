@@ -2235,6 +2235,45 @@ void orc_get_psi_in(const orc_ctx* c, uint32_t* bid, orc_real* val) {
     if (val) memcpy(val, p->val, sizeof(real) * ns * c->L);
 }
 
+/* K4 on caller arrays, the checker of the raw K4 entry: nb buckets of Kb
+ * ids (bbid) and Kb x L values (bval), c2b[Nc] the first of a listed cell's
+ * four buckets (faces +z, -z, +x, -x; -1: not listed); the psi_out ids and
+ * values are updated in place and drop2[0..1] gains the weight and energy K4
+ * could not place.  The buckets and psi_out stand in for the context's own
+ * while k4 runs. */
+void orc_k4_raw(orc_ctx* c, int nb, const uint32_t* bbid, const orc_real* bval, const int* c2b, uint32_t* obid,
+                orc_real* oval, double* drop2) {
+    bucket* saved_b = c->buckets;
+    int* saved_c2b = c->cell_to_bucket;
+    psi_buf* po = psi_out(c);
+    const psi_buf saved_po = *po;
+    bucket* tmp = (bucket*)calloc((size_t)(nb > 0 ? nb : 1), sizeof(bucket));
+    uint8_t* occ = (uint8_t*)calloc((size_t)c->Nc, 1);
+    for (int i = 0; i < nb; ++i) {
+        tmp[i].bid = (uint32_t*)(bbid + (size_t)i * c->Kb);
+        tmp[i].val = (real*)(bval + (size_t)i * c->Kb * c->L);
+    }
+    for (int cell = 0; cell < c->Nc; ++cell)
+        for (int k = 0; k < c->Kb; ++k)
+            if (obid[(size_t)cell * c->Kb + k] != ORC_EMPTY) occ[cell] = 1;
+    c->buckets = tmp;
+    c->cell_to_bucket = (int*)c2b;
+    po->bid = obid;
+    po->val = oval;
+    po->occ = occ;
+    const double w0 = c->k4_slot_w, e0 = c->k4_slot_e;
+    k4(c);
+    drop2[0] += c->k4_slot_w - w0;
+    drop2[1] += c->k4_slot_e - e0;
+    c->k4_slot_w = w0;
+    c->k4_slot_e = e0;
+    *po = saved_po;
+    c->buckets = saved_b;
+    c->cell_to_bucket = saved_c2b;
+    free(occ);
+    free(tmp);
+}
+
 void orc_get_mask(const orc_ctx* c, uint8_t* m) { memcpy(m, c->mask, (size_t)c->Nc); }
 
 int orc_get_lists(const orc_ctx* c, uint32_t* a, int* na, uint32_t* co, int* nco) {

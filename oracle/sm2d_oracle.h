@@ -172,6 +172,12 @@ void orc_redistribution_table(const orc_ctx* c, int n, const float* feats, float
  * block ids aimed at one container (a psi_out cell, or one bucket of one
  * batch) within one iteration since tracking began */
 void orc_track_claims(orc_ctx* c, int on);
+/* K4 on caller arrays (checker of the raw K4 entry): nb buckets of Kb ids
+ * and Kb x L values, c2b[Nc] the first of a listed cell's four buckets (-1:
+ * none); psi_out ids and values updated in place, drop2 += dropped weight
+ * and energy */
+void orc_k4_raw(orc_ctx* c, int nb, const uint32_t* bbid, const orc_real* bval, const int* c2b, uint32_t* obid,
+                orc_real* oval, double* drop2);
 /* the expectation form's angular masses Mt[8] for s = sigma_theta / dtheta
  * and energy masses Me[4] for a Gaussian (Em, sE) over the centres cen[0..emax]
  * (sm2d_redist.h), evaluated in this build's precision */

@@ -1,4 +1,7 @@
-"""In-tree build of libsm2d.so: the sm_103a CUDA kernels + C ABI.
+"""In-tree build of libsm2d.so: the sm_103a CUDA kernels + C ABI; and of the
+C++ drop-in layer over it (libsm2d_ref.so: the reference's pipeline and
+wrapper entry points; libsm2d_ref_host.so: its grid and LUT types for programs
+built without the reference's host code).
 
 nvcc compiles the three CUDA translation units (the engine, the stage
 entries and the redistribution surrogate) for sm_103a only, g++ compiles the host tables, the output writers
@@ -18,6 +21,7 @@ from concurrent.futures import ThreadPoolExecutor
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
+SHIM = os.path.join(PKG, "shim")
 OUT = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT, "libsm2d.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -34,7 +38,9 @@ def _cuda_home() -> str:
 
 
 def _sources():
-    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))] + [os.path.join(ROOT, "include", "sm2d.h")]
+    return ([os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))] +
+            [os.path.join(SHIM, f) for f in sorted(os.listdir(SHIM)) if f.endswith((".cpp", ".hpp"))] +
+            [os.path.join(ROOT, "include", f) for f in ("sm2d.h", "sm2d_ref_types.hpp")])
 
 
 def up_to_date() -> bool:
@@ -88,6 +94,18 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     run(["gcc", "-O2", "-std=c11", *inc, os.path.join(CSRC, "sm2d_run_simulation.c"), "-o", exe + ".tmp",
          "-L" + OUT, "-lsm2d", "-Wl,-rpath,$ORIGIN"])
     os.replace(exe + ".tmp", exe)
+    # the C++ drop-in layer: the reference's entry points over the C ABI
+    cuda_inc = ["-I" + os.path.join(cuda, "include"), "-I" + os.path.join(cuda, "targets", "sbsa-linux", "include"),
+                "-I" + os.path.join(cuda, "targets", "x86_64-linux", "include")]
+    cuda_lib = ["-L" + os.path.join(cuda, "lib64"), "-L" + os.path.join(cuda, "targets", "sbsa-linux", "lib"),
+                "-L" + os.path.join(cuda, "targets", "x86_64-linux", "lib")]
+    for name, src, extra in (("libsm2d_ref.so", "sm2d_ref_shim.cpp", ["-lcudart"]),
+                             ("libsm2d_ref_host.so", "sm2d_ref_grids.cpp", [])):
+        out = os.path.join(OUT, name)
+        run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", *inc, *cuda_inc, os.path.join(SHIM, src), "-o",
+             out + ".tmp", "-L" + OUT, "-lsm2d", *cuda_lib, *extra, "-Wl,-rpath,$ORIGIN",
+             "-Wl,-rpath," + os.path.join(cuda, "lib64")])
+        os.replace(out + ".tmp", out)
     return LIB
 
 

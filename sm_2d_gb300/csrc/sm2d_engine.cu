@@ -2213,6 +2213,69 @@ int sm2d_get_psi_in(sm2d_handle h, uint32_t* bid, float* val) {
     return 0;
 }
 
+// psi_in from device arrays in the same layout: the ids come to the host
+// once to list the occupied cells, the values are copied on the device
+int sm2d_set_psi_in_device(sm2d_handle h, const uint32_t* d_bid, const float* d_val) {
+    if (!h || !d_bid || !d_val) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    if (c.B != 1) return fail(SM2D_ERR_STATE, "sm2d_set_psi_in_device needs a single-lane engine");
+    int rc = sync_state(c);
+    if (rc) return rc;
+    if ((rc = DISPATCH(c, clear_all, 0))) return rc;
+    const int par = c.gs_host->parity;
+    const size_t ns = (size_t)c.d.Nc * kKb;
+    std::vector<uint32_t> bid(ns);
+    CK(cudaMemcpyAsync(bid.data(), d_bid, ns * 4, cudaMemcpyDeviceToHost, c.s));
+    CK(cudaMemcpyAsync(c.d.bid, d_bid, ns * 4, cudaMemcpyDeviceToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.val, d_val, ns * c.L * 4, cudaMemcpyDeviceToDevice, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    std::vector<int> occ(c.d.Nc, 0), list;
+    for (int cell = 0; cell < c.d.Nc; ++cell)
+        for (int k = 0; k < kKb; ++k)
+            if (bid[(size_t)cell * kKb + k] != kEmpty) {
+                occ[cell] = 1;
+                list.push_back(cell);
+                break;
+            }
+    CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, c.s));
+    if (!list.empty())
+        CK(cudaMemcpyAsync(c.d.occ_list[par], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, c.s));
+    c.gs_host->occ_n[par] = (int)list.size();
+    c.gs_host->occ_n[par ^ 1] = 0;
+    c.ls_host[0].done = 0;
+    if ((rc = push_state(c))) return rc;
+    CK(cudaStreamSynchronize(c.s));
+    c.injected = true;
+    return 0;
+}
+
+int sm2d_get_psi_in_device(sm2d_handle h, uint32_t* d_bid, float* d_val) {
+    if (!h || !d_bid) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    const size_t ns = (size_t)c.d.Nc * kKb;
+    CK(cudaMemcpyAsync(d_bid, c.d.bid, ns * 4, cudaMemcpyDeviceToDevice, c.s));
+    if (d_val) CK(cudaMemcpyAsync(d_val, c.d.val, ns * c.L * 4, cudaMemcpyDeviceToDevice, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+
+int sm2d_set_source_accounting(sm2d_handle h, const double* v7) {
+    if (!h || !v7) return fail(SM2D_ERR_ARG, "null argument");
+    Ctx& c = *h;
+    int rc = sync_state(c);
+    if (rc) return rc;
+    LaneState& L = c.ls_host[0];
+    L.src_inj_w = (float)v7[0];
+    L.src_oog_w = (float)v7[1];
+    L.src_slot_w = (float)v7[2];
+    L.src_inj_e = v7[3];
+    L.src_oog_e = v7[4];
+    L.src_slot_e = v7[5];
+    L.src_rep_loss = v7[6];
+    L.include_source = 1;
+    return push_state(c);
+}
+
 int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse) {
     if (!h) return fail(SM2D_ERR_ARG, "null handle");
     Ctx& c = *h;

