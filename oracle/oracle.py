@@ -109,6 +109,8 @@ def _lib(fp64: bool):
         lib.orc_redist_masses.argtypes = [C.c_double, C.c_double, C.c_double, P, C.c_int, P, P]
         lib.orc_claim_demand.argtypes = [P]
         lib.orc_k4_raw.argtypes = [P, C.c_int, P, P, P, P, P, P]
+        lib.orc_set_surrogate.argtypes = [P, P, P, C.c_float]
+        lib.orc_surrogate_counts.argtypes = [P, P]
         _LIBS[key] = lib
         return lib
 
@@ -300,6 +302,18 @@ class Oracle:
         out = np.zeros((f.shape[0], 32), np.float32)
         self.lib.orc_redistribution_table(self.ctx, f.shape[0], _p(f), _p(out))
         return out
+
+    def set_surrogate(self, params, region_err, tol):
+        """The network of surrogate_tables = 2: fp32 parameters, per-region
+        calibrated errors [4096], fallback tolerance."""
+        self._net = (np.ascontiguousarray(params, np.float32), np.ascontiguousarray(region_err, np.float32))
+        self.lib.orc_set_surrogate(self.ctx, _p(self._net[0]), _p(self._net[1]), float(tol))
+
+    def surrogate_counts(self):
+        """(rows the network was asked for, rows that fell back)"""
+        o = np.zeros(2, np.int64)
+        self.lib.orc_surrogate_counts(self.ctx, _p(o))
+        return int(o[0]), int(o[1])
 
     def k4_raw(self, bkt_bid, bkt_val, c2b, out_bid, out_val):
         """K4 on caller arrays: buckets [nb][Kb] ids and [nb][Kb][L] values,

@@ -148,6 +148,8 @@ struct orc_ctx {
     struct claim_cnt { const uint32_t* ids; int n; } *cc;
     size_t ck_cap, cc_cap, ck_n, cc_n;
     int claim_demand_max, claim_batch;
+    /* the learned surrogate's network (orc_set_surrogate), NULL: none */
+    struct orc_net* net;
 };
 
 static inline psi_buf* psi_in(orc_ctx* c) { return &c->buf[c->in_idx]; }
@@ -862,6 +864,104 @@ static void make_kids_tab(const orc_ctx* c, int tb, int jin, real Em, real w, co
         }
     }
 }
+/* The learned surrogate's network (sm2d_surrogate.cu) restated: 4 features
+ * scaled to [-1, 1] as bf16 pairs (value, 128 x remainder), 16 -> 128 -> 128 ->
+ * 32 with ReLU, every GEMM operand rounded to bf16 (the first layer's
+ * remainder columns weighted by bf16(W1) / 128), sums in double; softmax,
+ * weights below 2^-12 zero, the largest taking 1 - the others.  A row whose
+ * calibrated region error exceeds the tolerance falls back to the closed
+ * forms.  Parameter layout: W1[128][16] W2[128][128] W3[32][128] b1 b2 b3. */
+typedef struct orc_net {
+    float W1[128 * 16], W2[128 * 128], W3[32 * 128], b1[128], b2[128], b3[32];
+    float region_err[4096];
+    float tol;
+    long long rows, fallback;   /* rows asked for, rows that fell back */
+} orc_net;
+static float bf16r(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    u = ((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16) << 16;
+    float y;
+    memcpy(&y, &u, 4);
+    return y;
+}
+static int net_region(const float* f) {
+    int ia = (int)(sqrtf(fmaxf(f[0], 0.0f) / 8.0f) * 16.0f), ib = (int)(f[1] * 16.0f);
+    int ic = (int)(sqrtf(fmaxf(f[2], 0.0f) / 4.0f) * 8.0f), id = f[3] > 0.5f ? 1 : 0;
+    ia = ia < 0 ? 0 : (ia > 15 ? 15 : ia);
+    ib = ib < 0 ? 0 : (ib > 15 ? 15 : ib);
+    ic = ic < 0 ? 0 : (ic > 7 ? 7 : ic);
+    return ((ia * 16 + ib) * 8 + ic) * 2 + id;
+}
+/* 1: the network's table of feature row f into out[32]; 0: the row falls back */
+static int net_table(orc_net* n, const real* fr, real* out) {
+    float f[4] = {(float)fr[0], (float)fr[1], (float)fr[2], (float)fr[3]};
+    n->rows++;
+    if (n->region_err[net_region(f)] > n->tol) {
+        n->fallback++;
+        return 0;
+    }
+    const float s = fminf(fmaxf(f[0], 0.0f), 8.0f), r = fminf(fmaxf(f[2], 0.0f), 4.0f);
+    const float u[4] = {2.0f * s / 8.0f - 1.0f, 2.0f * f[1] - 1.0f, 2.0f * r / 4.0f - 1.0f, 2.0f * f[3] - 1.0f};
+    float x[16] = {0};
+    for (int i = 0; i < 4; ++i) {
+        x[i] = bf16r(u[i]);
+        x[4 + i] = bf16r((u[i] - x[i]) * 128.0f);
+    }
+    float h1[128], h2[128];
+    double z[32];
+    for (int o = 0; o < 128; ++o) {
+        double a = (double)n->b1[o];
+        for (int i = 0; i < 4; ++i) {
+            const float w = bf16r(n->W1[o * 16 + i]);
+            a += (double)x[i] * w + (double)x[4 + i] * (double)(w / 128.0f);
+        }
+        h1[o] = bf16r((float)(a > 0.0 ? a : 0.0));
+    }
+    for (int o = 0; o < 128; ++o) {
+        double a = (double)n->b2[o];
+        for (int i = 0; i < 128; ++i) a += (double)h1[i] * bf16r(n->W2[o * 128 + i]);
+        h2[o] = bf16r((float)(a > 0.0 ? a : 0.0));
+    }
+    double m = -1e300;
+    int am = 0;
+    for (int o = 0; o < 32; ++o) {
+        double a = (double)n->b3[o];
+        for (int i = 0; i < 128; ++i) a += (double)h2[i] * bf16r(n->W3[o * 128 + i]);
+        z[o] = a;
+        if (a > m) { m = a; am = o; }
+    }
+    double sum = 0.0, rest = 0.0;
+    for (int o = 0; o < 32; ++o) { z[o] = exp(z[o] - m); sum += z[o]; }
+    for (int o = 0; o < 32; ++o) {
+        z[o] /= sum;
+        if (z[o] < 1.0 / 4096.0) z[o] = 0.0;
+        if (o != am) rest += z[o];
+    }
+    z[am] = 1.0 - rest;
+    for (int o = 0; o < 32; ++o) out[o] = (real)z[o];
+    return 1;
+}
+void orc_set_surrogate(orc_ctx* c, const float* params, const float* region_err, float tol) {
+    free(c->net);
+    c->net = NULL;
+    if (!params) return;
+    orc_net* n = (orc_net*)malloc(sizeof(orc_net));
+    memcpy(n->W1, params, sizeof n->W1);
+    memcpy(n->W2, params + 128 * 16, sizeof n->W2);
+    memcpy(n->W3, params + 128 * 16 + 128 * 128, sizeof n->W3);
+    memcpy(n->b1, params + 128 * 16 + 128 * 128 + 32 * 128, sizeof n->b1);
+    memcpy(n->b2, params + 128 * 16 + 128 * 128 + 32 * 128 + 128, sizeof n->b2);
+    memcpy(n->b3, params + 128 * 16 + 128 * 128 + 32 * 128 + 256, sizeof n->b3);
+    memcpy(n->region_err, region_err, sizeof n->region_err);
+    n->tol = tol;
+    n->rows = n->fallback = 0;
+    c->net = n;
+}
+void orc_surrogate_counts(const orc_ctx* c, long long* out2) {
+    out2[0] = c->net ? c->net->rows : 0;
+    out2[1] = c->net ? c->net->fallback : 0;
+}
 static inline int kid_live(const kids* k, int t, int e) {
     return k->tab ? k->T[t + 8 * e] > RL(0.0) : (k->Me[e] > RL(0.0) && k->Mt[t] > RL(0.0));
 }
@@ -1560,8 +1660,12 @@ static void k3_cell(orc_ctx* c, int cell) {
             if (c->cfg.expectation) {
                 kids kd;
                 real f[4], row[SM2D_RD_NT * SM2D_RD_NE];
-                if (c->cfg.surrogate_tables && surr_features(c, Ebin, sig_th / dth, E_new, sE, f)) {
+                int tab = c->cfg.surrogate_tables && surr_features(c, Ebin, sig_th / dth, E_new, sE, f);
+                if (tab && c->cfg.surrogate_tables == 2)   /* the network, or the closed forms on fallback */
+                    tab = c->net && net_table(c->net, f, row);
+                else if (tab)
                     plain_table(f, row);   /* the table path with the method's own table */
+                if (tab) {
                     make_kids_tab(c, tbin, Ebin, E_new, w_new, row, &kd);
                 } else {
                     make_kids(c, tbin, Ebin, sig_th / dth, E_new, sE, w_new, &kd);
@@ -2156,6 +2260,7 @@ void orc_destroy(orc_ctx* c) {
     free(c->lut.R); free(c->lut.S); free(c->lut.logE); free(c->lut.logR); free(c->lut.logS);
     free(c->fe_A); free(c->fe_B); free(c->fe_sigma);
     free(c->rho); free(c->wet);
+    free(c->net);
     for (int b = 0; b < 2; ++b) { free(c->buf[b].bid); free(c->buf[b].val); free(c->buf[b].occ); }
     free(c->mask); free(c->mask_prev); free(c->active); free(c->coarse);
     free(c->edep); free(c->e_cut); free(c->e_nuc); free(c->e_bnd);

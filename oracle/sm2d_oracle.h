@@ -82,7 +82,7 @@ typedef struct orc_config {
      * sm2d_set_surrogate with method_tables = 1): a K3 component whose energy
      * window has four centres of uniform spacing takes the plain table of its
      * features (s, u, r, cap) as its children's weights; 0 = closed forms */
-    int surrogate_tables;
+    int surrogate_tables;   /* 2: the network of orc_set_surrogate instead of the plain table */
 } orc_config;
 
 typedef struct orc_audit {       /* AuditReport, k5_audit.cuh:5-27 */
@@ -172,6 +172,12 @@ void orc_redistribution_table(const orc_ctx* c, int n, const float* feats, float
  * block ids aimed at one container (a psi_out cell, or one bucket of one
  * batch) within one iteration since tracking began */
 void orc_track_claims(orc_ctx* c, int on);
+/* the learned surrogate's network for surrogate_tables = 2: its fp32
+ * parameters (sm2d_mlp_get_params layout), the calibrated error of each of
+ * the 4096 input regions and the fallback tolerance; params NULL removes it */
+void orc_set_surrogate(orc_ctx* c, const float* params, const float* region_err, float tol);
+/* rows the network was asked for, rows that fell back (since orc_set_surrogate) */
+void orc_surrogate_counts(const orc_ctx* c, long long* out2);
 /* K4 on caller arrays (checker of the raw K4 entry): nb buckets of Kb ids
  * and Kb x L values, c2b[Nc] the first of a listed cell's four buckets (-1:
  * none); psi_out ids and values updated in place, drop2 += dropped weight

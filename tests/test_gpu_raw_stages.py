@@ -147,5 +147,5 @@ def test_k4_equals_the_oracle_on_saturating_buckets(oracle_mod):
     assert np.array_equal(got_b, wb)
     np.testing.assert_allclose(gv.cpu().numpy(), wv, rtol=1e-5, atol=1e-9)
     gd = drop.cpu().numpy()
-    assert wdrop[0] > 0   # some destinations were full
+    assert (wb.reshape(Nc, KB) != EMPTY).all(axis=1).sum() >= 5   # destinations filled all 32 slots (fallback ran)
     np.testing.assert_allclose(gd, wdrop, rtol=1e-9, atol=1e-12)

@@ -9,10 +9,14 @@ sm2d_redist.h (the per-bin redistribution of k3_finetransport.cu:263-366).
   dose within 1e-4 of its maximum, the same Bragg-peak row.
 * With a network whose every region falls back (tolerance 0 on an untrained
   network), the run equals the expectation form without the surrogate.
-* With the trained network: every row's weights sum to 1, so the weight audit
-  passes every iteration; energy is conserved; the dose stays close to the
-  closed forms', and its error against the FP64 oracle of the expectation
-  form is stated.
+* With the trained network: the oracle running the same network (the C
+  restatement of its arithmetic, sums in double) gives the same iteration
+  count and dose within 1e-3 of its maximum; every row's weights sum to 1, so
+  weight is conserved to 1e-6 of the injected weight over the run and energy
+  to 1e-6 of the injected energy; the dose error against the FP64 oracle of
+  the closed forms is stated and bounded (the network's angular weights for
+  steps of 1-3 angle bins move the Bragg peak by a fraction of a row on the
+  40 MeV beam: about 9 % of the peak cell dose, 4 % in depth dose).
 """
 import numpy as np
 import pytest
@@ -74,7 +78,7 @@ def trained():
     s.set_params(so.init_params())
     f = s.features(1 << 21, 101)
     s.train(f, s.plain(f), steps=6000)
-    s.calibrate(s.features(1 << 20, 102))
+    s.region_err = s.calibrate(s.features(1 << 20, 102))
     yield s
     s.close()
 
@@ -96,8 +100,14 @@ def test_trained_network_in_the_transport(trained, oracle_mod, E0, sx):
         st = b.surrogate_stats()
     assert 0 < nb < bench.MAX_IT and abs(nb - na) <= 2, (na, nb)
     assert st["rows"] > 1000 and st["fallback_rows"] < st["rows"] and st["overflow_bins"] == 0, st
-    # every row sums to 1: no iteration fails the weight audit
-    assert all(h["W_pass"] for h in hist), [h["W_error"] for h in hist if not h["W_pass"]][:5]
+    # every row sums to 1: the weight audit fails on rounding at most rarely,
+    # and the run's weight balance closes
+    fails = sum(1 for h in hist if not h["W_pass"])
+    assert fails <= 0.02 * len(hist) and max(h["W_error"] for h in hist) < 1e-5, fails
+    wsum = (tal["w_cut"].astype(np.float64).sum() + tal["w_nuc"].astype(np.float64).sum()
+            + tal["w_bnd"].astype(np.float64).sum() + sc["transport_dropped_weight"])
+    w_in = sc["source_injected_weight"] - sc["source_out_of_grid_weight"] - sc["source_slot_dropped_weight"]
+    assert abs(wsum - w_in) <= 1e-6 * sc["source_injected_weight"], (wsum, w_in)
     # energy: deposits, cutoff, nuclear and boundary losses and drops add up to
     # the injected energy (less what the source could not represent)
     total = (tal["edep"].sum() + tal["e_cut"].sum() + tal["e_nuc"].sum() + tal["e_bnd"].sum()
@@ -113,8 +123,18 @@ def test_trained_network_in_the_transport(trained, oracle_mod, E0, sx):
     err64 = float(np.abs(db - ref64).max() / ref64.max())
     err64_closed = float(np.abs(da - ref64).max() / ref64.max())
     pdd_err = float(np.abs(db.sum(1) - ref64.sum(1)).max() / ref64.sum(1).max())
-    print(f"surrogate transport E0={E0}: rows {st['rows']}, fallback {st['fallback_rows'] / st['rows']:.3f}, "
-          f"dose vs closed forms {err_closed:.2e}, vs FP64 {err64:.2e} (closed forms {err64_closed:.2e}), "
+    # the oracle with the same network and calibration
+    on = oracle_mod.Oracle(dict(cfg.oracle_config(), surrogate_tables=2), cfg.theta_edges, cfg.E_edges)
+    on.set_surrogate(trained.params(), trained.region_err, 0.005)
+    on.inject(**beam)
+    n_on = on.run(bench.MAX_IT)
+    ref_net = _oracle_dose(oracle_mod, on, cfg)
+    err_net = float(np.abs(db - ref_net).max() / ref_net.max())
+    rows_on, fb_on = on.surrogate_counts()
+    print(f"surrogate transport E0={E0}: rows {st['rows']}, fallback {st['fallback_rows'] / st['rows']:.3f} "
+          f"(oracle {rows_on}, {fb_on / max(rows_on, 1):.3f}), dose vs oracle with the network {err_net:.2e}, "
+          f"vs closed forms {err_closed:.2e}, vs FP64 {err64:.2e} (closed forms {err64_closed:.2e}), "
           f"PDD vs FP64 {pdd_err:.2e}")
+    assert n_on == nb and err_net <= 1e-3, (n_on, nb, err_net)
     assert abs(sm.bragg_peak_row(db) - sm.bragg_peak_row(ref64)) <= 1
-    assert pdd_err <= 0.1 and err64 <= 0.2, (pdd_err, err64)
+    assert pdd_err <= 0.05 and err64 <= 0.12, (pdd_err, err64)
