@@ -79,6 +79,8 @@ def make_config(grid: str, workload: str = "plan512", method: str = "sampled"):
         cfg.energy_split = 1
         cfg.expectation = 1
         cfg.production()
+    if method == "precision":
+        cfg.precision_form = 1
     return cfg
 
 
@@ -136,7 +138,8 @@ def oracle_problem(grid: str, workload: str = "plan512", method: str = "sampled"
                weight_active_min=1e-12, step_coarse=5.0, sigma_x_initial=sx, E0=E0, enable_straggling=1,
                enable_nuclear=1, seed_slot_mode=1, energy_split=split, grid_E_min=0.1, grid_E_max=250.0,
                prune_coarse=0.0, prune_fine=0.0, split_min_weight=1e-7 if split else 0.0,
-               stop_weight_fraction=1e-6, floor_cutoff=1, seed_iteration_salt=1, expectation=expect, **layout)
+               stop_weight_fraction=1e-6, floor_cutoff=1, seed_iteration_salt=1, expectation=expect,
+               precision_form=1 if method == "precision" else 0, **layout)
     return cfg, th, ee, rho
 
 
@@ -653,6 +656,12 @@ def run_gpu_arm(args):
         extra["expectation"]["method"] = ("expectation form: K2/K3 emit the expected re-binning of their MCS angle "
                                           "and straggling loss (up to 15 theta x 4 E children per component) "
                                           "instead of one hashed draw; energy split")
+        # the precision form on its own workload (C3: 230 MeV through the slab
+        # phantom, 64 spots): weight increments in the audit, the R-LUT
+        # inverted in double below 10 MeV; and on the 512-spot plan
+        extra["precision"] = plan_rate(args.grid, "c3", 64, 0, 2, 1, "precision", accuracy=True)
+        extra["precision"]["workload"] = workload_desc("c3", args.grid, 64)
+        extra["precision_plan512"] = plan_rate(args.grid, args.workload, n, 0, 2, 1, "precision", accuracy=True)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -105,6 +105,15 @@ typedef struct sm2d_problem {
      * result no longer depends on random seeds or on arithmetic rounding
      * through them. */
     int expectation;
+    /* precision form (no counterpart in the reference): 1 books each
+     * iteration's cutoff, nuclear and boundary weight in the K5 audit from the
+     * iteration's own per-cell increments, instead of the difference of the
+     * cumulative float tallies (whose rounding, relative to the cumulative
+     * weight, otherwise enters the iteration's balance), and inverts the
+     * R-LUT (range -> energy) in double below 10 MeV, where a step's energy
+     * loss is a small difference of large ranges.  psi, the transport
+     * arithmetic and the per-cell tallies stay as they are. */
+    int precision_form;
 } sm2d_problem;
 
 typedef struct sm2d_beam {

@@ -36,7 +36,7 @@ class OrcConfig(C.Structure):
         ("split_min_weight", C.c_float), ("stop_weight_fraction", C.c_float),
         ("claim_reserve_weight", C.c_float), ("slots_per_cell", C.c_int),
         ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int), ("expectation", C.c_int),
-        ("surrogate_tables", C.c_int),
+        ("surrogate_tables", C.c_int), ("precision_form", C.c_int),
     ]
 
 
@@ -189,7 +189,7 @@ class Oracle:
                         weight_active_min=1e-12, step_coarse=5.0, sigma_x_initial=0.0, E0=0.0,
                         enable_straggling=1, enable_nuclear=1, seed_slot_mode=0, energy_split=0,
                         grid_E_min=0.0, grid_E_max=0.0, prune_coarse=0.0, prune_fine=0.0, split_min_weight=0.0, stop_weight_fraction=0.0, claim_reserve_weight=0.0, slots_per_cell=32, floor_cutoff=0, seed_iteration_salt=0, expectation=0,
-                        surrogate_tables=0)
+                        surrogate_tables=0, precision_form=0)
         defaults.update(cfg)
         for name, _ in OrcConfig._fields_:
             setattr(c, name, defaults[name])

@@ -93,6 +93,8 @@ typedef struct rlut {             /* DeviceRLUT, device_lut.cuh:16-26 */
     float Emin, Emax;
     real *R, *S, *logE, *logR, *logS;
     const real* edges;
+    int precise;                  /* precision form: invert in double below R_prec = R(10 MeV) */
+    real R_prec;
 } rlut;
 
 typedef struct psi_buf {
@@ -122,6 +124,7 @@ struct orc_ctx {
     float *w_cut, *w_nuc, *w_bnd;
     double *p_edep, *p_e_cut, *p_e_nuc, *p_e_bnd;
     float *p_w_cut, *p_w_nuc, *p_w_bnd;
+    float *dw_cut, *dw_nuc, *dw_bnd;   /* this iteration's weight increments (precision form) */
     /* bucket scratch for the current batch */
     bucket* buckets;
     int n_buckets_cap;
@@ -449,6 +452,13 @@ static real lut_E_inverse(const rlut* l, real Rin) {
     int b = lo;
     if (b > l->N - 2) b = l->N - 2;
     if (b < 0) b = 0;
+    if (l->precise && Rin < l->R_prec) {   /* precision form: the interpolation in double */
+        const double dl = (double)l->logR[b + 1] - (double)l->logR[b];
+        if (fabs(dl) < 1e-10) return (real)(float)exp((double)l->logE[b]);
+        const double le = (double)l->logE[b] +
+                          ((double)l->logE[b + 1] - (double)l->logE[b]) * (log((double)Rin) - (double)l->logR[b]) / dl;
+        return (real)(float)exp(le);
+    }
     real lr = r_log(Rin);
     real dlr = l->logR[b + 1] - l->logR[b];
     if (r_fabs(dlr) < RL(1e-10)) return r_exp(l->logE[b]);
@@ -1418,6 +1428,9 @@ static void emit_cross(orc_ctx* c, int k3, int cell, int face, real theta_new, r
 }
 
 static void commit_tally(orc_ctx* c, int cell, const tally* t) {
+    c->dw_cut[cell] += t->w_cut;
+    c->dw_nuc[cell] += t->w_nuc;
+    c->dw_bnd[cell] += t->w_bnd;
     c->edep[cell] += t->edep;
     c->w_cut[cell] += t->w_cut;
     c->e_cut[cell] += t->e_cut;
@@ -1845,9 +1858,10 @@ static void k5(orc_ctx* c, float drop_w, double drop_e, int include_source) {
                 }
             }
         }
-        float Wc = fmaxf(0.0f, c->w_cut[cell] - c->p_w_cut[cell]);
-        float Wn = fmaxf(0.0f, c->w_nuc[cell] - c->p_w_nuc[cell]);
-        float Wb = fmaxf(0.0f, c->w_bnd[cell] - c->p_w_bnd[cell]);
+        const int pf = c->cfg.precision_form;
+        float Wc = fmaxf(0.0f, pf ? c->dw_cut[cell] : c->w_cut[cell] - c->p_w_cut[cell]);
+        float Wn = fmaxf(0.0f, pf ? c->dw_nuc[cell] : c->w_nuc[cell] - c->p_w_nuc[cell]);
+        float Wb = fmaxf(0.0f, pf ? c->dw_bnd[cell] : c->w_bnd[cell] - c->p_w_bnd[cell]);
         double Ed = fmax(0.0, c->edep[cell] - c->p_edep[cell]);
         double En = fmax(0.0, c->e_nuc[cell] - c->p_e_nuc[cell]);
         double Eb = fmax(0.0, c->e_bnd[cell] - c->p_e_bnd[cell]);
@@ -2006,6 +2020,9 @@ int orc_step(orc_ctx* c) {
     c->transport_drop_e += de;
     k5(c, (float)dw, de, c->iter == 1);
     memcpy(c->p_w_cut, c->w_cut, sizeof(float) * c->Nc);
+    memset(c->dw_cut, 0, sizeof(float) * c->Nc);
+    memset(c->dw_nuc, 0, sizeof(float) * c->Nc);
+    memset(c->dw_bnd, 0, sizeof(float) * c->Nc);
     memcpy(c->p_e_cut, c->e_cut, sizeof(double) * c->Nc);
     memcpy(c->p_w_nuc, c->w_nuc, sizeof(float) * c->Nc);
     memcpy(c->p_w_bnd, c->w_bnd, sizeof(float) * c->Nc);
@@ -2218,6 +2235,9 @@ orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* th_edges, i
         for (int i = 0; i < N_E; ++i) (*dst[k])[i] = (real)tmp[k * N_E + i];
     }
     c->lut.edges = c->E_edges;
+    c->lut.precise = 0;
+    c->lut.R_prec = lut_R(&c->lut, r_max(RL(10.0), (real)c->lut.Emin));
+    c->lut.precise = cfg->precision_form ? 1 : 0;
     free(rep);
     free(tmp);
     c->fe_A = (float*)calloc(cfg->Nz, sizeof(float));
@@ -2249,6 +2269,9 @@ orc_ctx* orc_create(const orc_config* cfg, int N_theta, const float* th_edges, i
     c->p_w_cut = (float*)calloc(c->Nc, sizeof(float));
     c->p_w_nuc = (float*)calloc(c->Nc, sizeof(float));
     c->p_w_bnd = (float*)calloc(c->Nc, sizeof(float));
+    c->dw_cut = (float*)calloc(c->Nc, sizeof(float));
+    c->dw_nuc = (float*)calloc(c->Nc, sizeof(float));
+    c->dw_bnd = (float*)calloc(c->Nc, sizeof(float));
     c->cell_to_bucket = (int*)malloc(sizeof(int) * c->Nc);
     for (int i = 0; i < c->Nc; ++i) c->cell_to_bucket[i] = -1;
     return c;
@@ -2267,6 +2290,7 @@ void orc_destroy(orc_ctx* c) {
     free(c->w_cut); free(c->w_nuc); free(c->w_bnd);
     free(c->p_edep); free(c->p_e_cut); free(c->p_e_nuc); free(c->p_e_bnd);
     free(c->p_w_cut); free(c->p_w_nuc); free(c->p_w_bnd);
+    free(c->dw_cut); free(c->dw_nuc); free(c->dw_bnd);
     for (int i = 0; i < c->n_buckets_cap; ++i) {
         free(c->buckets[i].val);
         free(c->buckets[i].bid);

@@ -83,6 +83,10 @@ typedef struct orc_config {
      * window has four centres of uniform spacing takes the plain table of its
      * features (s, u, r, cap) as its children's weights; 0 = closed forms */
     int surrogate_tables;   /* 2: the network of orc_set_surrogate instead of the plain table */
+    /* precision form: the audit books each iteration's cutoff, nuclear and
+     * boundary weight from the iteration's own per-cell increments, and the
+     * R-LUT is inverted in double below 10 MeV; 0 = reference */
+    int precision_form;
 } orc_config;
 
 typedef struct orc_audit {       /* AuditReport, k5_audit.cuh:5-27 */

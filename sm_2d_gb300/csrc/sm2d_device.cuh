@@ -196,6 +196,10 @@ struct Dev {
     float4* brec2;        // expectation form, per bin: sigma_theta / dtheta, straggling sigma,
                           // the bin's row of the surrogate's tables (int bits, -1: none)
     int expect;           // 1: expectation form (redistribution weights instead of draws)
+    // precision form: weight tallies booked as increments in the audit, the
+    // R-LUT inverted in double below R_prec = lut_range(10 MeV)
+    int precise;
+    float R_prec;
     // expectation form with the learned surrogate: the claim pass gives each
     // K3 bin inside the network's domain a row (its feature row (s, u, r,
     // cap) and its bin-list entry) and leaves its claims for later; the
@@ -269,6 +273,13 @@ __device__ __forceinline__ float lut_energy_of_range(const Dev& d, float r) {
     int lo = d.r_slot[slot_of(r, d.r_base, d.r_nslot)];   // first index with R[lo] >= r
     while (lo < d.lutN && d.R[lo] < r) ++lo;
     int b = max(0, min(lo, d.lutN - 2));
+    if (d.precise && r < d.R_prec) {   // precision form: the interpolation in double below 10 MeV
+        const double dl = (double)d.logR[b + 1] - (double)d.logR[b];
+        if (fabs(dl) < 1e-10) return (float)exp((double)d.logE[b]);
+        const double le =
+            (double)d.logE[b] + ((double)d.logE[b + 1] - (double)d.logE[b]) * (log((double)r) - (double)d.logR[b]) / dl;
+        return (float)exp(le);
+    }
     float lr = sm2d_logf(r);
     float dl = d.logR[b + 1] - d.logR[b];
     if (fabsf(dl) < 1e-10f) return sm2d_expf(d.logE[b]);

@@ -1073,7 +1073,9 @@ __device__ __forceinline__ double fold_tally(const Dev& d, int c, int k) {
     const float w0 = cum[c], w1 = w0 + x;
     cum[c] = w1;
     dl[c] = 0.0f;
-    return (double)fmaxf(0.0f, w1 - w0);
+    // the precision form books the increment itself (its rounding is its own,
+    // not the cumulative tally's)
+    return (double)fmaxf(0.0f, d.precise ? x : w1 - w0);
 }
 
 // K5 audit of the iteration, warp per cell of psi_in's list (whose storage
@@ -1889,6 +1891,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     d.floor_cutoff = p->floor_cutoff;
     d.salt = p->seed_iteration_salt;
     d.expect = p->expectation ? 1 : 0;
+    d.precise = p->precision_form ? 1 : 0;
     const size_t Nc = (size_t)d.Nc, NcB = Nc * B, ns = NcB * kKb;
     void* q;
     int rc;
@@ -2031,6 +2034,11 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
         float* rf = static_cast<float*>(q1);
         k_eval_range<<<1, 1, 0, s>>>(d, fmaxf(p->E_fine_on, d.lutEmin), rf);
         if (cudaMemcpyAsync(&d.R_fine_on, rf, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return bail(fail(SM2D_ERR_CUDA, "LUT setup"));
+        // the range below which the precision form inverts the LUT in double
+        k_eval_range<<<1, 1, 0, s>>>(d, fmaxf(10.0f, d.lutEmin), rf);
+        if (cudaMemcpyAsync(&d.R_prec, rf, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return bail(fail(SM2D_ERR_CUDA, "LUT setup"));
         void* q2 = nullptr;

@@ -44,7 +44,7 @@ class Problem(C.Structure):
         ("max_iterations", C.c_int),
         ("prune_coarse", C.c_float), ("prune_fine", C.c_float), ("split_min_weight", C.c_float),
         ("stop_weight_fraction", C.c_float), ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
-        ("lanes", C.c_int), ("density_z", C.c_void_p), ("expectation", C.c_int),
+        ("lanes", C.c_int), ("density_z", C.c_void_p), ("expectation", C.c_int), ("precision_form", C.c_int),
     ]
 
 
@@ -285,6 +285,7 @@ class Config:
     lanes: int = 1          # spots transported together by Transport.batch_run
     density_z: np.ndarray = None   # slab phantom: density per depth row (None: water)
     expectation: int = 0    # 1: expectation form (redistribution weights instead of MCS/straggling draws)
+    precision_form: int = 0  # 1: audit books weight increments; R-LUT inverted in double below 10 MeV
 
     def production(self):
         """Options of a production run: deterministic rank-ordered seeds salted
@@ -318,6 +319,7 @@ class Config:
                     split_min_weight=self.split_min_weight, stop_weight_fraction=self.stop_weight_fraction,
                     floor_cutoff=self.floor_cutoff, seed_iteration_salt=self.seed_iteration_salt, lanes=self.lanes,
                     density_z=None if rho is None else rho.ctypes.data, expectation=self.expectation,
+                    precision_form=self.precision_form,
                     **self.layout)
         return p, (th, E, rho)
 
@@ -332,7 +334,8 @@ class Config:
                     grid_E_min=self.E_min, grid_E_max=self.E_max, prune_coarse=self.prune_coarse,
                     prune_fine=self.prune_fine, split_min_weight=self.split_min_weight,
                     stop_weight_fraction=self.stop_weight_fraction, floor_cutoff=self.floor_cutoff,
-                    seed_iteration_salt=self.seed_iteration_salt, expectation=self.expectation, **self.layout)
+                    seed_iteration_salt=self.seed_iteration_salt, expectation=self.expectation,
+                    precision_form=self.precision_form, **self.layout)
 
     @staticmethod
     def reference_runner(Nx, Nz, dx, dz, N_theta=36, E_fine_on=10.0, E_fine_off=11.0, **kw):
