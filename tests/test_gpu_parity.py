@@ -265,3 +265,34 @@ def test_async_spot_pipeline_matches_blocking_api():
         assert n_it == n_ref and per * (n_it + 1) <= launches <= per * (n_it + 16)
         assert passes == n_it   # one lane: a pass per iteration
         assert ms["transport"] > 0 and all(v >= 0 for v in ms.values())
+
+
+@pytest.mark.parametrize("name", ["A", "B", "C", "D"])
+def test_ten_iterations_match_reference_gpu_build_per_bin(name):
+    """The engine against the reference tree's own GPU build (its dumps of ten
+    iterations of the four validation cases, tests/golden/ref_gpu/): each
+    iteration from the dumped phase space of the one before, every bin of more
+    than 1e-8 weight on both sides with the same cell, block id and local bin,
+    weights within 2e-8 + 1e-3 of themselves (the bars of
+    tests/test_oracle_golden.py, which explains them)."""
+    import os
+    from golden_cases import read_rows, rows_to_dense
+    ref = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_gpu", f"case_{name}")
+    case = load_case(name)
+    Nc, L = case["cfg"]["Nx"] * case["cfg"]["Nz"], case["L"]
+    with sm.Transport(_gpu_cfg(case)) as t:
+        for k in range(1, 11):
+            if k == 1:
+                b = case["beam"]
+                t.inject(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
+                         b["n_samples"], b["seed"])
+            else:
+                rows = read_rows(os.path.join(ref, f"debug_ps_raw_iter_{k - 1:02d}_after_K4.csv"))
+                t.set_psi_in(*rows_to_dense(rows, Nc, L))
+            t.step()
+            got = _rows(*t.psi_in(), t.L, thresh=0.0)
+            want = row_key_sets(read_rows(os.path.join(ref, f"debug_ps_raw_iter_{k:02d}_after_K4.csv")))
+            heavy = {x for x in set(got) | set(want) if max(got.get(x, 0.0), want.get(x, 0.0)) > 1e-8}
+            assert heavy <= set(got) and heavy <= set(want), (name, k)
+            for x in heavy:
+                assert abs(got[x] - want[x]) <= 2e-8 + 1e-3 * want[x], (name, k, x, got[x], want[x])

@@ -1,30 +1,23 @@
 """Pins the CPU oracle to the reference's own outputs (no GPU needed).
 
-* injection rows of results/one_step_case_{A..D}: bit-exact keys, weights to
-  the dump's 8-decimal print precision;
-* one K1..K6 iteration from the dumped input: per-cell weight, and the weight
-  marginalised over theta for every (cell, energy bin, x_sub, z_sub), to the
-  print precision; the channel totals to their 6 printed digits.  The theta
-  neighbour rows of the dumps come from a build whose MCS draw differs from
-  the reference tree's seed formula, so rows are compared theta-marginal.
+* injection rows of results/one_step_case_{A..D} (the reference repository's
+  dumps): bit-exact keys, weights to the dump's print precision;
+* ten K1..K6 iterations of the same four cases dumped by the reference tree's
+  own GPU build, compiled for sm_103a and run on a GB300
+  (tests/golden/ref_gpu/, tests/golden/make_golden_gpu.py): each iteration
+  from the dumped phase space of the one before (the injection for the first),
+  compared per bin -- cell, block id and local bin (angle, energy, sub-cell
+  position) -- not marginalised over any coordinate; and the first
+  iteration's channel totals.
 """
+import os
+
 import numpy as np
 import pytest
 
-from golden_cases import load_case, row_key_sets
+from golden_cases import load_case, read_channels, read_rows, row_key_sets, rows_to_dense
 
 CASES = "ABCD"
-
-
-def _marginal(rows, nt=4, ne=2, nxs=8):
-    out = {}
-    for (cell, bid, lidx), w in rows.items():
-        bE = (bid >> 12) & 0xFFF
-        el = (lidx // nt) % ne
-        rest = lidx // (nt * ne)
-        key = (cell, bE * ne + el, rest)
-        out[key] = out.get(key, 0.0) + w
-    return out
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -47,61 +40,90 @@ def test_injection_matches_reference_dump(oracle_mod, name):
                - ch[(1, "source_representation_loss_energy")]) < 2e-6
 
 
-@pytest.mark.parametrize("name", CASES)
-def test_one_step_matches_reference_dump(oracle_mod, name):
-    case = load_case(name)
+REF_GPU = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_gpu")
+ITERATIONS = 10
+
+
+def _ref_rows(name, k):
+    stage = "initial" if k == 0 else "after_K4"
+    return row_key_sets(read_rows(os.path.join(REF_GPU, f"case_{name}", f"debug_ps_raw_iter_{k:02d}_{stage}.csv")))
+
+
+def _injected(oracle_mod, case):
     o = oracle_mod.Oracle(case["cfg"], case["theta_edges"], case["E_edges"])
-    o.set_psi_in(case["bid_in"], case["val_in"])
-    assert o.step() == 1
-    bid, val = o.psi_in()
-    got = row_key_sets(oracle_mod.psi_rows(bid, val, o.L, thresh=0.0))
-    want = row_key_sets(case["rows_out"])
-    # per-cell weight
-    cw_g, cw_w = {}, {}
-    for (c, _, _), w in got.items():
-        cw_g[c] = cw_g.get(c, 0.0) + w
-    for (c, _, _), w in want.items():
-        cw_w[c] = cw_w.get(c, 0.0) + w
-    assert set(cw_g) == set(cw_w)
-    for c in cw_w:
-        assert abs(cw_g[c] - cw_w[c]) <= 2e-8 * 4 + 1e-6 * cw_w[c], c
-    # theta-marginal (cell, E bin, x_sub/z_sub) weights
-    mg, mw = _marginal(got), _marginal(want)
-    for k, w in mw.items():
-        assert abs(mg.get(k, 0.0) - w) <= 5e-8 + 1e-6 * w, k
-    assert sum(v for k, v in mg.items() if k not in mw) < 1e-7
-    # channel totals
-    t = o.tallies()
-    s = o.scalars()
-    ch = case["channels"]
-    # The nuclear channel is w - w*exp(-sigma*s) in float: with s*sigma ~ 5e-4
-    # the subtraction keeps ~13 bits, so one ulp of expf (CUDA vs glibc)
-    # moves it by ~1e-4 relative.  Its tolerance is that cancellation bound.
-    for key, val_, rtol in [("EdepC", t["edep"].sum(), 5e-6),
+    b = case["beam"]
+    o.inject(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
+             b["n_samples"], b["seed"])
+    return o
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_injection_matches_reference_gpu_build(oracle_mod, name):
+    case = load_case(name)
+    o = _injected(oracle_mod, case)
+    got = row_key_sets(oracle_mod.psi_rows(*o.psi_in(), o.L))
+    want = _ref_rows(name, 0)
+    assert set(got) == set(want)
+    for k, w in want.items():
+        assert abs(got[k] - w) <= 6e-7 + 1e-7 * w, k   # the initial dump prints 6 decimals
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_ten_iterations_match_reference_gpu_build_per_bin(oracle_mod, name):
+    """Every bin holding more than 1e-8 of weight on either side is on both
+    (the same cell, block id and local bin: the MCS and straggling draws of the
+    reference's hashed seeds land in the same bins), and its weight agrees to
+    1e-8 + 1e-3 of itself.  The inputs are the dumps' 8-decimal prints (5e-9
+    per bin).  The reference evaluates log, cos, sin and erf with CUDA's
+    functions and this oracle with sm2d_math.h (within 2 ulp of them); the
+    variance-preserving split of a sampled angle between two bins multiplies
+    such differences by 1 / bin width, which on the 360-bin grid of case D
+    reaches 1.7e-4 of a bin's weight; and the dumps' rounding, propagated through
+    a step, reaches 1.04e-8 on a bin of 2.3e-7."""
+    case = load_case(name)
+    Nc, L = case["cfg"]["Nx"] * case["cfg"]["Nz"], case["L"]
+    for k in range(1, ITERATIONS + 1):
+        if k == 1:
+            o = _injected(oracle_mod, case)
+        else:
+            o = oracle_mod.Oracle(case["cfg"], case["theta_edges"], case["E_edges"])
+            rows = read_rows(os.path.join(REF_GPU, f"case_{name}", f"debug_ps_raw_iter_{k - 1:02d}_after_K4.csv"))
+            o.set_psi_in(*rows_to_dense(rows, Nc, L))
+        assert o.step() == 1
+        got = row_key_sets(oracle_mod.psi_rows(*o.psi_in(), o.L, thresh=0.0))
+        want = _ref_rows(name, k)
+        heavy = {x for x in set(got) | set(want) if max(got.get(x, 0.0), want.get(x, 0.0)) > 1e-8}
+        assert heavy <= set(got) and heavy <= set(want), (name, k, sorted(heavy - set(got))[:3],
+                                                          sorted(heavy - set(want))[:3])
+        for x in heavy:
+            assert abs(got[x] - want[x]) <= 2e-8 + 1e-3 * want[x], (name, k, x, got[x], want[x])
+        assert abs(sum(got.values()) - sum(want.values())) <= 1e-6 * sum(want.values()) + 1e-6, (name, k)
+        o.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_channel_totals_match_reference_gpu_build(oracle_mod, name):
+    """The totals file the reference writes at the end of its run (here ten
+    iterations from the injection), against the oracle's ten iterations."""
+    case = load_case(name)
+    o = _injected(oracle_mod, case)
+    assert o.run(ITERATIONS) == ITERATIONS
+    t, s = o.tallies(), o.scalars()
+    ch = read_channels(os.path.join(REF_GPU, f"case_{name}", "debug_channels_totals_iter01.csv"))
+    # the nuclear channel is w - w exp(-sigma s) in float: with sigma s ~ 5e-4
+    # the subtraction keeps ~13 bits, so one ulp of exp (CUDA vs sm2d_math.h)
+    # moves it by ~1e-4 relative; a coarse step's loss E - E(R(E) - s) at
+    # 150 MeV is 2.3 MeV, and one ulp of 150 MeV is 6.6e-6 of it, so ten steps
+    # of the pencil (case A) differ by up to 5.2e-5 in the deposit
+    for key, val_, rtol in [("EdepC", t["edep"].sum(), 1e-4),
                             ("AbsorbedWeight_nuclear", t["w_nuc"].sum(), 5e-4),
                             ("AbsorbedEnergy_nuclear", t["e_nuc"].sum(), 5e-4),
                             ("AbsorbedWeight_cutoff", t["w_cut"].sum(), 5e-6),
                             ("BoundaryLoss_weight", t["w_bnd"].sum(), 5e-6),
-                            ("transport_dropped_weight", s["transport_dropped_weight"], 5e-6)]:
+                            ("transport_dropped_weight", s["transport_dropped_weight"], 5e-6),
+                            ("source_injected_weight", s["source_injected_weight"], 1e-6)]:
         ref = ch[(1, key)]
         assert abs(val_ - ref) <= rtol * max(abs(ref), 1e-3), (key, val_, ref)
-    assert abs(s["audit_residual_energy"] - ch[(1, "transport_audit_residual_energy")]) < 2e-6 + 5e-4 * ch[(1, "AbsorbedEnergy_nuclear")]
-    a = o.audit()
-    assert a["W_pass"] == 1
-
-
-def test_theta_split_statistics_case_c(oracle_mod):
-    """The split neighbour weight is the per-component angular variance; its
-    total must agree with the dump's in distribution (sigma^2/dtheta^2)."""
-    case = load_case("C")
-    o = oracle_mod.Oracle(case["cfg"], case["theta_edges"], case["E_edges"])
-    o.set_psi_in(case["bid_in"], case["val_in"])
-    o.step()
-    bid, val = o.psi_in()
-    got = row_key_sets(oracle_mod.psi_rows(bid, val, o.L, thresh=0.0))
-    want = row_key_sets(case["rows_out"])
-    frac = lambda rows: sum(w for (c, b, l), w in rows.items() if l % 4 != 2) / sum(rows.values())
-    fg, fw = frac(got), frac(want)
-    expected = (1.2626e-3 / (0.7 / 36)) ** 2
-    assert 0.3 * expected < fg < 3 * expected
-    assert 0.3 * expected < fw < 3 * expected
+    res = ch[(1, "transport_audit_residual_energy")]
+    assert abs(s["audit_residual_energy"] - res) < 2e-6 + 5e-4 * ch[(1, "AbsorbedEnergy_nuclear")]
+    assert abs(s["source_representation_loss_energy"] - ch[(1, "source_representation_loss_energy")]) < 2e-6
