@@ -542,6 +542,9 @@ def run_gpu_arm(args):
     # before the timed region; each step transports the whole plan and
     # leaves the post-convolved dose of every spot in HBM
     t.plan_load(beams, MAX_IT, dose=True)
+    # the launch shape (blocks per SM of each pass kernel) from the autotuner,
+    # on this plan, before the timed region
+    shape, tune_ms = t.autotune() if not args.no_tune else (t.launch_shape(), None)
     for _ in range(max(args.warmup, 3)):
         t.plan_run_async()
     torch.cuda.synchronize()
@@ -696,6 +699,10 @@ def run_gpu_arm(args):
                            "method": "plain K1-K6 (direct neighbour scatter), deterministic slot claims",
                            "step": f"one plan of {n} spots, {B} in flight (lanes), lanes refilled on the device",
                            "lanes": B, "spots_per_step": n, "iterations_per_spot": float(np.mean(iters)),
+                           "launch_shape": {"blocks_per_sm": dict(zip(["cell_kernels", "finalize", "claim_pass",
+                                                                       "deposit_pass"], shape)),
+                                            "source": "sm2d_autotune on this plan" if tune_ms else "default",
+                                            "tuned_plan_ms": tune_ms},
                            "unfinished_spots": unfinished,
                            "l2": "inputs larger than L2 (GBs of phase space per step); 256 MB flush between steps",
                            "parallelism": f"{n} spots per GPU per step, replicas by spot x{world}"},
@@ -723,6 +730,7 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the dose-error leg against the oracles")
     ap.add_argument("--no-context", action="store_true", help="skip the log-grid and single-lane context figures")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no autotuner run)")
     ap.add_argument("--lanes", type=int, default=0, help="spots in flight (0: from free device memory)")
     ap.add_argument("--workload", default="plan512", choices=["plan512", "c2", "c3"])
     ap.add_argument("--spots", type=int, default=0, help="spots per step, the plan (0: 512; 64 for c3)")

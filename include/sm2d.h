@@ -294,6 +294,20 @@ int sm2d_batch_dose(sm2d_handle h, double* dose, int n);
  * capacity, problem.max_iterations) */
 int sm2d_batch_audit_history(sm2d_handle h, int lane, sm2d_audit* out, int max_entries, int* n_entries);
 
+/* ---- launch shape and its autotuner (no counterpart in the reference, whose
+ * launches are sized by the grid) ---- */
+/* blocks per SM of [0] the warp-per-cell kernels (classification, slot
+ * selection; default 8), [1] finalize (4), [2] the claim pass and [3] the
+ * deposit pass (0: every block the SM holds at once); the kernels stride over
+ * their work, so the shape changes speed, not results */
+int sm2d_get_launch_shape(sm2d_handle h, int* shape4);
+int sm2d_set_launch_shape(sm2d_handle h, const int* shape4);
+/* coordinate descent over the launch shape on the plan that sm2d_plan_load
+ * staged: each entry's candidates are timed on a run of the whole plan and the
+ * fastest is kept (about 20 plan runs); shape4 and best_ms (may be NULL)
+ * receive the chosen shape and its plan time */
+int sm2d_autotune(sm2d_handle h, int* shape4, float* best_ms);
+
 /* ---- host tables (no GPU needed) ---- */
 /* EnergyGrid(E_min,E_max,N) log grid (grids.cpp:6-24): edges[N+1], rep[N] */
 int sm2d_energy_grid_log(float E_min, float E_max, int N, float* edges, float* rep);

@@ -1481,6 +1481,9 @@ struct Ctx {
     cudaEvent_t ev[10] = {};   // 0..7 one iteration's stages, 8..9 a whole run
     float step_ms[7] = {};
     int grid_cell = 0, grid_transport = 0, grid_keys = 0;   // warp-per-cell kernels, deposit pass, claim pass
+    int shape[4] = {8, 4, 0, 0};   // blocks per SM: warp-per-cell kernels, finalize, claim pass, deposit
+                                   // pass (0: every resident block)
+    int sms = 1;
     int grid_fin = 0;   // finalize: four blocks per SM (its per-block flushes of per-lane sums are atomics on a
                         // few addresses; 13.2 ms per wave of 80 spots against 14.2 at eight, 14.8 at three)
     size_t ctab_words = 0;                   // claim-table size in 64-bit words
@@ -1585,6 +1588,8 @@ struct Impl {
         if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
         const long long blocks_for_cap = ((long long)c.d.bins_cap + kThreads - 1) / kThreads;
         const long long s = std::max(sms, 1);
+        if (c.shape[3] > 0) per_sm = std::min(per_sm, c.shape[3]);
+        if (c.shape[2] > 0) per_sm_keys = std::min(per_sm_keys, c.shape[2]);
         c.grid_transport = (int)std::max(1LL, std::min((long long)std::max(per_sm, 1) * s, blocks_for_cap));
         c.grid_keys = (int)std::max(1LL, std::min((long long)std::max(per_sm_keys, 1) * s, blocks_for_cap));
         return 0;
@@ -1643,6 +1648,17 @@ static int push_state(Ctx& c) {
     CK(cudaMemcpyAsync(c.d.gs, c.gs_host, sizeof(IterGlobal), cudaMemcpyHostToDevice, c.s));
     CK(cudaMemcpyAsync(c.d.ls, c.ls_host, sizeof(LaneState) * c.B, cudaMemcpyHostToDevice, c.s));
     return 0;
+}
+
+// grids of the pass kernels from the launch shape (blocks per SM)
+static int apply_shape(Ctx& c) {
+    const long long NcB = (long long)c.B * c.d.Nc;
+    const long long cells = std::max(1LL, (NcB + kThreads / 32 - 1) / (kThreads / 32));
+    c.grid_cell = (int)std::max(1LL, std::min(cells, (long long)c.shape[0] * c.sms));
+    c.grid_fin = (int)std::max(1LL, std::min((long long)c.grid_cell, (long long)c.shape[1] * c.sms));
+    int rc = DISPATCH(c, transport_grid, c.sms);
+    if (!rc && c.d.surr) rc = DISPATCH(c, rows_grid, c.sms);
+    return rc;
 }
 
 static int build_graph(Ctx& c) {
@@ -2073,9 +2089,8 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     // warp-per-cell kernels: 8 blocks per SM (the selection kernels are
     // latency-bound and gain from the warps in flight; finalize's last-block
     // step grows with the grid beyond that)
-    c->grid_cell = std::max(1, std::min((int)((NcB + kThreads / 32 - 1) / (kThreads / 32)), 8 * std::max(sms, 1)));
-    c->grid_fin = std::max(1, std::min(c->grid_cell, 4 * std::max(sms, 1)));
-    if ((rc = DISPATCH(*c, transport_grid, sms))) return bail(rc);
+    c->sms = std::max(sms, 1);
+    if ((rc = apply_shape(*c))) return bail(rc);
     if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(SM2D_ERR_CUDA, "create sync"));
     *out = c;
     return 0;
@@ -2667,8 +2682,9 @@ int sm2d_plan_run_async(sm2d_handle h) {
     if (!h) return fail(SM2D_ERR_ARG, "null handle");
     Ctx& c = *h;
     if (c.plan_n == 0) return 0;
-    int rc = reset_lanes(c);
+    int rc = build_graph(c);   // captured again after a change of the pass (surrogate, launch shape)
     if (rc) return rc;
+    if ((rc = reset_lanes(c))) return rc;
     k_plan_begin<<<1, 1, 0, c.s>>>(c.d, c.plan_beams_dev, c.plan_fe_dev, c.plan_dose_on ? c.plan_dose_dev : nullptr,
                                    c.plan_res_dev, c.plan_n, c.plan_max_it);
     CK(cudaGetLastError());
@@ -2767,6 +2783,97 @@ int sm2d_surrogate_stats(sm2d_handle h, double* out3) {
     out3[0] = (double)h->gs_host->k3_total + (double)std::min(std::max(h->gs_host->k3_rows, 0), h->d.k3_cap);
     out3[1] = (double)h->gs_host->k3_fb;
     out3[2] = (double)h->gs_host->k3_ovf;
+    return 0;
+}
+
+// ---------------------------------------------------------------- launch shape and its autotuner
+int sm2d_get_launch_shape(sm2d_handle h, int* shape4) {
+    if (!h || !shape4) return fail(SM2D_ERR_ARG, "null argument");
+    std::copy_n(h->shape, 4, shape4);
+    return 0;
+}
+
+int sm2d_set_launch_shape(sm2d_handle h, const int* shape4) {
+    if (!h || !shape4) return fail(SM2D_ERR_ARG, "null argument");
+    for (int k = 0; k < 4; ++k)
+        if (shape4[k] < (k < 2 ? 1 : 0) || shape4[k] > 32) return fail(SM2D_ERR_ARG, "launch shape entry %d: %d", k, shape4[k]);
+    Ctx& c = *h;
+    CK(cudaStreamSynchronize(c.s));
+    std::copy_n(shape4, 4, c.shape);
+    int rc = apply_shape(c);
+    if (rc) return rc;
+    if (c.exec) cudaGraphExecDestroy(c.exec);
+    if (c.graph) cudaGraphDestroy(c.graph);
+    c.exec = nullptr;
+    c.graph = nullptr;
+    return 0;
+}
+
+// Coordinate descent over the launch shape on the loaded plan: for each entry
+// in turn (deposit pass, claim pass, warp-per-cell kernels, finalize) every
+// candidate is timed on one run of the whole plan (CUDA events on the engine's
+// stream, after one untimed run of the shape) and the fastest is kept.  The
+// result does not depend on the shape (claims follow keys, not launch order).
+int sm2d_autotune(sm2d_handle h, int* shape4, float* best_ms) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    if (c.plan_n == 0) return fail(SM2D_ERR_STATE, "sm2d_autotune before sm2d_plan_load");
+    int per_sm_keys = 0, per_sm_dep = 0;
+    {
+        int k = 0, t = 0;
+        cudaError_t e = c.layout == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_transport<LayoutRef, PASS_KEYS>, kThreads, 0)
+                                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_transport<LayoutB128, PASS_KEYS>, kThreads, 0);
+        if (e == cudaSuccess)
+            e = c.layout == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_transport<LayoutRef, PASS_DIRECT>, kThreads, 0)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_transport<LayoutB128, PASS_DIRECT>, kThreads, 0);
+        if (e != cudaSuccess) return fail(SM2D_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+        per_sm_keys = std::max(k, 1);
+        per_sm_dep = std::max(t, 1);
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto time_shape = [&](const int* sh, float* ms) -> int {
+        int rc = sm2d_set_launch_shape(h, sh);
+        if (!rc) rc = sm2d_plan_run_async(h);   // captures the loop, warms the shape
+        if (!rc && cudaEventRecord(e0, c.s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event");
+        if (!rc) rc = sm2d_plan_run_async(h);
+        if (!rc && cudaEventRecord(e1, c.s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event");
+        if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event sync");
+        if (!rc && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event time");
+        return rc;
+    };
+    int best[4];
+    std::copy_n(c.shape, 4, best);
+    float best_t = 0.0f;
+    int rc = time_shape(best, &best_t);
+    const int order[4] = {3, 2, 0, 1};
+    for (int oi = 0; oi < 4 && !rc; ++oi) {
+        const int k = order[oi];
+        std::vector<int> cand;
+        if (k == 3) for (int v = 1; v <= per_sm_dep; ++v) cand.push_back(v);
+        if (k == 2) for (int v = 1; v <= per_sm_keys; ++v) cand.push_back(v);
+        if (k == 0) cand = {2, 4, 6, 8, 12, 16};
+        if (k == 1) cand = {2, 4, 6, 8};
+        for (int v : cand) {
+            int trial[4];
+            std::copy_n(best, 4, trial);
+            if (trial[k] == v || (k >= 2 && trial[k] == 0 && v == (k == 3 ? per_sm_dep : per_sm_keys))) continue;
+            trial[k] = v;
+            float t = 0.0f;
+            if ((rc = time_shape(trial, &t))) break;
+            if (t < best_t) {
+                best_t = t;
+                std::copy_n(trial, 4, best);
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = sm2d_set_launch_shape(h, best))) return rc;
+    if (shape4) std::copy_n(best, 4, shape4);
+    if (best_ms) *best_ms = best_t;
     return 0;
 }
 

@@ -186,6 +186,9 @@ def lib(build_if_needed: bool = True):
         L.sm2d_plan_results.argtypes = [P, P, P]
         L.sm2d_plan_stats.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(D)]
         L.sm2d_set_surrogate.argtypes = [P, P, F, I, I]
+        L.sm2d_get_launch_shape.argtypes = [P, P]
+        L.sm2d_set_launch_shape.argtypes = [P, P]
+        L.sm2d_autotune.argtypes = [P, P, P]
         L.sm2d_surrogate_stats.argtypes = [P, P]
         _LIB = L
         return L
@@ -386,6 +389,23 @@ class Transport:
 
     def __exit__(self, *a):
         self.close()
+
+    # -- launch shape
+    def launch_shape(self):
+        """blocks per SM: warp-per-cell kernels, finalize, claim pass, deposit pass (0: all resident)"""
+        o = np.zeros(4, np.int32)
+        check(self._lib.sm2d_get_launch_shape(self.h, _p(o)))
+        return o.tolist()
+
+    def set_launch_shape(self, shape):
+        check(self._lib.sm2d_set_launch_shape(self.h, _p(np.ascontiguousarray(shape, np.int32))))
+
+    def autotune(self):
+        """Tune the launch shape on the loaded plan; returns (shape, plan ms)."""
+        o = np.zeros(4, np.int32)
+        ms = C.c_float()
+        check(self._lib.sm2d_autotune(self.h, _p(o), C.byref(ms)))
+        return o.tolist(), ms.value
 
     # -- learned surrogate in the fine step (expectation form)
     def set_surrogate(self, surrogate, tol=0.005, max_rows=0, method_tables=False):

@@ -162,3 +162,25 @@ def test_plan_in_bucket_mode_equals_direct_mode(singles):
         dose, res = many.batch_run(beams, 3000)
     for i in range(len(beams)):
         _check_spot(i, res[i], dose[i], singles[i])
+
+
+def test_launch_shape_changes_speed_not_results():
+    """The kernels stride over their work and the claims follow keys, so a
+    plan transported with another launch shape (blocks per SM of each pass
+    kernel) gives the same spots to float-summation noise; the autotuner
+    returns a shape within the candidates and keeps it."""
+    cfg = sm.Config.reference_runner(40, 60, 0.5, 0.5, sigma_x_initial=1.5, E0=30.0).production()
+    cfg.lanes = 3
+    beams = [Beam(0.0, 0.0, 0.0, 20.0 + 3.0 * i, 1.0, 1.0 + 0.2 * i, 0.002, 0.2, 200, 40 + i) for i in range(5)]
+    with sm.Transport(cfg) as t:
+        d0, r0 = t.batch_run(beams, 2000)
+        t.set_launch_shape([2, 2, 1, 1])
+        assert t.launch_shape() == [2, 2, 1, 1]
+        d1, r1 = t.batch_run(beams, 2000)
+        t.plan_load(beams, 2000)
+        shape, ms = t.autotune()
+        assert ms > 0 and t.launch_shape() == shape and 1 <= shape[0] <= 16 and 1 <= shape[1] <= 8
+        d2, r2 = t.batch_run(beams, 2000)
+    for d in (d1, d2):
+        assert np.abs(d - d0).max() <= 1e-5 * d0.max()
+    assert [r["iterations"] for r in r1] == [r["iterations"] for r in r0] == [r["iterations"] for r in r2]
