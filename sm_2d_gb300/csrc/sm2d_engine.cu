@@ -419,11 +419,14 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
                 if (lane == 0) atomicAdd(&gs->bin_ovf, 1);
             } else {
                 // seed slot of each claimed slot: the rank of its block id
+                // (seed_slot_mode 1), or the storage slot itself as the
+                // reference's seeds take it (0)
                 int rk = 0;
                 for (int t = 0; t < kKb; ++t) {
                     const uint32_t bt = __shfl_sync(kFull, b, t);
                     rk += (bt != kEmpty && bt < b) ? 1 : 0;
                 }
+                if (!d.seed_mode) rk = lane;
                 const uint32_t k3 = cls == 2 ? 1u : 0u;
                 int off = base;
                 for (int f0 = 0; f0 < F; f0 += 32 * U) {
