@@ -175,6 +175,11 @@ struct Dev {
     // same storage receives psi_out
     uint32_t* bid;
     float* val;
+    // per slot, one bit per float4 of its values (L / 4 <= 64 bits, two
+    // words): set by every writer of a value, so a clear bit means four zero
+    // values; the classify kernel reads only the marked float4s and clears
+    // the bits with them
+    uint2* vmask;
     int* occ[2];          // per gc: on occupancy list k
     int* occ_list[2];     // occupancy lists (gc), in claim order
     double *edep, *e_cut, *e_nuc, *e_bnd;
@@ -476,6 +481,32 @@ __device__ __forceinline__ int remap_lidx(int l, uint32_t src, uint32_t dst) {
     int ed = max(0, min(eg - (int)((dst >> 12) & 0xFFFu) * Lay::NE, Lay::NE - 1));
     return Lay::enc(td, ed, x, z);
 }
+
+// Phase-space value writes: the value and the bit of its float4 in the
+// slot's occupancy mask (a reduction whose result nobody waits for).
+// slot = gc * 32 + storage slot.
+__device__ __forceinline__ void vmark(const Dev& d, size_t slot, int lidx) {
+    atomicOr(reinterpret_cast<uint32_t*>(d.vmask + slot) + (lidx >> 7), 1u << ((lidx >> 2) & 31));
+}
+__device__ __forceinline__ void vadd(const Dev& d, size_t slot, int L, int lidx, float w) {
+    atomicAdd(d.val + slot * (size_t)L + lidx, w);
+    vmark(d, slot, lidx);
+}
+// the float4 bits of a set of local bins, per mask word, then one
+// reduction per word that received any
+struct VBits {
+    uint32_t w0 = 0u, w1 = 0u;
+    __device__ __forceinline__ void add(int lidx) {
+        const uint32_t b = 1u << ((lidx >> 2) & 31);
+        if (lidx >> 7) w1 |= b;
+        else w0 |= b;
+    }
+    __device__ __forceinline__ void flush(const Dev& d, size_t slot) const {
+        uint32_t* m = reinterpret_cast<uint32_t*>(d.vmask + slot);
+        if (w0) atomicOr(m, w0);
+        if (w1) atomicOr(m + 1, w1);
+    }
+};
 
 // DeviceOutflowBucket (device_bucket.cuh:48-57) with L local bins.
 __host__ __device__ constexpr int bucket_bytes_for(int L) { return 32 * 4 + 32 * 2 + 32 * L * 4 + 12; }

@@ -226,7 +226,7 @@ __global__ void k_inject_deposit(Dev d, const BeamArgs* beams, float x_min, floa
             s = cand_find(psi_row(d, gc), d.gs->ctag, o.want);
             if (s >= 0 && d.bid[(size_t)gc * kKb + s] != o.want) s = -1;
         }
-        if (s >= 0) atomicAdd(d.val + ((size_t)gc * kKb + s) * Lay::L + o.l, o.w);
+        if (s >= 0) vadd(d, (size_t)gc * kKb + s, Lay::L, o.l, o.w);
         if (!beam_gaussian(b)) continue;
         if (!in) {
             atomicAdd(&L.src_oog_w, o.w);
@@ -325,20 +325,24 @@ __device__ __forceinline__ void block_add(const double (&v)[N], double* dst) {
 // warp per cell: the cell's class (active / coarse with w > 0,
 // compact_coarse_list k1k6_pipeline.cu:625-665), its place in this pass's
 // cell list and bucket map, and, for a listed cell, its w > 0 bins appended
-// to the bin list (contiguous per cell) for the transport.  The slot values
-// are read as a flat run of float4s, eight loads in flight per lane; the
-// cell is then cleared, so that the storage can receive psi_out.  A lane
-// whose stopping rule was met consumes its cells without transport.  The
-// last block publishes the counts, settles each lane, resets the per-lane
-// accumulators and sets the device loop condition; in a spot plan it also
-// lists the lanes whose spot just finished and sets the refill condition.
+// to the bin list (contiguous per cell, by slot and local bin).  Only the
+// float4s the slots' occupancy masks mark are read (the others hold zeros):
+// each lane lists its slot's marked float4s in the warp's shared list, and
+// the warp then reads the list as a flat run, U loads in flight per lane.
+// The marked float4s and the masks are then cleared, so that the storage
+// can receive psi_out.  A lane whose stopping rule was met consumes its
+// cells without transport.  The last block publishes the counts, settles
+// each lane, resets the per-lane accumulators and sets the device loop
+// condition; in a spot plan it also lists the lanes whose spot just
+// finished and sets the refill condition.
 template <class Lay>
 __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphConditionalHandle cond,
                                                        cudaGraphConditionalHandle rcond, int use_cond) {
-    constexpr int Q = Lay::L / 4, NW = kThreads / 32, U = 8;
+    constexpr int Q = Lay::L / 4, NW = kThreads / 32, U = 4;
+    static_assert(Q <= 64, "a slot's occupancy mask has 64 bits");
     __shared__ int s_cnt[kMaxLanes][3];   // listed active, listed coarse, their slots
     __shared__ int s_last;
-    __shared__ uint8_t s_slot[NW][kKb];   // r-th claimed slot of the warp's cell
+    __shared__ uint16_t s_f4[NW][kKb * Q];   // the warp's cell: marked float4s, slot << 6 | float4
     IterGlobal* gs = d.gs;
     if (gs->pass >= gs->max_pass) {   // paused: leave the phase space as it is
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -355,7 +359,8 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     const unsigned long long g = gs->gen + 1;   // number of this classification
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    const unsigned lt = (1u << lane) - 1u;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint16_t* fl = s_f4[wid];
     for (int i = threadIdx.x; i < d.B * 3; i += blockDim.x) (&s_cnt[0][0])[i] = 0;
     __syncthreads();
     for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < nocc; wi += nw) {
@@ -363,25 +368,42 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         const int ln = lane_of(d, c);
         const bool light = d.ls[ln].light != 0;
         uint32_t* ids = d.bid + (size_t)c * kKb;
+        const size_t slot = (size_t)c * kKb + lane;
         const uint32_t b = ids[lane];
+        const uint2 mw = __ldcg(d.vmask + slot);
         const bool used = b != kEmpty;
+        const unsigned long long mk = used ? ((unsigned long long)mw.y << 32) | mw.x : 0ull;
         const uint32_t be = (b >> 12) & 0xFFFu;
         const bool c_on = __any_sync(kFull, used && be <= (uint32_t)d.b_on);
         const bool c_off = __any_sync(kFull, used && be <= (uint32_t)d.b_off);
         const unsigned um = __ballot_sync(kFull, used);
-        __syncwarp();   // the previous cell's slot table is no longer read
-        if (used) s_slot[wid][__popc(um & lt)] = (uint8_t)lane;
+        // the marked float4s of the cell as one list, by slot and float4
+        const int nm = __popcll(mk);
+        int pm = nm;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, pm, o);
+            if (lane >= o) pm += y;
+        }
+        const int M = __shfl_sync(kFull, pm, 31);
+        pm -= nm;
+        __syncwarp();   // the previous cell's list is no longer read
+        for (unsigned long long m = mk; m;) {
+            const int q = __ffsll((long long)m) - 1;
+            m &= m - 1;
+            fl[pm++] = (uint16_t)((lane << 6) | q);
+        }
         __syncwarp();
-        const int F = __popc(um) * Q;   // float4s of the claimed slots
-        float4* vc = reinterpret_cast<float4*>(d.val + (size_t)c * kKb * Lay::L);
+        const float4* vc = reinterpret_cast<const float4*>(d.val) + (size_t)c * kKb * Q;
         float ws = 0.0f;
         int nz = 0;
-        for (int f0 = 0; f0 < F; f0 += 32 * U) {
+        for (int f0 = 0; f0 < M; f0 += 32 * U) {
             float4 r[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int f = f0 + 32 * u + lane;
-                r[u] = f < F ? __ldcg(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const int e = f < M ? fl[f] : 0;
+                r[u] = f < M ? __ldcg(vc + (e >> 6) * Q + (e & 63)) : z4;
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -429,18 +451,18 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
                 if (!d.seed_mode) rk = lane;
                 const uint32_t k3 = cls == 2 ? 1u : 0u;
                 int off = base;
-                for (int f0 = 0; f0 < F; f0 += 32 * U) {
+                for (int f0 = 0; f0 < M; f0 += 32 * U) {
                     float4 r[U];
+                    int e[U];
 #pragma unroll
                     for (int u = 0; u < U; ++u) {   // all loads first (L2 hits of the first read)
                         const int f = f0 + 32 * u + lane;
-                        r[u] = f < F ? __ldcg(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q)
-                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+                        e[u] = f < M ? fl[f] : 0;
+                        r[u] = f < M ? __ldcg(vc + (e[u] >> 6) * Q + (e[u] & 63)) : z4;
                     }
 #pragma unroll
                     for (int u = 0; u < U; ++u) {
-                        const int f = f0 + 32 * u + lane;
-                        const int s = f < F ? s_slot[wid][f / Q] : 0;
+                        const int s = e[u] >> 6, q = e[u] & 63;
                         const int cnt = (r[u].x > 0.0f) + (r[u].y > 0.0f) + (r[u].z > 0.0f) + (r[u].w > 0.0f);
                         int inc = cnt;
 #pragma unroll
@@ -455,7 +477,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
 #pragma unroll
                         for (int k = 0; k < 4; ++k)
                             if (c4[k] > 0.0f)
-                                d.bins[p++] = make_uint4((uint32_t)c, meta | ((uint32_t)(4 * (f % Q) + k) << 10),
+                                d.bins[p++] = make_uint4((uint32_t)c, meta | ((uint32_t)(4 * q + k) << 10),
                                                          __float_as_uint(c4[k]), bs);
                         off += __shfl_sync(kFull, inc, 31);
                     }
@@ -463,7 +485,13 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
             }
         }
         // psi_in of the cell is consumed: clear it for psi_out
-        for (int f = lane; f < F; f += 32) __stcs(vc + (size_t)s_slot[wid][f / Q] * Q + f % Q, make_float4(0.f, 0.f, 0.f, 0.f));
+        float4* vw = reinterpret_cast<float4*>(d.val) + slot * Q;
+        for (unsigned long long m = mk; m;) {
+            const int q = __ffsll((long long)m) - 1;
+            m &= m - 1;
+            __stcs(vw + q, z4);
+        }
+        if (mw.x | mw.y) d.vmask[slot] = make_uint2(0u, 0u);
         ids[lane] = kEmpty;
     }
     __syncthreads();
@@ -472,9 +500,13 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         if (s_cnt[i][1]) atomicAdd(&d.ls[i].acc_coarse, s_cnt[i][1]);
         if (s_cnt[i][2]) atomicAdd(&d.ls[i].acc_slots, s_cnt[i][2]);
     }
-    __threadfence();
+    // the block's writes before its count (one fence after the barrier, by
+    // the thread that counts: the barrier orders the others' writes before it)
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&gs->blocks_done, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&gs->blocks_done, 1u) == gridDim.x - 1;
+    }
     __syncthreads();
     if (!s_last) return;
     __threadfence();
@@ -762,13 +794,15 @@ struct SelScratch {
 };
 __device__ int select_row(unsigned long long* row, int* count, uint32_t tag, SelScratch& sh, uint32_t* kept, int lane) {
     const unsigned lt = (1u << lane) - 1u;
+    // every entry's id and key words in one 16-byte load, all in flight
+    // together with the row's count (entries of earlier passes carry older
+    // tags and are skipped)
+    ulonglong2 e[kCand / 32];
+#pragma unroll
+    for (int q = 0; q < kCand / 32; ++q) e[q] = __ldcg(reinterpret_cast<const ulonglong2*>(row + 2 * (q * 32 + lane)));
     const bool any = *(volatile int*)count > 0;
     int n = 0;
     if (any) {
-        // every entry's id and key words in one 16-byte load, all in flight
-        ulonglong2 e[kCand / 32];
-#pragma unroll
-        for (int q = 0; q < kCand / 32; ++q) e[q] = __ldcg(reinterpret_cast<const ulonglong2*>(row + 2 * (q * 32 + lane)));
 #pragma unroll
         for (int q = 0; q < kCand / 32; ++q) {
             const int i = q * 32 + lane;
@@ -895,23 +929,58 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
         const int nk = select_row(psi_row(d, gc), d.ccount + gc, tag, s_sel[wid], d.bid + (size_t)gc * kKb, lane);
         if (!which) continue;
         if (lane == 0) atomicAdd(&s_sum.v[lane_of(d, gc)][0], (double)nk);
+        // the four bucket rows that lead into the cell, resolved side by
+        // side (each step's loads of the four in flight together): the
+        // source cells' bucket bases, the rows' kept ids, their first probes
+        // in this cell's claim row; the kept ids of this cell come from the
+        // selection just made (shuffles, not loads)
         const int ix = gc % d.Nx, iz = (gc / d.Nx) % d.Nz;
+        int src[4];
+        src[FACE_ZP] = iz > 0 ? gc - d.Nx : -1;
+        src[FACE_ZM] = iz + 1 < d.Nz ? gc + d.Nx : -1;
+        src[FACE_XP] = ix > 0 ? gc - 1 : -1;
+        src[FACE_XM] = ix + 1 < d.Nx ? gc + 1 : -1;
+        int base[4];
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {   // the source cell whose face f leads here
-            int src = -1;
-            if (f == FACE_ZP && iz > 0) src = gc - d.Nx;
-            if (f == FACE_ZM && iz + 1 < d.Nz) src = gc + d.Nx;
-            if (f == FACE_XP && ix > 0) src = gc - 1;
-            if (f == FACE_XM && ix + 1 < d.Nx) src = gc + 1;
-            if (src < 0) continue;
-            const int base = d.c2b[src];
-            if (base < 0) continue;
-            const size_t e = (size_t)(base + f) * kKb + lane;
-            const uint32_t id = d.bkt_ids[e];
-            int os = -1;
-            uint32_t sel = kEmpty;
-            if (id != kEmpty) os = resolve(d, psi_row(d, gc), d.bid + (size_t)gc * kKb, tag, id, sel);
-            d.bkt_os[e] = make_uint2((uint32_t)os, sel);
+        for (int f = 0; f < 4; ++f) base[f] = src[f] >= 0 ? __ldcg(d.c2b + src[f]) : -1;
+        uint32_t id[4];
+#pragma unroll
+        for (int f = 0; f < 4; ++f) id[f] = base[f] >= 0 ? __ldcg(d.bkt_ids + (size_t)(base[f] + f) * kKb + lane) : kEmpty;
+        const unsigned long long* row = psi_row(d, gc);
+        ulonglong2 pr[4];
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+            pr[f] = id[f] != kEmpty ? __ldcg(reinterpret_cast<const ulonglong2*>(row + 2 * cand_hash(id[f])))
+                                    : make_ulonglong2(0ull, 0ull);
+        const uint32_t kp = lane < nk ? s_sel[wid].kept[lane] : kEmpty;   // this cell's kept ids
+        int os[4];
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const unsigned long long tb = ((unsigned long long)tag << 32) | id[f];
+            os[f] = -1;
+            if (id[f] != kEmpty) {
+                if (pr[f].x == tb) os[f] = (int)((uint32_t)pr[f].y & 31u);
+                else if ((uint32_t)(pr[f].x >> 32) == tag) os[f] = cand_find(row, tag, id[f]);   // probe on
+            }
+            // an id the row did not gather: the nearest kept id (resolve)
+            const bool miss = id[f] != kEmpty && os[f] < 0;
+            if (__any_sync(kFull, miss)) {
+                if (miss) atomicAdd(&d.gs->cand_miss, 1);
+                int bd = 0x7fffffff;
+                for (int k = 0; k < kKb; ++k) {
+                    const uint32_t x = __shfl_sync(kFull, kp, k);
+                    if (!miss || x == kEmpty) continue;
+                    const int dd = bid_distance(x, id[f]);
+                    if (dd < bd) { bd = dd; os[f] = k; }
+                }
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const uint32_t sel = __shfl_sync(kFull, kp, os[f] >= 0 ? os[f] : 0);
+            if (base[f] >= 0)
+                d.bkt_os[(size_t)(base[f] + f) * kKb + lane] =
+                    make_uint2((uint32_t)os[f], os[f] >= 0 ? sel : (id[f] != kEmpty ? id[f] : kEmpty));
         }
     }
     __syncthreads();
@@ -971,6 +1040,7 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
                 }
                 const int le = sel != bid ? remap_lidx<Lay>(l, bid, sel) : l;
                 atomicAdd(o + le, w);
+                vmark(d, (size_t)dst * kKb + os, le);
                 if (sel != bid && d.esplit)
                     eshift += (double)((e_center(d, ebin_of<Lay>(d, bid, l)) - e_center(d, ebin_of<Lay>(d, sel, le))) * w);
             }
@@ -1101,35 +1171,53 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
     __syncthreads();
     // psi_out's weight and bin-centre energy per lane, from the values the
     // deposit pass left (K5_ConservationAudit's psi_out sums,
-    // k5_audit.cu:22-167): warp per (occupied psi_out cell, slot), all of a
-    // slot's loads in flight at once as float4s.  A lane's float4s (4 q .. 4 q
-    // + 3 for q = lane + 32 k) lie in one energy bin of the slot's block
-    // (NT is a multiple of 4 and 128 / NT a multiple of NE), so one bin
-    // centre serves them.  Float sums per slot and per block (FP64 is a
-    // scarce pipe on this part), converted to double once per block; a slot's
-    // sum of at most 256 values keeps about 1e-7 of relative precision.
-    static_assert(Lay::NT % 4 == 0 && (128 / Lay::NT) % Lay::NE == 0 && Lay::L % 128 == 0,
-                  "a lane's float4s share one local energy bin");
+    // k5_audit.cu:22-167): warp per occupied psi_out cell, lane per slot, the
+    // float4s its occupancy mask marks, U loads in flight.  The four values of
+    // a float4 lie in one energy bin of the slot's block (NT is a multiple of
+    // 4).  Float sums per slot, per cell and per block (FP64 is a scarce pipe
+    // on this part), converted to double once per block.
+    static_assert(Lay::NT % 4 == 0 && Lay::NE <= 4 && Lay::L / 4 <= 64, "a float4 lies in one local energy bin");
+    constexpr int Q = Lay::L / 4, U = 4;
     const int nout = gs->occ_n[in ^ 1];
-    for (int wi = blockIdx.x * NW + wid; wi < nout * kKb; wi += nw) {
-        const int gc = d.occ_list[in ^ 1][wi / kKb];
-        const int s = wi % kKb;
-        const uint32_t bs = d.bid[(size_t)gc * kKb + s];
-        if (bs == kEmpty) continue;
-        const float4* v = reinterpret_cast<const float4*>(d.val + ((size_t)gc * kKb + s) * Lay::L);
-        float4 wv[Lay::L / 128];
+    for (int wi = blockIdx.x * NW + wid; wi < nout; wi += nw) {
+        const int gc = d.occ_list[in ^ 1][wi];
+        const size_t slot = (size_t)gc * kKb + lane;
+        const uint32_t bs = d.bid[slot];
+        const uint2 mw = __ldcg(d.vmask + slot);
+        unsigned long long m = bs != kEmpty ? ((unsigned long long)mw.y << 32) | mw.x : 0ull;
+        float W = 0.0f, E = 0.0f;
+        if (m) {
+            const float4* v = reinterpret_cast<const float4*>(d.val) + slot * Q;
+            const int eb0 = (int)((bs >> 12) & 0xFFFu) * Lay::NE;
+            float ec[Lay::NE];
 #pragma unroll
-        for (int k = 0; k < Lay::L / 128; ++k) wv[k] = __ldcg(v + lane + 32 * k);
-        const int Eb = max(0, min((int)((bs >> 12) & 0xFFFu) * Lay::NE + (4 * lane / Lay::NT) % Lay::NE, d.N_E - 1));
-        float W = 0.0f;
+            for (int e = 0; e < Lay::NE; ++e) ec[e] = e_center(d, max(0, min(eb0 + e, d.N_E - 1)));
+            while (m) {
+                float4 r[U];
+                int qq[U];
 #pragma unroll
-        for (int k = 0; k < Lay::L / 128; ++k) {
-            if (wv[k].x > 0.0f) W += wv[k].x;
-            if (wv[k].y > 0.0f) W += wv[k].y;
-            if (wv[k].z > 0.0f) W += wv[k].z;
-            if (wv[k].w > 0.0f) W += wv[k].w;
+                for (int u = 0; u < U; ++u) {
+                    qq[u] = __ffsll((long long)m) - 1;
+                    m &= m - 1;
+                    r[u] = qq[u] >= 0 ? __ldcg(v + qq[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    float w = 0.0f;
+                    if (r[u].x > 0.0f) w += r[u].x;
+                    if (r[u].y > 0.0f) w += r[u].y;
+                    if (r[u].z > 0.0f) w += r[u].z;
+                    if (r[u].w > 0.0f) w += r[u].w;
+                    const int e = ((4 * max(qq[u], 0)) / Lay::NT) % Lay::NE;
+                    float ce = ec[0];
+#pragma unroll
+                    for (int k = 1; k < Lay::NE; ++k)
+                        if (e == k) ce = ec[k];
+                    W += w;
+                    E += w * ce;
+                }
+            }
         }
-        float E = W * e_center(d, Eb);
         W = warp_sumf(W);
         E = warp_sumf(E);
         if (lane == 0 && W != 0.0f) {
@@ -1157,9 +1245,13 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
         const float x = (&s_out[0][0])[i];
         if (x != 0.0f) atomicAdd(reinterpret_cast<double*>(d.ls + i / 2) + LANE_DOUBLE(Wout) + i % 2, (double)x);
     }
-    __threadfence();
+    // the block's writes before its count (one fence after the barrier, by
+    // the thread that counts: the barrier orders the others' writes before it)
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&gs->blocks_done, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&gs->blocks_done, 1u) == gridDim.x - 1;
+    }
     __syncthreads();
     if (!s_last) return;
     __threadfence();
@@ -1195,8 +1287,27 @@ __global__ void __launch_bounds__(kThreads) k_clear_all(Dev d) {
                 for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             ids[lane] = kEmpty;
+            d.vmask[(size_t)c * kKb + lane] = make_uint2(0u, 0u);
             if (lane == 0) { d.occ[k][c] = 0; d.cls[c] = 0; d.c2b[c] = -1; }
         }
+    }
+}
+
+// Occupancy masks of slots 0..n-1 from the values a caller wrote (thread
+// per slot; an empty slot's mask is zero).
+template <class Lay>
+__global__ void k_vmask_build(Dev d, size_t n) {
+    constexpr int Q = Lay::L / 4;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        unsigned long long m = 0ull;
+        if (d.bid[i] != kEmpty) {
+            const float4* v = reinterpret_cast<const float4*>(d.val) + i * Q;
+            for (int q = 0; q < Q; ++q) {
+                const float4 x = v[q];
+                if (x.x != 0.0f || x.y != 0.0f || x.z != 0.0f || x.w != 0.0f) m |= 1ull << q;
+            }
+        }
+        d.vmask[i] = make_uint2((uint32_t)m, (uint32_t)(m >> 32));
     }
 }
 
@@ -1611,6 +1722,11 @@ struct Impl {
         CK(cudaGetLastError());
         return 0;
     }
+    static int build_masks(Ctx& c, size_t n) {
+        k_vmask_build<Lay><<<(unsigned)std::min<size_t>((n + 255) / 256, 8192), 256, 0, c.s>>>(c.d, n);
+        CK(cudaGetLastError());
+        return 0;
+    }
     // injection of the beams in beams_dev (one per lane; the kernels stride
     // over a lane's samples, max_n sizes the grid): claim pass, slot
     // selection, deposit pass, source accounting.  refill_only: the lanes
@@ -1966,6 +2082,7 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     d.feA = c->fe_dev; d.feB = c->fe_dev + BN; d.feS = c->fe_dev + 2 * BN; d.sx0 = c->fe_dev + 3 * BN;
     A(d.bid, uint32_t, ns);
     A(d.val, float, ns * c->L);
+    A(d.vmask, uint2, ns);
     for (int k = 0; k < 2; ++k) {
         A(d.occ[k], int, NcB);
         A(d.occ_list[k], int, NcB);
@@ -2032,7 +2149,8 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
         ok = cudaMemcpyAsync(rho_d, c->rho_host.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess &&
              cudaMemcpyAsync(wet_d, wet.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.bid, 0xFF, ns * 4, s) == cudaSuccess &&
-         cudaMemsetAsync(d.val, 0, ns * c->L * 4, s) == cudaSuccess;
+         cudaMemsetAsync(d.val, 0, ns * c->L * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.vmask, 0, ns * sizeof(uint2), s) == cudaSuccess;
     for (int k = 0; k < 2 && ok; ++k) ok = cudaMemsetAsync(d.occ[k], 0, NcB * 4, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.edep, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_cut, 0, NcB * 8, s) == cudaSuccess &&
          cudaMemsetAsync(d.e_nuc, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_bnd, 0, NcB * 8, s) == cudaSuccess &&
@@ -2217,6 +2335,7 @@ int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
             }
     CK(cudaMemcpyAsync(c.d.bid, bid, ns * 4, cudaMemcpyHostToDevice, c.s));
     CK(cudaMemcpyAsync(c.d.val, val, ns * c.L * 4, cudaMemcpyHostToDevice, c.s));
+    if ((rc = DISPATCH(c, build_masks, ns))) return rc;
     CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, c.s));
     if (!list.empty())
         CK(cudaMemcpyAsync(c.d.occ_list[par], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, c.s));
@@ -2254,6 +2373,7 @@ int sm2d_set_psi_in_device(sm2d_handle h, const uint32_t* d_bid, const float* d_
     CK(cudaMemcpyAsync(bid.data(), d_bid, ns * 4, cudaMemcpyDeviceToHost, c.s));
     CK(cudaMemcpyAsync(c.d.bid, d_bid, ns * 4, cudaMemcpyDeviceToDevice, c.s));
     CK(cudaMemcpyAsync(c.d.val, d_val, ns * c.L * 4, cudaMemcpyDeviceToDevice, c.s));
+    if ((rc = DISPATCH(c, build_masks, ns))) return rc;
     CK(cudaStreamSynchronize(c.s));
     std::vector<int> occ(c.d.Nc, 0), list;
     for (int cell = 0; cell < c.d.Nc; ++cell)

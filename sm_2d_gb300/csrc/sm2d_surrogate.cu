@@ -684,129 +684,146 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_infer(InferArgs a) {
     uint32_t pm = 0;
     // rows: a count the transport's claim pass left on the device, or n
     const int n = a.n_dev ? min(max(__ldcg(a.n_dev), 0), a.n) : a.n;
-    // this warpgroup's first row, loaded ahead; each tile loads the next tile's row
-    float4 qn = make_float4(1.0f, 0.0f, 1.0f, 1.0f);
+    // Per tile and warpgroup: X (features) -> L1 -> H1 -> L2 -> H2 -> L3 -> Z.
+    // The softmax and stores of a tile run while the next tile's first GEMM
+    // does, and the next tile's features are written to X while the second
+    // GEMM runs (X is free once the first has completed).  A wait that runs
+    // out of time marks the thread; the barrier before each tile's first
+    // GEMM (and one after the loop) sends the warpgroup to the exit.
+    const int stride = gridDim.x * inf::WG;
+    bool bad = false;
+    float4 qn = make_float4(1.0f, 0.0f, 1.0f, 1.0f);   // the next tile's row, loaded ahead
+    float f[4];                                        // this tile's inputs
+    // features of tile t into X (t's row read ahead in qn; loads t + stride's)
+    auto stage_x = [&](int t) {
+        const int i = t * kTile + row;
+        const float4 q = qn;
+        const long long inext = (long long)(t + stride) * kTile + row;
+        if (inext < n) qn = __ldcg(a.feats + inext);
+        float x[kIn];
+        f[0] = 1.0f; f[1] = 0.0f; f[2] = 1.0f; f[3] = 1.0f;
+        if (i < n) {
+            f[0] = q.x; f[1] = q.y; f[2] = q.z; f[3] = q.w;
+            feature_row(f, x);
+        } else {
+            for (int k = 0; k < kIn; ++k) x[k] = 0.0f;
+        }
+        x[kBiasCol] = 1.0f;       // picks up b1 (hi, lo) from the W1 image
+        x[kBiasCol + 1] = 1.0f;
+        st_row16(X, row, 0, kIn, x);
+    };
+    // softmax of a finished tile's logits z (row i, inputs fz) and its stores
+    auto finish = [&](float* z, int i, const float* fz) {
+        if (i >= n) return;
+        float m = -3.0e38f;
+        int am = 0;
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) {
+            if (z[k] > m) { m = z[k]; am = k; }
+        }
+        float s = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) { z[k] = __expf(z[k] - m); s += z[k]; }
+        const float inv = 1.0f / s;
+        float t = 0.0f;
+        // weights below the floor are zero (a component's children
+        // stay as few as the closed forms give), the rest sum to 1
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) {
+            z[k] *= inv;
+            if (z[k] < kFloor) z[k] = 0.0f;
+            if (k != am) t += z[k];
+        }
+#pragma unroll
+        for (int k = 0; k < kOut; ++k)
+            if (k == am) z[k] = 1.0f - t;   // the row sums to 1: the component's weight is conserved
+        int fb = 0;
+        if (a.mode == INFER_METHOD) {
+            plain_table(fz, z);
+        } else if (a.err_bits && __int_as_float(a.err_bits[region_of(fz)]) > a.tol) {
+            if (a.mode == INFER_TABLES) plain_table(fz, z);
+            fb = 1;
+        }
+        if (a.fallback) a.fallback[i] = fb;
+        if (!(fb && a.mode == INFER_TRANSPORT)) {
+            float4* o = reinterpret_cast<float4*>(a.out + (size_t)i * kOut);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) o[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+        }
+    };
+    int tile = blockIdx.x * inf::WG + g;
     {
-        const int i0 = (blockIdx.x * inf::WG + g) * kTile + row;
+        const int i0 = tile * kTile + row;
         if (i0 < n) qn = __ldcg(a.feats + i0);
     }
     bool ok = bar_wait(bar_w, 0);
     if (wg_any(g, !ok)) goto fail;
-    for (int tile = blockIdx.x * inf::WG + g; tile * kTile < n; tile += gridDim.x * inf::WG) {
-        const int i = tile * kTile + row;
-        const bool live = i < n;
-        float f[4] = {1.0f, 0.0f, 1.0f, 1.0f};
-        const float4 q = qn;
-        {
-            const long long inext = (long long)(tile + gridDim.x * inf::WG) * kTile + row;
-            if (inext < n) qn = __ldcg(a.feats + inext);
-        }
-        {
-            float x[kIn];
-            if (live) {
-                f[0] = q.x; f[1] = q.y; f[2] = q.z; f[3] = q.w;
-                feature_row(f, x);
-            } else {
-                for (int k = 0; k < kIn; ++k) x[k] = 0.0f;
+    if (tile * kTile < n) stage_x(tile);
+    {
+        float zp[kOut];   // logits of the tile before, its softmax pending
+        float fp[4] = {1.0f, 0.0f, 1.0f, 1.0f};
+        int ip = n;       // its row (n: none)
+        for (; tile * kTile < n; tile += stride) {
+            const int i = tile * kTile + row;
+            const float fc[4] = {f[0], f[1], f[2], f[3]};
+            fence_async_smem();
+            fence_before();
+            if (wg_any(g, bad)) goto fail;   // X holds this tile's rows; TMEM is free
+            if (row == 0) {
+                fence_after();
+                mma(tm, sdesc(su32(X), 256), sdesc(su32(sm + inf::W1), 256), idesc(128, 128), 0);
+                mma_commit(bar_m);
             }
-            x[kBiasCol] = 1.0f;       // picks up b1 (hi, lo) from the W1 image
-            x[kBiasCol + 1] = 1.0f;
-            st_row16(X, row, 0, kIn, x);
-        }
-        fence_async_smem();
-        wg_sync(g);
-        if (row == 0) {
+            finish(zp, ip, fp);
+            bad |= !bar_wait(bar_m, pm);
+            pm ^= 1;
             fence_after();
-            mma(tm, sdesc(su32(X), 256), sdesc(su32(sm + inf::W1), 256), idesc(128, 128), 0);
-            mma_commit(bar_m);
-        }
-        ok = bar_wait(bar_m, pm);
-        pm ^= 1;
-        if (wg_any(g, !ok)) goto fail;
-        fence_after();
-        for (int c = 0; c < kHid; c += 32) {
-            float v[32];
-            tmem_ld32(tm + lane_base + c, v);
-            st_row32_relu(H, row, c, kHid, v);
-        }
-        fence_before();
-        fence_async_smem();
-        wg_sync(g);
-        if (row == 0) {
-            fence_after();
-            for (int k = 0; k < kHid / 16; ++k)
-                mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W2) + 256 * k, 2048), idesc(128, 128),
-                    k > 0);
-            mma(tm, sdesc(su32(sm + inf::ONES), 256), sdesc(su32(sm + inf::B2X), 256), idesc(128, 128), 1);   // + b2
-            mma_commit(bar_m);
-        }
-        ok = bar_wait(bar_m, pm);
-        pm ^= 1;
-        if (wg_any(g, !ok)) goto fail;
-        fence_after();
-        for (int c = 0; c < kHid; c += 32) {
-            float v[32];
-            tmem_ld32(tm + lane_base + c, v);
-            st_row32_relu(H, row, c, kHid, v);
-        }
-        fence_before();
-        fence_async_smem();
-        wg_sync(g);
-        if (row == 0) {
-            fence_after();
-            for (int k = 0; k < kHid / 16; ++k)
-                mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W3) + 256 * k, 2048), idesc(128, kOut),
-                    k > 0);
-            mma(tm, sdesc(su32(sm + inf::ONES), 256), sdesc(su32(sm + inf::B3X), 256), idesc(128, kOut), 1);   // + b3
-            mma_commit(bar_m);
-        }
-        ok = bar_wait(bar_m, pm);
-        pm ^= 1;
-        if (wg_any(g, !ok)) goto fail;
-        fence_after();
-        {
-            float z[kOut];
-            tmem_ld32(tm + lane_base, z);
-            if (live) {
-                float m = -3.0e38f;
-                int am = 0;
-#pragma unroll
-                for (int k = 0; k < kOut; ++k) {
-                    if (z[k] > m) { m = z[k]; am = k; }
-                }
-                float s = 0.0f;
-#pragma unroll
-                for (int k = 0; k < kOut; ++k) { z[k] = __expf(z[k] - m); s += z[k]; }
-                const float inv = 1.0f / s;
-                float t = 0.0f;
-                // weights below the floor are zero (a component's children
-                // stay as few as the closed forms give), the rest sum to 1
-#pragma unroll
-                for (int k = 0; k < kOut; ++k) {
-                    z[k] *= inv;
-                    if (z[k] < kFloor) z[k] = 0.0f;
-                    if (k != am) t += z[k];
-                }
-#pragma unroll
-                for (int k = 0; k < kOut; ++k)
-                    if (k == am) z[k] = 1.0f - t;   // the row sums to 1: the component's weight is conserved
-                int fb = 0;
-                if (a.mode == INFER_METHOD) {
-                    plain_table(f, z);
-                } else if (a.err_bits && __int_as_float(a.err_bits[region_of(f)]) > a.tol) {
-                    if (a.mode == INFER_TABLES) plain_table(f, z);
-                    fb = 1;
-                }
-                if (a.fallback) a.fallback[i] = fb;
-                if (!(fb && a.mode == INFER_TRANSPORT)) {
-                    float4* o = reinterpret_cast<float4*>(a.out + (size_t)i * kOut);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) o[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
-                }
+            for (int c = 0; c < kHid; c += 32) {
+                float v[32];
+                tmem_ld32(tm + lane_base + c, v);
+                st_row32_relu(H, row, c, kHid, v);
             }
+            fence_before();
+            fence_async_smem();
+            wg_sync(g);
+            if (row == 0) {
+                fence_after();
+                for (int k = 0; k < kHid / 16; ++k)
+                    mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W2) + 256 * k, 2048), idesc(128, 128),
+                        k > 0);
+                mma(tm, sdesc(su32(sm + inf::ONES), 256), sdesc(su32(sm + inf::B2X), 256), idesc(128, 128), 1);   // + b2
+                mma_commit(bar_m);
+            }
+            if ((tile + stride) * kTile < n) stage_x(tile + stride);
+            bad |= !bar_wait(bar_m, pm);
+            pm ^= 1;
+            fence_after();
+            for (int c = 0; c < kHid; c += 32) {
+                float v[32];
+                tmem_ld32(tm + lane_base + c, v);
+                st_row32_relu(H, row, c, kHid, v);
+            }
+            fence_before();
+            fence_async_smem();
+            wg_sync(g);
+            if (row == 0) {
+                fence_after();
+                for (int k = 0; k < kHid / 16; ++k)
+                    mma(tm, sdesc(su32(H) + 256 * k, 2048), sdesc(su32(sm + inf::W3) + 256 * k, 2048), idesc(128, kOut),
+                        k > 0);
+                mma(tm, sdesc(su32(sm + inf::ONES), 256), sdesc(su32(sm + inf::B3X), 256), idesc(128, kOut), 1);   // + b3
+                mma_commit(bar_m);
+            }
+            bad |= !bar_wait(bar_m, pm);
+            pm ^= 1;
+            fence_after();
+            tmem_ld32(tm + lane_base, zp);
+            ip = i;
+            fp[0] = fc[0]; fp[1] = fc[1]; fp[2] = fc[2]; fp[3] = fc[3];
         }
         fence_before();
-        wg_sync(g);   // TMEM and X are reused by the next tile
+        if (wg_any(g, bad)) goto fail;
+        finish(zp, ip, fp);
     }
     goto done;
 fail:

@@ -240,7 +240,7 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
                 if (seld != selb && d.esplit)
                     atomicAdd(d.dl_edep + bcell,
                               (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, ebin_of<Lay>(d, seld, le2))) * w));
-                atomicAdd(d.val + ((size_t)dcell * kKb + os) * Lay::L + le2, w);
+                vadd(d, (size_t)dcell * kKb + os, Lay::L, le2, w);
                 return 0.0f;
             }
             stage = 2;
@@ -605,14 +605,18 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             else if (Ebe != Eb) t.edep += (double)((e_center(d, Eb) - e_center(d, Ebe)) * wpart * wcf);
             const int tl = tbe % Lay::NT, El = Ebe % Lay::NE;
             float* vs = vals + (size_t)os * Lay::L;
+            VBits vb;
 #pragma unroll
             for (int xs = 0; xs < Lay::NX; ++xs) {
                 if (w[xs] <= 0.0f) continue;   // its share would be 0
                 const float wf = (w[xs] / wsum) * wcf;
                 if (wf <= 0.0f) continue;
                 const float ws = wpart * wf;
-                atomicAdd(vs + Lay::enc(tl, El, xs, zst), ws);
+                const int l = Lay::enc(tl, El, xs, zst);
+                atomicAdd(vs + l, ws);
+                vb.add(l);
             }
+            vb.flush(d, (size_t)cell * kKb + os);
         }
     }
     float wl = 0.0f, wr = 0.0f;
@@ -752,13 +756,17 @@ __device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, c
                 if (Ebe != Eb) t.edep += (double)((e_center(d, Eb) - e_center(d, Ebe)) * wk * wcf);
                 const int tl = tbe % Lay::NT, El = Ebe % Lay::NE;
                 float* vs = vals + (size_t)os * Lay::L;
+                VBits vb;
 #pragma unroll
                 for (int xs = 0; xs < Lay::NX; ++xs) {
                     if (w[xs] <= 0.0f) continue;
                     const float wf = (w[xs] / wsum) * wcf;
                     if (wf <= 0.0f) continue;
-                    atomicAdd(vs + Lay::enc(tl, El, xs, zst), wk * wf);
+                    const int l = Lay::enc(tl, El, xs, zst);
+                    atomicAdd(vs + l, wk * wf);
+                    vb.add(l);
                 }
+                vb.flush(d, (size_t)cell * kKb + os);
             }
         }
     }
