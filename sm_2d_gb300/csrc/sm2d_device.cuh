@@ -229,7 +229,9 @@ struct Dev {
     unsigned long long* ctab;  // claim tables: B * Nc psi_out rows, then 4 * listed_cap bucket rows
     int* ccount;               // gathered ids per claim-table row
     uint32_t* bkt_ids;         // kept ids of each bucket row [4 * listed_cap][32]
-    uint2* bkt_os;             // psi_out slot of each kept bucket id in the cell behind the face
+    // per kept bucket id (bucket row, position): the id, its psi_out slot in
+    // the cell behind the face and that slot's id (bkt_slot_pack)
+    uint2* bkt_os;
                                // (x = slot or -1, y = the kept id there), resolved once per pass by
                                // the selection [4 * listed_cap][32]
 };
@@ -452,15 +454,28 @@ __device__ __forceinline__ void cand_insert(unsigned long long* row, int* count,
 // Slot assigned to `bid` by the selection of this pass, -1 if not gathered.
 // An entry's id and slot words are read together (entries are 16-byte
 // aligned), one L2 round trip per probe.
-__device__ __forceinline__ int cand_find(const unsigned long long* row, uint32_t tag, uint32_t bid) {
+// After the selection an entry's key word holds slot | kept id << 5 (the id
+// the slot holds: the entry's own, or the nearer kept id it folded into).
+// RO: the tables are read-only for the rest of the kernel (the deposit
+// passes), so the probes may hit in L1 (a cell's bins probe the same rows).
+template <bool RO = false>
+__device__ __forceinline__ int cand_find(const unsigned long long* row, uint32_t tag, uint32_t bid, uint32_t& sel) {
     const unsigned long long tb = ((unsigned long long)tag << 32) | bid;
     const unsigned h = cand_hash(bid);
     for (int p = 0; p < kCand; ++p) {
-        const ulonglong2 e = __ldcg(reinterpret_cast<const ulonglong2*>(row + 2 * ((h + p) & (kCand - 1))));
-        if (e.x == tb) return (int)((uint32_t)e.y & 31u);
+        const ulonglong2* a = reinterpret_cast<const ulonglong2*>(row + 2 * ((h + p) & (kCand - 1)));
+        const ulonglong2 e = RO ? __ldg(a) : __ldcg(a);
+        if (e.x == tb) {
+            sel = ((uint32_t)e.y >> 5) & 0xFFFFFFu;
+            return (int)((uint32_t)e.y & 31u);
+        }
         if ((uint32_t)(e.x >> 32) != tag) return -1;
     }
     return -1;
+}
+__device__ __forceinline__ int cand_find(const unsigned long long* row, uint32_t tag, uint32_t bid) {
+    uint32_t sel;
+    return cand_find(row, tag, bid, sel);
 }
 
 // The first claim in cell gc puts it on occupancy list k.
@@ -481,6 +496,15 @@ __device__ __forceinline__ int remap_lidx(int l, uint32_t src, uint32_t dst) {
     int ed = max(0, min(eg - (int)((dst >> 12) & 0xFFFu) * Lay::NE, Lay::NE - 1));
     return Lay::enc(td, ed, x, z);
 }
+
+// An entry of bkt_os: x = the bucket's kept id (24 bits) | (psi_out slot + 1)
+// << 24, y = the id of that psi_out slot (kEmpty: none); one 8-byte load
+// gives the fused K4 everything its resolve of a bucket id needs.
+__device__ __forceinline__ uint2 bkt_slot_pack(uint32_t id, int os, uint32_t sel) {
+    return make_uint2((id & 0xFFFFFFu) | ((uint32_t)(os + 1) << 24), sel);
+}
+__device__ __forceinline__ uint32_t bkt_slot_id(uint2 m) { return m.x & 0xFFFFFFu; }
+__device__ __forceinline__ int bkt_slot_os(uint2 m) { return (int)(m.x >> 24) - 1; }
 
 // Phase-space value writes: the value and the bit of its float4 in the
 // slot's occupancy mask (a reduction whose result nobody waits for).

@@ -223,8 +223,9 @@ __global__ void k_inject_deposit(Dev d, const BeamArgs* beams, float x_min, floa
         const int gc = lane * d.Nc + o.cell;
         int s = -1;
         if (in && !L.inj_skip && o.w > 0.0f) {
-            s = cand_find(psi_row(d, gc), d.gs->ctag, o.want);
-            if (s >= 0 && d.bid[(size_t)gc * kKb + s] != o.want) s = -1;
+            uint32_t sel;
+            s = cand_find(psi_row(d, gc), d.gs->ctag, o.want, sel);
+            if (s >= 0 && sel != o.want) s = -1;   // folded into another block: a slot drop
         }
         if (s >= 0) vadd(d, (size_t)gc * kKb + s, Lay::L, o.l, o.w);
         if (!beam_gaussian(b)) continue;
@@ -730,30 +731,45 @@ __device__ __forceinline__ void tally_cell(const Dev& d, int idx, int lane, Lane
     double Wi = 0.0, Ei = 0.0, ed = 0.0, en = 0.0, pw = 0.0, pe = 0.0;
     float wn = 0.0f;
     int pn = 0, k3c = 0;
-    for (int i = r.x + lane; i < r.x + r.y; i += 32) {
-        const uint4 b = __ldcg(d.bins + i);
-        const bool k3 = ((b.y >> 18) & 1u) != 0;
-        const int lidx = (int)((b.y >> 10) & 0xFFu);
-        const float w = __uint_as_float(b.z);
-        int tl, El, xs, zs;
-        Lay::dec(lidx, tl, El, xs, zs);
-        int Ebin = (int)((b.w >> 12) & 0xFFFu) * Lay::NE + El;
-        if (k3) Ebin = max(0, min(Ebin, d.N_E - 1));
-        const float E = d.Ee[Ebin] + 1.0f * ((d.Ee[Ebin + 1] - d.Ee[Ebin]) * 0.5f);
-        Wi += (double)w;
-        Ei += (double)w * (double)E;
-        if (w < (k3 ? d.prune_fine : d.prune_coarse)) {   // the transport's prune drop
-            pw += (double)w;
-            pe += (double)(E * w);
-            ++pn;
-            k3c = k3;
-            continue;
+    // U bins per lane in flight: their list entries and step records
+    // together, then the bin-centre energies (sums in bin order per lane)
+    constexpr int U = 4;
+    const int end = r.x + r.y;
+    for (int i0 = r.x + lane; i0 < end; i0 += 32 * U) {
+        uint4 bb[U];
+        float4 rr[U];   // z, sigma, deposit, nuclear weight
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + 32 * u;
+            bb[u] = i < end ? __ldcg(d.bins + i) : make_uint4(0u, 0u, 0u, 0u);
+            rr[u] = i < end ? __ldcg(rec + 2 * (size_t)i + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        if (E <= 0.1f) continue;
-        const float4 r1 = __ldcg(rec + 2 * (size_t)i + 1);   // z, sigma, deposit, nuclear weight
-        ed += (double)r1.z;
-        wn += r1.w;
-        en += (double)(r1.w * E);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (i0 + 32 * u >= end) continue;
+            const uint4 b = bb[u];
+            const bool k3 = ((b.y >> 18) & 1u) != 0;
+            const int lidx = (int)((b.y >> 10) & 0xFFu);
+            const float w = __uint_as_float(b.z);
+            int tl, El, xs, zs;
+            Lay::dec(lidx, tl, El, xs, zs);
+            int Ebin = (int)((b.w >> 12) & 0xFFFu) * Lay::NE + El;
+            if (k3) Ebin = max(0, min(Ebin, d.N_E - 1));
+            const float E = d.Ee[Ebin] + 1.0f * ((d.Ee[Ebin + 1] - d.Ee[Ebin]) * 0.5f);
+            Wi += (double)w;
+            Ei += (double)w * (double)E;
+            if (w < (k3 ? d.prune_fine : d.prune_coarse)) {   // the transport's prune drop
+                pw += (double)w;
+                pe += (double)(E * w);
+                ++pn;
+                k3c = k3;
+                continue;
+            }
+            if (E <= 0.1f) continue;
+            ed += (double)rr[u].z;
+            wn += rr[u].w;
+            en += (double)(rr[u].w * E);
+        }
     }
     Wi = warp_sum(Wi);
     Ei = warp_sum(Ei);
@@ -840,7 +856,10 @@ __device__ int select_row(unsigned long long* row, int* count, uint32_t tag, Sel
                 if (dd < bd) { bd = dd; slot = k; }
             }
         }
-        row[2 * (int)sh.idx[j] + 1] = ((unsigned long long)(0xFFFFFFFFu - tag) << 32) | (uint32_t)slot;
+        // the slot and the id it holds: a found id resolves in one probe
+        const uint32_t sel = sh.rank[j] < kKb ? sh.bid[j] : sh.kept[slot];
+        row[2 * (int)sh.idx[j] + 1] =
+            ((unsigned long long)(0xFFFFFFFFu - tag) << 32) | (uint32_t)slot | ((sel & 0xFFFFFFu) << 5);
     }
     if (kept) kept[lane] = lane < nk ? sh.kept[lane] : kEmpty;
     if (lane == 0 && any) *count = 0;
@@ -980,7 +999,7 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
             const uint32_t sel = __shfl_sync(kFull, kp, os[f] >= 0 ? os[f] : 0);
             if (base[f] >= 0)
                 d.bkt_os[(size_t)(base[f] + f) * kKb + lane] =
-                    make_uint2((uint32_t)os[f], os[f] >= 0 ? sel : (id[f] != kEmpty ? id[f] : kEmpty));
+                    bkt_slot_pack(id[f], os[f], os[f] >= 0 ? sel : (id[f] != kEmpty ? id[f] : kEmpty));
         }
     }
     __syncthreads();

@@ -109,21 +109,25 @@ __device__ __forceinline__ int ebin_of(const Dev& d, uint32_t bid, int l) {
 // Slot of block `want` in a selected container and the kept id there (want
 // itself or the nearest kept id it folds into).  An id that was not
 // gathered (claim-table overflow) takes the nearest kept id and is counted.
+// An id the row did not gather: the slot of the nearest kept id, -1 if none.
+static __device__ __noinline__ int resolve_miss(const Dev& d, const uint32_t* kept, uint32_t want) {
+    atomicAdd(&d.gs->cand_miss, 1);
+    int s = -1, bd = 0x7fffffff;
+    for (int k = 0; k < kKb; ++k) {
+        const uint32_t x = kept[k];
+        if (x == kEmpty) continue;
+        const int dd = bid_distance(x, want);
+        if (dd < bd) { bd = dd; s = k; }
+    }
+    return s;
+}
+template <bool RO = false>
 __device__ __forceinline__ int resolve(const Dev& d, const unsigned long long* row, const uint32_t* kept, uint32_t tag,
                                        uint32_t want, uint32_t& sel) {
-    int s = cand_find(row, tag, want);
-    if (s < 0) {
-        atomicAdd(&d.gs->cand_miss, 1);
-        int bd = 0x7fffffff;
-        for (int k = 0; k < kKb; ++k) {
-            const uint32_t x = kept[k];
-            if (x == kEmpty) continue;
-            const int dd = bid_distance(x, want);
-            if (dd < bd) { bd = dd; s = k; }
-        }
-        if (s < 0) { sel = want; return -1; }
-    }
-    sel = kept[s];
+    int s = cand_find<RO>(row, tag, want, sel);
+    if (s >= 0) return s;
+    s = resolve_miss(d, kept, want);
+    sel = s >= 0 ? kept[s] : want;
     return s;
 }
 
@@ -219,9 +223,12 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
                         &d.gs->cand_ovf);
             return 0.0f;
         }
+        // the bucket's kept id from the probe; for the fused pass its psi_out
+        // slot and that slot's id in one entry (bkt_slot_pack)
         uint32_t selb;
-        const int kb = resolve(d, bucket_row(d, bf), d.bkt_ids + (size_t)bf * kKb, src.tag, want, selb);
+        const int kb = resolve<true>(d, bucket_row(d, bf), d.bkt_ids + (size_t)bf * kKb, src.tag, want, selb);
         if (kb >= 0) {
+            const uint2 m = PASS == PASS_BUCKET ? make_uint2(0u, 0u) : __ldg(d.bkt_os + (size_t)bf * kKb + kb);
             const int le = (selb == want) ? lidx : remap_lidx<Lay>(lidx, want, selb);
             if (selb != want && d.esplit)   // split method: a re-binned part keeps its energy
                 t.edep += (double)((e_center(d, ebin_of<Lay>(d, want, lidx)) - e_center(d, ebin_of<Lay>(d, selb, le))) * w);
@@ -232,8 +239,7 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
             }
             // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
             // slot that the selection resolved for it
-            const uint2 m = __ldcg(d.bkt_os + (size_t)bf * kKb + kb);
-            const int os = (int)m.x;
+            const int os = bkt_slot_os(m);
             if (os >= 0) {
                 const uint32_t seld = m.y;
                 const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
@@ -586,7 +592,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             const int Eb = ep.bin[ei];
             const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
             uint32_t sel;
-            const int os = resolve(d, psi_row(d, cell), kept, sc.tag, want, sel);
+            const int os = resolve<true>(d, psi_row(d, cell), kept, sc.tag, want, sel);
             const float wpart = d.esplit ? w_new * ep.frac[ei] : w_new;
             if (os < 0) {
                 t.drop_w += (double)wpart;
@@ -740,7 +746,7 @@ __device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, c
                 const int tbn = kid_tbin(d, kd, k);
                 const uint32_t want = make_bid((uint32_t)(tbn / Lay::NT), bE);
                 uint32_t sel;
-                const int os = resolve(d, psi_row(d, cell), kept, sc.tag, want, sel);
+                const int os = resolve<true>(d, psi_row(d, cell), kept, sc.tag, want, sel);
                 if (os < 0) {
                     t.drop_w += (double)wk;
                     t.drop_e += (double)(E_new * wk);
