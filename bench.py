@@ -233,7 +233,7 @@ def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", a
     import sm_2d_gb300 as sm
     from sm_2d_gb300.runtime import Beam
     cfg = make_config(grid, workload, method)
-    cfg.lanes = lanes if lanes > 0 else auto_lanes(cfg, torch.cuda.mem_get_info()[0])
+    cfg.lanes = lanes if lanes > 0 else min(auto_lanes(cfg, torch.cuda.mem_get_info()[0]), n_spots)
     spots = plan_spots(workload, 0, n_spots)
     beams = [Beam(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
                   b["n_samples"], b["seed"]) for b in spots]
@@ -286,20 +286,23 @@ def max_over_ranks(x, dist, device):
 
 
 def lane_bytes(cfg):
-    """Device bytes one lane of the engine holds (sm2d_create's allocation)."""
+    """Device bytes one lane of a batch engine holds (sm2d_create's allocation):
+    ids and page bases per cell, the lane's value pages (16 384 unless the
+    config says otherwise), tallies, claim rows, bin list and step records."""
     nc = cfg.Nx * cfg.Nz
     L = cfg.layout["nt_local"] * cfg.layout["ne_local"] * cfg.layout["nx_sub"] * cfg.layout["nz_sub"]
-    psi = nc * 32 * (4 + 4 * L)
+    pages = min(nc * 32, getattr(cfg, "slot_pages_per_lane", 0) or 16384)
+    psi = nc * 32 * 4 + nc * 3 * 4 + pages * (8 + 4 * L)
     per_cell = nc * (2 * 8 + 44 + 44 + 8 + 1 + 4 + 8)
     rows = nc * 4096 + (nc // 8) * 4 * (4096 + 128 + 4)
     bins = nc * L // 4 * (56 if getattr(cfg, "expectation", 0) else 48)   # bin list (16 B) + step records (32 B, 40 B)
     return psi + per_cell + rows + bins
 
 
-def auto_lanes(cfg, free_bytes, cap=80):
-    """Lanes filling at most 85 % of the free device memory (at most `cap`).
-    On the 512-spot plan the rate grows with the lanes up to about 72 and is
-    flat beyond: 64 lanes 731, 72 lanes 752, 80 lanes 756 spots/s."""
+def auto_lanes(cfg, free_bytes, cap=256):
+    """Lanes filling at most 85 % of the free device memory (at most `cap`,
+    the engine's limit).  A pass has a fixed cost that the lanes share: on the
+    512-spot plan 16 lanes ran 571, 37 lanes 987 and 74 lanes 1280 spots/s."""
     return int(max(1, min(cap, 0.85 * free_bytes // lane_bytes(cfg))))
 
 
@@ -524,7 +527,7 @@ def run_gpu_arm(args):
             torch.cuda.synchronize()
 
     cfg = make_config(args.grid, args.workload)
-    cfg.lanes = args.lanes if args.lanes > 0 else auto_lanes(cfg, torch.cuda.mem_get_info()[0])
+    cfg.lanes = args.lanes if args.lanes > 0 else min(auto_lanes(cfg, torch.cuda.mem_get_info()[0]), args.spots)
     t = sm.Transport(cfg)
     B = t.lanes
     ext = torch.cuda.ExternalStream(t.stream())

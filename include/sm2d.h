@@ -114,6 +114,16 @@ typedef struct sm2d_problem {
      * loss is a small difference of large ranges.  psi, the transport
      * arithmetic and the per-cell tallies stay as they are. */
     int precision_form;
+    /* value pages per lane of an engine of several lanes (0: 16384).  A
+     * claimed slot's L values live in a page of the lane's region, handed out
+     * by the selection of its cell and returned when the next classification
+     * consumes it; the ids, masks and tallies stay per cell.  One lane holds
+     * the pages its occupied slots need in one iteration (a spot of the
+     * 512-spot plan peaks below 2000); a pass that needs more stops the run
+     * with SM2D_ERR_ALLOC.  A single-lane engine always has one page per slot
+     * (no counterpart in the reference, whose DevicePsiC holds every slot of
+     * every cell). */
+    int slot_pages_per_lane;
 } sm2d_problem;
 
 typedef struct sm2d_beam {
@@ -281,6 +291,10 @@ int sm2d_plan_load(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_i
 int sm2d_plan_run_async(sm2d_handle h);
 int sm2d_plan_results(sm2d_handle h, double* dose, sm2d_spot_result* results);
 int sm2d_plan_stats(sm2d_handle h, int* passes, int* refills, double* bins);
+/* Value pages of one lane (sm2d_problem.slot_pages_per_lane) and the most
+ * pages one lane held at once since the last plan's start or reset (no
+ * counterpart in the reference, which stores every slot densely). */
+int sm2d_page_stats(sm2d_handle h, int* pages_per_lane, int* peak_pages);
 /* One wave of spots, for callers that drive the loop themselves:
  * sm2d_batch_inject resets every lane and injects beams[i] into lane i
  * (lanes past n_beams stay empty; asynchronous, like sm2d_inject_async);

@@ -74,7 +74,9 @@ struct IterGlobal {
     int n_items;           // claimed slots of the listed cells
     int n_bins;            // w > 0 local bins of the listed cells (transport work)
     int acc_listed, acc_items, acc_bins;   // classify counters
-    int bin_ovf;           // the bin list outgrew its capacity (since the last reset)
+    int pool_peak;         // the most value pages one lane held (since the last reset)
+    int bin_ovf;           // the cell list, bin list or a lane's value pages outgrew their capacity
+                           // (since the last reset)
     int cand_ovf;          // claim-table inserts that found no free entry (cumulative)
     int cand_miss;         // deposits whose block id was not gathered (cumulative)
     int wipe;              // claim tables are cleared before the next pass
@@ -123,6 +125,9 @@ struct LaneState {
     int spot;              // plan spot in this lane (-1: none)
     int refill;            // the next injection fills this lane
     int stopped;           // the spot reached the iteration limit of a plan
+    // value pages of this lane's region handed out since its psi_in was
+    // last consumed
+    int pool_top, pad2;
     // per-iteration accumulators, 14 consecutive doubles (reset by the
     // classify kernel); the transport adds to the first seven, the finalize
     // kernel to the last seven, in this order
@@ -170,18 +175,26 @@ struct Dev {
     int straggle, nuclear, seed_mode, esplit;
     float prune_coarse, prune_fine, split_min_w, stop_frac;
     int floor_cutoff, salt;
-    // phase space, one buffer [B * Nc][32] ids + [B * Nc][32][L] values: the
-    // classify kernel copies psi_in into the bin list and clears it, so the
-    // same storage receives psi_out
+    // phase space: ids [B * Nc][32]; values in pages of L floats.  A cell's
+    // claimed slots hold consecutive pages from pbase[gc] on (slot s in page
+    // pbase[gc] + s); the psi_out selection hands each cell its run from the
+    // lane's region [lane * pool_lane, (lane + 1) * pool_lane), and pages
+    // pool_lane * B .. + 31 take the writes of a cell whose lane ran out
+    // (the run stops with SM2D_ERR_ALLOC).  The classify kernel copies
+    // psi_in into the bin list and clears its pages, so free pages hold
+    // zeros and the lane's region is handed out again from its start.
     uint32_t* bid;
     float* val;
-    // per slot, one bit per float4 of its values (L / 4 <= 64 bits, two
+    int* pbase;           // [B * Nc]: first page of the cell's slots
+    int pool_lane;        // pages per lane
+    // per page, one bit per float4 of its values (L / 4 <= 64 bits, two
     // words): set by every writer of a value, so a clear bit means four zero
     // values; the classify kernel reads only the marked float4s and clears
     // the bits with them
     uint2* vmask;
     int* occ[2];          // per gc: on occupancy list k
     int* occ_list[2];     // occupancy lists (gc), in claim order
+    int* occ_pg[2];       // first value page of each listed cell (its pbase), set with the pages
     double *edep, *e_cut, *e_nuc, *e_bnd;
     float *w_cut, *w_nuc, *w_bnd;
     // this iteration's per-cell tally increments (folded into the cumulative
@@ -506,15 +519,21 @@ __device__ __forceinline__ uint2 bkt_slot_pack(uint32_t id, int os, uint32_t sel
 __device__ __forceinline__ uint32_t bkt_slot_id(uint2 m) { return m.x & 0xFFFFFFu; }
 __device__ __forceinline__ int bkt_slot_os(uint2 m) { return (int)(m.x >> 24) - 1; }
 
-// Phase-space value writes: the value and the bit of its float4 in the
-// slot's occupancy mask (a reduction whose result nobody waits for).
-// slot = gc * 32 + storage slot.
-__device__ __forceinline__ void vmark(const Dev& d, size_t slot, int lidx) {
-    atomicOr(reinterpret_cast<uint32_t*>(d.vmask + slot) + (lidx >> 7), 1u << ((lidx >> 2) & 31));
+// Value page of storage slot s of cell gc.  RO: pbase is read-only for the
+// rest of the kernel (written by an earlier kernel of the pass).
+template <bool RO = false>
+__device__ __forceinline__ size_t page_of(const Dev& d, int gc, int s) {
+    return (size_t)(RO ? __ldg(d.pbase + gc) : __ldcg(d.pbase + gc)) + (size_t)s;
 }
-__device__ __forceinline__ void vadd(const Dev& d, size_t slot, int L, int lidx, float w) {
-    atomicAdd(d.val + slot * (size_t)L + lidx, w);
-    vmark(d, slot, lidx);
+
+// Phase-space value writes: the value and the bit of its float4 in the
+// page's occupancy mask (a reduction whose result nobody waits for).
+__device__ __forceinline__ void vmark(const Dev& d, size_t page, int lidx) {
+    atomicOr(reinterpret_cast<uint32_t*>(d.vmask + page) + (lidx >> 7), 1u << ((lidx >> 2) & 31));
+}
+__device__ __forceinline__ void vadd(const Dev& d, size_t page, int L, int lidx, float w) {
+    atomicAdd(d.val + page * (size_t)L + lidx, w);
+    vmark(d, page, lidx);
 }
 // the float4 bits of a set of local bins, per mask word, then one
 // reduction per word that received any
@@ -525,8 +544,8 @@ struct VBits {
         if (lidx >> 7) w1 |= b;
         else w0 |= b;
     }
-    __device__ __forceinline__ void flush(const Dev& d, size_t slot) const {
-        uint32_t* m = reinterpret_cast<uint32_t*>(d.vmask + slot);
+    __device__ __forceinline__ void flush(const Dev& d, size_t page) const {
+        uint32_t* m = reinterpret_cast<uint32_t*>(d.vmask + page);
         if (w0) atomicOr(m, w0);
         if (w1) atomicOr(m + 1, w1);
     }

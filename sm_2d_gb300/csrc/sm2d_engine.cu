@@ -227,7 +227,7 @@ __global__ void k_inject_deposit(Dev d, const BeamArgs* beams, float x_min, floa
             s = cand_find(psi_row(d, gc), d.gs->ctag, o.want, sel);
             if (s >= 0 && sel != o.want) s = -1;   // folded into another block: a slot drop
         }
-        if (s >= 0) vadd(d, (size_t)gc * kKb + s, Lay::L, o.l, o.w);
+        if (s >= 0) vadd(d, page_of<true>(d, gc, s), Lay::L, o.l, o.w);
         if (!beam_gaussian(b)) continue;
         if (!in) {
             atomicAdd(&L.src_oog_w, o.w);
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(kThreads) k_totals(Dev d) {
             const int s = __ffs(used) - 1;
             used &= used - 1;
             const uint32_t bs = __shfl_sync(kFull, b, s);
-            const float* v = d.val + ((size_t)gc * kKb + s) * Lay::L;
+            const float* v = d.val + page_of<true>(d, gc, s) * Lay::L;
             for (int l = lane; l < Lay::L; l += 32) {
                 const float w = v[l];
                 if (w <= 0.0f) continue;
@@ -366,12 +366,16 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     __syncthreads();
     for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < nocc; wi += nw) {
         const int c = d.occ_list[par][wi];
+        // the cell's value pages: slot s in page pg0 + s (pages past the
+        // cell's own run belong to other cells or to the overflow pages, and
+        // only the used slots' masks and values are taken)
+        const int pg0 = __ldcg(d.occ_pg[par] + wi);
         const int ln = lane_of(d, c);
         const bool light = d.ls[ln].light != 0;
         uint32_t* ids = d.bid + (size_t)c * kKb;
-        const size_t slot = (size_t)c * kKb + lane;
+        const int page = pg0 + lane;
         const uint32_t b = ids[lane];
-        const uint2 mw = __ldcg(d.vmask + slot);
+        const uint2 mw = __ldcg(d.vmask + page);
         const bool used = b != kEmpty;
         const unsigned long long mk = used ? ((unsigned long long)mw.y << 32) | mw.x : 0ull;
         const uint32_t be = (b >> 12) & 0xFFFu;
@@ -395,7 +399,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
             fl[pm++] = (uint16_t)((lane << 6) | q);
         }
         __syncwarp();
-        const float4* vc = reinterpret_cast<const float4*>(d.val) + (size_t)c * kKb * Q;
+        const float4* vc = reinterpret_cast<const float4*>(d.val) + (size_t)pg0 * Q;
         float ws = 0.0f;
         int nz = 0;
         for (int f0 = 0; f0 < M; f0 += 32 * U) {
@@ -485,14 +489,14 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
                 }
             }
         }
-        // psi_in of the cell is consumed: clear it for psi_out
-        float4* vw = reinterpret_cast<float4*>(d.val) + slot * Q;
+        // psi_in of the cell is consumed: its pages return to zeros
+        float4* vw = reinterpret_cast<float4*>(d.val) + (size_t)page * Q;
         for (unsigned long long m = mk; m;) {
             const int q = __ffsll((long long)m) - 1;
             m &= m - 1;
             __stcs(vw + q, z4);
         }
-        if (mw.x | mw.y) d.vmask[slot] = make_uint2(0u, 0u);
+        if (used && (mw.x | mw.y)) d.vmask[page] = make_uint2(0u, 0u);
         ids[lane] = kEmpty;
     }
     __syncthreads();
@@ -523,6 +527,9 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         const bool was_running = v->done == 0;
         const int na = v->acc_active, nc = v->acc_coarse, nsl = v->acc_slots;
         L.acc_active = L.acc_coarse = L.acc_slots = 0;
+        // every psi_in page of the lane is cleared: its region starts again
+        atomicMax(&gs->pool_peak, L.pool_top);
+        L.pool_top = 0;
         if (L.light) {
             // in-flight weight below a fraction of the injected weight ends
             // the spot; the rest is booked as a terminal transport drop
@@ -946,6 +953,17 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
     for (int wi = (which ? 0 : gs->occ_mark) + blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
         const int gc = d.occ_list[k][wi];
         const int nk = select_row(psi_row(d, gc), d.ccount + gc, tag, s_sel[wid], d.bid + (size_t)gc * kKb, lane);
+        if (lane == 0) {   // one page per kept slot, consecutive, from the lane's region
+            const int ln = lane_of(d, gc);
+            int pb = d.pool_lane * d.B;   // no slot, or the region is full: the overflow pages
+            if (nk > 0) {
+                const int p0 = atomicAdd(&d.ls[ln].pool_top, nk);
+                if (p0 + nk <= d.pool_lane) pb = ln * d.pool_lane + p0;
+                else atomicAdd(&gs->bin_ovf, 1);
+            }
+            d.pbase[gc] = pb;
+            d.occ_pg[k][wi] = pb;
+        }
         if (!which) continue;
         if (lane == 0) atomicAdd(&s_sum.v[lane_of(d, gc)][0], (double)nk);
         // the four bucket rows that lead into the cell, resolved side by
@@ -1045,7 +1063,8 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
             uint32_t sel = bid;
             const int os = resolve(d, psi_row(d, dst), kept, tag, bid, sel);
             const float* v = bv + (size_t)s * Lay::L;
-            float* o = os >= 0 ? d.val + ((size_t)dst * kKb + os) * Lay::L : nullptr;
+            const size_t pg = os >= 0 ? page_of<true>(d, dst, os) : 0;
+            float* o = os >= 0 ? d.val + pg * Lay::L : nullptr;
             double eshift = 0.0;
             for (int l = lane; l < Lay::L; l += 32) {
                 const float w = v[l];
@@ -1059,7 +1078,7 @@ __global__ void __launch_bounds__(kThreads) k_bucket_push(Dev d) {
                 }
                 const int le = sel != bid ? remap_lidx<Lay>(l, bid, sel) : l;
                 atomicAdd(o + le, w);
-                vmark(d, (size_t)dst * kKb + os, le);
+                vmark(d, pg, le);
                 if (sel != bid && d.esplit)
                     eshift += (double)((e_center(d, ebin_of<Lay>(d, bid, l)) - e_center(d, ebin_of<Lay>(d, sel, le))) * w);
             }
@@ -1200,13 +1219,13 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Dev d) {
     const int nout = gs->occ_n[in ^ 1];
     for (int wi = blockIdx.x * NW + wid; wi < nout; wi += nw) {
         const int gc = d.occ_list[in ^ 1][wi];
-        const size_t slot = (size_t)gc * kKb + lane;
-        const uint32_t bs = d.bid[slot];
-        const uint2 mw = __ldcg(d.vmask + slot);
+        const size_t page = (size_t)__ldcg(d.occ_pg[in ^ 1] + wi) + lane;
+        const uint32_t bs = d.bid[(size_t)gc * kKb + lane];
+        const uint2 mw = __ldcg(d.vmask + page);
         unsigned long long m = bs != kEmpty ? ((unsigned long long)mw.y << 32) | mw.x : 0ull;
         float W = 0.0f, E = 0.0f;
         if (m) {
-            const float4* v = reinterpret_cast<const float4*>(d.val) + slot * Q;
+            const float4* v = reinterpret_cast<const float4*>(d.val) + page * Q;
             const int eb0 = (int)((bs >> 12) & 0xFFFu) * Lay::NE;
             float ec[Lay::NE];
 #pragma unroll
@@ -1296,24 +1315,36 @@ __global__ void __launch_bounds__(kThreads) k_clear_all(Dev d) {
         const int n = d.gs->occ_n[k];
         for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n; wi += nw) {
             const int c = d.occ_list[k][wi];
+            const size_t pg0 = (size_t)d.occ_pg[k][wi];
             uint32_t* ids = d.bid + (size_t)c * kKb;
             const uint32_t x = ids[lane];
             unsigned um = __ballot_sync(kFull, x != kEmpty);
+            const unsigned used = um;
             while (um) {
                 const int s = __ffs(um) - 1;
                 um &= um - 1;
-                float4* v = reinterpret_cast<float4*>(d.val + ((size_t)c * kKb + s) * Lay::L);
+                float4* v = reinterpret_cast<float4*>(d.val + (pg0 + s) * Lay::L);
                 for (int q = lane; q < Lay::L / 4; q += 32) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             ids[lane] = kEmpty;
-            d.vmask[(size_t)c * kKb + lane] = make_uint2(0u, 0u);
+            if (used & (1u << lane)) d.vmask[pg0 + lane] = make_uint2(0u, 0u);
             if (lane == 0) { d.occ[k][c] = 0; d.cls[c] = 0; d.c2b[c] = -1; }
         }
     }
+    // the overflow pages (written only by a run that ran out of pages), and
+    // every lane's region starts again
+    const size_t sink = (size_t)d.pool_lane * d.B;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)kKb * Lay::L / 4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        reinterpret_cast<float4*>(d.val + sink * Lay::L)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < kKb) d.vmask[sink + i] = make_uint2(0u, 0u);
+    }
+    for (int ln = blockIdx.x * blockDim.x + threadIdx.x; ln < d.B; ln += gridDim.x * blockDim.x) d.ls[ln].pool_top = 0;
 }
 
-// Occupancy masks of slots 0..n-1 from the values a caller wrote (thread
-// per slot; an empty slot's mask is zero).
+// Occupancy masks of slots 0..n-1 of a single-lane engine from the values a
+// caller wrote, in pages numbered like the slots (pbase[gc] = 32 gc); thread
+// per slot, an empty slot's mask is zero.
 template <class Lay>
 __global__ void k_vmask_build(Dev d, size_t n) {
     constexpr int Q = Lay::L / 4;
@@ -1327,6 +1358,28 @@ __global__ void k_vmask_build(Dev d, size_t n) {
             }
         }
         d.vmask[i] = make_uint2((uint32_t)m, (uint32_t)(m >> 32));
+    }
+}
+
+// psi_in values of lane 0 in the dense layout [Nc][32][L] (zeros for an
+// empty slot), gathered from the cells' pages; thread per value.
+template <class Lay>
+__global__ void k_gather_psi(Dev d, float* out) {
+    const size_t n = (size_t)d.Nc * kKb * Lay::L;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t slot = i / Lay::L;
+        const int l = (int)(i % Lay::L);
+        float x = 0.0f;
+        if (d.bid[slot] != kEmpty) x = d.val[page_of(d, (int)(slot / kKb), (int)(slot % kKb)) * Lay::L + l];
+        out[i] = x;
+    }
+}
+// Pages numbered like the slots for a phase space a caller wrote (single
+// lane: pbase[gc] = 32 gc, the occupancy list's pages likewise).
+__global__ void k_pages_identity(Dev d, int list_k, int n_listed) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.Nc; i += gridDim.x * blockDim.x) {
+        d.pbase[i] = i * kKb;
+        if (i < n_listed) d.occ_pg[list_k][i] = d.occ_list[list_k][i] * kKb;
     }
 }
 
@@ -1619,6 +1672,7 @@ struct Ctx {
     int sms = 1;
     int grid_fin = 0;   // finalize: four blocks per SM (its per-block flushes of per-lane sums are atomics on a
                         // few addresses; 13.2 ms per wave of 80 spots against 14.2 at eight, 14.8 at three)
+    size_t pages = 0;                        // value pages (every lane's region and the overflow pages)
     size_t ctab_words = 0;                   // claim-table size in 64-bit words
     size_t ccount_n = 0;
     bool injected = false;
@@ -1743,6 +1797,12 @@ struct Impl {
     }
     static int build_masks(Ctx& c, size_t n) {
         k_vmask_build<Lay><<<(unsigned)std::min<size_t>((n + 255) / 256, 8192), 256, 0, c.s>>>(c.d, n);
+        CK(cudaGetLastError());
+        return 0;
+    }
+    static int gather_psi(Ctx& c, float* out) {
+        const size_t n = (size_t)c.d.Nc * kKb * c.L;
+        k_gather_psi<Lay><<<(unsigned)std::min<size_t>((n + 255) / 256, 16384), 256, 0, c.s>>>(c.d, out);
         CK(cudaGetLastError());
         return 0;
     }
@@ -2099,12 +2159,21 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(c->fe_dev, float, 3 * BN + B);
     d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d;
     d.feA = c->fe_dev; d.feB = c->fe_dev + BN; d.feS = c->fe_dev + 2 * BN; d.sx0 = c->fe_dev + 3 * BN;
+    // value pages: a single lane has one per slot of every cell; a lane of a
+    // batch has slot_pages_per_lane (default 16384; a spot of the 512-spot
+    // plan peaks below 2000), plus 32 overflow pages after the last region
+    d.pool_lane = B == 1 ? (int)(Nc * kKb)
+                         : (int)std::min<size_t>(Nc * kKb, p->slot_pages_per_lane > 0 ? (size_t)p->slot_pages_per_lane : 16384);
+    if ((size_t)d.pool_lane * B + kKb > (size_t)INT_MAX) return bail(fail(SM2D_ERR_ARG, "too many value pages"));
+    c->pages = (size_t)d.pool_lane * B + kKb;
     A(d.bid, uint32_t, ns);
-    A(d.val, float, ns * c->L);
-    A(d.vmask, uint2, ns);
+    A(d.val, float, c->pages * c->L);
+    A(d.vmask, uint2, c->pages);
+    A(d.pbase, int, NcB);
     for (int k = 0; k < 2; ++k) {
         A(d.occ[k], int, NcB);
         A(d.occ_list[k], int, NcB);
+        A(d.occ_pg[k], int, NcB);
     }
     A(d.edep, double, NcB); A(d.e_cut, double, NcB); A(d.e_nuc, double, NcB); A(d.e_bnd, double, NcB);
     A(d.w_cut, float, NcB); A(d.w_nuc, float, NcB); A(d.w_bnd, float, NcB);
@@ -2168,8 +2237,9 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
         ok = cudaMemcpyAsync(rho_d, c->rho_host.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess &&
              cudaMemcpyAsync(wet_d, wet.data(), sizeof(float) * p->Nz, cudaMemcpyHostToDevice, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.bid, 0xFF, ns * 4, s) == cudaSuccess &&
-         cudaMemsetAsync(d.val, 0, ns * c->L * 4, s) == cudaSuccess &&
-         cudaMemsetAsync(d.vmask, 0, ns * sizeof(uint2), s) == cudaSuccess;
+         cudaMemsetAsync(d.val, 0, c->pages * c->L * 4, s) == cudaSuccess &&
+         cudaMemsetAsync(d.vmask, 0, c->pages * sizeof(uint2), s) == cudaSuccess &&
+         cudaMemsetAsync(d.pbase, 0, NcB * 4, s) == cudaSuccess;
     for (int k = 0; k < 2 && ok; ++k) ok = cudaMemsetAsync(d.occ[k], 0, NcB * 4, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(d.edep, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_cut, 0, NcB * 8, s) == cudaSuccess &&
          cudaMemsetAsync(d.e_nuc, 0, NcB * 8, s) == cudaSuccess && cudaMemsetAsync(d.e_bnd, 0, NcB * 8, s) == cudaSuccess &&
@@ -2334,6 +2404,16 @@ int sm2d_inject_quadrature(sm2d_handle h, const sm2d_beam* b) {
     return 0;
 }
 
+// A caller's phase space in a single-lane engine: its values were copied in
+// the dense layout, so the pages of cell gc are 32 gc .. 32 gc + 31, all of
+// the lane's region held until the next classification consumes them.
+static int pages_identity(Ctx& c, int par, int n_listed) {
+    k_pages_identity<<<(unsigned)std::min((c.d.Nc + 255) / 256, 4096), 256, 0, c.s>>>(c.d, par, n_listed);
+    CK(cudaGetLastError());
+    c.ls_host[0].pool_top = n_listed > 0 ? c.d.pool_lane : 0;
+    return 0;
+}
+
 int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
     if (!h || !bid || !val) return fail(SM2D_ERR_ARG, "null argument");
     Ctx& c = *h;
@@ -2353,11 +2433,12 @@ int sm2d_set_psi_in(sm2d_handle h, const uint32_t* bid, const float* val) {
                 break;
             }
     CK(cudaMemcpyAsync(c.d.bid, bid, ns * 4, cudaMemcpyHostToDevice, c.s));
-    CK(cudaMemcpyAsync(c.d.val, val, ns * c.L * 4, cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.val, val, ns * c.L * 4, cudaMemcpyHostToDevice, c.s));   // pages numbered like the slots
     if ((rc = DISPATCH(c, build_masks, ns))) return rc;
     CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, c.s));
     if (!list.empty())
         CK(cudaMemcpyAsync(c.d.occ_list[par], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, c.s));
+    if ((rc = pages_identity(c, par, (int)list.size()))) return rc;
     c.gs_host->occ_n[par] = (int)list.size();
     c.gs_host->occ_n[par ^ 1] = 0;
     c.ls_host[0].done = 0;
@@ -2372,7 +2453,15 @@ int sm2d_get_psi_in(sm2d_handle h, uint32_t* bid, float* val) {
     Ctx& c = *h;
     const size_t ns = (size_t)c.d.Nc * kKb;
     CK(cudaMemcpyAsync(bid, c.d.bid, ns * 4, cudaMemcpyDeviceToHost, c.s));
-    if (val) CK(cudaMemcpyAsync(val, c.d.val, ns * c.L * 4, cudaMemcpyDeviceToHost, c.s));
+    if (val) {   // the values in the dense layout, through a device buffer of that size
+        float* tmp = nullptr;
+        CK(cudaMallocAsync(reinterpret_cast<void**>(&tmp), ns * c.L * 4, c.s));
+        int rc = DISPATCH(c, gather_psi, tmp);
+        if (!rc && cudaMemcpyAsync(val, tmp, ns * c.L * 4, cudaMemcpyDeviceToHost, c.s) != cudaSuccess)
+            rc = fail(SM2D_ERR_CUDA, "psi copy");
+        cudaFreeAsync(tmp, c.s);
+        if (rc) return rc;
+    }
     CK(cudaStreamSynchronize(c.s));
     return 0;
 }
@@ -2391,7 +2480,7 @@ int sm2d_set_psi_in_device(sm2d_handle h, const uint32_t* d_bid, const float* d_
     std::vector<uint32_t> bid(ns);
     CK(cudaMemcpyAsync(bid.data(), d_bid, ns * 4, cudaMemcpyDeviceToHost, c.s));
     CK(cudaMemcpyAsync(c.d.bid, d_bid, ns * 4, cudaMemcpyDeviceToDevice, c.s));
-    CK(cudaMemcpyAsync(c.d.val, d_val, ns * c.L * 4, cudaMemcpyDeviceToDevice, c.s));
+    CK(cudaMemcpyAsync(c.d.val, d_val, ns * c.L * 4, cudaMemcpyDeviceToDevice, c.s));   // pages numbered like the slots
     if ((rc = DISPATCH(c, build_masks, ns))) return rc;
     CK(cudaStreamSynchronize(c.s));
     std::vector<int> occ(c.d.Nc, 0), list;
@@ -2405,6 +2494,7 @@ int sm2d_set_psi_in_device(sm2d_handle h, const uint32_t* d_bid, const float* d_
     CK(cudaMemcpyAsync(c.d.occ[par], occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, c.s));
     if (!list.empty())
         CK(cudaMemcpyAsync(c.d.occ_list[par], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, c.s));
+    if ((rc = pages_identity(c, par, (int)list.size()))) return rc;
     c.gs_host->occ_n[par] = (int)list.size();
     c.gs_host->occ_n[par ^ 1] = 0;
     c.ls_host[0].done = 0;
@@ -2419,7 +2509,10 @@ int sm2d_get_psi_in_device(sm2d_handle h, uint32_t* d_bid, float* d_val) {
     Ctx& c = *h;
     const size_t ns = (size_t)c.d.Nc * kKb;
     CK(cudaMemcpyAsync(d_bid, c.d.bid, ns * 4, cudaMemcpyDeviceToDevice, c.s));
-    if (d_val) CK(cudaMemcpyAsync(d_val, c.d.val, ns * c.L * 4, cudaMemcpyDeviceToDevice, c.s));
+    if (d_val) {
+        const int rc = DISPATCH(c, gather_psi, d_val);
+        if (rc) return rc;
+    }
     CK(cudaStreamSynchronize(c.s));
     return 0;
 }
@@ -2448,7 +2541,7 @@ int sm2d_step(sm2d_handle h, int* n_active, int* n_coarse) {
     int rc = DISPATCH(c, launch_body, true, false, true);
     if (rc) return rc;
     if ((rc = sync_state(c))) return rc;
-    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
+    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell list, bin list or value pages of a lane: capacity exceeded");
     // classify, lists, claim pass, selection, deposit pass, K4 bucket move, finalize
     for (int k = 0; k < 7; ++k) CK(cudaEventElapsedTime(&c.step_ms[k], c.ev[k], c.ev[k + 1]));
     if (n_active) *n_active = c.ls_host[0].done ? 0 : c.ls_host[0].n_active;
@@ -2475,7 +2568,7 @@ static int run_impl(Ctx& c, int max_it, int* done_iters, float* ms) {
     if ((rc = push_state(c))) return rc;
     CK(cudaStreamSynchronize(c.s));
     if (done_iters) *done_iters = c.ls_host[0].iter - start;
-    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
+    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell list, bin list or value pages of a lane: capacity exceeded");
     return 0;
 }
 
@@ -2851,7 +2944,16 @@ int sm2d_plan_results(sm2d_handle h, double* dose, sm2d_spot_result* results) {
         CK(cudaMemcpyAsync(dose, c.plan_dose_dev, sizeof(double) * (size_t)c.d.Nc * n, cudaMemcpyDeviceToHost, c.s));
     int rc = sync_state(c);
     if (rc) return rc;
-    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell or bin list capacity exceeded");
+    if (c.gs_host->bin_ovf) return fail(SM2D_ERR_ALLOC, "cell list, bin list or value pages of a lane: capacity exceeded");
+    return 0;
+}
+
+int sm2d_page_stats(sm2d_handle h, int* pages_per_lane, int* peak_pages) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    int rc = sync_state(*h);
+    if (rc) return rc;
+    if (pages_per_lane) *pages_per_lane = h->d.pool_lane;
+    if (peak_pages) *peak_pages = h->gs_host->pool_peak;
     return 0;
 }
 

@@ -246,7 +246,7 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
                 if (seld != selb && d.esplit)
                     atomicAdd(d.dl_edep + bcell,
                               (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, ebin_of<Lay>(d, seld, le2))) * w));
-                vadd(d, (size_t)dcell * kKb + os, Lay::L, le2, w);
+                vadd(d, page_of<true>(d, dcell, os), Lay::L, le2, w);
                 return 0.0f;
             }
             stage = 2;
@@ -587,7 +587,8 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
             wsum = 1.0f;
         }
         const uint32_t* kept = d.bid + (size_t)cell * kKb;
-        float* vals = d.val + (size_t)cell * kKb * Lay::L;
+        const size_t pg0 = page_of<true>(d, cell, 0);   // the cell's psi_out pages
+        float* vals = d.val + pg0 * Lay::L;
         for (int ei = 0; ei < ep.n; ++ei) {
             const int Eb = ep.bin[ei];
             const uint32_t want = ((uint32_t)(Eb / Lay::NE) << 12) | ((uint32_t)(tbn / Lay::NT) & 0xFFFu);
@@ -622,7 +623,7 @@ __device__ void emit_stay(const Dev& d, const Src& sc, int par, bool k3, int cel
                 atomicAdd(vs + l, ws);
                 vb.add(l);
             }
-            vb.flush(d, (size_t)cell * kKb + os);
+            vb.flush(d, pg0 + os);
         }
     }
     float wl = 0.0f, wr = 0.0f;
@@ -735,7 +736,8 @@ __device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, c
             wsum = 1.0f;
         }
         const uint32_t* kept = d.bid + (size_t)cell * kKb;
-        float* vals = d.val + (size_t)cell * kKb * Lay::L;
+        const size_t pg0 = page_of<true>(d, cell, 0);   // the cell's psi_out pages
+        float* vals = d.val + pg0 * Lay::L;
         for (int e = 0; e <= kid_emax(kd); ++e) {
             const int Eb = kd.j - e;
             const uint32_t bE = (uint32_t)(Eb / Lay::NE);
@@ -772,7 +774,7 @@ __device__ void emit_stay_kids(const Dev& d, const Src& sc, int par, int cell, c
                     atomicAdd(vs + l, wk * wf);
                     vb.add(l);
                 }
-                vb.flush(d, (size_t)cell * kKb + os);
+                vb.flush(d, pg0 + os);
             }
         }
     }

@@ -45,6 +45,7 @@ class Problem(C.Structure):
         ("prune_coarse", C.c_float), ("prune_fine", C.c_float), ("split_min_weight", C.c_float),
         ("stop_weight_fraction", C.c_float), ("floor_cutoff", C.c_int), ("seed_iteration_salt", C.c_int),
         ("lanes", C.c_int), ("density_z", C.c_void_p), ("expectation", C.c_int), ("precision_form", C.c_int),
+        ("slot_pages_per_lane", C.c_int),
     ]
 
 
@@ -185,6 +186,7 @@ def lib(build_if_needed: bool = True):
         L.sm2d_plan_run_async.argtypes = [P]
         L.sm2d_plan_results.argtypes = [P, P, P]
         L.sm2d_plan_stats.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(D)]
+        L.sm2d_page_stats.argtypes = [P, C.POINTER(I), C.POINTER(I)]
         L.sm2d_set_surrogate.argtypes = [P, P, F, I, I]
         L.sm2d_get_launch_shape.argtypes = [P, P]
         L.sm2d_set_launch_shape.argtypes = [P, P]
@@ -289,6 +291,7 @@ class Config:
     density_z: np.ndarray = None   # slab phantom: density per depth row (None: water)
     expectation: int = 0    # 1: expectation form (redistribution weights instead of MCS/straggling draws)
     precision_form: int = 0  # 1: audit books weight increments; R-LUT inverted in double below 10 MeV
+    slot_pages_per_lane: int = 0  # value pages per lane of a batch engine (0: 16384)
 
     def production(self):
         """Options of a production run: deterministic rank-ordered seeds salted
@@ -322,7 +325,7 @@ class Config:
                     split_min_weight=self.split_min_weight, stop_weight_fraction=self.stop_weight_fraction,
                     floor_cutoff=self.floor_cutoff, seed_iteration_salt=self.seed_iteration_salt, lanes=self.lanes,
                     density_z=None if rho is None else rho.ctypes.data, expectation=self.expectation,
-                    precision_form=self.precision_form,
+                    precision_form=self.precision_form, slot_pages_per_lane=self.slot_pages_per_lane,
                     **self.layout)
         return p, (th, E, rho)
 
@@ -583,6 +586,13 @@ class Transport:
         p, r, b = C.c_int(), C.c_int(), C.c_double()
         check(self._lib.sm2d_plan_stats(self.h, C.byref(p), C.byref(r), C.byref(b)))
         return p.value, r.value, b.value
+
+    def page_stats(self):
+        """(value pages per lane, the most pages one lane held) since the last
+        plan's start or reset."""
+        n, pk = C.c_int(), C.c_int()
+        check(self._lib.sm2d_page_stats(self.h, C.byref(n), C.byref(pk)))
+        return n.value, pk.value
 
     def batch_inject(self, beams):
         """Reset every lane and inject beams[i] into lane i (asynchronous)."""

@@ -121,6 +121,35 @@ def test_plan_repeats():
     assert np.abs(d1 - d2).max() <= 1e-6 * d1.max()
 
 
+def test_value_pages_hold_the_plan_and_a_short_region_stops_it():
+    """Each lane's claimed slots take value pages from the lane's region.  The
+    plan's peak stays inside the default region; a region cut to exactly that
+    peak gives the same spots; a region smaller than the peak stops the run
+    with SM2D_ERR_ALLOC (cells past the region write to the overflow pages)
+    instead of writing over another lane's pages, and the engine runs again
+    after a reset."""
+    beams = _beams()
+    with sm.Transport(_cfg(3)) as many:
+        d1, r1 = many.batch_run(beams, 3000)
+        per_lane, peak = many.page_stats()
+    assert per_lane == min(40 * 70 * 32, 16384) and 0 < peak <= per_lane, (per_lane, peak)
+    cfg = _cfg(3)
+    cfg.slot_pages_per_lane = peak
+    with sm.Transport(cfg) as tight:
+        d2, r2 = tight.batch_run(beams, 3000)
+        assert tight.page_stats() == (peak, peak)
+    assert [r["iterations"] for r in r1] == [r["iterations"] for r in r2]
+    assert np.abs(d1 - d2).max() <= 1e-6 * d1.max()
+    cfg.slot_pages_per_lane = max(1, peak // 4)
+    with sm.Transport(cfg) as short:
+        with pytest.raises(sm.Sm2dError, match="value pages"):
+            short.batch_run(beams, 3000)
+        short.reset()
+        b = Beam(0.0, 0.0, 0.0, 20.0, 1.0, 0.3, 0.0, 0.0, 1, 1)   # a pencil: a few pages
+        short.inject(b.x0, b.z0, b.theta0, b.E0, b.W_total, b.sigma_x, b.sigma_theta, b.sigma_E, b.n_samples, b.seed)
+        assert short.run(3000) > 0 and short.dose().max() > 0
+
+
 def test_batch_refuses_bad_beams():
     with sm.Transport(_cfg(2)) as t:
         bad = [Beam(0.0, 0.0, 0.0, 40.0, 1.0, 1.5, 0.002, 0.4, 0, 1)]   # Gaussian without samples
