@@ -242,6 +242,8 @@ def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", a
             t.set_surrogate(surrogate, tol=tol)
         ext = torch.cuda.ExternalStream(t.stream())
         t.plan_load(beams, MAX_IT, dose=accuracy)
+        if cfg.lanes > 1:   # the lanes in flight that run this plan fastest (speed only)
+            t.tune_lanes_in_flight()
         for _ in range(warmup):
             t.plan_run_async()
         torch.cuda.synchronize()
@@ -257,8 +259,10 @@ def plan_rate(grid, workload, n_spots, lanes, steps, warmup, method="sampled", a
         passes, _, bins = t.plan_stats()
         sc = t.scalars()
         lanes_used = t.lanes
+        in_flight = t.lanes_in_flight()
         sst = t.surrogate_stats() if surrogate is not None else None
-    out = {"value": n_spots * steps / (sum(ms) / 1e3), "unit": "spots/s", "lanes": lanes_used, "spots": n_spots,
+    out = {"value": n_spots * steps / (sum(ms) / 1e3), "unit": "spots/s", "lanes": lanes_used,
+           "lanes_in_flight": in_flight, "spots": n_spots,
            "ms_per_step": float(np.mean(ms)), "passes_per_step": passes, "bins_per_step": bins,
            "iterations_per_spot": float(np.mean([r["iterations"] for r in rs])),
            "unfinished_spots": sum(1 for r in rs if not r["finished"]),
@@ -287,19 +291,21 @@ def max_over_ranks(x, dist, device):
 
 def lane_bytes(cfg):
     """Device bytes one lane of a batch engine holds (sm2d_create's allocation):
-    ids and page bases per cell, the lane's value pages (16 384 unless the
-    config says otherwise), tallies, claim rows, bin list and step records."""
+    ids and page bases per cell, the lane's value pages (32 MB of values
+    unless the config says otherwise), tallies, claim rows, bin list and step
+    records."""
     nc = cfg.Nx * cfg.Nz
     L = cfg.layout["nt_local"] * cfg.layout["ne_local"] * cfg.layout["nx_sub"] * cfg.layout["nz_sub"]
-    pages = min(nc * 32, getattr(cfg, "slot_pages_per_lane", 0) or 16384)
+    pages = min(nc * 32, getattr(cfg, "slot_pages_per_lane", 0) or (8 << 20) // L)
     psi = nc * 32 * 4 + nc * 3 * 4 + pages * (8 + 4 * L)
     per_cell = nc * (2 * 8 + 44 + 44 + 8 + 1 + 4 + 8)
-    rows = nc * 4096 + (nc // 8) * 4 * (4096 + 128 + 4)
-    bins = nc * L // 4 * (56 if getattr(cfg, "expectation", 0) else 48)   # bin list (16 B) + step records (32 B, 40 B)
+    listed = min(nc, 2048)
+    rows = nc * 4096 + listed * 4 * (4096 + 128 + 256 + 4)   # psi_out rows; bucket rows, kept ids, slot map
+    bins = min(nc * L // 4, pages * 32) * (56 if getattr(cfg, "expectation", 0) else 48)   # bin list + step records
     return psi + per_cell + rows + bins
 
 
-def auto_lanes(cfg, free_bytes, cap=256):
+def auto_lanes(cfg, free_bytes, cap=512):
     """Lanes filling at most 85 % of the free device memory (at most `cap`,
     the engine's limit).  A pass has a fixed cost that the lanes share: on the
     512-spot plan 16 lanes ran 571, 37 lanes 987 and 74 lanes 1280 spots/s."""
@@ -548,6 +554,7 @@ def run_gpu_arm(args):
     # the launch shape (blocks per SM of each pass kernel) from the autotuner,
     # on this plan, before the timed region
     shape, tune_ms = t.autotune() if not args.no_tune else (t.launch_shape(), None)
+    lif = t.lanes_in_flight()   # the tuner's choice of lanes in flight (every lane with --no-tune)
     for _ in range(max(args.warmup, 3)):
         t.plan_run_async()
     torch.cuda.synchronize()
@@ -605,7 +612,7 @@ def run_gpu_arm(args):
 
     # ---- per-kernel device time: eager replay of one wave of the plan's first
     # `lanes` spots with CUDA events around every launch on the library stream
-    t.batch_inject(beams[:B])
+    t.batch_inject(beams[:lif])   # the wave holds as many spots as a plan keeps in flight
     n_it, ms, n_launch, wave_passes = t.run_profiled(MAX_IT)
     prs = t.batch_results(min(B, n))
     L = t.L
@@ -700,8 +707,9 @@ def run_gpu_arm(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": workload_desc(args.workload, args.grid, n), "grid": args.grid,
                            "method": "plain K1-K6 (direct neighbour scatter), deterministic slot claims",
-                           "step": f"one plan of {n} spots, {B} in flight (lanes), lanes refilled on the device",
-                           "lanes": B, "spots_per_step": n, "iterations_per_spot": float(np.mean(iters)),
+                           "step": f"one plan of {n} spots, {lif} in flight on {B} lanes, lanes refilled on the device",
+                           "lanes": B, "lanes_in_flight": lif, "spots_per_step": n,
+                           "iterations_per_spot": float(np.mean(iters)),
                            "launch_shape": {"blocks_per_sm": dict(zip(["cell_kernels", "finalize", "claim_pass",
                                                                        "deposit_pass"], shape)),
                                             "source": "sm2d_autotune on this plan" if tune_ms else "default",

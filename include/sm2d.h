@@ -114,15 +114,16 @@ typedef struct sm2d_problem {
      * loss is a small difference of large ranges.  psi, the transport
      * arithmetic and the per-cell tallies stay as they are. */
     int precision_form;
-    /* value pages per lane of an engine of several lanes (0: 16384).  A
-     * claimed slot's L values live in a page of the lane's region, handed out
-     * by the selection of its cell and returned when the next classification
-     * consumes it; the ids, masks and tallies stay per cell.  One lane holds
-     * the pages its occupied slots need in one iteration (a spot of the
-     * 512-spot plan peaks below 2000); a pass that needs more stops the run
-     * with SM2D_ERR_ALLOC.  A single-lane engine always has one page per slot
-     * (no counterpart in the reference, whose DevicePsiC holds every slot of
-     * every cell). */
+    /* value pages per lane of an engine of several lanes (0: 32 MB of values,
+     * 2^23 / L pages).  A claimed slot's L values live in a page of the lane's
+     * region, handed out by the selection of its cell and returned when the
+     * next classification consumes it; the ids, masks and tallies stay per
+     * cell.  One lane holds the pages its occupied slots need in one
+     * iteration (the widest 70 MeV spot of the 512-spot plan peaks at 4422
+     * on the reference grids, about 20000 on the 256 log-E / 512 theta
+     * grid); a pass that needs more stops the run with SM2D_ERR_ALLOC.  A
+     * single-lane engine always has one page per slot (no counterpart in the
+     * reference, whose DevicePsiC holds every slot of every cell). */
     int slot_pages_per_lane;
 } sm2d_problem;
 
@@ -321,6 +322,16 @@ int sm2d_set_launch_shape(sm2d_handle h, const int* shape4);
  * fastest is kept (about 20 plan runs); shape4 and best_ms (may be NULL)
  * receive the chosen shape and its plan time */
 int sm2d_autotune(sm2d_handle h, int* shape4, float* best_ms);
+/* Lanes in flight of a plan (no counterpart in the reference): a plan fills
+ * lanes 0 .. n-1 only (0 or n >= lanes: every lane).  Fewer lanes in flight
+ * make each pass's working set smaller (claim rows, step records, pages) at
+ * the price of more passes; the results do not change.
+ * sm2d_tune_lanes_in_flight times every lane, 3/4, 1/2, 1/4, 1/8 and 1/16 of
+ * them (at least 8) on the plan sm2d_plan_load staged and keeps the fastest
+ * (sm2d_autotune does this first, then the launch shape). */
+int sm2d_set_lanes_in_flight(sm2d_handle h, int n);
+int sm2d_get_lanes_in_flight(sm2d_handle h, int* n);
+int sm2d_tune_lanes_in_flight(sm2d_handle h, int* lanes, float* best_ms);
 
 /* ---- host tables (no GPU needed) ---- */
 /* EnergyGrid(E_min,E_max,N) log grid (grids.cpp:6-24): edges[N+1], rep[N] */

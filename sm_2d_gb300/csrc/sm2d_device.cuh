@@ -16,7 +16,7 @@ namespace sm2d {
 constexpr uint32_t kEmpty = 0xFFFFFFFFu;
 constexpr int kKb = 32;
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr int kMaxLanes = 256;   // per-lane sums are staged in shared memory
+constexpr int kMaxLanes = 512;   // per-lane sums are staged in shared memory
 
 // One beam on the device (sm2d_beam).  kind 0: the runner's source (pencil
 // or LCG Gaussian, n samples); kind 1: the quadrature source, n samples over
@@ -89,6 +89,7 @@ struct IterGlobal {
     // spot plan (sm2d_batch_run): lanes that finish take the plan's next
     // spot inside the device loop; plan_n == 0 outside a plan
     int plan_n;            // spots of the plan
+    int lane_limit;        // lanes 0 .. lane_limit - 1 take the plan's spots (0: every lane)
     int plan_next;         // next spot to hand out
     int lane_max_it;       // iteration limit of one spot
     int refills;           // refill rounds run

@@ -553,15 +553,22 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         }
     }
     __syncthreads();
+    // the finished lanes, ascending (warp 0, 32 lanes a step)
+    if (threadIdx.x >= 32) return;
+    int nf = 0;
+    for (int l0 = 0; l0 < d.B; l0 += 32) {
+        const int ln = l0 + (int)threadIdx.x;
+        const bool f = ln < d.B && s_fin[ln];
+        const unsigned m = __ballot_sync(kFull, f);
+        if (f) gs->fin[nf + __popc(m & ((1u << threadIdx.x) - 1u))] = ln;
+        nf += __popc(m);
+    }
     if (threadIdx.x != 0) return;
     volatile IterGlobal* v = gs;
     const int nl = v->acc_listed, ni = v->acc_items, nb = v->acc_bins;
     gs->acc_listed = gs->acc_items = gs->acc_bins = 0;
     gs->gen = g;
     gs->ctag += 1u;   // claim pass of this iteration
-    int nf = 0;
-    for (int ln = 0; ln < d.B; ++ln)
-        if (s_fin[ln]) gs->fin[nf++] = ln;
     gs->n_fin = nf;
     // a cell or bin list that outgrew its capacity ends the run (reported by
     // the host API as SM2D_ERR_ALLOC); a plan runs on while a spot finished
@@ -1526,10 +1533,11 @@ __host__ __device__ inline void lane_result(const LaneState& L, sm2d_spot_result
 
 // Opens a plan of n spots, each limited to max_it iterations.
 __global__ void k_plan_begin(Dev d, const BeamArgs* beams, const float* fe, double* dose, sm2d_spot_result* res, int n,
-                             int max_it) {
+                             int max_it, int lane_limit) {
     if (threadIdx.x || blockIdx.x) return;
     IterGlobal* gs = d.gs;
     gs->plan_n = n;
+    gs->lane_limit = lane_limit;
     gs->plan_next = 0;
     gs->lane_max_it = max_it;
     gs->refills = 0;
@@ -1608,7 +1616,8 @@ __global__ void __launch_bounds__(256) k_lane_assign(Dev d, BeamArgs* beams) {
         }
         gs->n_fin = 0;
         int n = 0;
-        for (int ln = 0; ln < d.B && gs->plan_next < gs->plan_n; ++ln)
+        const int lim = gs->lane_limit > 0 ? min(gs->lane_limit, d.B) : d.B;
+        for (int ln = 0; ln < lim && gs->plan_next < gs->plan_n; ++ln)
             if (d.ls[ln].done && d.ls[ln].spot < 0) {
                 s_lane[n] = ln;
                 s_spot[n] = gs->plan_next++;
@@ -1618,21 +1627,23 @@ __global__ void __launch_bounds__(256) k_lane_assign(Dev d, BeamArgs* beams) {
         gs->refills += 1;
     }
     __syncthreads();
+    // each assigned lane's state cleared, its spot's tables and beam copied:
+    // one flat loop over (lane, element), every load independent
     const int Nz = d.Nz;
-    for (int k = 0; k < s_n; ++k) {
+    constexpr int NW = (int)(sizeof(LaneState) / 4);
+    for (int i = threadIdx.x; i < s_n * NW; i += blockDim.x)
+        reinterpret_cast<int*>(d.ls + s_lane[i / NW])[i % NW] = 0;
+    for (int i = threadIdx.x; i < s_n * Nz; i += blockDim.x) {
+        const int k = i / Nz, z = i % Nz, ln = s_lane[k];
+        const float* fe = gs->plan_fe + (size_t)s_spot[k] * (3 * Nz + 1);
+        d.feA[(size_t)ln * Nz + z] = fe[z];
+        d.feB[(size_t)ln * Nz + z] = fe[Nz + z];
+        d.feS[(size_t)ln * Nz + z] = fe[2 * Nz + z];
+    }
+    for (int k = threadIdx.x; k < s_n; k += blockDim.x) {
         const int ln = s_lane[k], sp = s_spot[k];
-        int* w = reinterpret_cast<int*>(d.ls + ln);
-        for (int i = threadIdx.x; i < (int)(sizeof(LaneState) / 4); i += blockDim.x) w[i] = 0;
-        const float* fe = gs->plan_fe + (size_t)sp * (3 * Nz + 1);
-        for (int i = threadIdx.x; i < Nz; i += blockDim.x) {
-            d.feA[(size_t)ln * Nz + i] = fe[i];
-            d.feB[(size_t)ln * Nz + i] = fe[Nz + i];
-            d.feS[(size_t)ln * Nz + i] = fe[2 * Nz + i];
-        }
-        if (threadIdx.x == 0) {
-            d.sx0[ln] = fe[3 * Nz];
-            beams[ln] = gs->plan_beams[sp];
-        }
+        d.sx0[ln] = gs->plan_fe[(size_t)sp * (3 * Nz + 1) + 3 * Nz];
+        beams[ln] = gs->plan_beams[sp];
     }
     __syncthreads();
     for (int k = threadIdx.x; k < s_n; k += blockDim.x) {
@@ -1670,6 +1681,7 @@ struct Ctx {
     int shape[4] = {8, 4, 0, 0};   // blocks per SM: warp-per-cell kernels, finalize, claim pass, deposit
                                    // pass (0: every resident block)
     int sms = 1;
+    int lanes_in_flight = 0;   // a plan fills lanes 0 .. lanes_in_flight - 1 (0: every lane)
     int grid_fin = 0;   // finalize: four blocks per SM (its per-block flushes of per-lane sums are atomics on a
                         // few addresses; 13.2 ms per wave of 80 spots against 14.2 at eight, 14.8 at three)
     size_t pages = 0;                        // value pages (every lane's region and the overflow pages)
@@ -2160,10 +2172,13 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     d.th = th_d; d.Ee = Ee_d; d.R = R_d; d.logE = lE_d; d.logR = lR_d;
     d.feA = c->fe_dev; d.feB = c->fe_dev + BN; d.feS = c->fe_dev + 2 * BN; d.sx0 = c->fe_dev + 3 * BN;
     // value pages: a single lane has one per slot of every cell; a lane of a
-    // batch has slot_pages_per_lane (default 16384; a spot of the 512-spot
-    // plan peaks below 2000), plus 32 overflow pages after the last region
+    // batch has slot_pages_per_lane, by default 32 MB of values (32768 pages of
+    // 256 values, 65536 of 128: the widest 70 MeV spot of the 512-spot plan
+    // peaks at 4422 slots on the reference grids and at about 20000 on the
+    // 256 log-E / 512 theta grid), plus 32 overflow pages after the last region
+    const size_t def_pages = ((size_t)8 << 20) / (size_t)c->L;
     d.pool_lane = B == 1 ? (int)(Nc * kKb)
-                         : (int)std::min<size_t>(Nc * kKb, p->slot_pages_per_lane > 0 ? (size_t)p->slot_pages_per_lane : 16384);
+                         : (int)std::min<size_t>(Nc * kKb, p->slot_pages_per_lane > 0 ? (size_t)p->slot_pages_per_lane : def_pages);
     if ((size_t)d.pool_lane * B + kKb > (size_t)INT_MAX) return bail(fail(SM2D_ERR_ARG, "too many value pages"));
     c->pages = (size_t)d.pool_lane * B + kKb;
     A(d.bid, uint32_t, ns);
@@ -2180,14 +2195,16 @@ int sm2d_create(const sm2d_problem* p, sm2d_handle* out) {
     A(d.dl_edep, double, NcB); A(d.dl_ecut, double, NcB); A(d.dl_enuc, double, NcB); A(d.dl_ebnd, double, NcB);
     A(d.dl_wcut, float, NcB); A(d.dl_wnuc, float, NcB); A(d.dl_wbnd, float, NcB);
     A(d.act_gen, unsigned long long, NcB); A(d.cls, uint8_t, NcB); A(d.c2b, int, NcB);
-    // cell list: every cell of a single lane; an eighth of the cells (at
-    // least 4096) per lane of a batch -- a spot lists a few percent
-    d.listed_cap = B == 1 ? (int)Nc : (int)std::min<size_t>(NcB, (size_t)B * std::max<size_t>(Nc / 8, 4096));
+    // cell list: every cell of a single lane; 2048 cells per lane of a batch,
+    // shared by its lanes (a plan spot lists about a hundred cells a pass)
+    d.listed_cap = B == 1 ? (int)Nc : (int)std::min<size_t>(NcB, (size_t)B * std::min<size_t>(Nc, 2048));
     A(d.listed, uint32_t, d.listed_cap);
     // bin list: the w > 0 bins of one full slot per cell of a single lane on
-    // average, a quarter of that per lane of a batch (a spot holds a few
-    // hundred thousand); a pass that needs more stops with SM2D_ERR_ALLOC
-    d.bins_cap = (int)std::min<size_t>((B == 1 ? Nc * c->L : NcB * c->L / 4), (size_t)INT_MAX);
+    // average; per lane of a batch 32 per value page, shared by the lanes (a
+    // plan spot transports about 4000 a pass on average); a pass that needs
+    // more stops with SM2D_ERR_ALLOC
+    d.bins_cap = (int)std::min<size_t>((B == 1 ? Nc * c->L : (size_t)B * std::min<size_t>(Nc * c->L / 4, (size_t)d.pool_lane * 32)),
+                                       (size_t)INT_MAX);
     A(d.bins, uint4, d.bins_cap);
     A(d.cell_bins, int2, d.listed_cap);
     A(d.brec, uint4, 2 * (size_t)d.bins_cap);
@@ -2921,7 +2938,7 @@ int sm2d_plan_run_async(sm2d_handle h) {
     if (rc) return rc;
     if ((rc = reset_lanes(c))) return rc;
     k_plan_begin<<<1, 1, 0, c.s>>>(c.d, c.plan_beams_dev, c.plan_fe_dev, c.plan_dose_on ? c.plan_dose_dev : nullptr,
-                                   c.plan_res_dev, c.plan_n, c.plan_max_it);
+                                   c.plan_res_dev, c.plan_n, c.plan_max_it, c.lanes_in_flight);
     CK(cudaGetLastError());
     if ((rc = DISPATCH(c, refill, 0))) return rc;   // the first spots into every lane
     CK(cudaGraphLaunch(c.exec, c.s));
@@ -3058,10 +3075,74 @@ int sm2d_set_launch_shape(sm2d_handle h, const int* shape4) {
 // candidate is timed on one run of the whole plan (CUDA events on the engine's
 // stream, after one untimed run of the shape) and the fastest is kept.  The
 // result does not depend on the shape (claims follow keys, not launch order).
+int sm2d_set_lanes_in_flight(sm2d_handle h, int n) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    if (n < 0) return fail(SM2D_ERR_ARG, "lanes in flight %d", n);
+    h->lanes_in_flight = n >= h->B ? 0 : n;
+    return 0;
+}
+
+int sm2d_get_lanes_in_flight(sm2d_handle h, int* n) {
+    if (!h || !n) return fail(SM2D_ERR_ARG, "null argument");
+    *n = h->lanes_in_flight > 0 ? h->lanes_in_flight : h->B;
+    return 0;
+}
+
+// One run of the loaded plan to warm the current settings, then one timed.
+static int time_plan(sm2d_handle h, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+    Ctx& c = *h;
+    int rc = sm2d_plan_run_async(h);
+    if (!rc && cudaEventRecord(e0, c.s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event");
+    if (!rc) rc = sm2d_plan_run_async(h);
+    if (!rc && cudaEventRecord(e1, c.s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event");
+    if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event sync");
+    if (!rc && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event time");
+    return rc;
+}
+
+int sm2d_tune_lanes_in_flight(sm2d_handle h, int* lanes, float* best_ms) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    Ctx& c = *h;
+    if (c.plan_n == 0) return fail(SM2D_ERR_STATE, "sm2d_tune_lanes_in_flight before sm2d_plan_load");
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    // every lane, then 3/4, 1/2, 1/4, 1/8 and 1/16 of them (at most the
+    // plan's spots, at least 8): each fewer lane in flight is a smaller working
+    // set a pass, against a fixed cost per pass shared by fewer lanes
+    const int top = std::min(c.B, c.plan_n);
+    const int frac16[6] = {16, 12, 8, 4, 2, 1};
+    int best = 0, rc = 0, prev = -1;
+    float best_t = 0.0f;
+    for (int q = 0; q < 6 && !rc; ++q) {
+        const int n = std::max(std::min(top, 8), top * frac16[q] / 16);
+        if (n == prev) continue;
+        prev = n;
+        c.lanes_in_flight = n >= c.B ? 0 : n;
+        float t = 0.0f;
+        rc = time_plan(h, e0, e1, &t);
+        if (!rc && (best == 0 || t < best_t)) {
+            best_t = t;
+            best = n;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    c.lanes_in_flight = best >= c.B ? 0 : best;
+    if (lanes) *lanes = best;
+    if (best_ms) *best_ms = best_t;
+    return 0;
+}
+
 int sm2d_autotune(sm2d_handle h, int* shape4, float* best_ms) {
     if (!h) return fail(SM2D_ERR_ARG, "null handle");
     Ctx& c = *h;
     if (c.plan_n == 0) return fail(SM2D_ERR_STATE, "sm2d_autotune before sm2d_plan_load");
+    {   // the lanes in flight first, with the current shape
+        const int rc = sm2d_tune_lanes_in_flight(h, nullptr, nullptr);
+        if (rc) return rc;
+    }
     int per_sm_keys = 0, per_sm_dep = 0;
     {
         int k = 0, t = 0;
@@ -3077,14 +3158,9 @@ int sm2d_autotune(sm2d_handle h, int* shape4, float* best_ms) {
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    auto time_shape = [&](const int* sh, float* ms) -> int {
+    auto time_shape = [&](const int* sh, float* ms) -> int {   // the first run captures the loop again
         int rc = sm2d_set_launch_shape(h, sh);
-        if (!rc) rc = sm2d_plan_run_async(h);   // captures the loop, warms the shape
-        if (!rc && cudaEventRecord(e0, c.s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event");
-        if (!rc) rc = sm2d_plan_run_async(h);
-        if (!rc && cudaEventRecord(e1, c.s) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event");
-        if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event sync");
-        if (!rc && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) rc = fail(SM2D_ERR_CUDA, "event time");
+        if (!rc) rc = time_plan(h, e0, e1, ms);
         return rc;
     };
     int best[4];

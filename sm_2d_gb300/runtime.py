@@ -187,6 +187,9 @@ def lib(build_if_needed: bool = True):
         L.sm2d_plan_results.argtypes = [P, P, P]
         L.sm2d_plan_stats.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(D)]
         L.sm2d_page_stats.argtypes = [P, C.POINTER(I), C.POINTER(I)]
+        L.sm2d_set_lanes_in_flight.argtypes = [P, I]
+        L.sm2d_get_lanes_in_flight.argtypes = [P, C.POINTER(I)]
+        L.sm2d_tune_lanes_in_flight.argtypes = [P, C.POINTER(I), C.POINTER(F)]
         L.sm2d_set_surrogate.argtypes = [P, P, F, I, I]
         L.sm2d_get_launch_shape.argtypes = [P, P]
         L.sm2d_set_launch_shape.argtypes = [P, P]
@@ -291,7 +294,7 @@ class Config:
     density_z: np.ndarray = None   # slab phantom: density per depth row (None: water)
     expectation: int = 0    # 1: expectation form (redistribution weights instead of MCS/straggling draws)
     precision_form: int = 0  # 1: audit books weight increments; R-LUT inverted in double below 10 MeV
-    slot_pages_per_lane: int = 0  # value pages per lane of a batch engine (0: 16384)
+    slot_pages_per_lane: int = 0  # value pages per lane of a batch engine (0: 2^23 / local bins)
 
     def production(self):
         """Options of a production run: deterministic rank-ordered seeds salted
@@ -404,11 +407,28 @@ class Transport:
         check(self._lib.sm2d_set_launch_shape(self.h, _p(np.ascontiguousarray(shape, np.int32))))
 
     def autotune(self):
-        """Tune the launch shape on the loaded plan; returns (shape, plan ms)."""
+        """Tune the lanes in flight, then the launch shape, on the loaded plan;
+        returns (shape, plan ms)."""
         o = np.zeros(4, np.int32)
         ms = C.c_float()
         check(self._lib.sm2d_autotune(self.h, _p(o), C.byref(ms)))
         return o.tolist(), ms.value
+
+    def lanes_in_flight(self):
+        n = C.c_int()
+        check(self._lib.sm2d_get_lanes_in_flight(self.h, C.byref(n)))
+        return n.value
+
+    def set_lanes_in_flight(self, n):
+        """A plan fills lanes 0..n-1 only (0: every lane); speed, not results."""
+        check(self._lib.sm2d_set_lanes_in_flight(self.h, int(n)))
+
+    def tune_lanes_in_flight(self):
+        """Time every lane, 3/4, 1/2, 1/4, 1/8 and 1/16 of them (at least 8) on
+        the loaded plan and keep the fastest; returns (lanes, plan ms)."""
+        n, ms = C.c_int(), C.c_float()
+        check(self._lib.sm2d_tune_lanes_in_flight(self.h, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
 
     # -- learned surrogate in the fine step (expectation form)
     def set_surrogate(self, surrogate, tol=0.005, max_rows=0, method_tables=False):

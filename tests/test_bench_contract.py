@@ -37,13 +37,13 @@ def test_lanes_follow_free_memory(workload):
     per = bench.lane_bytes(cfg)
     nc = cfg.Nx * cfg.Nz
     dense = nc * 32 * 1028                     # every slot of every cell with its 256 values
-    pages = min(nc * 32, 16384) * 1024         # the lane's value pages
+    pages = min(nc * 32, 32768) * 1024         # the lane's value pages
     assert pages + nc * 4096 < per < dense / 2  # pages and psi_out claim rows, far below a dense phase space
     assert bench.auto_lanes(cfg, 0) == 1       # always at least one lane
-    assert bench.auto_lanes(cfg, 10 ** 15) == 256
+    assert bench.auto_lanes(cfg, 10 ** 15) == 512
     free = 280 * 2 ** 30
     n = bench.auto_lanes(cfg, free)
-    assert n * per <= 0.85 * free < (n + 1) * per or n == 256
+    assert n * per <= 0.85 * free < (n + 1) * per or n == 512
 
 
 @pytest.mark.parametrize("grid,workload", [("reference", "plan512"), ("log", "plan512"), ("reference", "c3")])
