@@ -243,11 +243,10 @@ struct Dev {
     unsigned long long* ctab;  // claim tables: B * Nc psi_out rows, then 4 * listed_cap bucket rows
     int* ccount;               // gathered ids per claim-table row
     uint32_t* bkt_ids;         // kept ids of each bucket row [4 * listed_cap][32]
-    // per kept bucket id (bucket row, position): the id, its psi_out slot in
-    // the cell behind the face and that slot's id (bkt_slot_pack)
+    // per kept bucket id (bucket row, position): the value page of its psi_out
+    // slot in the cell behind the face and that slot's id (bkt_slot_pack),
+    // resolved once per pass by the selection [4 * listed_cap][32]
     uint2* bkt_os;
-                               // (x = slot or -1, y = the kept id there), resolved once per pass by
-                               // the selection [4 * listed_cap][32]
 };
 
 __device__ __forceinline__ int lane_of(const Dev& d, int gc) { return gc / d.Nc; }
@@ -511,14 +510,12 @@ __device__ __forceinline__ int remap_lidx(int l, uint32_t src, uint32_t dst) {
     return Lay::enc(td, ed, x, z);
 }
 
-// An entry of bkt_os: x = the bucket's kept id (24 bits) | (psi_out slot + 1)
-// << 24, y = the id of that psi_out slot (kEmpty: none); one 8-byte load
-// gives the fused K4 everything its resolve of a bucket id needs.
-__device__ __forceinline__ uint2 bkt_slot_pack(uint32_t id, int os, uint32_t sel) {
-    return make_uint2((id & 0xFFFFFFu) | ((uint32_t)(os + 1) << 24), sel);
-}
-__device__ __forceinline__ uint32_t bkt_slot_id(uint2 m) { return m.x & 0xFFFFFFu; }
-__device__ __forceinline__ int bkt_slot_os(uint2 m) { return (int)(m.x >> 24) - 1; }
+// An entry of bkt_os: x = the value page of the psi_out slot that the
+// bucket's kept id lands in (0xFFFFFFFF: none), y = the id that slot holds;
+// one 8-byte load gives the fused K4 everything its resolve of a bucket id
+// needs, the page included.
+__device__ __forceinline__ uint2 bkt_slot_pack(int page, uint32_t sel) { return make_uint2((uint32_t)page, sel); }
+__device__ __forceinline__ int bkt_slot_page(uint2 m) { return (int)m.x; }
 
 // Value page of storage slot s of cell gc.  RO: pbase is read-only for the
 // rest of the kernel (written by an earlier kernel of the pass).

@@ -960,9 +960,10 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
     for (int wi = (which ? 0 : gs->occ_mark) + blockIdx.x * NW + wid; wi < n; wi += gridDim.x * NW) {
         const int gc = d.occ_list[k][wi];
         const int nk = select_row(psi_row(d, gc), d.ccount + gc, tag, s_sel[wid], d.bid + (size_t)gc * kKb, lane);
+        int pb = 0;
         if (lane == 0) {   // one page per kept slot, consecutive, from the lane's region
             const int ln = lane_of(d, gc);
-            int pb = d.pool_lane * d.B;   // no slot, or the region is full: the overflow pages
+            pb = d.pool_lane * d.B;   // no slot, or the region is full: the overflow pages
             if (nk > 0) {
                 const int p0 = atomicAdd(&d.ls[ln].pool_top, nk);
                 if (p0 + nk <= d.pool_lane) pb = ln * d.pool_lane + p0;
@@ -1019,12 +1020,13 @@ __global__ void __launch_bounds__(kThreads) k_select_psi(Dev d, int which) {
                 }
             }
         }
+        pb = __shfl_sync(kFull, pb, 0);   // the cell's first page (lane 0's allocation)
 #pragma unroll
         for (int f = 0; f < 4; ++f) {
             const uint32_t sel = __shfl_sync(kFull, kp, os[f] >= 0 ? os[f] : 0);
             if (base[f] >= 0)
                 d.bkt_os[(size_t)(base[f] + f) * kKb + lane] =
-                    bkt_slot_pack(id[f], os[f], os[f] >= 0 ? sel : (id[f] != kEmpty ? id[f] : kEmpty));
+                    bkt_slot_pack(os[f] >= 0 ? pb + os[f] : -1, os[f] >= 0 ? sel : (id[f] != kEmpty ? id[f] : kEmpty));
         }
     }
     __syncthreads();

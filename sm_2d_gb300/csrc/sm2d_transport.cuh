@@ -238,15 +238,15 @@ __device__ __forceinline__ float put(const Dev& d, const Src& src, int par, int 
                 return 0.0f;
             }
             // K4 of the fused pass: the bucket's kept id lands in dcell's psi_out
-            // slot that the selection resolved for it
-            const int os = bkt_slot_os(m);
-            if (os >= 0) {
+            // slot (its value page) that the selection resolved for it
+            const int pg = bkt_slot_page(m);
+            if (pg >= 0) {
                 const uint32_t seld = m.y;
                 const int le2 = (seld == selb) ? le : remap_lidx<Lay>(le, selb, seld);
                 if (seld != selb && d.esplit)
                     atomicAdd(d.dl_edep + bcell,
                               (double)((e_center(d, ebin_of<Lay>(d, selb, le)) - e_center(d, ebin_of<Lay>(d, seld, le2))) * w));
-                vadd(d, page_of<true>(d, dcell, os), Lay::L, le2, w);
+                vadd(d, (size_t)pg, Lay::L, le2, w);
                 return 0.0f;
             }
             stage = 2;
