@@ -664,11 +664,13 @@ __device__ __forceinline__ T seg_sum(T v, const unsigned (&same)[5]) {
 // increments in the dl_* arrays (one atomic per cell run of a warp) and the
 // per-lane drop sums (staged per block in shared memory); psi_out's weight
 // and energy for the audit are summed by the finalize kernel.  Resident blocks
-// per SM: five for the claim pass (47 registers, no spills; 27.2 -> 24.1 ms
-// per wave of 80 spots against four), four for the deposit passes (five
-// would spill).
+// per SM: five for the claim passes (48 registers, no spills; 27.2 -> 24.1 ms
+// per wave of 80 spots against four) and for the sampled form's deposit pass,
+// which spills 88 bytes and still gains from the warps (175.1 -> 170.2 us a
+// pass at 512 lanes; 196 at three blocks); four for the expectation form's
+// and the bucket mode's deposit passes (five would spill 0.7-1 KB).
 template <class Lay, int PASS, bool EXP = false>
-__global__ void __launch_bounds__(kThreads, PASS == PASS_KEYS ? 5 : 4) k_transport(Dev d) {
+__global__ void __launch_bounds__(kThreads, (PASS == PASS_KEYS || (PASS == PASS_DIRECT && !EXP)) ? 5 : 4) k_transport(Dev d) {
     __shared__ LaneSums<2> s_sum;   // drop_w, drop_e
     IterGlobal* gs = d.gs;
     if (gs->halt) return;
