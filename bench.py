@@ -577,11 +577,12 @@ def run_gpu_arm(args):
             cell_steps += sum(r["cell_steps"] for r in rs)
             bins_done += bins
             iters = [r["iterations"] for r in rs]
-            # reset 3, plan begin 1, first fill 8 (dose/tally clear, lane
-            # assignment, injection 6), plan end 1; per pass of the device loop
-            # (the halting one included) classify, claim pass, bucket and psi_out
-            # selection, deposit pass, finalize (+ bucket move); 8 per refill
-            launches += 13 + (passes + 1) * per_pass + 8 * (refills - 1)
+            # reset 3, plan begin 1, first fill 9 (dose/tally clear, lane
+            # assignment and fill, injection 6), plan end 1; per pass of the
+            # device loop (the halting one included) classify, claim pass,
+            # bucket and psi_out selection, deposit pass, finalize (+ bucket
+            # move); 9 per refill
+            launches += 14 + (passes + 1) * per_pass + 9 * (refills - 1)
     barrier()
     total_ms = max_over_ranks(np.sum(times), dist, "cuda")
     value = args.steps * n * world / (total_ms / 1e3)

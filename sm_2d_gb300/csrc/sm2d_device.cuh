@@ -97,6 +97,8 @@ struct IterGlobal {
     int occ_mark;          // psi_in's occupancy list length when the injection opened
     int n_fin;             // lanes whose spot finished at this classification
     int fin[kMaxLanes];    // those lanes, ascending
+    int n_fill;            // lanes the last refill assigned, and their spots
+    int fill_lane[kMaxLanes], fill_spot[kMaxLanes];
     const BeamArgs* plan_beams;   // [plan_n]
     const float* plan_fe;         // [plan_n][3 Nz + 1]: A(z), B(z), sigma_total(z), sigma_x
     double* plan_dose;            // [plan_n][Nc] convolved dose, or null

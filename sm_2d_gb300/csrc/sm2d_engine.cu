@@ -1608,53 +1608,81 @@ __global__ void __launch_bounds__(128) k_lane_complete(Dev d) {
 // Results of the finished spots, then the plan's next spots into the idle
 // lanes in lane order: lane state cleared, beam and Fermi-Eyges tables of
 // the spot, refill flag for the injection kernels that follow.  One block.
-__global__ void __launch_bounds__(256) k_lane_assign(Dev d, BeamArgs* beams) {
-    __shared__ int s_lane[kMaxLanes], s_spot[kMaxLanes];
-    __shared__ int s_n;
+__global__ void __launch_bounds__(256) k_lane_assign(Dev d) {
+    __shared__ int s_cnt[256];
     IterGlobal* gs = d.gs;
-    if (threadIdx.x == 0) {
-        for (int j = 0; j < gs->n_fin; ++j) {
-            LaneState& L = d.ls[gs->fin[j]];
-            if (L.spot >= 0 && gs->plan_res) lane_result(L, gs->plan_res[L.spot]);
-            L.spot = -1;
-        }
-        gs->n_fin = 0;
-        int n = 0;
-        const int lim = gs->lane_limit > 0 ? min(gs->lane_limit, d.B) : d.B;
-        for (int ln = 0; ln < lim && gs->plan_next < gs->plan_n; ++ln)
-            if (d.ls[ln].done && d.ls[ln].spot < 0) {
-                s_lane[n] = ln;
-                s_spot[n] = gs->plan_next++;
-                ++n;
-            }
-        s_n = n;
-        gs->refills += 1;
+    const int tid = threadIdx.x;
+    // results of the lanes whose spot just finished
+    for (int j = tid; j < gs->n_fin; j += blockDim.x) {
+        LaneState& L = d.ls[gs->fin[j]];
+        if (L.spot >= 0 && gs->plan_res) lane_result(L, gs->plan_res[L.spot]);
+        L.spot = -1;
     }
     __syncthreads();
-    // each assigned lane's state cleared, its spot's tables and beam copied:
-    // one flat loop over (lane, element), every load independent
-    const int Nz = d.Nz;
+    // idle lanes in lane order take the plan's next spots: thread t looks at
+    // the lanes t * per .. t * per + per - 1, a block scan orders them
+    const int lim = gs->lane_limit > 0 ? min(gs->lane_limit, d.B) : d.B;
+    const int per = (lim + blockDim.x - 1) / blockDim.x;
+    int mine = 0;
+    for (int k = 0; k < per; ++k) {
+        const int ln = tid * per + k;
+        if (ln < lim && d.ls[ln].done && d.ls[ln].spot < 0) ++mine;
+    }
+    s_cnt[tid] = mine;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {   // inclusive scan
+        const int y = tid >= o ? s_cnt[tid - o] : 0;
+        __syncthreads();
+        s_cnt[tid] += y;
+        __syncthreads();
+    }
+    const int next = gs->plan_next, left = max(gs->plan_n - next, 0);
+    const int total = min(s_cnt[blockDim.x - 1], left);
+    int r = s_cnt[tid] - mine;
+    for (int k = 0; k < per && r < total; ++k) {
+        const int ln = tid * per + k;
+        if (ln < lim && d.ls[ln].done && d.ls[ln].spot < 0) {
+            gs->fill_lane[r] = ln;
+            gs->fill_spot[r] = next + r;
+            ++r;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        gs->n_fin = 0;
+        gs->n_fill = total;
+        gs->plan_next = next + total;
+        gs->refills += 1;
+    }
+}
+
+// The lanes the refill assigned: state cleared, the spot's tables and beam
+// copied, marked for the injection; a grid over (lane, element).
+__global__ void __launch_bounds__(256) k_lane_fill(Dev d, BeamArgs* beams) {
+    const IterGlobal* gs = d.gs;
+    const int n = gs->n_fill, Nz = d.Nz;
     constexpr int NW = (int)(sizeof(LaneState) / 4);
-    for (int i = threadIdx.x; i < s_n * NW; i += blockDim.x)
-        reinterpret_cast<int*>(d.ls + s_lane[i / NW])[i % NW] = 0;
-    for (int i = threadIdx.x; i < s_n * Nz; i += blockDim.x) {
-        const int k = i / Nz, z = i % Nz, ln = s_lane[k];
-        const float* fe = gs->plan_fe + (size_t)s_spot[k] * (3 * Nz + 1);
+    const int per = NW + Nz;   // LaneState words, then the depth rows of the tables
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x, st = gridDim.x * blockDim.x;
+    for (int i = i0; i < n * per; i += st) {
+        const int k = i / per, e = i % per, ln = gs->fill_lane[k], sp = gs->fill_spot[k];
+        if (e < NW) {
+            int v = 0;
+            if (e == (int)(offsetof(LaneState, spot) / 4)) v = sp;
+            if (e == (int)(offsetof(LaneState, refill) / 4)) v = 1;
+            if (e == (int)(offsetof(LaneState, done) / 4)) v = 1;
+            reinterpret_cast<int*>(d.ls + ln)[e] = v;
+            continue;
+        }
+        const int z = e - NW;
+        const float* fe = gs->plan_fe + (size_t)sp * (3 * Nz + 1);
         d.feA[(size_t)ln * Nz + z] = fe[z];
         d.feB[(size_t)ln * Nz + z] = fe[Nz + z];
         d.feS[(size_t)ln * Nz + z] = fe[2 * Nz + z];
-    }
-    for (int k = threadIdx.x; k < s_n; k += blockDim.x) {
-        const int ln = s_lane[k], sp = s_spot[k];
-        d.sx0[ln] = gs->plan_fe[(size_t)sp * (3 * Nz + 1) + 3 * Nz];
-        beams[ln] = gs->plan_beams[sp];
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < s_n; k += blockDim.x) {
-        LaneState& L = d.ls[s_lane[k]];
-        L.spot = s_spot[k];
-        L.refill = 1;
-        L.done = 1;
+        if (z == 0) {
+            d.sx0[ln] = fe[3 * Nz];
+            beams[ln] = gs->plan_beams[sp];
+        }
     }
 }
 
@@ -1844,7 +1872,8 @@ struct Impl {
     static int refill(Ctx& c, int) {
         const size_t smem = sizeof(double) * (size_t)c.dose_stride;
         k_lane_complete<<<dim3((unsigned)c.d.Nz, (unsigned)c.B), 128, smem, c.s>>>(c.d);
-        k_lane_assign<<<1, 256, 0, c.s>>>(c.d, c.beams_dev);
+        k_lane_assign<<<1, 256, 0, c.s>>>(c.d);
+        k_lane_fill<<<(unsigned)std::min(c.B * 4, 2048), 256, 0, c.s>>>(c.d, c.beams_dev);
         CK(cudaGetLastError());
         return inject(c, c.plan_max_n, false, true);
     }

@@ -175,6 +175,27 @@ def test_lanes_in_flight_change_speed_not_results():
     assert passes_two > max(x["iterations"] for x in r_all)
 
 
+def test_plan_on_the_engine_lane_limit():
+    """600 small uneven spots on 512 lanes, the engine's limit: the first fill
+    takes 512 spots, the refills the other 88 (finished-lane lists over 16
+    warp steps, per-lane sums staged for 512 lanes).  Spots taken from the
+    start, the middle and the refills equal the same spots run alone."""
+    rng = np.random.default_rng(77)
+    beams = [Beam(float(rng.uniform(-3.0, 3.0)), 0.0, 0.0, float(rng.choice([20.0, 25.0, 30.0, 35.0])), 1.0,
+                  float(rng.uniform(0.8, 2.0)), 0.002, 0.3, 100, 1000 + i) for i in range(600)]
+    with sm.Transport(_cfg(512)) as many:
+        assert many.lanes == 512
+        dose, res = many.batch_run(beams, 3000)
+        passes, refills, _ = many.plan_stats()
+    assert all(r["finished"] for r in res) and refills >= 2
+    assert passes < max(r["iterations"] for r in res) * 2
+    for i in (0, 257, 511, 512, 599):
+        ref = _single(beams[i])
+        assert res[i]["iterations"] == ref["n"], (i, res[i]["iterations"], ref["n"])
+        m = ref["dose"].max()
+        assert np.abs(dose[i] - ref["dose"]).max() <= 1e-5 * m, i
+
+
 def test_batch_refuses_bad_beams():
     with sm.Transport(_cfg(2)) as t:
         bad = [Beam(0.0, 0.0, 0.0, 40.0, 1.0, 1.5, 0.002, 0.4, 0, 1)]   # Gaussian without samples
