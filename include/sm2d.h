@@ -276,9 +276,12 @@ int sm2d_lanes(sm2d_handle h);
  * `lanes` spots are in flight; a lane whose spot finishes takes the next
  * spot of the plan inside the device loop (one graph launch for the plan).
  * dose: host [n_spots][Nz][Nx] for the post-convolved EdepC of each spot,
- * or NULL; results: host [n_spots] or NULL.  A spot that reaches
- * max_iterations ends there: its remaining weight is booked as a transport
- * drop and its result reads finished = 0.  Blocking. */
+ * or NULL; results: host [n_spots] or NULL.  When dose is pinned host memory
+ * (cudaHostAlloc, cudaHostRegister) the device writes each spot's map there as
+ * the spot completes, overlapped with the other spots' transport; other
+ * memory receives one copy at the end.  A spot that reaches max_iterations
+ * ends there: its remaining weight is booked as a transport drop and its
+ * result reads finished = 0.  Blocking. */
 int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, double* dose,
                    sm2d_spot_result* results);
 /* The three steps of sm2d_batch_run: sm2d_plan_load stages the plan on the

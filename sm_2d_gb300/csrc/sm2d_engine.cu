@@ -1737,6 +1737,7 @@ struct Ctx {
     float* plan_fe_dev = nullptr;
     sm2d_spot_result* plan_res_dev = nullptr;
     double* plan_dose_dev = nullptr;
+    double* plan_dose_ext = nullptr;  // sm2d_batch_run: the caller's pinned host maps, written by the device
     std::vector<BeamArgs> plan_beams_host;
     std::vector<float> plan_fe_host;
     // the learned surrogate in the expectation form's K3 (sm2d_set_surrogate)
@@ -2970,7 +2971,8 @@ int sm2d_plan_run_async(sm2d_handle h) {
     int rc = build_graph(c);   // captured again after a change of the pass (surrogate, launch shape)
     if (rc) return rc;
     if ((rc = reset_lanes(c))) return rc;
-    k_plan_begin<<<1, 1, 0, c.s>>>(c.d, c.plan_beams_dev, c.plan_fe_dev, c.plan_dose_on ? c.plan_dose_dev : nullptr,
+    double* dose_out = c.plan_dose_on ? (c.plan_dose_ext ? c.plan_dose_ext : c.plan_dose_dev) : nullptr;
+    k_plan_begin<<<1, 1, 0, c.s>>>(c.d, c.plan_beams_dev, c.plan_fe_dev, dose_out,
                                    c.plan_res_dev, c.plan_n, c.plan_max_it, c.lanes_in_flight);
     CK(cudaGetLastError());
     if ((rc = DISPATCH(c, refill, 0))) return rc;   // the first spots into every lane
@@ -3232,10 +3234,24 @@ int sm2d_autotune(sm2d_handle h, int* shape4, float* best_ms) {
 
 int sm2d_batch_run(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_iterations, double* dose,
                    sm2d_spot_result* results) {
+    if (!h) return fail(SM2D_ERR_ARG, "null handle");
+    // dose maps into pinned host memory are written there by the device as
+    // each spot completes, overlapped with the transport of the others;
+    // other memory receives one copy at the end
+    double* ext = nullptr;
+    if (dose) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, dose) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer)
+            ext = static_cast<double*>(a.devicePointer);
+        (void)cudaGetLastError();
+    }
     int rc = sm2d_plan_load(h, beams, n_spots, max_iterations, dose ? 1 : 0);
     if (rc) return rc;
-    if ((rc = sm2d_plan_run_async(h))) return rc;
-    return sm2d_plan_results(h, dose, results);
+    h->plan_dose_ext = ext;
+    rc = sm2d_plan_run_async(h);
+    if (!rc) rc = sm2d_plan_results(h, ext ? nullptr : dose, results);
+    h->plan_dose_ext = nullptr;
+    return rc;
 }
 
 }  // extern "C"
