@@ -820,7 +820,7 @@ __device__ __forceinline__ void tally_cell(const Dev& d, int idx, int lane, Lane
 // ties).  Each entry's key is replaced by its slot for the deposit pass.
 // Returns the number of kept ids.
 struct SelScratch {
-    uint32_t bid[kCand], key[kCand];
+    unsigned long long kb[kCand];   // claim key << 32 | block id: the order of the row's ids
     uint8_t idx[kCand], rank[kCand];
     uint32_t kept[kKb];
 };
@@ -842,30 +842,45 @@ __device__ int select_row(unsigned long long* row, int* count, uint32_t tag, Sel
             const unsigned m = __ballot_sync(kFull, cur);
             if (cur) {
                 const int p = n + __popc(m & lt);
-                sh.bid[p] = (uint32_t)e[q].x;
-                sh.key[p] = (uint32_t)e[q].y;
+                sh.kb[p] = ((unsigned long long)(uint32_t)e[q].y << 32) | (uint32_t)e[q].x;
                 sh.idx[p] = (uint8_t)i;
             }
             n += __popc(m);
         }
     }
     __syncwarp();
-    for (int j = lane; j < n; j += 32) {
-        const uint32_t kj = sh.key[j], bj = sh.bid[j];
-        int r = 0;
-        for (int m = 0; m < n; ++m) {
-            const uint32_t km = sh.key[m];
-            r += (km < kj || (km == kj && sh.bid[m] < bj)) ? 1 : 0;
+    // the rank of each gathered id by (key, id): every entry is read once
+    // (one 8-byte broadcast load) and compared with the lane's entries held in
+    // registers, four a lane a round
+    for (int j0 = 0; j0 < n; j0 += 128) {
+        unsigned long long c[4];
+        int r[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = j0 + 32 * u + lane;
+            c[u] = j < n ? sh.kb[j] : ~0ull;
+            r[u] = 0;
         }
-        sh.rank[j] = (uint8_t)r;
-        if (r < kKb) sh.kept[r] = bj;
+        for (int m = 0; m < n; ++m) {
+            const unsigned long long x = sh.kb[m];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) r[u] += x < c[u] ? 1 : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = j0 + 32 * u + lane;
+            if (j < n) {
+                sh.rank[j] = (uint8_t)r[u];
+                if (r[u] < kKb) sh.kept[r[u]] = (uint32_t)c[u];
+            }
+        }
     }
     __syncwarp();
     const int nk = min(n, kKb);
     for (int j = lane; j < n; j += 32) {
         int slot = sh.rank[j];
         if (slot >= kKb) {
-            const uint32_t want = sh.bid[j];
+            const uint32_t want = (uint32_t)sh.kb[j];
             int bd = 0x7fffffff;
             for (int k = 0; k < kKb; ++k) {
                 const int dd = bid_distance(sh.kept[k], want);
@@ -873,7 +888,7 @@ __device__ int select_row(unsigned long long* row, int* count, uint32_t tag, Sel
             }
         }
         // the slot and the id it holds: a found id resolves in one probe
-        const uint32_t sel = sh.rank[j] < kKb ? sh.bid[j] : sh.kept[slot];
+        const uint32_t sel = sh.rank[j] < kKb ? (uint32_t)sh.kb[j] : sh.kept[slot];
         row[2 * (int)sh.idx[j] + 1] =
             ((unsigned long long)(0xFFFFFFFFu - tag) << 32) | (uint32_t)slot | ((sel & 0xFFFFFFu) << 5);
     }
