@@ -73,7 +73,7 @@ struct IterGlobal {
     int n_listed;          // cells of this pass (active + coarse, all lanes)
     int n_items;           // claimed slots of the listed cells
     int n_bins;            // w > 0 local bins of the listed cells (transport work)
-    int acc_listed, acc_items, acc_bins;   // classify counters
+    unsigned long long acc_lb;   // classify: listed cells << 32 | their w > 0 bins (one reservation a cell)
     int pool_peak;         // the most value pages one lane held (since the last reset)
     int bin_ovf;           // the cell list, bin list or a lane's value pages outgrew their capacity
                            // (since the last reset)

@@ -422,25 +422,27 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         const bool prev = d.act_gen[c] == g - 1;
         const bool act = !light && (c_on || (prev && c_off)) && ws > d.wmin;
         const int cls = light ? 0 : (act ? 2 : (hw ? 1 : 0));
-        int base = 0;
+        int base = 0, in_list = 0;
         if (lane == 0) {
             d.cls[c] = (uint8_t)cls;
             if (act) d.act_gen[c] = g;
             if (cls) {
-                const int idx = atomicAdd(&gs->acc_listed, 1);
-                atomicAdd(&gs->acc_items, __popc(um));
-                base = atomicAdd(&gs->acc_bins, nz);
+                // the cell's list position and its first bin in one reservation
+                const unsigned long long o = atomicAdd(&gs->acc_lb, (1ull << 32) | (unsigned)nz);
+                const int idx = (int)(o >> 32);
+                base = (int)(uint32_t)o;
                 if (idx < d.listed_cap) {
                     d.listed[idx] = (uint32_t)c;
                     d.c2b[c] = 4 * idx;
                     d.cell_bins[idx] = make_int2(base, nz);
+                    in_list = 1;
                 }
                 atomicAdd(&s_cnt[ln][act ? 0 : 1], 1);
                 atomicAdd(&s_cnt[ln][2], __popc(um));
             }
         }
         if (cls) {
-            const int idx_ok = __shfl_sync(kFull, lane == 0 ? (d.c2b[c] >= 0 ? 1 : 0) : 0, 0);
+            const int idx_ok = __shfl_sync(kFull, in_list, 0);
             base = __shfl_sync(kFull, base, 0);
             if (!idx_ok || base + nz > d.bins_cap) {   // no room: the last block stops the run
                 if (lane == 0) atomicAdd(&gs->bin_ovf, 1);
@@ -516,10 +518,10 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     if (!s_last) return;
     __threadfence();
     // settle each lane: counts, C1 stopping rule, accumulators
-    __shared__ int s_work;
+    __shared__ int s_work, s_items;
     __shared__ uint8_t s_fin[kMaxLanes];
     const bool plan = gs->plan_n > 0;
-    if (threadIdx.x == 0) s_work = 0;
+    if (threadIdx.x == 0) s_work = s_items = 0;
     __syncthreads();
     for (int ln = threadIdx.x; ln < d.B; ln += blockDim.x) {
         LaneState& L = d.ls[ln];
@@ -527,6 +529,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
         const bool was_running = v->done == 0;
         const int na = v->acc_active, nc = v->acc_coarse, nsl = v->acc_slots;
         L.acc_active = L.acc_coarse = L.acc_slots = 0;
+        if (nsl) atomicAdd(&s_items, nsl);
         // every psi_in page of the lane is cleared: its region starts again
         atomicMax(&gs->pool_peak, L.pool_top);
         L.pool_top = 0;
@@ -565,8 +568,9 @@ __global__ void __launch_bounds__(kThreads) k_classify(Dev d, cudaGraphCondition
     }
     if (threadIdx.x != 0) return;
     volatile IterGlobal* v = gs;
-    const int nl = v->acc_listed, ni = v->acc_items, nb = v->acc_bins;
-    gs->acc_listed = gs->acc_items = gs->acc_bins = 0;
+    const unsigned long long lb = v->acc_lb;
+    const int nl = (int)(lb >> 32), ni = s_items, nb = (int)(uint32_t)lb;
+    gs->acc_lb = 0ull;
     gs->gen = g;
     gs->ctag += 1u;   // claim pass of this iteration
     gs->n_fin = nf;
