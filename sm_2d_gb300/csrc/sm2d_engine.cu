@@ -1419,6 +1419,12 @@ __global__ void k_pages_identity(Dev d, int list_k, int n_listed) {
 // runs on too, and restarts after a wipe of the claim tables when it nears
 // its 32-bit limit.
 __global__ void k_reset_state(Dev d) {
+    // every lane's state, a thread per lane
+    for (int ln = blockIdx.x * blockDim.x + threadIdx.x; ln < d.B; ln += gridDim.x * blockDim.x) {
+        memset(&d.ls[ln], 0, sizeof(LaneState));
+        d.ls[ln].done = 1;
+        d.ls[ln].spot = -1;
+    }
     if (threadIdx.x || blockIdx.x) return;
     IterGlobal* gs = d.gs;
     const unsigned long long g = gs->gen;
@@ -1436,11 +1442,6 @@ __global__ void k_reset_state(Dev d) {
     gs->cand_miss = miss;
     gs->wipe = wipe;
     gs->max_pass = INT_MAX;
-    for (int ln = 0; ln < d.B; ++ln) {
-        memset(&d.ls[ln], 0, sizeof(LaneState));
-        d.ls[ln].done = 1;
-        d.ls[ln].spot = -1;
-    }
 }
 
 // Clear every claim-table row when a tag wrap is pending (grid-stride).
@@ -1985,7 +1986,7 @@ static int reset_lanes(Ctx& c) {
     CK(cudaMemsetAsync(d.w_nuc, 0, n * 4, c.s));
     CK(cudaMemsetAsync(d.w_bnd, 0, n * 4, c.s));
     CK(cudaMemsetAsync(d.cls, 0, n, c.s));
-    k_reset_state<<<1, 1, 0, c.s>>>(c.d);
+    k_reset_state<<<(unsigned)((c.B + 127) / 128), 128, 0, c.s>>>(c.d);
     k_wipe<<<c.grid_cell, kThreads, 0, c.s>>>(c.d, c.ctab_words, c.ccount_n);
     CK(cudaGetLastError());
     c.injected = false;
