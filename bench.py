@@ -691,7 +691,7 @@ def run_gpu_arm(args):
         if args.workload == "plan512" and not args.no_context:
             # surrogate + batched: the plan in the expectation form with K3's
             # redistribution weights from the network, the per-row fallback at
-            # BASELINE's 0.5 % and at a stricter 0.2 %
+            # the workload's 0.5 % and at a stricter 0.2 %
             for key, tol in (("transport", 0.005), ("transport_tol_0.002", 0.002)):
                 st = plan_rate(args.grid, args.workload, n, 0, 2, 1, "expect", accuracy=True, surrogate=net, tol=tol)
                 st["method"] = ("expectation form with the learned surrogate: K3 bins whose energy window has "

@@ -15,7 +15,7 @@ the benchmark's workloads and writes their wall times (the reference_gpu
 figure of the design notes) to the output directory.
 
 Usage on the GPU machine, from the repository root:
-    python tests/golden/make_golden_gpu.py --out gpurun_out/ref_gpu [--timing]
+    python tests/golden/make_golden_gpu.py --out <output folder> [--timing]
 """
 import argparse
 import configparser
