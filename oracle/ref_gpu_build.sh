@@ -9,7 +9,7 @@
 #                                      IMPL_CUDA_SOURCES, CUDA_KERNEL_SOURCES,
 #                                      run_simulation.cpp), their headers and the
 #                                      PSTAR table into oracle/_ref/tree (ignored
-#                                      by git, carried to the GPU machine with the
+#                                      by git, carried to the GB300 host with the
 #                                      checkout), unmodified
 #   sh oracle/ref_gpu_build.sh build   compiles that copy with nvcc and g++
 #                                      (separable compilation, as the CMake build

@@ -1,4 +1,4 @@
-"""Golden fixtures from the reference's own GPU build, run on the GPU machine.
+"""Golden fixtures from the reference's own GPU build, run on a GB300.
 
 ``oracle/ref_gpu_build.sh stage`` (where the SM_2D tree is mounted) and
 ``oracle/ref_gpu_build.sh build`` (on the box) give
@@ -14,7 +14,7 @@ With --timing it also runs the reference's plain build (no dumps) on spots of
 the benchmark's workloads and writes their wall times (the reference_gpu
 figure of the design notes) to the output directory.
 
-Usage on the GPU machine, from the repository root:
+Usage on a GB300, from the repository root:
     python tests/golden/make_golden_gpu.py --out <output folder> [--timing]
 """
 import argparse
