@@ -299,6 +299,7 @@ struct Kids {
     int c, j, emax;
     float Mt[SM2D_RD_NT], Me[SM2D_RD_NE];
     float Erep;   // represented energy of the children
+    uint32_t live;   // bit t + 8 e: the child of angular distance t, energy offset e has weight
 };
 __device__ __forceinline__ int kid_window_top(const Dev& d, int jin, float Em) {
     const float Ec = fmaxf(d.Ee[0], fminf(Em, d.Ee[d.N_E]));
@@ -335,6 +336,13 @@ __device__ __forceinline__ void make_kids(const Dev& d, int c, int jin, float s,
     sm2d_rd_theta(s, k.Mt);
     sm2d_rd_energy(Em, sE, cen, k.emax, k.Me);
     k.Erep = sm2d_rd_fold(w, d.split_min_w, k.Mt, k.Me, cen, k.emax);
+    uint32_t live = 0u;
+#pragma unroll
+    for (int e = 0; e < SM2D_RD_NE; ++e)
+#pragma unroll
+        for (int t = 0; t < SM2D_RD_NT; ++t)
+            if (e <= k.emax && k.Me[e] > 0.0f && k.Mt[t] > 0.0f) live |= 1u << (t + 8 * e);
+    k.live = live;
 }
 // The children from the learned surrogate's table of the component (its
 // row of the network's output, T[t + 8 e]; the window is complete, emax 3).
@@ -345,6 +353,7 @@ struct KidsT {
     int c, j;
     float T[SM2D_RD_NT * SM2D_RD_NE];
     float Erep;
+    uint32_t live;   // bit t + 8 e: T[t + 8 e] > 0
 };
 __device__ __forceinline__ void make_kids_t(const Dev& d, int c, int jin, float Em, float w, const float* row,
                                             KidsT& k) {
@@ -380,12 +389,17 @@ __device__ __forceinline__ void make_kids_t(const Dev& d, int c, int jin, float 
             }
         }
     }
+    uint32_t live = 0u;
+#pragma unroll
+    for (int q = 0; q < SM2D_RD_NT * SM2D_RD_NE; ++q)
+        if (k.T[q] > 0.0f) live |= 1u << q;
+    k.live = live;
 }
 // accessors shared by both kinds of children
 __device__ __forceinline__ int kid_emax(const Kids& k) { return k.emax; }
 __device__ __forceinline__ int kid_emax(const KidsT&) { return SM2D_RD_NE - 1; }
-__device__ __forceinline__ bool kid_live(const Kids& k, int t, int e) { return k.Me[e] > 0.0f && k.Mt[t] > 0.0f; }
-__device__ __forceinline__ bool kid_live(const KidsT& k, int t, int e) { return k.T[t + 8 * e] > 0.0f; }
+__device__ __forceinline__ bool kid_live(const Kids& k, int t, int e) { return (k.live >> (t + 8 * e)) & 1u; }
+__device__ __forceinline__ bool kid_live(const KidsT& k, int t, int e) { return (k.live >> (t + 8 * e)) & 1u; }
 __device__ __forceinline__ float kid_weight(const Kids& k, float w, int kk, int e) {
     return sm2d_rd_kid_w(w, k.Mt, k.Me, kk, e);
 }
