@@ -88,7 +88,8 @@ typedef struct sm2d_problem {
     int seed_iteration_salt;     /* salt MCS/straggling seeds with the iteration index */
     /* engine shape */
     int lanes;                   /* spots transported together by sm2d_batch_run
-                                    (0 or 1: one; the single-spot entries use lane 0) */
+                                    (0 or 1: one; at most 512; the single-spot entries
+                                    use lane 0) */
     /* slab phantom (no counterpart in the reference, which transports water):
      * density of each depth row [Nz] in g/cm^3, or NULL for water.  Energy
      * loss, range limits, straggling, nuclear attenuation and the Highland
