@@ -732,6 +732,33 @@ def run_gpu_arm(args):
     return 0
 
 
+def stage_profile(lanes=128):
+    """Per-pass device time of each stage (µs, CUDA events around every kernel
+    of an eager replay) for one wave of the plan's first `lanes` spots, in the
+    sampled form, the expectation form and the expectation form with the
+    learned surrogate serving K3's redistribution (fallback at 0.5 %)."""
+    import sm_2d_gb300 as sm
+    from sm_2d_gb300.runtime import Beam
+    spots = plan_spots("plan512", 0, lanes)
+    beams = [Beam(b["x0"], b["z0"], b["theta0"], b["E0"], b["W"], b["sigma_x"], b["sigma_theta"], b["sigma_E"],
+                  b["n_samples"], b["seed"]) for b in spots]
+    _, net = surrogate_leg()
+    out = {}
+    for key, method, use_net in (("sampled", "sampled", False), ("expectation", "expect", False),
+                                 ("surrogate", "expect", True)):
+        cfg = make_config("reference", "plan512", method)
+        cfg.lanes = lanes
+        with sm.Transport(cfg) as t:
+            if use_net:
+                t.set_surrogate(net, tol=0.005)
+            t.batch_inject(beams)
+            _, ms, _, passes = t.run_profiled(MAX_IT)
+        out[key] = {"passes": passes, "us_per_pass": {k: round(v / passes * 1000.0, 1) for k, v in ms.items()},
+                    "wave_ms": round(sum(ms.values()), 1)}
+    net.close()
+    return {"workload": f"the 512-spot plan's first {lanes} spots as one wave on {lanes} lanes", "forms": out}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -749,7 +776,14 @@ def main():
     ap.add_argument("--spots", type=int, default=0, help="spots per step, the plan (0: 512; 64 for c3)")
     ap.add_argument("--small", action="store_true",
                     help="100x200 cells, 80 MeV beam: a small case for profiler captures (not a bench line)")
+    ap.add_argument("--stage-profile", action="store_true",
+                    help="print the per-pass stage times of the sampled, expectation and surrogate forms (not a bench line)")
     args = ap.parse_args()
+    if args.stage_profile:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(stage_profile()))
+        return 0
     if args.spots <= 0:
         args.spots = 64 if args.workload == "c3" else 512
     if args.small:
