@@ -100,6 +100,7 @@ struct IterGlobal {
     int n_fill;            // lanes the last refill assigned, and their spots
     int fill_lane[kMaxLanes], fill_spot[kMaxLanes];
     const BeamArgs* plan_beams;   // [plan_n]
+    const int* plan_order;        // [plan_n]: the spots in the order lanes take them (longest first)
     const float* plan_fe;         // [plan_n][3 Nz + 1]: A(z), B(z), sigma_total(z), sigma_x
     double* plan_dose;            // [plan_n][Nc] convolved dose, or null
     sm2d_spot_result* plan_res;   // [plan_n]

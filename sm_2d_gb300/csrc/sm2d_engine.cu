@@ -1557,10 +1557,11 @@ __host__ __device__ inline void lane_result(const LaneState& L, sm2d_spot_result
 
 // Opens a plan of n spots, each limited to max_it iterations.
 __global__ void k_plan_begin(Dev d, const BeamArgs* beams, const float* fe, double* dose, sm2d_spot_result* res, int n,
-                             int max_it, int lane_limit) {
+                             int max_it, int lane_limit, const int* order) {
     if (threadIdx.x || blockIdx.x) return;
     IterGlobal* gs = d.gs;
     gs->plan_n = n;
+    gs->plan_order = order;
     gs->lane_limit = lane_limit;
     gs->plan_next = 0;
     gs->lane_max_it = max_it;
@@ -1663,7 +1664,7 @@ __global__ void __launch_bounds__(256) k_lane_assign(Dev d) {
         const int ln = tid * per + k;
         if (ln < lim && d.ls[ln].done && d.ls[ln].spot < 0) {
             gs->fill_lane[r] = ln;
-            gs->fill_spot[r] = next + r;
+            gs->fill_spot[r] = gs->plan_order ? gs->plan_order[next + r] : next + r;
             ++r;
         }
     }
@@ -1756,6 +1757,8 @@ struct Ctx {
     BeamArgs* plan_beams_dev = nullptr;
     float* plan_fe_dev = nullptr;
     sm2d_spot_result* plan_res_dev = nullptr;
+    int* plan_order_dev = nullptr;    // the order lanes take the plan's spots
+    std::vector<int> plan_order_host;
     double* plan_dose_dev = nullptr;
     double* plan_dose_ext = nullptr;  // sm2d_batch_run: the caller's pinned host maps, written by the device
     std::vector<BeamArgs> plan_beams_host;
@@ -2389,7 +2392,8 @@ int sm2d_destroy(sm2d_handle h) {
     if (h->gs_host) cudaFreeHost(h->gs_host);
     if (h->ls_host) cudaFreeHost(h->ls_host);
     if (h->beams_host) cudaFreeHost(h->beams_host);
-    for (void* p : {(void*)h->plan_beams_dev, (void*)h->plan_fe_dev, (void*)h->plan_res_dev, (void*)h->plan_dose_dev})
+    for (void* p : {(void*)h->plan_beams_dev, (void*)h->plan_fe_dev, (void*)h->plan_res_dev, (void*)h->plan_dose_dev,
+                    (void*)h->plan_order_dev})
         if (p) cudaFree(p);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
@@ -2931,7 +2935,8 @@ int sm2d_plan_load(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_i
             c.plan_cap = 0;
             if ((rc = grow((void**)&c.plan_beams_dev, sizeof(BeamArgs) * n)) ||
                 (rc = grow((void**)&c.plan_fe_dev, sizeof(float) * per * n)) ||
-                (rc = grow((void**)&c.plan_res_dev, sizeof(sm2d_spot_result) * n)))
+                (rc = grow((void**)&c.plan_res_dev, sizeof(sm2d_spot_result) * n)) ||
+                (rc = grow((void**)&c.plan_order_dev, sizeof(int) * n)))
                 return rc;
             c.plan_cap = n;
         }
@@ -2973,8 +2978,16 @@ int sm2d_plan_load(sm2d_handle h, const sm2d_beam* beams, int n_spots, int max_i
     }
     for (size_t i = 0; i < n; ++i)
         if (src[i] != (int)i) std::copy_n(c.plan_fe_host.data() + per * src[i], per, c.plan_fe_host.data() + per * i);
+    // the order the lanes take the spots: the longest first (the highest
+    // energy, the deepest range), so that the plan does not end on a long
+    // spot started late; results and dose maps stay in the plan's order
+    c.plan_order_host.resize(n);
+    for (size_t i = 0; i < n; ++i) c.plan_order_host[i] = (int)i;
+    std::stable_sort(c.plan_order_host.begin(), c.plan_order_host.end(),
+                     [&](int a, int b) { return beams[a].E0 > beams[b].E0; });
     // pageable sources: each copy has read its source when it returns
     if (n) {
+        CK(cudaMemcpyAsync(c.plan_order_dev, c.plan_order_host.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c.s));
         CK(cudaMemcpyAsync(c.plan_beams_dev, c.plan_beams_host.data(), sizeof(BeamArgs) * n, cudaMemcpyHostToDevice, c.s));
         CK(cudaMemcpyAsync(c.plan_fe_dev, c.plan_fe_host.data(), sizeof(float) * per * n, cudaMemcpyHostToDevice, c.s));
     }
@@ -2993,7 +3006,7 @@ int sm2d_plan_run_async(sm2d_handle h) {
     if ((rc = reset_lanes(c))) return rc;
     double* dose_out = c.plan_dose_on ? (c.plan_dose_ext ? c.plan_dose_ext : c.plan_dose_dev) : nullptr;
     k_plan_begin<<<1, 1, 0, c.s>>>(c.d, c.plan_beams_dev, c.plan_fe_dev, dose_out,
-                                   c.plan_res_dev, c.plan_n, c.plan_max_it, c.lanes_in_flight);
+                                   c.plan_res_dev, c.plan_n, c.plan_max_it, c.lanes_in_flight, c.plan_order_dev);
     CK(cudaGetLastError());
     if ((rc = DISPATCH(c, refill, 0))) return rc;   // the first spots into every lane
     CK(cudaGraphLaunch(c.exec, c.s));
