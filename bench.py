@@ -631,10 +631,10 @@ def run_gpu_arm(args):
     traffic = None
     tp = os.path.join(ROOT, "profiles", f"k_transport_traffic_{args.workload}.json")
     if os.path.exists(tp) and not SMALL and args.grid == "reference":
-        # DRAM bytes per deposit launch from an ncu capture of the same wave at
-        # fewer lanes, scaled by the lane count (the lanes' work adds up)
+        # DRAM bytes per deposit launch from an ncu capture of the same kind of
+        # wave, per lane, scaled by the wave's lanes (the lanes' work adds up)
         tr = json.load(open(tp))
-        traffic = tr["dram_bytes_per_launch_per_lane"] * B
+        traffic = tr["dram_bytes_per_launch_per_lane"] * lif
     step_total = sum(ms.values())
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_src, "kernel": "k_transport (deposit pass)",
