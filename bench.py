@@ -555,6 +555,8 @@ def run_gpu_arm(args):
     # the launch shape (blocks per SM of each pass kernel) from the autotuner,
     # on this plan, before the timed region
     shape, tune_ms = t.autotune() if not args.no_tune else (t.launch_shape(), None)
+    if args.lanes_in_flight > 0:   # a fixed number of lanes in flight instead of the tuner's choice
+        t.set_lanes_in_flight(min(args.lanes_in_flight, B))
     lif = t.lanes_in_flight()   # the tuner's choice of lanes in flight (every lane with --no-tune)
     for _ in range(max(args.warmup, 3)):
         t.plan_run_async()
@@ -772,6 +774,8 @@ def main():
     ap.add_argument("--no-context", action="store_true", help="skip the log-grid and single-lane context figures")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no autotuner run)")
     ap.add_argument("--lanes", type=int, default=0, help="spots in flight (0: from free device memory)")
+    ap.add_argument("--lanes-in-flight", type=int, default=0,
+                    help="lanes a plan keeps in flight (0: the autotuner's choice, every lane with --no-tune)")
     ap.add_argument("--workload", default="plan512", choices=["plan512", "c2", "c3"])
     ap.add_argument("--spots", type=int, default=0, help="spots per step, the plan (0: 512; 64 for c3)")
     ap.add_argument("--small", action="store_true",
